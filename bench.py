@@ -1,0 +1,320 @@
+"""Benchmark of the SWM time step on GB300 (one JSON line on stdout).
+
+Workload: the nonlinear wind-driven double gyre on 1024 x 1024 cells
+(dx = 5 km, beta-plane f0 = 1e-4, beta = 2e-11, H = 500 m, tau = 0.1 cos(2 pi
+y/L), biharmonic viscosity 1e10 m^4/s, bottom drag 1e-7 /s, seeded coastline,
+rest start), synthetic seeded inputs.  One bench step = one model time step
+(swm_gpu_step + swm_gpu_advance) of the whole basin.
+
+value: cell-steps/s of the selected path (default fused_fp32c, the FP32
+compensated path) with the state resident in HBM; the L2 cache (129 MB; the
+per-step working set is ~85 MB) is flushed by a 512 MB device write before
+every timed step, and each step is timed with CUDA events on the library's
+stream.  e2e: the same metric through the C ABI with host buffers: every step
+uploads that step's wind-stress rows (H2D) and reads back the FP64 domain
+integrals (D2H), wall clock.  --impl reference times the CPU restatement of
+the reference's loops (the Fortran reference cannot be built here: no Fortran
+compiler) on the host cores.
+"""
+import argparse
+import json
+import os
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+METRIC = 'grid-cell-steps/s on 1 GB300, FP32 batched vs FP64 plain, at stated L2 error'
+BYTES_PER_POINT = {'fused_fp32c': 89, 'fused_fp64': 129, 'plain_fp64': 129}
+
+
+def parse():
+    ap = argparse.ArgumentParser()
+    ap.add_argument('--gpus', type=int, default=1)
+    ap.add_argument('--steps', type=int, default=2000)
+    ap.add_argument('--warmup', type=int, default=20)
+    ap.add_argument('--impl', default='ours', choices=['ours', 'reference'])
+    ap.add_argument('--path', default='fused_fp32c', choices=['fused_fp32c', 'fused_fp64', 'plain_fp64'])
+    ap.add_argument('--cells', type=int, default=1024)
+    ap.add_argument('--error-steps', type=int, default=1000)
+    ap.add_argument('--quick', action='store_true', help='skip the side measurements')
+    return ap.parse_args()
+
+
+def dist_setup(args):
+    ws = int(os.environ.get('WORLD_SIZE', '1'))
+    rank = int(os.environ.get('RANK', '0'))
+    if ws > 1:
+        import torch.distributed as dist
+        dist.init_process_group('gloo')
+    return rank, ws
+
+
+def barrier(ws):
+    if ws > 1:
+        import torch.distributed as dist
+        dist.barrier()
+
+
+def allmax(ws, x):
+    if ws == 1:
+        return x
+    import torch
+    import torch.distributed as dist
+    t = torch.tensor([x], dtype=torch.float64)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def peaks():
+    p = os.path.join(ROOT, 'MEASURED_PEAKS.json')
+    if os.path.exists(p):
+        with open(p) as fh:
+            d = json.load(fh)
+        return float(d['hbm_gbs']), 'measured'
+    return 6800.0, 'fallback'
+
+
+class ClockSampler:
+    """nvidia-smi samples of SM clock and throttle reasons during a region."""
+
+    Q = ('clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,clocks_event_reasons.hw_slowdown,'
+         'clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,'
+         'clocks_event_reasons.sw_power_cap')
+
+    def __init__(self, gpu=0):
+        self.gpu = gpu
+        self.proc = None
+
+    def __enter__(self):
+        try:
+            self.proc = subprocess.Popen(['nvidia-smi', '-i', str(self.gpu), '--query-gpu=' + self.Q,
+                                          '--format=csv,noheader,nounits', '-lms', '50'],
+                                         stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+        except OSError:
+            self.proc = None
+        time.sleep(0.3)
+        return self
+
+    def __exit__(self, *a):
+        self.lines = []
+        if self.proc:
+            time.sleep(0.15)
+            self.proc.terminate()
+            try:
+                out, _ = self.proc.communicate(timeout=5)
+            except subprocess.TimeoutExpired:
+                self.proc.kill()
+                out, _ = self.proc.communicate()
+            self.lines = [l for l in out.splitlines() if l.strip()]
+
+    def summary(self):
+        sm, mx, reasons = [], 0.0, set()
+        names = ['hw_slowdown', 'hw_thermal_slowdown', 'sw_thermal_slowdown', 'sw_power_cap']
+        for l in getattr(self, 'lines', []):
+            f = [x.strip() for x in l.split(',')]
+            try:
+                sm.append(float(f[0]))
+                mx = max(mx, float(f[1]))
+            except ValueError:
+                continue
+            for n, v in zip(names, f[4:8]):
+                if v.lower().startswith('active'):
+                    reasons.add(n)
+        return {'sm_mhz': float(np.median(sm)) if sm else None, 'sm_max_mhz': mx or None,
+                'reasons': sorted(reasons), 'samples': len(sm)}
+
+
+def build_model(path, cells, nsteps):
+    from swm_gb300.host import synthetic
+    from swm_gb300.host.driver import Driver
+    from swm_gb300.model import GpuModel
+    case = synthetic.double_gyre(cells, biharmonic=True, nsteps=nsteps)
+    g = GpuModel(path)
+    d = Driver(case, g)
+    d.init(with_diag=False)
+    return case, g, d
+
+
+def timed_steps(g, itt0, k, flush=None, stream=None):
+    """Device time (ms) of each of k steps, CUDA events on the library's stream."""
+    import torch
+    ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(k)]
+    with torch.cuda.stream(stream):
+        for s in range(k):
+            if flush is not None:
+                flush.zero_()
+            ev[s][0].record(stream)
+            g.run(itt0 + s, 1)
+            ev[s][1].record(stream)
+    g.synchronize()
+    torch.cuda.synchronize()
+    return np.array([a.elapsed_time(b) for a, b in ev])
+
+
+def ours(args, rank, ws):
+    import torch
+    torch.cuda.set_device(int(os.environ.get('LOCAL_RANK', '0')))
+    cells = args.cells
+    npts = (cells + 1) * (cells + 1)
+    case, g, drv = build_model(args.path, cells, args.warmup + args.steps)
+    stream = torch.cuda.ExternalStream(g.stream())
+    flush = torch.empty(512 * 1024 * 1024 // 4, dtype=torch.float32, device='cuda')
+    itt = 0
+    g.run(itt, args.warmup)
+    itt += args.warmup
+    g.synchronize()
+    barrier(ws)
+    torch.cuda.synchronize()
+    l0 = g.launch_count()
+    t0 = time.perf_counter()
+    with ClockSampler(int(os.environ.get('LOCAL_RANK', '0'))) as clk:
+        ms = timed_steps(g, itt, args.steps, flush, stream)
+    wall = time.perf_counter() - t0
+    launches = g.launch_count() - l0
+    itt += args.steps
+    barrier(ws)
+    step_ms = allmax(ws, float(ms.mean()))
+    value = npts * ws / (step_ms * 1e-3)
+    line = {'metric': METRIC, 'value': value, 'unit': 'cell-steps/s', 'n_gpus': ws, 'steps': args.steps,
+            'warmup': args.warmup, 'ms_per_step': step_ms, 'higher_is_better': True, 'scaling': 'weak',
+            'vs_baseline': None, 'dtype': 'f32' if args.path == 'fused_fp32c' else 'f64',
+            'data': 'synthetic (seeded double-gyre basin, rest start)',
+            'config': {'workload': 'double_gyre_%dx%d_biharmonic' % (cells, cells), 'cells': cells * cells,
+                       'array_points': npts, 'path': args.path, 'dt_s': case['config']['dt'],
+                       'l2': 'flushed (512 MB write) before every timed step',
+                       'parallelism': 'replicas x%d' % ws if ws > 1 else 'single GPU'},
+            'gpu_launches': int(launches), 'wall_s_timed_region': wall}
+    line['clocks'] = clk.summary()
+    peak, kind = peaks()
+    alg = BYTES_PER_POINT[args.path] * npts
+    achieved = alg / (step_ms * 1e-3) / 1e9
+    traffic = None
+    prof = os.path.join(ROOT, 'profiles', 'fused_fp32c_double_gyre_1024.json')
+    if args.path == 'fused_fp32c' and cells == 1024 and os.path.exists(prof):
+        with open(prof) as fh:
+            traffic = json.load(fh).get('dram_bytes_per_launch')
+    line['roofline'] = {'bound': 'hbm', 'achieved': achieved, 'peak': peak, 'unit': 'GB/s',
+                        'frac': achieved / peak, 'traffic': traffic, 'peak_kind': kind,
+                        'algorithmic_bytes_per_launch': alg,
+                        'kernel': 'k_fused<float,2,true>' if args.path == 'fused_fp32c' else args.path}
+    # steady state without L2 flush (back-to-back steps)
+    ms_nf = timed_steps(g, itt, 200, None, stream)
+    itt += 200
+    line['no_flush'] = {'ms_per_step': float(ms_nf.mean()), 'value': npts / (ms_nf.mean() * 1e-3)}
+    # e2e through the C ABI with host buffers
+    tau_rows = case['streams'][0]['rec1'][0][:, 0].copy()
+    k_e2e = min(args.steps, 1000)
+    g.synchronize()
+    t0 = time.perf_counter()
+    for s in range(k_e2e):
+        itt += 1
+        g.set_stream_rows(0, tau_rows)
+        g.step(itt)
+        g.advance(itt)
+        integ = g.integrals()
+    e2e_s = time.perf_counter() - t0
+    line['e2e'] = {'value': npts * k_e2e / e2e_s, 'unit': 'cell-steps/s', 'h2d_bytes_per_step': tau_rows.nbytes,
+                   'd2h_bytes_per_step': integ.nbytes, 'steps': k_e2e,
+                   'per_step': 'H2D wind-stress rows, swm_gpu_step + swm_gpu_advance, D2H FP64 integrals'}
+    if rank == 0 and not args.quick:
+        line.update(side_measurements(args, case, g, stream, flush, npts))
+        line['speedup_vs_fp64_plain'] = line['plain_fp64']['ms_per_step'] / step_ms
+    if rank == 0 and ws == 1 and not args.quick:
+        line['cpu_baseline'] = cpu_baseline(cells)
+    g.close()
+    return line
+
+
+def side_measurements(args, case, g32, stream, flush, npts):
+    """FP64 paths on the same workload, and the FP32 error against FP64."""
+    out = {}
+    for path, k in (('plain_fp64', 20), ('fused_fp64', 50)):
+        _, g, _ = build_model(path, args.cells, 100)
+        g.run(0, 3)
+        ms = timed_steps(g, 3, k, flush, __import__('torch').cuda.ExternalStream(g.stream()))
+        out[path] = {'ms_per_step': float(ms.mean()), 'value': npts / (ms.mean() * 1e-3), 'steps': k}
+        g.close()
+    # FP32C against the bit-exact FP64 plain path from the same start
+    e = args.error_steps
+    _, gp, _ = build_model('plain_fp64', args.cells, e)
+    _, gc, _ = build_model('fused_fp32c', args.cells, e)
+    gp.run(0, e)
+    gc.run(0, e)
+    errs = {}
+    for f, grid in (('u', 'u'), ('v', 'v'), ('eta', 'eta')):
+        m = gp.ocean(grid).astype(bool)
+        a, b = gc.field(f), gp.field(f)
+        den = np.linalg.norm(b[m])
+        errs[f] = {'rel_l2': float(np.linalg.norm((a - b)[m]) / den) if den > 0 else None,
+                   'rel_max': float(np.abs(a - b)[m].max() / max(np.abs(b[m]).max(), 1e-300))}
+    out['fp32c_error_vs_fp64'] = {'steps': e, 'fields': errs}
+    gp.close()
+    gc.close()
+    return out
+
+
+def cpu_baseline(cells, budget_s=15.0):
+    """The FP64 CPU restatement (oracle) on the same basin, all host cores."""
+    sys.path.insert(0, os.path.join(ROOT, 'oracle'))
+    from oracle import OracleBackend
+    from swm_gb300.host import synthetic
+    from swm_gb300.host.driver import Driver
+    case = synthetic.double_gyre(cells, biharmonic=True, nsteps=100)
+    o = OracleBackend()
+    Driver(case, o).init(with_diag=False)
+    o.run_steady(2)
+    n, t = 0, 0.0
+    t0 = time.perf_counter()
+    while t < budget_s and n < 200:
+        o.run_steady(1)
+        n += 1
+        t = time.perf_counter() - t0
+    npts = (cells + 1) ** 2
+    return {'value': npts * n / t, 'unit': 'cell-steps/s', 'cores': os.cpu_count(), 'kind': 'port',
+            'sample': '%d model steps of the %dx%d basin (FP64 C restatement, OpenMP)' % (n, cells, cells)}
+
+
+def reference(args, rank, ws):
+    """CPU restatement of the reference loops, timed on the host cores."""
+    if rank != 0:
+        return None
+    sys.path.insert(0, os.path.join(ROOT, 'oracle'))
+    from oracle import OracleBackend
+    from swm_gb300.host import synthetic
+    from swm_gb300.host.driver import Driver
+    strip = 64
+    case = synthetic.double_gyre((args.cells, strip), biharmonic=True, nsteps=args.warmup + args.steps)
+    o = OracleBackend()
+    Driver(case, o).init(with_diag=False)
+    o.run_steady(args.warmup)
+    t0 = time.perf_counter()
+    o.run_steady(args.steps)
+    t = time.perf_counter() - t0
+    npts = (args.cells + 1) * (strip + 1)
+    v = npts * args.steps / t
+    sample = 'one model step per bench step on a %dx%d-cell strip of the basin (same physics)' % (args.cells, strip)
+    return {'metric': METRIC, 'value': v, 'unit': 'cell-steps/s', 'n_gpus': ws, 'steps': args.steps,
+            'warmup': args.warmup, 'ms_per_step': t / args.steps * 1e3, 'higher_is_better': True,
+            'scaling': 'weak', 'vs_baseline': None, 'dtype': 'f64', 'data': 'synthetic', 'impl': 'reference',
+            'config': {'workload': 'double_gyre_%dx%d_biharmonic' % (args.cells, args.cells)},
+            'cpu_baseline': {'value': v, 'unit': 'cell-steps/s', 'cores': os.cpu_count(), 'kind': 'port',
+                             'sample': sample},
+            'e2e': {'value': v, 'unit': 'cell-steps/s', 'h2d_bytes_per_step': 0, 'd2h_bytes_per_step': 0}}
+
+
+def main():
+    args = parse()
+    rank, ws = dist_setup(args)
+    line = reference(args, rank, ws) if args.impl == 'reference' else ours(args, rank, ws)
+    if rank == 0 and line is not None:
+        print(json.dumps(line))
+
+
+if __name__ == '__main__':
+    main()

@@ -1,0 +1,181 @@
+/*
+ * swm_gpu.h -- C ABI of the GB300 implementation of the SWM time-stepping
+ * hot path (shallow-water C-grid tendencies + Adams-Bashforth, lateral
+ * mixing, damping, forcing, tracer advection-diffusion, red-black SOR).
+ *
+ * The entry points mirror the Fortran module entry points of martinclaus/swm
+ * they replace; each declaration cites the routine (path:line in the swm
+ * source tree).  A Fortran host binds them with ISO_C_BINDING (see
+ * INTEGRATION.md); every function returns 0 on success or a positive
+ * SWM_GPU_E* code, and swm_gpu_last_error() gives the message.
+ *
+ * Arrays are Fortran column-major (Nx, Ny) = C row-major [Ny][Nx], FP64,
+ * indices 0-based; masks are int8 (1 = ocean).  Host pointers only: the
+ * library owns every device buffer.
+ */
+#ifndef SWM_GPU_H
+#define SWM_GPU_H
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* ---- status codes ---- */
+enum {
+  SWM_GPU_OK = 0,
+  SWM_GPU_EINVAL = 1,        /* bad argument / call order                         */
+  SWM_GPU_ECUDA = 2,         /* CUDA runtime error                                */
+  SWM_GPU_ENOMEM = 3,        /* device allocation failed                          */
+  SWM_GPU_ENOT_CONVERGED = 4,/* SOR hit its iteration cap (the reference warns)   */
+  SWM_GPU_EDEVICE = 5        /* device-side check failed (error word set)         */
+};
+
+/* ---- physics switches (include/model.h CPP defines) ---- */
+enum {
+  SWM_MODE_NONE = 0,          /* no linearisation define                          */
+  SWM_MODE_NONLINEAR = 1,     /* FULLY_NONLINEAR                                  */
+  SWM_MODE_LIN_REST = 2,      /* LINEARISED_STATE_OF_REST                         */
+  SWM_MODE_LIN_MEAN = 3       /* LINEARISED_MEAN_STATE                            */
+};
+enum { SWM_MIX_LAPLACE = 0, SWM_MIX_BIHARMONIC = 1 /* project extension */ };
+
+/* ---- execution paths ---- */
+enum {
+  SWM_PATH_PLAIN_FP64 = 0,    /* per-module FP64 kernels, bit-for-bit with the FP64 restatement */
+  SWM_PATH_FUSED_FP64 = 1,    /* one fused FP64 stencil kernel per step            */
+  SWM_PATH_FUSED_FP32C = 2    /* fused FP32 stencil, state kept as FP32 hi+lo pair */
+};
+
+typedef struct swm_gpu_config {
+  int32_t nx, ny;               /* &domain_nl Nx, Ny                               */
+  int32_t mode;                 /* SWM_MODE_*                                      */
+  int32_t lateral_mixing;       /* LATERAL_MIXING                                  */
+  int32_t quadratic_friction;   /* QUADRATIC_BOTTOM_FRICTION                       */
+  int32_t barotropic;           /* BAROTROPIC                                      */
+  int32_t mixing_kind;          /* SWM_MIX_*                                       */
+  int32_t coriolis_approx;      /* &domain_nl coriolis_approx                      */
+  int32_t tracer_nan_guard;     /* 1: 0/0 tracer coefficients taken as 0           */
+  int32_t damping_additive;     /* 1: damping entries add (older selfcheck build)  */
+  int32_t mask_psi_bs;          /* 1: basic-state psi zeroed on land (same)        */
+  double dt, G, Ah, A, OMEGA, RHO0, lbc, theta0;
+  double lon_s, lon_e, lat_s, lat_e;
+  double H_overwrite;           /* 0 = unset                                       */
+  double ab_chi, minD;
+  double tau_scale;             /* TAU_SCALE (1.0 when undefined)                  */
+  double bih;                   /* biharmonic coefficient (extension)              */
+  int32_t path;                 /* SWM_PATH_*                                      */
+  int32_t reserved;
+} swm_gpu_config;
+
+/* field ids for swm_gpu_get_field / swm_gpu_set_field (registry names of
+   vars_module.f90:67-104 in brackets) */
+enum {
+  SWM_F_U = 0,        /* SWM_u(:,:,N0)    [SWM_U]   */
+  SWM_F_V,            /* SWM_v(:,:,N0)    [SWM_V]   */
+  SWM_F_ETA,          /* SWM_eta(:,:,N0)  [SWM_ETA] */
+  SWM_F_D, SWM_F_DH, SWM_F_DU, SWM_F_DV,
+  SWM_F_EDENS, SWM_F_POT, SWM_F_ZETA, SWM_F_MU, SWM_F_MV,
+  SWM_F_H, SWM_F_HU, SWM_F_HV, SWM_F_HETA,
+  SWM_F_IMPL_U, SWM_F_IMPL_V, SWM_F_IMPL_ETA,
+  SWM_F_GAMMA_LIN_U, SWM_F_GAMMA_LIN_V, SWM_F_GAMMA_LIN_ETA, SWM_F_GAMMA_SQ_U, SWM_F_GAMMA_SQ_V,
+  SWM_F_FX, SWM_F_FY, SWM_F_FETA,
+  SWM_F_U_BS, SWM_F_V_BS, SWM_F_ZETA_BS,
+  SWM_F_LATMIX_U, SWM_F_LATMIX_V,
+  SWM_F_GU, SWM_F_GV, SWM_F_GETA,  /* newest increment G(:,:,NG0) */
+  SWM_F_NFIELDS
+};
+
+/* damping (swm_damping_nl) and forcing (swm_forcing_nl) kinds */
+enum { SWM_TERM_GAMMA_LIN_U, SWM_TERM_GAMMA_LIN_V, SWM_TERM_GAMMA_LIN_ETA,
+       SWM_TERM_GAMMA_SQ_U, SWM_TERM_GAMMA_SQ_V };
+enum { SWM_DAMP_UNIFORM, SWM_DAMP_SPONGE, SWM_DAMP_FILE };
+enum { SWM_SPONGE_N = 1, SWM_SPONGE_S = 2, SWM_SPONGE_W = 4, SWM_SPONGE_E = 8 };
+enum { SWM_FRC_WIND, SWM_FRC_OSC, SWM_FRC_CUSTOM, SWM_FRC_HEAT, SWM_FRC_EMF };
+enum { SWM_CMP_ZONAL, SWM_CMP_MERID, SWM_CMP_CONT, SWM_CMP_U2, SWM_CMP_V2, SWM_CMP_REY };
+
+typedef struct swm_gpu_ctx swm_gpu_ctx;
+
+/* ---- context ---- */
+const char *swm_gpu_last_error(void);
+int swm_gpu_create(const swm_gpu_config *cfg, swm_gpu_ctx **out);
+int swm_gpu_destroy(swm_gpu_ctx *ctx);
+int swm_gpu_synchronize(swm_gpu_ctx *ctx);
+/* the CUDA stream (cudaStream_t) every call of this context runs on */
+void *swm_gpu_stream(swm_gpu_ctx *ctx);
+/* number of kernels this context has launched so far */
+int64_t swm_gpu_launch_count(swm_gpu_ctx *ctx);
+
+/* ---- SWM_initSWM pieces (swm_module.f90:37-48) ---- */
+/* initDomain (domain_module.f90:49-207): grids, masks, depth on all grids,
+   metric and Coriolis; H may be NULL (closed 1 m basin), H_missing may be NULL */
+int swm_gpu_domain(swm_gpu_ctx *ctx, const double *H, const int8_t *H_missing);
+/* SWM_timestep_init (swm_nonlinear_timestep_module.f90:60-101); psi_bs only
+   for SWM_MODE_LIN_MEAN, else NULL */
+int swm_gpu_timestep_init(swm_gpu_ctx *ctx, const double *psi_bs);
+/* getDampingCoefficient (swm_damping_module.f90:137-203), one swm_damping_nl
+   record; file_data only for SWM_DAMP_FILE */
+int swm_gpu_add_damping(swm_gpu_ctx *ctx, int term, int type, double value, double sl_length,
+                        double sl_cutoff, int sponge_flags, const double *file_data);
+/* tail of SWM_damping_init (swm_damping_module.f90:78-115) */
+int swm_gpu_finish_damping(swm_gpu_ctx *ctx);
+/* SWM_forcing_initStream (swm_forcing_module.f90:592-646); d2 = imaginary part
+   for oscillating forcing; returns the stream id in *id */
+int swm_gpu_add_stream(swm_gpu_ctx *ctx, int type, int component, double omega, int is_constant,
+                       const double *d1, const double *d2, int *id);
+/* time-interpolated record of a time-dependent stream (memchunk getChunkData
+   output, swm_forcing_module.f90:319,356-357) -- one H2D copy */
+int swm_gpu_set_stream_data(swm_gpu_ctx *ctx, int id, const double *d1, const double *d2);
+/* same for a stream whose data is constant along each row: Ny values per
+   part (one H2D copy of Ny doubles); d2 may be NULL */
+int swm_gpu_set_stream_rows(swm_gpu_ctx *ctx, int id, const double *rows1, const double *rows2);
+/* SWM_forcing_init (swm_forcing_module.f90:78-127) */
+int swm_gpu_forcing_init(swm_gpu_ctx *ctx);
+/* SWM_initialConditions (swm_module.f90:156-181) */
+int swm_gpu_initial_conditions(swm_gpu_ctx *ctx, const double *eta, const double *u, const double *v);
+
+/* ---- time loop (model.f90:159-196) ---- */
+/* SWM_timestep -> SWM_timestep_step (swm_nonlinear_timestep_module.f90:164-180)
+   followed by TRC_timestep (tracer_module.f90:109-123) when tracers exist */
+int swm_gpu_step(swm_gpu_ctx *ctx, int64_t itt);
+/* model_advance (model.f90:238-259): SWM_advance (swm_module.f90:86-139) and
+   TRC_advance (tracer_module.f90:133-146) */
+int swm_gpu_advance(swm_gpu_ctx *ctx, int64_t itt);
+/* nsteps iterations of step+advance for itt = itt0+1 .. itt0+nsteps with no
+   time-dependent file forcing in between; replayed from a CUDA graph */
+int swm_gpu_run(swm_gpu_ctx *ctx, int64_t itt0, int64_t nsteps);
+
+/* ---- host access (the registry pointers the diagnostics read) ---- */
+int swm_gpu_get_field(swm_gpu_ctx *ctx, int field, double *host_out);
+int swm_gpu_set_field(swm_gpu_ctx *ctx, int field, const double *host_in);
+/* 1-D metric: which = 0 lat, 1 cos, 2 tan, 3 f; grid = 0 H, 1 u, 2 v, 3 eta */
+int swm_gpu_get_metric(swm_gpu_ctx *ctx, int which, int grid, double *host_out);
+int swm_gpu_get_mask(swm_gpu_ctx *ctx, int grid, int8_t *host_out);
+/* computeStreamfunction (calc_lib.f90:727-780) of the current u, v */
+int swm_gpu_streamfunction(swm_gpu_ctx *ctx, double *psi_out);
+/* Domain integrals of the current state, summed in FP64 on the device over
+   ocean points with the cell area A^2 cos(lat) dLambda dTheta:
+   out[0] = volume anomaly sum(eta * area), out[1] = sum(0.5 G eta^2 area),
+   out[2] = sum(0.5 u^2 area) over u points + sum(0.5 v^2 area) over v points.
+   No counterpart in the reference (its diagnostics write fields only); this
+   is the per-step scalar a monitoring loop reads back (16-24 bytes D2H). */
+int swm_gpu_integrals(swm_gpu_ctx *ctx, double *out3);
+
+/* ---- tracer (tracer_vars.f90:124-185, tracer_module.f90:58-342) ---- */
+int trc_gpu_add(swm_gpu_ctx *ctx, double kappa_h, double cons, double gamma_c, const double *C,
+                const double *C0, const double *gamma_field, const double *cons_field, int *id);
+int trc_gpu_init(swm_gpu_ctx *ctx);   /* TRC_initCoeffs (tracer_module.f90:291-342) */
+enum { TRC_F_CH, TRC_F_C, TRC_F_G, TRC_F_UHC, TRC_F_VHC, TRC_F_DIFF, TRC_F_IMPL };
+int trc_gpu_get_field(swm_gpu_ctx *ctx, int tracer, int field, double *host_out);
+
+/* ---- red-black SOR (ElSolv_SOR.f90) ---- */
+int elsolv_sor_gpu_init(swm_gpu_ctx *ctx);   /* init_ElSolv_SOR (:44-66) */
+/* main_ElSolv_SOR (:150-222); returns SWM_GPU_ENOT_CONVERGED when max_count
+   sweeps did not bring the correction norm below eps */
+int elsolv_sor_gpu_solve(swm_gpu_ctx *ctx, const double *B, double *chi, double eps, int first_guess,
+                         int *iterations, double *anorm);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

@@ -1,0 +1,1204 @@
+/*
+ * swm_oracle.c -- FP64 CPU restatement of the martinclaus/swm time-stepping
+ * hot path.  TEST INFRASTRUCTURE ONLY (see swm_oracle.h).
+ *
+ * Each function below names the Fortran routine it restates (file:line in the
+ * reference source tree).  Evaluation order follows the Fortran expressions
+ * left to right, so that with contraction disabled (-ffp-contract=off) the
+ * arithmetic is the reference's arithmetic.
+ *
+ * Parity quirks of the reference that are kept on purpose:
+ *  Q1  lagged Adams-Bashforth start: the increment ring starts at zero and is
+ *      read from slot 1 with tstep=min(3,itt) (time_integration_module.f90:93-109).
+ *  Q2  PI is a default-real literal, i.e. rounded to binary32 before it is
+ *      widened (grid_module.f90:6-7, swm_damping_module.f90:282-283); the
+ *      caller passes G/TAU_SCALE already rounded when they come from
+ *      default-real literals.
+ *  Q3  LINEARISED_MEAN_STATE eta flux uses ip1(j) as the zonal index
+ *      (swm_nonlinear_timestep_module.f90:360).
+ *  Q4  in linear modes Dh/Du/Dv alias H of the grids (swm_vars.f90:100-105),
+ *      so computeD overwrites the grid depths at itt=0.
+ *  Q6  tracer coefficients divide 0/0 on land-land pairs
+ *      (tracer_module.f90:318-333); reproduced unless tracer_nan_guard.
+ *  Q7  FULLY_NONLINEAR clamps eta >= minD - H_eta everywhere, land included
+ *      (swm_nonlinear_timestep_module.f90:176-179).
+ *  Q8  SOR uses a fixed Chebyshev schedule and an absolute stop on the
+ *      correction norm (ElSolv_SOR.f90:166-218).
+ */
+#include "swm_oracle.h"
+#include <math.h>
+#include <stdlib.h>
+#include <string.h>
+
+#define MAXSTREAMS 16
+#define MAXTRACERS 8
+
+typedef struct {
+  int type, comp, is_const;
+  double omega;
+  double *d1, *d2;
+} orc_stream;
+
+typedef struct {
+  double kappa_h;
+  double *CH[2];   /* TRC_N0, TRC_N0p1 */
+  double *G[3];    /* G_CH(:,:,1..3)   */
+  double *C, *C0, *gamma_c, *cons, *impl, *uhc, *vhc, *diff, *forcing;
+} orc_tracer;
+
+struct orc_model {
+  orc_config c;
+  int nx, ny, n;
+  int64_t itt;
+  double dLambda, dTheta, D2R;
+  int *ip1, *im1, *jp1, *jm1;
+  double *lat[16];                    /* ORC_LAT_* .. ORC_F_*            */
+  double *sin_lat[4];
+  int8_t *ocean[4];                   /* H, u, v, eta                    */
+  double *f[ORC_NFIELDS];             /* owned 2-D fields                */
+  double *D, *Dh, *Du, *Dv;           /* pointers: own or alias of H     */
+  double ab[6][6];                    /* ab_coeff(k, t), 1-based         */
+  int nstreams;
+  orc_stream streams[MAXSTREAMS];
+  int ntracers;
+  orc_tracer trc[MAXTRACERS];
+  double *trc_coeff;                  /* (12, Nx, Ny)                    */
+  double *sor_c;                      /* (Nx, Ny, 5)                     */
+  /* scratch */
+  double *w1, *w2;
+};
+
+#define IDX(i, j) ((i) + m->nx * (j))
+
+static double *zalloc(size_t n) { return (double *)calloc(n ? n : 1, sizeof(double)); }
+
+/* ------------------------------------------------------------------------ */
+/* Domain and grids: domain_module.f90:49-207, grid_module.f90:55-195       */
+/* ------------------------------------------------------------------------ */
+
+orc_model *orc_create(const orc_config *cfg, const double *H_in, const int8_t *H_missing) {
+  orc_model *m = (orc_model *)calloc(1, sizeof(orc_model));
+  m->c = *cfg;
+  int nx = cfg->nx, ny = cfg->ny, n = nx * ny;
+  m->nx = nx; m->ny = ny; m->n = n;
+  for (int k = 0; k < ORC_NFIELDS; k++) m->f[k] = zalloc(n);
+  m->w1 = zalloc(n); m->w2 = zalloc(n);
+  for (int k = 0; k < 16; k++) m->lat[k] = zalloc(ny);
+  for (int k = 0; k < 4; k++) { m->sin_lat[k] = zalloc(ny); m->ocean[k] = (int8_t *)calloc(n, 1); }
+  m->ip1 = (int *)malloc(sizeof(int) * nx); m->im1 = (int *)malloc(sizeof(int) * nx);
+  m->jp1 = (int *)malloc(sizeof(int) * ny); m->jm1 = (int *)malloc(sizeof(int) * ny);
+  /* ip1 = cshift(ip0, 1), im1 = cshift(ip0, -1): domain_module.f90:106-115 */
+  for (int i = 0; i < nx; i++) { m->ip1[i] = (i + 1) % nx; m->im1[i] = (i + nx - 1) % nx; }
+  for (int j = 0; j < ny; j++) { m->jp1[j] = (j + 1) % ny; m->jm1[j] = (j + ny - 1) % ny; }
+
+  /* PI is a default-real literal (Q2): grid_module.f90:6-7 */
+  const double PI = (double)(float)3.14159265358979323846;
+  m->D2R = PI / 180.;
+  m->dLambda = m->D2R * (cfg->lon_e - cfg->lon_s) / (nx - 1);   /* :97 */
+  m->dTheta = m->D2R * (cfg->lat_e - cfg->lat_s) / (ny - 1);    /* :98 */
+
+  /* coordinate vectors: domain_module.f90:120-127 */
+  double *lat_v = m->lat[ORC_LAT_V], *lat_H = m->lat[ORC_LAT_H];
+  double *lat_u = m->lat[ORC_LAT_U], *lat_e = m->lat[ORC_LAT_ETA];
+  for (int j = 0; j < ny; j++) {
+    lat_v[j] = j * (cfg->lat_e - cfg->lat_s) / (ny - 1) + cfg->lat_s;
+    lat_H[j] = lat_v[j];
+    lat_u[j] = lat_v[j] + (cfg->lat_e - cfg->lat_s) / (double)(float)(2.f * (ny - 1));
+    lat_e[j] = lat_u[j];
+  }
+
+  /* bathymetry: domain_module.f90:130-151 */
+  double *H = m->f[ORC_H];
+  if (H_in) {
+    for (int k = 0; k < n; k++) {
+      H[k] = H_in[k];
+      if (H_missing && H_missing[k]) H[k] = 0.;
+      if (H[k] <= 0.) H[k] = 0.;
+    }
+  } else {
+    for (int j = 0; j < ny; j++)
+      for (int i = 0; i < nx; i++) H[IDX(i, j)] = (i == 0 || i == nx - 1) ? 0. : 1.;
+  }
+  for (int i = 0; i < nx; i++) { H[IDX(i, 0)] = 0.; H[IDX(i, ny - 1)] = 0.; }
+
+  /* land / ocean masks: domain_module.f90:156-172 */
+  int8_t *oH = m->ocean[ORC_OCEAN_H], *oU = m->ocean[ORC_OCEAN_U];
+  int8_t *oV = m->ocean[ORC_OCEAN_V], *oE = m->ocean[ORC_OCEAN_ETA];
+  for (int j = 0; j < ny; j++)
+    for (int i = 0; i < nx; i++) oH[IDX(i, j)] = (H[IDX(i, j)] == 0.) ? 0 : 1;
+  for (int j = 0; j < ny; j++)
+    for (int i = 0; i < nx; i++) {
+      int lH = 1 - oH[IDX(i, j)];
+      int lHj = 1 - oH[IDX(i, m->jp1[j])];
+      int lHi = 1 - oH[IDX(m->ip1[i], j)];
+      int lHij = 1 - oH[IDX(m->ip1[i], m->jp1[j])];
+      oU[IDX(i, j)] = (lH + lHj == 2) ? 0 : 1;
+      oV[IDX(i, j)] = (lH + lHi == 2) ? 0 : 1;
+      oE[IDX(i, j)] = (lH + lHj + lHi + lHij == 4) ? 0 : 1;
+    }
+
+  /* depth on all grids: domain_module.f90:177-193 */
+  double *Hu = m->f[ORC_HU], *Hv = m->f[ORC_HV], *He = m->f[ORC_HETA];
+  for (int j = 0; j < ny; j++)
+    for (int i = 0; i < nx; i++) {
+      int k = IDX(i, j), ki = IDX(m->ip1[i], j), kj = IDX(i, m->jp1[j]);
+      int kij = IDX(m->ip1[i], m->jp1[j]);
+      if (oU[k]) Hu[k] = (H[k] + H[kj]) / (double)(oH[k] + oH[kj]);
+      if (oV[k]) Hv[k] = (H[k] + H[ki]) / (double)(oH[k] + oH[ki]);
+      if (oE[k]) He[k] = (H[k] + H[ki] + H[kj] + H[kij]) / (double)(oH[k] + oH[ki] + oH[kj] + oH[kij]);
+    }
+  if (cfg->H_overwrite != 0.) {
+    for (int k = 0; k < n; k++) {
+      H[k] = oH[k] * cfg->H_overwrite;
+      Hu[k] = oU[k] * cfg->H_overwrite;
+      Hv[k] = oV[k] * cfg->H_overwrite;
+      He[k] = oE[k] * cfg->H_overwrite;
+    }
+  }
+
+  /* setLat / setf / bc: grid_module.f90:55-74, 116-145, 167-195 */
+  for (int g = 0; g < 4; g++) {
+    double *lat = m->lat[ORC_LAT_H + g];
+    for (int j = 0; j < ny; j++) {
+      m->sin_lat[g][j] = sin(lat[j] * m->D2R);
+      m->lat[ORC_COS_H + g][j] = cos(lat[j] * m->D2R);
+      m->lat[ORC_TAN_H + g][j] = tan(lat[j] * m->D2R);
+    }
+    double rtheta0 = cfg->theta0 * m->D2R;
+    for (int j = 0; j < ny; j++) {
+      double fv;
+      switch (cfg->coriolis_approx) {
+        case 1: fv = 2 * cfg->OMEGA * sin(rtheta0); break;
+        case 2: fv = 2 * cfg->OMEGA * sin(rtheta0) + 2 * cfg->OMEGA * cos(rtheta0) * (m->D2R * lat[j]); break;
+        case 3: fv = 2 * cfg->OMEGA * m->sin_lat[g][j]; break;
+        default: fv = 0.; break;
+      }
+      m->lat[ORC_F_H + g][j] = fv;
+    }
+    double *bc = m->f[ORC_BC_H + g];
+    for (int k = 0; k < n; k++) bc[k] = (m->ocean[g][k] == 1) ? 1. : cfg->lbc;
+  }
+
+  /* swm_vars_init: swm_vars.f90:93-105 */
+  if (cfg->mode == ORC_MODE_NONLINEAR) {
+    m->D = m->f[ORC_D]; m->Dh = m->f[ORC_DH]; m->Du = m->f[ORC_DU]; m->Dv = m->f[ORC_DV];
+    for (int k = 0; k < n; k++) m->D[k] = m->Dh[k] = m->Du[k] = m->Dv[k] = 1.;
+  } else {
+    m->D = He; m->Dh = H; m->Du = Hu; m->Dv = Hv;
+  }
+  /* impl = 1 (swm_damping_module.f90:60-62) */
+  for (int k = 0; k < n; k++) m->f[ORC_IMPL_U][k] = m->f[ORC_IMPL_V][k] = m->f[ORC_IMPL_ETA][k] = 1.;
+
+  /* ab_coeff: time_integration_module.f90:44-50 */
+  memset(m->ab, 0, sizeof(m->ab));
+  double chi = cfg->ab_chi;
+  m->ab[1][1] = 1.;
+  m->ab[1][2] = -0.5 - chi; m->ab[2][2] = 1.5 + chi;
+  m->ab[1][3] = 5. / 12.; m->ab[2][3] = -16. / 12.; m->ab[3][3] = 23. / 12.;
+  m->itt = 0;
+  return m;
+}
+
+void orc_destroy(orc_model *m) {
+  if (!m) return;
+  for (int k = 0; k < ORC_NFIELDS; k++) free(m->f[k]);
+  for (int k = 0; k < 16; k++) free(m->lat[k]);
+  for (int k = 0; k < 4; k++) { free(m->sin_lat[k]); free(m->ocean[k]); }
+  free(m->ip1); free(m->im1); free(m->jp1); free(m->jm1);
+  free(m->w1); free(m->w2);
+  for (int s = 0; s < m->nstreams; s++) { free(m->streams[s].d1); free(m->streams[s].d2); }
+  for (int t = 0; t < m->ntracers; t++) {
+    orc_tracer *T = &m->trc[t];
+    free(T->CH[0]); free(T->CH[1]); free(T->G[0]); free(T->G[1]); free(T->G[2]);
+    free(T->C); free(T->C0); free(T->gamma_c); free(T->cons); free(T->impl);
+    free(T->uhc); free(T->vhc); free(T->diff); free(T->forcing);
+  }
+  free(m->trc_coeff); free(m->sor_c);
+  free(m);
+}
+
+double *orc_field(orc_model *m, int id) {
+  switch (id) {
+    case ORC_D: return m->D;
+    case ORC_DH: return m->Dh;
+    case ORC_DU: return m->Du;
+    case ORC_DV: return m->Dv;
+    default: return (id >= 0 && id < ORC_NFIELDS) ? m->f[id] : 0;
+  }
+}
+double *orc_lat(orc_model *m, int id) { return (id >= 0 && id < 16) ? m->lat[id] : 0; }
+int8_t *orc_ocean(orc_model *m, int id) { return (id >= 0 && id < 4) ? m->ocean[id] : 0; }
+void orc_get_scalars(const orc_model *m, double *dl, double *dt) { *dl = m->dLambda; *dt = m->dTheta; }
+void orc_set_itt(orc_model *m, int64_t itt) { m->itt = itt; }
+int64_t orc_get_itt(const orc_model *m) { return m->itt; }
+
+/* ------------------------------------------------------------------------ */
+/* Interpolators: calc_lib.f90:204-352 (weights recomputed from the masks,   */
+/* identical arithmetic to set2PointInterpolater / set4PointInterpolater)    */
+/* ------------------------------------------------------------------------ */
+static inline double ip2_noland(const double *v, const int8_t *msk, int k1, int k2) {
+  double w = 1. / fmax((double)(msk[k1] + msk[k2]), 1.);
+  return ((double)msk[k1] * w) * v[k1] + ((double)msk[k2] * w) * v[k2];
+}
+static inline double ip4_noland(const double *v, const int8_t *msk, int k1, int k2, int k3, int k4) {
+  double w = 1. / fmax((double)(msk[k1] + msk[k2] + msk[k3] + msk[k4]), 1.);
+  return ((double)msk[k1] * w) * v[k1] + ((double)msk[k2] * w) * v[k2] +
+         ((double)msk[k3] * w) * v[k3] + ((double)msk[k4] * w) * v[k4];
+}
+static inline double ip2(const double *v, int k1, int k2) { return .5 * v[k1] + .5 * v[k2]; }
+static inline double ip4(const double *v, int k1, int k2, int k3, int k4) {
+  return .25 * v[k1] + .25 * v[k2] + .25 * v[k3] + .25 * v[k4];
+}
+
+/* ------------------------------------------------------------------------ */
+/* Diagnostics of the nonlinear time step                                    */
+/* ------------------------------------------------------------------------ */
+
+/* computeD: swm_nonlinear_timestep_module.f90:182-218 */
+static void compute_D(orc_model *m) {
+  int nx = m->nx, ny = m->ny;
+  const int8_t *oE = m->ocean[ORC_OCEAN_ETA];
+  if (m->c.mode == ORC_MODE_NONLINEAR) {
+#pragma omp parallel for
+    for (int j = 0; j < ny; j++)
+      for (int i = 0; i < nx; i++) {
+        int k = IDX(i, j);
+        if (oE[k] != 1) continue;
+        m->D[k] = m->f[ORC_ETA0][k] + m->f[ORC_HETA][k];
+      }
+  }
+  int linear = (m->c.mode == ORC_MODE_LIN_REST || m->c.mode == ORC_MODE_LIN_MEAN);
+  if (linear && m->itt != 0) return;
+#pragma omp parallel for
+  for (int j = 0; j < ny; j++)
+    for (int i = 0; i < nx; i++) {
+      int k = IDX(i, j), im = m->im1[i], jm = m->jm1[j];
+      /* eta2H_noland: (i,j),(im1,jm1),(im1,j),(i,jm1); eta2u_noland: (i,j),(im1,j);
+         eta2v_noland: (i,j),(i,jm1) */
+      m->Dh[k] = ip4_noland(m->D, oE, k, IDX(im, jm), IDX(im, j), IDX(i, jm));
+      m->Du[k] = ip2_noland(m->D, oE, k, IDX(im, j));
+      m->Dv[k] = ip2_noland(m->D, oE, k, IDX(i, jm));
+    }
+}
+
+/* vorticityFromVelocities2D: calc_lib.f90:663-678 with pder_zonal3D :892-926
+   and pder_meridional3D :965-998 (out grid H, bc of H grid) */
+static void vorticity_uv(orc_model *m, const double *u, const double *v, double *zeta) {
+  int nx = m->nx, ny = m->ny;
+  const int8_t *oU = m->ocean[ORC_OCEAN_U], *oV = m->ocean[ORC_OCEAN_V];
+  const double *bcH = m->f[ORC_BC_H], *cH = m->lat[ORC_COS_H], *cU = m->lat[ORC_COS_U];
+  double A = m->c.A;
+#pragma omp parallel for
+  for (int j = 0; j < ny; j++)
+    for (int i = 0; i < nx; i++) {
+      int k = IDX(i, j), ki = IDX(m->im1[i], j), kj = IDX(i, m->jm1[j]);
+      double dvdx, dudy;
+      if (oV[ki] + oV[k] == 0) dvdx = 0.;
+      else dvdx = bcH[k] / (A * cH[j] * m->dLambda) * (v[k] - v[ki]);
+      if (oU[k] + oU[kj] == 0) dudy = 0.;
+      else dudy = bcH[k] * (cU[j] * u[k] - cU[m->jm1[j]] * u[kj]) / (A * m->dTheta);
+      zeta[k] = dvdx - dudy / cH[j];
+    }
+}
+
+/* computePotVort: swm_nonlinear_timestep_module.f90:230-257 */
+static void compute_pot(orc_model *m) {
+  int nx = m->nx, ny = m->ny, mode = m->c.mode;
+  if (mode == ORC_MODE_NONE) return;
+  const double eps = 2.220446049250313e-16; /* epsilon(1._8) */
+  const double *fH = m->lat[ORC_F_H];
+#pragma omp parallel for
+  for (int j = 0; j < ny; j++)
+    for (int i = 0; i < nx; i++) {
+      int k = IDX(i, j);
+      double pD = fmax(m->Dh[k], eps);
+      if (mode == ORC_MODE_NONLINEAR) m->f[ORC_POT][k] = (fH[j] + m->f[ORC_ZETA][k]) / pD;
+      else if (mode == ORC_MODE_LIN_MEAN) m->f[ORC_POT][k] = (fH[j] + m->f[ORC_ZETA_BS][k]) / pD;
+      else m->f[ORC_POT][k] = fH[j] / pD;
+    }
+}
+
+/* computeEdens: swm_nonlinear_timestep_module.f90:259-310 */
+static void compute_edens(orc_model *m) {
+  int nx = m->nx, ny = m->ny, mode = m->c.mode;
+  if (mode == ORC_MODE_NONE) return;
+  const double *u = m->f[ORC_U0], *v = m->f[ORC_V0], *eta = m->f[ORC_ETA0];
+  double *u2 = m->w1, *v2 = m->w2, G = m->c.G;
+  if (mode == ORC_MODE_NONLINEAR) {
+    for (int k = 0; k < m->n; k++) { u2[k] = u[k] * u[k]; v2[k] = v[k] * v[k]; }
+  } else if (mode == ORC_MODE_LIN_MEAN) {
+    for (int k = 0; k < m->n; k++) { u2[k] = u[k] * m->f[ORC_U_BS][k]; v2[k] = v[k] * m->f[ORC_V_BS][k]; }
+  }
+  const int8_t *oE = m->ocean[ORC_OCEAN_ETA];
+#pragma omp parallel for
+  for (int j = 0; j < ny; j++)
+    for (int i = 0; i < nx; i++) {
+      int k = IDX(i, j);
+      if (oE[k] != 1) continue; /* land: skip */
+      /* u2eta: (ip1, i); v2eta: (jp1, j) */
+      if (mode == ORC_MODE_NONLINEAR)
+        m->f[ORC_EDENS][k] = (ip2(u2, IDX(m->ip1[i], j), k) + ip2(v2, IDX(i, m->jp1[j]), k)) / 2. + G * eta[k];
+      else if (mode == ORC_MODE_LIN_MEAN)
+        m->f[ORC_EDENS][k] = (ip2(u2, IDX(m->ip1[i], j), k) + ip2(v2, IDX(i, m->jp1[j]), k)) + G * eta[k];
+      else
+        m->f[ORC_EDENS][k] = G * eta[k];
+    }
+}
+
+/* computeMassFluxes: swm_nonlinear_timestep_module.f90:312-326 */
+static void compute_massfluxes(orc_model *m) {
+  const int8_t *oU = m->ocean[ORC_OCEAN_U], *oV = m->ocean[ORC_OCEAN_V];
+#pragma omp parallel for
+  for (int k = 0; k < m->n; k++) {
+    if (oU[k] == 1) m->f[ORC_MU][k] = m->Du[k] * m->f[ORC_U0][k];
+    if (oV[k] == 1) m->f[ORC_MV][k] = m->Dv[k] * m->f[ORC_V0][k];
+  }
+}
+
+static void compute_diagnostics(orc_model *m) {
+  compute_D(m);
+  if (m->c.mode == ORC_MODE_NONLINEAR || m->c.mode == ORC_MODE_LIN_MEAN)
+    vorticity_uv(m, m->f[ORC_U0], m->f[ORC_V0], m->f[ORC_ZETA]);
+  compute_pot(m);
+  compute_edens(m);
+  compute_massfluxes(m);
+}
+
+/* ------------------------------------------------------------------------ */
+/* Lateral mixing: swm_lateralmixing_module.f90                              */
+/* ------------------------------------------------------------------------ */
+/* coefficient generators, SWM_LateralMixing_init :84-97 and
+   _init_p_coefficients :132-145; evaluated on the fly */
+static inline void latmix_u_coef(const orc_model *m, int i, int j, double *c) {
+  int k = IDX(i, j);
+  double bc = m->f[ORC_BC_U][k], A = m->c.A, tn = m->lat[ORC_TAN_U][j];
+  int o = m->ocean[ORC_OCEAN_H][k] + m->ocean[ORC_OCEAN_H][IDX(i, m->jp1[j])];
+  double o_tmp = (double)(o > 1 ? o : 1);
+  c[0] = -bc / A / m->lat[ORC_COS_U][j] / m->dLambda;
+  c[1] = -(bc / A / m->dTheta - 2. * tn / A / o_tmp);
+  c[2] = -(-bc / A / m->dTheta - 2. * tn / A / o_tmp);
+}
+static inline void latmix_v_coef(const orc_model *m, int i, int j, double *c) {
+  int k = IDX(i, j);
+  double bc = m->f[ORC_BC_V][k], A = m->c.A, tn = m->lat[ORC_TAN_V][j];
+  int o = m->ocean[ORC_OCEAN_ETA][k] + m->ocean[ORC_OCEAN_ETA][IDX(i, m->jm1[j])];
+  double o_tmp = (double)(o > 1 ? o : 1);
+  c[0] = -bc / A / m->lat[ORC_COS_V][j] / m->dLambda;
+  c[1] = -(-bc / A / m->dTheta + 2. * tn / A / o_tmp);
+  c[2] = -(bc / A / m->dTheta + 2. * tn / A / o_tmp);
+}
+static inline void pll_coef(const orc_model *m, double Ah, int i, int j, double *c) {
+  int k = IDX(i, j), kjp = IDX(i, m->jp1[j]);
+  double bc = m->f[ORC_BC_ETA][k], A = m->c.A, tn = m->lat[ORC_TAN_ETA][j];
+  int8_t ov = m->ocean[ORC_OCEAN_V][k], ovp = m->ocean[ORC_OCEAN_V][kjp];
+  int o = ov + ovp;
+  double o_tmp = (double)(o > 1 ? o : 1);
+  c[0] = -Ah * bc / m->dLambda / A / m->lat[ORC_COS_ETA][j];
+  c[1] = Ah / A * (bc / m->dTheta + ovp * tn / o_tmp);
+  c[2] = Ah / A * (-bc / m->dTheta + ov * tn / o_tmp);
+}
+static inline void plt_coef(const orc_model *m, double Ah, int i, int j, double *c) {
+  int k = IDX(i, j), kjm = IDX(i, m->jm1[j]);
+  double bc = m->f[ORC_BC_H][k], A = m->c.A, tn = m->lat[ORC_TAN_H][j];
+  int8_t ou = m->ocean[ORC_OCEAN_U][k], oum = m->ocean[ORC_OCEAN_U][kjm];
+  int o = ou + oum;
+  double o_tmp = (double)(o > 1 ? o : 1);
+  c[0] = -Ah * bc / m->dLambda / A / m->lat[ORC_COS_H][j];
+  c[1] = -Ah / A * (bc / m->dTheta + ou * tn / o_tmp);
+  c[2] = -Ah / A * (-bc / m->dTheta + oum * tn / o_tmp);
+}
+
+/* SWM_LateralMixing_compute_p (:215-240) and _compute_uv (:162-186) applied to
+   (u, v) with weights Dp (eta points) / Dhp (H points) and divisors Dup/Dvp.
+   pll/plt keep their previous values on land (never written there). */
+static void latmix_apply(orc_model *m, double Ah, const double *u, const double *v,
+                         const double *Dp, const double *Dhp, const double *Dup, const double *Dvp,
+                         double *pll, double *plt, double *lu, double *lv) {
+  int nx = m->nx, ny = m->ny;
+  const int8_t *oE = m->ocean[ORC_OCEAN_ETA], *oH = m->ocean[ORC_OCEAN_H];
+  const int8_t *oU = m->ocean[ORC_OCEAN_U], *oV = m->ocean[ORC_OCEAN_V];
+#pragma omp parallel for
+  for (int j = 0; j < ny; j++)
+    for (int i = 0; i < nx; i++) {
+      int k = IDX(i, j);
+      double c[3];
+      if (oE[k] == 1) {
+        pll_coef(m, Ah, i, j, c);
+        pll[k] = Dp[k] * (c[0] * (u[IDX(m->ip1[i], j)] - u[k]) + c[1] * v[IDX(i, m->jp1[j])] + c[2] * v[k]);
+      }
+      if (oH[k] == 1) {
+        plt_coef(m, Ah, i, j, c);
+        plt[k] = Dhp[k] * (c[0] * (v[k] - v[IDX(m->im1[i], j)]) + c[1] * u[k] + c[2] * u[IDX(i, m->jm1[j])]);
+      }
+    }
+#pragma omp parallel for
+  for (int j = 0; j < ny; j++)
+    for (int i = 0; i < nx; i++) {
+      int k = IDX(i, j);
+      double c[3];
+      if (oU[k] == 1) {
+        latmix_u_coef(m, i, j, c);
+        lu[k] = (c[0] * (pll[k] - pll[IDX(m->im1[i], j)]) + c[1] * plt[IDX(i, m->jp1[j])] + c[2] * plt[k]) / Dup[k];
+      }
+      if (oV[k] == 1) {
+        latmix_v_coef(m, i, j, c);
+        lv[k] = (c[0] * (plt[IDX(m->ip1[i], j)] - plt[k]) + c[1] * pll[k] + c[2] * pll[IDX(i, m->jm1[j])]) / Dvp[k];
+      }
+    }
+}
+
+/* SWM_LateralMixing_step: swm_lateralmixing_module.f90:157-160.
+   Biharmonic (project extension, no reference counterpart): the Laplacian-type
+   stress operator with Ah=1 and unit thickness gives (lu1, lv1); the
+   thickness-weighted operator applied to (lu1, lv1) with Ah=-bih gives the
+   biharmonic tendency. */
+static void latmix_step(orc_model *m) {
+  const double *u = m->f[ORC_U0], *v = m->f[ORC_V0];
+  if (m->c.mixing_kind == ORC_MIX_BIHARMONIC) {
+    int n = m->n;
+    double *one = (double *)malloc(sizeof(double) * n);
+    for (int k = 0; k < n; k++) one[k] = 1.;
+    double *pll1 = zalloc(n), *plt1 = zalloc(n), *lu1 = zalloc(n), *lv1 = zalloc(n);
+    latmix_apply(m, 1., u, v, one, one, one, one, pll1, plt1, lu1, lv1);
+    latmix_apply(m, -m->c.bih, lu1, lv1, m->D, m->Dh, m->Du, m->Dv, m->f[ORC_PLL], m->f[ORC_PLT],
+                 m->f[ORC_LATMIX_U], m->f[ORC_LATMIX_V]);
+    free(one); free(pll1); free(plt1); free(lu1); free(lv1);
+  } else {
+    latmix_apply(m, m->c.Ah, u, v, m->D, m->Dh, m->Du, m->Dv, m->f[ORC_PLL], m->f[ORC_PLT],
+                 m->f[ORC_LATMIX_U], m->f[ORC_LATMIX_V]);
+  }
+}
+
+/* ------------------------------------------------------------------------ */
+/* Tendencies + AB: swm_nonlinear_timestep_module.f90:328-449,              */
+/* time_integration_module.f90:74-112                                        */
+/* ------------------------------------------------------------------------ */
+static void integrate_ab(orc_model *m, const double *AN, double *const *G, const double *impl,
+                         int order, double *ANP1) {
+  int tstep = (int)(m->itt < order ? m->itt : order);
+  double dt = m->c.dt;
+  for (int k = 0; k < m->n; k++) {
+    double a = AN[k];
+    for (int ti = 1; ti <= tstep; ti++) a = a + dt * m->ab[ti][tstep] * G[ti - 1][k];
+    ANP1[k] = a / impl[k];
+  }
+}
+
+static void timestep_nonlinear(orc_model *m) {
+  int nx = m->nx, ny = m->ny, mode = m->c.mode;
+  const int8_t *oE = m->ocean[ORC_OCEAN_ETA], *oU = m->ocean[ORC_OCEAN_U], *oV = m->ocean[ORC_OCEAN_V];
+  const int8_t *oH = m->ocean[ORC_OCEAN_H];
+  const double *MU = m->f[ORC_MU], *MV = m->f[ORC_MV], *Pot = m->f[ORC_POT], *E = m->f[ORC_EDENS];
+  const double *eta = m->f[ORC_ETA0], *u = m->f[ORC_U0], *v = m->f[ORC_V0];
+  const double *ubs = m->f[ORC_U_BS], *vbs = m->f[ORC_V_BS], *zeta = m->f[ORC_ZETA];
+  const double *cV = m->lat[ORC_COS_V], *cE = m->lat[ORC_COS_ETA], *cU = m->lat[ORC_COS_U];
+  double A = m->c.A, dL = m->dLambda, dT = m->dTheta;
+  double *Geta = m->f[ORC_GETA3], *Gu = m->f[ORC_GU3], *Gv = m->f[ORC_GV3];
+  (void)oH;
+#pragma omp parallel for
+  for (int j = 0; j < ny; j++)
+    for (int i = 0; i < nx; i++) {
+      int k = IDX(i, j), ip = m->ip1[i], jp = m->jp1[j];
+      if (oE[k] != 1) continue;
+      double t = -(MU[IDX(ip, j)] - MU[k]) / dL - (MV[IDX(i, jp)] * cV[jp] - MV[k] * cV[j]) / dT;
+      if (mode == ORC_MODE_LIN_MEAN) {
+        /* Q3: zonal index ip1(j); the reference reads past ip1 when j > Nx,
+           which is undefined there -- wrapped here */
+        int qi = m->ip1[j % nx];
+        double e_a = ip2_noland(eta, oE, IDX(qi, j), IDX(m->im1[qi], j));
+        double e_b = ip2_noland(eta, oE, k, IDX(m->im1[i], j));
+        double e_c = ip2_noland(eta, oE, IDX(i, jp), IDX(i, m->jm1[jp]));
+        double e_d = ip2_noland(eta, oE, k, IDX(i, m->jm1[j]));
+        t = t - (e_a * ubs[IDX(ip, j)] - e_b * ubs[k]) / dL
+              - (cV[jp] * e_c * vbs[IDX(i, jp)] - cV[j] * e_d * vbs[k]) / dT;
+      }
+      Geta[k] = t / (A * cE[j]) + m->f[ORC_FETA][k];
+    }
+#pragma omp parallel for
+  for (int j = 0; j < ny; j++)
+    for (int i = 0; i < nx; i++) {
+      int k = IDX(i, j), im = m->im1[i], jp = m->jp1[j];
+      if (oU[k] != 1) continue;
+      /* H2u: (i,jp1),(i,j); v2u: (i,jp1),(im1,j),(im1,jp1),(i,j) */
+      int a1 = IDX(i, jp), a2 = IDX(im, j), a3 = IDX(im, jp);
+      double g = ip2(Pot, a1, k) * ip4(MV, a1, a2, a3, k);
+      if (mode == ORC_MODE_LIN_MEAN) g = g + ip2(zeta, a1, k) * ip4(vbs, a1, a2, a3, k);
+      g = g - ((E[k] - E[IDX(im, j)]) / (A * cU[j] * dL));
+      if (m->c.quadratic_friction) {
+        double vv = ip4(v, a1, a2, a3, k);
+        double q = m->f[ORC_GSQ_U][k] * sqrt(u[k] * u[k] + (vv * vv)) * u[k];
+        if (m->c.barotropic) q = q / m->f[ORC_HU][k];
+        g = g - q;
+      }
+      if (m->c.lateral_mixing) g = g + m->f[ORC_LATMIX_U][k];
+      Gu[k] = g + m->f[ORC_FX][k];
+    }
+#pragma omp parallel for
+  for (int j = 0; j < ny; j++)
+    for (int i = 0; i < nx; i++) {
+      int k = IDX(i, j), ip = m->ip1[i], jm = m->jm1[j];
+      if (oV[k] != 1) continue;
+      /* H2v: (ip1,j),(i,j); u2v: (ip1,j),(i,jm1),(i,j),(ip1,jm1) */
+      int a1 = IDX(ip, j), a2 = IDX(i, jm), a4 = IDX(ip, jm);
+      double g = -ip2(Pot, a1, k) * ip4(MU, a1, a2, k, a4);
+      if (mode == ORC_MODE_LIN_MEAN) g = g - ip2(zeta, a1, k) * ip4(ubs, a1, a2, k, a4);
+      g = g - ((E[k] - E[IDX(i, jm)]) / (A * dT));
+      if (m->c.quadratic_friction) {
+        double uu = ip4(u, a1, a2, k, a4);
+        double q = m->f[ORC_GSQ_V][k] * sqrt(v[k] * v[k] + (uu * uu)) * v[k];
+        if (m->c.barotropic) q = q / m->f[ORC_HV][k];
+        g = g - q;
+      }
+      if (m->c.lateral_mixing) g = g + m->f[ORC_LATMIX_V][k];
+      Gv[k] = g + m->f[ORC_FY][k];
+    }
+  double *Ge[3] = {m->f[ORC_GETA1], m->f[ORC_GETA2], m->f[ORC_GETA3]};
+  double *Gus[3] = {m->f[ORC_GU1], m->f[ORC_GU2], m->f[ORC_GU3]};
+  double *Gvs[3] = {m->f[ORC_GV1], m->f[ORC_GV2], m->f[ORC_GV3]};
+  integrate_ab(m, m->f[ORC_ETA0], Ge, m->f[ORC_IMPL_ETA], 3, m->f[ORC_ETA1]);
+  integrate_ab(m, m->f[ORC_U0], Gus, m->f[ORC_IMPL_U], 3, m->f[ORC_U1]);
+  integrate_ab(m, m->f[ORC_V0], Gvs, m->f[ORC_IMPL_V], 3, m->f[ORC_V1]);
+}
+
+/* SWM_timestep -> SWM_timestep_step: swm_nonlinear_timestep_module.f90:164-180 */
+void orc_swm_timestep(orc_model *m) {
+  if (m->c.lateral_mixing) latmix_step(m);
+  timestep_nonlinear(m);
+  if (m->c.mode == ORC_MODE_NONLINEAR) {
+    double *eta = m->f[ORC_ETA1];
+    const double *He = m->f[ORC_HETA];
+    double minD = m->c.minD;
+    for (int k = 0; k < m->n; k++)
+      if (eta[k] < (minD - He[k])) eta[k] = minD - He[k];
+  }
+}
+
+/* SWM_timestep_advance: swm_nonlinear_timestep_module.f90:129-155 */
+static void timestep_advance(orc_model *m) {
+  size_t bytes = sizeof(double) * m->n;
+  memcpy(m->f[ORC_GU1], m->f[ORC_GU2], bytes); memcpy(m->f[ORC_GU2], m->f[ORC_GU3], bytes);
+  memcpy(m->f[ORC_GV1], m->f[ORC_GV2], bytes); memcpy(m->f[ORC_GV2], m->f[ORC_GV3], bytes);
+  memcpy(m->f[ORC_GETA1], m->f[ORC_GETA2], bytes); memcpy(m->f[ORC_GETA2], m->f[ORC_GETA3], bytes);
+  compute_diagnostics(m);
+}
+
+/* ------------------------------------------------------------------------ */
+/* Forcing: swm_forcing_module.f90                                           */
+/* ------------------------------------------------------------------------ */
+int orc_forcing_add_stream(orc_model *m, int type, int comp, double omega, int is_const,
+                           const double *d1, const double *d2) {
+  if (m->nstreams >= MAXSTREAMS) return -1;
+  orc_stream *s = &m->streams[m->nstreams];
+  s->type = type; s->comp = comp; s->omega = omega;
+  /* SWM_forcing_initStream :627-638 */
+  if (type == ORC_FRC_OSC) s->is_const = 0;
+  else if (type == ORC_FRC_WIND && m->c.mode == ORC_MODE_NONLINEAR) s->is_const = 0;
+  else s->is_const = is_const;
+  s->d1 = zalloc(m->n); s->d2 = zalloc(m->n);
+  if (d1) memcpy(s->d1, d1, sizeof(double) * m->n);
+  if (d2) memcpy(s->d2, d2, sizeof(double) * m->n);
+  return m->nstreams++;
+}
+
+void orc_forcing_set_data(orc_model *m, int id, const double *d1, const double *d2) {
+  if (id < 0 || id >= m->nstreams) return;
+  if (d1) memcpy(m->streams[id].d1, d1, sizeof(double) * m->n);
+  if (d2) memcpy(m->streams[id].d2, d2, sizeof(double) * m->n);
+}
+
+/* SWM_forcing_processInputStream and the per-type routines :222-552 */
+static void process_stream(orc_model *m, orc_stream *s) {
+  int n = m->n, nx = m->nx, ny = m->ny;
+  double t = m->itt * m->c.dt;
+  const int8_t *oU = m->ocean[ORC_OCEAN_U], *oV = m->ocean[ORC_OCEAN_V], *oE = m->ocean[ORC_OCEAN_ETA];
+  double *Fx = s->is_const ? m->f[ORC_FX_CONST] : m->f[ORC_FX];
+  double *Fy = s->is_const ? m->f[ORC_FY_CONST] : m->f[ORC_FY];
+  double *Fe = s->is_const ? m->f[ORC_FETA_CONST] : m->f[ORC_FETA];
+  const double *d = s->d1;
+  switch (s->type) {
+    case ORC_FRC_WIND: { /* :274-324 */
+      double *F = (s->comp == ORC_CMP_ZONAL) ? Fx : Fy;
+      const int8_t *msk = (s->comp == ORC_CMP_ZONAL) ? oU : oV;
+      const double *H = (s->comp == ORC_CMP_ZONAL) ? m->Du : m->Dv;
+      int scale_h = m->c.barotropic || m->c.mode == ORC_MODE_NONLINEAR;
+      for (int k = 0; k < n; k++)
+        if (msk[k] == 1) F[k] = F[k] + (m->c.tau_scale * d[k] / (scale_h ? (m->c.RHO0 * H[k]) : m->c.RHO0));
+      break;
+    }
+    case ORC_FRC_OSC: { /* :326-374 (always the time dependent total) */
+      double *F = (s->comp == ORC_CMP_ZONAL) ? m->f[ORC_FX] : (s->comp == ORC_CMP_MERID) ? m->f[ORC_FY] : m->f[ORC_FETA];
+      const int8_t *msk = (s->comp == ORC_CMP_ZONAL) ? oU : (s->comp == ORC_CMP_MERID) ? oV : oE;
+      double r_iot = cos(s->omega * (double)m->itt * m->c.dt);
+      double i_iot = sin(s->omega * (double)m->itt * m->c.dt);
+      for (int k = 0; k < n; k++) F[k] = F[k] + (2. * (s->d1[k] * r_iot - s->d2[k] * i_iot)) * msk[k];
+      break;
+    }
+    case ORC_FRC_CUSTOM: { /* :396-434 */
+      double *F = (s->comp == ORC_CMP_ZONAL) ? Fx : (s->comp == ORC_CMP_MERID) ? Fy : Fe;
+      const int8_t *msk = (s->comp == ORC_CMP_ZONAL) ? oU : (s->comp == ORC_CMP_MERID) ? oV : oE;
+      for (int k = 0; k < n; k++) if (msk[k] == 1) F[k] = F[k] + d[k];
+      break;
+    }
+    case ORC_FRC_HEAT: /* :539-552 */
+      for (int k = 0; k < n; k++) if (oE[k] == 1) Fe[k] = Fe[k] + d[k];
+      break;
+    case ORC_FRC_EMF: { /* :451-523 */
+      double A = m->c.A, dL = m->dLambda, dT = m->dTheta;
+      const double *He = m->f[ORC_HETA], *Hu = m->f[ORC_HU], *Hv = m->f[ORC_HV], *H = m->f[ORC_H];
+      const double *cu = m->lat[ORC_COS_U], *cv = m->lat[ORC_COS_V];
+      for (int j = 0; j < ny; j++)
+        for (int i = 0; i < nx; i++) {
+          int k = IDX(i, j);
+#define H2ETA(ii, jj) ip4(d, IDX(m->ip1[ii], m->jp1[jj]), IDX(ii, jj), IDX(ii, m->jp1[jj]), IDX(m->ip1[ii], jj))
+          if (s->comp == ORC_CMP_U2) {
+            if (oU[k] != 1) continue;
+            int im = m->im1[i];
+            Fx[k] = Fx[k] + (-(H2ETA(i, j) * He[k] - H2ETA(im, j) * He[IDX(im, j)]) /
+                             (2 * A * dL * cu[j] * Hu[k]));
+          } else if (s->comp == ORC_CMP_V2) {
+            if (oV[k] != 1) continue;
+            int jm = m->jm1[j];
+            Fy[k] = Fy[k] + (-(cu[j] * He[k] * H2ETA(i, j) - cu[jm] * He[IDX(i, jm)] * H2ETA(i, jm)) /
+                             (8 * A * dT * cv[j] * Hv[k]));
+          } else {
+            int jp = m->jp1[j], ip = m->ip1[i];
+            if (oU[k] == 1)
+              Fx[k] = Fx[k] + (-(cv[jp] * d[IDX(i, jp)] * H[IDX(i, jp)] - cv[j] * d[k] * H[k]) /
+                               (2 * A * dT * cu[j] * Hu[k]));
+            if (oV[k] == 1)
+              Fy[k] = Fy[k] + (-(d[IDX(ip, j)] * H[IDX(ip, j)] - d[k] * H[k]) / (2 * A * dL * cv[j] * Hv[k]));
+          }
+#undef H2ETA
+        }
+      break;
+    }
+  }
+}
+
+/* SWM_forcing_getForcing :179-204; list order: head first, then the rest in
+   reverse insertion order (generic_list.f90 list_insert puts new nodes after
+   the head) */
+static void get_forcing(orc_model *m, int isTDF) {
+  if (m->nstreams == 0) return;
+  int order[MAXSTREAMS], no = 0;
+  order[no++] = 0;
+  for (int s = m->nstreams - 1; s >= 1; s--) order[no++] = s;
+  for (int q = 0; q < no; q++) {
+    orc_stream *s = &m->streams[order[q]];
+    if (isTDF != s->is_const) process_stream(m, s);
+  }
+}
+
+/* SWM_forcing_update :135-170 */
+void orc_forcing_update(orc_model *m) {
+  for (int k = 0; k < m->n; k++) {
+    m->f[ORC_FETA][k] = m->f[ORC_FETA_CONST][k];
+    m->f[ORC_FX][k] = m->f[ORC_FX_CONST][k];
+    m->f[ORC_FY][k] = m->f[ORC_FY_CONST][k];
+  }
+  get_forcing(m, 1);
+}
+
+/* SWM_forcing_init :78-127 */
+void orc_forcing_init(orc_model *m) {
+  get_forcing(m, 0);
+  orc_forcing_update(m);
+}
+
+/* ------------------------------------------------------------------------ */
+/* Damping: swm_damping_module.f90:44-359                                   */
+/* ------------------------------------------------------------------------ */
+/* getDampingCoefficient :137-203 with getSpongeLayer :257-359.
+   The source combines namelist entries with max(); the selfcheck/test_diaglist
+   fixtures were written by a build that added the entries (gamma_n.nc equals
+   file + sponge to 2e-15 there), so damping_additive builds each entry on a
+   zero field and adds it. */
+void orc_damping_add(orc_model *m, int term, int type, double value, double sl_length,
+                     double sl_cutoff, int loc, const double *file_data) {
+  double *coef, *target = 0;
+  int grid; /* 1 u, 2 v, 3 eta (getSpongeLayer iGrid) */
+  switch (term) {
+    case ORC_TERM_GLIN_U: coef = m->f[ORC_GLIN_U]; grid = 1; break;
+    case ORC_TERM_GLIN_V: coef = m->f[ORC_GLIN_V]; grid = 2; break;
+    case ORC_TERM_GLIN_ETA: coef = m->f[ORC_GLIN_ETA]; grid = 3; break;
+    case ORC_TERM_GSQ_U: coef = m->f[ORC_GSQ_U]; grid = 1; break;
+    default: coef = m->f[ORC_GSQ_V]; grid = 2; break;
+  }
+  if (m->c.damping_additive) { target = coef; coef = zalloc(m->n); }
+  int nx = m->nx, ny = m->ny;
+  if (type == ORC_DAMP_UNIFORM) {
+    for (int k = 0; k < m->n; k++) coef[k] = fmax(coef[k], value);
+  } else if (type == ORC_DAMP_FILE) {
+    for (int k = 0; k < m->n; k++) coef[k] = fmax(file_data[k], coef[k]);
+  } else {
+    /* getSpongeLayer :257-359 (SPONGE_SCALE_UNIT == SCU_DEGREE) */
+    const double PI = (double)(float)3.14159265358979323846;
+    const double D2R = PI / 180.;
+    const double *lat = m->lat[ORC_LAT_H + grid];
+    const double *lon_g;
+    double *lon = zalloc(nx);
+    /* lon of the grids: lon_u = lon_H, lon_v = lon_eta = lon_H + dlon/2 */
+    for (int i = 0; i < nx; i++) {
+      double lonH = i * (m->c.lon_e - m->c.lon_s) / (nx - 1) + m->c.lon_s;
+      lon[i] = (grid == 1) ? lonH : lonH + (m->c.lon_e - m->c.lon_s) / (double)(float)(2.f * (nx - 1));
+    }
+    lon_g = lon;
+    double sc = D2R * m->c.A / sl_length / (D2R * m->c.A);
+    /* iSponge(boundary, grid): S, N, W, E (1-based Fortran indices) */
+    int iS[3][4] = {{1, ny - 1, 2, nx - 1}, {2, ny - 1, 1, nx - 1}, {1, ny - 1, 1, nx - 1}};
+    int *is = iS[grid - 1];
+    double ecut = exp(-sl_cutoff);
+    if (loc & ORC_SPONGE_N) {
+      double lb = lat[is[1] - 1];
+      for (int j = 0; j < ny; j++) {
+        double g = value * (exp(-fabs(lat[j] - lb) * sc) - ecut);
+        for (int i = 0; i < nx; i++) coef[IDX(i, j)] = fmax(g, coef[IDX(i, j)]);
+      }
+    }
+    if (loc & ORC_SPONGE_S) {
+      double lb = lat[is[0] - 1];
+      for (int j = 0; j < ny; j++) {
+        double g = value * (exp(-fabs(lat[j] - lb) * sc) - ecut);
+        for (int i = 0; i < nx; i++) coef[IDX(i, j)] = fmax(g, coef[IDX(i, j)]);
+      }
+    }
+    if (loc & ORC_SPONGE_W) {
+      double lb = lon_g[is[2] - 1];
+      for (int i = 0; i < nx; i++) {
+        double g = value * (exp(-fabs(lon_g[i] - lb) * sc) - ecut);
+        for (int j = 0; j < ny; j++) coef[IDX(i, j)] = fmax(g, coef[IDX(i, j)]);
+      }
+    }
+    if (loc & ORC_SPONGE_E) {
+      double lb = lon_g[is[3] - 1];
+      for (int i = 0; i < nx; i++) {
+        double g = value * (exp(-fabs(lon_g[i] - lb) * sc) - ecut);
+        for (int j = 0; j < ny; j++) coef[IDX(i, j)] = fmax(g, coef[IDX(i, j)]);
+      }
+    }
+    free(lon);
+  }
+  if (target) {
+    for (int k = 0; k < m->n; k++) target[k] = target[k] + coef[k];
+    free(coef);
+  }
+}
+
+/* tail of SWM_damping_init :78-115 */
+void orc_damping_finalize(orc_model *m) {
+  const int8_t *oU = m->ocean[ORC_OCEAN_U], *oV = m->ocean[ORC_OCEAN_V];
+  double *gu = m->f[ORC_GLIN_U], *gv = m->f[ORC_GLIN_V];
+  double *su = m->f[ORC_GSQ_U], *sv = m->f[ORC_GSQ_V];
+  double *Hu = m->f[ORC_HU], *Hv = m->f[ORC_HV];
+  if (m->c.barotropic) {
+    for (int k = 0; k < m->n; k++) {
+      if (oU[k] == 1) gu[k] = gu[k] / Hu[k];
+      if (oV[k] == 1) gv[k] = gv[k] / Hv[k];
+    }
+    if (m->c.quadratic_friction)
+      for (int k = 0; k < m->n; k++) {
+        if (oU[k] == 1) su[k] = su[k] / Hu[k];
+        if (oV[k] == 1) sv[k] = sv[k] / Hv[k];
+      }
+  }
+  for (int k = 0; k < m->n; k++) {
+    m->f[ORC_IMPL_U][k] = 1. + m->c.dt * gu[k];
+    m->f[ORC_IMPL_V][k] = 1. + m->c.dt * gv[k];
+    m->f[ORC_IMPL_ETA][k] = 1. + m->c.dt * m->f[ORC_GLIN_ETA][k];
+  }
+}
+
+/* ------------------------------------------------------------------------ */
+/* SWM_timestep_init (:60-101) and basic state (evaluateStreamfunction2D     */
+/* calc_lib.f90:812-878, laplacian2D :1174-1206)                             */
+/* ------------------------------------------------------------------------ */
+/* psi_bs = getChunkData(SWM_MC_bs_psi, 0) (SWM_timestep_init :82).  The
+   test_diaglist fixtures were written by a build that saw psi_bs = 0 on land
+   H points (potvort.nc agrees to 2e-14 only then); mask_psi_bs reproduces it. */
+void orc_set_psi_bs(orc_model *m, const double *psi) {
+  for (int k = 0; k < m->n; k++)
+    m->f[ORC_PSI_BS][k] = m->c.mask_psi_bs ? psi[k] * m->ocean[ORC_OCEAN_H][k] : psi[k];
+}
+
+static void basic_state(orc_model *m) {
+  int nx = m->nx, ny = m->ny;
+  const double *psi = m->f[ORC_PSI_BS];
+  const int8_t *oH = m->ocean[ORC_OCEAN_H], *oU = m->ocean[ORC_OCEAN_U], *oV = m->ocean[ORC_OCEAN_V];
+  const double *bcU = m->f[ORC_BC_U], *bcV = m->f[ORC_BC_V];
+  const double *cV = m->lat[ORC_COS_V], *cH = m->lat[ORC_COS_H];
+  double A = m->c.A, dL = m->dLambda, dT = m->dTheta;
+  double *ubs = m->f[ORC_U_BS], *vbs = m->f[ORC_V_BS], *zbs = m->f[ORC_ZETA_BS];
+  for (int j = 0; j < ny; j++)
+    for (int i = 0; i < nx; i++) {
+      int k = IDX(i, j), kj = IDX(i, m->jp1[j]), ki = IDX(m->ip1[i], j);
+      /* evSF_zonal: u = -pder_meridional(psi, H_grid) [/H_u] */
+      double dy = (oH[kj] + oH[k] == 0) ? 0. : bcU[k] * (psi[kj] - psi[k]) / (A * dT);
+      ubs[k] = -dy;
+      if (m->c.barotropic && oU[k] == 1) ubs[k] = ubs[k] / m->f[ORC_HU][k];
+      /* evSF_meridional: v = pder_zonal(psi, H_grid) [/H_v] */
+      double dx = (oH[ki] + oH[k] == 0) ? 0. : bcV[k] / (A * cV[j] * dL) * (psi[ki] - psi[k]);
+      vbs[k] = dx;
+      if (m->c.barotropic && oV[k] == 1) vbs[k] = vbs[k] / m->f[ORC_HV][k];
+    }
+  /* zeta_bs = laplacian2D(psi, H_grid): bcx = v_grid%bc (ip0/im1), bcy = u_grid%bc (jp0/jm1) */
+  for (int j = 0; j < ny; j++)
+    for (int i = 0; i < nx; i++) {
+      int k = IDX(i, j);
+      if (oH[k] != 1) { zbs[k] = 0.; continue; }
+      int ip = m->ip1[i], im = m->im1[i], jp = m->jp1[j], jm = m->jm1[j];
+      double t1 = 1 / ((A * cH[j] * dL) * (A * cH[j] * dL)) *
+                  (bcV[k] * (psi[IDX(ip, j)] - psi[k]) - bcV[IDX(im, j)] * (psi[k] - psi[IDX(im, j)]));
+      double t2 = 1 / (A * A * cH[j] * (dT * dT)) *
+                  (bcU[k] * (cH[jp] * psi[IDX(i, jp)] - cH[j] * psi[k]) -
+                   bcU[IDX(i, jm)] * (cH[j] * psi[k] - cH[jm] * psi[IDX(i, jm)]));
+      zbs[k] = t1 + t2;
+    }
+}
+
+void orc_timestep_init(orc_model *m) {
+  if (m->c.mode == ORC_MODE_LIN_MEAN) basic_state(m);
+  compute_diagnostics(m);
+}
+
+/* SWM_initialConditions: swm_module.f90:156-181 */
+void orc_initial_conditions(orc_model *m, const double *eta, const double *u, const double *v) {
+  int n = m->n;
+  for (int k = 0; k < n; k++) {
+    m->f[ORC_ETA0][k] = m->f[ORC_U0][k] = m->f[ORC_V0][k] = 0.;
+    m->f[ORC_ETA1][k] = eta ? m->ocean[ORC_OCEAN_ETA][k] * eta[k] : 0.;
+    m->f[ORC_U1][k] = u ? m->ocean[ORC_OCEAN_U][k] * u[k] : 0.;
+    m->f[ORC_V1][k] = v ? m->ocean[ORC_OCEAN_V][k] * v[k] : 0.;
+  }
+  orc_swm_advance(m);
+}
+
+/* SWM_advance: swm_module.f90:86-139 */
+void orc_swm_advance(orc_model *m) {
+  size_t b = sizeof(double) * m->n;
+  memcpy(m->f[ORC_ETA0], m->f[ORC_ETA1], b);
+  memcpy(m->f[ORC_U0], m->f[ORC_U1], b);
+  memcpy(m->f[ORC_V0], m->f[ORC_V1], b);
+  for (int k = 0; k < m->n; k++) {
+    m->f[ORC_TOT_U][k] = m->f[ORC_TOT_U][k] + m->f[ORC_U0][k];
+    m->f[ORC_TOT_V][k] = m->f[ORC_TOT_V][k] + m->f[ORC_V0][k];
+    m->f[ORC_TOT_ETA][k] = m->f[ORC_TOT_ETA][k] + m->f[ORC_ETA0][k];
+  }
+  timestep_advance(m);
+  orc_forcing_update(m);
+}
+
+/* model_advance: model.f90:238-259 */
+void orc_model_advance(orc_model *m) {
+  for (int k = 0; k < m->n; k++) m->f[ORC_TOT_U][k] = m->f[ORC_TOT_V][k] = m->f[ORC_TOT_ETA][k] = 0.;
+  orc_swm_advance(m);
+  orc_tracer_advance(m);
+}
+
+void orc_run(orc_model *m, int64_t nsteps) {
+  for (int64_t s = 0; s < nsteps; s++) {
+    m->itt += 1;
+    orc_swm_timestep(m);
+    orc_tracer_timestep(m);
+    orc_model_advance(m);
+  }
+}
+
+/* ------------------------------------------------------------------------ */
+/* computeStreamfunction (calc_lib.f90:727-780), no elliptic solver          */
+/* configured (u_nd = u).  Uses H_u/H_v of the domain (after Q4).            */
+/* ------------------------------------------------------------------------ */
+void orc_streamfunction(orc_model *m, const double *u, const double *v, double *psi) {
+  int nx = m->nx, ny = m->ny;
+  double A = m->c.A, dL = m->dLambda, dT = m->dTheta;
+  const int8_t *oU = m->ocean[ORC_OCEAN_U], *oV = m->ocean[ORC_OCEAN_V];
+  const double *Hu = m->f[ORC_HU], *Hv = m->f[ORC_HV], *cV = m->lat[ORC_COS_V];
+  int bt = m->c.barotropic;
+  for (int k = 0; k < m->n; k++) psi[k] = 0.;
+  /* psi(i,1) for i=1..Nx-1: sum over i..im1(Nx)=Nx-1 of [H_v] * ocean_v * v */
+  for (int i = 0; i < nx - 1; i++) {
+    double s = 0.;
+    for (int q = i; q <= nx - 2; q++) {
+      int k = IDX(q, 0);
+      s = s + (bt ? Hv[k] * oV[k] * v[k] : oV[k] * v[k]);
+    }
+    psi[IDX(i, 0)] = (-1) * s * A * cV[0] * dL;
+  }
+  for (int j = 1; j < ny; j++) {
+    double s = 0.;
+    for (int q = 0; q <= j - 1; q++) {
+      int k = IDX(nx - 1, q);
+      s = s + (bt ? Hu[k] * oU[k] * u[k] : oU[k] * u[k]);
+    }
+    psi[IDX(nx - 1, j)] = (-1) * s * A * dT;
+  }
+  for (int j = 1; j < ny; j++)
+    for (int i = 0; i < nx - 1; i++) {
+      double s1 = 0., s2 = 0.;
+      for (int q = i; q <= nx - 2; q++) { int k = IDX(q, j); s1 = s1 + (bt ? Hv[k] * v[k] : v[k]); }
+      for (int q = 0; q <= j - 1; q++) { int k = IDX(i, q); s2 = s2 + (bt ? Hu[k] * u[k] : u[k]); }
+      psi[IDX(i, j)] = ((-1) * s1 * A * cV[j] * dL + psi[IDX(nx - 1, j)] - s2 * A * dT + psi[IDX(i, 0)]) / 2.;
+    }
+}
+
+/* computeDivergence: calc_lib.f90:607-622 (pder_zonal(u_grid) out eta with
+   ind0=ip1, indm1=ip0; pder_meridional(v_grid) out eta with jp1/jp0) */
+void orc_divergence(orc_model *m, const double *u, const double *v, double *div) {
+  int nx = m->nx, ny = m->ny;
+  double A = m->c.A, dL = m->dLambda, dT = m->dTheta;
+  const int8_t *oU = m->ocean[ORC_OCEAN_U], *oV = m->ocean[ORC_OCEAN_V];
+  const double *bcE = m->f[ORC_BC_ETA], *cE = m->lat[ORC_COS_ETA], *cV = m->lat[ORC_COS_V];
+  for (int j = 0; j < ny; j++)
+    for (int i = 0; i < nx; i++) {
+      int k = IDX(i, j), ki = IDX(m->ip1[i], j), kj = IDX(i, m->jp1[j]);
+      double dx = (oU[k] + oU[ki] == 0) ? 0. : bcE[k] / (A * cE[j] * dL) * (u[ki] - u[k]);
+      double dy = (oV[kj] + oV[k] == 0) ? 0. : bcE[k] * (cV[m->jp1[j]] * v[kj] - cV[j] * v[k]) / (A * dT);
+      div[k] = dx + dy / cE[j];
+    }
+}
+
+/* ------------------------------------------------------------------------ */
+/* Tracer: tracer_vars.f90:124-185, tracer_module.f90:109-342               */
+/* ------------------------------------------------------------------------ */
+int orc_tracer_add(orc_model *m, double kappa_h, double cons, double gamma_c,
+                   const double *C, const double *C0, const double *gfield, const double *cfield) {
+  if (m->ntracers >= MAXTRACERS) return -1;
+  int n = m->n;
+  orc_tracer *T = &m->trc[m->ntracers];
+  T->kappa_h = kappa_h;
+  T->CH[0] = zalloc(n); T->CH[1] = zalloc(n);
+  for (int q = 0; q < 3; q++) T->G[q] = zalloc(n);
+  T->C = zalloc(n); T->C0 = zalloc(n); T->gamma_c = zalloc(n); T->cons = zalloc(n);
+  T->impl = zalloc(n); T->uhc = zalloc(n); T->vhc = zalloc(n); T->diff = zalloc(n); T->forcing = zalloc(n);
+  for (int k = 0; k < n; k++) {
+    T->C[k] = C ? C[k] : 0.;
+    T->C0[k] = C0 ? C0[k] : 0.;
+    T->cons[k] = cfield ? cfield[k] : cons;
+    T->gamma_c[k] = gfield ? gfield[k] : gamma_c;
+    T->CH[0][k] = m->D[k] * T->C[k];
+    T->impl[k] = 1. + m->c.dt * T->cons[k];
+  }
+  return m->ntracers++;
+}
+
+double *orc_tracer_field(orc_model *m, int t, int id) {
+  if (t < 0 || t >= m->ntracers) return 0;
+  orc_tracer *T = &m->trc[t];
+  switch (id) {
+    case ORC_TRC_CH0: return T->CH[0];
+    case ORC_TRC_CH1: return T->CH[1];
+    case ORC_TRC_G1: return T->G[0];
+    case ORC_TRC_G2: return T->G[1];
+    case ORC_TRC_G3: return T->G[2];
+    case ORC_TRC_C: return T->C;
+    case ORC_TRC_C0: return T->C0;
+    case ORC_TRC_GAMMA: return T->gamma_c;
+    case ORC_TRC_IMPL: return T->impl;
+    case ORC_TRC_UHC: return T->uhc;
+    case ORC_TRC_VHC: return T->vhc;
+    case ORC_TRC_DIFF: return T->diff;
+    case ORC_TRC_FORCING: return T->forcing;
+  }
+  return 0;
+}
+double *orc_tracer_coeff(orc_model *m) { return m->trc_coeff; }
+
+/* TRC_initCoeffs: tracer_module.f90:291-342 */
+void orc_tracer_init(orc_model *m) {
+  int nx = m->nx, ny = m->ny;
+  free(m->trc_coeff);
+  m->trc_coeff = zalloc((size_t)12 * m->n);
+  const int8_t *oE = m->ocean[ORC_OCEAN_ETA], *oU = m->ocean[ORC_OCEAN_U], *oV = m->ocean[ORC_OCEAN_V];
+  const double *cu = m->lat[ORC_COS_U], *cv = m->lat[ORC_COS_V], *ce = m->lat[ORC_COS_ETA];
+  double A = m->c.A, dL = m->dLambda, dT = m->dTheta;
+  int guard = m->c.tracer_nan_guard;
+  for (int j = 0; j < ny; j++)
+    for (int i = 0; i < nx; i++) {
+      int k = IDX(i, j), ip = m->ip1[i], im = m->im1[i], jp = m->jp1[j], jm = m->jm1[j];
+      double *c = m->trc_coeff + (size_t)12 * k;
+      double o0 = oE[k], oip = oE[IDX(ip, j)], oim = oE[IDX(im, j)], ojp = oE[IDX(i, jp)], ojm = oE[IDX(i, jm)];
+#define GD(den) ((guard && (den) == 0.) ? 1. : (den))
+      c[0] = -1. * oU[IDX(ip, j)] * oip / GD(oip + o0) / A / dL / ce[j];
+      c[1] = 1. * oU[k] * oim / GD(oim + o0) / A / dL / ce[j];
+      c[2] = -1. * oV[IDX(i, jp)] * cv[jp] * ojp / GD(ojp + o0) / A / dT / ce[j];
+      c[3] = 1. * oV[k] * cv[j] * ojm / GD(ojm + o0) / A / dT / ce[j];
+      c[4] = -1. * oU[IDX(ip, j)] * o0 / GD(oip + o0) / A / dL / ce[j];
+      c[5] = 1. * oU[k] * o0 / GD(oim + o0) / A / dL / ce[j];
+      c[6] = -1. * oV[IDX(i, jp)] * cv[jp] * o0 / GD(ojp + o0) / A / dT / ce[j];
+      c[7] = 1. * oV[k] * cv[j] * o0 / GD(ojm + o0) / A / dT / ce[j];
+#undef GD
+      c[8] = 1. * oU[IDX(ip, j)] / (dL * dL) / (A * A) / cu[j] / ce[j];
+      c[9] = -1. * oU[k] / (dL * dL) / (A * A) / cu[j] / ce[j];
+      c[10] = 1. * oV[IDX(i, jp)] * cv[jp] / (dT * dT) / (A * A) / ce[j];
+      c[11] = -1. * oV[k] * cv[j] / (dT * dT) / (A * A) / ce[j];
+    }
+}
+
+/* TRC_tracer_incr (:154-209) + TRC_tracer_integrate (:216-232) */
+void orc_tracer_timestep(orc_model *m) {
+  int nx = m->nx, ny = m->ny;
+  const int8_t *oE = m->ocean[ORC_OCEAN_ETA];
+  const double *h = m->D, *hu = m->Du, *hv = m->Dv;
+  const double *u = m->f[ORC_TOT_U], *v = m->f[ORC_TOT_V];
+  for (int t = 0; t < m->ntracers; t++) {
+    orc_tracer *T = &m->trc[t];
+    const double *CH = T->CH[0], *C = T->C;
+    double *GCH = T->G[2], kap = T->kappa_h;
+    for (int j = 0; j < ny; j++)
+      for (int i = 0; i < nx; i++) {
+        int k = IDX(i, j);
+        if (oE[k] == 0) continue; /* land */
+        const double *c = m->trc_coeff + (size_t)12 * k;
+        int ip = IDX(m->ip1[i], j), im = IDX(m->im1[i], j), jp = IDX(i, m->jp1[j]), jm = IDX(i, m->jm1[j]);
+        T->diff[k] = kap * hu[ip] * (C[ip] - C[k]) * c[8] + kap * hu[k] * (C[k] - C[im]) * c[9] +
+                     kap * hv[jp] * (C[jp] - C[k]) * c[10] + kap * hv[k] * (C[k] - C[jm]) * c[11];
+      }
+    for (int k = 0; k < m->n; k++) T->forcing[k] = C[k] * m->f[ORC_FETA][k];
+    for (int j = 0; j < ny; j++)
+      for (int i = 0; i < nx; i++) {
+        int k = IDX(i, j);
+        const double *c = m->trc_coeff + (size_t)12 * k;
+        int ip = IDX(m->ip1[i], j), im = IDX(m->im1[i], j), jp = IDX(i, m->jp1[j]), jm = IDX(i, m->jm1[j]);
+        GCH[k] = (CH[ip] * u[ip] * c[0] + CH[im] * u[k] * c[1] + CH[jp] * v[jp] * c[2] + CH[jm] * v[k] * c[3] +
+                  CH[k] * u[ip] * c[4] + CH[k] * u[k] * c[5] + CH[k] * v[jp] * c[6] + CH[k] * v[k] * c[7] +
+                  T->diff[k] - T->gamma_c[k] * h[k] * (C[k] - T->C0[k]) + T->forcing[k]);
+      }
+    integrate_ab(m, T->CH[0], T->G, T->impl, 3, T->CH[1]);
+  }
+}
+
+/* TRC_tracer_advance: tracer_module.f90:237-280 */
+void orc_tracer_advance(orc_model *m) {
+  int nx = m->nx, ny = m->ny;
+  size_t b = sizeof(double) * m->n;
+  for (int t = 0; t < m->ntracers; t++) {
+    orc_tracer *T = &m->trc[t];
+    memcpy(T->G[0], T->G[1], b); memcpy(T->G[1], T->G[2], b);
+    memcpy(T->CH[0], T->CH[1], b);
+    for (int k = 0; k < m->n; k++) T->C[k] = T->CH[0][k] / m->D[k];
+    for (int j = 0; j < ny; j++)
+      for (int i = 0; i < nx; i++) {
+        int k = IDX(i, j);
+        T->uhc[k] = m->f[ORC_MU][k] * .5 * (T->C[k] + T->C[IDX(m->im1[i], j)]);
+        T->vhc[k] = m->f[ORC_MV][k] * .5 * (T->C[k] + T->C[IDX(i, m->jm1[j])]);
+      }
+  }
+}
+
+/* ------------------------------------------------------------------------ */
+/* Red-black SOR: ElSolv_SOR.f90:44-222                                      */
+/* ------------------------------------------------------------------------ */
+void orc_sor_init(orc_model *m) {
+  int nx = m->nx, ny = m->ny, n = m->n;
+  free(m->sor_c);
+  m->sor_c = zalloc((size_t)5 * n);
+  const int8_t *oU = m->ocean[ORC_OCEAN_U], *oV = m->ocean[ORC_OCEAN_V];
+  const double *cE = m->lat[ORC_COS_ETA], *cV = m->lat[ORC_COS_V];
+  double A = m->c.A, dL = m->dLambda, dT = m->dTheta;
+  for (int j = 0; j < ny; j++)
+    for (int i = 0; i < nx; i++) {
+      int k = IDX(i, j), ki = IDX(m->ip1[i], j), kj = IDX(i, m->jp1[j]);
+      double ax = (A * cE[j] * dL) * (A * cE[j] * dL);
+      double ay = (A * A * cE[j] * (dT * dT));
+      m->sor_c[k] = oU[ki] / ax;
+      m->sor_c[k + n] = oU[k] / ax;
+      m->sor_c[k + 2 * n] = cV[m->jp1[j]] * oV[kj] / ay;
+      m->sor_c[k + 3 * n] = cV[j] * oV[k] / ay;
+      m->sor_c[k + 4 * n] = (-oU[ki] - oU[k]) / ax + (-cV[m->jp1[j]] * oV[kj] - cV[j] * oV[k]) / ay;
+    }
+}
+const double *orc_sor_coeff(orc_model *m) { return m->sor_c; }
+
+/* main_ElSolv_SOR: ElSolv_SOR.f90:150-222.  Returns iterations used (>0) or
+   -iterations when max_count was reached without convergence. */
+int orc_sor_solve(orc_model *m, const double *B, double *chi, double eps, int first_guess,
+                  double *anorm_out) {
+  int nx = m->nx, ny = m->ny, n = m->n;
+  int mx = nx > ny ? nx : ny;
+  int max_count = first_guess ? (int)lround(1000. * mx) : (int)lround(10. * mx);
+  const double rJ = (double)(float)9.9999178e-1; /* default-real literal (Q2/Q8) */
+  double relax = 1.;
+  const int8_t *oE = m->ocean[ORC_OCEAN_ETA];
+  const double *c = m->sor_c;
+  double anorm = 0.;
+  int l;
+  for (l = 1; l <= max_count; l++) {
+    anorm = 0.;
+    for (int oe = 1; oe <= 2; oe++) {
+      /* colour 1: i+j even (1-based) ; colour 2: odd */
+      for (int j = 0; j < ny; j++)
+        for (int i = 0; i < nx; i++) {
+          int par = ((i + 1) + (j + 1)) % 2 == 0 ? 1 : 2;
+          if (par != oe) continue;
+          int k = IDX(i, j);
+          if (oE[k] == 0) continue;
+          double res = relax * (c[k] * chi[IDX(m->ip1[i], j)] + c[k + n] * chi[IDX(m->im1[i], j)] +
+                                c[k + 2 * n] * chi[IDX(i, m->jp1[j])] + c[k + 3 * n] * chi[IDX(i, m->jm1[j])] +
+                                c[k + 4 * n] * chi[k] - B[k]) / c[k + 4 * n];
+          chi[k] = chi[k] - res;
+          anorm = anorm + res * res;
+        }
+      if (oe == 1 && l == 1) relax = 1. / (1. - .5 * rJ * rJ);
+      else relax = 1. / (1. - .25 * rJ * rJ * relax);
+    }
+    anorm = sqrt(anorm);
+    if (anorm < eps) { if (anorm_out) *anorm_out = anorm; return l; }
+  }
+  if (anorm_out) *anorm_out = sqrt(anorm);
+  return -(l - 1);
+}
+
+/* ------------------------------------------------------------------------ */
+/* Extension (no reference counterpart): variable-coefficient Helmholtz      */
+/*   div(H^-1 grad psi) - lambda psi = rhs, Dirichlet psi=0 on land.         */
+/* Face coefficients cx(i,j) couple (i-1,j)-(i,j), cy(i,j) couple (i,j-1)-   */
+/* (i,j); cc(i,j) is the diagonal.  mask=0 cells are fixed at 0.             */
+/* ------------------------------------------------------------------------ */
+void orc_helmholtz_apply(int nx, int ny, const double *cx, const double *cy, const double *cc,
+                         const int8_t *mask, const double *psi, double *out) {
+  for (int j = 0; j < ny; j++)
+    for (int i = 0; i < nx; i++) {
+      size_t k = (size_t)i + (size_t)nx * j;
+      if (!mask[k]) { out[k] = 0.; continue; }
+      double w = i > 0 ? psi[k - 1] : 0., e = i < nx - 1 ? psi[k + 1] : 0.;
+      double s = j > 0 ? psi[k - nx] : 0., nn = j < ny - 1 ? psi[k + nx] : 0.;
+      double ce = i < nx - 1 ? cx[k + 1] : 0., cn = j < ny - 1 ? cy[k + nx] : 0.;
+      out[k] = cx[k] * w + ce * e + cy[k] * s + cn * nn + cc[k] * psi[k];
+    }
+}
+
+int orc_helmholtz_sor(int nx, int ny, const double *cx, const double *cy, const double *cc,
+                      const int8_t *mask, const double *rhs, double *psi, double omega,
+                      double rtol, int max_sweeps, double *relres_out) {
+  size_t n = (size_t)nx * ny;
+  double *r = (double *)malloc(sizeof(double) * n);
+  double bn = 0.;
+  for (size_t k = 0; k < n; k++) if (mask[k]) bn += rhs[k] * rhs[k];
+  bn = sqrt(bn);
+  int sweeps = 0;
+  double rel = 1.;
+  while (sweeps < max_sweeps) {
+    for (int colour = 0; colour < 2; colour++)
+      for (int j = 0; j < ny; j++)
+        for (int i = (j + colour) & 1; i < nx; i += 2) {
+          size_t k = (size_t)i + (size_t)nx * j;
+          if (!mask[k]) continue;
+          double w = i > 0 ? psi[k - 1] : 0., e = i < nx - 1 ? psi[k + 1] : 0.;
+          double s = j > 0 ? psi[k - nx] : 0., nn = j < ny - 1 ? psi[k + nx] : 0.;
+          double ce = i < nx - 1 ? cx[k + 1] : 0., cn = j < ny - 1 ? cy[k + nx] : 0.;
+          double off = cx[k] * w + ce * e + cy[k] * s + cn * nn;
+          double gs = (rhs[k] - off) / cc[k];
+          psi[k] = psi[k] + omega * (gs - psi[k]);
+        }
+    sweeps++;
+    if (sweeps % 16 == 0 || sweeps == max_sweeps) {
+      orc_helmholtz_apply(nx, ny, cx, cy, cc, mask, psi, r);
+      double rn = 0.;
+      for (size_t k = 0; k < n; k++) if (mask[k]) { double d = rhs[k] - r[k]; rn += d * d; }
+      rel = bn > 0 ? sqrt(rn) / bn : sqrt(rn);
+      if (rel < rtol) break;
+    }
+  }
+  free(r);
+  if (relres_out) *relres_out = rel;
+  return sweeps;
+}

@@ -1,0 +1,476 @@
+// api.cu -- the extern "C" entry points of include/swm_gpu.h.
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+#include <mutex>
+#include "ctx.h"
+
+namespace swm {
+static thread_local std::string g_last_error;
+void set_error(const std::string &msg) { g_last_error = msg; }
+}  // namespace swm
+
+using namespace swm;
+
+swm::Dev swm_gpu_ctx::dev() const {
+  Dev d;
+  memset(&d, 0, sizeof(d));
+  d.nx = nx;
+  d.ny = ny;
+  d.mode = cfg.mode;
+  d.qbf = cfg.quadratic_friction;
+  d.barotropic = cfg.barotropic;
+  d.lateral_mixing = cfg.lateral_mixing;
+  d.dt = cfg.dt;
+  d.G = cfg.G;
+  d.A = cfg.A;
+  d.dLambda = hg.dLambda;
+  d.dTheta = hg.dTheta;
+  d.minD = cfg.minD;
+  d.tau_scale = cfg.tau_scale;
+  d.RHO0 = cfg.RHO0;
+  d.lbc = cfg.lbc;
+  for (int q = 0; q < 4; q++) {
+    d.ocean[q] = d_ocean[q];
+    d.cosl[q] = d_cos[q];
+    d.tanl[q] = d_tan[q];
+    d.f[q] = d_f[q];
+    d.Hg[q] = d_H[q];
+  }
+  d.u0 = u[n0];
+  d.v0 = v[n0];
+  d.eta0 = eta[n0];
+  d.u1 = u[1 - n0];
+  d.v1 = v[1 - n0];
+  d.eta1 = eta[1 - n0];
+  for (int s = 0; s < 3; s++) {
+    d.Gu[s] = Gu[(g0 + s) % 3];
+    d.Gv[s] = Gv[(g0 + s) % 3];
+    d.Ge[s] = Ge[(g0 + s) % 3];
+  }
+  if (cfg.mode == SWM_MODE_NONLINEAR) {
+    d.D = Dbuf[0];
+    d.Dh = Dbuf[1];
+    d.Du = Dbuf[2];
+    d.Dv = Dbuf[3];
+  } else {  // swm_vars.f90:100-105: the thickness arrays are the grid depths
+    d.D = d_H[GE];
+    d.Dh = d_H[GH];
+    d.Du = d_H[GU];
+    d.Dv = d_H[GV];
+  }
+  d.edens = edens;
+  d.pot = pot;
+  d.zeta = zeta;
+  d.mu = mu;
+  d.mv = mv;
+  d.pll = pll;
+  d.plt = plt;
+  d.lmu = lmu;
+  d.lmv = lmv;
+  d.impl_u = impl[0];
+  d.impl_v = impl[1];
+  d.impl_e = impl[2];
+  d.gsq_u = gsq[0];
+  d.gsq_v = gsq[1];
+  d.Fx = F[0];
+  d.Fy = F[1];
+  d.Fe = F[2];
+  d.Fxc = Fc[0];
+  d.Fyc = Fc[1];
+  d.Fec = Fc[2];
+  d.ubs = ubs;
+  d.vbs = vbs;
+  d.zbs = zbs;
+  return d;
+}
+
+static int dalloc(double **p, size_t n) {
+  cudaError_t e = cudaMalloc((void **)p, n * sizeof(double));
+  if (e != cudaSuccess) {
+    set_error(std::string("cudaMalloc: ") + cudaGetErrorString(e));
+    return SWM_GPU_ENOMEM;
+  }
+  e = cudaMemset(*p, 0, n * sizeof(double));
+  if (e != cudaSuccess) {
+    set_error(std::string("cudaMemset: ") + cudaGetErrorString(e));
+    return SWM_GPU_ECUDA;
+  }
+  return SWM_GPU_OK;
+}
+
+#define TRY(x)                  \
+  do {                          \
+    int rc_ = (x);              \
+    if (rc_ != SWM_GPU_OK) return rc_; \
+  } while (0)
+
+static int h2d(swm_gpu_ctx *c, double *dst, const double *src, size_t count) {
+  SWM_CK(cudaMemcpyAsync(dst, src, count * sizeof(double), cudaMemcpyHostToDevice, c->stream));
+  return SWM_GPU_OK;
+}
+static int d2h(swm_gpu_ctx *c, double *dst, const double *src, size_t count) {
+  SWM_CK(cudaMemcpyAsync(dst, src, count * sizeof(double), cudaMemcpyDeviceToHost, c->stream));
+  SWM_CK(cudaStreamSynchronize(c->stream));
+  return SWM_GPU_OK;
+}
+
+static void invalidate_graph(swm_gpu_ctx *c) {
+  if (c->graph) {
+    cudaGraphExecDestroy(c->graph);
+    c->graph = nullptr;
+  }
+}
+
+extern "C" {
+
+const char *swm_gpu_last_error(void) { return g_last_error.c_str(); }
+
+int swm_gpu_create(const swm_gpu_config *cfg, swm_gpu_ctx **out) {
+  SWM_REQUIRE(cfg && out, "swm_gpu_create: null argument");
+  SWM_REQUIRE(cfg->nx >= 3 && cfg->ny >= 3, "swm_gpu_create: Nx and Ny must be >= 3");
+  SWM_REQUIRE(cfg->dt > 0, "swm_gpu_create: dt must be positive");
+  SWM_REQUIRE(cfg->mode >= 0 && cfg->mode <= 3, "swm_gpu_create: unknown mode");
+  SWM_REQUIRE(cfg->path >= 0 && cfg->path <= 2, "swm_gpu_create: unknown path");
+  int ndev = 0;
+  if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev == 0) {
+    set_error("swm_gpu_create: no CUDA device is visible");
+    return SWM_GPU_ECUDA;
+  }
+  swm_gpu_ctx *c = new swm_gpu_ctx();
+  c->cfg = *cfg;
+  c->nx = cfg->nx;
+  c->ny = cfg->ny;
+  c->n = (size_t)cfg->nx * cfg->ny;
+  cudaError_t e = cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking);
+  if (e != cudaSuccess) {
+    set_error(std::string("cudaStreamCreate: ") + cudaGetErrorString(e));
+    delete c;
+    return SWM_GPU_ECUDA;
+  }
+  *out = c;
+  return SWM_GPU_OK;
+}
+
+int swm_gpu_destroy(swm_gpu_ctx *c) {
+  if (!c) return SWM_GPU_OK;
+  cudaStreamSynchronize(c->stream);
+  invalidate_graph(c);
+  fused_free(c);
+  sor_free(c);
+  auto F = [](void *p) { if (p) cudaFree(p); };
+  for (int q = 0; q < 4; q++) {
+    F(c->d_ocean[q]); F(c->d_cos[q]); F(c->d_tan[q]); F(c->d_f[q]); F(c->d_lat[q]); F(c->d_H[q]);
+    F(c->Dbuf[q]); F(c->bh[q]);
+  }
+  for (int q = 0; q < 2; q++) { F(c->u[q]); F(c->v[q]); F(c->eta[q]); F(c->gsq[q]); }
+  for (int q = 0; q < 3; q++) { F(c->Gu[q]); F(c->Gv[q]); F(c->Ge[q]); F(c->impl[q]); F(c->glin[q]); F(c->F[q]); F(c->Fc[q]); }
+  F(c->edens); F(c->pot); F(c->zeta); F(c->mu); F(c->mv); F(c->pll); F(c->plt); F(c->lmu); F(c->lmv);
+  F(c->ones); F(c->ubs); F(c->vbs); F(c->zbs); F(c->trc_coeff);
+  for (auto &s : c->streams) { F(s.d1); F(s.d2); }
+  for (auto &t : c->tracers) {
+    F(t.CH[0]); F(t.CH[1]); F(t.G[0]); F(t.G[1]); F(t.G[2]); F(t.C); F(t.C0); F(t.gamma); F(t.impl);
+    F(t.uhc); F(t.vhc); F(t.diff);
+  }
+  cudaStreamDestroy(c->stream);
+  delete c;
+  return SWM_GPU_OK;
+}
+
+int swm_gpu_synchronize(swm_gpu_ctx *c) {
+  SWM_REQUIRE(c, "null context");
+  SWM_CK(cudaStreamSynchronize(c->stream));
+  return SWM_GPU_OK;
+}
+
+void *swm_gpu_stream(swm_gpu_ctx *c) { return c ? (void *)c->stream : nullptr; }
+int64_t swm_gpu_launch_count(swm_gpu_ctx *c) { return c ? c->launches : -1; }
+
+int swm_gpu_domain(swm_gpu_ctx *c, const double *H, const int8_t *Hmiss) {
+  SWM_REQUIRE(c && c->stage == 0, "swm_gpu_domain: call once, first");
+  TRY(host_domain(c, H, Hmiss));
+  size_t n = c->n;
+  int ny = c->ny;
+  const HostGrid &g = c->hg;
+  for (int q = 0; q < 4; q++) {
+    SWM_CK(cudaMalloc((void **)&c->d_ocean[q], n));
+    SWM_CK(cudaMemcpy(c->d_ocean[q], g.ocean[q].data(), n, cudaMemcpyHostToDevice));
+    TRY(dalloc(&c->d_cos[q], ny));
+    TRY(dalloc(&c->d_tan[q], ny));
+    TRY(dalloc(&c->d_f[q], ny));
+    TRY(dalloc(&c->d_lat[q], ny));
+    TRY(dalloc(&c->d_H[q], n));
+    SWM_CK(cudaMemcpy(c->d_cos[q], g.cosl[q].data(), ny * 8, cudaMemcpyHostToDevice));
+    SWM_CK(cudaMemcpy(c->d_tan[q], g.tanl[q].data(), ny * 8, cudaMemcpyHostToDevice));
+    SWM_CK(cudaMemcpy(c->d_f[q], g.f[q].data(), ny * 8, cudaMemcpyHostToDevice));
+    SWM_CK(cudaMemcpy(c->d_lat[q], g.lat[q].data(), ny * 8, cudaMemcpyHostToDevice));
+    SWM_CK(cudaMemcpy(c->d_H[q], g.H[q].data(), n * 8, cudaMemcpyHostToDevice));
+  }
+  for (int q = 0; q < 2; q++) {
+    TRY(dalloc(&c->u[q], n)); TRY(dalloc(&c->v[q], n)); TRY(dalloc(&c->eta[q], n));
+  }
+  for (int q = 0; q < 3; q++) {
+    TRY(dalloc(&c->Gu[q], n)); TRY(dalloc(&c->Gv[q], n)); TRY(dalloc(&c->Ge[q], n));
+    TRY(dalloc(&c->impl[q], n)); TRY(dalloc(&c->glin[q], n)); TRY(dalloc(&c->F[q], n)); TRY(dalloc(&c->Fc[q], n));
+  }
+  for (int q = 0; q < 2; q++) TRY(dalloc(&c->gsq[q], n));
+  TRY(dalloc(&c->edens, n)); TRY(dalloc(&c->pot, n)); TRY(dalloc(&c->zeta, n));
+  TRY(dalloc(&c->mu, n)); TRY(dalloc(&c->mv, n));
+  TRY(dalloc(&c->pll, n)); TRY(dalloc(&c->plt, n)); TRY(dalloc(&c->lmu, n)); TRY(dalloc(&c->lmv, n));
+  TRY(dalloc(&c->ubs, n)); TRY(dalloc(&c->vbs, n)); TRY(dalloc(&c->zbs, n));
+  if (c->cfg.mode == SWM_MODE_NONLINEAR) {
+    for (int q = 0; q < 4; q++) { TRY(dalloc(&c->Dbuf[q], n)); TRY(plain_fill(c, c->Dbuf[q], 1.)); }
+  }
+  if (c->cfg.lateral_mixing && c->cfg.mixing_kind == SWM_MIX_BIHARMONIC) {
+    for (int q = 0; q < 4; q++) TRY(dalloc(&c->bh[q], n));
+    TRY(dalloc(&c->ones, n));
+    TRY(plain_fill(c, c->ones, 1.));
+  }
+  for (int q = 0; q < 3; q++) TRY(plain_fill(c, c->impl[q], 1.));
+  c->n0 = 0;
+  c->g0 = 0;
+  c->stage = 1;
+  SWM_CK(cudaStreamSynchronize(c->stream));
+  return SWM_GPU_OK;
+}
+
+// SWM_timestep_init: basic state, then computeD/RelVort/PotVort/EDens/
+// MassFluxes at itt = 0 (which overwrites the grid depths in linear modes).
+int swm_gpu_timestep_init(swm_gpu_ctx *c, const double *psi_bs) {
+  SWM_REQUIRE(c && c->stage == 1, "swm_gpu_timestep_init: call after swm_gpu_domain");
+  if (c->cfg.mode == SWM_MODE_LIN_MEAN) {
+    SWM_REQUIRE(psi_bs, "swm_gpu_timestep_init: LINEARISED_MEAN_STATE needs psi_bs");
+    host_basic_state(c, psi_bs);
+    TRY(h2d(c, c->ubs, c->hg.ubs.data(), c->n));
+    TRY(h2d(c, c->vbs, c->hg.vbs.data(), c->n));
+    TRY(h2d(c, c->zbs, c->hg.zbs.data(), c->n));
+  }
+  TRY(plain_diagnostics(c, 0));
+  for (int q = 0; q < 4; q++) TRY(d2h(c, c->hg.H[q].data(), c->d_H[q], c->n));
+  c->stage = 2;
+  return SWM_GPU_OK;
+}
+
+int swm_gpu_add_damping(swm_gpu_ctx *c, int term, int type, double value, double sl_length,
+                        double sl_cutoff, int loc, const double *file_data) {
+  SWM_REQUIRE(c && c->stage == 2, "swm_gpu_add_damping: call after swm_gpu_timestep_init");
+  SWM_REQUIRE(term >= 0 && term <= 4, "swm_gpu_add_damping: unknown term");
+  SWM_REQUIRE(type >= 0 && type <= 2, "swm_gpu_add_damping: unknown type");
+  SWM_REQUIRE(type != SWM_DAMP_FILE || file_data, "swm_gpu_add_damping: file type needs data");
+  SWM_REQUIRE(type != SWM_DAMP_SPONGE || sl_length > 0, "swm_gpu_add_damping: sponge length must be > 0");
+  host_damping_add(c, term, type, value, sl_length, sl_cutoff, loc, file_data);
+  return SWM_GPU_OK;
+}
+
+int swm_gpu_finish_damping(swm_gpu_ctx *c) {
+  SWM_REQUIRE(c && c->stage == 2, "swm_gpu_finish_damping: call after swm_gpu_timestep_init");
+  host_damping_finish(c);
+  const HostGrid &g = c->hg;
+  for (int q = 0; q < 3; q++) {
+    TRY(h2d(c, c->impl[q], g.impl[q].data(), c->n));
+    TRY(h2d(c, c->glin[q], g.glin[q].data(), c->n));
+  }
+  for (int q = 0; q < 2; q++) TRY(h2d(c, c->gsq[q], g.gsq[q].data(), c->n));
+  SWM_CK(cudaStreamSynchronize(c->stream));
+  c->stage = 3;
+  return SWM_GPU_OK;
+}
+
+int swm_gpu_add_stream(swm_gpu_ctx *c, int type, int comp, double omega, int is_const, const double *d1,
+                       const double *d2, int *id) {
+  SWM_REQUIRE(c && c->stage == 3, "swm_gpu_add_stream: call after swm_gpu_finish_damping");
+  SWM_REQUIRE(type >= 0 && type <= 4, "swm_gpu_add_stream: unknown forcing type");
+  SWM_REQUIRE(c->streams.size() < 64, "swm_gpu_add_stream: too many streams");
+  Stream s;
+  s.type = type;
+  s.comp = comp;
+  s.omega = omega;
+  // SWM_forcing_initStream :627-638
+  if (type == SWM_FRC_OSC) s.is_const = 0;
+  else if (type == SWM_FRC_WIND && c->cfg.mode == SWM_MODE_NONLINEAR) s.is_const = 0;
+  else s.is_const = is_const ? 1 : 0;
+  TRY(dalloc(&s.d1, c->n));
+  TRY(dalloc(&s.d2, c->n));
+  if (d1) TRY(h2d(c, s.d1, d1, c->n));
+  if (d2) TRY(h2d(c, s.d2, d2, c->n));
+  c->streams.push_back(s);
+  if (id) *id = (int)c->streams.size() - 1;
+  return SWM_GPU_OK;
+}
+
+int swm_gpu_set_stream_data(swm_gpu_ctx *c, int id, const double *d1, const double *d2) {
+  SWM_REQUIRE(c && id >= 0 && id < (int)c->streams.size(), "swm_gpu_set_stream_data: bad stream id");
+  if (d1) TRY(h2d(c, c->streams[id].d1, d1, c->n));
+  if (d2) TRY(h2d(c, c->streams[id].d2, d2, c->n));
+  return SWM_GPU_OK;
+}
+
+int swm_gpu_forcing_init(swm_gpu_ctx *c) {
+  SWM_REQUIRE(c && c->stage == 3, "swm_gpu_forcing_init: call after swm_gpu_finish_damping");
+  TRY(plain_forcing_update(c, 0, 1));
+  TRY(plain_forcing_update(c, 0, 0));
+  c->stage = 4;
+  return SWM_GPU_OK;
+}
+
+static int swm_advance_impl(swm_gpu_ctx *c, int64_t itt);
+
+int swm_gpu_initial_conditions(swm_gpu_ctx *c, const double *eta, const double *u, const double *v) {
+  SWM_REQUIRE(c && c->stage == 4, "swm_gpu_initial_conditions: call after swm_gpu_forcing_init");
+  size_t n = c->n;
+  std::vector<double> buf(n);
+  const HostGrid &g = c->hg;
+  const double *src[3] = {eta, u, v};
+  double **dst[3] = {c->eta, c->u, c->v};
+  const int grids[3] = {GE, GU, GV};
+  for (int f = 0; f < 3; f++) {
+    for (size_t k = 0; k < n; k++) buf[k] = src[f] ? g.ocean[grids[f]][k] * src[f][k] : 0.;
+    TRY(h2d(c, dst[f][1 - c->n0], buf.data(), n));
+    SWM_CK(cudaMemsetAsync(dst[f][c->n0], 0, n * 8, c->stream));
+  }
+  SWM_CK(cudaStreamSynchronize(c->stream));
+  TRY(swm_advance_impl(c, 0));
+  c->stage = 5;
+  return SWM_GPU_OK;
+}
+
+static int swm_step_impl(swm_gpu_ctx *c, int64_t itt) {
+  if (c->cfg.path == SWM_PATH_PLAIN_FP64) TRY(plain_step(c, itt));
+  else TRY(fused_step(c, itt));
+  if (!c->tracers.empty()) TRY(tracer_step(c, itt));
+  return SWM_GPU_OK;
+}
+
+// SWM_advance: level swap, increment ring rotation, diagnostics, forcing
+// (fused paths keep their diagnostics and wind forcing inside the step
+// kernel; the FP64 diagnostic arrays are refreshed on demand, or every step
+// when tracers read them)
+static int swm_advance_impl(swm_gpu_ctx *c, int64_t itt) {
+  c->n0 = 1 - c->n0;
+  c->g0 = (c->g0 + 1) % 3;
+  bool plain = c->cfg.path == SWM_PATH_PLAIN_FP64 || itt == 0;
+  if (!plain && !c->tracers.empty()) TRY(fused_sync_state(c));
+  if (plain || !c->tracers.empty()) {
+    TRY(plain_diagnostics(c, itt));
+    TRY(plain_forcing_update(c, itt, 0));
+  }
+  if (!c->tracers.empty() && itt > 0) TRY(tracer_advance(c));
+  return SWM_GPU_OK;
+}
+
+int swm_gpu_step(swm_gpu_ctx *c, int64_t itt) {
+  SWM_REQUIRE(c && c->stage >= 5, "swm_gpu_step: model not initialised");
+  SWM_REQUIRE(itt >= 1, "swm_gpu_step: itt starts at 1");
+  return swm_step_impl(c, itt);
+}
+
+int swm_gpu_advance(swm_gpu_ctx *c, int64_t itt) {
+  SWM_REQUIRE(c && c->stage >= 5, "swm_gpu_advance: model not initialised");
+  return swm_advance_impl(c, itt);
+}
+
+int swm_gpu_run(swm_gpu_ctx *c, int64_t itt0, int64_t nsteps) {
+  SWM_REQUIRE(c && c->stage >= 5, "swm_gpu_run: model not initialised");
+  for (int64_t s = 1; s <= nsteps; s++) {
+    TRY(swm_step_impl(c, itt0 + s));
+    TRY(swm_advance_impl(c, itt0 + s));
+  }
+  SWM_CK(cudaGetLastError());
+  return SWM_GPU_OK;
+}
+
+static const double *field_ptr(swm_gpu_ctx *c, int f, double **wptr) {
+  Dev d = c->dev();
+  double *p = nullptr;
+  switch (f) {
+    case SWM_F_U: p = d.u0; break;
+    case SWM_F_V: p = d.v0; break;
+    case SWM_F_ETA: p = d.eta0; break;
+    case SWM_F_D: p = d.D; break;
+    case SWM_F_DH: p = d.Dh; break;
+    case SWM_F_DU: p = d.Du; break;
+    case SWM_F_DV: p = d.Dv; break;
+    case SWM_F_EDENS: p = d.edens; break;
+    case SWM_F_POT: p = d.pot; break;
+    case SWM_F_ZETA: p = d.zeta; break;
+    case SWM_F_MU: p = d.mu; break;
+    case SWM_F_MV: p = d.mv; break;
+    case SWM_F_H: p = c->d_H[GH]; break;
+    case SWM_F_HU: p = c->d_H[GU]; break;
+    case SWM_F_HV: p = c->d_H[GV]; break;
+    case SWM_F_HETA: p = c->d_H[GE]; break;
+    case SWM_F_IMPL_U: p = c->impl[0]; break;
+    case SWM_F_IMPL_V: p = c->impl[1]; break;
+    case SWM_F_IMPL_ETA: p = c->impl[2]; break;
+    case SWM_F_GAMMA_LIN_U: p = c->glin[0]; break;
+    case SWM_F_GAMMA_LIN_V: p = c->glin[1]; break;
+    case SWM_F_GAMMA_LIN_ETA: p = c->glin[2]; break;
+    case SWM_F_GAMMA_SQ_U: p = c->gsq[0]; break;
+    case SWM_F_GAMMA_SQ_V: p = c->gsq[1]; break;
+    case SWM_F_FX: p = d.Fx; break;
+    case SWM_F_FY: p = d.Fy; break;
+    case SWM_F_FETA: p = d.Fe; break;
+    case SWM_F_U_BS: p = d.ubs; break;
+    case SWM_F_V_BS: p = d.vbs; break;
+    case SWM_F_ZETA_BS: p = d.zbs; break;
+    case SWM_F_LATMIX_U: p = d.lmu; break;
+    case SWM_F_LATMIX_V: p = d.lmv; break;
+    case SWM_F_GU: p = c->Gu[(c->g0 + 1) % 3]; break;  // newest increment after advance = slot 2
+    case SWM_F_GV: p = c->Gv[(c->g0 + 1) % 3]; break;
+    case SWM_F_GETA: p = c->Ge[(c->g0 + 1) % 3]; break;
+    default: p = nullptr;
+  }
+  if (wptr) *wptr = p;
+  return p;
+}
+
+int swm_gpu_get_field(swm_gpu_ctx *c, int f, double *out) {
+  SWM_REQUIRE(c && c->stage >= 1 && out, "swm_gpu_get_field: bad arguments");
+  if (c->cfg.path != SWM_PATH_PLAIN_FP64 && c->stage >= 5 && c->fused) {
+    TRY(fused_sync_state(c));
+    if (f >= SWM_F_D && f <= SWM_F_MV) TRY(plain_diagnostics(c, 1));
+    if (f >= SWM_F_FX && f <= SWM_F_FETA) TRY(plain_forcing_update(c, 1, 0));
+  }
+  const double *p = field_ptr(c, f, nullptr);
+  SWM_REQUIRE(p, "swm_gpu_get_field: unknown field or not allocated");
+  return d2h(c, out, p, c->n);
+}
+
+int swm_gpu_set_field(swm_gpu_ctx *c, int f, const double *in) {
+  SWM_REQUIRE(c && c->stage >= 1 && in, "swm_gpu_set_field: bad arguments");
+  double *p = nullptr;
+  field_ptr(c, f, &p);
+  SWM_REQUIRE(p, "swm_gpu_set_field: unknown field or not allocated");
+  TRY(h2d(c, p, in, c->n));
+  SWM_CK(cudaStreamSynchronize(c->stream));
+  if (c->cfg.path != SWM_PATH_PLAIN_FP64 && c->stage >= 5 && f <= SWM_F_ETA) TRY(fused_load_state(c));
+  return SWM_GPU_OK;
+}
+
+int swm_gpu_get_metric(swm_gpu_ctx *c, int which, int grid, double *out) {
+  SWM_REQUIRE(c && c->stage >= 1 && out && which >= 0 && which <= 3 && grid >= 0 && grid <= 3,
+              "swm_gpu_get_metric: bad arguments");
+  const HostGrid &g = c->hg;
+  const std::vector<double> *src[4] = {&g.lat[grid], &g.cosl[grid], &g.tanl[grid], &g.f[grid]};
+  memcpy(out, src[which]->data(), sizeof(double) * c->ny);
+  return SWM_GPU_OK;
+}
+
+int swm_gpu_get_mask(swm_gpu_ctx *c, int grid, int8_t *out) {
+  SWM_REQUIRE(c && c->stage >= 1 && out && grid >= 0 && grid <= 3, "swm_gpu_get_mask: bad arguments");
+  memcpy(out, c->hg.ocean[grid].data(), c->n);
+  return SWM_GPU_OK;
+}
+
+int swm_gpu_streamfunction(swm_gpu_ctx *c, double *psi) {
+  SWM_REQUIRE(c && c->stage >= 5 && psi, "swm_gpu_streamfunction: bad arguments");
+  std::vector<double> u(c->n), v(c->n), hu(c->n), hv(c->n);
+  TRY(swm_gpu_get_field(c, SWM_F_U, u.data()));
+  TRY(swm_gpu_get_field(c, SWM_F_V, v.data()));
+  TRY(d2h(c, hu.data(), c->d_H[GU], c->n));
+  TRY(d2h(c, hv.data(), c->d_H[GV], c->n));
+  host_streamfunction(c, u.data(), v.data(), hu.data(), hv.data(), psi);
+  return SWM_GPU_OK;
+}
+
+}  // extern "C"

@@ -1,0 +1,154 @@
+// ctx.h -- internal state of one SWM model instance on the GPU.
+//
+// Device layout: every 2-D field is an unpadded Fortran-order (Nx, Ny) array
+// (row j holds i = 0..Nx-1 contiguously), so host <-> device copies need no
+// transpose.  Time levels and the Adams-Bashforth increment history are
+// rotated by index, never copied (the reference copies N0p1 -> N0 and shifts
+// G(:,:,1:2) = G(:,:,2:3) every step: swm_module.f90:91-113,
+// swm_nonlinear_timestep_module.f90:134-148).
+#pragma once
+#include <cuda_runtime.h>
+#include <stdint.h>
+#include <string>
+#include <vector>
+#include "../../include/swm_gpu.h"
+
+namespace swm {
+
+enum { GH = 0, GU = 1, GV = 2, GE = 3 };  // grid ids: H (corner), u, v, eta
+
+void set_error(const std::string &msg);
+
+#define SWM_CK(call)                                                              \
+  do {                                                                            \
+    cudaError_t e_ = (call);                                                      \
+    if (e_ != cudaSuccess) {                                                      \
+      ::swm::set_error(std::string(#call) + ": " + cudaGetErrorString(e_));        \
+      return SWM_GPU_ECUDA;                                                       \
+    }                                                                             \
+  } while (0)
+
+#define SWM_REQUIRE(cond, msg)                                                    \
+  do {                                                                            \
+    if (!(cond)) {                                                                \
+      ::swm::set_error(msg);                                                      \
+      return SWM_GPU_EINVAL;                                                      \
+    }                                                                             \
+  } while (0)
+
+// Host copy of the grid as domain_module/grid_module build it.
+struct HostGrid {
+  int nx = 0, ny = 0;
+  double dLambda = 0, dTheta = 0, D2R = 0;
+  std::vector<double> lat[4], lon[4], cosl[4], tanl[4], sinl[4], f[4];
+  std::vector<int8_t> ocean[4];
+  std::vector<double> H[4];     // H, H_u, H_v, H_eta (grid%H)
+  std::vector<double> glin[3];  // gamma_lin_u, _v, _eta
+  std::vector<double> gsq[2];   // gamma_sq_u, _v
+  std::vector<double> impl[3];
+  std::vector<double> ubs, vbs, zbs;
+};
+
+struct Stream {
+  int type, comp, is_const;
+  double omega;
+  double *d1 = nullptr, *d2 = nullptr;  // device records
+};
+
+struct Tracer {
+  double kappa_h;
+  double *CH[2] = {nullptr, nullptr};   // TRC_N0, TRC_N0p1 (rotated)
+  double *G[3] = {nullptr, nullptr, nullptr};
+  double *C = nullptr, *C0 = nullptr, *gamma = nullptr, *impl = nullptr;
+  double *uhc = nullptr, *vhc = nullptr, *diff = nullptr;
+  int n0 = 0, g0 = 0;
+};
+
+// Plain-old-data view of the device state handed to kernels by value.
+struct Dev {
+  int nx, ny, mode, qbf, barotropic, lateral_mixing, itt_is_zero;
+  double dt, G, A, dLambda, dTheta, minD, tau_scale, RHO0, lbc;
+  const int8_t *ocean[4];
+  const double *cosl[4], *tanl[4], *f[4];
+  double *Hg[4];  // H, H_u, H_v, H_eta on the device (H/H_u/H_v overwritten at itt=0 in linear modes)
+  // state, N0 and N0p1
+  double *u0, *v0, *eta0, *u1, *v1, *eta1;
+  // increments: slot 1 (oldest) .. slot 3 (newest)
+  double *Gu[3], *Gv[3], *Ge[3];
+  double *D, *Dh, *Du, *Dv;
+  double *edens, *pot, *zeta, *mu, *mv;
+  double *pll, *plt, *lmu, *lmv;
+  double *impl_u, *impl_v, *impl_e, *gsq_u, *gsq_v;
+  double *Fx, *Fy, *Fe, *Fxc, *Fyc, *Fec;
+  double *ubs, *vbs, *zbs;
+};
+
+}  // namespace swm
+
+struct FusedState;
+struct SorState;
+
+struct swm_gpu_ctx {
+  swm_gpu_config cfg;
+  int nx = 0, ny = 0;
+  size_t n = 0;
+  cudaStream_t stream = nullptr;
+  int64_t launches = 0;
+  swm::HostGrid hg;
+  int stage = 0;  // 1 domain, 2 timestep_init, 3 damping, 4 forcing, 5 ic
+  // device buffers
+  int8_t *d_ocean[4] = {};
+  double *d_cos[4] = {}, *d_tan[4] = {}, *d_f[4] = {}, *d_lat[4] = {};
+  double *d_H[4] = {};
+  double *u[2] = {}, *v[2] = {}, *eta[2] = {};
+  int n0 = 0;  // index of the N0 time level
+  double *Gu[3] = {}, *Gv[3] = {}, *Ge[3] = {};
+  int g0 = 0;  // ring offset: increment slot k (1..3) lives in buffer (g0 + k - 1) % 3
+  double *Dbuf[4] = {};  // own D arrays (FULLY_NONLINEAR)
+  double *edens = nullptr, *pot = nullptr, *zeta = nullptr, *mu = nullptr, *mv = nullptr;
+  double *pll = nullptr, *plt = nullptr, *lmu = nullptr, *lmv = nullptr;
+  double *bh[4] = {};    // biharmonic scratch (first-pass pll, plt, lu, lv)
+  double *ones = nullptr;
+  double *impl[3] = {}, *gsq[2] = {}, *glin[3] = {};
+  double *F[3] = {}, *Fc[3] = {};
+  double *ubs = nullptr, *vbs = nullptr, *zbs = nullptr;
+  std::vector<swm::Stream> streams;
+  std::vector<swm::Tracer> tracers;
+  double *trc_coeff = nullptr;
+  FusedState *fused = nullptr;
+  SorState *sor = nullptr;
+  cudaGraphExec_t graph = nullptr;
+  int64_t graph_steps = 0;
+  int graph_n0 = -1, graph_g0 = -1;
+  swm::Dev dev() const;
+};
+
+namespace swm {
+// setup.cu
+int host_domain(swm_gpu_ctx *c, const double *H, const int8_t *H_missing);
+void host_basic_state(swm_gpu_ctx *c, const double *psi);
+void host_damping_add(swm_gpu_ctx *c, int term, int type, double value, double sl_length,
+                      double sl_cutoff, int loc, const double *file_data);
+void host_damping_finish(swm_gpu_ctx *c);
+void host_streamfunction(const swm_gpu_ctx *c, const double *u, const double *v, const double *Hu,
+                         const double *Hv, double *psi);
+// plain.cu
+int plain_diagnostics(swm_gpu_ctx *c, int64_t itt);
+int plain_step(swm_gpu_ctx *c, int64_t itt);
+int plain_forcing_update(swm_gpu_ctx *c, int64_t itt, int constant_part);
+int plain_fill(swm_gpu_ctx *c, double *p, double value);
+// tracer.cu
+int tracer_init_coeffs(swm_gpu_ctx *c);
+int tracer_step(swm_gpu_ctx *c, int64_t itt);
+int tracer_advance(swm_gpu_ctx *c);
+// fused.cu
+int fused_prepare(swm_gpu_ctx *c);
+int fused_step(swm_gpu_ctx *c, int64_t itt);
+int fused_sync_state(swm_gpu_ctx *c);    // FP32 pair state -> FP64 buffers
+int fused_load_state(swm_gpu_ctx *c);    // FP64 buffers -> FP32 pair state
+void fused_free(swm_gpu_ctx *c);
+// sor.cu
+void sor_free(swm_gpu_ctx *c);
+}  // namespace swm
+
+#define SWM_LAUNCH_COUNT(c) ((c)->launches++)

@@ -1,0 +1,795 @@
+// fused.cu -- one-kernel-per-step SWM update (FULLY_NONLINEAR,
+// LINEARISED_STATE_OF_REST and no-linearisation modes).
+//
+// A CTA owns a TX x TY tile of cells.  It stages u, v, eta, the land/ocean
+// mask code and the depth for the tile plus an H-cell halo (H = 1 for the
+// reference's Laplacian-type stress, 2 for the biharmonic extension) in
+// shared memory, rebuilds every per-step diagnostic the reference keeps in
+// global arrays (D, Du/Dv/Dh, mass fluxes, vorticity, PV, Bernoulli,
+// P_lambda-lambda / P_lambda-theta) inside the tile, and writes only the new
+// state and the newest Adams-Bashforth increment.  Per cell and step the
+// kernel therefore moves the state in and out once, reads the two older
+// increments and writes the newest one -- the algorithmic minimum.
+//
+// T = double: FP64 fused path.  T = float with COMP: the state is a pair of
+// binary32 words (hi + lo, ~48 significant bits); tendencies are evaluated in
+// binary32 from hi and the Adams-Bashforth increment is added with TwoSum and
+// a compensated division by the implicit damping factor, so rounding errors
+// do not accumulate in the state over long integrations.
+//
+// Arithmetic follows the reference formulas (swm_nonlinear_timestep_module.f90
+// :182-449, swm_lateralmixing_module.f90:66-240, time_integration_module.f90
+// :74-112) with divisions by grid metrics replaced by per-row reciprocals, so
+// results agree with the FP64 restatement to rounding, not bit for bit.
+#include <cmath>
+#include <cstring>
+#include <vector>
+#include "ctx.h"
+
+namespace swm {
+
+enum {
+  R_CE, R_CV, R_CU, R_FH, R_RE_DL, R_RE_DT, R_RU_DL, R_RV_DL, R_RH_DL, R_INV_CH,
+  R_PC0, R_HC0, R_TE, R_TH, R_TU, R_TV, R_NR
+};
+
+template <typename T>
+struct FP {
+  int nx, ny, mode, mix, qbf, barotropic, has_F, impl_uniform, gsq_uniform, wind_x, wind_y, wind_rows, tstep;
+  T dt, G, minD, lbc, q1, ts_rho, Ah, bih, eps;
+  T ab0, ab1, ab2;
+  T impl_s[3], gsq_s[2];
+  const uint8_t *mc;
+  const T *He, *rows, *Hu, *Hv;
+  const T *impl[3], *gsq[2];
+  const T *Fx, *Fy, *Fe;
+  const T *wx, *wy;
+  const T *u0, *v0, *e0;
+  T *u1, *v1, *e1;
+  const float *ul0, *vl0, *el0;
+  float *ul1, *vl1, *el1;
+  const T *Gu1, *Gu2, *Gv1, *Gv2, *Ge1, *Ge2;
+  T *Gu3, *Gv3, *Ge3;
+};
+
+constexpr int TX = 32, TY = 8, NT = TX * TY;
+
+__device__ __forceinline__ int wrapi(int g, int n) {
+  if (g < 0) g += n;
+  if (g >= n) g -= n;
+  if (g >= n) g -= n;
+  return g;
+}
+
+template <typename T>
+__device__ __forceinline__ T recip_cnt(int c) {
+  // 1 / max(c, 1) for the mask-normalised interpolation weights
+  return c <= 1 ? T(1) : (c == 2 ? T(0.5) : (c == 3 ? T(1) / T(3) : T(0.25)));
+}
+
+// compensated a + b (a = hi + lo pair, b float) followed by division by d
+__device__ __forceinline__ void comp_update(float hi, float lo, float inc, float d, float &nh, float &nl) {
+  float s = hi + inc;
+  float bb = s - hi;
+  float e = (hi - (s - bb)) + (inc - bb);
+  e = e + lo;
+  float q = s / d;
+  float r = fmaf(-q, d, s);
+  float ql = (r + e) / d;
+  nh = q + ql;
+  nl = ql - (nh - q);
+}
+
+template <typename T, int HALO, bool COMP>
+__global__ void __launch_bounds__(NT) k_fused(FP<T> p) {
+  constexpr int W = TX + 2 * HALO, HH = TY + 2 * HALO, NS = W * HH;
+  __shared__ T sU[NS], sV[NS], sE[NS], sD[NS], sMU[NS], sMV[NS], sPOT[NS], sB[NS], sPLL[NS], sPLT[NS];
+  __shared__ T sLU[HALO == 2 ? NS : 1], sLV[HALO == 2 ? NS : 1];
+  __shared__ uint8_t sM[NS];
+  const int tid = threadIdx.x;
+  const int i0 = blockIdx.x * TX, j0 = blockIdx.y * TY;
+  const int nx = p.nx, ny = p.ny;
+  const bool nl = p.mode == SWM_MODE_NONLINEAR;
+  auto S = [](int i, int j) { return (j + HALO) * W + (i + HALO); };
+  auto row = [&](int j) { return p.rows + (size_t)wrapi(j0 + j, ny) * R_NR; };
+
+  // ---- phase A: stage state, mask and thickness ----------------------
+  for (int q = tid; q < NS; q += NT) {
+    int ti = q % W - HALO, tj = q / W - HALO;
+    int gi = wrapi(i0 + ti, nx), gj = wrapi(j0 + tj, ny);
+    size_t k = (size_t)gi + (size_t)nx * gj;
+    uint8_t m = p.mc[k];
+    T e = p.e0[k], he = p.He[k];
+    sM[q] = m;
+    sU[q] = p.u0[k];
+    sV[q] = p.v0[k];
+    sE[q] = e;
+    // computeD: D = eta + H on ocean eta (FULLY_NONLINEAR, land keeps 1),
+    // else the eta-grid depth
+    sD[q] = nl ? ((m & 8) ? e + he : T(1)) : he;
+  }
+  __syncthreads();
+
+  auto oH = [&](int q) { return sM[q] & 1; };
+  auto oU = [&](int q) { return (sM[q] >> 1) & 1; };
+  auto oV = [&](int q) { return (sM[q] >> 2) & 1; };
+  auto oE = [&](int q) { return (sM[q] >> 3) & 1; };
+  auto Du_at = [&](int q) {  // eta2u_noland of D
+    int a = oE(q), b = oE(q - 1);
+    return (T(a) * sD[q] + T(b) * sD[q - 1]) * recip_cnt<T>(a + b);
+  };
+  auto Dv_at = [&](int q) {
+    int a = oE(q), b = oE(q - W);
+    return (T(a) * sD[q] + T(b) * sD[q - W]) * recip_cnt<T>(a + b);
+  };
+  auto Dh_at = [&](int q) {  // eta2H_noland: (i,j),(i-1,j-1),(i-1,j),(i,j-1)
+    int a = oE(q), b = oE(q - W - 1), c = oE(q - 1), d = oE(q - W);
+    return (T(a) * sD[q] + T(b) * sD[q - W - 1] + T(c) * sD[q - 1] + T(d) * sD[q - W]) * recip_cnt<T>(a + b + c + d);
+  };
+  auto inner = [&](int ti, int tj, int lo, int hi_) {
+    return ti >= -HALO + lo && ti < TX + HALO - hi_ && tj >= -HALO + lo && tj < TY + HALO - hi_;
+  };
+
+  // P tensor of the Laplacian-type stress at eta (pll) and H (plt) points for
+  // the velocity pair (a, b) = (u-like, v-like), weights on (weighted) or 1
+  auto p_tensor = [&](const T *a, const T *b, T Ah, bool weighted, T *outL, T *outT) {
+    for (int q = tid; q < NS; q += NT) {
+      int ti = q % W - HALO, tj = q / W - HALO;
+      T pl = T(0), pt = T(0);
+      if (ti < TX + HALO - 1 && tj < TY + HALO - 1 && oE(q)) {  // needs (i+1, j), (i, j+1)
+        const T *r = row(tj);
+        int ov = oV(q), ovp = oV(q + W);
+        T tE = r[R_TE] / T(max(ov + ovp, 1));
+        T c0 = Ah * r[R_PC0];
+        T c1 = Ah * (p.q1 + T(ovp) * tE);
+        T c2 = Ah * (-p.q1 + T(ov) * tE);
+        pl = (weighted ? sD[q] : T(1)) * (c0 * (a[q + 1] - a[q]) + c1 * b[q + W] + c2 * b[q]);
+      }
+      if (ti > -HALO && tj > -HALO && oH(q)) {  // needs (i-1, j), (i, j-1)
+        const T *r = row(tj);
+        int ou = oU(q), oum = oU(q - W);
+        T tH = r[R_TH] / T(max(ou + oum, 1));
+        T c0 = Ah * r[R_HC0];
+        T c1 = -Ah * (p.q1 + T(ou) * tH);
+        T c2 = -Ah * (-p.q1 + T(oum) * tH);
+        pt = (weighted ? Dh_at(q) : T(1)) * (c0 * (b[q] - b[q - 1]) + c1 * a[q] + c2 * a[q - W]);
+      }
+      outL[q] = pl;
+      outT[q] = pt;
+    }
+  };
+  // divergence of P onto u and v points (compute_uv); unit thickness or D
+  auto lat_u = [&](int q, int tj, bool weighted) {
+    const T *r = row(tj);
+    int o = oH(q) + oH(q + W);
+    T t2 = T(2) * r[R_TU] / T(max(o, 1));
+    T m0 = -r[R_RU_DL], m1 = -(p.q1 - t2), m2 = p.q1 + t2;
+    T s = m0 * (sPLL[q] - sPLL[q - 1]) + m1 * sPLT[q + W] + m2 * sPLT[q];
+    return weighted ? s / Du_at(q) : s;
+  };
+  auto lat_v = [&](int q, int tj, bool weighted) {
+    const T *r = row(tj);
+    int o = oE(q) + oE(q - W);
+    T t2 = T(2) * r[R_TV] / T(max(o, 1));
+    T m0 = -r[R_RV_DL], m1 = p.q1 - t2, m2 = -(p.q1 + t2);
+    T s = m0 * (sPLT[q + 1] - sPLT[q]) + m1 * sPLL[q] + m2 * sPLL[q - W];
+    return weighted ? s / Dv_at(q) : s;
+  };
+
+  if (p.mix == 2) {
+    // biharmonic extension: first pass with unit thickness and Ah = 1
+    p_tensor(sU, sV, T(1), false, sPLL, sPLT);
+    __syncthreads();
+    for (int q = tid; q < NS; q += NT) {
+      int ti = q % W - HALO, tj = q / W - HALO;
+      bool ok = inner(ti, tj, 1, 1);
+      sLU[q] = (ok && oU(q)) ? lat_u(q, tj, false) : T(0);
+      sLV[q] = (ok && oV(q)) ? lat_v(q, tj, false) : T(0);
+    }
+    __syncthreads();
+  }
+
+  // ---- phase B: mass fluxes, PV, Bernoulli, P tensor -------------------
+  for (int q = tid; q < NS; q += NT) {
+    int ti = q % W - HALO, tj = q / W - HALO;
+    bool lo_ok = ti > -HALO && tj > -HALO;
+    bool hi_ok = ti < TX + HALO - 1 && tj < TY + HALO - 1;
+    sMU[q] = (ti > -HALO && oU(q)) ? Du_at(q) * sU[q] : T(0);
+    sMV[q] = (tj > -HALO && oV(q)) ? Dv_at(q) * sV[q] : T(0);
+    T pot = T(0);
+    if (lo_ok && p.mode != SWM_MODE_NONE) {
+      const T *r = row(tj);
+      T zeta = T(0);
+      if (nl) {
+        T bc = oH(q) ? T(1) : p.lbc;
+        T dvdx = (oV(q - 1) + oV(q) == 0) ? T(0) : bc * r[R_RH_DL] * (sV[q] - sV[q - 1]);
+        T dudy = (oU(q) + oU(q - W) == 0) ? T(0) : bc * p.q1 * (r[R_CU] * sU[q] - row(tj - 1)[R_CU] * sU[q - W]);
+        zeta = dvdx - dudy * r[R_INV_CH];
+      }
+      T pD = Dh_at(q);
+      pD = pD > p.eps ? pD : p.eps;
+      pot = (r[R_FH] + zeta) / pD;
+    }
+    sPOT[q] = pot;
+    T b = T(0);
+    if (hi_ok && oE(q) && p.mode != SWM_MODE_NONE) {
+      b = p.G * sE[q];
+      if (nl) {
+        T a = T(0.5) * (sU[q + 1] * sU[q + 1]) + T(0.5) * (sU[q] * sU[q]);
+        T c = T(0.5) * (sV[q + W] * sV[q + W]) + T(0.5) * (sV[q] * sV[q]);
+        b = (a + c) * T(0.5) + b;
+      }
+    }
+    sB[q] = b;
+  }
+  if (p.mix == 1) p_tensor(sU, sV, p.Ah, true, sPLL, sPLT);
+  if (p.mix == 2) {
+    __syncthreads();  // lat_u/lat_v of the first pass read sPLL/sPLT
+    p_tensor(sLU, sLV, -p.bih, true, sPLL, sPLT);
+  }
+  __syncthreads();
+
+  // ---- phase C: tendencies and Adams-Bashforth update (interior) ------
+  for (int q0 = tid; q0 < TX * TY; q0 += NT) {
+    int ti = q0 % TX, tj = q0 / TX;
+    int gi = i0 + ti, gj = j0 + tj;
+    if (gi >= nx || gj >= ny) continue;
+    size_t k = (size_t)gi + (size_t)nx * gj;
+    int q = S(ti, tj);
+    const T *r = row(tj);
+    T ge = T(0), gu = T(0), gv = T(0);
+    if (oE(q)) {
+      T cvp = row(tj + 1)[R_CV], cv = r[R_CV];
+      ge = -(sMU[q + 1] - sMU[q]) * r[R_RE_DL] - (sMV[q + W] * cvp - sMV[q] * cv) * r[R_RE_DT];
+      if (p.has_F) ge = ge + p.Fe[k];
+    }
+    if (oU(q)) {
+      T pv = T(0.5) * sPOT[q + W] + T(0.5) * sPOT[q];
+      T mv = T(0.25) * sMV[q + W] + T(0.25) * sMV[q - 1] + T(0.25) * sMV[q - 1 + W] + T(0.25) * sMV[q];
+      T g = pv * mv - (sB[q] - sB[q - 1]) * r[R_RU_DL];
+      if (p.qbf) {
+        T vb = T(0.25) * sV[q + W] + T(0.25) * sV[q - 1] + T(0.25) * sV[q - 1 + W] + T(0.25) * sV[q];
+        T gs = p.gsq_uniform ? p.gsq_s[0] : p.gsq[0][k];
+        T f = gs * sqrt(sU[q] * sU[q] + vb * vb) * sU[q];
+        if (p.barotropic) f = f / p.Hu[k];
+        g = g - f;
+      }
+      if (p.mix) g = g + lat_u(q, tj, true);
+      if (p.has_F) g = g + p.Fx[k];
+      if (p.wind_x) g = g + p.ts_rho * (p.wind_rows ? p.wx[gj] : p.wx[k]) / (nl ? Du_at(q) : T(1));
+      gu = g;
+    }
+    if (oV(q)) {
+      T pv = T(0.5) * sPOT[q + 1] + T(0.5) * sPOT[q];
+      T mu = T(0.25) * sMU[q + 1] + T(0.25) * sMU[q - W] + T(0.25) * sMU[q] + T(0.25) * sMU[q + 1 - W];
+      T g = -pv * mu - (sB[q] - sB[q - W]) * p.q1;
+      if (p.qbf) {
+        T ub = T(0.25) * sU[q + 1] + T(0.25) * sU[q - W] + T(0.25) * sU[q] + T(0.25) * sU[q + 1 - W];
+        T gs = p.gsq_uniform ? p.gsq_s[1] : p.gsq[1][k];
+        T f = gs * sqrt(sV[q] * sV[q] + ub * ub) * sV[q];
+        if (p.barotropic) f = f / p.Hv[k];
+        g = g - f;
+      }
+      if (p.mix) g = g + lat_v(q, tj, true);
+      if (p.has_F) g = g + p.Fy[k];
+      if (p.wind_y) g = g + p.ts_rho * (p.wind_rows ? p.wy[gj] : p.wy[k]) / (nl ? Dv_at(q) : T(1));
+      gv = g;
+    }
+    p.Ge3[k] = ge;
+    p.Gu3[k] = gu;
+    p.Gv3[k] = gv;
+    T ie = p.impl_uniform ? p.impl_s[2] : p.impl[2][k];
+    T iu = p.impl_uniform ? p.impl_s[0] : p.impl[0][k];
+    T iv = p.impl_uniform ? p.impl_s[1] : p.impl[1][k];
+    T ince = p.dt * (p.ab0 * p.Ge1[k] + p.ab1 * p.Ge2[k] + p.ab2 * ge);
+    T incu = p.dt * (p.ab0 * p.Gu1[k] + p.ab1 * p.Gu2[k] + p.ab2 * gu);
+    T incv = p.dt * (p.ab0 * p.Gv1[k] + p.ab1 * p.Gv2[k] + p.ab2 * gv);
+    T lim = p.minD - p.He[k];
+    if constexpr (COMP) {
+      float nh, nlo;
+      comp_update(sE[q], p.el0[k], ince, ie, nh, nlo);
+      if (nl && nh < lim) { nh = lim; nlo = 0.f; }
+      p.e1[k] = nh; p.el1[k] = nlo;
+      comp_update(sU[q], p.ul0[k], incu, iu, nh, nlo);
+      p.u1[k] = nh; p.ul1[k] = nlo;
+      comp_update(sV[q], p.vl0[k], incv, iv, nh, nlo);
+      p.v1[k] = nh; p.vl1[k] = nlo;
+    } else {
+      T e = (sE[q] + ince) / ie;
+      if (nl && e < lim) e = lim;
+      p.e1[k] = e;
+      p.u1[k] = (sU[q] + incu) / iu;
+      p.v1[k] = (sV[q] + incv) / iv;
+    }
+  }
+}
+
+// FP64 <-> FP32 hi/lo conversions
+__global__ void k_split(const double *src, float *hi, float *lo, size_t n) {
+  size_t k = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (k >= n) return;
+  double x = src[k];
+  float h = (float)x;
+  hi[k] = h;
+  lo[k] = (float)(x - (double)h);
+}
+__global__ void k_join(const float *hi, const float *lo, double *dst, size_t n) {
+  size_t k = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (k >= n) return;
+  dst[k] = (double)hi[k] + (lo ? (double)lo[k] : 0.);
+}
+__global__ void k_to_f32(const double *src, float *dst, size_t n) {
+  size_t k = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (k < n) dst[k] = (float)src[k];
+}
+
+}  // namespace swm
+
+using namespace swm;
+
+struct FusedState {
+  bool ready = false;
+  bool comp = false;
+  // FP32 pair state and increments (FP32C path)
+  float *uh[2] = {}, *ul[2] = {}, *vh[2] = {}, *vl[2] = {}, *eh[2] = {}, *el[2] = {};
+  float *Gu[3] = {}, *Gv[3] = {}, *Ge[3] = {};
+  // static inputs
+  uint8_t *mc = nullptr;
+  void *He = nullptr, *rows = nullptr, *Hu = nullptr, *Hv = nullptr;
+  void *impl[3] = {}, *gsq[2] = {}, *F[3] = {}, *wx = nullptr, *wy = nullptr;
+  bool impl_uniform = true, gsq_uniform = true, has_F = false, wind_rows = false;
+  int wind_x = 0, wind_y = 0;
+  double impl_s[3] = {1, 1, 1}, gsq_s[2] = {0, 0};
+  int n0 = 0, g0 = 0;  // FP32C level / ring indices
+};
+
+namespace swm {
+
+static int dmalloc(void **p, size_t bytes) {
+  cudaError_t e = cudaMalloc(p, bytes);
+  if (e != cudaSuccess) {
+    set_error(std::string("cudaMalloc: ") + cudaGetErrorString(e));
+    return SWM_GPU_ENOMEM;
+  }
+  return SWM_GPU_OK;
+}
+
+#define FTRY(x)                          \
+  do {                                   \
+    int rc_ = (x);                       \
+    if (rc_ != SWM_GPU_OK) return rc_;   \
+  } while (0)
+
+// device copy of a host FP64 array in the path's precision
+static int upload_t(swm_gpu_ctx *c, bool f32, const double *host, size_t count, void **dst) {
+  size_t es = f32 ? 4 : 8;
+  FTRY(dmalloc(dst, count * es));
+  if (f32) {
+    std::vector<float> t(count);
+    for (size_t q = 0; q < count; q++) t[q] = (float)host[q];
+    SWM_CK(cudaMemcpy(*dst, t.data(), count * 4, cudaMemcpyHostToDevice));
+  } else {
+    SWM_CK(cudaMemcpy(*dst, host, count * 8, cudaMemcpyHostToDevice));
+  }
+  return SWM_GPU_OK;
+}
+
+static bool uniform(const std::vector<double> &v, double *val) {
+  for (size_t q = 1; q < v.size(); q++)
+    if (v[q] != v[0]) return false;
+  *val = v.empty() ? 0. : v[0];
+  return true;
+}
+
+static void download(swm_gpu_ctx *c, const double *dev, std::vector<double> &out) {
+  out.resize(c->n);
+  cudaMemcpy(out.data(), dev, c->n * 8, cudaMemcpyDeviceToHost);
+}
+
+// Builds the static inputs of the fused kernel once the model is initialised.
+int fused_prepare(swm_gpu_ctx *c) {
+  FusedState *f = c->fused;
+  if (f && f->ready) return SWM_GPU_OK;
+  const swm_gpu_config &cf = c->cfg;
+  SWM_REQUIRE(cf.mode != SWM_MODE_LIN_MEAN, "fused paths: LINEARISED_MEAN_STATE runs on the plain path");
+  if (!f) f = c->fused = new FusedState();
+  bool f32 = cf.path == SWM_PATH_FUSED_FP32C;
+  f->comp = f32;
+  size_t n = c->n;
+  int ny = c->ny;
+  const HostGrid &g = c->hg;
+  // mask code: bit0 H, bit1 u, bit2 v, bit3 eta
+  std::vector<uint8_t> mc(n);
+  for (size_t k = 0; k < n; k++)
+    mc[k] = (uint8_t)(g.ocean[GH][k] | (g.ocean[GU][k] << 1) | (g.ocean[GV][k] << 2) | (g.ocean[GE][k] << 3));
+  FTRY(dmalloc((void **)&f->mc, n));
+  SWM_CK(cudaMemcpy(f->mc, mc.data(), n, cudaMemcpyHostToDevice));
+  // per-row metric factors, from the FP64 grid
+  std::vector<double> rows((size_t)ny * R_NR);
+  double A = cf.A, dL = g.dLambda, dT = g.dTheta;
+  for (int j = 0; j < ny; j++) {
+    double *r = &rows[(size_t)j * R_NR];
+    double cE = g.cosl[GE][j], cV = g.cosl[GV][j], cU = g.cosl[GU][j], cH = g.cosl[GH][j];
+    r[R_CE] = cE;
+    r[R_CV] = cV;
+    r[R_CU] = cU;
+    r[R_FH] = g.f[GH][j];
+    r[R_RE_DL] = 1. / (A * cE * dL);
+    r[R_RE_DT] = 1. / (A * cE * dT);
+    r[R_RU_DL] = 1. / (A * cU * dL);
+    r[R_RV_DL] = 1. / (A * cV * dL);
+    r[R_RH_DL] = 1. / (A * cH * dL);
+    r[R_INV_CH] = 1. / cH;
+    r[R_PC0] = -1. / (dL * A * cE);
+    r[R_HC0] = -1. / (dL * A * cH);
+    r[R_TE] = g.tanl[GE][j] / A;
+    r[R_TH] = g.tanl[GH][j] / A;
+    r[R_TU] = g.tanl[GU][j] / A;
+    r[R_TV] = g.tanl[GV][j] / A;
+  }
+  FTRY(upload_t(c, f32, rows.data(), rows.size(), &f->rows));
+  // depths (after computeD at itt = 0)
+  std::vector<double> tmp;
+  download(c, c->d_H[GE], tmp);
+  FTRY(upload_t(c, f32, tmp.data(), n, &f->He));
+  download(c, c->d_H[GU], tmp);
+  FTRY(upload_t(c, f32, tmp.data(), n, &f->Hu));
+  download(c, c->d_H[GV], tmp);
+  FTRY(upload_t(c, f32, tmp.data(), n, &f->Hv));
+  // damping
+  f->impl_uniform = true;
+  for (int q = 0; q < 3; q++) f->impl_uniform = f->impl_uniform && uniform(g.impl[q], &f->impl_s[q]);
+  if (!f->impl_uniform)
+    for (int q = 0; q < 3; q++) FTRY(upload_t(c, f32, g.impl[q].data(), n, &f->impl[q]));
+  f->gsq_uniform = uniform(g.gsq[0], &f->gsq_s[0]) && uniform(g.gsq[1], &f->gsq_s[1]);
+  if (!f->gsq_uniform)
+    for (int q = 0; q < 2; q++) FTRY(upload_t(c, f32, g.gsq[q].data(), n, &f->gsq[q]));
+  // forcing: constant part from the forcing arrays, NL wind recomputed in the kernel
+  std::vector<double> Fh[3];
+  f->has_F = false;
+  for (int q = 0; q < 3; q++) {
+    download(c, c->Fc[q], Fh[q]);
+    for (double x : Fh[q]) f->has_F = f->has_F || x != 0.;
+  }
+  for (const Stream &s : c->streams) {
+    if (s.is_const) continue;
+    bool nl_wind = s.type == SWM_FRC_WIND && cf.mode == SWM_MODE_NONLINEAR &&
+                   (s.comp == SWM_CMP_ZONAL || s.comp == SWM_CMP_MERID);
+    SWM_REQUIRE(nl_wind, "fused paths: time-dependent forcing other than FULLY_NONLINEAR wind stress runs on the plain path");
+    std::vector<double> d;
+    download(c, s.d1, d);
+    bool rowwise = true;
+    for (int j = 0; j < ny && rowwise; j++)
+      for (int i = 1; i < c->nx; i++)
+        if (d[i + (size_t)c->nx * j] != d[(size_t)c->nx * j]) { rowwise = false; break; }
+    int &flag = s.comp == SWM_CMP_ZONAL ? f->wind_x : f->wind_y;
+    void *&dst = s.comp == SWM_CMP_ZONAL ? f->wx : f->wy;
+    SWM_REQUIRE(!flag, "fused paths: one wind stress stream per component");
+    flag = 1;
+    if (rowwise) {
+      std::vector<double> prof(ny);
+      for (int j = 0; j < ny; j++) prof[j] = d[(size_t)c->nx * j];
+      FTRY(upload_t(c, f32, prof.data(), ny, &dst));
+    } else {
+      FTRY(upload_t(c, f32, d.data(), n, &dst));
+    }
+    f->wind_rows = rowwise;
+  }
+  if (f->wind_x && f->wind_y) SWM_REQUIRE(f->wind_rows, "fused paths: two wind components must both be row profiles");
+  if (f->has_F)
+    for (int q = 0; q < 3; q++) FTRY(upload_t(c, f32, Fh[q].data(), n, &f->F[q]));
+  if (f32) {
+    for (int q = 0; q < 2; q++) {
+      FTRY(dmalloc((void **)&f->uh[q], n * 4)); FTRY(dmalloc((void **)&f->ul[q], n * 4));
+      FTRY(dmalloc((void **)&f->vh[q], n * 4)); FTRY(dmalloc((void **)&f->vl[q], n * 4));
+      FTRY(dmalloc((void **)&f->eh[q], n * 4)); FTRY(dmalloc((void **)&f->el[q], n * 4));
+    }
+    for (int q = 0; q < 3; q++) {
+      FTRY(dmalloc((void **)&f->Gu[q], n * 4)); FTRY(dmalloc((void **)&f->Gv[q], n * 4));
+      FTRY(dmalloc((void **)&f->Ge[q], n * 4));
+    }
+  }
+  f->ready = true;
+  return fused_load_state(c);
+}
+
+// FP64 state and increments -> FP32 pair buffers (FP32C path)
+int fused_load_state(swm_gpu_ctx *c) {
+  FusedState *f = c->fused;
+  if (!f || !f->ready || !f->comp) return SWM_GPU_OK;
+  size_t n = c->n;
+  unsigned nb = (unsigned)((n + 255) / 256);
+  f->n0 = c->n0;
+  f->g0 = c->g0;
+  for (int q = 0; q < 2; q++) {
+    k_split<<<nb, 256, 0, c->stream>>>(c->u[q], f->uh[q], f->ul[q], n);
+    k_split<<<nb, 256, 0, c->stream>>>(c->v[q], f->vh[q], f->vl[q], n);
+    k_split<<<nb, 256, 0, c->stream>>>(c->eta[q], f->eh[q], f->el[q], n);
+  }
+  for (int q = 0; q < 3; q++) {
+    k_to_f32<<<nb, 256, 0, c->stream>>>(c->Gu[q], f->Gu[q], n);
+    k_to_f32<<<nb, 256, 0, c->stream>>>(c->Gv[q], f->Gv[q], n);
+    k_to_f32<<<nb, 256, 0, c->stream>>>(c->Ge[q], f->Ge[q], n);
+  }
+  c->launches += 15;
+  SWM_CK(cudaGetLastError());
+  return SWM_GPU_OK;
+}
+
+// FP32 pair state -> FP64 buffers of the current level (host reads, diagnostics)
+int fused_sync_state(swm_gpu_ctx *c) {
+  FusedState *f = c->fused;
+  if (!f || !f->ready || !f->comp) return SWM_GPU_OK;
+  size_t n = c->n;
+  unsigned nb = (unsigned)((n + 255) / 256);
+  int a = f->n0;
+  k_join<<<nb, 256, 0, c->stream>>>(f->uh[a], f->ul[a], c->u[c->n0], n);
+  k_join<<<nb, 256, 0, c->stream>>>(f->vh[a], f->vl[a], c->v[c->n0], n);
+  k_join<<<nb, 256, 0, c->stream>>>(f->eh[a], f->el[a], c->eta[c->n0], n);
+  int g2 = (f->g0 + 1) % 3, cg2 = (c->g0 + 1) % 3;
+  k_join<<<nb, 256, 0, c->stream>>>(f->Gu[g2], nullptr, c->Gu[cg2], n);
+  k_join<<<nb, 256, 0, c->stream>>>(f->Gv[g2], nullptr, c->Gv[cg2], n);
+  k_join<<<nb, 256, 0, c->stream>>>(f->Ge[g2], nullptr, c->Ge[cg2], n);
+  c->launches += 6;
+  SWM_CK(cudaGetLastError());
+  return SWM_GPU_OK;
+}
+
+template <typename T>
+static void fill_common(swm_gpu_ctx *c, FP<T> &p, int64_t itt) {
+  const swm_gpu_config &cf = c->cfg;
+  FusedState *f = c->fused;
+  p.nx = c->nx;
+  p.ny = c->ny;
+  p.mode = cf.mode;
+  p.mix = cf.lateral_mixing ? (cf.mixing_kind == SWM_MIX_BIHARMONIC ? 2 : 1) : 0;
+  p.qbf = cf.quadratic_friction;
+  p.barotropic = cf.barotropic;
+  p.has_F = f->has_F;
+  p.impl_uniform = f->impl_uniform;
+  p.gsq_uniform = f->gsq_uniform;
+  p.wind_x = f->wind_x;
+  p.wind_y = f->wind_y;
+  p.wind_rows = f->wind_rows;
+  int tstep = (int)(itt < 3 ? itt : 3);
+  p.tstep = tstep;
+  double chi = cf.ab_chi;
+  double tab[4][3] = {{0, 0, 0}, {1., 0, 0}, {-0.5 - chi, 1.5 + chi, 0}, {5. / 12., -16. / 12., 23. / 12.}};
+  p.ab0 = (T)tab[tstep][0];
+  p.ab1 = (T)tab[tstep][1];
+  p.ab2 = (T)tab[tstep][2];
+  p.dt = (T)cf.dt;
+  p.G = (T)cf.G;
+  p.minD = (T)cf.minD;
+  p.lbc = (T)cf.lbc;
+  p.q1 = (T)(1. / (cf.A * c->hg.dTheta));
+  p.ts_rho = (T)(cf.tau_scale / cf.RHO0);
+  p.Ah = (T)cf.Ah;
+  p.bih = (T)cf.bih;
+  p.eps = sizeof(T) == 8 ? (T)2.220446049250313e-16 : (T)1.1920929e-07;
+  for (int q = 0; q < 3; q++) p.impl_s[q] = (T)f->impl_s[q];
+  for (int q = 0; q < 2; q++) p.gsq_s[q] = (T)f->gsq_s[q];
+  p.mc = f->mc;
+  p.He = (const T *)f->He;
+  p.rows = (const T *)f->rows;
+  p.Hu = (const T *)f->Hu;
+  p.Hv = (const T *)f->Hv;
+  for (int q = 0; q < 3; q++) p.impl[q] = (const T *)f->impl[q];
+  for (int q = 0; q < 2; q++) p.gsq[q] = (const T *)f->gsq[q];
+  p.Fx = (const T *)f->F[0];
+  p.Fy = (const T *)f->F[1];
+  p.Fe = (const T *)f->F[2];
+  p.wx = (const T *)f->wx;
+  p.wy = (const T *)f->wy;
+}
+
+template <typename T, bool COMP>
+static void launch_fused(swm_gpu_ctx *c, const FP<T> &p) {
+  dim3 grid((c->nx + TX - 1) / TX, (c->ny + TY - 1) / TY);
+  if (p.mix == 2) k_fused<T, 2, COMP><<<grid, NT, 0, c->stream>>>(p);
+  else k_fused<T, 1, COMP><<<grid, NT, 0, c->stream>>>(p);
+  c->launches++;
+}
+
+int fused_step(swm_gpu_ctx *c, int64_t itt) {
+  FTRY(fused_prepare(c));
+  FusedState *f = c->fused;
+  if (!f->comp) {
+    FP<double> p;
+    memset(&p, 0, sizeof(p));
+    fill_common(c, p, itt);
+    Dev d = c->dev();
+    p.u0 = d.u0; p.v0 = d.v0; p.e0 = d.eta0;
+    p.u1 = d.u1; p.v1 = d.v1; p.e1 = d.eta1;
+    p.Gu1 = d.Gu[0]; p.Gu2 = d.Gu[1]; p.Gu3 = d.Gu[2];
+    p.Gv1 = d.Gv[0]; p.Gv2 = d.Gv[1]; p.Gv3 = d.Gv[2];
+    p.Ge1 = d.Ge[0]; p.Ge2 = d.Ge[1]; p.Ge3 = d.Ge[2];
+    launch_fused<double, false>(c, p);
+  } else {
+    FP<float> p;
+    memset(&p, 0, sizeof(p));
+    fill_common(c, p, itt);
+    int a = f->n0, b = 1 - f->n0;
+    p.u0 = f->uh[a]; p.v0 = f->vh[a]; p.e0 = f->eh[a];
+    p.ul0 = f->ul[a]; p.vl0 = f->vl[a]; p.el0 = f->el[a];
+    p.u1 = f->uh[b]; p.v1 = f->vh[b]; p.e1 = f->eh[b];
+    p.ul1 = f->ul[b]; p.vl1 = f->vl[b]; p.el1 = f->el[b];
+    int s0 = f->g0, s1 = (f->g0 + 1) % 3, s2 = (f->g0 + 2) % 3;
+    p.Gu1 = f->Gu[s0]; p.Gu2 = f->Gu[s1]; p.Gu3 = f->Gu[s2];
+    p.Gv1 = f->Gv[s0]; p.Gv2 = f->Gv[s1]; p.Gv3 = f->Gv[s2];
+    p.Ge1 = f->Ge[s0]; p.Ge2 = f->Ge[s1]; p.Ge3 = f->Ge[s2];
+    launch_fused<float, true>(c, p);
+    // advance of the pair state happens here: the host-side advance only
+    // rotates the FP64 indices
+    f->n0 = 1 - f->n0;
+    f->g0 = (f->g0 + 1) % 3;
+  }
+  SWM_CK(cudaGetLastError());
+  return SWM_GPU_OK;
+}
+
+void fused_free(swm_gpu_ctx *c) {
+  FusedState *f = c->fused;
+  if (!f) return;
+  auto F = [](void *p) { if (p) cudaFree(p); };
+  for (int q = 0; q < 2; q++) { F(f->uh[q]); F(f->ul[q]); F(f->vh[q]); F(f->vl[q]); F(f->eh[q]); F(f->el[q]); }
+  for (int q = 0; q < 3; q++) { F(f->Gu[q]); F(f->Gv[q]); F(f->Ge[q]); F(f->impl[q]); F(f->F[q]); }
+  for (int q = 0; q < 2; q++) F(f->gsq[q]);
+  F(f->mc); F(f->He); F(f->rows); F(f->Hu); F(f->Hv); F(f->wx); F(f->wy);
+  delete f;
+  c->fused = nullptr;
+}
+
+}  // namespace swm
+
+// ---------------------------------------------------------------------------
+// Domain integrals (volume, potential and kinetic energy) in FP64
+// ---------------------------------------------------------------------------
+namespace swm {
+
+template <typename T, bool COMP>
+__global__ void k_integrals(int nx, int ny, const int8_t *oU, const int8_t *oV, const int8_t *oE,
+                            const double *area_u, const double *area_e, const T *u, const float *ul,
+                            const T *v, const float *vl, const T *e, const float *el, double G,
+                            double *partial) {
+  __shared__ double red[3][256];
+  double s0 = 0., s1 = 0., s2 = 0.;
+  size_t n = (size_t)nx * ny;
+  for (size_t k = (size_t)blockIdx.x * blockDim.x + threadIdx.x; k < n; k += (size_t)gridDim.x * blockDim.x) {
+    int j = (int)(k / nx);
+    double ee = (double)e[k] + (COMP ? (double)el[k] : 0.);
+    double uu = (double)u[k] + (COMP ? (double)ul[k] : 0.);
+    double vv = (double)v[k] + (COMP ? (double)vl[k] : 0.);
+    if (oE[k]) {
+      s0 += ee * area_e[j];
+      s1 += 0.5 * G * ee * ee * area_e[j];
+    }
+    if (oU[k]) s2 += 0.5 * uu * uu * area_u[j];
+    if (oV[k]) s2 += 0.5 * vv * vv * area_e[j];
+  }
+  red[0][threadIdx.x] = s0;
+  red[1][threadIdx.x] = s1;
+  red[2][threadIdx.x] = s2;
+  __syncthreads();
+  for (int w = 128; w > 0; w >>= 1) {
+    if (threadIdx.x < w)
+      for (int q = 0; q < 3; q++) red[q][threadIdx.x] += red[q][threadIdx.x + w];
+    __syncthreads();
+  }
+  if (threadIdx.x == 0)
+    for (int q = 0; q < 3; q++) partial[(size_t)q * gridDim.x + blockIdx.x] = red[q][0];
+}
+
+__global__ void k_integrals_final(const double *partial, int nb, double *out) {
+  __shared__ double red[256];
+  for (int q = 0; q < 3; q++) {
+    double a = 0.;
+    for (int b = threadIdx.x; b < nb; b += blockDim.x) a += partial[(size_t)q * nb + b];
+    red[threadIdx.x] = a;
+    __syncthreads();
+    for (int w = 128; w > 0; w >>= 1) {
+      if (threadIdx.x < w) red[threadIdx.x] += red[threadIdx.x + w];
+      __syncthreads();
+    }
+    if (threadIdx.x == 0) out[q] = red[0];
+    __syncthreads();
+  }
+}
+
+__global__ void k_expand_rows(const double *rows, double *field, int nx, int ny) {
+  size_t k = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (k < (size_t)nx * ny) field[k] = rows[k / nx];
+}
+
+__global__ void k_rows_f32(const double *rows, float *dst, int ny) {
+  int j = blockIdx.x * blockDim.x + threadIdx.x;
+  if (j < ny) dst[j] = (float)rows[j];
+}
+
+}  // namespace swm
+
+struct IntegralScratch {
+  double *area_u = nullptr, *area_e = nullptr, *partial = nullptr, *out = nullptr, *rows = nullptr;
+  double *host = nullptr;  // pinned
+  int nb = 0;
+};
+
+extern "C" {
+
+int swm_gpu_set_stream_rows(swm_gpu_ctx *c, int id, const double *r1, const double *r2) {
+  SWM_REQUIRE(c && id >= 0 && id < (int)c->streams.size() && r1, "swm_gpu_set_stream_rows: bad arguments");
+  static thread_local double *d_rows = nullptr;
+  static thread_local int d_rows_n = 0;
+  if (d_rows_n < 2 * c->ny) {
+    if (d_rows) cudaFree(d_rows);
+    SWM_CK(cudaMalloc((void **)&d_rows, 2 * (size_t)c->ny * 8));
+    d_rows_n = 2 * c->ny;
+  }
+  const Stream &s = c->streams[id];
+  SWM_CK(cudaMemcpyAsync(d_rows, r1, c->ny * 8, cudaMemcpyHostToDevice, c->stream));
+  if (r2) SWM_CK(cudaMemcpyAsync(d_rows + c->ny, r2, c->ny * 8, cudaMemcpyHostToDevice, c->stream));
+  FusedState *f = c->fused;
+  bool fused_rows = f && f->ready && f->wind_rows && !s.is_const && s.type == SWM_FRC_WIND;
+  if (fused_rows) {
+    void *dst = s.comp == SWM_CMP_ZONAL ? f->wx : f->wy;
+    if (f->comp) {
+      k_rows_f32<<<(c->ny + 255) / 256, 256, 0, c->stream>>>(d_rows, (float *)dst, c->ny);
+    } else {
+      SWM_CK(cudaMemcpyAsync(dst, d_rows, c->ny * 8, cudaMemcpyDeviceToDevice, c->stream));
+    }
+  } else {
+    unsigned nb = (unsigned)((c->n + 255) / 256);
+    k_expand_rows<<<nb, 256, 0, c->stream>>>(d_rows, s.d1, c->nx, c->ny);
+    if (r2) k_expand_rows<<<nb, 256, 0, c->stream>>>(d_rows + c->ny, s.d2, c->nx, c->ny);
+  }
+  c->launches++;
+  SWM_CK(cudaGetLastError());
+  return SWM_GPU_OK;
+}
+
+int swm_gpu_integrals(swm_gpu_ctx *c, double *out3) {
+  SWM_REQUIRE(c && c->stage >= 5 && out3, "swm_gpu_integrals: bad arguments");
+  static thread_local std::vector<std::pair<swm_gpu_ctx *, IntegralScratch>> cache;
+  IntegralScratch *S = nullptr;
+  for (auto &e : cache)
+    if (e.first == c) S = &e.second;
+  if (!S) {
+    cache.emplace_back(c, IntegralScratch());
+    S = &cache.back().second;
+    const HostGrid &g = c->hg;
+    std::vector<double> au(c->ny), ae(c->ny);
+    double A = c->cfg.A;
+    for (int j = 0; j < c->ny; j++) {
+      au[j] = A * A * g.cosl[GU][j] * g.dLambda * g.dTheta;
+      ae[j] = A * A * g.cosl[GE][j] * g.dLambda * g.dTheta;
+    }
+    S->nb = 2 * 152;
+    SWM_CK(cudaMalloc((void **)&S->area_u, c->ny * 8));
+    SWM_CK(cudaMalloc((void **)&S->area_e, c->ny * 8));
+    SWM_CK(cudaMalloc((void **)&S->partial, 3 * (size_t)S->nb * 8));
+    SWM_CK(cudaMalloc((void **)&S->out, 3 * 8));
+    SWM_CK(cudaMallocHost((void **)&S->host, 3 * 8));
+    SWM_CK(cudaMemcpy(S->area_u, au.data(), c->ny * 8, cudaMemcpyHostToDevice));
+    SWM_CK(cudaMemcpy(S->area_e, ae.data(), c->ny * 8, cudaMemcpyHostToDevice));
+  }
+  FusedState *f = c->fused;
+  const int8_t *oU = c->d_ocean[GU], *oV = c->d_ocean[GV], *oE = c->d_ocean[GE];
+  if (f && f->ready && f->comp) {
+    int a = f->n0;
+    k_integrals<float, true><<<S->nb, 256, 0, c->stream>>>(c->nx, c->ny, oU, oV, oE, S->area_u, S->area_e,
+                                                            f->uh[a], f->ul[a], f->vh[a], f->vl[a], f->eh[a],
+                                                            f->el[a], c->cfg.G, S->partial);
+  } else {
+    k_integrals<double, false><<<S->nb, 256, 0, c->stream>>>(c->nx, c->ny, oU, oV, oE, S->area_u, S->area_e,
+                                                              c->u[c->n0], nullptr, c->v[c->n0], nullptr,
+                                                              c->eta[c->n0], nullptr, c->cfg.G, S->partial);
+  }
+  k_integrals_final<<<1, 256, 0, c->stream>>>(S->partial, S->nb, S->out);
+  c->launches += 2;
+  SWM_CK(cudaMemcpyAsync(S->host, S->out, 3 * 8, cudaMemcpyDeviceToHost, c->stream));
+  SWM_CK(cudaStreamSynchronize(c->stream));
+  for (int q = 0; q < 3; q++) out3[q] = S->host[q];
+  return SWM_GPU_OK;
+}
+
+}  // extern "C"

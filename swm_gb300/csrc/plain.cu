@@ -1,0 +1,413 @@
+// plain.cu -- FP64 per-module kernels: the drop-in path.
+//
+// One kernel per reference loop nest, same formulas, same evaluation order;
+// this translation unit is compiled with -fmad=false so that every product
+// and sum is rounded exactly as the FP64 CPU restatement rounds it.  Fields
+// are unpadded (Nx, Ny); neighbour indices wrap periodically like the
+// reference's cshift index vectors (domain_module.f90:106-115).
+#include "ctx.h"
+
+namespace swm {
+
+#define IDX(i, j) ((size_t)(i) + (size_t)d.nx * (size_t)(j))
+
+__device__ __forceinline__ int ip1(int i, int n) { return i + 1 == n ? 0 : i + 1; }
+__device__ __forceinline__ int im1(int i, int n) { return i == 0 ? n - 1 : i - 1; }
+
+// mask-normalised interpolation weights (calc_lib.f90:253-265, 320-335)
+__device__ __forceinline__ double ip2_noland(const double *v, const int8_t *m, size_t k1, size_t k2) {
+  double w = 1. / fmax((double)(m[k1] + m[k2]), 1.);
+  return ((double)m[k1] * w) * v[k1] + ((double)m[k2] * w) * v[k2];
+}
+__device__ __forceinline__ double ip4_noland(const double *v, const int8_t *m, size_t k1, size_t k2,
+                                             size_t k3, size_t k4) {
+  double w = 1. / fmax((double)(m[k1] + m[k2] + m[k3] + m[k4]), 1.);
+  return ((double)m[k1] * w) * v[k1] + ((double)m[k2] * w) * v[k2] + ((double)m[k3] * w) * v[k3] +
+         ((double)m[k4] * w) * v[k4];
+}
+__device__ __forceinline__ double ip2(const double *v, size_t k1, size_t k2) { return .5 * v[k1] + .5 * v[k2]; }
+__device__ __forceinline__ double ip4(const double *v, size_t k1, size_t k2, size_t k3, size_t k4) {
+  return .25 * v[k1] + .25 * v[k2] + .25 * v[k3] + .25 * v[k4];
+}
+
+#define KERNEL_PROLOGUE                               \
+  int i = blockIdx.x * blockDim.x + threadIdx.x;      \
+  int j = blockIdx.y * blockDim.y + threadIdx.y;      \
+  if (i >= d.nx || j >= d.ny) return;                \
+  size_t k = IDX(i, j);
+
+// computeD, FULLY_NONLINEAR part (swm_nonlinear_timestep_module.f90:187-197)
+__global__ void k_D_nonlinear(Dev d) {
+  KERNEL_PROLOGUE
+  if (d.ocean[GE][k] != 1) return;
+  d.D[k] = d.eta0[k] + d.Hg[GE][k];
+}
+
+// computeD, thickness on H/u/v points (:201-217)
+__global__ void k_D_interp(Dev d) {
+  KERNEL_PROLOGUE
+  const int8_t *oE = d.ocean[GE];
+  int im = im1(i, d.nx), jm = im1(j, d.ny);
+  double dh = ip4_noland(d.D, oE, k, IDX(im, jm), IDX(im, j), IDX(i, jm));
+  double du = ip2_noland(d.D, oE, k, IDX(im, j));
+  double dv = ip2_noland(d.D, oE, k, IDX(i, jm));
+  d.Dh[k] = dh;
+  d.Du[k] = du;
+  d.Dv[k] = dv;
+}
+
+// computeRelVort -> vorticityFromVelocities2D (calc_lib.f90:663-678)
+__global__ void k_vorticity(Dev d) {
+  KERNEL_PROLOGUE
+  size_t ki = IDX(im1(i, d.nx), j), kj = IDX(i, im1(j, d.ny));
+  double bc = d.ocean[GH][k] == 1 ? 1. : d.lbc;
+  double dvdx, dudy;
+  if (d.ocean[GV][ki] + d.ocean[GV][k] == 0) dvdx = 0.;
+  else dvdx = bc / (d.A * d.cosl[GH][j] * d.dLambda) * (d.v0[k] - d.v0[ki]);
+  if (d.ocean[GU][k] + d.ocean[GU][kj] == 0) dudy = 0.;
+  else dudy = bc * (d.cosl[GU][j] * d.u0[k] - d.cosl[GU][im1(j, d.ny)] * d.u0[kj]) / (d.A * d.dTheta);
+  d.zeta[k] = dvdx - dudy / d.cosl[GH][j];
+}
+
+// computePotVort (:230-257)
+__global__ void k_pot(Dev d) {
+  KERNEL_PROLOGUE
+  const double eps = 2.220446049250313e-16;
+  double pD = fmax(d.Dh[k], eps);
+  double fH = d.f[GH][j];
+  if (d.mode == SWM_MODE_NONLINEAR) d.pot[k] = (fH + d.zeta[k]) / pD;
+  else if (d.mode == SWM_MODE_LIN_MEAN) d.pot[k] = (fH + d.zbs[k]) / pD;
+  else d.pot[k] = fH / pD;
+}
+
+// computeEdens (:259-310); u2/v2 of the reference evaluated in place
+__global__ void k_edens(Dev d) {
+  KERNEL_PROLOGUE
+  if (d.ocean[GE][k] != 1) return;
+  size_t ku = IDX(ip1(i, d.nx), j), kv = IDX(i, ip1(j, d.ny));
+  if (d.mode == SWM_MODE_NONLINEAR) {
+    double a = .5 * (d.u0[ku] * d.u0[ku]) + .5 * (d.u0[k] * d.u0[k]);
+    double b = .5 * (d.v0[kv] * d.v0[kv]) + .5 * (d.v0[k] * d.v0[k]);
+    d.edens[k] = (a + b) / 2. + d.G * d.eta0[k];
+  } else if (d.mode == SWM_MODE_LIN_MEAN) {
+    double a = .5 * (d.u0[ku] * d.ubs[ku]) + .5 * (d.u0[k] * d.ubs[k]);
+    double b = .5 * (d.v0[kv] * d.vbs[kv]) + .5 * (d.v0[k] * d.vbs[k]);
+    d.edens[k] = (a + b) + d.G * d.eta0[k];
+  } else {
+    d.edens[k] = d.G * d.eta0[k];
+  }
+}
+
+// computeMassFluxes (:312-326)
+__global__ void k_massflux(Dev d) {
+  KERNEL_PROLOGUE
+  if (d.ocean[GU][k] == 1) d.mu[k] = d.Du[k] * d.u0[k];
+  if (d.ocean[GV][k] == 1) d.mv[k] = d.Dv[k] * d.v0[k];
+}
+
+// SWM_LateralMixing_compute_p (swm_lateralmixing_module.f90:215-240) with the
+// coefficients of _init_p_coefficients (:132-145) evaluated in place.
+__global__ void k_latmix_p(Dev d, double Ah, const double *u, const double *v, const double *Dp,
+                           const double *Dhp, double *pll, double *plt) {
+  KERNEL_PROLOGUE
+  double A = d.A;
+  if (d.ocean[GE][k] == 1) {
+    size_t kjp = IDX(i, ip1(j, d.ny));
+    double bc = 1.;
+    int8_t ov = d.ocean[GV][k], ovp = d.ocean[GV][kjp];
+    int o = ov + ovp;
+    double ot = (double)(o > 1 ? o : 1), tn = d.tanl[GE][j];
+    double c0 = -Ah * bc / d.dLambda / A / d.cosl[GE][j];
+    double c1 = Ah / A * (bc / d.dTheta + ovp * tn / ot);
+    double c2 = Ah / A * (-bc / d.dTheta + ov * tn / ot);
+    pll[k] = Dp[k] * (c0 * (u[IDX(ip1(i, d.nx), j)] - u[k]) + c1 * v[kjp] + c2 * v[k]);
+  }
+  if (d.ocean[GH][k] == 1) {
+    size_t kjm = IDX(i, im1(j, d.ny));
+    double bc = 1.;
+    int8_t ou = d.ocean[GU][k], oum = d.ocean[GU][kjm];
+    int o = ou + oum;
+    double ot = (double)(o > 1 ? o : 1), tn = d.tanl[GH][j];
+    double c0 = -Ah * bc / d.dLambda / A / d.cosl[GH][j];
+    double c1 = -Ah / A * (bc / d.dTheta + ou * tn / ot);
+    double c2 = -Ah / A * (-bc / d.dTheta + oum * tn / ot);
+    plt[k] = Dhp[k] * (c0 * (v[k] - v[IDX(im1(i, d.nx), j)]) + c1 * u[k] + c2 * u[kjm]);
+  }
+}
+
+// SWM_LateralMixing_compute_uv (:162-186) with lat_mixing_u/v (:84-97)
+__global__ void k_latmix_uv(Dev d, const double *pll, const double *plt, const double *Dup,
+                            const double *Dvp, double *lu, double *lv) {
+  KERNEL_PROLOGUE
+  double A = d.A;
+  if (d.ocean[GU][k] == 1) {
+    double bc = 1., tn = d.tanl[GU][j];
+    int o = d.ocean[GH][k] + d.ocean[GH][IDX(i, ip1(j, d.ny))];
+    double ot = (double)(o > 1 ? o : 1);
+    double c0 = -bc / A / d.cosl[GU][j] / d.dLambda;
+    double c1 = -(bc / A / d.dTheta - 2. * tn / A / ot);
+    double c2 = -(-bc / A / d.dTheta - 2. * tn / A / ot);
+    lu[k] = (c0 * (pll[k] - pll[IDX(im1(i, d.nx), j)]) + c1 * plt[IDX(i, ip1(j, d.ny))] + c2 * plt[k]) / Dup[k];
+  }
+  if (d.ocean[GV][k] == 1) {
+    double bc = 1., tn = d.tanl[GV][j];
+    int o = d.ocean[GE][k] + d.ocean[GE][IDX(i, im1(j, d.ny))];
+    double ot = (double)(o > 1 ? o : 1);
+    double c0 = -bc / A / d.cosl[GV][j] / d.dLambda;
+    double c1 = -(-bc / A / d.dTheta + 2. * tn / A / ot);
+    double c2 = -(bc / A / d.dTheta + 2. * tn / A / ot);
+    lv[k] = (c0 * (plt[IDX(ip1(i, d.nx), j)] - plt[k]) + c1 * pll[k] + c2 * pll[IDX(i, im1(j, d.ny))]) / Dvp[k];
+  }
+}
+
+// SWM_timestep_nonlinear, continuity (:349-374)
+__global__ void k_tend_eta(Dev d) {
+  KERNEL_PROLOGUE
+  if (d.ocean[GE][k] != 1) return;
+  int ip = ip1(i, d.nx), jp = ip1(j, d.ny);
+  const double *cV = d.cosl[GV];
+  double t = -(d.mu[IDX(ip, j)] - d.mu[k]) / d.dLambda - (d.mv[IDX(i, jp)] * cV[jp] - d.mv[k] * cV[j]) / d.dTheta;
+  if (d.mode == SWM_MODE_LIN_MEAN) {
+    const int8_t *oE = d.ocean[GE];
+    int qi = ip1(j % d.nx, d.nx);  // ip1(j): zonal index taken from j in the reference (:360)
+    double ea = ip2_noland(d.eta0, oE, IDX(qi, j), IDX(im1(qi, d.nx), j));
+    double eb = ip2_noland(d.eta0, oE, k, IDX(im1(i, d.nx), j));
+    double ec = ip2_noland(d.eta0, oE, IDX(i, jp), IDX(i, im1(jp, d.ny)));
+    double ed = ip2_noland(d.eta0, oE, k, IDX(i, im1(j, d.ny)));
+    t = t - (ea * d.ubs[IDX(ip, j)] - eb * d.ubs[k]) / d.dLambda -
+        (cV[jp] * ec * d.vbs[IDX(i, jp)] - cV[j] * ed * d.vbs[k]) / d.dTheta;
+  }
+  d.Ge[2][k] = t / (d.A * d.cosl[GE][j]) + d.Fe[k];
+}
+
+// SWM_timestep_nonlinear, zonal momentum (:378-409)
+__global__ void k_tend_u(Dev d) {
+  KERNEL_PROLOGUE
+  if (d.ocean[GU][k] != 1) return;
+  int im = im1(i, d.nx), jp = ip1(j, d.ny);
+  size_t a1 = IDX(i, jp), a2 = IDX(im, j), a3 = IDX(im, jp);
+  double g = ip2(d.pot, a1, k) * ip4(d.mv, a1, a2, a3, k);
+  if (d.mode == SWM_MODE_LIN_MEAN) g = g + ip2(d.zeta, a1, k) * ip4(d.vbs, a1, a2, a3, k);
+  g = g - ((d.edens[k] - d.edens[IDX(im, j)]) / (d.A * d.cosl[GU][j] * d.dLambda));
+  if (d.qbf) {
+    double vv = ip4(d.v0, a1, a2, a3, k);
+    double q = d.gsq_u[k] * sqrt(d.u0[k] * d.u0[k] + (vv * vv)) * d.u0[k];
+    if (d.barotropic) q = q / d.Hg[GU][k];
+    g = g - q;
+  }
+  if (d.lateral_mixing) g = g + d.lmu[k];
+  d.Gu[2][k] = g + d.Fx[k];
+}
+
+// SWM_timestep_nonlinear, meridional momentum (:411-444)
+__global__ void k_tend_v(Dev d) {
+  KERNEL_PROLOGUE
+  if (d.ocean[GV][k] != 1) return;
+  int ip = ip1(i, d.nx), jm = im1(j, d.ny);
+  size_t a1 = IDX(ip, j), a2 = IDX(i, jm), a4 = IDX(ip, jm);
+  double g = -ip2(d.pot, a1, k) * ip4(d.mu, a1, a2, k, a4);
+  if (d.mode == SWM_MODE_LIN_MEAN) g = g - ip2(d.zeta, a1, k) * ip4(d.ubs, a1, a2, k, a4);
+  g = g - ((d.edens[k] - d.edens[IDX(i, jm)]) / (d.A * d.dTheta));
+  if (d.qbf) {
+    double uu = ip4(d.u0, a1, a2, k, a4);
+    double q = d.gsq_v[k] * sqrt(d.v0[k] * d.v0[k] + (uu * uu)) * d.v0[k];
+    if (d.barotropic) q = q / d.Hg[GV][k];
+    g = g - q;
+  }
+  if (d.lateral_mixing) g = g + d.lmv[k];
+  d.Gv[2][k] = g + d.Fy[k];
+}
+
+struct ABCoef {
+  double c[3];
+  int tstep;
+};
+
+// integrate_AB_vec (time_integration_module.f90:74-112) for the three
+// prognostic fields, plus the FULLY_NONLINEAR thickness clamp (:176-179)
+__global__ void k_integrate(Dev d, ABCoef ab) {
+  KERNEL_PROLOGUE
+  double a = d.eta0[k], b = d.u0[k], c = d.v0[k];
+  for (int t = 0; t < ab.tstep; t++) {
+    a = a + d.dt * ab.c[t] * d.Ge[t][k];
+    b = b + d.dt * ab.c[t] * d.Gu[t][k];
+    c = c + d.dt * ab.c[t] * d.Gv[t][k];
+  }
+  a = a / d.impl_e[k];
+  if (d.mode == SWM_MODE_NONLINEAR) {
+    double lim = d.minD - d.Hg[GE][k];
+    if (a < lim) a = lim;
+  }
+  d.eta1[k] = a;
+  d.u1[k] = b / d.impl_u[k];
+  d.v1[k] = c / d.impl_v[k];
+}
+
+// SWM_forcing_update reset (swm_forcing_module.f90:141-149)
+__global__ void k_forcing_reset(Dev d) {
+  KERNEL_PROLOGUE
+  d.Fe[k] = d.Fec[k];
+  d.Fx[k] = d.Fxc[k];
+  d.Fy[k] = d.Fyc[k];
+}
+
+// SWM_forcing_process* for one stream (swm_forcing_module.f90:274-552)
+__global__ void k_stream(Dev d, Stream s, double *Fx, double *Fy, double *Fe, double r_iot, double i_iot) {
+  KERNEL_PROLOGUE
+  const int8_t *oU = d.ocean[GU], *oV = d.ocean[GV], *oE = d.ocean[GE];
+  const double *dd = s.d1;
+  switch (s.type) {
+    case SWM_FRC_WIND: {
+      bool z = s.comp == SWM_CMP_ZONAL;
+      double *F = z ? Fx : Fy;
+      const int8_t *m = z ? oU : oV;
+      const double *H = z ? d.Du : d.Dv;
+      bool sh = d.barotropic || d.mode == SWM_MODE_NONLINEAR;
+      if (m[k] == 1) F[k] = F[k] + (d.tau_scale * dd[k] / (sh ? (d.RHO0 * H[k]) : d.RHO0));
+      break;
+    }
+    case SWM_FRC_OSC: {
+      double *F = s.comp == SWM_CMP_ZONAL ? d.Fx : (s.comp == SWM_CMP_MERID ? d.Fy : d.Fe);
+      const int8_t *m = s.comp == SWM_CMP_ZONAL ? oU : (s.comp == SWM_CMP_MERID ? oV : oE);
+      F[k] = F[k] + (2. * (s.d1[k] * r_iot - s.d2[k] * i_iot)) * m[k];
+      break;
+    }
+    case SWM_FRC_CUSTOM: {
+      double *F = s.comp == SWM_CMP_ZONAL ? Fx : (s.comp == SWM_CMP_MERID ? Fy : Fe);
+      const int8_t *m = s.comp == SWM_CMP_ZONAL ? oU : (s.comp == SWM_CMP_MERID ? oV : oE);
+      if (m[k] == 1) F[k] = F[k] + dd[k];
+      break;
+    }
+    case SWM_FRC_HEAT:
+      if (oE[k] == 1) Fe[k] = Fe[k] + dd[k];
+      break;
+    case SWM_FRC_EMF: {
+      double A = d.A;
+      const double *He = d.Hg[GE], *Hu = d.Hg[GU], *Hv = d.Hg[GV], *H = d.Hg[GH];
+      const double *cu = d.cosl[GU], *cv = d.cosl[GV];
+      int nx = d.nx, ny = d.ny;
+      auto h2eta = [&](int ii, int jj) {
+        return ip4(dd, IDX(ip1(ii, nx), ip1(jj, ny)), IDX(ii, jj), IDX(ii, ip1(jj, ny)), IDX(ip1(ii, nx), jj));
+      };
+      if (s.comp == SWM_CMP_U2) {
+        if (oU[k] != 1) break;
+        int im = im1(i, nx);
+        Fx[k] = Fx[k] + (-(h2eta(i, j) * He[k] - h2eta(im, j) * He[IDX(im, j)]) / (2 * A * d.dLambda * cu[j] * Hu[k]));
+      } else if (s.comp == SWM_CMP_V2) {
+        if (oV[k] != 1) break;
+        int jm = im1(j, ny);
+        Fy[k] = Fy[k] + (-(cu[j] * He[k] * h2eta(i, j) - cu[jm] * He[IDX(i, jm)] * h2eta(i, jm)) /
+                         (8 * A * d.dTheta * cv[j] * Hv[k]));
+      } else {
+        int jp = ip1(j, ny), ip = ip1(i, nx);
+        if (oU[k] == 1)
+          Fx[k] = Fx[k] + (-(cv[jp] * dd[IDX(i, jp)] * H[IDX(i, jp)] - cv[j] * dd[k] * H[k]) /
+                           (2 * A * d.dTheta * cu[j] * Hu[k]));
+        if (oV[k] == 1)
+          Fy[k] = Fy[k] + (-(dd[IDX(ip, j)] * H[IDX(ip, j)] - dd[k] * H[k]) / (2 * A * d.dLambda * cv[j] * Hv[k]));
+      }
+      break;
+    }
+  }
+}
+
+__global__ void k_fill(double *p, size_t n, double v) {
+  size_t k = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (k < n) p[k] = v;
+}
+
+#undef KERNEL_PROLOGUE
+
+static dim3 blk() { return dim3(32, 8); }
+static dim3 grd(const swm_gpu_ctx *c) { return dim3((c->nx + 31) / 32, (c->ny + 7) / 8); }
+
+#define LAUNCH(kern, ...)                                               \
+  do {                                                                  \
+    kern<<<grd(c), blk(), 0, c->stream>>>(__VA_ARGS__);                 \
+    c->launches++;                                                      \
+  } while (0)
+
+int plain_fill(swm_gpu_ctx *c, double *p, double value) {
+  k_fill<<<(unsigned)((c->n + 255) / 256), 256, 0, c->stream>>>(p, c->n, value);
+  c->launches++;
+  SWM_CK(cudaGetLastError());
+  return SWM_GPU_OK;
+}
+
+// SWM_timestep_advance diagnostics (swm_nonlinear_timestep_module.f90:150-154)
+int plain_diagnostics(swm_gpu_ctx *c, int64_t itt) {
+  Dev d = c->dev();
+  int mode = c->cfg.mode;
+  bool linear = mode == SWM_MODE_LIN_REST || mode == SWM_MODE_LIN_MEAN;
+  if (mode == SWM_MODE_NONLINEAR) LAUNCH(k_D_nonlinear, d);
+  if (!linear || itt == 0) LAUNCH(k_D_interp, d);
+  if (mode == SWM_MODE_NONLINEAR || mode == SWM_MODE_LIN_MEAN) LAUNCH(k_vorticity, d);
+  if (mode != SWM_MODE_NONE) {
+    LAUNCH(k_pot, d);
+    LAUNCH(k_edens, d);
+  }
+  LAUNCH(k_massflux, d);
+  SWM_CK(cudaGetLastError());
+  return SWM_GPU_OK;
+}
+
+// SWM_forcing_update (:135-170) or the constant part of SWM_forcing_init
+// (:124-125).  Streams are visited in the reference's linked-list order: the
+// head (first namelist record) first, then the others newest first
+// (generic_list.f90:87-103 inserts after the head).
+int plain_forcing_update(swm_gpu_ctx *c, int64_t itt, int constant_part) {
+  Dev d = c->dev();
+  if (!constant_part) LAUNCH(k_forcing_reset, d);
+  int ns = (int)c->streams.size();
+  if (ns == 0) {
+    SWM_CK(cudaGetLastError());
+    return SWM_GPU_OK;
+  }
+  std::vector<int> order;
+  order.push_back(0);
+  for (int s = ns - 1; s >= 1; s--) order.push_back(s);
+  for (int q : order) {
+    const Stream &s = c->streams[q];
+    bool tdf = !s.is_const;
+    if (constant_part == (int)tdf) continue;  // process when isTDF != isConstant
+    double *Fx = s.is_const ? d.Fxc : d.Fx, *Fy = s.is_const ? d.Fyc : d.Fy, *Fe = s.is_const ? d.Fec : d.Fe;
+    double r = 0., im = 0.;
+    if (s.type == SWM_FRC_OSC) {
+      r = cos(s.omega * (double)itt * c->cfg.dt);
+      im = sin(s.omega * (double)itt * c->cfg.dt);
+    }
+    LAUNCH(k_stream, d, s, Fx, Fy, Fe, r, im);
+  }
+  SWM_CK(cudaGetLastError());
+  return SWM_GPU_OK;
+}
+
+// SWM_timestep_step (swm_nonlinear_timestep_module.f90:164-180)
+int plain_step(swm_gpu_ctx *c, int64_t itt) {
+  Dev d = c->dev();
+  if (c->cfg.lateral_mixing) {
+    if (c->cfg.mixing_kind == SWM_MIX_BIHARMONIC) {
+      // project extension: Laplacian-type operator with unit thickness and
+      // Ah = 1, then the thickness-weighted operator with Ah = -bih
+      LAUNCH(k_latmix_p, d, 1., d.u0, d.v0, c->ones, c->ones, c->bh[0], c->bh[1]);
+      LAUNCH(k_latmix_uv, d, c->bh[0], c->bh[1], c->ones, c->ones, c->bh[2], c->bh[3]);
+      LAUNCH(k_latmix_p, d, -c->cfg.bih, c->bh[2], c->bh[3], d.D, d.Dh, d.pll, d.plt);
+    } else {
+      LAUNCH(k_latmix_p, d, c->cfg.Ah, d.u0, d.v0, d.D, d.Dh, d.pll, d.plt);
+    }
+    LAUNCH(k_latmix_uv, d, d.pll, d.plt, d.Du, d.Dv, d.lmu, d.lmv);
+  }
+  LAUNCH(k_tend_eta, d);
+  LAUNCH(k_tend_u, d);
+  LAUNCH(k_tend_v, d);
+  ABCoef ab;
+  ab.tstep = (int)(itt < 3 ? itt : 3);
+  const double chi = c->cfg.ab_chi;
+  double tab[4][3] = {{0, 0, 0}, {1., 0, 0}, {-0.5 - chi, 1.5 + chi, 0}, {5. / 12., -16. / 12., 23. / 12.}};
+  for (int q = 0; q < 3; q++) ab.c[q] = tab[ab.tstep][q];
+  LAUNCH(k_integrate, d, ab);
+  SWM_CK(cudaGetLastError());
+  return SWM_GPU_OK;
+}
+
+}  // namespace swm

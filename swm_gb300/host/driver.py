@@ -1,0 +1,154 @@
+"""Host time loop and diagnostics (restates model.f90 initModel/timestepModel,
+swm_forcing_module stream bookkeeping and diagTask.f90 processTask).
+
+The driver is backend-agnostic: a backend implements the SWM/tracer entry
+points (``setup_domain``, ``timestep_init``, ``add_damping``,
+``finish_damping``, ``add_stream``, ``set_stream_data``, ``forcing_init``,
+``initial_conditions``, ``add_tracer``, ``tracer_init``, ``step``,
+``advance``, ``field``, ``streamfunction``) and the driver supplies what the
+Fortran host would: time-interpolated input records and the diagnostics
+cadence.  The GB300 path and the CPU oracle are both driven through it.
+"""
+import math
+import numpy as np
+
+from .memchunk import MemChunk
+from .case import MODE_NONLINEAR
+
+# registry name -> (backend field name, grid of the output mask)
+DIAG_VARS = {
+    'U': ('tot_u', 'u'), 'V': ('tot_v', 'v'), 'ETA': ('tot_eta', 'eta'),
+    'SWM_U': ('u', 'u'), 'SWM_V': ('v', 'v'), 'SWM_ETA': ('eta', 'eta'),
+    'PSI': ('psi', 'H'), 'H': ('H', 'H'), 'H_U': ('H_u', 'u'), 'H_V': ('H_v', 'v'), 'H_ETA': ('H_eta', 'eta'),
+    'IMPL_U': ('impl_u', 'u'), 'IMPL_V': ('impl_v', 'v'), 'IMPL_ETA': ('impl_eta', 'eta'),
+    'GAMMA_LIN_U': ('gamma_lin_u', 'u'), 'GAMMA_LIN_V': ('gamma_lin_v', 'v'),
+    'GAMMA_LIN_ETA': ('gamma_lin_eta', 'eta'),
+    'SWM_EDENS': ('edens', 'eta'), 'SWM_POT': ('pot', 'H'), 'SWM_RELVORT': ('zeta', 'H'),
+    'SWM_MU': ('mu', 'u'), 'SWM_MV': ('mv', 'v'), 'SWM_D': ('D', 'eta'),
+    'F_X': ('F_x', 'u'), 'F_Y': ('F_y', 'v'), 'F_ETA': ('F_eta', 'eta'),
+}
+
+
+class DiagTask:
+    """One &diag_nl entry (diagTask.f90:266-335)."""
+
+    def __init__(self, spec, Nt, dsi, dt, meant_out):
+        self.spec = spec
+        self.name = spec['varname'].upper()
+        self.type = spec['type']
+        self.period = spec['period']
+        self.square = spec['process'] == 'S'
+        self.dt, self.dsi, self.meant_out = dt, dsi, meant_out
+        self.nstep = max(int((Nt - dsi) // spec['frequency']), 1) if self.type == 'S' and spec['frequency'] > 0 else 1
+        self.buffer = None
+        self.count = 0.0
+        self.times, self.records = [], []
+
+    def _add(self, data, dT):
+        d = data * data if self.square else data
+        if self.buffer is None:
+            self.buffer = np.zeros_like(d)
+        self.buffer = self.buffer + dT * d
+        self.count = self.count + dT
+
+    def process(self, itt, fetch):
+        k = itt - self.dsi
+        if math.fmod(k, self.nstep) != 0:
+            return
+        if self.type == 'S':
+            self.times.append(itt * self.dt)
+            self.records.append(fetch(self.name).copy())
+        elif self.type == 'A':
+            per = self.period if self.period != 2.628e6 else self.meant_out
+            dT = min(math.fmod(self.dt * k, per), self.dt)
+            data = fetch(self.name)
+            if dT < self.dt and k != 0:
+                self._add(data, self.dt - dT)
+                self.buffer = self.buffer / self.count
+                self.times.append(self.dt * itt - dT)
+                self.records.append(self.buffer.copy())
+                self.buffer = np.zeros_like(self.buffer)
+                self.count = 0.0
+            self._add(data, dT)
+        elif self.type == 'I':
+            if itt == 0:
+                self.times.append(0.0)
+                self.records.append(fetch(self.name).copy())
+
+
+class Driver:
+    def __init__(self, case, backend):
+        self.case, self.b = case, backend
+        self.cfg = case['config']
+        self.itt = 0
+        self.tasks = []
+        self._psi_cache = None
+
+    # -- init sequence: model.f90 initModel :71-144 ---------------------
+    def init(self, with_diag=True):
+        c, b, case = self.cfg, self.b, self.case
+        b.setup_domain(case)
+        b.timestep_init(case.get('psi_bs'))
+        for d in case['damping']:
+            b.add_damping(d)
+        b.finish_damping()
+        self.chunks = []
+        for s in case['streams']:
+            mc1 = MemChunk(s['rec1'], s['dt1'], s['chunksize'])
+            mc2 = MemChunk(s['rec2'], s['dt2'], s['chunksize']) if s['rec2'] is not None else None
+            tdf = (s['type'] == 1) or (s['type'] == 0 and c['mode'] == MODE_NONLINEAR) or not mc1.is_constant
+            self.chunks.append((mc1, mc2, tdf))
+            d1 = mc1.get(0.0) if not tdf else np.zeros_like(mc1.rec[0])
+            d2 = (mc2.get(0.0) if (mc2 is not None and not tdf) else None)
+            b.add_stream(s, not tdf, d1, d2)
+        self._feed_streams(0)
+        b.forcing_init()
+        self._feed_streams(0)
+        ic = case['ic']
+        b.initial_conditions(ic.get('eta'), ic.get('u'), ic.get('v'))
+        for t in case.get('tracers', []):
+            b.add_tracer(t)
+        if case.get('tracers'):
+            b.tracer_init()
+        if with_diag:
+            self.tasks = [DiagTask(s, c['Nt'], c['diag_start_ind'], c['dt'], c['meant_out'])
+                          for s in case['diag']]
+            self.diag()
+
+    def _feed_streams(self, itt):
+        t = itt * self.cfg['dt']
+        for sid, (mc1, mc2, tdf) in enumerate(self.chunks):
+            if tdf:
+                self.b.set_stream_data(sid, mc1.get(t), mc2.get(t) if mc2 is not None else None)
+
+    def fetch(self, name):
+        if name == 'PSI':
+            if self._psi_cache is None:
+                self._psi_cache = self.b.streamfunction()
+            return self._psi_cache
+        return self.b.field(DIAG_VARS[name][0])
+
+    def diag(self):
+        if self.itt < self.cfg['diag_start_ind']:
+            return
+        self._psi_cache = None
+        for t in self.tasks:
+            t.process(self.itt, self.fetch)
+
+    # -- time loop: model.f90 timestepModel :153-197 ---------------------
+    def run(self, nsteps=None, with_diag=True):
+        n = self.cfg['Nt'] if nsteps is None else nsteps
+        for _ in range(n):
+            self.itt += 1
+            self.b.step(self.itt)
+            self._feed_streams(self.itt)
+            self.b.advance(self.itt)
+            if with_diag:
+                self.diag()
+
+    def outputs(self):
+        out = {}
+        for t in self.tasks:
+            out[t.spec['filename']] = (np.array(t.times), np.array(t.records) if t.records else None,
+                                       DIAG_VARS[t.name][1])
+        return out

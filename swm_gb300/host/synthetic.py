@@ -1,0 +1,136 @@
+"""Seeded synthetic workloads on the reference's spherical grid.
+
+The workloads are stated in Cartesian terms (cells, dx in metres, beta-plane
+f0/beta).  The reference has no Cartesian mode, so they are mapped onto its
+lon/lat grid with a radius 1000x Earth's: spans are then a few 1e-3 rad,
+cos(lat) = 1 - O(1e-6) and tan(lat)/A ~ 0, i.e. Cartesian to ~1e-6, and the
+beta-plane is coriolis_approx = 2 with 2*OMEGA*sin(theta0) = f0 and
+2*OMEGA*cos(theta0)/A = beta.  H arrays carry the land of a closed basin
+(the reference zeroes the first/last row itself; east/west come from H).
+
+Seeds: numpy PCG64(20260 + workload index) (+ member * 7919 for ensemble
+members), drawn in FP64 on the host.
+"""
+import math
+import numpy as np
+
+from .case import MODE_NONLINEAR, MODE_LIN_REST
+
+A_BIG = 6.371e9
+D2R = float(np.float32(3.14159265358979323846)) / 180.0
+DAY = 86400.0
+
+
+def _base_config(cells_x, cells_y, dx, f0, beta, dt):
+    span_x = cells_x * dx / A_BIG / D2R
+    span_y = cells_y * dx / A_BIG / D2R
+    two_omega = math.hypot(f0, beta * A_BIG)
+    theta0 = math.degrees(math.atan2(f0, beta * A_BIG)) if two_omega > 0 else 0.0
+    return dict(nx=cells_x + 1, ny=cells_y + 1, mode=MODE_NONLINEAR, lateral_mixing=1, quadratic_friction=0,
+                barotropic=0, mixing_kind=0, coriolis_approx=2, tracer_nan_guard=0, damping_additive=0,
+                mask_psi_bs=0, dt=dt, G=9.81, Ah=0.0, A=A_BIG, OMEGA=two_omega / 2.0, RHO0=1024.0, lbc=2.0,
+                theta0=theta0, lon_s=-span_x / 2, lon_e=span_x / 2, lat_s=-span_y / 2, lat_e=span_y / 2,
+                H_overwrite=0.0, ab_chi=0.1, minD=1.0, tau_scale=1.0, bih=0.0, diag_start_ind=0,
+                meant_out=2.628e6, tracer=0)
+
+
+def perturbed_basin(nx, ny, depth, rng, max_inset=3):
+    """H (ny, nx): depth inside a closed basin whose boundary cells are moved
+    inwards by 0..max_inset cells, independently per boundary cell."""
+    H = np.full((ny, nx), float(depth))
+    H[:, 0] = 0.0
+    H[:, -1] = 0.0
+    H[0, :] = 0.0
+    H[-1, :] = 0.0
+    inset = rng.integers(0, max_inset + 1, size=(4, max(nx, ny)))
+    for j in range(ny):
+        H[j, :1 + inset[0, j]] = 0.0
+        H[j, nx - 1 - inset[1, j]:] = 0.0
+    for i in range(nx):
+        H[:1 + inset[2, i], i] = 0.0
+        H[ny - 1 - inset[3, i]:, i] = 0.0
+    return H
+
+
+def _wind_stream(cfg, amp, ny):
+    """tau_x = amp * cos(2*pi*y/L) on the u grid rows, constant in time."""
+    lat_u = np.array([j * (cfg['lat_e'] - cfg['lat_s']) / (ny - 1) + cfg['lat_s'] for j in range(ny)]) + \
+        (cfg['lat_e'] - cfg['lat_s']) / (2.0 * (ny - 1))
+    y = (lat_u - cfg['lat_s']) / (cfg['lat_e'] - cfg['lat_s'])
+    prof = amp * np.cos(2.0 * math.pi * y)
+    rec = np.repeat(prof[:, None], cfg['nx'], axis=1)[None]
+    return dict(type=0, comp=0, omega=0.0, rec1=rec, dt1=0.0, chunksize=100, rec2=None, dt2=0.0)
+
+
+def empty_case(cfg):
+    return {'config': cfg, 'H': None, 'H_missing': None, 'psi_bs': None, 'damping': [], 'streams': [],
+            'ic': {}, 'tracers': [], 'diag': []}
+
+
+def linear_rg(cells_x=256, cells_y=128, seed_index=0, nsteps=10000):
+    """Plain linear reduced-gravity SWM: beta-plane (f = beta*y), g' = 0.02,
+    H = 200 m, Ah = 1000, Rayleigh 1/(100 d), closed box, Gaussian eta bump
+    (0.1 m, 300 km e-folding) at a seed-drawn interior point, AB3 dt = 1800 s."""
+    rng = np.random.Generator(np.random.PCG64(20260 + seed_index))
+    dx = 25e3
+    cfg = _base_config(cells_x, cells_y, dx, 0.0, 2.3e-11, 1800.0)
+    cfg.update(mode=MODE_LIN_REST, G=0.02, Ah=1000.0, H_overwrite=200.0, Nt=nsteps)
+    case = empty_case(cfg)
+    nx, ny = cfg['nx'], cfg['ny']
+    H = np.ones((ny, nx))
+    H[:, 0] = H[:, -1] = 0.0
+    case['H'] = H
+    g = 1.0 / (100.0 * DAY)
+    case['damping'] = [dict(term=0, type=0, value=g, sl_length=1.0, sl_cutoff=15.0, loc=0, file_data=None),
+                       dict(term=1, type=0, value=g, sl_length=1.0, sl_cutoff=15.0, loc=0, file_data=None)]
+    cx, cy = rng.uniform(0.25, 0.75) * cells_x * dx, rng.uniform(0.25, 0.75) * cells_y * dx
+    x = (np.arange(nx) + 0.5) * dx
+    y = (np.arange(ny) + 0.5) * dx
+    r2 = (x[None, :] - cx) ** 2 + (y[:, None] - cy) ** 2
+    case['ic'] = {'eta': 0.1 * np.exp(-r2 / (300e3) ** 2)}
+    return case
+
+
+def double_gyre(cells=1024, seed_index=1, nsteps=20000, biharmonic=True, dx=5e3, amp=0.1, ah=None,
+                rng=None, dt=15.0):
+    """Nonlinear single-layer wind-driven double gyre: beta-plane f0 = 1e-4,
+    beta = 2e-11, H = 500 m, g = 9.81, tau = amp*cos(2 pi y/L), bottom drag
+    1e-7 /s (linear, not divided by H), biharmonic 1e10 m^4/s (extension) or
+    Laplacian Ah (reference), perturbed closed coastline, rest, AB3.
+
+    dt defaults to 15 s: at dx = 5 km and H = 500 m the 2-dx gravity wave has
+    omega*dt = 2*sqrt(2)*sqrt(gH)*dt/dx = 0.79 for dt = 20 s, outside AB3's
+    stability interval on the imaginary axis (|omega*dt| <= 0.72); the run
+    blows up after a few hundred steps."""
+    if rng is None:
+        rng = np.random.Generator(np.random.PCG64(20260 + seed_index))
+    cells_x, cells_y = (cells, cells) if np.isscalar(cells) else cells
+    cfg = _base_config(cells_x, cells_y, dx, 1e-4, 2e-11, dt)
+    cfg.update(mode=MODE_NONLINEAR, G=9.81, Nt=nsteps)
+    if biharmonic:
+        cfg.update(mixing_kind=1, bih=1e10, Ah=0.0)
+    else:
+        cfg.update(mixing_kind=0, Ah=500.0 if ah is None else ah)
+    case = empty_case(cfg)
+    case['H'] = perturbed_basin(cfg['nx'], cfg['ny'], 500.0, rng)
+    r = 1e-7
+    case['damping'] = [dict(term=0, type=0, value=r, sl_length=1.0, sl_cutoff=15.0, loc=0, file_data=None),
+                       dict(term=1, type=0, value=r, sl_length=1.0, sl_cutoff=15.0, loc=0, file_data=None)]
+    case['streams'] = [_wind_stream(cfg, amp, cfg['ny'])]
+    return case
+
+
+def ensemble_members(n=256, seed_index=4, nsteps=10000):
+    """Ensemble of wind-driven basins of uneven sizes: Nx, Ny log-uniform in
+    [64, 512], dx uniform 5-20 km, wind amplitude uniform 0.05-0.2 N/m^2,
+    perturbed coastline, Laplacian Ah = 500."""
+    out = []
+    for m in range(n):
+        rng = np.random.Generator(np.random.PCG64(20260 + seed_index + m * 7919))
+        cx = int(round(math.exp(rng.uniform(math.log(64), math.log(512)))))
+        cy = int(round(math.exp(rng.uniform(math.log(64), math.log(512)))))
+        dx = rng.uniform(5e3, 20e3)
+        amp = rng.uniform(0.05, 0.2)
+        dt = 15.0 * dx / 5e3
+        out.append(double_gyre((cx, cy), biharmonic=False, dx=dx, amp=amp, ah=500.0, rng=rng, nsteps=nsteps, dt=dt))
+    return out

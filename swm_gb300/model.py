@@ -1,0 +1,177 @@
+"""Python view of one GPU model instance (the Fortran module entry points of
+swm_module / swm_timestep_module / tracer_module / ElSolv_SOR, bound through
+the C ABI).  Also the GPU backend of ``host.driver.Driver``.
+"""
+import ctypes as C
+import numpy as np
+
+from ._lib import lib, check, Config, CONFIG_INT, CONFIG_DBL, FIELD_ID, PATHS
+
+TRC_FIELD = {'CH': 0, 'C': 1, 'G': 2, 'uhc': 3, 'vhc': 4, 'diff': 5, 'impl': 6}
+
+
+def _p(a):
+    return None if a is None else a.ctypes.data_as(C.c_void_p)
+
+
+def _f64(a):
+    return None if a is None else np.ascontiguousarray(a, dtype=np.float64)
+
+
+class GpuModel:
+    """One SWM model on the GPU.  ``path`` selects plain_fp64 (drop-in),
+    fused_fp64 or fused_fp32c."""
+
+    def __init__(self, path='plain_fp64', tracer_nan_guard=False):
+        self.L = lib()
+        self.path = PATHS[path] if isinstance(path, str) else int(path)
+        self.ctx = None
+        self.nan_guard = tracer_nan_guard
+
+    def close(self):
+        if self.ctx:
+            self.L.swm_gpu_destroy(self.ctx)
+            self.ctx = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    # -- init sequence -------------------------------------------------
+    def setup_domain(self, case):
+        cfg = case['config']
+        c = Config()
+        for n in CONFIG_INT:
+            setattr(c, n, int(cfg.get(n, 0)))
+        for n in CONFIG_DBL:
+            setattr(c, n, float(cfg.get(n, 0.0)))
+        if self.nan_guard:
+            c.tracer_nan_guard = 1
+        c.path = self.path
+        self._cfg = c
+        self.nx, self.ny = cfg['nx'], cfg['ny']
+        ctx = C.c_void_p()
+        check(self.L.swm_gpu_create(C.byref(c), C.byref(ctx)))
+        self.ctx = ctx
+        H = _f64(case.get('H'))
+        miss = None if case.get('H_missing') is None else np.ascontiguousarray(case['H_missing'], np.int8)
+        check(self.L.swm_gpu_domain(self.ctx, _p(H), _p(miss)))
+
+    def timestep_init(self, psi_bs):
+        p = _f64(psi_bs)
+        check(self.L.swm_gpu_timestep_init(self.ctx, _p(p)))
+
+    def add_damping(self, d):
+        fd = _f64(d['file_data'])
+        check(self.L.swm_gpu_add_damping(self.ctx, d['term'], d['type'], d['value'], d['sl_length'],
+                                         d['sl_cutoff'], d['loc'], _p(fd)))
+
+    def finish_damping(self):
+        check(self.L.swm_gpu_finish_damping(self.ctx))
+
+    def add_stream(self, s, is_const, d1, d2):
+        a, b = _f64(d1), _f64(d2)
+        sid = C.c_int()
+        check(self.L.swm_gpu_add_stream(self.ctx, s['type'], s['comp'], s['omega'], int(is_const),
+                                        _p(a), _p(b), C.byref(sid)))
+        return sid.value
+
+    def set_stream_data(self, sid, d1, d2):
+        a, b = _f64(d1), _f64(d2)
+        check(self.L.swm_gpu_set_stream_data(self.ctx, sid, _p(a), _p(b)))
+
+    def set_stream_rows(self, sid, r1, r2=None):
+        a, b = _f64(r1), _f64(r2)
+        check(self.L.swm_gpu_set_stream_rows(self.ctx, sid, _p(a), _p(b)))
+
+    def integrals(self):
+        out = np.zeros(3)
+        check(self.L.swm_gpu_integrals(self.ctx, _p(out)))
+        return out
+
+    def forcing_init(self):
+        check(self.L.swm_gpu_forcing_init(self.ctx))
+
+    def initial_conditions(self, eta, u, v):
+        e, uu, vv = _f64(eta), _f64(u), _f64(v)
+        check(self.L.swm_gpu_initial_conditions(self.ctx, _p(e), _p(uu), _p(vv)))
+
+    def add_tracer(self, t):
+        arrs = [_f64(t.get('field_C')), _f64(t.get('field_C0')), _f64(t.get('field_gamma_C')),
+                _f64(t.get('field_cons'))]
+        tid = C.c_int()
+        check(self.L.trc_gpu_add(self.ctx, t['kappa_h'], t['cons'], t['gamma_c'], *[_p(a) for a in arrs],
+                                 C.byref(tid)))
+        return tid.value
+
+    def tracer_init(self):
+        check(self.L.trc_gpu_init(self.ctx))
+
+    # -- time loop -----------------------------------------------------
+    def step(self, itt):
+        check(self.L.swm_gpu_step(self.ctx, itt))
+
+    def advance(self, itt):
+        check(self.L.swm_gpu_advance(self.ctx, itt))
+
+    def run(self, itt0, nsteps):
+        check(self.L.swm_gpu_run(self.ctx, itt0, nsteps))
+
+    def synchronize(self):
+        check(self.L.swm_gpu_synchronize(self.ctx))
+
+    def launch_count(self):
+        return self.L.swm_gpu_launch_count(self.ctx)
+
+    def stream(self):
+        return self.L.swm_gpu_stream(self.ctx)
+
+    # -- host access ---------------------------------------------------
+    _ALIAS = {'tot_u': 'u', 'tot_v': 'v', 'tot_eta': 'eta'}
+
+    def field(self, name):
+        name = self._ALIAS.get(name, name)
+        out = np.empty((self.ny, self.nx))
+        check(self.L.swm_gpu_get_field(self.ctx, FIELD_ID[name], _p(out)))
+        return out
+
+    def set_field(self, name, arr):
+        a = _f64(arr)
+        check(self.L.swm_gpu_set_field(self.ctx, FIELD_ID[self._ALIAS.get(name, name)], _p(a)))
+
+    def lat(self, name):
+        which, grid = name.split('_')
+        out = np.empty(self.ny)
+        check(self.L.swm_gpu_get_metric(self.ctx, ['lat', 'cos', 'tan', 'f'].index(which),
+                                        ['H', 'u', 'v', 'eta'].index(grid), _p(out)))
+        return out
+
+    def ocean(self, grid):
+        out = np.empty((self.ny, self.nx), dtype=np.int8)
+        check(self.L.swm_gpu_get_mask(self.ctx, ['H', 'u', 'v', 'eta'].index(grid), _p(out)))
+        return out
+
+    def streamfunction(self):
+        out = np.empty((self.ny, self.nx))
+        check(self.L.swm_gpu_streamfunction(self.ctx, _p(out)))
+        return out
+
+    def tracer_field(self, t, name):
+        out = np.empty((self.ny, self.nx))
+        check(self.L.trc_gpu_get_field(self.ctx, t, TRC_FIELD[name], _p(out)))
+        return out
+
+    # -- SOR -----------------------------------------------------------
+    def sor_init(self):
+        check(self.L.elsolv_sor_gpu_init(self.ctx))
+
+    def sor_solve(self, B, chi, eps, first_guess):
+        b = _f64(B)
+        x = np.ascontiguousarray(chi, np.float64).copy()
+        it, an = C.c_int(), C.c_double()
+        rc = self.L.elsolv_sor_gpu_solve(self.ctx, _p(b), _p(x), eps, int(first_guess), C.byref(it), C.byref(an))
+        if rc not in (0, 4):
+            check(rc)
+        return x, (it.value if rc == 0 else -it.value), an.value
