@@ -85,13 +85,16 @@ swm::Dev swm_gpu_ctx::dev() const {
   return d;
 }
 
+// allocations are zeroed on the context's stream, so that later kernels on
+// that (non-blocking) stream are ordered after the zeroing
+static cudaStream_t g_alloc_stream = nullptr;
 static int dalloc(double **p, size_t n) {
   cudaError_t e = cudaMalloc((void **)p, n * sizeof(double));
   if (e != cudaSuccess) {
     set_error(std::string("cudaMalloc: ") + cudaGetErrorString(e));
     return SWM_GPU_ENOMEM;
   }
-  e = cudaMemset(*p, 0, n * sizeof(double));
+  e = cudaMemsetAsync(*p, 0, n * sizeof(double), g_alloc_stream);
   if (e != cudaSuccess) {
     set_error(std::string("cudaMemset: ") + cudaGetErrorString(e));
     return SWM_GPU_ECUDA;
@@ -189,6 +192,7 @@ int64_t swm_gpu_launch_count(swm_gpu_ctx *c) { return c ? c->launches : -1; }
 int swm_gpu_domain(swm_gpu_ctx *c, const double *H, const int8_t *Hmiss) {
   SWM_REQUIRE(c && c->stage == 0, "swm_gpu_domain: call once, first");
   TRY(host_domain(c, H, Hmiss));
+  g_alloc_stream = c->stream;
   size_t n = c->n;
   int ny = c->ny;
   const HostGrid &g = c->hg;
@@ -289,6 +293,7 @@ int swm_gpu_add_stream(swm_gpu_ctx *c, int type, int comp, double omega, int is_
   if (type == SWM_FRC_OSC) s.is_const = 0;
   else if (type == SWM_FRC_WIND && c->cfg.mode == SWM_MODE_NONLINEAR) s.is_const = 0;
   else s.is_const = is_const ? 1 : 0;
+  g_alloc_stream = c->stream;
   TRY(dalloc(&s.d1, c->n));
   TRY(dalloc(&s.d2, c->n));
   if (d1) TRY(h2d(c, s.d1, d1, c->n));

