@@ -202,7 +202,7 @@ def ours(args, rank, ws):
     line['roofline'] = {'bound': 'hbm', 'achieved': achieved, 'peak': peak, 'unit': 'GB/s',
                         'frac': achieved / peak, 'traffic': traffic, 'peak_kind': kind,
                         'algorithmic_bytes_per_launch': alg,
-                        'kernel': 'k_fused<float,2,true>' if args.path == 'fused_fp32c' else args.path}
+                        'kernel': 'k_march<2,16>' if args.path == 'fused_fp32c' else args.path}
     # steady state without L2 flush (back-to-back steps)
     ms_nf = timed_steps(g, itt, 200, None, stream)
     itt += 200

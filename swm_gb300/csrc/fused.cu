@@ -323,6 +323,8 @@ __global__ void k_to_f32(const double *src, float *dst, size_t n) {
   if (k < n) dst[k] = (float)src[k];
 }
 
+struct P32;
+std::vector<double> fp32c_rows(const swm_gpu_ctx *c);
 }  // namespace swm
 
 using namespace swm;
@@ -337,6 +339,10 @@ struct FusedState {
   uint8_t *mc = nullptr;
   void *He = nullptr, *rows = nullptr, *Hu = nullptr, *Hv = nullptr;
   void *impl[3] = {}, *gsq[2] = {}, *F[3] = {}, *wx = nullptr, *wy = nullptr;
+  void *rows32c = nullptr;
+  uint16_t *mask16 = nullptr;
+  void *dp[3] = {};
+  double dp_s[3] = {0, 0, 0};
   bool impl_uniform = true, gsq_uniform = true, has_F = false, wind_rows = false;
   int wind_x = 0, wind_y = 0;
   double impl_s[3] = {1, 1, 1}, gsq_s[2] = {0, 0};
@@ -480,6 +486,27 @@ int fused_prepare(swm_gpu_ctx *c) {
   if (f->has_F)
     for (int q = 0; q < 3; q++) FTRY(upload_t(c, f32, Fh[q].data(), n, &f->F[q]));
   if (f32) {
+    std::vector<double> r32 = fp32c_rows(c);
+    FTRY(upload_t(c, true, r32.data(), r32.size(), &f->rows32c));
+    // mask word with the x-neighbours' bits (bits 4-7: i-1, 8-11: i+1)
+    std::vector<uint16_t> m16(n);
+    int nx = c->nx;
+    for (int j = 0; j < ny; j++)
+      for (int i = 0; i < nx; i++) {
+        size_t k = i + (size_t)nx * j;
+        size_t kl = (i == 0 ? nx - 1 : i - 1) + (size_t)nx * j, kr = (i + 1 == nx ? 0 : i + 1) + (size_t)nx * j;
+        m16[k] = (uint16_t)(mc[k] | (mc[kl] << 4) | (mc[kr] << 8));
+      }
+    FTRY(dmalloc((void **)&f->mask16, n * 2));
+    SWM_CK(cudaMemcpy(f->mask16, m16.data(), n * 2, cudaMemcpyHostToDevice));
+    // implicit damping as the removed fraction dt*gamma/(1 + dt*gamma)
+    for (int q = 0; q < 3; q++) f->dp_s[q] = (f->impl_s[q] - 1.) / f->impl_s[q];
+    if (!f->impl_uniform)
+      for (int q = 0; q < 3; q++) {
+        std::vector<double> dpq(n);
+        for (size_t k = 0; k < n; k++) dpq[k] = (g.impl[q][k] - 1.) / g.impl[q][k];
+        FTRY(upload_t(c, true, dpq.data(), n, &f->dp[q]));
+      }
     for (int q = 0; q < 2; q++) {
       FTRY(dmalloc((void **)&f->uh[q], n * 4)); FTRY(dmalloc((void **)&f->ul[q], n * 4));
       FTRY(dmalloc((void **)&f->vh[q], n * 4)); FTRY(dmalloc((void **)&f->vl[q], n * 4));
@@ -592,6 +619,70 @@ static void launch_fused(swm_gpu_ctx *c, const FP<T> &p) {
   c->launches++;
 }
 
+}  // namespace swm
+#include "fused32.h"
+namespace swm {
+
+static void launch_fp32c(swm_gpu_ctx *c, int64_t itt) {
+  const swm_gpu_config &cf = c->cfg;
+  FusedState *f = c->fused;
+  P32 p;
+  memset(&p, 0, sizeof(p));
+  p.nx = c->nx;
+  p.ny = c->ny;
+  p.nl = cf.mode == SWM_MODE_NONLINEAR;
+  p.has_mode = cf.mode != SWM_MODE_NONE;
+  p.mix = cf.lateral_mixing ? (cf.mixing_kind == SWM_MIX_BIHARMONIC ? 2 : 1) : 0;
+  p.qbf = cf.quadratic_friction;
+  p.barotropic = cf.barotropic;
+  p.has_F = f->has_F;
+  p.impl_uniform = f->impl_uniform;
+  p.gsq_uniform = f->gsq_uniform;
+  p.wind_x = f->wind_x;
+  p.wind_y = f->wind_y;
+  p.wind_rows = f->wind_rows;
+  int tstep = (int)(itt < 3 ? itt : 3);
+  double chi = cf.ab_chi;
+  double tab[4][3] = {{0, 0, 0}, {1., 0, 0}, {-0.5 - chi, 1.5 + chi, 0}, {5. / 12., -16. / 12., 23. / 12.}};
+  p.ab0 = (float)tab[tstep][0];
+  p.ab1 = (float)tab[tstep][1];
+  p.ab2 = (float)tab[tstep][2];
+  p.dt = (float)cf.dt;
+  p.G = (float)cf.G;
+  p.minD = (float)cf.minD;
+  p.lbc = (float)cf.lbc;
+  p.q1 = (float)(1. / (cf.A * c->hg.dTheta));
+  p.ts_rho = (float)(cf.tau_scale / cf.RHO0);
+  p.Ah = (float)cf.Ah;
+  p.bih = (float)cf.bih;
+  for (int q = 0; q < 3; q++) {
+    p.impl_s[q] = (float)f->impl_s[q];
+    p.dp_s[q] = (float)f->dp_s[q];
+    p.dp[q] = (const float *)f->dp[q];
+  }
+  for (int q = 0; q < 2; q++) p.gsq_s[q] = (float)f->gsq_s[q];
+  p.mask16 = f->mask16;
+  p.He = (const float *)f->He;
+  p.rows = (const float *)f->rows32c;
+  p.Hu = (const float *)f->Hu;
+  p.Hv = (const float *)f->Hv;
+  for (int q = 0; q < 3; q++) p.impl[q] = (const float *)f->impl[q];
+  for (int q = 0; q < 2; q++) p.gsq[q] = (const float *)f->gsq[q];
+  p.Fx = (const float *)f->F[0];
+  p.Fy = (const float *)f->F[1];
+  p.Fe = (const float *)f->F[2];
+  p.wx = (const float *)f->wx;
+  p.wy = (const float *)f->wy;
+  int a = f->n0, b = 1 - f->n0;
+  p.uh0 = f->uh[a]; p.ul0 = f->ul[a]; p.vh0 = f->vh[a]; p.vl0 = f->vl[a]; p.eh0 = f->eh[a]; p.el0 = f->el[a];
+  p.uh1 = f->uh[b]; p.ul1 = f->ul[b]; p.vh1 = f->vh[b]; p.vl1 = f->vl[b]; p.eh1 = f->eh[b]; p.el1 = f->el[b];
+  int s0 = f->g0, s1 = (f->g0 + 1) % 3, s2 = (f->g0 + 2) % 3;
+  p.Gu1 = f->Gu[s0]; p.Gu2 = f->Gu[s1]; p.Gu3 = f->Gu[s2];
+  p.Gv1 = f->Gv[s0]; p.Gv2 = f->Gv[s1]; p.Gv3 = f->Gv[s2];
+  p.Ge1 = f->Ge[s0]; p.Ge2 = f->Ge[s1]; p.Ge3 = f->Ge[s2];
+  march_launch(c, p);
+}
+
 int fused_step(swm_gpu_ctx *c, int64_t itt) {
   FTRY(fused_prepare(c));
   FusedState *f = c->fused;
@@ -607,21 +698,9 @@ int fused_step(swm_gpu_ctx *c, int64_t itt) {
     p.Ge1 = d.Ge[0]; p.Ge2 = d.Ge[1]; p.Ge3 = d.Ge[2];
     launch_fused<double, false>(c, p);
   } else {
-    FP<float> p;
-    memset(&p, 0, sizeof(p));
-    fill_common(c, p, itt);
-    int a = f->n0, b = 1 - f->n0;
-    p.u0 = f->uh[a]; p.v0 = f->vh[a]; p.e0 = f->eh[a];
-    p.ul0 = f->ul[a]; p.vl0 = f->vl[a]; p.el0 = f->el[a];
-    p.u1 = f->uh[b]; p.v1 = f->vh[b]; p.e1 = f->eh[b];
-    p.ul1 = f->ul[b]; p.vl1 = f->vl[b]; p.el1 = f->el[b];
-    int s0 = f->g0, s1 = (f->g0 + 1) % 3, s2 = (f->g0 + 2) % 3;
-    p.Gu1 = f->Gu[s0]; p.Gu2 = f->Gu[s1]; p.Gu3 = f->Gu[s2];
-    p.Gv1 = f->Gv[s0]; p.Gv2 = f->Gv[s1]; p.Gv3 = f->Gv[s2];
-    p.Ge1 = f->Ge[s0]; p.Ge2 = f->Ge[s1]; p.Ge3 = f->Ge[s2];
-    launch_fused<float, true>(c, p);
-    // advance of the pair state happens here: the host-side advance only
-    // rotates the FP64 indices
+    launch_fp32c(c, itt);
+    // the pair state advances here; the host-side advance only rotates the
+    // FP64 level and ring indices
     f->n0 = 1 - f->n0;
     f->g0 = (f->g0 + 1) % 3;
   }
@@ -636,7 +715,8 @@ void fused_free(swm_gpu_ctx *c) {
   for (int q = 0; q < 2; q++) { F(f->uh[q]); F(f->ul[q]); F(f->vh[q]); F(f->vl[q]); F(f->eh[q]); F(f->el[q]); }
   for (int q = 0; q < 3; q++) { F(f->Gu[q]); F(f->Gv[q]); F(f->Ge[q]); F(f->impl[q]); F(f->F[q]); }
   for (int q = 0; q < 2; q++) F(f->gsq[q]);
-  F(f->mc); F(f->He); F(f->rows); F(f->Hu); F(f->Hv); F(f->wx); F(f->wy);
+  F(f->mc); F(f->He); F(f->rows); F(f->Hu); F(f->Hv); F(f->wx); F(f->wy); F(f->rows32c); F(f->mask16);
+  for (int q = 0; q < 3; q++) F(f->dp[q]);
   delete f;
   c->fused = nullptr;
 }

@@ -1,0 +1,446 @@
+// march.cu -- FP32 fused SWM step, register-resident row marching.
+//
+// Each warp owns a strip of 32 columns (lane = column) and S output rows.  It
+// walks up the strip one row per iteration, keeping the last rows of every
+// intermediate field in registers; x-neighbours come from warp shuffles, so
+// the kernel uses no shared memory and no block barrier.  When row J has
+// been loaded, the stress tensor and fluxes needed by row J-2 are complete
+// and row J-2 is updated (the biharmonic operator needs two rows of
+// look-ahead).  The outer HALO lanes of a strip are recomputed by the
+// neighbouring strip, so a strip updates 32 - 2*HALO columns.
+//
+// Precision: tendencies in binary32; first differences of prognostic fields
+// from the (hi, lo) pairs; mass fluxes split into an exact static-depth
+// product and the small free-surface product; compensated Adams-Bashforth
+// update with the implicit damping applied as x - x*dt*gamma/(1+dt*gamma), so
+// the small damping rate keeps its binary32 relative precision (1 + dt*gamma
+// itself would lose it).
+//
+// Formulas: swm_nonlinear_timestep_module.f90:182-449 (diagnostics and
+// tendencies), swm_lateralmixing_module.f90:66-240 (stress tensor),
+// time_integration_module.f90:74-112 (Adams-Bashforth).
+#include <cmath>
+#include <cstdlib>
+#include <type_traits>
+#include <vector>
+#include "fused32.h"
+
+namespace swm {
+
+constexpr unsigned FULL = 0xffffffffu;
+__device__ __forceinline__ float shl(float x) { return __shfl_up_sync(FULL, x, 1); }    // lane - 1
+__device__ __forceinline__ float shr(float x) { return __shfl_down_sync(FULL, x, 1); }  // lane + 1
+
+__device__ __forceinline__ int wrapm(int g, int n) {
+  g = g < 0 ? g + n : g;
+  return g >= n ? g - n : g;
+}
+__device__ __forceinline__ float rcnt(int c) { return c <= 1 ? 1.f : (c == 2 ? 0.5f : (c == 3 ? 0.33333334f : 0.25f)); }
+
+// mask word: bits 0-3 own (H, u, v, eta), 4-7 column i-1, 8-11 column i+1
+#define MH(m) ((m) & 1)
+#define MU_(m) (((m) >> 1) & 1)
+#define MV_(m) (((m) >> 2) & 1)
+#define ME(m) (((m) >> 3) & 1)
+#define LV(m) (((m) >> 6) & 1)
+#define LE(m) (((m) >> 7) & 1)
+
+// (hi + lo + inc) * (1 - dp) as a new (hi, lo) pair
+__device__ __forceinline__ void comp_damp(float hi, float lo, float inc, float dp, float &nh, float &nl) {
+  float s = hi + inc;
+  float bb = s - hi;
+  float e = (hi - (s - bb)) + (inc - bb) + lo;
+  float c = s * dp;
+  float t = s - c;
+  float bt = t - s;
+  float e2 = (s - (t - bt)) + (-c - bt);
+  e = e + e2 - e * dp;
+  nh = t + e;
+  nl = e - (nh - t);
+}
+
+template <int MIX, int S>
+__global__ void __launch_bounds__(128) k_march(P32 p) {
+  constexpr int H = MIX == 2 ? 2 : 1;
+  constexpr int TI = 32 - 2 * H;
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  const int nx = p.nx, ny = p.ny;
+  const int ry0 = (blockIdx.y * 4 + warp) * S;
+  if (ry0 >= ny) return;  // whole warp leaves together
+  const int gx = blockIdx.x * TI - H + lane;
+  const int gi = wrapm(gx, nx);
+  const bool nl = p.nl;
+  const bool store_lane = lane >= H && lane < 32 - H && gx < nx;
+  const float q1 = p.q1, G = p.G;
+
+  // sliding windows, index a = row J - a
+  float uh[4] = {}, ul[4] = {}, vh[4] = {}, vl[4] = {}, eh[4] = {}, el[4] = {}, he[4] = {};
+  unsigned m[4] = {};
+  float pll1[2] = {}, plt1[2] = {}, lu1[2] = {}, lv1[2] = {}, pll2[2] = {}, plt2[2] = {};
+  float muh[4] = {}, mul[4] = {}, mvh[3] = {}, mvl[3] = {}, pot[3] = {}, ke[3] = {};
+  int off[3] = {};            // row offsets nx * j of rows J, J-1, J-2
+  const float *rr[3] = {};    // per-row factors of rows J, J-1, J-2
+
+  int J = ry0 - 3;
+  const int jend = min(ry0 + S, ny) + 2;
+  int noff = nx * wrapm(J, ny);
+  const float *nrow = p.rows + (size_t)wrapm(J, ny) * Q_NR;
+  unsigned n_m = p.mask16[gi + noff];
+  float n_uh = p.uh0[gi + noff], n_ul = p.ul0[gi + noff], n_vh = p.vh0[gi + noff], n_vl = p.vl0[gi + noff];
+  float n_eh = p.eh0[gi + noff], n_el = p.el0[gi + noff], n_he = p.He[gi + noff];
+
+  // one iteration; FAST: every cell of the warp's 4-row window is ocean on
+  // all four grids, so every mask test is compile-time true
+  auto body = [&](auto fast_tag) {
+    constexpr bool FAST = decltype(fast_tag)::value;
+#define XH(m_) (FAST ? 1u : MH(m_))
+#define XU(m_) (FAST ? 1u : MU_(m_))
+#define XV(m_) (FAST ? 1u : MV_(m_))
+#define XE(m_) (FAST ? 1u : ME(m_))
+#define XLV(m_) (FAST ? 1u : LV(m_))
+#define XLE(m_) (FAST ? 1u : LE(m_))
+#define W2(a_, b_) (FAST ? 0.5f : rcnt((a_) + (b_)))
+#define W4(a_, b_, c_, d_) (FAST ? 0.25f : rcnt((a_) + (b_) + (c_) + (d_)))
+#define HALF2(a_, b_) (FAST ? 0.5f : ((a_) + (b_) > 1 ? 0.5f : 1.f))
+    auto dval = [&](int a) { return nl ? (XE(m[a]) ? he[a] + eh[a] : 1.f) : he[a]; };
+    const float *r0 = rr[0], *r1 = rr[1], *r2 = rr[2];
+    const int o = J - 2;
+    const bool upd = o >= ry0 && o < ry0 + S && o < ny && store_lane;
+    const int ko = gi + off[2];
+    float g1e = 0, g2e = 0, g1u = 0, g2u = 0, g1v = 0, g2v = 0;
+    if (upd) {
+      g1e = p.Ge1[ko]; g2e = p.Ge2[ko]; g1u = p.Gu1[ko]; g2u = p.Gu2[ko]; g1v = p.Gv1[ko]; g2v = p.Gv2[ko];
+    }
+
+    // ---- row J: mass fluxes and PV; row J-1: kinetic energy ----------
+    const float d0 = dval(0), d1 = dval(1), d2 = dval(2), d3 = dval(3);
+    const float he_l = shl(he[0]), eh_l = shl(eh[0]);
+    const float dl0 = shl(d0), dl1 = shl(d1), dl2 = shl(d2);
+    const float vh0_l = shl(vh[0]), vl0_l = shl(vl[0]);
+    const float uh1_r = shr(uh[1]), ul1_r = shr(ul[1]);
+    {
+      const unsigned mm = m[0];
+      float a_h = 0.f, a_l = 0.f;
+      if (XU(mm)) {
+        unsigned a = XE(mm), b = XLE(mm);
+        float w = W2(a, b);
+        float hs = ((a ? he[0] : 0.f) + (b ? he_l : 0.f)) * w;
+        float es = nl ? ((a ? eh[0] : 0.f) + (b ? eh_l : 0.f)) * w : 0.f;
+        a_h = hs * uh[0];
+        a_l = fmaf(hs, uh[0], -a_h) + fmaf(hs, ul[0], es * uh[0]);
+      }
+      muh[0] = a_h; mul[0] = a_l;
+      float b_h = 0.f, b_l = 0.f;
+      if (XV(mm)) {
+        unsigned a = XE(mm), b = XE(m[1]);
+        float w = W2(a, b);
+        float hs = ((a ? he[0] : 0.f) + (b ? he[1] : 0.f)) * w;
+        float es = nl ? ((a ? eh[0] : 0.f) + (b ? eh[1] : 0.f)) * w : 0.f;
+        b_h = hs * vh[0];
+        b_l = fmaf(hs, vh[0], -b_h) + fmaf(hs, vl[0], es * vh[0]);
+      }
+      mvh[0] = b_h; mvl[0] = b_l;
+      float pv = 0.f;
+      if (p.has_mode) {
+        float zeta = 0.f;
+        if (nl) {
+          float bc = XH(mm) ? 1.f : p.lbc;
+          float dvdx = (XLV(mm) + XV(mm) == 0) ? 0.f : bc * r0[Q_RH_DL] * ((vh[0] - vh0_l) + (vl[0] - vl0_l));
+          float dudy = (XU(mm) + XU(m[1]) == 0)
+                           ? 0.f
+                           : bc * q1 * (r0[Q_CU] * ((uh[0] - uh[1]) + (ul[0] - ul[1])) + r0[Q_DCU] * uh[1]);
+          zeta = dvdx - dudy * r0[Q_INV_CH];
+        }
+        unsigned a = XE(mm), b = XLE(m[1]), c = XLE(mm), d = XE(m[1]);
+        float dh = ((a ? d0 : 0.f) + (b ? dl1 : 0.f) + (c ? dl0 : 0.f) + (d ? d1 : 0.f)) * W4(a, b, c, d);
+        pv = __fdividef(r0[Q_FH] + zeta, fmaxf(dh, 2.220446e-16f));
+      }
+      pot[0] = pv;
+      float k1 = 0.f;
+      if (nl && XE(m[1])) {
+        float a = 0.5f * (uh1_r * uh1_r) + 0.5f * (uh[1] * uh[1]);
+        float c = 0.5f * (vh[0] * vh[0]) + 0.5f * (vh[1] * vh[1]);
+        k1 = (a + c) * 0.5f;
+      }
+      ke[0] = k1;
+    }
+
+    // ---- lateral stress: pll2 at row J-2, plt2 at row J-1 -------------
+    if (MIX == 2) {
+      {  // first pass, unit thickness, Ah = 1: pll1 at J-1, plt1 at J
+        const unsigned m1 = m[1], m0 = m[0];
+        float pl = 0.f, pt = 0.f;
+        if (XE(m1)) {
+          unsigned ov = XV(m1), ovp = XV(m0);
+          float tE = r1[Q_TE] * HALF2(ov, ovp);
+          float du = (uh1_r - uh[1]) + (ul1_r - ul[1]);
+          float dv = (vh[0] - vh[1]) + (vl[0] - vl[1]);
+          pl = r1[Q_PC0] * du + q1 * dv + tE * ((ovp ? vh[0] : 0.f) + (ov ? vh[1] : 0.f));
+        }
+        if (XH(m0)) {
+          unsigned ou = XU(m0), oum = XU(m1);
+          float tH = r0[Q_TH] * HALF2(ou, oum);
+          float dv = (vh[0] - vh0_l) + (vl[0] - vl0_l);
+          float du = (uh[0] - uh[1]) + (ul[0] - ul[1]);
+          pt = r0[Q_HC0] * dv - q1 * du - tH * ((ou ? uh[0] : 0.f) + (oum ? uh[1] : 0.f));
+        }
+        pll1[0] = pl;
+        plt1[0] = pt;
+      }
+      {  // lu1, lv1 at row J-1
+        const float pll1_l = shl(pll1[0]), plt1_r = shr(plt1[1]);
+        const unsigned m1 = m[1];
+        float a = 0.f, b = 0.f;
+        if (XU(m1)) {
+          float t2 = 2.f * r1[Q_TU] * HALF2(XH(m1), XH(m[0]));
+          a = -r1[Q_RU_DL] * (pll1[0] - pll1_l) + q1 * (plt1[1] - plt1[0]) + t2 * (plt1[0] + plt1[1]);
+        }
+        if (XV(m1)) {
+          float t2 = 2.f * r1[Q_TV] * HALF2(XE(m1), XE(m[2]));
+          b = -r1[Q_RV_DL] * (plt1_r - plt1[1]) + q1 * (pll1[0] - pll1[1]) - t2 * (pll1[0] + pll1[1]);
+        }
+        lu1[0] = a;
+        lv1[0] = b;
+      }
+      {  // second pass, thickness weighted, Ah = -bih
+        const float lu1_r = shr(lu1[1]), lv1_l = shl(lv1[0]);
+        const unsigned m2 = m[2], m1 = m[1];
+        float pl = 0.f, pt = 0.f;
+        if (XE(m2)) {
+          unsigned ov = XV(m2), ovp = XV(m1);
+          float tE = r2[Q_TE] * HALF2(ov, ovp);
+          float s = r2[Q_PC0] * (lu1_r - lu1[1]) + q1 * (lv1[0] - lv1[1]) +
+                    tE * ((ovp ? lv1[0] : 0.f) + (ov ? lv1[1] : 0.f));
+          pl = -p.bih * d2 * s;
+        }
+        if (XH(m1)) {
+          unsigned ou = XU(m1), oum = XU(m2);
+          float tH = r1[Q_TH] * HALF2(ou, oum);
+          float s = r1[Q_HC0] * (lv1[0] - lv1_l) - q1 * (lu1[0] - lu1[1]) -
+                    tH * ((ou ? lu1[0] : 0.f) + (oum ? lu1[1] : 0.f));
+          unsigned a = XE(m1), b = XLE(m2), c = XLE(m1), d = XE(m2);
+          float dh = ((a ? d1 : 0.f) + (b ? dl2 : 0.f) + (c ? dl1 : 0.f) + (d ? d2 : 0.f)) * W4(a, b, c, d);
+          pt = -p.bih * dh * s;
+        }
+        pll2[0] = pl;
+        plt2[0] = pt;
+      }
+    } else if (MIX == 1) {
+      const float uh2_r = shr(uh[2]), ul2_r = shr(ul[2]);
+      const float vh1_l = shl(vh[1]), vl1_l = shl(vl[1]);
+      const unsigned m2 = m[2], m1 = m[1];
+      float pl = 0.f, pt = 0.f;
+      if (XE(m2)) {
+        unsigned ov = XV(m2), ovp = XV(m1);
+        float tE = r2[Q_TE] * HALF2(ov, ovp);
+        float du = (uh2_r - uh[2]) + (ul2_r - ul[2]);
+        float dv = (vh[1] - vh[2]) + (vl[1] - vl[2]);
+        float s = r2[Q_PC0] * du + q1 * dv + tE * ((ovp ? vh[1] : 0.f) + (ov ? vh[2] : 0.f));
+        pl = p.Ah * d2 * s;
+      }
+      if (XH(m1)) {
+        unsigned ou = XU(m1), oum = XU(m2);
+        float tH = r1[Q_TH] * HALF2(ou, oum);
+        float dv = (vh[1] - vh1_l) + (vl[1] - vl1_l);
+        float du = (uh[1] - uh[2]) + (ul[1] - ul[2]);
+        float s = r1[Q_HC0] * dv - q1 * du - tH * ((ou ? uh[1] : 0.f) + (oum ? uh[2] : 0.f));
+        unsigned a = XE(m1), b = XLE(m2), c = XLE(m1), d = XE(m2);
+        float dh = ((a ? d1 : 0.f) + (b ? dl2 : 0.f) + (c ? dl1 : 0.f) + (d ? d2 : 0.f)) * W4(a, b, c, d);
+        pt = p.Ah * dh * s;
+      }
+      pll2[0] = pl;
+      plt2[0] = pt;
+    }
+
+    // ---- tendencies and compensated update of row o = J-2 ------------
+    // every lane takes part in the shuffles; updating lanes use the values
+    const float muh2_r = shr(muh[2]), mul2_r = shr(mul[2]), muh3_r = shr(muh[3]);
+    const float mvh2_l = shl(mvh[2]), mvh1_l = shl(mvh[1]);
+    const float eh2_l = shl(eh[2]), el2_l = shl(el[2]), ke1_l = shl(ke[1]);
+    const float pot2_r = shr(pot[2]);
+    const float vh2_l = shl(vh[2]), vh1_lo = shl(vh[1]);
+    const float uh2_r = shr(uh[2]), uh3_r = shr(uh[3]);
+    const float pll2_l = shl(pll2[0]), plt2_r = shr(plt2[1]);
+    if (upd) {
+      const unsigned mm = m[2];
+      float ge = 0.f, gu = 0.f, gv = 0.f;
+      if (XE(mm)) {
+        float dmv = r1[Q_CV] * ((mvh[1] - mvh[2]) + (mvl[1] - mvl[2])) + r1[Q_DCV] * mvh[2];
+        ge = -((muh2_r - muh[2]) + (mul2_r - mul[2])) * r2[Q_RE_DL] - dmv * r2[Q_RE_DT];
+        if (p.has_F) ge += p.Fe[ko];
+      }
+      if (XU(mm)) {
+        float pv = 0.5f * (pot[1] + pot[2]);
+        float mv = 0.25f * ((mvh[1] + mvh2_l) + (mvh1_l + mvh[2]));
+        float dE = G * ((eh[2] - eh2_l) + (el[2] - el2_l)) + (ke[1] - ke1_l);
+        float g = pv * mv - dE * r2[Q_RU_DL];
+        unsigned a = XE(mm), b = XLE(mm);
+        float du = ((a ? d2 : 0.f) + (b ? dl2 : 0.f)) * W2(a, b);
+        if (p.qbf) {
+          float vb = 0.25f * ((vh[1] + vh2_l) + (vh1_lo + vh[2]));
+          float gs = p.gsq_uniform ? p.gsq_s[0] : p.gsq[0][ko];
+          float f = gs * sqrtf(uh[2] * uh[2] + vb * vb) * uh[2];
+          if (p.barotropic) f = __fdividef(f, p.Hu[ko]);
+          g -= f;
+        }
+        if (MIX) {
+          float t2 = 2.f * r2[Q_TU] * HALF2(XH(mm), XH(m[1]));
+          float lat = -r2[Q_RU_DL] * (pll2[0] - pll2_l) + q1 * (plt2[1] - plt2[0]) + t2 * (plt2[0] + plt2[1]);
+          g += __fdividef(lat, du);
+        }
+        if (p.has_F) g += p.Fx[ko];
+        if (p.wind_x) g += __fdividef(p.ts_rho * (p.wind_rows ? p.wx[o] : p.wx[ko]), nl ? du : 1.f);
+        gu = g;
+      }
+      if (XV(mm)) {
+        float pv = 0.5f * (pot2_r + pot[2]);
+        float mu = 0.25f * ((muh2_r + muh[3]) + (muh[2] + muh3_r));
+        float dE = G * ((eh[2] - eh[3]) + (el[2] - el[3])) + (ke[1] - ke[2]);
+        float g = -pv * mu - dE * q1;
+        unsigned a = XE(mm), b = XE(m[3]);
+        float dv = ((a ? d2 : 0.f) + (b ? d3 : 0.f)) * W2(a, b);
+        if (p.qbf) {
+          float ub = 0.25f * ((uh2_r + uh[3]) + (uh[2] + uh3_r));
+          float gs = p.gsq_uniform ? p.gsq_s[1] : p.gsq[1][ko];
+          float f = gs * sqrtf(vh[2] * vh[2] + ub * ub) * vh[2];
+          if (p.barotropic) f = __fdividef(f, p.Hv[ko]);
+          g -= f;
+        }
+        if (MIX) {
+          float t2 = 2.f * r2[Q_TV] * HALF2(XE(mm), XE(m[3]));
+          float lat = -r2[Q_RV_DL] * (plt2_r - plt2[1]) + q1 * (pll2[0] - pll2[1]) - t2 * (pll2[0] + pll2[1]);
+          g += __fdividef(lat, dv);
+        }
+        if (p.has_F) g += p.Fy[ko];
+        if (p.wind_y) g += __fdividef(p.ts_rho * (p.wind_rows ? p.wy[o] : p.wy[ko]), nl ? dv : 1.f);
+        gv = g;
+      }
+      p.Ge3[ko] = ge;
+      p.Gu3[ko] = gu;
+      p.Gv3[ko] = gv;
+      float dpu, dpv, dpe;
+      if (p.impl_uniform) {
+        dpu = p.dp_s[0]; dpv = p.dp_s[1]; dpe = p.dp_s[2];
+      } else {
+        dpu = p.dp[0][ko]; dpv = p.dp[1][ko]; dpe = p.dp[2][ko];
+      }
+      float ince = p.dt * (p.ab0 * g1e + p.ab1 * g2e + p.ab2 * ge);
+      float incu = p.dt * (p.ab0 * g1u + p.ab1 * g2u + p.ab2 * gu);
+      float incv = p.dt * (p.ab0 * g1v + p.ab1 * g2v + p.ab2 * gv);
+      float nh, nlo;
+      comp_damp(eh[2], el[2], ince, dpe, nh, nlo);
+      if (nl) {
+        float lim = p.minD - he[2];
+        if (nh < lim) { nh = lim; nlo = 0.f; }
+      }
+      p.eh1[ko] = nh; p.el1[ko] = nlo;
+      comp_damp(uh[2], ul[2], incu, dpu, nh, nlo);
+      p.uh1[ko] = nh; p.ul1[ko] = nlo;
+      comp_damp(vh[2], vl[2], incv, dpv, nh, nlo);
+      p.vh1[ko] = nh; p.vl1[ko] = nlo;
+    }
+#undef XH
+#undef XU
+#undef XV
+#undef XE
+#undef XLV
+#undef XLE
+#undef W2
+#undef W4
+#undef HALF2
+  };
+
+  for (; J < jend; J++) {
+#pragma unroll
+    for (int a = 3; a > 0; a--) {
+      uh[a] = uh[a - 1]; ul[a] = ul[a - 1]; vh[a] = vh[a - 1]; vl[a] = vl[a - 1];
+      eh[a] = eh[a - 1]; el[a] = el[a - 1]; he[a] = he[a - 1]; m[a] = m[a - 1];
+      muh[a] = muh[a - 1]; mul[a] = mul[a - 1];
+    }
+#pragma unroll
+    for (int a = 2; a > 0; a--) {
+      mvh[a] = mvh[a - 1]; mvl[a] = mvl[a - 1]; pot[a] = pot[a - 1]; ke[a] = ke[a - 1];
+      off[a] = off[a - 1]; rr[a] = rr[a - 1];
+    }
+    pll1[1] = pll1[0]; plt1[1] = plt1[0]; lu1[1] = lu1[0]; lv1[1] = lv1[0];
+    pll2[1] = pll2[0]; plt2[1] = plt2[0];
+    m[0] = n_m; uh[0] = n_uh; ul[0] = n_ul; vh[0] = n_vh; vl[0] = n_vl;
+    eh[0] = n_eh; el[0] = n_el; he[0] = n_he;
+    off[0] = noff;
+    rr[0] = nrow;
+    if (J + 1 < jend) {  // prefetch row J+1
+      int jw = wrapm(J + 1, ny);
+      noff = nx * jw;
+      nrow = p.rows + (size_t)jw * Q_NR;
+      const int kn = gi + noff;
+      n_m = p.mask16[kn];
+      n_uh = p.uh0[kn]; n_ul = p.ul0[kn]; n_vh = p.vh0[kn]; n_vl = p.vl0[kn];
+      n_eh = p.eh0[kn]; n_el = p.el0[kn]; n_he = p.He[kn];
+    }
+    const bool interior = __all_sync(FULL, (m[0] & m[1] & m[2] & m[3] & 0xFFFu) == 0xFFFu);
+    if (interior) body(std::true_type{});
+    else body(std::false_type{});
+  }
+}
+
+// per-row factors for the FP32 kernel
+std::vector<double> fp32c_rows(const swm_gpu_ctx *c) {
+  const HostGrid &g = c->hg;
+  int ny = c->ny;
+  double A = c->cfg.A, dL = g.dLambda, dT = g.dTheta;
+  std::vector<double> rows((size_t)ny * Q_NR);
+  for (int j = 0; j < ny; j++) {
+    double *r = &rows[(size_t)j * Q_NR];
+    int jm = j == 0 ? ny - 1 : j - 1;
+    double cE = g.cosl[GE][j], cV = g.cosl[GV][j], cU = g.cosl[GU][j], cH = g.cosl[GH][j];
+    r[Q_CV] = cV;
+    r[Q_DCV] = cV - g.cosl[GV][jm];
+    r[Q_CU] = cU;
+    r[Q_DCU] = cU - g.cosl[GU][jm];
+    r[Q_FH] = g.f[GH][j];
+    r[Q_RE_DL] = 1. / (A * cE * dL);
+    r[Q_RE_DT] = 1. / (A * cE * dT);
+    r[Q_RU_DL] = 1. / (A * cU * dL);
+    r[Q_RV_DL] = 1. / (A * cV * dL);
+    r[Q_RH_DL] = 1. / (A * cH * dL);
+    r[Q_INV_CH] = 1. / cH;
+    r[Q_PC0] = -1. / (dL * A * cE);
+    r[Q_HC0] = -1. / (dL * A * cH);
+    r[Q_TE] = g.tanl[GE][j] / A;
+    r[Q_TH] = g.tanl[GH][j] / A;
+    r[Q_TU] = g.tanl[GU][j] / A;
+    r[Q_TV] = g.tanl[GV][j] / A;
+  }
+  return rows;
+}
+
+// rows per warp strip: longer strips recompute fewer look-ahead rows, shorter
+// ones give more warps; SWM_GB300_MARCH_S (8, 16 or 32) overrides the default
+template <int MIX, int S>
+static void launch_s(swm_gpu_ctx *c, const P32 &p) {
+  int H = MIX == 2 ? 2 : 1;
+  int ti = 32 - 2 * H;
+  dim3 grid((c->nx + ti - 1) / ti, (c->ny + 4 * S - 1) / (4 * S));
+  k_march<MIX, S><<<grid, 128, 0, c->stream>>>(p);
+}
+
+template <int MIX>
+static void launch_mix(swm_gpu_ctx *c, const P32 &p, int s) {
+  if (s == 8) launch_s<MIX, 8>(c, p);
+  else if (s == 32) launch_s<MIX, 32>(c, p);
+  else launch_s<MIX, 16>(c, p);
+}
+
+void march_launch(swm_gpu_ctx *c, const P32 &p) {
+  static int s_rows = -1;
+  if (s_rows < 0) {
+    const char *e = getenv("SWM_GB300_MARCH_S");
+    s_rows = e ? atoi(e) : 16;
+  }
+  if (p.mix == 2) launch_mix<2>(c, p, s_rows);
+  else if (p.mix == 1) launch_mix<1>(c, p, s_rows);
+  else launch_mix<0>(c, p, s_rows);
+  c->launches++;
+}
+
+}  // namespace swm
