@@ -254,8 +254,12 @@ __global__ void __launch_bounds__(128) k_march(P32 p) {
 
     // ---- tendencies and compensated update of row o = J-2 ------------
     // every lane takes part in the shuffles; updating lanes use the values
-    const float muh2_r = shr(muh[2]), mul2_r = shr(mul[2]), muh3_r = shr(muh[3]);
-    const float mvh2_l = shl(mvh[2]), mvh1_l = shl(mvh[1]);
+    // the PV fluxes take the whole mass flux, hi + lo: lo carries the
+    // free-surface part eta * u, which is not a rounding-level correction
+    const float mvs1 = mvh[1] + mvl[1], mvs2 = mvh[2] + mvl[2];
+    const float mus2 = muh[2] + mul[2], mus3 = muh[3] + mul[3];
+    const float muh2_r = shr(muh[2]), mul2_r = shr(mul[2]), mus3_r = shr(mus3);
+    const float mvs2_l = shl(mvs2), mvs1_l = shl(mvs1);
     const float eh2_l = shl(eh[2]), el2_l = shl(el[2]), ke1_l = shl(ke[1]);
     const float pot2_r = shr(pot[2]);
     const float vh2_l = shl(vh[2]), vh1_lo = shl(vh[1]);
@@ -271,7 +275,7 @@ __global__ void __launch_bounds__(128) k_march(P32 p) {
       }
       if (XU(mm)) {
         float pv = 0.5f * (pot[1] + pot[2]);
-        float mv = 0.25f * ((mvh[1] + mvh2_l) + (mvh1_l + mvh[2]));
+        float mv = 0.25f * ((mvs1 + mvs2_l) + (mvs1_l + mvs2));
         float dE = G * ((eh[2] - eh2_l) + (el[2] - el2_l)) + (ke[1] - ke1_l);
         float g = pv * mv - dE * r2[Q_RU_DL];
         unsigned a = XE(mm), b = XLE(mm);
@@ -294,7 +298,7 @@ __global__ void __launch_bounds__(128) k_march(P32 p) {
       }
       if (XV(mm)) {
         float pv = 0.5f * (pot2_r + pot[2]);
-        float mu = 0.25f * ((muh2_r + muh[3]) + (muh[2] + muh3_r));
+        float mu = 0.25f * (((muh2_r + mul2_r) + mus3) + (mus2 + mus3_r));
         float dE = G * ((eh[2] - eh[3]) + (el[2] - el[3])) + (ke[1] - ke[2]);
         float g = -pv * mu - dE * q1;
         unsigned a = XE(mm), b = XE(m[3]);
