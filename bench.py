@@ -43,6 +43,8 @@ def parse():
     ap.add_argument('--cells', type=int, default=1024)
     ap.add_argument('--error-steps', type=int, default=1000)
     ap.add_argument('--quick', action='store_true', help='skip the side measurements')
+    ap.add_argument('--device-only', action='store_true',
+                    help='only the warm-up and timed device steps (the form to run under ncu)')
     return ap.parse_args()
 
 
@@ -194,21 +196,23 @@ def ours(args, rank, ws):
     peak, kind = peaks()
     alg = BYTES_PER_POINT[args.path] * npts
     achieved = alg / (step_ms * 1e-3) / 1e9
-    traffic = None
-    prof = os.path.join(ROOT, 'profiles', 'fused_fp32c_double_gyre_1024.json')
-    if args.path == 'fused_fp32c' and cells == 1024 and os.path.exists(prof):
-        with open(prof) as fh:
-            traffic = json.load(fh).get('dram_bytes_per_launch')
+    traffic = profiled_traffic(args.path, cells)
     line['roofline'] = {'bound': 'hbm', 'achieved': achieved, 'peak': peak, 'unit': 'GB/s',
                         'frac': achieved / peak, 'traffic': traffic, 'peak_kind': kind,
                         'algorithmic_bytes_per_launch': alg,
                         'kernel': 'k_march<2,16>' if args.path == 'fused_fp32c' else args.path}
+    if args.device_only:
+        g.close()
+        return line
     # steady state without L2 flush (back-to-back steps)
     ms_nf = timed_steps(g, itt, 200, None, stream)
     itt += 200
     line['no_flush'] = {'ms_per_step': float(ms_nf.mean()), 'value': npts / (ms_nf.mean() * 1e-3)}
     # e2e through the C ABI with host buffers
-    tau_rows = case['streams'][0]['rec1'][0][:, 0].copy()
+    # the step's input (wind-stress rows) and result (integrals) in pinned host memory
+    tau_pin = torch.empty(case['config']['ny'], dtype=torch.float64).pin_memory()
+    tau_rows = tau_pin.numpy()
+    tau_rows[:] = case['streams'][0]['rec1'][0][:, 0]
     k_e2e = min(args.steps, 1000)
     g.synchronize()
     t0 = time.perf_counter()
@@ -229,6 +233,19 @@ def ours(args, rank, ws):
         line['cpu_baseline'] = cpu_baseline(cells)
     g.close()
     return line
+
+
+def profiled_traffic(path, cells):
+    """DRAM bytes per launch of the step kernel from the committed ncu summary."""
+    name = {'fused_fp32c': 'k_march', 'fused_fp64': 'k_fused'}.get(path)
+    f = os.path.join(ROOT, 'profiles', '%s_double_gyre_%d.md' % (name, cells))
+    if name is None or not os.path.exists(f):
+        return None
+    with open(f) as fh:
+        for l in fh:
+            if l.startswith('dram_bytes_per_launch:'):
+                return float(l.split(':')[1])
+    return None
 
 
 def side_measurements(args, case, g32, stream, flush, npts):

@@ -5,9 +5,9 @@
  *
  * The entry points mirror the Fortran module entry points of martinclaus/swm
  * they replace; each declaration cites the routine (path:line in the swm
- * source tree).  A Fortran host binds them with ISO_C_BINDING (see
- * INTEGRATION.md); every function returns 0 on success or a positive
- * SWM_GPU_E* code, and swm_gpu_last_error() gives the message.
+ * source tree).  A Fortran host binds them with ISO_C_BINDING interfaces;
+ * every function returns 0 on success or a positive SWM_GPU_E* code, and
+ * swm_gpu_last_error() gives the message.
  *
  * Arrays are Fortran column-major (Nx, Ny) = C row-major [Ny][Nx], FP64,
  * indices 0-based; masks are int8 (1 = ocean).  Host pointers only: the
@@ -142,7 +142,9 @@ int swm_gpu_step(swm_gpu_ctx *ctx, int64_t itt);
    TRC_advance (tracer_module.f90:133-146) */
 int swm_gpu_advance(swm_gpu_ctx *ctx, int64_t itt);
 /* nsteps iterations of step+advance for itt = itt0+1 .. itt0+nsteps with no
-   time-dependent file forcing in between; replayed from a CUDA graph */
+   time-dependent file forcing in between.  From itt = 3 on, without tracers
+   or oscillating forcing, blocks of six steps replay one captured CUDA graph
+   (bit-identical to single steps) */
 int swm_gpu_run(swm_gpu_ctx *ctx, int64_t itt0, int64_t nsteps);
 
 /* ---- host access (the registry pointers the diagnostics read) ---- */

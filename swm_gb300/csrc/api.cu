@@ -374,11 +374,74 @@ int swm_gpu_advance(swm_gpu_ctx *c, int64_t itt) {
   return swm_advance_impl(c, itt);
 }
 
+// From itt = 3 on the Adams-Bashforth weights are fixed, and without tracers
+// or oscillating forcing no kernel argument depends on itt; the pointers
+// cycle with the two time levels and the three increment slots, so a block of
+// six steps is captured once and replayed as a CUDA graph.
+constexpr int GRAPH_STEPS = 6;
+
+static bool graph_eligible(const swm_gpu_ctx *c) {
+  if (!c->tracers.empty()) return false;
+  for (const Stream &s : c->streams)
+    if (s.type == SWM_FRC_OSC) return false;
+  return true;
+}
+
+// records steps itt0+1 .. itt0+GRAPH_STEPS without running them; the host
+// indices go round the full cycle and end where they started
+static int graph_capture(swm_gpu_ctx *c, int64_t itt0) {
+  invalidate_graph(c);
+  if (c->cfg.path != SWM_PATH_PLAIN_FP64) TRY(fused_prepare(c));  // allocates on first use
+  const int n0 = c->n0, g0 = c->g0;
+  const int64_t l0 = c->launches;
+  SWM_CK(cudaStreamBeginCapture(c->stream, cudaStreamCaptureModeThreadLocal));
+  int rc = SWM_GPU_OK;
+  for (int s = 1; s <= GRAPH_STEPS && rc == SWM_GPU_OK; s++) {
+    rc = swm_step_impl(c, itt0 + s);
+    if (rc == SWM_GPU_OK) rc = swm_advance_impl(c, itt0 + s);
+  }
+  cudaGraph_t g = nullptr;
+  cudaError_t e = cudaStreamEndCapture(c->stream, &g);
+  const int64_t nl = c->launches - l0;
+  c->launches = l0;
+  if (rc != SWM_GPU_OK || e != cudaSuccess) {
+    if (g) cudaGraphDestroy(g);
+    if (rc != SWM_GPU_OK) return rc;
+    set_error(std::string("cudaStreamEndCapture: ") + cudaGetErrorString(e));
+    return SWM_GPU_ECUDA;
+  }
+  SWM_REQUIRE(c->n0 == n0 && c->g0 == g0, "swm_gpu_run: index cycle is not a multiple of the graph length");
+  e = cudaGraphInstantiate(&c->graph, g, 0);
+  cudaGraphDestroy(g);
+  if (e != cudaSuccess) {
+    c->graph = nullptr;
+    set_error(std::string("cudaGraphInstantiate: ") + cudaGetErrorString(e));
+    return SWM_GPU_ECUDA;
+  }
+  c->graph_launches = nl;
+  c->graph_n0 = n0;
+  c->graph_g0 = g0;
+  return SWM_GPU_OK;
+}
+
 int swm_gpu_run(swm_gpu_ctx *c, int64_t itt0, int64_t nsteps) {
   SWM_REQUIRE(c && c->stage >= 5, "swm_gpu_run: model not initialised");
-  for (int64_t s = 1; s <= nsteps; s++) {
-    TRY(swm_step_impl(c, itt0 + s));
-    TRY(swm_advance_impl(c, itt0 + s));
+  const bool graphs = graph_eligible(c) && nsteps >= 2 * GRAPH_STEPS;
+  int64_t s = 1;
+  while (s <= nsteps) {
+    const int64_t itt = itt0 + s;
+    if (graphs && itt >= 3 && nsteps - s + 1 >= GRAPH_STEPS) {
+      if (!c->graph) TRY(graph_capture(c, itt - 1));
+      if (c->n0 == c->graph_n0 && c->g0 == c->graph_g0) {
+        SWM_CK(cudaGraphLaunch(c->graph, c->stream));
+        c->launches += c->graph_launches;
+        s += GRAPH_STEPS;
+        continue;
+      }
+    }
+    TRY(swm_step_impl(c, itt));
+    TRY(swm_advance_impl(c, itt));
+    s++;
   }
   SWM_CK(cudaGetLastError());
   return SWM_GPU_OK;

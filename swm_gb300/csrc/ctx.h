@@ -117,9 +117,9 @@ struct swm_gpu_ctx {
   double *trc_coeff = nullptr;
   FusedState *fused = nullptr;
   SorState *sor = nullptr;
-  cudaGraphExec_t graph = nullptr;
-  int64_t graph_steps = 0;
-  int graph_n0 = -1, graph_g0 = -1;
+  cudaGraphExec_t graph = nullptr;  // GRAPH_STEPS captured steps (swm_gpu_run)
+  int64_t graph_launches = 0;       // kernels in one replay
+  int graph_n0 = -1, graph_g0 = -1; // level and ring offsets the replay starts from
   swm::Dev dev() const;
 };
 
