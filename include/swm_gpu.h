@@ -162,6 +162,18 @@ int swm_gpu_streamfunction(swm_gpu_ctx *ctx, double *psi_out);
    No counterpart in the reference (its diagnostics write fields only); this
    is the per-step scalar a monitoring loop reads back (16-24 bytes D2H). */
 int swm_gpu_integrals(swm_gpu_ctx *ctx, double *out3);
+/* The same three integrals, bit for bit, computed without allocating any
+   memory (no device, pinned or library allocation): all scratch is one fixed
+   array inside the library, for hosts that cannot allocate inside their time
+   loop (device memory fully reserved by their own pool, or other streams
+   that an implicit device synchronisation of cudaMalloc/cudaFree would
+   stall).  No counterpart in the reference.  Grids of at most
+   SWM_NOALLOC_MAX_NY rows (SWM_GPU_EINVAL beyond).  The first call on a
+   device looks up the array's device address; make that first call before
+   any stream capture.  The array is shared by all contexts on a device:
+   calls that overlap in time on one device race and must be serialised. */
+#define SWM_NOALLOC_MAX_NY 8192
+int swm_gpu_integrals_noalloc(swm_gpu_ctx *ctx, double *out3);
 
 /* ---- tracer (tracer_vars.f90:124-185, tracer_module.f90:58-342) ---- */
 int trc_gpu_add(swm_gpu_ctx *ctx, double kappa_h, double cons, double gamma_c, const double *C,

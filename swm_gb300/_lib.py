@@ -44,6 +44,7 @@ def _sigs():
         'swm_gpu_add_stream': (I, [P, I, I, D, I, P, P, C.POINTER(C.c_int)]),
         'swm_gpu_set_stream_data': (I, [P, I, P, P]), 'swm_gpu_forcing_init': (I, [P]),
         'swm_gpu_set_stream_rows': (I, [P, I, P, P]), 'swm_gpu_integrals': (I, [P, P]),
+        'swm_gpu_integrals_noalloc': (I, [P, P]),
         'swm_gpu_initial_conditions': (I, [P, P, P, P]), 'swm_gpu_step': (I, [P, I64]),
         'swm_gpu_advance': (I, [P, I64]), 'swm_gpu_run': (I, [P, I64, I64]),
         'swm_gpu_get_field': (I, [P, I, P]), 'swm_gpu_set_field': (I, [P, I, P]),

@@ -21,6 +21,7 @@
 // :182-449, swm_lateralmixing_module.f90:66-240, time_integration_module.f90
 // :74-112) with divisions by grid metrics replaced by per-row reciprocals, so
 // results agree with the FP64 restatement to rounding, not bit for bit.
+#include <atomic>
 #include <cmath>
 #include <cstring>
 #include <vector>
@@ -874,3 +875,84 @@ int swm_gpu_integrals(swm_gpu_ctx *c, double *out3) {
 }
 
 }  // extern "C"
+
+// ---------------------------------------------------------------------------
+// Domain integrals without any allocation
+//
+// The same reduction as swm_gpu_integrals (same kernels, block count and cell
+// areas, so the same sums bit for bit), but every intermediate lives in one
+// fixed array compiled into this library.  It is meant for callers that must
+// not allocate in the middle of a time loop: a host whose device memory is
+// already reserved in full by its own pool (a cudaMalloc there fails or makes
+// the pool give memory back), and a host that runs other streams concurrently
+// (cudaFree and the first cudaMallocHost can synchronise the whole device and
+// so stall them).  Limits: grids of at most SWM_NOALLOC_MAX_NY rows; one
+// scratch array per device, so two calls that overlap in time on one device
+// (from two threads, or two contexts) race on it and must be serialised by
+// the caller.
+// ---------------------------------------------------------------------------
+namespace swm {
+
+constexpr int NOALLOC_NB = 2 * 152;  // partial-sum blocks, as in swm_gpu_integrals
+constexpr size_t NOALLOC_DOUBLES = 2 * (size_t)SWM_NOALLOC_MAX_NY + 3 * NOALLOC_NB + 3;
+// area_u[MAX_NY] | area_e[MAX_NY] | partial[3 * NB] | out[3]  (138 KB per device)
+static __device__ __align__(256) double g_noalloc_scratch[NOALLOC_DOUBLES];
+// device address of the scratch per device ordinal, looked up on first use
+constexpr int NOALLOC_MAX_DEVICES = 64;
+static std::atomic<double *> g_noalloc_ptr[NOALLOC_MAX_DEVICES];
+
+// cell areas per row, A^2 cos(lat) dLambda dTheta, the product in the order
+// swm_gpu_integrals forms it on the host
+__global__ void k_area_rows(const double *cos_u, const double *cos_e, double A, double dL, double dT, int ny,
+                            double *area_u, double *area_e) {
+  int j = blockIdx.x * blockDim.x + threadIdx.x;
+  if (j < ny) {
+    area_u[j] = A * A * cos_u[j] * dL * dT;
+    area_e[j] = A * A * cos_e[j] * dL * dT;
+  }
+}
+
+}  // namespace swm
+
+extern "C" int swm_gpu_integrals_noalloc(swm_gpu_ctx *c, double *out3) {
+  using namespace swm;
+  SWM_REQUIRE(c && c->stage >= 5 && out3, "swm_gpu_integrals_noalloc: bad arguments");
+  if (c->ny > SWM_NOALLOC_MAX_NY) {
+    set_error("swm_gpu_integrals_noalloc: the grid has " + std::to_string(c->ny) +
+              " rows; the fixed scratch serves at most " + std::to_string(SWM_NOALLOC_MAX_NY));
+    return SWM_GPU_EINVAL;
+  }
+  int dev = -1;
+  SWM_CK(cudaGetDevice(&dev));
+  SWM_REQUIRE(dev >= 0 && dev < NOALLOC_MAX_DEVICES, "swm_gpu_integrals_noalloc: device ordinal out of range");
+  // set-up, once per device: the address of this device's copy of the array
+  double *scr = g_noalloc_ptr[dev].load(std::memory_order_acquire);
+  if (!scr) {
+    SWM_CK(cudaGetSymbolAddress((void **)&scr, g_noalloc_scratch));
+    g_noalloc_ptr[dev].store(scr, std::memory_order_release);
+  }
+  // every slot below is written before it is read, so nothing needs clearing
+  double *area_u = scr, *area_e = scr + SWM_NOALLOC_MAX_NY;
+  double *partial = scr + 2 * (size_t)SWM_NOALLOC_MAX_NY, *out = partial + 3 * NOALLOC_NB;
+  const HostGrid &g = c->hg;
+  k_area_rows<<<(c->ny + 127) / 128, 128, 0, c->stream>>>(c->d_cos[GU], c->d_cos[GE], c->cfg.A, g.dLambda,
+                                                          g.dTheta, c->ny, area_u, area_e);
+  FusedState *f = c->fused;
+  const int8_t *oU = c->d_ocean[GU], *oV = c->d_ocean[GV], *oE = c->d_ocean[GE];
+  if (f && f->ready && f->comp) {
+    int a = f->n0;
+    k_integrals<float, true><<<NOALLOC_NB, 256, 0, c->stream>>>(c->nx, c->ny, oU, oV, oE, area_u, area_e,
+                                                                f->uh[a], f->ul[a], f->vh[a], f->vl[a],
+                                                                f->eh[a], f->el[a], c->cfg.G, partial);
+  } else {
+    k_integrals<double, false><<<NOALLOC_NB, 256, 0, c->stream>>>(c->nx, c->ny, oU, oV, oE, area_u, area_e,
+                                                                  c->u[c->n0], nullptr, c->v[c->n0], nullptr,
+                                                                  c->eta[c->n0], nullptr, c->cfg.G, partial);
+  }
+  k_integrals_final<<<1, 256, 0, c->stream>>>(partial, NOALLOC_NB, out);
+  c->launches += 3;
+  SWM_CK(cudaGetLastError());
+  SWM_CK(cudaMemcpyAsync(out3, out, 3 * sizeof(double), cudaMemcpyDeviceToHost, c->stream));
+  SWM_CK(cudaStreamSynchronize(c->stream));
+  return SWM_GPU_OK;
+}
