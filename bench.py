@@ -163,7 +163,8 @@ def ours(args, rank, ws):
     import torch
     torch.cuda.set_device(int(os.environ.get('LOCAL_RANK', '0')))
     cells = args.cells
-    npts = (cells + 1) * (cells + 1)
+    npts = (cells + 1) * (cells + 1)  # array points (Nx, Ny) = cells + 1: the bytes moved
+    ncell = cells * cells              # cells: the unit of the metric
     case, g, drv = build_model(args.path, cells, args.warmup + args.steps)
     stream = torch.cuda.ExternalStream(g.stream())
     flush = torch.empty(512 * 1024 * 1024 // 4, dtype=torch.float32, device='cuda')
@@ -182,7 +183,7 @@ def ours(args, rank, ws):
     itt += args.steps
     barrier(ws)
     step_ms = allmax(ws, float(ms.mean()))
-    value = npts * ws / (step_ms * 1e-3)
+    value = ncell * ws / (step_ms * 1e-3)
     line = {'metric': METRIC, 'value': value, 'unit': 'cell-steps/s', 'n_gpus': ws, 'steps': args.steps,
             'warmup': args.warmup, 'ms_per_step': step_ms, 'higher_is_better': True, 'scaling': 'weak',
             'vs_baseline': None, 'dtype': 'f32' if args.path == 'fused_fp32c' else 'f64',
@@ -207,7 +208,7 @@ def ours(args, rank, ws):
     # steady state without L2 flush (back-to-back steps)
     ms_nf = timed_steps(g, itt, 200, None, stream)
     itt += 200
-    line['no_flush'] = {'ms_per_step': float(ms_nf.mean()), 'value': npts / (ms_nf.mean() * 1e-3)}
+    line['no_flush'] = {'ms_per_step': float(ms_nf.mean()), 'value': ncell / (ms_nf.mean() * 1e-3)}
     # e2e through the C ABI with host buffers
     # the step's input (wind-stress rows) and result (integrals) in pinned host memory
     tau_pin = torch.empty(case['config']['ny'], dtype=torch.float64).pin_memory()
@@ -223,12 +224,13 @@ def ours(args, rank, ws):
         g.advance(itt)
         integ = g.integrals()
     e2e_s = time.perf_counter() - t0
-    line['e2e'] = {'value': npts * k_e2e / e2e_s, 'unit': 'cell-steps/s', 'h2d_bytes_per_step': tau_rows.nbytes,
+    line['e2e'] = {'value': ncell * k_e2e / e2e_s, 'unit': 'cell-steps/s', 'h2d_bytes_per_step': tau_rows.nbytes,
                    'd2h_bytes_per_step': integ.nbytes, 'steps': k_e2e,
                    'per_step': 'H2D wind-stress rows, swm_gpu_step + swm_gpu_advance, D2H FP64 integrals'}
     if rank == 0 and not args.quick:
-        line.update(side_measurements(args, case, g, stream, flush, npts))
+        line.update(side_measurements(args, case, g, stream, flush, ncell))
         line['speedup_vs_fp64_plain'] = line['plain_fp64']['ms_per_step'] / step_ms
+        line['ensemble'] = ensemble_measurement(args)
     if rank == 0 and ws == 1 and not args.quick:
         line['cpu_baseline'] = cpu_baseline(cells)
     g.close()
@@ -248,14 +250,14 @@ def profiled_traffic(path, cells):
     return None
 
 
-def side_measurements(args, case, g32, stream, flush, npts):
+def side_measurements(args, case, g32, stream, flush, ncell):
     """FP64 paths on the same workload, and the FP32 error against FP64."""
     out = {}
     for path, k in (('plain_fp64', 20), ('fused_fp64', 50)):
         _, g, _ = build_model(path, args.cells, 100)
         g.run(0, 3)
         ms = timed_steps(g, 3, k, flush, __import__('torch').cuda.ExternalStream(g.stream()))
-        out[path] = {'ms_per_step': float(ms.mean()), 'value': npts / (ms.mean() * 1e-3), 'steps': k}
+        out[path] = {'ms_per_step': float(ms.mean()), 'value': ncell / (ms.mean() * 1e-3), 'steps': k}
         g.close()
     # FP32C against the bit-exact FP64 plain path from the same start
     e = args.error_steps
@@ -276,6 +278,65 @@ def side_measurements(args, case, g32, stream, flush, npts):
     return out
 
 
+def ensemble_measurement(args, n_members=256, steps=200):
+    """The batched FP32 path on 256 basins of uneven sizes (Nx, Ny
+    log-uniform in 64-512, Laplacian Ah = 500), against the same members
+    stepped one by one on the FP64 plain path."""
+    import torch
+    from swm_gb300.host import synthetic
+    from swm_gb300.host.driver import Driver
+    from swm_gb300.model import GpuEnsemble, GpuModel
+    cases = synthetic.ensemble_members(n=n_members, nsteps=steps + 100)
+    cells = sum((c['config']['nx'] - 1) * (c['config']['ny'] - 1) for c in cases)
+    pts = sum(c['config']['nx'] * c['config']['ny'] for c in cases)
+    ms = []
+    for c in cases:
+        g = GpuModel('fused_fp32c')
+        Driver(c, g).init(with_diag=False)
+        ms.append(g)
+    ens = GpuEnsemble(ms)
+    st = torch.cuda.ExternalStream(ens.stream())
+    ens.run(0, 12)
+    ens.synchronize()
+    a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    l0 = ens.launch_count()
+    a.record(st)
+    ens.run(12, steps)
+    b.record(st)
+    ens.synchronize()
+    launches = ens.launch_count() - l0
+    ms_step = a.elapsed_time(b) / steps
+    ints = ens.integrals()
+    out = {'members': n_members, 'cells': cells, 'array_points': pts, 'steps': steps,
+           'ms_per_step': ms_step, 'value': cells / (ms_step * 1e-3), 'unit': 'cell-steps/s',
+           'rows_per_strip': ens.rows(), 'gpu_launches': launches,
+           'l2': 'not flushed: the ensemble state (%.2f GB) is larger than L2' % (89 * pts / 1e9),
+           'finite_integrals': bool(np.isfinite(ints).all())}
+    peak, kind = peaks()
+    ach = 89 * pts / (ms_step * 1e-3) / 1e9
+    out['roofline'] = {'bound': 'hbm', 'achieved': ach, 'peak': peak, 'unit': 'GB/s', 'frac': ach / peak,
+                       'peak_kind': kind, 'kernel': 'k_march_ens<1,%d>' % ens.rows()}
+    ens.close()
+    for g in ms:
+        g.close()
+    # the same members one by one on the FP64 plain path (3 steps each, after start-up)
+    tot = 0.0
+    for c in cases:
+        g = GpuModel('plain_fp64')
+        Driver(c, g).init(with_diag=False)
+        g.run(0, 3)
+        g.synchronize()
+        t0 = time.perf_counter()
+        g.run(3, 3)
+        g.synchronize()
+        tot += (time.perf_counter() - t0) / 3
+        g.close()
+    out['plain_fp64_one_by_one'] = {'ms_per_step': tot * 1e3, 'value': cells / tot, 'unit': 'cell-steps/s',
+                                    'timing': 'wall clock per member, summed'}
+    out['speedup_vs_plain_fp64_one_by_one'] = tot * 1e3 / ms_step
+    return out
+
+
 def cpu_baseline(cells, budget_s=15.0):
     """The FP64 CPU restatement (oracle) on the same basin, all host cores."""
     sys.path.insert(0, os.path.join(ROOT, 'oracle'))
@@ -292,8 +353,7 @@ def cpu_baseline(cells, budget_s=15.0):
         o.run_steady(1)
         n += 1
         t = time.perf_counter() - t0
-    npts = (cells + 1) ** 2
-    return {'value': npts * n / t, 'unit': 'cell-steps/s', 'cores': os.cpu_count(), 'kind': 'port',
+    return {'value': cells * cells * n / t, 'unit': 'cell-steps/s', 'cores': os.cpu_count(), 'kind': 'port',
             'sample': '%d model steps of the %dx%d basin (FP64 C restatement, OpenMP)' % (n, cells, cells)}
 
 
@@ -313,8 +373,7 @@ def reference(args, rank, ws):
     t0 = time.perf_counter()
     o.run_steady(args.steps)
     t = time.perf_counter() - t0
-    npts = (args.cells + 1) * (strip + 1)
-    v = npts * args.steps / t
+    v = args.cells * strip * args.steps / t
     sample = 'one model step per bench step on a %dx%d-cell strip of the basin (same physics)' % (args.cells, strip)
     return {'metric': METRIC, 'value': v, 'unit': 'cell-steps/s', 'n_gpus': ws, 'steps': args.steps,
             'warmup': args.warmup, 'ms_per_step': t / args.steps * 1e3, 'higher_is_better': True,

@@ -175,6 +175,29 @@ int swm_gpu_integrals(swm_gpu_ctx *ctx, double *out3);
 #define SWM_NOALLOC_MAX_NY 8192
 int swm_gpu_integrals_noalloc(swm_gpu_ctx *ctx, double *out3);
 
+/* ---- ensemble of basins (extension; the reference runs one basin per
+   process) ----
+   Members are contexts created and initialised through the calls above on
+   SWM_PATH_FUSED_FP32C, without tracers, sharing the lateral-mixing kind and
+   the current step.  swm_gpu_ensemble_run steps all of them with one
+   persistent launch per step that takes (member, strip, row group) tiles
+   from a device queue; from itt = 3 on, blocks of six steps replay a CUDA
+   graph.  Members stay usable through their own contexts between runs
+   (get_field etc.).  The ensemble does not own the members: destroy it
+   before them. */
+typedef struct swm_gpu_ensemble swm_gpu_ensemble;
+int swm_gpu_ensemble_create(swm_gpu_ctx *const *members, int n, swm_gpu_ensemble **out);
+int swm_gpu_ensemble_destroy(swm_gpu_ensemble *ens);
+/* steps itt0+1 .. itt0+nsteps of every member (SWM_timestep + model_advance) */
+int swm_gpu_ensemble_run(swm_gpu_ensemble *ens, int64_t itt0, int64_t nsteps);
+/* FP64 domain integrals of every member, 3 per member as swm_gpu_integrals */
+int swm_gpu_ensemble_integrals(swm_gpu_ensemble *ens, double *out);
+int swm_gpu_ensemble_synchronize(swm_gpu_ensemble *ens);
+void *swm_gpu_ensemble_stream(swm_gpu_ensemble *ens);
+int64_t swm_gpu_ensemble_launch_count(swm_gpu_ensemble *ens);
+/* rows per warp strip the ensemble picked by timing its step */
+int swm_gpu_ensemble_rows(swm_gpu_ensemble *ens);
+
 /* ---- tracer (tracer_vars.f90:124-185, tracer_module.f90:58-342) ---- */
 int trc_gpu_add(swm_gpu_ctx *ctx, double kappa_h, double cons, double gamma_c, const double *C,
                 const double *C0, const double *gamma_field, const double *cons_field, int *id);

@@ -52,6 +52,10 @@ def _sigs():
         'swm_gpu_streamfunction': (I, [P, P]),
         'trc_gpu_add': (I, [P, D, D, D, P, P, P, P, C.POINTER(C.c_int)]), 'trc_gpu_init': (I, [P]),
         'trc_gpu_get_field': (I, [P, I, I, P]),
+        'swm_gpu_ensemble_create': (I, [P, I, PP]), 'swm_gpu_ensemble_destroy': (I, [P]),
+        'swm_gpu_ensemble_run': (I, [P, I64, I64]), 'swm_gpu_ensemble_integrals': (I, [P, P]),
+        'swm_gpu_ensemble_synchronize': (I, [P]), 'swm_gpu_ensemble_stream': (P, [P]),
+        'swm_gpu_ensemble_launch_count': (I64, [P]), 'swm_gpu_ensemble_rows': (I, [P]),
         'elsolv_sor_gpu_init': (I, [P]),
         'elsolv_sor_gpu_solve': (I, [P, P, P, D, I, C.POINTER(C.c_int), C.POINTER(C.c_double)]),
     }

@@ -161,6 +161,7 @@ int swm_gpu_destroy(swm_gpu_ctx *c) {
   invalidate_graph(c);
   fused_free(c);
   sor_free(c);
+  integrals_free(c);
   auto F = [](void *p) { if (p) cudaFree(p); };
   for (int q = 0; q < 4; q++) {
     F(c->d_ocean[q]); F(c->d_cos[q]); F(c->d_tan[q]); F(c->d_f[q]); F(c->d_lat[q]); F(c->d_H[q]);

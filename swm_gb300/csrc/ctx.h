@@ -87,6 +87,7 @@ struct Dev {
 
 struct FusedState;
 struct SorState;
+struct IntegralScratch;
 
 struct swm_gpu_ctx {
   swm_gpu_config cfg;
@@ -117,6 +118,8 @@ struct swm_gpu_ctx {
   double *trc_coeff = nullptr;
   FusedState *fused = nullptr;
   SorState *sor = nullptr;
+  IntegralScratch *integrals = nullptr;
+  int march_rows = 0;                // rows per warp strip of the FP32 step kernel (0: not tuned yet)
   cudaGraphExec_t graph = nullptr;  // GRAPH_STEPS captured steps (swm_gpu_run)
   int64_t graph_launches = 0;       // kernels in one replay
   int graph_n0 = -1, graph_g0 = -1; // level and ring offsets the replay starts from
@@ -147,6 +150,7 @@ int fused_step(swm_gpu_ctx *c, int64_t itt);
 int fused_sync_state(swm_gpu_ctx *c);    // FP32 pair state -> FP64 buffers
 int fused_load_state(swm_gpu_ctx *c);    // FP64 buffers -> FP32 pair state
 void fused_free(swm_gpu_ctx *c);
+void integrals_free(swm_gpu_ctx *c);
 // sor.cu
 void sor_free(swm_gpu_ctx *c);
 }  // namespace swm

@@ -1,0 +1,350 @@
+// ensemble.cu -- an ensemble of basins of uneven sizes stepped together.
+//
+// Extension: the reference runs one basin per process.  Each member is an
+// ordinary context on the FP32 compensated path, set up through the usual
+// entry points; the ensemble gathers their kernel parameter blocks into a
+// device table and cuts every member into warp tiles (strip of columns x
+// group of rows).  One persistent launch per step drains a device queue of
+// all members' tiles (k_march_ens), so small and large basins share the GPU
+// without one launch per member.  The members' time levels and increment
+// slots rotate in step, so the table holds one parameter block per member
+// for each of the six phases of that rotation, and blocks of six steps replay
+// one captured CUDA graph.  Per-member volume and energy sums are taken in
+// FP64.
+#include <cstring>
+#include <string>
+#include <vector>
+#include "ctx.h"
+#include "fused32.h"
+
+using swm::P32;
+
+namespace swm {
+
+constexpr int ENS_PHASES = 6;  // lcm of the 2 levels and 3 increment slots
+
+struct EnsInt {
+  const float *uh, *ul, *vh, *vl, *eh, *el;
+  const int8_t *oU, *oV, *oE;
+  const double *cU, *cE;
+  int nx, ny;
+  double A2dLdT, G;
+};
+
+// one block per member: sums in FP64 of eta*area, 0.5*G*eta^2*area and the
+// kinetic energy over the member's ocean points, as swm_gpu_integrals
+__global__ void k_ens_integrals(const EnsInt *__restrict__ d, double *__restrict__ out) {
+  __shared__ double red[3][256];
+  const EnsInt q = d[blockIdx.x];
+  double s0 = 0., s1 = 0., s2 = 0.;
+  const int n = q.nx * q.ny;
+  for (int k = threadIdx.x; k < n; k += blockDim.x) {
+    const int j = k / q.nx;
+    const double ae = q.A2dLdT * q.cE[j], au = q.A2dLdT * q.cU[j];
+    const double ee = (double)q.eh[k] + (double)q.el[k];
+    const double uu = (double)q.uh[k] + (double)q.ul[k];
+    const double vv = (double)q.vh[k] + (double)q.vl[k];
+    if (q.oE[k]) {
+      s0 += ee * ae;
+      s1 += 0.5 * q.G * ee * ee * ae;
+    }
+    if (q.oU[k]) s2 += 0.5 * uu * uu * au;
+    if (q.oV[k]) s2 += 0.5 * vv * vv * ae;
+  }
+  red[0][threadIdx.x] = s0;
+  red[1][threadIdx.x] = s1;
+  red[2][threadIdx.x] = s2;
+  __syncthreads();
+  for (int w = 128; w > 0; w >>= 1) {
+    if (threadIdx.x < w)
+      for (int r = 0; r < 3; r++) red[r][threadIdx.x] += red[r][threadIdx.x + w];
+    __syncthreads();
+  }
+  if (threadIdx.x < 3) out[3 * (size_t)blockIdx.x + threadIdx.x] = red[threadIdx.x][0];
+}
+
+static int rows_index(int r) {
+  for (int i = 0; i < 3; i++)
+    if (MARCH_ROWS[i] == r) return i;
+  return 1;
+}
+
+}  // namespace swm
+
+struct swm_gpu_ensemble {
+  std::vector<swm_gpu_ctx *> m;
+  int mix = 0, rows = 16, phase = 0, graph_phase = -1;
+  cudaStream_t stream = nullptr;
+  cudaEvent_t done = nullptr;
+  std::vector<cudaEvent_t> ev;
+  P32 *tab = nullptr;  // [ENS_PHASES][n]
+  int2 *tiles[3] = {};
+  int ntiles[3] = {};
+  int *next = nullptr;  // queue heads, one per phase
+  cudaGraphExec_t graph = nullptr;
+  int64_t launches = 0, graph_launches = 0;
+  swm::EnsInt *d_int = nullptr;
+  double *d_out = nullptr;
+};
+
+namespace {
+
+using namespace swm;
+
+int join_members(swm_gpu_ensemble *e) {  // ensemble stream waits for every member stream
+  for (size_t i = 0; i < e->m.size(); i++) {
+    SWM_CK(cudaEventRecord(e->ev[i], e->m[i]->stream));
+    SWM_CK(cudaStreamWaitEvent(e->stream, e->ev[i], 0));
+  }
+  return SWM_GPU_OK;
+}
+
+int release_members(swm_gpu_ensemble *e) {  // member streams wait for the ensemble stream
+  SWM_CK(cudaEventRecord(e->done, e->stream));
+  for (auto *c : e->m) SWM_CK(cudaStreamWaitEvent(c->stream, e->done, 0));
+  return SWM_GPU_OK;
+}
+
+// host side of one ensemble step: every member's level and slot offsets
+// advance as swm_gpu_step + swm_gpu_advance would advance them
+int rotate_members(swm_gpu_ensemble *e, int64_t itt) {
+  for (auto *c : e->m) {
+    int n0, g0;
+    fused_indices(c, &n0, &g0);
+    fused_set_indices(c, 1 - n0, (g0 + 1) % 3);
+    int rc = swm_gpu_advance(c, itt);
+    if (rc != SWM_GPU_OK) return rc;
+  }
+  e->phase = (e->phase + 1) % ENS_PHASES;
+  return SWM_GPU_OK;
+}
+
+int ens_step(swm_gpu_ensemble *e, int64_t itt) {
+  const size_t n = e->m.size();
+  const int ri = rows_index(e->rows);
+  SWM_CK(cudaMemsetAsync(e->next + e->phase, 0, sizeof(int), e->stream));
+  int rc = march_ens_launch(e->mix, e->rows, e->tab + (size_t)e->phase * n, e->tiles[ri], e->ntiles[ri],
+                            e->next + e->phase, e->stream);
+  if (rc != SWM_GPU_OK) return rc;
+  e->launches++;
+  return rotate_members(e, itt);
+}
+
+int ens_capture(swm_gpu_ensemble *e, int64_t itt0) {
+  if (e->graph) {
+    cudaGraphExecDestroy(e->graph);
+    e->graph = nullptr;
+  }
+  const int phase0 = e->phase;
+  const int64_t l0 = e->launches;
+  SWM_CK(cudaStreamBeginCapture(e->stream, cudaStreamCaptureModeThreadLocal));
+  int rc = SWM_GPU_OK;
+  for (int s = 1; s <= ENS_PHASES && rc == SWM_GPU_OK; s++) rc = ens_step(e, itt0 + s);
+  cudaGraph_t g = nullptr;
+  cudaError_t ce = cudaStreamEndCapture(e->stream, &g);
+  e->graph_launches = e->launches - l0;
+  e->launches = l0;
+  if (rc != SWM_GPU_OK || ce != cudaSuccess) {
+    if (g) cudaGraphDestroy(g);
+    if (rc != SWM_GPU_OK) return rc;
+    set_error(std::string("cudaStreamEndCapture: ") + cudaGetErrorString(ce));
+    return SWM_GPU_ECUDA;
+  }
+  SWM_REQUIRE(e->phase == phase0, "swm_gpu_ensemble_run: phase cycle mismatch");
+  ce = cudaGraphInstantiate(&e->graph, g, 0);
+  cudaGraphDestroy(g);
+  if (ce != cudaSuccess) {
+    e->graph = nullptr;
+    set_error(std::string("cudaGraphInstantiate: ") + cudaGetErrorString(ce));
+    return SWM_GPU_ECUDA;
+  }
+  e->graph_phase = phase0;
+  return SWM_GPU_OK;
+}
+
+void ens_free(swm_gpu_ensemble *e) {
+  if (e->stream) cudaStreamSynchronize(e->stream);
+  if (e->graph) cudaGraphExecDestroy(e->graph);
+  cudaFree(e->tab);
+  for (auto *t : e->tiles) cudaFree(t);
+  cudaFree(e->next);
+  cudaFree(e->d_int);
+  cudaFree(e->d_out);
+  for (auto ev : e->ev) cudaEventDestroy(ev);
+  if (e->done) cudaEventDestroy(e->done);
+  if (e->stream) cudaStreamDestroy(e->stream);
+  delete e;
+}
+
+}  // namespace
+
+extern "C" {
+
+int swm_gpu_ensemble_create(swm_gpu_ctx *const *members, int n, swm_gpu_ensemble **out) {
+  SWM_REQUIRE(members && n > 0 && out, "swm_gpu_ensemble_create: bad arguments");
+  *out = nullptr;
+  int n0 = -1, g0 = -1, mix = -1;
+  for (int i = 0; i < n; i++) {
+    swm_gpu_ctx *c = members[i];
+    SWM_REQUIRE(c && c->stage >= 5, "swm_gpu_ensemble_create: members must be initialised");
+    SWM_REQUIRE(c->cfg.path == SWM_PATH_FUSED_FP32C, "swm_gpu_ensemble_create: members must use SWM_PATH_FUSED_FP32C");
+    SWM_REQUIRE(c->tracers.empty(), "swm_gpu_ensemble_create: members with tracers are not batched");
+    SWM_REQUIRE(c->nx <= 65535 * 28 && c->ny <= 65535 * 8, "swm_gpu_ensemble_create: member too large for a tile index");
+    if (!c->march_rows) c->march_rows = 16;  // the ensemble tunes its own strip rows
+    int rc = fused_prepare(c);
+    if (rc != SWM_GPU_OK) return rc;
+    int a, b;
+    fused_indices(c, &a, &b);
+    int mx = c->cfg.lateral_mixing ? (c->cfg.mixing_kind == SWM_MIX_BIHARMONIC ? 2 : 1) : 0;
+    if (i == 0) { n0 = a; g0 = b; mix = mx; }
+    SWM_REQUIRE(a == n0 && b == g0, "swm_gpu_ensemble_create: members must be at the same step");
+    SWM_REQUIRE(mx == mix, "swm_gpu_ensemble_create: members must share the lateral-mixing kind");
+  }
+  swm_gpu_ensemble *e = new swm_gpu_ensemble();
+  e->m.assign(members, members + n);
+  e->mix = mix;
+  auto fail = [&](int rc) { ens_free(e); return rc; };
+  if (cudaStreamCreateWithFlags(&e->stream, cudaStreamNonBlocking) != cudaSuccess ||
+      cudaEventCreateWithFlags(&e->done, cudaEventDisableTiming) != cudaSuccess) {
+    set_error("swm_gpu_ensemble_create: stream or event creation failed");
+    return fail(SWM_GPU_ECUDA);
+  }
+  e->ev.resize(n);
+  for (int i = 0; i < n; i++)
+    if (cudaEventCreateWithFlags(&e->ev[i], cudaEventDisableTiming) != cudaSuccess) {
+      set_error("swm_gpu_ensemble_create: event creation failed");
+      return fail(SWM_GPU_ECUDA);
+    }
+  // parameter blocks for the six phases (AB3 weights: the table serves itt >= 3)
+  std::vector<P32> tab((size_t)ENS_PHASES * n);
+  for (int k = 0; k < ENS_PHASES; k++)
+    for (int i = 0; i < n; i++) {
+      fused_set_indices(members[i], (n0 + k) % 2, (g0 + k) % 3);
+      make_p32(members[i], 3, tab[(size_t)k * n + i]);
+    }
+  for (int i = 0; i < n; i++) fused_set_indices(members[i], n0, g0);
+  // tiles for each candidate strip length
+  const int ti = march_tile_cols(mix);
+  for (int r = 0; r < 3; r++) {
+    const int S = MARCH_ROWS[r];
+    std::vector<int2> t;
+    for (int i = 0; i < n; i++) {
+      const int nbx = (members[i]->nx + ti - 1) / ti, nrg = (members[i]->ny + S - 1) / S;
+      for (int rg = 0; rg < nrg; rg++)
+        for (int bx = 0; bx < nbx; bx++) t.push_back(make_int2(i, (bx << 16) | rg));
+    }
+    e->ntiles[r] = (int)t.size();
+    if (cudaMalloc((void **)&e->tiles[r], t.size() * sizeof(int2)) != cudaSuccess ||
+        cudaMemcpy(e->tiles[r], t.data(), t.size() * sizeof(int2), cudaMemcpyHostToDevice) != cudaSuccess) {
+      set_error("swm_gpu_ensemble_create: tile list upload failed");
+      return fail(SWM_GPU_ENOMEM);
+    }
+  }
+  if (cudaMalloc((void **)&e->tab, tab.size() * sizeof(P32)) != cudaSuccess ||
+      cudaMemcpy(e->tab, tab.data(), tab.size() * sizeof(P32), cudaMemcpyHostToDevice) != cudaSuccess ||
+      cudaMalloc((void **)&e->next, ENS_PHASES * sizeof(int)) != cudaSuccess ||
+      cudaMalloc((void **)&e->d_int, n * sizeof(EnsInt)) != cudaSuccess ||
+      cudaMalloc((void **)&e->d_out, 3 * (size_t)n * sizeof(double)) != cudaSuccess) {
+    set_error("swm_gpu_ensemble_create: device allocation failed");
+    return fail(SWM_GPU_ENOMEM);
+  }
+  // strip rows by timing the ensemble step at the current phase (the step
+  // rewrites level N0p1 and slot 3 only, which the first real step rewrites)
+  if (join_members(e) != SWM_GPU_OK) return fail(SWM_GPU_ECUDA);
+  int best = 16;
+  int rc = march_pick_rows(e->stream, 3, [&](int r) {
+    const int ri = rows_index(r);
+    cudaMemsetAsync(e->next, 0, sizeof(int), e->stream);
+    march_ens_launch(mix, r, e->tab, e->tiles[ri], e->ntiles[ri], e->next, e->stream);
+  }, &best);
+  if (rc != SWM_GPU_OK) return fail(rc);
+  e->rows = best;
+  if (release_members(e) != SWM_GPU_OK) return fail(SWM_GPU_ECUDA);
+  *out = e;
+  return SWM_GPU_OK;
+}
+
+int swm_gpu_ensemble_destroy(swm_gpu_ensemble *e) {
+  if (e) ens_free(e);
+  return SWM_GPU_OK;
+}
+
+int swm_gpu_ensemble_run(swm_gpu_ensemble *e, int64_t itt0, int64_t nsteps) {
+  SWM_REQUIRE(e && nsteps >= 0, "swm_gpu_ensemble_run: bad arguments");
+  int64_t s = 1;
+  // Adams-Bashforth start-up steps (itt 1, 2): each member on its own stream
+  for (; s <= nsteps && itt0 + s < 3; s++) {
+    for (auto *c : e->m) {
+      int rc = swm_gpu_step(c, itt0 + s);
+      if (rc == SWM_GPU_OK) rc = swm_gpu_advance(c, itt0 + s);
+      if (rc != SWM_GPU_OK) return rc;
+    }
+    e->phase = (e->phase + 1) % ENS_PHASES;
+  }
+  if (s > nsteps) return SWM_GPU_OK;
+  int rc = join_members(e);
+  if (rc != SWM_GPU_OK) return rc;
+  while (s <= nsteps) {
+    const int64_t itt = itt0 + s;
+    if (nsteps - s + 1 >= ENS_PHASES) {
+      if (!e->graph) {
+        rc = ens_capture(e, itt - 1);
+        if (rc != SWM_GPU_OK) return rc;
+      }
+      if (e->phase == e->graph_phase) {
+        SWM_CK(cudaGraphLaunch(e->graph, e->stream));
+        e->launches += e->graph_launches;
+        s += ENS_PHASES;
+        continue;
+      }
+    }
+    rc = ens_step(e, itt);
+    if (rc != SWM_GPU_OK) return rc;
+    s++;
+  }
+  rc = release_members(e);
+  if (rc != SWM_GPU_OK) return rc;
+  SWM_CK(cudaGetLastError());
+  return SWM_GPU_OK;
+}
+
+int swm_gpu_ensemble_integrals(swm_gpu_ensemble *e, double *out) {
+  SWM_REQUIRE(e && out, "swm_gpu_ensemble_integrals: bad arguments");
+  const size_t n = e->m.size();
+  std::vector<EnsInt> d(n);
+  for (size_t i = 0; i < n; i++) {
+    swm_gpu_ctx *c = e->m[i];
+    const float *lv[6];
+    fused_pair_level(c, lv);
+    EnsInt &q = d[i];
+    q.uh = lv[0]; q.ul = lv[1]; q.vh = lv[2]; q.vl = lv[3]; q.eh = lv[4]; q.el = lv[5];
+    q.oU = c->d_ocean[GU]; q.oV = c->d_ocean[GV]; q.oE = c->d_ocean[GE];
+    q.cU = c->d_cos[GU]; q.cE = c->d_cos[GE];
+    q.nx = c->nx; q.ny = c->ny;
+    q.A2dLdT = c->cfg.A * c->cfg.A * c->hg.dLambda * c->hg.dTheta;
+    q.G = c->cfg.G;
+  }
+  int rc = join_members(e);
+  if (rc != SWM_GPU_OK) return rc;
+  SWM_CK(cudaMemcpyAsync(e->d_int, d.data(), n * sizeof(EnsInt), cudaMemcpyHostToDevice, e->stream));
+  k_ens_integrals<<<(unsigned)n, 256, 0, e->stream>>>(e->d_int, e->d_out);
+  e->launches++;
+  SWM_CK(cudaGetLastError());
+  SWM_CK(cudaMemcpyAsync(out, e->d_out, 3 * n * sizeof(double), cudaMemcpyDeviceToHost, e->stream));
+  SWM_CK(cudaStreamSynchronize(e->stream));
+  return SWM_GPU_OK;
+}
+
+int swm_gpu_ensemble_synchronize(swm_gpu_ensemble *e) {
+  SWM_REQUIRE(e, "swm_gpu_ensemble_synchronize: null ensemble");
+  SWM_CK(cudaStreamSynchronize(e->stream));
+  return SWM_GPU_OK;
+}
+
+void *swm_gpu_ensemble_stream(swm_gpu_ensemble *e) { return e ? (void *)e->stream : nullptr; }
+
+int64_t swm_gpu_ensemble_launch_count(swm_gpu_ensemble *e) { return e ? e->launches : -1; }
+
+int swm_gpu_ensemble_rows(swm_gpu_ensemble *e) { return e ? e->rows : 0; }
+
+}  // extern "C"

@@ -26,6 +26,7 @@
 #include <cstring>
 #include <vector>
 #include "ctx.h"
+#include "fused32.h"
 
 namespace swm {
 
@@ -519,7 +520,16 @@ int fused_prepare(swm_gpu_ctx *c) {
     }
   }
   f->ready = true;
-  return fused_load_state(c);
+  FTRY(fused_load_state(c));
+  if (f32 && !c->march_rows) {
+    // rows per warp strip, by timing the step on this basin (the repeated
+    // step rewrites level N0p1 and slot 3 only, which the first real step
+    // rewrites again)
+    P32 p;
+    make_p32(c, 3, p);
+    FTRY(march_autotune(c, p));
+  }
+  return SWM_GPU_OK;
 }
 
 // FP64 state and increments -> FP32 pair buffers (FP32C path)
@@ -588,7 +598,9 @@ static void fill_common(swm_gpu_ctx *c, FP<T> &p, int64_t itt) {
   p.ab1 = (T)tab[tstep][1];
   p.ab2 = (T)tab[tstep][2];
   p.dt = (T)cf.dt;
-  p.G = (T)cf.G;
+  // without a linearisation define EDens stays 0: no pressure gradient
+  // (swm_nonlinear_timestep_module.f90:291-305)
+  p.G = cf.mode == SWM_MODE_NONE ? (T)0 : (T)cf.G;
   p.minD = (T)cf.minD;
   p.lbc = (T)cf.lbc;
   p.q1 = (T)(1. / (cf.A * c->hg.dTheta));
@@ -620,14 +632,12 @@ static void launch_fused(swm_gpu_ctx *c, const FP<T> &p) {
   c->launches++;
 }
 
-}  // namespace swm
-#include "fused32.h"
-namespace swm {
 
-static void launch_fp32c(swm_gpu_ctx *c, int64_t itt) {
+// parameter block of the FP32 step kernel for step itt from the context's
+// current level and ring offsets
+void make_p32(const swm_gpu_ctx *c, int64_t itt, P32 &p) {
   const swm_gpu_config &cf = c->cfg;
-  FusedState *f = c->fused;
-  P32 p;
+  const FusedState *f = c->fused;
   memset(&p, 0, sizeof(p));
   p.nx = c->nx;
   p.ny = c->ny;
@@ -649,7 +659,7 @@ static void launch_fp32c(swm_gpu_ctx *c, int64_t itt) {
   p.ab1 = (float)tab[tstep][1];
   p.ab2 = (float)tab[tstep][2];
   p.dt = (float)cf.dt;
-  p.G = (float)cf.G;
+  p.G = cf.mode == SWM_MODE_NONE ? 0.f : (float)cf.G;  // EDens stays 0 without a mode define
   p.minD = (float)cf.minD;
   p.lbc = (float)cf.lbc;
   p.q1 = (float)(1. / (cf.A * c->hg.dTheta));
@@ -681,6 +691,26 @@ static void launch_fp32c(swm_gpu_ctx *c, int64_t itt) {
   p.Gu1 = f->Gu[s0]; p.Gu2 = f->Gu[s1]; p.Gu3 = f->Gu[s2];
   p.Gv1 = f->Gv[s0]; p.Gv2 = f->Gv[s1]; p.Gv3 = f->Gv[s2];
   p.Ge1 = f->Ge[s0]; p.Ge2 = f->Ge[s1]; p.Ge3 = f->Ge[s2];
+}
+
+// the FP32 pair state: level and ring offsets, and the current level's arrays
+void fused_indices(const swm_gpu_ctx *c, int *n0, int *g0) {
+  *n0 = c->fused ? c->fused->n0 : 0;
+  *g0 = c->fused ? c->fused->g0 : 0;
+}
+void fused_set_indices(swm_gpu_ctx *c, int n0, int g0) {
+  c->fused->n0 = n0;
+  c->fused->g0 = g0;
+}
+void fused_pair_level(const swm_gpu_ctx *c, const float *out[6]) {
+  const FusedState *f = c->fused;
+  int a = f->n0;
+  out[0] = f->uh[a]; out[1] = f->ul[a]; out[2] = f->vh[a]; out[3] = f->vl[a]; out[4] = f->eh[a]; out[5] = f->el[a];
+}
+
+static void launch_fp32c(swm_gpu_ctx *c, int64_t itt) {
+  P32 p;
+  make_p32(c, itt, p);
   march_launch(c, p);
 }
 
@@ -790,11 +820,27 @@ __global__ void k_rows_f32(const double *rows, float *dst, int ny) {
 
 }  // namespace swm
 
+// scratch of swm_gpu_integrals, owned by its context (allocated on the first
+// call, freed with the context)
 struct IntegralScratch {
-  double *area_u = nullptr, *area_e = nullptr, *partial = nullptr, *out = nullptr, *rows = nullptr;
+  double *area_u = nullptr, *area_e = nullptr, *partial = nullptr, *out = nullptr;
   double *host = nullptr;  // pinned
   int nb = 0;
 };
+
+namespace swm {
+void integrals_free(swm_gpu_ctx *c) {
+  IntegralScratch *S = c->integrals;
+  if (!S) return;
+  cudaFree(S->area_u);
+  cudaFree(S->area_e);
+  cudaFree(S->partial);
+  cudaFree(S->out);
+  cudaFreeHost(S->host);
+  delete S;
+  c->integrals = nullptr;
+}
+}  // namespace swm
 
 extern "C" {
 
@@ -831,13 +877,9 @@ int swm_gpu_set_stream_rows(swm_gpu_ctx *c, int id, const double *r1, const doub
 
 int swm_gpu_integrals(swm_gpu_ctx *c, double *out3) {
   SWM_REQUIRE(c && c->stage >= 5 && out3, "swm_gpu_integrals: bad arguments");
-  static thread_local std::vector<std::pair<swm_gpu_ctx *, IntegralScratch>> cache;
-  IntegralScratch *S = nullptr;
-  for (auto &e : cache)
-    if (e.first == c) S = &e.second;
+  IntegralScratch *S = c->integrals;
   if (!S) {
-    cache.emplace_back(c, IntegralScratch());
-    S = &cache.back().second;
+    S = c->integrals = new IntegralScratch();
     const HostGrid &g = c->hg;
     std::vector<double> au(c->ny), ae(c->ny);
     double A = c->cfg.A;

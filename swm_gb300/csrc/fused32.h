@@ -1,5 +1,6 @@
 // fused32.h -- parameter block of the FP32 compensated step kernel (march.cu).
 #pragma once
+#include <functional>
 #include <vector>
 #include "ctx.h"
 
@@ -28,7 +29,21 @@ struct P32 {
   float *Gu3, *Gv3, *Ge3;
 };
 
+// candidate rows per warp strip of the step kernel
+constexpr int MARCH_ROWS[3] = {8, 16, 32};
+
 std::vector<double> fp32c_rows(const swm_gpu_ctx *c);
+void make_p32(const swm_gpu_ctx *c, int64_t itt, P32 &p);
 void march_launch(swm_gpu_ctx *c, const P32 &p);
+int march_tile_cols(int mix);          // columns a warp strip updates
+int march_rows_override();             // SWM_GB300_MARCH_S, 0 when unset
+int march_pick_rows(cudaStream_t st, int reps, const std::function<void(int)> &launch, int *best);
+int march_autotune(swm_gpu_ctx *c, const P32 &p);
+void fused_indices(const swm_gpu_ctx *c, int *n0, int *g0);
+void fused_set_indices(swm_gpu_ctx *c, int n0, int g0);
+void fused_pair_level(const swm_gpu_ctx *c, const float *out[6]);
+// one launch of the ensemble step: tiles {member, strip << 16 | row group}
+int march_ens_launch(int mix, int rows, const P32 *tab, const int2 *tiles, int ntiles, int *next,
+                     cudaStream_t st);
 
 }  // namespace swm

@@ -59,15 +59,14 @@ __device__ __forceinline__ void comp_damp(float hi, float lo, float inc, float d
   nl = e - (nh - t);
 }
 
+// One warp updates rows ry0 .. ry0+S-1 of strip bx (columns bx*TI ..
+// bx*TI+TI-1) of the basin p describes.
 template <int MIX, int S>
-__global__ void __launch_bounds__(128) k_march(P32 p) {
+__device__ __forceinline__ void march_strip(const P32 &p, const int bx, const int ry0, const int lane) {
   constexpr int H = MIX == 2 ? 2 : 1;
   constexpr int TI = 32 - 2 * H;
-  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
   const int nx = p.nx, ny = p.ny;
-  const int ry0 = (blockIdx.y * 4 + warp) * S;
-  if (ry0 >= ny) return;  // whole warp leaves together
-  const int gx = blockIdx.x * TI - H + lane;
+  const int gx = bx * TI - H + lane;
   const int gi = wrapm(gx, nx);
   const bool nl = p.nl;
   const bool store_lane = lane >= H && lane < 32 - H && gx < nx;
@@ -387,6 +386,38 @@ __global__ void __launch_bounds__(128) k_march(P32 p) {
   }
 }
 
+template <int MIX, int S>
+__global__ void __launch_bounds__(128) k_march(P32 p) {
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  const int ry0 = (blockIdx.y * 4 + warp) * S;
+  if (ry0 >= p.ny) return;  // whole warp leaves together
+  march_strip<MIX, S>(p, blockIdx.x, ry0, lane);
+}
+
+// Ensemble of basins in one persistent launch: every warp takes (member,
+// strip, row group) tiles from the queue until it is empty.  A tile is
+// int2 {member, strip << 16 | row group}; the member's parameter block is
+// copied into the warp's slice of shared memory first.
+template <int MIX, int S>
+__global__ void __launch_bounds__(128) k_march_ens(const P32 *__restrict__ tab, const int2 *__restrict__ tiles,
+                                                   int ntiles, int *__restrict__ next) {
+  __shared__ P32 sp[4];
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  for (;;) {
+    int t = 0;
+    if (lane == 0) t = atomicAdd(next, 1);
+    t = __shfl_sync(FULL, t, 0);
+    if (t >= ntiles) return;
+    const int2 d = tiles[t];
+    const int *src = reinterpret_cast<const int *>(tab + d.x);
+    int *dst = reinterpret_cast<int *>(&sp[warp]);
+    for (int k = lane; k < (int)(sizeof(P32) / sizeof(int)); k += 32) dst[k] = src[k];
+    __syncwarp();
+    march_strip<MIX, S>(sp[warp], d.y >> 16, (d.y & 0xffff) * S, lane);
+    __syncwarp();
+  }
+}
+
 // per-row factors for the FP32 kernel
 std::vector<double> fp32c_rows(const swm_gpu_ctx *c) {
   const HostGrid &g = c->hg;
@@ -418,33 +449,113 @@ std::vector<double> fp32c_rows(const swm_gpu_ctx *c) {
   return rows;
 }
 
+int march_tile_cols(int mix) { return 32 - 2 * (mix == 2 ? 2 : 1); }
+
 // rows per warp strip: longer strips recompute fewer look-ahead rows, shorter
-// ones give more warps; SWM_GB300_MARCH_S (8, 16 or 32) overrides the default
+// ones give more warps.  One of MARCH_ROWS, picked by timing (march_autotune)
+// unless SWM_GB300_MARCH_S names one.
 template <int MIX, int S>
-static void launch_s(swm_gpu_ctx *c, const P32 &p) {
-  int H = MIX == 2 ? 2 : 1;
-  int ti = 32 - 2 * H;
-  dim3 grid((c->nx + ti - 1) / ti, (c->ny + 4 * S - 1) / (4 * S));
-  k_march<MIX, S><<<grid, 128, 0, c->stream>>>(p);
+static void launch_s(const P32 &p, cudaStream_t st) {
+  const int ti = march_tile_cols(MIX);
+  dim3 grid((p.nx + ti - 1) / ti, (p.ny + 4 * S - 1) / (4 * S));
+  k_march<MIX, S><<<grid, 128, 0, st>>>(p);
 }
 
 template <int MIX>
-static void launch_mix(swm_gpu_ctx *c, const P32 &p, int s) {
-  if (s == 8) launch_s<MIX, 8>(c, p);
-  else if (s == 32) launch_s<MIX, 32>(c, p);
-  else launch_s<MIX, 16>(c, p);
+static void launch_mix(const P32 &p, int s, cudaStream_t st) {
+  if (s == 8) launch_s<MIX, 8>(p, st);
+  else if (s == 32) launch_s<MIX, 32>(p, st);
+  else launch_s<MIX, 16>(p, st);
+}
+
+static void launch_any(const P32 &p, int s, cudaStream_t st) {
+  if (p.mix == 2) launch_mix<2>(p, s, st);
+  else if (p.mix == 1) launch_mix<1>(p, s, st);
+  else launch_mix<0>(p, s, st);
+}
+
+int march_rows_override() {
+  const char *e = getenv("SWM_GB300_MARCH_S");
+  if (!e) return 0;
+  int s = atoi(e);
+  for (int r : MARCH_ROWS)
+    if (r == s) return s;
+  return 0;
 }
 
 void march_launch(swm_gpu_ctx *c, const P32 &p) {
-  static int s_rows = -1;
-  if (s_rows < 0) {
-    const char *e = getenv("SWM_GB300_MARCH_S");
-    s_rows = e ? atoi(e) : 16;
-  }
-  if (p.mix == 2) launch_mix<2>(c, p, s_rows);
-  else if (p.mix == 1) launch_mix<1>(c, p, s_rows);
-  else launch_mix<0>(c, p, s_rows);
+  launch_any(p, c->march_rows ? c->march_rows : 16, c->stream);
   c->launches++;
+}
+
+// Mean time of `reps` launches per candidate; the step reads level n0 and
+// slots 1-2 and writes level n0p1 and slot 3 only, so repeating it leaves
+// the model state as one launch leaves it.
+int march_pick_rows(cudaStream_t st, int reps, const std::function<void(int)> &launch, int *best) {
+  int s = march_rows_override();
+  if (s) {
+    *best = s;
+    return SWM_GPU_OK;
+  }
+  cudaEvent_t a, b;
+  SWM_CK(cudaEventCreate(&a));
+  SWM_CK(cudaEventCreate(&b));
+  float tbest = 1e30f;
+  *best = 16;
+  for (int r : MARCH_ROWS) {
+    launch(r);  // warm-up
+    SWM_CK(cudaEventRecord(a, st));
+    for (int k = 0; k < reps; k++) launch(r);
+    SWM_CK(cudaEventRecord(b, st));
+    SWM_CK(cudaEventSynchronize(b));
+    float ms = 0.f;
+    SWM_CK(cudaEventElapsedTime(&ms, a, b));
+    if (ms < tbest) {
+      tbest = ms;
+      *best = r;
+    }
+  }
+  cudaEventDestroy(a);
+  cudaEventDestroy(b);
+  SWM_CK(cudaGetLastError());
+  return SWM_GPU_OK;
+}
+
+int march_autotune(swm_gpu_ctx *c, const P32 &p) {
+  int s = 16;
+  int rc = march_pick_rows(c->stream, 5, [&](int r) { launch_any(p, r, c->stream); }, &s);
+  if (rc != SWM_GPU_OK) return rc;
+  c->march_rows = s;
+  return SWM_GPU_OK;
+}
+
+// ---- ensemble launch ------------------------------------------------------
+template <int MIX, int S>
+static int ens_launch_s(const P32 *tab, const int2 *tiles, int ntiles, int *next, cudaStream_t st) {
+  static int blocks = 0;
+  if (!blocks) {
+    int per_sm = 0, sms = 0, dev = 0;
+    SWM_CK(cudaGetDevice(&dev));
+    SWM_CK(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
+    SWM_CK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_march_ens<MIX, S>, 128, 0));
+    blocks = sms * (per_sm > 0 ? per_sm : 1);
+  }
+  int need = (ntiles + 3) / 4;
+  k_march_ens<MIX, S><<<need < blocks ? need : blocks, 128, 0, st>>>(tab, tiles, ntiles, next);
+  return SWM_GPU_OK;
+}
+
+template <int MIX>
+static int ens_launch_mix(int s, const P32 *tab, const int2 *tiles, int ntiles, int *next, cudaStream_t st) {
+  if (s == 8) return ens_launch_s<MIX, 8>(tab, tiles, ntiles, next, st);
+  if (s == 32) return ens_launch_s<MIX, 32>(tab, tiles, ntiles, next, st);
+  return ens_launch_s<MIX, 16>(tab, tiles, ntiles, next, st);
+}
+
+int march_ens_launch(int mix, int s, const P32 *tab, const int2 *tiles, int ntiles, int *next, cudaStream_t st) {
+  if (mix == 2) return ens_launch_mix<2>(s, tab, tiles, ntiles, next, st);
+  if (mix == 1) return ens_launch_mix<1>(s, tab, tiles, ntiles, next, st);
+  return ens_launch_mix<0>(s, tab, tiles, ntiles, next, st);
 }
 
 }  // namespace swm

@@ -175,3 +175,47 @@ class GpuModel:
         if rc not in (0, 4):
             check(rc)
         return x, (it.value if rc == 0 else -it.value), an.value
+
+
+class GpuEnsemble:
+    """Members (GpuModel, fused_fp32c, initialised) stepped together by one
+    persistent launch per step (swm_gpu_ensemble_*)."""
+
+    def __init__(self, members):
+        self.L = lib()
+        self.members = list(members)
+        arr = (C.c_void_p * len(self.members))(*[m.ctx for m in self.members])
+        out = C.c_void_p()
+        check(self.L.swm_gpu_ensemble_create(arr, len(self.members), C.byref(out)))
+        self.ens = out
+
+    def close(self):
+        if self.ens:
+            self.L.swm_gpu_ensemble_destroy(self.ens)
+            self.ens = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def run(self, itt0, nsteps):
+        check(self.L.swm_gpu_ensemble_run(self.ens, itt0, nsteps))
+
+    def integrals(self):
+        out = np.zeros((len(self.members), 3))
+        check(self.L.swm_gpu_ensemble_integrals(self.ens, _p(out)))
+        return out
+
+    def synchronize(self):
+        check(self.L.swm_gpu_ensemble_synchronize(self.ens))
+
+    def stream(self):
+        return self.L.swm_gpu_ensemble_stream(self.ens)
+
+    def launch_count(self):
+        return self.L.swm_gpu_ensemble_launch_count(self.ens)
+
+    def rows(self):
+        return self.L.swm_gpu_ensemble_rows(self.ens)

@@ -1,0 +1,101 @@
+"""Batched ensemble of uneven basins (swm_gpu_ensemble_*): the persistent
+queue kernel against the same members stepped one at a time on the
+single-basin FP32 path, and against the FP64 oracle.
+
+The batched kernel reads each member's parameters from shared memory, the
+single-basin kernel from its launch parameters; the two are compiled
+separately and the compiler may fuse different multiply-adds, so they agree
+to binary32 rounding (about 1e-7 relative after tens of steps), not bit for
+bit.  The strip length does not change either kernel's results."""
+import math
+
+import numpy as np
+import pytest
+
+from harness import rel_l2
+from oracle import OracleBackend
+from swm_gb300 import SwmGpuError
+from swm_gb300.host import synthetic
+from swm_gb300.host.driver import Driver
+from swm_gb300.model import GpuEnsemble, GpuModel
+
+pytestmark = pytest.mark.gpu
+
+
+def _cases(n, biharmonic=False, lo=20, hi=90, seed=11):
+    rng = np.random.Generator(np.random.PCG64(seed))
+    out = []
+    for _ in range(n):
+        cx = int(round(math.exp(rng.uniform(math.log(lo), math.log(hi)))))
+        cy = int(round(math.exp(rng.uniform(math.log(lo), math.log(hi)))))
+        dx = rng.uniform(5e3, 20e3)
+        out.append(synthetic.double_gyre((cx, cy), biharmonic=biharmonic, dx=dx, amp=rng.uniform(0.05, 0.2),
+                                         ah=500.0, rng=rng, nsteps=500, dt=15.0 * dx / 5e3))
+    return out
+
+
+def _models(cases, path='fused_fp32c'):
+    ms = []
+    for c in cases:
+        g = GpuModel(path)
+        Driver(c, g).init(with_diag=False)
+        ms.append(g)
+    return ms
+
+
+@pytest.mark.parametrize('biharmonic', [False, True])
+def test_ensemble_matches_members_stepped_alone(biharmonic):
+    cases = _cases(12, biharmonic=biharmonic)
+    batched, alone = _models(cases), _models(cases)
+    ens = GpuEnsemble(batched)
+    assert ens.rows() in (8, 16, 32)
+    itt = 0
+    for n in (40, 17, 12):  # start-up steps, graph blocks and single steps
+        ens.run(itt, n)
+        for g in alone:
+            g.run(itt, n)
+        itt += n
+        for a, b in zip(batched, alone):
+            for f in ('u', 'v', 'eta'):
+                x, y = a.field(f), b.field(f)
+                assert np.isfinite(x).all()
+                assert np.abs(x - y).max() <= 1e-6 * max(np.abs(y).max(), 1e-30), (n, f)
+    ints = ens.integrals()
+    for k, b in enumerate(alone):
+        # potential and kinetic energy; the volume anomaly is a sum that
+        # cancels to ~0 and has no relative precision
+        np.testing.assert_allclose(ints[k][1:], b.integrals()[1:], rtol=1e-6)
+    assert (ints[:, 1] > 0).all()
+    ens.close()
+
+
+def test_ensemble_against_fp64_oracle():
+    cases = _cases(3, lo=30, hi=60, seed=5)
+    ms = _models(cases)
+    ens = GpuEnsemble(ms)
+    ens.run(0, 200)
+    for c, g in zip(cases, ms):
+        o = OracleBackend()
+        d = Driver(c, o)
+        d.init(with_diag=False)
+        d.run(200, with_diag=False)
+        for f in ('u', 'v', 'eta'):
+            m = o.ocean(f).astype(bool)
+            assert rel_l2(g.field(f), o.field(f), m) <= 1e-5, f
+
+
+def test_ensemble_one_launch_per_step():
+    ms = _models(_cases(5))
+    ens = GpuEnsemble(ms)
+    ens.run(0, 5)
+    l0 = ens.launch_count()
+    ens.run(5, 24)
+    ens.synchronize()
+    assert ens.launch_count() - l0 == 24
+
+
+def test_ensemble_rejects_other_paths():
+    cases = _cases(2)
+    ms = _models(cases[:1]) + _models(cases[1:], path='plain_fp64')
+    with pytest.raises(SwmGpuError):
+        GpuEnsemble(ms)

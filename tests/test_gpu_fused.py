@@ -24,6 +24,11 @@ def _case(variant, nsteps):
     if variant == 'linear_rg':
         return synthetic.linear_rg(48, 32, nsteps=nsteps)
     case = synthetic.double_gyre((64, 48), biharmonic=(variant == 'biharmonic'), nsteps=nsteps)
+    if variant == 'no_mode':
+        # neither FULLY_NONLINEAR nor a LINEARISED define: no pressure
+        # gradient and no Coriolis term (Pot and EDens stay 0)
+        case['config'].update(mode=0)
+        case['ic'] = {'eta': 0.05 * np.ones(case['H'].shape)}
     if variant == 'laplace_qbf':
         case['config'].update(quadratic_friction=1, barotropic=1)
         case['damping'] += [dict(term=3, type=0, value=2e-3, sl_length=1.0, sl_cutoff=15.0, loc=0, file_data=None),
@@ -32,7 +37,7 @@ def _case(variant, nsteps):
 
 
 @pytest.mark.parametrize('path', ['fused_fp64', 'fused_fp32c'])
-@pytest.mark.parametrize('variant', ['biharmonic', 'laplace', 'laplace_qbf', 'linear_rg'])
+@pytest.mark.parametrize('variant', ['biharmonic', 'laplace', 'laplace_qbf', 'linear_rg', 'no_mode'])
 def test_fused_vs_oracle(path, variant):
     nsteps = 300
     case = _case(variant, nsteps)
