@@ -45,6 +45,8 @@ def parse():
     ap.add_argument('--quick', action='store_true', help='skip the side measurements')
     ap.add_argument('--device-only', action='store_true',
                     help='only the warm-up and timed device steps (the form to run under ncu)')
+    ap.add_argument('--workload', default='double_gyre', choices=['double_gyre', 'ensemble', 'tracer'],
+                    help='ensemble / tracer: print that measurement alone (profiling)')
     return ap.parse_args()
 
 
@@ -231,6 +233,7 @@ def ours(args, rank, ws):
         line.update(side_measurements(args, case, g, stream, flush, ncell))
         line['speedup_vs_fp64_plain'] = line['plain_fp64']['ms_per_step'] / step_ms
         line['ensemble'] = ensemble_measurement(args)
+        line['tracer'] = tracer_measurement(args)
     if rank == 0 and ws == 1 and not args.quick:
         line['cpu_baseline'] = cpu_baseline(cells)
     g.close()
@@ -278,7 +281,7 @@ def side_measurements(args, case, g32, stream, flush, ncell):
     return out
 
 
-def ensemble_measurement(args, n_members=256, steps=200):
+def ensemble_measurement(args, n_members=256, steps=200, one_by_one=True):
     """The batched FP32 path on 256 basins of uneven sizes (Nx, Ny
     log-uniform in 64-512, Laplacian Ah = 500), against the same members
     stepped one by one on the FP64 plain path."""
@@ -315,10 +318,12 @@ def ensemble_measurement(args, n_members=256, steps=200):
     peak, kind = peaks()
     ach = 89 * pts / (ms_step * 1e-3) / 1e9
     out['roofline'] = {'bound': 'hbm', 'achieved': ach, 'peak': peak, 'unit': 'GB/s', 'frac': ach / peak,
-                       'peak_kind': kind, 'kernel': 'k_march_ens<1,%d>' % ens.rows()}
+                       'peak_kind': kind, 'kernel': 'k_march_ens<1,%d>' % ens.rows(), 'bytes_per_point': 89}
     ens.close()
     for g in ms:
         g.close()
+    if not one_by_one:
+        return out
     # the same members one by one on the FP64 plain path (3 steps each, after start-up)
     tot = 0.0
     for c in cases:
@@ -334,6 +339,64 @@ def ensemble_measurement(args, n_members=256, steps=200):
     out['plain_fp64_one_by_one'] = {'ms_per_step': tot * 1e3, 'value': cells / tot, 'unit': 'cell-steps/s',
                                     'timing': 'wall clock per member, summed'}
     out['speedup_vs_plain_fp64_one_by_one'] = tot * 1e3 / ms_step
+    return out
+
+
+def tracer_measurement(args, cells=2048, steps=200, err_steps=1000):
+    """Two tracers in a steady nondivergent flow (2048^2 cells at 2.5 km,
+    upwind-biased flux, kappa = 50, 30-day relaxation, dt = 60 s) on the FP32
+    compensated tracer kernel; error and tracer-mass drift against the FP64
+    plain tracer kernels (bit-exact with the oracle) after err_steps."""
+    import torch
+    from swm_gb300.host import synthetic
+    from swm_gb300.host.driver import Driver
+    from swm_gb300.model import GpuModel
+    case = synthetic.tracer_flow(cells, nsteps=err_steps + steps + 10)
+    pts = case['config']['nx'] * case['config']['ny']
+    g = GpuModel('fused_fp32c', tracer_nan_guard=True)
+    Driver(case, g).init(with_diag=False)
+    st = torch.cuda.ExternalStream(g.stream())
+    g.run(0, 6)
+    g.synchronize()
+    a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    l0 = g.launch_count()
+    a.record(st)
+    g.run(6, steps)
+    b.record(st)
+    g.synchronize()
+    launches = g.launch_count() - l0
+    ms = a.elapsed_time(b) / steps
+    bpp = 78  # per point: u, v, H, mask 14 B; per tracer CH pair r/w 16, increments r2/w1 12, C0 4
+    peak, kind = peaks()
+    ach = bpp * pts / (ms * 1e-3) / 1e9
+    out = {'workload': 'tracer_flow_%dx%d_2tracers_upwind_biased' % (cells, cells), 'cells': cells * cells,
+           'array_points': pts, 'steps': steps, 'ms_per_step': ms, 'value': cells * cells / (ms * 1e-3),
+           'unit': 'cell-steps/s', 'gpu_launches': launches,
+           'l2': 'not flushed: the tracer state (%.0f MB) is larger than L2' % (bpp * pts / 1e6),
+           'roofline': {'bound': 'hbm', 'achieved': ach, 'peak': peak, 'unit': 'GB/s', 'frac': ach / peak,
+                        'peak_kind': kind, 'kernel': 'k_trc32', 'bytes_per_point': bpp}}
+    g.close()
+    if err_steps <= 0:
+        return out
+    # accuracy and mass drift against the FP64 tracer kernels from the same start
+    cos = None
+    res = {}
+    for path in ('fused_fp32c', 'plain_fp64'):
+        m = GpuModel(path, tracer_nan_guard=True)
+        Driver(case, m).init(with_diag=False)
+        if cos is None:
+            cos = m.lat('cos_eta')[:, None]
+            ocean = m.ocean('eta').astype(bool)
+        mass0 = [float((m.tracer_field(t, 'CH') * cos).sum()) for t in range(2)]
+        m.run(0, err_steps)
+        ch = [m.tracer_field(t, 'CH') for t in range(2)]
+        res[path] = (ch, [float((c * cos).sum()) / m0 - 1.0 for c, m0 in zip(ch, mass0)])
+        m.close()
+    errs = [float(np.linalg.norm((res['fused_fp32c'][0][t] - res['plain_fp64'][0][t])[ocean]) /
+                  np.linalg.norm(res['plain_fp64'][0][t][ocean])) for t in range(2)]
+    out['fp32c_error_vs_fp64'] = {'steps': err_steps, 'rel_l2_CH': errs}
+    out['mass_change'] = {'steps': err_steps, 'fp32c': res['fused_fp32c'][1], 'fp64': res['plain_fp64'][1],
+                          'note': 'relative change of sum(CH*cos) over the run (relaxation changes it too)'}
     return out
 
 
@@ -386,6 +449,16 @@ def reference(args, rank, ws):
 
 def main():
     args = parse()
+    if args.workload != 'double_gyre':
+        import torch
+        torch.cuda.set_device(0)
+        if args.workload == 'tracer':
+            out = tracer_measurement(args, cells=args.cells, steps=args.steps,
+                                     err_steps=0 if args.device_only else 1000)
+        else:
+            out = ensemble_measurement(args, steps=args.steps, one_by_one=not args.device_only)
+        print(json.dumps(out))
+        return
     rank, ws = dist_setup(args)
     line = reference(args, rank, ws) if args.impl == 'reference' else ours(args, rank, ws)
     if rank == 0 and line is not None:

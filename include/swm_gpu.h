@@ -58,6 +58,10 @@ typedef struct swm_gpu_config {
   int32_t tracer_nan_guard;     /* 1: 0/0 tracer coefficients taken as 0           */
   int32_t damping_additive;     /* 1: damping entries add (older selfcheck build)  */
   int32_t mask_psi_bs;          /* 1: basic-state psi zeroed on land (same)        */
+  int32_t tracer_flux;          /* 0: reference centred tracer flux; 1: third-order
+                                   upwind-biased flux (extension)                  */
+  int32_t frozen_flow;          /* 1: SWM state held fixed after the initial
+                                   conditions, only tracers step (extension)      */
   double dt, G, Ah, A, OMEGA, RHO0, lbc, theta0;
   double lon_s, lon_e, lat_s, lat_e;
   double H_overwrite;           /* 0 = unset                                       */

@@ -28,7 +28,8 @@ TRC_FIELDS = ['CH0', 'CH1', 'G1', 'G2', 'G3', 'C', 'C0', 'gamma', 'impl', 'uhc',
 class Config(C.Structure):
     _fields_ = [(n, C.c_int32) for n in ('nx', 'ny', 'mode', 'lateral_mixing', 'quadratic_friction',
                                           'barotropic', 'mixing_kind', 'coriolis_approx', 'tracer_nan_guard',
-                                          'damping_additive', 'mask_psi_bs')] + \
+                                          'damping_additive', 'mask_psi_bs', 'tracer_flux',
+                                          'frozen_flow')] + \
                [(n, C.c_double) for n in ('dt', 'G', 'Ah', 'A', 'OMEGA', 'RHO0', 'lbc', 'theta0', 'lon_s',
                                           'lon_e', 'lat_s', 'lat_e', 'H_overwrite', 'ab_chi', 'minD',
                                           'tau_scale', 'bih')]

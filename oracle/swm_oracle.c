@@ -562,6 +562,7 @@ static void timestep_nonlinear(orc_model *m) {
 
 /* SWM_timestep -> SWM_timestep_step: swm_nonlinear_timestep_module.f90:164-180 */
 void orc_swm_timestep(orc_model *m) {
+  if (m->c.frozen_flow) return; /* prescribed flow: nothing to step */
   if (m->c.lateral_mixing) latmix_step(m);
   timestep_nonlinear(m);
   if (m->c.mode == ORC_MODE_NONLINEAR) {
@@ -609,7 +610,6 @@ void orc_forcing_set_data(orc_model *m, int id, const double *d1, const double *
 /* SWM_forcing_processInputStream and the per-type routines :222-552 */
 static void process_stream(orc_model *m, orc_stream *s) {
   int n = m->n, nx = m->nx, ny = m->ny;
-  double t = m->itt * m->c.dt;
   const int8_t *oU = m->ocean[ORC_OCEAN_U], *oV = m->ocean[ORC_OCEAN_V], *oE = m->ocean[ORC_OCEAN_ETA];
   double *Fx = s->is_const ? m->f[ORC_FX_CONST] : m->f[ORC_FX];
   double *Fy = s->is_const ? m->f[ORC_FY_CONST] : m->f[ORC_FY];
@@ -874,15 +874,21 @@ void orc_initial_conditions(orc_model *m, const double *eta, const double *u, co
 
 /* SWM_advance: swm_module.f90:86-139 */
 void orc_swm_advance(orc_model *m) {
+  /* frozen flow (extension): after the initial advance the state, its
+     diagnostics and the forcing stay as they are */
+  int frozen = m->c.frozen_flow && m->itt > 0;
   size_t b = sizeof(double) * m->n;
-  memcpy(m->f[ORC_ETA0], m->f[ORC_ETA1], b);
-  memcpy(m->f[ORC_U0], m->f[ORC_U1], b);
-  memcpy(m->f[ORC_V0], m->f[ORC_V1], b);
+  if (!frozen) {
+    memcpy(m->f[ORC_ETA0], m->f[ORC_ETA1], b);
+    memcpy(m->f[ORC_U0], m->f[ORC_U1], b);
+    memcpy(m->f[ORC_V0], m->f[ORC_V1], b);
+  }
   for (int k = 0; k < m->n; k++) {
     m->f[ORC_TOT_U][k] = m->f[ORC_TOT_U][k] + m->f[ORC_U0][k];
     m->f[ORC_TOT_V][k] = m->f[ORC_TOT_V][k] + m->f[ORC_V0][k];
     m->f[ORC_TOT_ETA][k] = m->f[ORC_TOT_ETA][k] + m->f[ORC_ETA0][k];
   }
+  if (frozen) return;
   timestep_advance(m);
   orc_forcing_update(m);
 }
@@ -1033,6 +1039,39 @@ void orc_tracer_init(orc_model *m) {
     }
 }
 
+/* Extension: third-order upwind-biased face value of CH between cells L and
+   R (R east or north of L), Lm west/south of L, Rp east/north of R, for the
+   face velocity vel.  Where any of the four cells is land the reference's
+   mask-weighted mean of CH[L] and CH[R] is used (0/0 taken as 0). */
+static double ub3_face(const double *CH, const int8_t *oE, int Lm, int L, int R, int Rp, double vel) {
+  if (oE[Lm] && oE[L] && oE[R] && oE[Rp]) {
+    if (vel >= 0.) return ((-1. * CH[Lm] + 5. * CH[L]) + 2. * CH[R]) / 6.;
+    return ((2. * CH[L] + 5. * CH[R]) - 1. * CH[Rp]) / 6.;
+  }
+  double den = (double)(oE[L] + oE[R]);
+  if (den == 0.) return 0.;
+  return ((double)oE[L] * CH[L] + (double)oE[R] * CH[R]) / den;
+}
+
+/* advective part of GCH with upwind-biased face values (flux form: the
+   same face value enters the two cells it separates) */
+static double ub3_advection(const orc_model *m, const double *CH, const double *u, const double *v, int i, int j) {
+  const int8_t *oE = m->ocean[ORC_OCEAN_ETA], *oU = m->ocean[ORC_OCEAN_U], *oV = m->ocean[ORC_OCEAN_V];
+  const double *cv = m->lat[ORC_COS_V], *ce = m->lat[ORC_COS_ETA];
+  int nx = m->nx;
+  int ip = m->ip1[i], im = m->im1[i], jp = m->jp1[j], jm = m->jm1[j];
+  int k = IDX(i, j);
+  double fe = ub3_face(CH, oE, IDX(im, j), k, IDX(ip, j), IDX(m->ip1[ip], j), u[IDX(ip, j)]);
+  double fw = ub3_face(CH, oE, IDX(m->im1[im], j), IDX(im, j), k, IDX(ip, j), u[k]);
+  double fn = ub3_face(CH, oE, IDX(i, jm), k, IDX(i, jp), IDX(i, m->jp1[jp]), v[IDX(i, jp)]);
+  double fs = ub3_face(CH, oE, IDX(i, m->jm1[jm]), IDX(i, jm), k, IDX(i, jp), v[k]);
+  double rdl = 1. / (m->c.A * m->dLambda * ce[j]), rdt = 1. / (m->c.A * m->dTheta * ce[j]);
+  double ax = -1. * oU[IDX(ip, j)] * u[IDX(ip, j)] * fe + (double)oU[k] * u[k] * fw;
+  double ay = -1. * oV[IDX(i, jp)] * cv[jp] * v[IDX(i, jp)] * fn + (double)oV[k] * cv[j] * v[k] * fs;
+  (void)nx;
+  return ax * rdl + ay * rdt;
+}
+
 /* TRC_tracer_incr (:154-209) + TRC_tracer_integrate (:216-232) */
 void orc_tracer_timestep(orc_model *m) {
   int nx = m->nx, ny = m->ny;
@@ -1058,6 +1097,12 @@ void orc_tracer_timestep(orc_model *m) {
         int k = IDX(i, j);
         const double *c = m->trc_coeff + (size_t)12 * k;
         int ip = IDX(m->ip1[i], j), im = IDX(m->im1[i], j), jp = IDX(i, m->jp1[j]), jm = IDX(i, m->jm1[j]);
+        if (m->c.tracer_flux == 1) {
+          GCH[k] = oE[k] ? (ub3_advection(m, CH, u, v, i, j) + T->diff[k] -
+                            T->gamma_c[k] * h[k] * (C[k] - T->C0[k]) + T->forcing[k])
+                         : 0.;
+          continue;
+        }
         GCH[k] = (CH[ip] * u[ip] * c[0] + CH[im] * u[k] * c[1] + CH[jp] * v[jp] * c[2] + CH[jm] * v[k] * c[3] +
                   CH[k] * u[ip] * c[4] + CH[k] * u[k] * c[5] + CH[k] * v[jp] * c[6] + CH[k] * v[k] * c[7] +
                   T->diff[k] - T->gamma_c[k] * h[k] * (C[k] - T->C0[k]) + T->forcing[k]);
@@ -1074,7 +1119,10 @@ void orc_tracer_advance(orc_model *m) {
     orc_tracer *T = &m->trc[t];
     memcpy(T->G[0], T->G[1], b); memcpy(T->G[1], T->G[2], b);
     memcpy(T->CH[0], T->CH[1], b);
-    for (int k = 0; k < m->n; k++) T->C[k] = T->CH[0][k] / m->D[k];
+    /* C = CH / h divides 0/0 on land where h = 0 (linear modes); the guard
+       extension takes it as 0 there */
+    for (int k = 0; k < m->n; k++)
+      T->C[k] = (m->c.tracer_nan_guard && m->D[k] == 0.) ? 0. : T->CH[0][k] / m->D[k];
     for (int j = 0; j < ny; j++)
       for (int i = 0; i < nx; i++) {
         int k = IDX(i, j);

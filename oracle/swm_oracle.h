@@ -41,6 +41,8 @@ typedef struct orc_config {
   int32_t tracer_nan_guard;    /* extension: 0/0 tracer coefficients -> 0 */
   int32_t damping_additive;    /* fixture compat: damping entries add up (see orc_damping_add) */
   int32_t mask_psi_bs;         /* fixture compat: basic-state psi zeroed on land H points */
+  int32_t tracer_flux;         /* 0 reference centred flux; 1 third-order upwind-biased (extension) */
+  int32_t frozen_flow;         /* extension: SWM state held fixed, only tracers step */
   double dt, G, Ah, A, OMEGA, RHO0, lbc, theta0;
   double lon_s, lon_e, lat_s, lat_e;
   double H_overwrite;          /* 0 = not set (H_OVERWRITE_DEF)        */

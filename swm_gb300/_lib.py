@@ -10,7 +10,8 @@ HERE = os.path.dirname(os.path.abspath(__file__))
 LIB_PATH = os.path.join(HERE, 'libswm_gb300.so')
 
 CONFIG_INT = ('nx', 'ny', 'mode', 'lateral_mixing', 'quadratic_friction', 'barotropic', 'mixing_kind',
-              'coriolis_approx', 'tracer_nan_guard', 'damping_additive', 'mask_psi_bs')
+              'coriolis_approx', 'tracer_nan_guard', 'damping_additive', 'mask_psi_bs', 'tracer_flux',
+              'frozen_flow')
 CONFIG_DBL = ('dt', 'G', 'Ah', 'A', 'OMEGA', 'RHO0', 'lbc', 'theta0', 'lon_s', 'lon_e', 'lat_s', 'lat_e',
               'H_overwrite', 'ab_chi', 'minD', 'tau_scale', 'bih')
 

@@ -162,6 +162,7 @@ int swm_gpu_destroy(swm_gpu_ctx *c) {
   fused_free(c);
   sor_free(c);
   integrals_free(c);
+  trc32_free(c);
   auto F = [](void *p) { if (p) cudaFree(p); };
   for (int q = 0; q < 4; q++) {
     F(c->d_ocean[q]); F(c->d_cos[q]); F(c->d_tan[q]); F(c->d_f[q]); F(c->d_lat[q]); F(c->d_H[q]);
@@ -341,9 +342,15 @@ int swm_gpu_initial_conditions(swm_gpu_ctx *c, const double *eta, const double *
 }
 
 static int swm_step_impl(swm_gpu_ctx *c, int64_t itt) {
+  // FP32 tracers read the level the SWM step reads, so they go first
+  if (trc32_active(c)) TRY(trc32_step(c, itt));
+  if (c->cfg.frozen_flow) {  // prescribed flow: only the tracers step
+    if (!c->tracers.empty() && !trc32_active(c)) TRY(tracer_step(c, itt));
+    return SWM_GPU_OK;
+  }
   if (c->cfg.path == SWM_PATH_PLAIN_FP64) TRY(plain_step(c, itt));
   else TRY(fused_step(c, itt));
-  if (!c->tracers.empty()) TRY(tracer_step(c, itt));
+  if (!c->tracers.empty() && !trc32_active(c)) TRY(tracer_step(c, itt));
   return SWM_GPU_OK;
 }
 
@@ -352,15 +359,25 @@ static int swm_step_impl(swm_gpu_ctx *c, int64_t itt) {
 // kernel; the FP64 diagnostic arrays are refreshed on demand, or every step
 // when tracers read them)
 static int swm_advance_impl(swm_gpu_ctx *c, int64_t itt) {
+  c->advances++;
+  const bool t32 = trc32_active(c), t64 = !c->tracers.empty() && !t32;
+  if (c->cfg.frozen_flow && itt > 0) {  // state, diagnostics and forcing stay
+    if (t32) trc32_advance(c);
+    if (t64) TRY(tracer_advance(c));
+    return SWM_GPU_OK;
+  }
   c->n0 = 1 - c->n0;
   c->g0 = (c->g0 + 1) % 3;
   bool plain = c->cfg.path == SWM_PATH_PLAIN_FP64 || itt == 0;
-  if (!plain && !c->tracers.empty()) TRY(fused_sync_state(c));
-  if (plain || !c->tracers.empty()) {
+  if (!plain && t64) TRY(fused_sync_state(c));
+  if (plain || t64) {
     TRY(plain_diagnostics(c, itt));
     TRY(plain_forcing_update(c, itt, 0));
   }
-  if (!c->tracers.empty() && itt > 0) TRY(tracer_advance(c));
+  if (itt > 0) {
+    if (t32) trc32_advance(c);
+    if (t64) TRY(tracer_advance(c));
+  }
   return SWM_GPU_OK;
 }
 
@@ -382,7 +399,7 @@ int swm_gpu_advance(swm_gpu_ctx *c, int64_t itt) {
 constexpr int GRAPH_STEPS = 6;
 
 static bool graph_eligible(const swm_gpu_ctx *c) {
-  if (!c->tracers.empty()) return false;
+  if (!c->tracers.empty() && !trc32_active(c)) return false;
   for (const Stream &s : c->streams)
     if (s.type == SWM_FRC_OSC) return false;
   return true;
@@ -393,7 +410,7 @@ static bool graph_eligible(const swm_gpu_ctx *c) {
 static int graph_capture(swm_gpu_ctx *c, int64_t itt0) {
   invalidate_graph(c);
   if (c->cfg.path != SWM_PATH_PLAIN_FP64) TRY(fused_prepare(c));  // allocates on first use
-  const int n0 = c->n0, g0 = c->g0;
+  const int n0 = c->n0, g0 = c->g0, phase = (int)(c->advances % GRAPH_STEPS);
   const int64_t l0 = c->launches;
   SWM_CK(cudaStreamBeginCapture(c->stream, cudaStreamCaptureModeThreadLocal));
   int rc = SWM_GPU_OK;
@@ -420,8 +437,7 @@ static int graph_capture(swm_gpu_ctx *c, int64_t itt0) {
     return SWM_GPU_ECUDA;
   }
   c->graph_launches = nl;
-  c->graph_n0 = n0;
-  c->graph_g0 = g0;
+  c->graph_phase = phase;
   return SWM_GPU_OK;
 }
 
@@ -433,7 +449,7 @@ int swm_gpu_run(swm_gpu_ctx *c, int64_t itt0, int64_t nsteps) {
     const int64_t itt = itt0 + s;
     if (graphs && itt >= 3 && nsteps - s + 1 >= GRAPH_STEPS) {
       if (!c->graph) TRY(graph_capture(c, itt - 1));
-      if (c->n0 == c->graph_n0 && c->g0 == c->graph_g0) {
+      if (c->advances % GRAPH_STEPS == c->graph_phase) {
         SWM_CK(cudaGraphLaunch(c->graph, c->stream));
         c->launches += c->graph_launches;
         s += GRAPH_STEPS;

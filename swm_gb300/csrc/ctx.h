@@ -88,6 +88,7 @@ struct Dev {
 struct FusedState;
 struct SorState;
 struct IntegralScratch;
+struct Trc32State;
 
 struct swm_gpu_ctx {
   swm_gpu_config cfg;
@@ -119,10 +120,12 @@ struct swm_gpu_ctx {
   FusedState *fused = nullptr;
   SorState *sor = nullptr;
   IntegralScratch *integrals = nullptr;
+  Trc32State *trc32 = nullptr;      // tracers of the FP32 compensated path
+  int64_t advances = 0;             // swm_gpu_advance calls (the rotation phase is advances mod 6)
   int march_rows = 0;                // rows per warp strip of the FP32 step kernel (0: not tuned yet)
   cudaGraphExec_t graph = nullptr;  // GRAPH_STEPS captured steps (swm_gpu_run)
   int64_t graph_launches = 0;       // kernels in one replay
-  int graph_n0 = -1, graph_g0 = -1; // level and ring offsets the replay starts from
+  int graph_phase = -1;             // rotation phase (advances mod 6) the replay starts from
   swm::Dev dev() const;
 };
 
@@ -153,6 +156,15 @@ void fused_free(swm_gpu_ctx *c);
 void integrals_free(swm_gpu_ctx *c);
 // sor.cu
 void sor_free(swm_gpu_ctx *c);
+// trc32.cu
+bool trc32_active(const swm_gpu_ctx *c);
+int trc32_add(swm_gpu_ctx *c, const std::vector<double> &CH, const std::vector<double> &C0,
+              const std::vector<double> &gamma, const std::vector<double> &impl, double kappa);
+int trc32_init(swm_gpu_ctx *c);
+int trc32_step(swm_gpu_ctx *c, int64_t itt);
+void trc32_advance(swm_gpu_ctx *c);
+int trc32_export(swm_gpu_ctx *c, int t, int conc, double *dst);
+void trc32_free(swm_gpu_ctx *c);
 }  // namespace swm
 
 #define SWM_LAUNCH_COUNT(c) ((c)->launches++)

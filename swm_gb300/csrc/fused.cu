@@ -702,6 +702,12 @@ void fused_set_indices(swm_gpu_ctx *c, int n0, int g0) {
   c->fused->n0 = n0;
   c->fused->g0 = g0;
 }
+void fused_static(const swm_gpu_ctx *c, const float **He, const uint16_t **mask16, const float **Fe) {
+  const FusedState *f = c->fused;
+  *He = (const float *)f->He;
+  *mask16 = f->mask16;
+  *Fe = f->has_F ? (const float *)f->F[2] : nullptr;
+}
 void fused_pair_level(const swm_gpu_ctx *c, const float *out[6]) {
   const FusedState *f = c->fused;
   int a = f->n0;

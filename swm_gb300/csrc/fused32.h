@@ -42,6 +42,7 @@ int march_autotune(swm_gpu_ctx *c, const P32 &p);
 void fused_indices(const swm_gpu_ctx *c, int *n0, int *g0);
 void fused_set_indices(swm_gpu_ctx *c, int n0, int g0);
 void fused_pair_level(const swm_gpu_ctx *c, const float *out[6]);
+void fused_static(const swm_gpu_ctx *c, const float **He, const uint16_t **mask16, const float **Fe);
 // one launch of the ensemble step: tiles {member, strip << 16 | row group}
 int march_ens_launch(int mix, int rows, const P32 *tab, const int2 *tiles, int ntiles, int *next,
                      cudaStream_t st);

@@ -56,9 +56,40 @@ __global__ void k_trc_diff(Dev d, TrcView t, const double *coeff) {
               kap * hv[jp] * (C[jp] - C[k]) * coeff[10 * n + k] + kap * hv[k] * (C[k] - C[jm]) * coeff[11 * n + k];
 }
 
+// Extension: third-order upwind-biased face value of CH between cells L and
+// R (R east or north of L; Lm behind L, Rp beyond R) for face velocity vel;
+// the reference's mask-weighted mean where one of the four cells is land
+__device__ double ub3_face(const double *CH, const int8_t *oE, size_t Lm, size_t L, size_t R, size_t Rp,
+                           double vel) {
+  if (oE[Lm] && oE[L] && oE[R] && oE[Rp]) {
+    if (vel >= 0.) return ((-1. * CH[Lm] + 5. * CH[L]) + 2. * CH[R]) / 6.;
+    return ((2. * CH[L] + 5. * CH[R]) - 1. * CH[Rp]) / 6.;
+  }
+  double den = (double)(oE[L] + oE[R]);
+  if (den == 0.) return 0.;
+  return ((double)oE[L] * CH[L] + (double)oE[R] * CH[R]) / den;
+}
+
+__device__ double ub3_advection(const Dev &d, const double *CH, const double *u, const double *v, int i, int j) {
+  const int8_t *oE = d.ocean[GE], *oU = d.ocean[GU], *oV = d.ocean[GV];
+  const double *cv = d.cosl[GV], *ce = d.cosl[GE];
+  const int nx = d.nx, ny = d.ny;
+  const int ip = tip1(i, nx), im = tim1(i, nx), jp = tip1(j, ny), jm = tim1(j, ny);
+  auto K = [nx](int a, int b) { return a + (size_t)nx * b; };
+  size_t k = K(i, j);
+  double fe = ub3_face(CH, oE, K(im, j), k, K(ip, j), K(tip1(ip, nx), j), u[K(ip, j)]);
+  double fw = ub3_face(CH, oE, K(tim1(im, nx), j), K(im, j), k, K(ip, j), u[k]);
+  double fn = ub3_face(CH, oE, K(i, jm), k, K(i, jp), K(i, tip1(jp, ny)), v[K(i, jp)]);
+  double fs = ub3_face(CH, oE, K(i, tim1(jm, ny)), K(i, jm), k, K(i, jp), v[k]);
+  double rdl = 1. / (d.A * d.dLambda * ce[j]), rdt = 1. / (d.A * d.dTheta * ce[j]);
+  double ax = -1. * oU[K(ip, j)] * u[K(ip, j)] * fe + (double)oU[k] * u[k] * fw;
+  double ay = -1. * oV[K(i, jp)] * cv[jp] * v[K(i, jp)] * fn + (double)oV[k] * cv[j] * v[k] * fs;
+  return ax * rdl + ay * rdt;
+}
+
 // TRC_tracer_incr, forcing and increment loops (:182-207); the increment is
 // written to slot 3 of the ring
-__global__ void k_trc_incr(Dev d, TrcView t, const double *coeff) {
+__global__ void k_trc_incr(Dev d, TrcView t, const double *coeff, int flux) {
   int i = blockIdx.x * blockDim.x + threadIdx.x, j = blockIdx.y * blockDim.y + threadIdx.y;
   if (i >= d.nx || j >= d.ny) return;
   size_t n = (size_t)d.nx * d.ny, k = i + (size_t)d.nx * j;
@@ -66,6 +97,12 @@ __global__ void k_trc_incr(Dev d, TrcView t, const double *coeff) {
   size_t jp = i + (size_t)d.nx * tip1(j, d.ny), jm = i + (size_t)d.nx * tim1(j, d.ny);
   const double *CH = t.CH0, *C = t.C, *u = d.u0, *v = d.v0;
   double forcing = C[k] * d.Fe[k];
+  if (flux == 1) {
+    t.G[2][k] = d.ocean[GE][k] ? (ub3_advection(d, CH, u, v, i, j) + t.diff[k] -
+                                  t.gamma[k] * d.D[k] * (C[k] - t.C0[k]) + forcing)
+                               : 0.;
+    return;
+  }
   const double *c = coeff;
   t.G[2][k] = (CH[ip] * u[ip] * c[0 * n + k] + CH[im] * u[k] * c[1 * n + k] + CH[jp] * v[jp] * c[2 * n + k] +
                CH[jm] * v[k] * c[3 * n + k] + CH[k] * u[ip] * c[4 * n + k] + CH[k] * u[k] * c[5 * n + k] +
@@ -84,10 +121,10 @@ __global__ void k_trc_integrate(Dev d, TrcView t, double c0, double c1, double c
 }
 
 // TRC_tracer_advance, diagnostic part (:263-278)
-__global__ void k_trc_C(Dev d, TrcView t) {
+__global__ void k_trc_C(Dev d, TrcView t, int guard) {
   size_t k = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (k >= (size_t)d.nx * d.ny) return;
-  t.C[k] = t.CH0[k] / d.D[k];
+  t.C[k] = (guard && d.D[k] == 0.) ? 0. : t.CH0[k] / d.D[k];  // guard: 0/0 on dry land -> 0
 }
 __global__ void k_trc_flux(Dev d, TrcView t) {
   int i = blockIdx.x * blockDim.x + threadIdx.x, j = blockIdx.y * blockDim.y + threadIdx.y;
@@ -129,7 +166,7 @@ int tracer_step(swm_gpu_ctx *c, int64_t itt) {
   for (auto &T : c->tracers) {
     TrcView v = view(T);
     k_trc_diff<<<tgrd(c), tblk(), 0, c->stream>>>(d, v, c->trc_coeff);
-    k_trc_incr<<<tgrd(c), tblk(), 0, c->stream>>>(d, v, c->trc_coeff);
+    k_trc_incr<<<tgrd(c), tblk(), 0, c->stream>>>(d, v, c->trc_coeff, c->cfg.tracer_flux);
     k_trc_integrate<<<nb, 256, 0, c->stream>>>(d, v, tab[tstep][0], tab[tstep][1], tab[tstep][2], tstep);
     c->launches += 3;
   }
@@ -144,7 +181,7 @@ int tracer_advance(swm_gpu_ctx *c) {
     T.g0 = (T.g0 + 1) % 3;
     T.n0 = 1 - T.n0;
     TrcView v = view(T);
-    k_trc_C<<<nb, 256, 0, c->stream>>>(d, v);
+    k_trc_C<<<nb, 256, 0, c->stream>>>(d, v, c->cfg.tracer_nan_guard);
     k_trc_flux<<<tgrd(c), tblk(), 0, c->stream>>>(d, v);
     c->launches += 2;
   }
@@ -197,6 +234,7 @@ int trc_gpu_add(swm_gpu_ctx *c, double kappa_h, double cons, double gamma_c, con
   SWM_CK(cudaMemcpy(T.C0, C0v.data(), n * 8, cudaMemcpyHostToDevice));
   SWM_CK(cudaMemcpy(T.gamma, gv.data(), n * 8, cudaMemcpyHostToDevice));
   SWM_CK(cudaMemcpy(T.impl, impl.data(), n * 8, cudaMemcpyHostToDevice));
+  if (c->cfg.path == SWM_PATH_FUSED_FP32C) TRY_T(trc32_add(c, CH, C0v, gv, impl, kappa_h));
   c->tracers.push_back(T);
   if (id) *id = (int)c->tracers.size() - 1;
   return SWM_GPU_OK;
@@ -204,12 +242,26 @@ int trc_gpu_add(swm_gpu_ctx *c, double kappa_h, double cons, double gamma_c, con
 
 int trc_gpu_init(swm_gpu_ctx *c) {
   SWM_REQUIRE(c && !c->tracers.empty(), "trc_gpu_init: no tracer added");
+  if (trc32_active(c)) return trc32_init(c);
   return tracer_init_coeffs(c);
 }
 
 int trc_gpu_get_field(swm_gpu_ctx *c, int t, int f, double *out) {
   SWM_REQUIRE(c && t >= 0 && t < (int)c->tracers.size() && out, "trc_gpu_get_field: bad arguments");
   const Tracer &T = c->tracers[t];
+  if (trc32_active(c)) {
+    // FP32 path: CH and C = CH / D are formed on request; the other fields
+    // are not kept
+    SWM_REQUIRE(f == TRC_F_CH || f == TRC_F_C, "trc_gpu_get_field: the FP32 tracer path keeps CH and C only");
+    if (f == TRC_F_C && !c->cfg.frozen_flow) {
+      TRY_T(fused_sync_state(c));
+      TRY_T(plain_diagnostics(c, 1));
+    }
+    TRY_T(trc32_export(c, t, f == TRC_F_C, T.uhc));
+    SWM_CK(cudaMemcpyAsync(out, T.uhc, c->n * 8, cudaMemcpyDeviceToHost, c->stream));
+    SWM_CK(cudaStreamSynchronize(c->stream));
+    return SWM_GPU_OK;
+  }
   const double *p = nullptr;
   switch (f) {
     case TRC_F_CH: p = T.CH[T.n0]; break;

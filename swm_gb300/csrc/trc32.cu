@@ -1,0 +1,450 @@
+// trc32.cu -- passive tracers on the FP32 compensated path, all tracers of a
+// basin in one kernel per step.
+//
+// Formulas: TRC_tracer_incr (tracer_module.f90:154-209), TRC_initCoeffs
+// (:291-342, coefficients rebuilt from the masks and per-row metric factors,
+// with the 0/0 of land-land pairs taken as 0), TRC_tracer_integrate
+// (:216-232); thickness and face thicknesses as computeD
+// (swm_nonlinear_timestep_module.f90:182-218).  The tracer content CH is a
+// (hi, lo) binary32 pair with a compensated Adams-Bashforth update and the
+// implicit decay applied as x - x*dt*cons/(1 + dt*cons); increments are
+// binary32.  Extension: third-order upwind-biased face values
+// (swm_gpu_config.tracer_flux = 1) with the reference's mask-weighted mean
+// next to land.
+#include <cmath>
+#include <cstring>
+#include <string>
+#include <vector>
+#include "ctx.h"
+#include "fused32.h"
+
+namespace swm {
+
+constexpr int TRC32_MAX = 4;  // tracers per launch (more run in several launches)
+enum { RT_RDL, RT_RDT, RT_CV, RT_D8, RT_D10, RT_NR };
+
+struct Tracer32 {
+  float *ch[2] = {}, *cl[2] = {};  // CH pair, levels TRC_N0 / TRC_N0p1 (rotated)
+  float *G[3] = {};
+  float *C0 = nullptr, *gamma = nullptr, *dp = nullptr;  // fields, or null when uniform
+  float gamma_s = 0.f, dp_s = 0.f, kappa = 0.f;
+  int n0 = 0, g0 = 0;
+};
+
+struct TrcP {
+  int nx, ny, nl, flux, ntr;
+  float dt, ab0, ab1, ab2;
+  const float *u, *v, *eta, *He, *Fe, *rows;
+  const uint16_t *mask16;
+  struct {
+    const float *ch, *cl, *G1, *G2, *C0, *gamma, *dp;
+    float *chn, *cln, *G3;
+    float gamma_s, dp_s, kappa;
+  } t[TRC32_MAX];
+};
+
+__device__ __forceinline__ int wr(int a, int n) { return a < 0 ? a + n : (a >= n ? a - n : a); }
+
+// 1 / thickness, 0 on dry land (C = CH * rD then takes the 0/0 there as 0)
+__device__ __forceinline__ float rthick(float d) { return d != 0.f ? __frcp_rn(d) : 0.f; }
+
+// face value of CH between L and R (R east/north of L), Lm behind L, Rp beyond R
+__device__ __forceinline__ float face(int flux, float vel, float cLm, float cL, float cR, float cRp, unsigned oLm,
+                                      unsigned oL, unsigned oR, unsigned oRp) {
+  if (flux == 1 && oLm && oL && oR && oRp)
+    return vel >= 0.f ? (5.f * cL + 2.f * cR - cLm) * (1.f / 6.f) : (2.f * cL + 5.f * cR - cRp) * (1.f / 6.f);
+  unsigned den = oL + oR;
+  if (den == 0) return 0.f;
+  return (oL ? cL : 0.f) * (den == 2 ? 0.5f : 1.f) + (oR ? cR : 0.f) * (den == 2 ? 0.5f : 1.f);
+}
+
+__device__ __forceinline__ void comp_update(float hi, float lo, float inc, float dp, float &nh, float &nl) {
+  float s = hi + inc;
+  float bb = s - hi;
+  float e = (hi - (s - bb)) + (inc - bb) + lo;
+  float c = s * dp;
+  float t = s - c;
+  float bt = t - s;
+  float e2 = (s - (t - bt)) + (-c - bt);
+  e = e + e2 - e * dp;
+  nh = t + e;
+  nl = e - (nh - t);
+}
+
+constexpr unsigned FULLM = 0xffffffffu;
+constexpr int TRC_ROWS = 16;  // output rows per warp
+
+// One warp owns a strip of 32 columns (lane = column; 2 halo lanes per side,
+// as the upwind-biased faces reach two cells) and TRC_ROWS output rows; it
+// walks up the strip keeping the last five rows of CH (hi + lo), thickness
+// and masks in registers, and updates row J-2 once row J is in.
+template <int NT, int FLUX>
+__global__ void __launch_bounds__(128) k_trc32(TrcP p) {
+  constexpr int H = 2, TI = 32 - 2 * H;
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  const int nx = p.nx, ny = p.ny;
+  const int ry0 = (blockIdx.y * 4 + warp) * TRC_ROWS;
+  if (ry0 >= ny) return;  // whole warp leaves together
+  const int gx = blockIdx.x * TI - H + lane;
+  const int gi = wr(gx, nx);
+  const bool store_lane = lane >= H && lane < 32 - H && gx < nx;
+
+  unsigned m[5] = {};
+  float D[5] = {}, rD[5] = {}, u[3] = {}, v[3] = {};
+  float chs[NT][5] = {}, chh[NT][3] = {}, chl[NT][3] = {};
+  int off[3] = {};
+  const float *rr[3] = {};
+
+  int J = ry0 - 2;
+  const int ylast = min(ry0 + TRC_ROWS, ny);  // one past the last output row
+  const int jend = ylast + 2;
+  // row loads run two rows ahead of the window; the update inputs (increments
+  // 1-2, C0) one output row ahead
+  struct Row {
+    unsigned m;
+    float D, u, v, h[NT], l[NT];
+    int off;
+    const float *rows;
+  };
+  auto load = [&](int jj, Row &r) {
+    const int jw = wr(jj, ny);
+    r.off = nx * jw;
+    r.rows = p.rows + (size_t)jw * RT_NR;
+    const int k = gi + r.off;
+    r.m = p.mask16[k];
+    r.D = p.nl ? ((r.m & 8u) ? p.He[k] + p.eta[k] : 1.f) : p.He[k];
+    r.u = p.u[k];
+    r.v = p.v[k];
+#pragma unroll
+    for (int q = 0; q < NT; q++) {
+      r.h[q] = p.t[q].ch[k];
+      r.l[q] = p.t[q].cl[k];
+    }
+  };
+  Row n1, n2;
+  load(J, n1);
+  load(J + 1, n2);
+  float pg1[NT] = {}, pg2[NT] = {}, pc0[NT] = {};
+
+  for (; J < jend; J++) {
+#pragma unroll
+    for (int a = 4; a > 0; a--) {
+      m[a] = m[a - 1];
+      D[a] = D[a - 1];
+      rD[a] = rD[a - 1];
+#pragma unroll
+      for (int q = 0; q < NT; q++) chs[q][a] = chs[q][a - 1];
+    }
+#pragma unroll
+    for (int a = 2; a > 0; a--) {
+      u[a] = u[a - 1];
+      v[a] = v[a - 1];
+      off[a] = off[a - 1];
+      rr[a] = rr[a - 1];
+#pragma unroll
+      for (int q = 0; q < NT; q++) {
+        chh[q][a] = chh[q][a - 1];
+        chl[q][a] = chl[q][a - 1];
+      }
+    }
+    m[0] = n1.m; D[0] = n1.D; rD[0] = rthick(n1.D); u[0] = n1.u; v[0] = n1.v; off[0] = n1.off; rr[0] = n1.rows;
+#pragma unroll
+    for (int q = 0; q < NT; q++) {
+      chh[q][0] = n1.h[q];
+      chl[q][0] = n1.l[q];
+      chs[q][0] = n1.h[q] + n1.l[q];
+    }
+    n1 = n2;
+    if (J + 2 < jend) load(J + 2, n2);
+
+    const int o = J - 2;
+    if (o >= ry0) {  // uniform across the warp
+      const bool upd = store_lane && o < ny;
+      // masks of row o and its neighbours
+      const unsigned mo = m[2];
+      const unsigned oE = (mo >> 3) & 1, oEim = (mo >> 7) & 1, oEip = (mo >> 11) & 1;
+      const unsigned oU = (mo >> 1) & 1, oUip = (mo >> 9) & 1, oV = (mo >> 2) & 1;
+      const unsigned oVjp = (m[1] >> 2) & 1, oEjp = (m[1] >> 3) & 1, oEjm = (m[3] >> 3) & 1;
+      const unsigned mr = __shfl_down_sync(FULLM, mo, 1), ml = __shfl_up_sync(FULLM, mo, 1);
+      const unsigned oEipp = (mr >> 11) & 1, oEimm = (ml >> 7) & 1;
+      const unsigned oEjpp = (m[0] >> 3) & 1, oEjmm = (m[4] >> 3) & 1;
+      const float Do = D[2], Dip = __shfl_down_sync(FULLM, Do, 1), Dim = __shfl_up_sync(FULLM, Do, 1);
+      const float Djp = D[1], Djm = D[3];
+      const float ro = rD[2], rip = __shfl_down_sync(FULLM, ro, 1), rim = __shfl_up_sync(FULLM, ro, 1);
+      const float rjp = rD[1], rjm = rD[3];
+      const float uo = u[2], uip = __shfl_down_sync(FULLM, uo, 1), vo = v[2], vjp = v[1];
+      float ch_r[NT], ch_l[NT], ch_rr[NT], ch_ll[NT];
+#pragma unroll
+      for (int q = 0; q < NT; q++) {
+        ch_r[q] = __shfl_down_sync(FULLM, chs[q][2], 1);
+        ch_l[q] = __shfl_up_sync(FULLM, chs[q][2], 1);
+        ch_rr[q] = FLUX ? __shfl_down_sync(FULLM, chs[q][2], 2) : 0.f;
+        ch_ll[q] = FLUX ? __shfl_up_sync(FULLM, chs[q][2], 2) : 0.f;
+      }
+      if (upd) {
+        const int ko = gi + off[2];
+        const float *r = rr[2], *rp = rr[1];
+        const float rdl = r[RT_RDL], rdt = r[RT_RDT], cv = r[RT_CV], cvp = rp[RT_CV];
+        auto avg2 = [](float a, unsigned oa, float b, unsigned ob) {
+          unsigned c = oa + ob;
+          return c == 0 ? 0.f : ((oa ? a : 0.f) + (ob ? b : 0.f)) * (c == 2 ? 0.5f : 1.f);
+        };
+        const float hu = avg2(Do, oE, Dim, oEim), huip = avg2(Dip, oEip, Do, oE);
+        const float hv = avg2(Do, oE, Djm, oEjm), hvjp = avg2(Djp, oEjp, Do, oE);
+        const float Fe = p.Fe ? p.Fe[ko] : 0.f;
+        const float c8 = oUip * r[RT_D8], c9 = -(float)oU * r[RT_D8];
+        const float c10 = oVjp * cvp * r[RT_D10], c11 = -(float)oV * cv * r[RT_D10];
+#pragma unroll
+        for (int q = 0; q < NT; q++) {
+          const auto &t = p.t[q];
+          const float ch = chs[q][2], chip = ch_r[q], chim = ch_l[q], chjp = chs[q][1], chjm = chs[q][3];
+          const float fe = face(FLUX, uip, chim, ch, chip, ch_rr[q], oEim, oE, oEip, oEipp);
+          const float fw = face(FLUX, uo, ch_ll[q], chim, ch, chip, oEimm, oEim, oE, oEip);
+          const float fn = face(FLUX, vjp, chjm, ch, chjp, chs[q][0], oEjm, oE, oEjp, oEjpp);
+          const float fs = face(FLUX, vo, chs[q][4], chjm, ch, chjp, oEjmm, oEjm, oE, oEjp);
+          float g = rdl * (oU * uo * fw - oUip * uip * fe) + rdt * (oV * cv * vo * fs - oVjp * cvp * vjp * fn);
+          if (FLUX == 1 && !oE) g = 0.f;
+          if (oE) {
+            const float C = ch * ro;
+            const float diff = t.kappa * (huip * (chip * rip - C) * c8 + hu * (C - chim * rim) * c9 +
+                                          hvjp * (chjp * rjp - C) * c10 + hv * (C - chjm * rjm) * c11);
+            const float gam = t.gamma ? t.gamma[ko] : t.gamma_s;
+            g += diff - gam * Do * (C - pc0[q]) + C * Fe;
+          }
+          t.G3[ko] = g;
+          const float inc = p.dt * (p.ab0 * pg1[q] + p.ab1 * pg2[q] + p.ab2 * g);
+          float nh, nl;
+          comp_update(chh[q][2], chl[q][2], inc, t.dp ? t.dp[ko] : t.dp_s, nh, nl);
+          t.chn[ko] = nh;
+          t.cln[ko] = nl;
+        }
+      }
+    }
+    // update inputs of the next output row (J - 1)
+    if (store_lane && J - 1 >= ry0 && J - 1 < ylast) {
+      const int kn = gi + off[1];
+#pragma unroll
+      for (int q = 0; q < NT; q++) {
+        pg1[q] = p.t[q].G1[kn];
+        pg2[q] = p.t[q].G2[kn];
+        pc0[q] = p.t[q].C0[kn];
+      }
+    }
+  }
+}
+
+template <int NT>
+static void trc_launch_nt(const TrcP &p, cudaStream_t st) {
+  dim3 grid((p.nx + 27) / 28, (p.ny + 4 * TRC_ROWS - 1) / (4 * TRC_ROWS));
+  if (p.flux == 1) k_trc32<NT, 1><<<grid, 128, 0, st>>>(p);
+  else k_trc32<NT, 0><<<grid, 128, 0, st>>>(p);
+}
+
+static void trc_launch(const TrcP &p, cudaStream_t st) {
+  switch (p.ntr) {
+    case 1: trc_launch_nt<1>(p, st); break;
+    case 2: trc_launch_nt<2>(p, st); break;
+    case 3: trc_launch_nt<3>(p, st); break;
+    default: trc_launch_nt<4>(p, st); break;
+  }
+}
+
+__global__ void k_trc32_export(const float *ch, const float *cl, const double *D, double *out, size_t n, int conc) {
+  size_t k = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (k >= n) return;
+  double v = (double)ch[k] + (double)cl[k];
+  out[k] = conc ? (D[k] != 0. ? v / D[k] : 0.) : v;
+}
+
+__global__ void k_f64_to_f32(const double *a, float *b, size_t n) {
+  size_t k = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (k < n) b[k] = (float)a[k];
+}
+
+}  // namespace swm
+
+struct Trc32State {
+  std::vector<swm::Tracer32> t;
+  float *rows = nullptr;
+  float *u = nullptr, *v = nullptr, *eta = nullptr;  // frozen-flow copies
+  bool ready = false;
+};
+
+namespace swm {
+
+static int t32_alloc(float **p, size_t n) {
+  if (cudaMalloc((void **)p, n * sizeof(float)) != cudaSuccess) {
+    set_error("trc32: cudaMalloc failed");
+    return SWM_GPU_ENOMEM;
+  }
+  return SWM_GPU_OK;
+}
+
+#define T32TRY(x)                        \
+  do {                                   \
+    int rc_ = (x);                       \
+    if (rc_ != SWM_GPU_OK) return rc_;   \
+  } while (0)
+
+static int upload_f32(swm_gpu_ctx *c, const std::vector<double> &h, float **dst) {
+  std::vector<float> f(h.size());
+  for (size_t k = 0; k < h.size(); k++) f[k] = (float)h[k];
+  T32TRY(t32_alloc(dst, h.size()));
+  SWM_CK(cudaMemcpyAsync(*dst, f.data(), f.size() * 4, cudaMemcpyHostToDevice, c->stream));
+  SWM_CK(cudaStreamSynchronize(c->stream));
+  return SWM_GPU_OK;
+}
+
+static bool uniform_of(const std::vector<double> &a, double *v) {
+  *v = a.empty() ? 0. : a[0];
+  for (double x : a)
+    if (x != *v) return false;
+  return true;
+}
+
+bool trc32_active(const swm_gpu_ctx *c) { return c->cfg.path == SWM_PATH_FUSED_FP32C && !c->tracers.empty(); }
+
+// FP32 copy of one tracer (called from trc_gpu_add with the FP64 host data)
+int trc32_add(swm_gpu_ctx *c, const std::vector<double> &CH, const std::vector<double> &C0,
+              const std::vector<double> &gamma, const std::vector<double> &impl, double kappa) {
+  if (!c->trc32) c->trc32 = new Trc32State();
+  Tracer32 T;
+  const size_t n = c->n;
+  std::vector<double> hi(n), lo(n);
+  for (size_t k = 0; k < n; k++) {
+    hi[k] = (double)(float)CH[k];
+    lo[k] = CH[k] - hi[k];
+  }
+  for (int q = 0; q < 2; q++) {
+    T32TRY(upload_f32(c, hi, &T.ch[q]));
+    T32TRY(upload_f32(c, lo, &T.cl[q]));
+  }
+  for (int q = 0; q < 3; q++) {
+    T32TRY(t32_alloc(&T.G[q], n));
+    SWM_CK(cudaMemsetAsync(T.G[q], 0, n * 4, c->stream));
+  }
+  T32TRY(upload_f32(c, C0, &T.C0));
+  double g;
+  if (uniform_of(gamma, &g)) T.gamma_s = (float)g;
+  else T32TRY(upload_f32(c, gamma, &T.gamma));
+  std::vector<double> dp(n);
+  for (size_t k = 0; k < n; k++) dp[k] = (impl[k] - 1.) / impl[k];
+  double d;
+  if (uniform_of(dp, &d)) T.dp_s = (float)d;
+  else T32TRY(upload_f32(c, dp, &T.dp));
+  T.kappa = (float)kappa;
+  c->trc32->t.push_back(T);
+  return SWM_GPU_OK;
+}
+
+// per-row factors and, for a frozen flow, FP32 copies of u, v, eta
+int trc32_init(swm_gpu_ctx *c) {
+  Trc32State *s = c->trc32;
+  if (!s) return SWM_GPU_OK;
+  T32TRY(fused_prepare(c));  // masks and depths of the FP32 path
+  const HostGrid &g = c->hg;
+  const double A = c->cfg.A, dL = g.dLambda, dT = g.dTheta;
+  std::vector<double> rows((size_t)c->ny * RT_NR);
+  for (int j = 0; j < c->ny; j++) {
+    double *r = &rows[(size_t)j * RT_NR];
+    double cE = g.cosl[GE][j], cU = g.cosl[GU][j], cV = g.cosl[GV][j];
+    r[RT_RDL] = 1. / (A * dL * cE);
+    r[RT_RDT] = 1. / (A * dT * cE);
+    r[RT_CV] = cV;
+    r[RT_D8] = 1. / (dL * dL) / (A * A) / cU / cE;
+    r[RT_D10] = 1. / (dT * dT) / (A * A) / cE;
+  }
+  if (s->rows) cudaFree(s->rows);
+  T32TRY(upload_f32(c, rows, &s->rows));
+  if (c->cfg.frozen_flow) {
+    const size_t n = c->n;
+    unsigned nb = (unsigned)((n + 255) / 256);
+    float **dst[3] = {&s->u, &s->v, &s->eta};
+    const double *src[3] = {c->u[c->n0], c->v[c->n0], c->eta[c->n0]};
+    for (int q = 0; q < 3; q++) {
+      if (!*dst[q]) T32TRY(t32_alloc(dst[q], n));
+      k_f64_to_f32<<<nb, 256, 0, c->stream>>>(src[q], *dst[q], n);
+    }
+    c->launches += 3;
+  }
+  s->ready = true;
+  SWM_CK(cudaGetLastError());
+  return SWM_GPU_OK;
+}
+
+int trc32_step(swm_gpu_ctx *c, int64_t itt) {
+  Trc32State *s = c->trc32;
+  SWM_REQUIRE(s && s->ready, "tracers: call trc_gpu_init before stepping");
+  int tstep = (int)(itt < 3 ? itt : 3);
+  const double chi = c->cfg.ab_chi;
+  double tab[4][3] = {{0, 0, 0}, {1., 0, 0}, {-0.5 - chi, 1.5 + chi, 0}, {5. / 12., -16. / 12., 23. / 12.}};
+  TrcP p;
+  memset(&p, 0, sizeof(p));
+  p.nx = c->nx;
+  p.ny = c->ny;
+  p.nl = c->cfg.mode == SWM_MODE_NONLINEAR;
+  p.flux = c->cfg.tracer_flux;
+  p.dt = (float)c->cfg.dt;
+  p.ab0 = (float)tab[tstep][0];
+  p.ab1 = (float)tab[tstep][1];
+  p.ab2 = (float)tab[tstep][2];
+  const float *six[6];
+  if (c->cfg.frozen_flow) {
+    p.u = s->u; p.v = s->v; p.eta = s->eta;
+  } else {
+    fused_pair_level(c, six);  // the level the SWM step reads (TRC_timestep runs before SWM_advance)
+    p.u = six[0]; p.v = six[2]; p.eta = six[4];
+  }
+  fused_static(c, &p.He, &p.mask16, &p.Fe);
+  p.rows = s->rows;
+  for (size_t t0 = 0; t0 < s->t.size(); t0 += TRC32_MAX) {
+    p.ntr = (int)std::min(s->t.size() - t0, (size_t)TRC32_MAX);
+    for (int q = 0; q < p.ntr; q++) {
+      const Tracer32 &T = s->t[t0 + q];
+      auto &d = p.t[q];
+      d.ch = T.ch[T.n0]; d.cl = T.cl[T.n0]; d.chn = T.ch[1 - T.n0]; d.cln = T.cl[1 - T.n0];
+      d.G1 = T.G[T.g0]; d.G2 = T.G[(T.g0 + 1) % 3]; d.G3 = T.G[(T.g0 + 2) % 3];
+      d.C0 = T.C0; d.gamma = T.gamma; d.dp = T.dp;
+      d.gamma_s = T.gamma_s; d.dp_s = T.dp_s; d.kappa = T.kappa;
+    }
+    trc_launch(p, c->stream);
+    c->launches++;
+  }
+  SWM_CK(cudaGetLastError());
+  return SWM_GPU_OK;
+}
+
+void trc32_advance(swm_gpu_ctx *c) {
+  for (auto &T : c->trc32->t) {
+    T.n0 = 1 - T.n0;
+    T.g0 = (T.g0 + 1) % 3;
+  }
+}
+
+// CH (field 0) or C = CH / D (field 1) of tracer t into a device FP64 buffer
+int trc32_export(swm_gpu_ctx *c, int t, int conc, double *dst) {
+  Trc32State *s = c->trc32;
+  SWM_REQUIRE(s && t >= 0 && t < (int)s->t.size(), "trc32: bad tracer");
+  const Tracer32 &T = s->t[t];
+  const size_t n = c->n;
+  k_trc32_export<<<(unsigned)((n + 255) / 256), 256, 0, c->stream>>>(T.ch[T.n0], T.cl[T.n0], c->dev().D, dst, n,
+                                                                     conc);
+  c->launches++;
+  SWM_CK(cudaGetLastError());
+  return SWM_GPU_OK;
+}
+
+void trc32_free(swm_gpu_ctx *c) {
+  Trc32State *s = c->trc32;
+  if (!s) return;
+  for (auto &T : s->t) {
+    for (int q = 0; q < 2; q++) { cudaFree(T.ch[q]); cudaFree(T.cl[q]); }
+    for (int q = 0; q < 3; q++) cudaFree(T.G[q]);
+    cudaFree(T.C0); cudaFree(T.gamma); cudaFree(T.dp);
+  }
+  cudaFree(s->rows); cudaFree(s->u); cudaFree(s->v); cudaFree(s->eta);
+  delete s;
+  c->trc32 = nullptr;
+}
+
+}  // namespace swm

@@ -14,7 +14,7 @@ members), drawn in FP64 on the host.
 import math
 import numpy as np
 
-from .case import MODE_NONLINEAR, MODE_LIN_REST
+from .case import MODE_NONE, MODE_NONLINEAR, MODE_LIN_REST
 
 A_BIG = 6.371e9
 D2R = float(np.float32(3.14159265358979323846)) / 180.0
@@ -134,3 +134,56 @@ def ensemble_members(n=256, seed_index=4, nsteps=10000):
         dt = 15.0 * dx / 5e3
         out.append(double_gyre((cx, cy), biharmonic=False, dx=dx, amp=amp, ah=500.0, rng=rng, nsteps=nsteps, dt=dt))
     return out
+
+
+def _grf(ny, nx, slope, rng):
+    """Gaussian random field on (ny, nx) whose Fourier amplitudes fall off as
+    |k|^slope (k in cycles per domain, mean removed)."""
+    kx = np.fft.fftfreq(nx) * nx
+    ky = np.fft.fftfreq(ny) * ny
+    k = np.hypot(ky[:, None], kx[None, :])
+    amp = np.zeros_like(k)
+    amp[k > 0] = k[k > 0] ** slope
+    z = rng.standard_normal((ny, nx)) + 1j * rng.standard_normal((ny, nx))
+    f = np.fft.ifft2(z * amp).real
+    return f - f.mean()
+
+
+def tracer_flow(cells=2048, dx=2.5e3, seed_index=3, nsteps=5000, depth=100.0, peak_speed=0.5, n_tracers=2,
+                kappa=50.0, relax_days=30.0, dt=60.0, flux=1):
+    """Two passive tracers in a steady nondivergent flow (prescribed: the SWM
+    state is frozen), closed box with a one-cell land rim, uniform depth.
+
+    Streamfunction: Gaussian random field whose kinetic-energy spectrum falls
+    off as k^-3 (psi amplitudes ~ k^-3), tapered to zero at the coast and
+    scaled to a peak speed of 0.5 m/s; u = -d(psi)/dy, v = d(psi)/dx on the
+    C grid, so the discrete divergence vanishes.  Tracers: random fields with
+    variance spectrum ~ k^-3 (amplitudes ~ k^-2) mapped to [0, 1]; kappa = 50
+    m^2/s; relaxation to the initial field on 30 days; flux 1 = upwind-biased
+    (extension), 0 = the reference's centred flux."""
+    rng = np.random.Generator(np.random.PCG64(20260 + seed_index))
+    cfg = _base_config(cells, cells, dx, 0.0, 0.0, dt)
+    cfg.update(mode=MODE_NONE, lateral_mixing=0, Ah=0.0, Nt=nsteps, frozen_flow=1, tracer_flux=flux,
+               tracer_nan_guard=1, tracer=1)
+    case = empty_case(cfg)
+    nx, ny = cfg['nx'], cfg['ny']
+    H = np.full((ny, nx), float(depth))
+    H[0, :] = H[-1, :] = 0.0
+    H[:, 0] = H[:, -1] = 0.0
+    case['H'] = H
+    psi = _grf(ny, nx, -3.0, rng)
+    wy = np.sin(np.pi * np.clip((np.arange(ny) - 1) / (ny - 3), 0, 1)) ** 2
+    wx = np.sin(np.pi * np.clip((np.arange(nx) - 1) / (nx - 3), 0, 1)) ** 2
+    psi = psi * wy[:, None] * wx[None, :]
+    u = np.zeros((ny, nx))
+    v = np.zeros((ny, nx))
+    u[:-1, :] = -(psi[1:, :] - psi[:-1, :]) / dx
+    v[:, :-1] = (psi[:, 1:] - psi[:, :-1]) / dx
+    s = peak_speed / max(np.abs(u).max(), np.abs(v).max())
+    case['ic'] = {'u': u * s, 'v': v * s}
+    for t in range(n_tracers):
+        c = _grf(ny, nx, -2.0, rng)
+        c = (c - c.min()) / (c.max() - c.min())
+        case['tracers'].append(dict(varid='C%d' % t, kappa_h=kappa, cons=0.0, gamma_c=1.0 / (relax_days * DAY),
+                                    field_C=c, field_C0=c.copy(), field_gamma_C=None, field_cons=None))
+    return case
