@@ -45,7 +45,7 @@ def parse():
     ap.add_argument('--quick', action='store_true', help='skip the side measurements')
     ap.add_argument('--device-only', action='store_true',
                     help='only the warm-up and timed device steps (the form to run under ncu)')
-    ap.add_argument('--workload', default='double_gyre', choices=['double_gyre', 'ensemble', 'tracer'],
+    ap.add_argument('--workload', default='double_gyre', choices=['double_gyre', 'ensemble', 'tracer', 'helmholtz'],
                     help='ensemble / tracer: print that measurement alone (profiling)')
     return ap.parse_args()
 
@@ -234,6 +234,7 @@ def ours(args, rank, ws):
         line['speedup_vs_fp64_plain'] = line['plain_fp64']['ms_per_step'] / step_ms
         line['ensemble'] = ensemble_measurement(args)
         line['tracer'] = tracer_measurement(args)
+        line['helmholtz'] = helmholtz_measurement(args)
     if rank == 0 and ws == 1 and not args.quick:
         line['cpu_baseline'] = cpu_baseline(cells)
     g.close()
@@ -400,6 +401,46 @@ def tracer_measurement(args, cells=2048, steps=200, err_steps=1000):
     return out
 
 
+def helmholtz_measurement(args, cells=4096, rtol=1e-10):
+    """div(H^-1 grad psi) - lam psi = rhs on 4096^2 cells at 5 km (seeded
+    depth 50-5000 m, coastline, wind-curl rhs): the autotuner picks the
+    relaxation factor in 1.8-1.99 and the sweep block shape; then FP64 SOR and
+    mixed-precision SOR (FP32 sweeps, FP64 residual refinement) each solve to
+    a relative residual of 1e-10 from psi = 0."""
+    import torch
+    from swm_gb300.host import synthetic
+    from swm_gb300.model import GpuHelmholtz
+    case = synthetic.helmholtz_case(cells)
+    g = GpuHelmholtz(case['H'], case['ocean'], case['dx'], case['dy'], case['lam'])
+    st = torch.cuda.ExternalStream(g.stream())
+    t0 = time.perf_counter()
+    om, blk = g.autotune(case['rhs'], 1.8, 1.99, 12, 64)
+    t_tune = time.perf_counter() - t0
+    out = {'workload': 'helmholtz_%dx%d' % (cells, cells), 'cells': cells * cells, 'lambda': case['lam'],
+           'rtol': rtol, 'omega': om, 'block': list(blk), 'autotune_s': t_tune}
+    peak, kind = peaks()
+    for name, mixed, bps in (('fp64', False, 32), ('mixed', True, 16)):
+        g.solve(case['rhs'], omega=om, rtol=1e-3, mixed=mixed)  # warm-up
+        a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        a.record(st)
+        psi, sweeps, outer, rel, rc = g.solve(case['rhs'], omega=om, rtol=rtol, mixed=mixed, inner_tol=1e-4)
+        b.record(st)
+        torch.cuda.synchronize()
+        wall = time.perf_counter() - t0
+        dev = a.elapsed_time(b) * 1e-3
+        ach = bps * case['H'].size * sweeps / dev / 1e9
+        out[name] = {'time_to_solution_s': wall, 'device_s': dev, 'sweeps': sweeps, 'outer_iterations': outer,
+                     'relres': rel, 'converged': rc == 0,
+                     'roofline': {'bound': 'hbm', 'achieved': ach, 'peak': peak, 'unit': 'GB/s', 'frac': ach / peak,
+                                  'peak_kind': kind, 'bytes_per_cell_sweep': bps,
+                                  'note': 'sweeps only counted; residual passes included in the time'}}
+    out['mixed_speedup'] = out['fp64']['time_to_solution_s'] / out['mixed']['time_to_solution_s']
+    g.close()
+    return out
+
+
 def cpu_baseline(cells, budget_s=15.0):
     """The FP64 CPU restatement (oracle) on the same basin, all host cores."""
     sys.path.insert(0, os.path.join(ROOT, 'oracle'))
@@ -455,6 +496,8 @@ def main():
         if args.workload == 'tracer':
             out = tracer_measurement(args, cells=args.cells, steps=args.steps,
                                      err_steps=0 if args.device_only else 1000)
+        elif args.workload == 'helmholtz':
+            out = helmholtz_measurement(args, cells=args.cells)
         else:
             out = ensemble_measurement(args, steps=args.steps, one_by_one=not args.device_only)
         print(json.dumps(out))

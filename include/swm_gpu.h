@@ -216,6 +216,35 @@ int elsolv_sor_gpu_init(swm_gpu_ctx *ctx);   /* init_ElSolv_SOR (:44-66) */
 int elsolv_sor_gpu_solve(swm_gpu_ctx *ctx, const double *B, double *chi, double eps, int first_guess,
                          int *iterations, double *anorm);
 
+/* ---- variable-coefficient Helmholtz solver (extension of ElSolv_SOR) ----
+   div(H^-1 grad psi) - lambda psi = rhs on an (nx, ny) grid of spacing dx,
+   dy; a face coefficient is the mean of 1/H of its two cells over dx^2 (dy^2);
+   cells with ocean == 0 hold psi = 0, and so does everything beyond the
+   outer frame.  Red-black sweeps in the reference's colour order; stopping
+   on the relative residual ||rhs - A psi|| / ||rhs||, checked every 16
+   sweeps.  The reference's own solver (elsolv_sor_gpu_*) keeps its operator,
+   relaxation schedule and absolute stopping rule. */
+typedef struct swm_helm swm_helm;
+int swm_helm_create(int nx, int ny, double dx, double dy, double lambda, const double *H, const int8_t *ocean,
+                    swm_helm **out);
+int swm_helm_destroy(swm_helm *h);
+void *swm_helm_stream(swm_helm *h);
+int64_t swm_helm_launch_count(swm_helm *h);
+/* out = A psi on ocean cells, 0 elsewhere */
+int swm_helm_apply(swm_helm *h, const double *psi, double *out);
+/* FP64 sweeps; SWM_GPU_ENOT_CONVERGED when rtol is not reached in max_sweeps */
+int swm_helm_solve_fp64(swm_helm *h, const double *rhs, double *psi, double omega, double rtol, int max_sweeps,
+                        int *sweeps, double *relres);
+/* FP32 sweeps on the correction equation, FP64 residual and accumulation
+   (iterative refinement); each correction solve stops when its own residual
+   has fallen by inner_tol */
+int swm_helm_solve_mixed(swm_helm *h, const double *rhs, double *psi, double omega, double rtol, double inner_tol,
+                         int max_sweeps, int *sweeps, int *outer, double *relres);
+/* block shape of the sweep kernel by timing, and the relaxation factor in
+   [omega_lo, omega_hi] (ngrid values) by trial solves of trial_sweeps */
+int swm_helm_autotune(swm_helm *h, const double *rhs, double omega_lo, double omega_hi, int ngrid,
+                      int trial_sweeps, double *omega, int *block_x, int *block_y);
+
 #ifdef __cplusplus
 }
 #endif

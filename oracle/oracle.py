@@ -66,6 +66,7 @@ def lib():
             'orc_sor_init': (V, [P]), 'orc_sor_solve': (I, [P, P, P, D, I, P]), 'orc_sor_coeff': (P, [P]),
             'orc_helmholtz_sor': (I, [I, I, P, P, P, P, P, P, D, D, I, P]),
             'orc_helmholtz_apply': (V, [I, I, P, P, P, P, P, P]),
+            'orc_helmholtz_coeffs': (V, [I, I, P, D, D, D, P, P, P]),
         }
         for name, (res, args) in sig.items():
             f = getattr(L, name)
@@ -226,6 +227,16 @@ def helmholtz_sor(cx, cy, cc, mask, rhs, psi0, omega, rtol, max_sweeps):
     it = L.orc_helmholtz_sor(nx, ny, ptr(a[0]), ptr(a[1]), ptr(a[2]), ptr(m), ptr(r), ptr(psi), omega, rtol,
                              max_sweeps, C.byref(rel))
     return psi, it, rel.value
+
+
+def helmholtz_coeffs(hinv, lam, dx, dy):
+    """cx, cy, cc of div(hinv grad psi) - lam psi (orc_helmholtz_coeffs)."""
+    L = lib()
+    ny, nx = hinv.shape
+    h = f64(hinv)
+    cx, cy, cc = np.zeros_like(h), np.zeros_like(h), np.zeros_like(h)
+    L.orc_helmholtz_coeffs(nx, ny, ptr(h), lam, dx, dy, ptr(cx), ptr(cy), ptr(cc))
+    return cx, cy, cc
 
 
 def helmholtz_apply(cx, cy, cc, mask, psi):

@@ -1201,6 +1201,26 @@ int orc_sor_solve(orc_model *m, const double *B, double *chi, double eps, int fi
 /* Face coefficients cx(i,j) couple (i-1,j)-(i,j), cy(i,j) couple (i,j-1)-   */
 /* (i,j); cc(i,j) is the diagonal.  mask=0 cells are fixed at 0.             */
 /* ------------------------------------------------------------------------ */
+/* Extension: coefficients of div(hinv grad psi) - lambda psi on a uniform
+   grid of spacing dx, dy; a face takes the mean inverse depth of its two
+   cells; faces on the outer frame are 0 (the frame is Dirichlet). */
+void orc_helmholtz_coeffs(int nx, int ny, const double *hinv, double lambda, double dx, double dy, double *cx,
+                          double *cy, double *cc) {
+  double rdx2 = 1. / (dx * dx), rdy2 = 1. / (dy * dy);
+  for (int j = 0; j < ny; j++)
+    for (int i = 0; i < nx; i++) {
+      size_t k = (size_t)i + (size_t)nx * j;
+      cx[k] = i > 0 ? (0.5 * (hinv[k] + hinv[k - 1])) * rdx2 : 0.;
+      cy[k] = j > 0 ? (0.5 * (hinv[k] + hinv[k - nx])) * rdy2 : 0.;
+    }
+  for (int j = 0; j < ny; j++)
+    for (int i = 0; i < nx; i++) {
+      size_t k = (size_t)i + (size_t)nx * j;
+      double ce = i < nx - 1 ? cx[k + 1] : 0., cn = j < ny - 1 ? cy[k + nx] : 0.;
+      cc[k] = -(((cx[k] + ce) + cy[k]) + cn) - lambda;
+    }
+}
+
 void orc_helmholtz_apply(int nx, int ny, const double *cx, const double *cy, const double *cc,
                          const int8_t *mask, const double *psi, double *out) {
   for (int j = 0; j < ny; j++)
@@ -1219,6 +1239,8 @@ int orc_helmholtz_sor(int nx, int ny, const double *cx, const double *cy, const 
                       double rtol, int max_sweeps, double *relres_out) {
   size_t n = (size_t)nx * ny;
   double *r = (double *)malloc(sizeof(double) * n);
+  double *rcc = (double *)malloc(sizeof(double) * n); /* 1 / diagonal, formed once */
+  for (size_t k = 0; k < n; k++) rcc[k] = 1. / cc[k];
   double bn = 0.;
   for (size_t k = 0; k < n; k++) if (mask[k]) bn += rhs[k] * rhs[k];
   bn = sqrt(bn);
@@ -1234,7 +1256,7 @@ int orc_helmholtz_sor(int nx, int ny, const double *cx, const double *cy, const 
           double s = j > 0 ? psi[k - nx] : 0., nn = j < ny - 1 ? psi[k + nx] : 0.;
           double ce = i < nx - 1 ? cx[k + 1] : 0., cn = j < ny - 1 ? cy[k + nx] : 0.;
           double off = cx[k] * w + ce * e + cy[k] * s + cn * nn;
-          double gs = (rhs[k] - off) / cc[k];
+          double gs = (rhs[k] - off) * rcc[k];
           psi[k] = psi[k] + omega * (gs - psi[k]);
         }
     sweeps++;
@@ -1247,6 +1269,7 @@ int orc_helmholtz_sor(int nx, int ny, const double *cx, const double *cy, const 
     }
   }
   free(r);
+  free(rcc);
   if (relres_out) *relres_out = rel;
   return sweeps;
 }

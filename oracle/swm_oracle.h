@@ -140,6 +140,8 @@ int orc_sor_solve(orc_model *m, const double *B, double *chi, double eps, int fi
 const double *orc_sor_coeff(orc_model *m); /* ElSolvSOR_c (Nx, Ny, 5) */
 
 /* ---- extension: variable-coefficient Helmholtz red-black SOR (standalone) ---- */
+void orc_helmholtz_coeffs(int nx, int ny, const double *hinv, double lambda, double dx, double dy, double *cx,
+                          double *cy, double *cc);
 int orc_helmholtz_sor(int nx, int ny, const double *cx, const double *cy, const double *cc,
                       const int8_t *mask, const double *rhs, double *psi, double omega,
                       double rtol, int max_sweeps, double *relres_out);

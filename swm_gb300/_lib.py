@@ -57,6 +57,13 @@ def _sigs():
         'swm_gpu_ensemble_run': (I, [P, I64, I64]), 'swm_gpu_ensemble_integrals': (I, [P, P]),
         'swm_gpu_ensemble_synchronize': (I, [P]), 'swm_gpu_ensemble_stream': (P, [P]),
         'swm_gpu_ensemble_launch_count': (I64, [P]), 'swm_gpu_ensemble_rows': (I, [P]),
+        'swm_helm_create': (I, [I, I, D, D, D, P, P, PP]), 'swm_helm_destroy': (I, [P]),
+        'swm_helm_stream': (P, [P]), 'swm_helm_launch_count': (I64, [P]), 'swm_helm_apply': (I, [P, P, P]),
+        'swm_helm_solve_fp64': (I, [P, P, P, D, D, I, C.POINTER(C.c_int), C.POINTER(C.c_double)]),
+        'swm_helm_solve_mixed': (I, [P, P, P, D, D, D, I, C.POINTER(C.c_int), C.POINTER(C.c_int),
+                                     C.POINTER(C.c_double)]),
+        'swm_helm_autotune': (I, [P, P, D, D, I, I, C.POINTER(C.c_double), C.POINTER(C.c_int),
+                                  C.POINTER(C.c_int)]),
         'elsolv_sor_gpu_init': (I, [P]),
         'elsolv_sor_gpu_solve': (I, [P, P, P, D, I, C.POINTER(C.c_int), C.POINTER(C.c_double)]),
     }

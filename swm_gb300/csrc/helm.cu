@@ -1,0 +1,456 @@
+// helm.cu -- red-black SOR for the variable-coefficient Helmholtz problem
+// div(H^-1 grad psi) - lambda psi = rhs (extension of ElSolv_SOR.f90, whose
+// operator is the masked spherical Laplacian with a fixed Chebyshev
+// relaxation schedule and an absolute stopping rule).
+//
+// Same sweep structure as main_ElSolv_SOR (:176-211): colour 0 then colour 1
+// of (i + j), each point relaxed with the new values of the other colour.
+// Face coefficients are formed on the fly from 1/H (mean of the two cells);
+// land cells and the outer frame hold psi = 0.  Stopping: relative residual
+// ||rhs - A psi||_2 / ||rhs||_2, checked every CHECK sweeps in FP64.
+//
+// Two solvers: FP64 sweeps (bit for bit with the FP64 restatement, this file
+// is compiled without FMA contraction), and mixed precision: FP32 sweeps on
+// the correction equation A e = r, with r = rhs - A psi formed in FP64 and
+// psi += e accumulated in FP64 (iterative refinement).  An autotuner picks
+// the relaxation factor in a given range from short trial solves and the
+// thread-block shape of the sweep kernel from timings.
+#include <cmath>
+#include <cstring>
+#include <string>
+#include <vector>
+#include "ctx.h"
+
+namespace swm {
+
+constexpr int HELM_CHECK = 16;  // sweeps between residual checks
+constexpr int HELM_RED = 1024;  // reduction blocks
+
+// FP64 coefficients formed once: west and south face coefficients and the
+// reciprocal of the diagonal (the sweeps would otherwise be bound by the
+// FP64 pipe, which forms them and divides at every point of every sweep)
+__global__ void k_h_coeff64(int nx, int ny, const double *__restrict__ h, double rdx2, double rdy2, double lambda,
+                            double *cx, double *cy, double *rcc) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x, j = blockIdx.y * blockDim.y + threadIdx.y;
+  if (i >= nx || j >= ny) return;
+  const size_t k = (size_t)i + (size_t)nx * j;
+  const double hk = h[k];
+  const double cxw = i > 0 ? (0.5 * (hk + h[k - 1])) * rdx2 : 0.;
+  const double cxe = i < nx - 1 ? (0.5 * (h[k + 1] + hk)) * rdx2 : 0.;
+  const double cys = j > 0 ? (0.5 * (hk + h[k - nx])) * rdy2 : 0.;
+  const double cyn = j < ny - 1 ? (0.5 * (h[k + nx] + hk)) * rdy2 : 0.;
+  cx[k] = cxw;
+  cy[k] = cys;
+  rcc[k] = 1. / (-(((cxw + cxe) + cys) + cyn) - lambda);
+}
+
+__global__ void k_h_sweep64(int nx, int ny, const double *__restrict__ cx, const double *__restrict__ cy,
+                            const double *__restrict__ rcc, const int8_t *__restrict__ mask,
+                            const double *__restrict__ rhs, double *psi, double omega, int colour) {
+  const int j = blockIdx.y * blockDim.y + threadIdx.y;
+  const int i = 2 * (blockIdx.x * blockDim.x + threadIdx.x) + ((j + colour) & 1);
+  if (i >= nx || j >= ny) return;
+  const size_t k = (size_t)i + (size_t)nx * j;
+  if (!mask[k]) return;
+  const double cxe = i < nx - 1 ? cx[k + 1] : 0., cyn = j < ny - 1 ? cy[k + nx] : 0.;
+  const double w = i > 0 ? psi[k - 1] : 0., e = i < nx - 1 ? psi[k + 1] : 0.;
+  const double s = j > 0 ? psi[k - nx] : 0., n = j < ny - 1 ? psi[k + nx] : 0.;
+  const double off = cx[k] * w + cxe * e + cy[k] * s + cyn * n;
+  const double gs = (rhs[k] - off) * rcc[k];
+  psi[k] = psi[k] + omega * (gs - psi[k]);
+}
+
+template <typename T>
+__global__ void k_h_sweep(int nx, int ny, const T *__restrict__ h, const int8_t *__restrict__ mask,
+                          const T *__restrict__ rhs, T *psi, T rdx2, T rdy2, T lambda, T omega, int colour) {
+  const int j = blockIdx.y * blockDim.y + threadIdx.y;
+  const int i = 2 * (blockIdx.x * blockDim.x + threadIdx.x) + ((j + colour) & 1);
+  if (i >= nx || j >= ny) return;
+  const size_t k = (size_t)i + (size_t)nx * j;
+  if (!mask[k]) return;
+  const T hk = h[k];
+  const T cxw = i > 0 ? (T(0.5) * (hk + h[k - 1])) * rdx2 : T(0);
+  const T cxe = i < nx - 1 ? (T(0.5) * (h[k + 1] + hk)) * rdx2 : T(0);
+  const T cys = j > 0 ? (T(0.5) * (hk + h[k - nx])) * rdy2 : T(0);
+  const T cyn = j < ny - 1 ? (T(0.5) * (h[k + nx] + hk)) * rdy2 : T(0);
+  const T cc = -(((cxw + cxe) + cys) + cyn) - lambda;
+  const T w = i > 0 ? psi[k - 1] : T(0), e = i < nx - 1 ? psi[k + 1] : T(0);
+  const T s = j > 0 ? psi[k - nx] : T(0), n = j < ny - 1 ? psi[k + nx] : T(0);
+  const T off = cxw * w + cxe * e + cys * s + cyn * n;
+  const T gs = (rhs[k] - off) / cc;
+  psi[k] = psi[k] + omega * (gs - psi[k]);
+}
+
+// r = rhs - A psi on ocean cells (0 elsewhere); per-block partial sums of r^2
+// in FP64.  r may be null.
+template <typename T>
+__global__ void k_h_resid(int nx, int ny, const T *__restrict__ h, const int8_t *__restrict__ mask,
+                          const T *__restrict__ rhs, const T *__restrict__ psi, T rdx2, T rdy2, T lambda, double *r,
+                          double *partial) {
+  __shared__ double red[256];
+  double acc = 0.;
+  const size_t n = (size_t)nx * ny;
+  for (size_t k = (size_t)blockIdx.x * blockDim.x + threadIdx.x; k < n; k += (size_t)gridDim.x * blockDim.x) {
+    const int i = (int)(k % nx), j = (int)(k / nx);
+    double rr = 0.;
+    if (mask[k]) {
+      // in FP64 whatever the storage type: the residual of the stored iterate
+      const double hk = h[k], dx2 = rdx2, dy2 = rdy2;
+      const double cxw = i > 0 ? (0.5 * (hk + (double)h[k - 1])) * dx2 : 0.;
+      const double cxe = i < nx - 1 ? (0.5 * ((double)h[k + 1] + hk)) * dx2 : 0.;
+      const double cys = j > 0 ? (0.5 * (hk + (double)h[k - nx])) * dy2 : 0.;
+      const double cyn = j < ny - 1 ? (0.5 * ((double)h[k + nx] + hk)) * dy2 : 0.;
+      const double cc = -(((cxw + cxe) + cys) + cyn) - (double)lambda;
+      const double w = i > 0 ? (double)psi[k - 1] : 0., e = i < nx - 1 ? (double)psi[k + 1] : 0.;
+      const double s = j > 0 ? (double)psi[k - nx] : 0., nn = j < ny - 1 ? (double)psi[k + nx] : 0.;
+      const double ap = cxw * w + cxe * e + cys * s + cyn * nn + cc * (double)psi[k];
+      rr = (double)rhs[k] - ap;
+    }
+    if (r) r[k] = rr;
+    acc += rr * rr;
+  }
+  red[threadIdx.x] = acc;
+  __syncthreads();
+  for (int w = blockDim.x / 2; w > 0; w >>= 1) {
+    if (threadIdx.x < w) red[threadIdx.x] += red[threadIdx.x + w];
+    __syncthreads();
+  }
+  if (threadIdx.x == 0) partial[blockIdx.x] = red[0];
+}
+
+__global__ void k_h_sumsq(const double *x, const int8_t *mask, size_t n, double *partial) {
+  __shared__ double red[256];
+  double acc = 0.;
+  for (size_t k = (size_t)blockIdx.x * blockDim.x + threadIdx.x; k < n; k += (size_t)gridDim.x * blockDim.x)
+    if (mask[k]) acc += x[k] * x[k];
+  red[threadIdx.x] = acc;
+  __syncthreads();
+  for (int w = blockDim.x / 2; w > 0; w >>= 1) {
+    if (threadIdx.x < w) red[threadIdx.x] += red[threadIdx.x + w];
+    __syncthreads();
+  }
+  if (threadIdx.x == 0) partial[blockIdx.x] = red[0];
+}
+
+__global__ void k_h_final(const double *partial, int nb, double *out) {
+  __shared__ double red[256];
+  double a = 0.;
+  for (int b = threadIdx.x; b < nb; b += blockDim.x) a += partial[b];
+  red[threadIdx.x] = a;
+  __syncthreads();
+  for (int w = blockDim.x / 2; w > 0; w >>= 1) {
+    if (threadIdx.x < w) red[threadIdx.x] += red[threadIdx.x + w];
+    __syncthreads();
+  }
+  if (threadIdx.x == 0) out[0] = red[0];
+}
+
+__global__ void k_h_to32(const double *r, float *r32, float *e32, size_t n, double inv_scale) {
+  size_t k = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (k < n) {
+    r32[k] = (float)(r[k] * inv_scale);
+    e32[k] = 0.f;
+  }
+}
+
+__global__ void k_h_axpy(double *psi, const float *e32, size_t n, double scale) {
+  size_t k = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (k < n) psi[k] = psi[k] + scale * (double)e32[k];
+}
+
+}  // namespace swm
+
+struct swm_helm {
+  double *cx = nullptr, *cy = nullptr, *rcc = nullptr;  // FP64 coefficients
+  int nx = 0, ny = 0;
+  size_t n = 0;
+  double dx = 0, dy = 0, lambda = 0;
+  cudaStream_t stream = nullptr;
+  double *hinv = nullptr, *psi = nullptr, *rhs = nullptr, *r = nullptr, *partial = nullptr, *out = nullptr;
+  double *host = nullptr;  // pinned, 1 double
+  float *hinv32 = nullptr, *e32 = nullptr, *r32 = nullptr;
+  int8_t *mask = nullptr;
+  dim3 blk = dim3(64, 4);
+  int64_t launches = 0;
+};
+
+namespace {
+using namespace swm;
+
+#define HTRY(x)                          \
+  do {                                   \
+    int rc_ = (x);                       \
+    if (rc_ != SWM_GPU_OK) return rc_;   \
+  } while (0)
+
+dim3 sweep_grid(const swm_helm *h, dim3 b) {
+  return dim3((unsigned)(((h->nx + 1) / 2 + b.x - 1) / b.x), (unsigned)((h->ny + b.y - 1) / b.y));
+}
+
+void sweep64(swm_helm *h, double omega, dim3 b) {
+  const dim3 g = sweep_grid(h, b);
+  for (int colour = 0; colour < 2; colour++)
+    k_h_sweep64<<<g, b, 0, h->stream>>>(h->nx, h->ny, h->cx, h->cy, h->rcc, h->mask, h->rhs, h->psi, omega, colour);
+  h->launches += 2;
+}
+
+template <typename T>
+void sweep(swm_helm *h, const T *hh, const T *rhs, T *psi, T omega, dim3 b) {
+  const dim3 g = sweep_grid(h, b);
+  const T rdx2 = T(1. / (h->dx * h->dx)), rdy2 = T(1. / (h->dy * h->dy)), lam = T(h->lambda);
+  for (int colour = 0; colour < 2; colour++)
+    k_h_sweep<T><<<g, b, 0, h->stream>>>(h->nx, h->ny, hh, h->mask, rhs, psi, rdx2, rdy2, lam, omega, colour);
+  h->launches += 2;
+}
+
+// ||rhs - A psi||^2 (FP64 accumulation); r written when wanted
+template <typename T>
+int resid2(swm_helm *h, const T *hh, const T *rhs, const T *psi, double *r, double *out) {
+  const T rdx2 = T(1. / (h->dx * h->dx)), rdy2 = T(1. / (h->dy * h->dy)), lam = T(h->lambda);
+  k_h_resid<T><<<HELM_RED, 256, 0, h->stream>>>(h->nx, h->ny, hh, h->mask, rhs, psi, rdx2, rdy2, lam, r,
+                                                h->partial);
+  k_h_final<<<1, 256, 0, h->stream>>>(h->partial, HELM_RED, h->out);
+  h->launches += 2;
+  SWM_CK(cudaGetLastError());
+  SWM_CK(cudaMemcpyAsync(h->host, h->out, 8, cudaMemcpyDeviceToHost, h->stream));
+  SWM_CK(cudaStreamSynchronize(h->stream));
+  *out = h->host[0];
+  return SWM_GPU_OK;
+}
+
+int rhs_norm(swm_helm *h, double *bn) {
+  k_h_sumsq<<<HELM_RED, 256, 0, h->stream>>>(h->rhs, h->mask, h->n, h->partial);
+  k_h_final<<<1, 256, 0, h->stream>>>(h->partial, HELM_RED, h->out);
+  h->launches += 2;
+  SWM_CK(cudaGetLastError());
+  SWM_CK(cudaMemcpyAsync(h->host, h->out, 8, cudaMemcpyDeviceToHost, h->stream));
+  SWM_CK(cudaStreamSynchronize(h->stream));
+  *bn = std::sqrt(h->host[0]);
+  return SWM_GPU_OK;
+}
+
+// FP32 sweeps on A e = r32 from e = 0 until ||r32 - A e|| <= tol ||r32||,
+// until binary32 rounding stops the progress (a check that gains less than
+// STALL over the previous one), or max_sweeps; returns the sweeps done and
+// the reached relative residual
+constexpr double STALL = 0.7;
+int inner32(swm_helm *h, float omega, double tol, int max_sweeps, int *sweeps, double *rel) {
+  double rn2 = 0.;
+  // ||r32||: residual of e = 0
+  HTRY(resid2<float>(h, h->hinv32, h->r32, h->e32, nullptr, &rn2));
+  const double rn = std::sqrt(rn2);
+  int s = 0, checks = 0;
+  double rr = 1., prev = 1.;
+  while (s < max_sweeps) {
+    int blk = std::min(HELM_CHECK, max_sweeps - s);
+    for (int q = 0; q < blk; q++) sweep<float>(h, h->hinv32, h->r32, h->e32, omega, h->blk);
+    s += blk;
+    double e2 = 0.;
+    HTRY(resid2<float>(h, h->hinv32, h->r32, h->e32, nullptr, &e2));
+    rr = rn > 0 ? std::sqrt(e2) / rn : 0.;
+    if (rr <= tol || (++checks >= 2 && rr > STALL * prev)) break;
+    prev = rr;
+  }
+  *sweeps = s;
+  *rel = rr;
+  return SWM_GPU_OK;
+}
+
+void helm_free(swm_helm *h) {
+  if (!h) return;
+  if (h->stream) cudaStreamSynchronize(h->stream);
+  cudaFree(h->hinv); cudaFree(h->psi); cudaFree(h->rhs); cudaFree(h->r); cudaFree(h->partial); cudaFree(h->out);
+  cudaFreeHost(h->host);
+  cudaFree(h->hinv32); cudaFree(h->e32); cudaFree(h->r32); cudaFree(h->mask);
+  cudaFree(h->cx); cudaFree(h->cy); cudaFree(h->rcc);
+  if (h->stream) cudaStreamDestroy(h->stream);
+  delete h;
+}
+
+}  // namespace
+
+extern "C" {
+
+int swm_helm_create(int nx, int ny, double dx, double dy, double lambda, const double *H, const int8_t *ocean,
+                    swm_helm **out) {
+  SWM_REQUIRE(nx >= 3 && ny >= 3 && dx > 0 && dy > 0 && H && ocean && out, "swm_helm_create: bad arguments");
+  *out = nullptr;
+  swm_helm *h = new swm_helm();
+  h->nx = nx; h->ny = ny; h->n = (size_t)nx * ny; h->dx = dx; h->dy = dy; h->lambda = lambda;
+  const size_t n = h->n;
+  std::vector<double> hinv(n);
+  std::vector<float> hinv32(n);
+  for (size_t k = 0; k < n; k++) {
+    if (!(H[k] > 0.)) {
+      helm_free(h);
+      set_error("swm_helm_create: depth must be positive everywhere (land is given by the ocean mask)");
+      return SWM_GPU_EINVAL;
+    }
+    hinv[k] = 1. / H[k];
+    hinv32[k] = (float)hinv[k];
+  }
+  bool ok = cudaStreamCreateWithFlags(&h->stream, cudaStreamNonBlocking) == cudaSuccess &&
+            cudaMalloc((void **)&h->hinv, n * 8) == cudaSuccess && cudaMalloc((void **)&h->psi, n * 8) == cudaSuccess &&
+            cudaMalloc((void **)&h->rhs, n * 8) == cudaSuccess && cudaMalloc((void **)&h->r, n * 8) == cudaSuccess &&
+            cudaMalloc((void **)&h->partial, HELM_RED * 8) == cudaSuccess &&
+            cudaMalloc((void **)&h->out, 8) == cudaSuccess && cudaMallocHost((void **)&h->host, 8) == cudaSuccess &&
+            cudaMalloc((void **)&h->hinv32, n * 4) == cudaSuccess && cudaMalloc((void **)&h->e32, n * 4) == cudaSuccess &&
+            cudaMalloc((void **)&h->r32, n * 4) == cudaSuccess && cudaMalloc((void **)&h->mask, n) == cudaSuccess &&
+            cudaMalloc((void **)&h->cx, n * 8) == cudaSuccess && cudaMalloc((void **)&h->cy, n * 8) == cudaSuccess &&
+            cudaMalloc((void **)&h->rcc, n * 8) == cudaSuccess;
+  if (!ok) {
+    helm_free(h);
+    set_error("swm_helm_create: device allocation failed");
+    return SWM_GPU_ENOMEM;
+  }
+  SWM_CK(cudaMemcpyAsync(h->hinv, hinv.data(), n * 8, cudaMemcpyHostToDevice, h->stream));
+  SWM_CK(cudaMemcpyAsync(h->hinv32, hinv32.data(), n * 4, cudaMemcpyHostToDevice, h->stream));
+  SWM_CK(cudaMemcpyAsync(h->mask, ocean, n, cudaMemcpyHostToDevice, h->stream));
+  dim3 b(32, 8), g((nx + 31) / 32, (ny + 7) / 8);
+  k_h_coeff64<<<g, b, 0, h->stream>>>(nx, ny, h->hinv, 1. / (dx * dx), 1. / (dy * dy), lambda, h->cx, h->cy, h->rcc);
+  h->launches++;
+  SWM_CK(cudaGetLastError());
+  SWM_CK(cudaStreamSynchronize(h->stream));
+  *out = h;
+  return SWM_GPU_OK;
+}
+
+int swm_helm_destroy(swm_helm *h) {
+  helm_free(h);
+  return SWM_GPU_OK;
+}
+
+void *swm_helm_stream(swm_helm *h) { return h ? (void *)h->stream : nullptr; }
+int64_t swm_helm_launch_count(swm_helm *h) { return h ? h->launches : -1; }
+
+// out = A psi (ocean cells; 0 elsewhere), FP64
+int swm_helm_apply(swm_helm *h, const double *psi, double *out) {
+  SWM_REQUIRE(h && psi && out, "swm_helm_apply: bad arguments");
+  SWM_CK(cudaMemcpyAsync(h->psi, psi, h->n * 8, cudaMemcpyHostToDevice, h->stream));
+  SWM_CK(cudaMemsetAsync(h->rhs, 0, h->n * 8, h->stream));
+  double r2;
+  HTRY(resid2<double>(h, h->hinv, h->rhs, h->psi, h->r, &r2));  // r = 0 - A psi
+  std::vector<double> t(h->n);
+  SWM_CK(cudaMemcpy(t.data(), h->r, h->n * 8, cudaMemcpyDeviceToHost));
+  for (size_t k = 0; k < h->n; k++) out[k] = -t[k];
+  return SWM_GPU_OK;
+}
+
+// FP64 red-black SOR from psi (in/out) to ||rhs - A psi|| < rtol ||rhs||
+// (checked every 16 sweeps) or max_sweeps.
+int swm_helm_solve_fp64(swm_helm *h, const double *rhs, double *psi, double omega, double rtol, int max_sweeps,
+                        int *sweeps, double *relres) {
+  SWM_REQUIRE(h && rhs && psi && max_sweeps > 0, "swm_helm_solve_fp64: bad arguments");
+  SWM_CK(cudaMemcpyAsync(h->rhs, rhs, h->n * 8, cudaMemcpyHostToDevice, h->stream));
+  SWM_CK(cudaMemcpyAsync(h->psi, psi, h->n * 8, cudaMemcpyHostToDevice, h->stream));
+  double bn;
+  HTRY(rhs_norm(h, &bn));
+  int s = 0;
+  double rel = 1.;
+  while (s < max_sweeps) {
+    int blk = std::min(HELM_CHECK, max_sweeps - s);
+    for (int q = 0; q < blk; q++) sweep64(h, omega, h->blk);
+    s += blk;
+    double r2;
+    HTRY(resid2<double>(h, h->hinv, h->rhs, h->psi, nullptr, &r2));
+    rel = bn > 0 ? std::sqrt(r2) / bn : std::sqrt(r2);
+    if (rel < rtol) break;
+  }
+  SWM_CK(cudaMemcpyAsync(psi, h->psi, h->n * 8, cudaMemcpyDeviceToHost, h->stream));
+  SWM_CK(cudaStreamSynchronize(h->stream));
+  if (sweeps) *sweeps = s;
+  if (relres) *relres = rel;
+  if (rel < rtol) return SWM_GPU_OK;
+  set_error("swm_helm_solve_fp64: relative residual above rtol after max_sweeps");
+  return SWM_GPU_ENOT_CONVERGED;
+}
+
+// Mixed precision: residual r = rhs - A psi in FP64, FP32 SOR sweeps on
+// A e = r / ||r|| until its residual falls by inner_tol, psi += ||r|| e in
+// FP64; repeated until the FP64 relative residual is below rtol.
+int swm_helm_solve_mixed(swm_helm *h, const double *rhs, double *psi, double omega, double rtol, double inner_tol,
+                         int max_sweeps, int *sweeps, int *outer, double *relres) {
+  SWM_REQUIRE(h && rhs && psi && max_sweeps > 0 && inner_tol > 0, "swm_helm_solve_mixed: bad arguments");
+  SWM_CK(cudaMemcpyAsync(h->rhs, rhs, h->n * 8, cudaMemcpyHostToDevice, h->stream));
+  SWM_CK(cudaMemcpyAsync(h->psi, psi, h->n * 8, cudaMemcpyHostToDevice, h->stream));
+  double bn;
+  HTRY(rhs_norm(h, &bn));
+  const unsigned nb = (unsigned)((h->n + 255) / 256);
+  int s = 0, o = 0;
+  double rel = 1.;
+  for (;;) {
+    double r2;
+    HTRY(resid2<double>(h, h->hinv, h->rhs, h->psi, h->r, &r2));
+    const double rn = std::sqrt(r2);
+    rel = bn > 0 ? rn / bn : rn;
+    if (rel < rtol || s >= max_sweeps || rn == 0.) break;
+    k_h_to32<<<nb, 256, 0, h->stream>>>(h->r, h->r32, h->e32, h->n, 1. / rn);
+    int si = 0;
+    double ri;
+    HTRY(inner32(h, (float)omega, inner_tol, max_sweeps - s, &si, &ri));
+    k_h_axpy<<<nb, 256, 0, h->stream>>>(h->psi, h->e32, h->n, rn);
+    h->launches += 2;
+    s += si;
+    o++;
+  }
+  SWM_CK(cudaGetLastError());
+  SWM_CK(cudaMemcpyAsync(psi, h->psi, h->n * 8, cudaMemcpyDeviceToHost, h->stream));
+  SWM_CK(cudaStreamSynchronize(h->stream));
+  if (sweeps) *sweeps = s;
+  if (outer) *outer = o;
+  if (relres) *relres = rel;
+  if (rel < rtol) return SWM_GPU_OK;
+  set_error("swm_helm_solve_mixed: relative residual above rtol after max_sweeps");
+  return SWM_GPU_ENOT_CONVERGED;
+}
+
+// Autotuner: the sweep kernel's block shape by timing FP32 sweeps, then the
+// relaxation factor in [omega_lo, omega_hi] (ngrid values) as the one whose
+// trial solve of trial_sweeps FP32 sweeps on A e = rhs / ||rhs|| from e = 0
+// reaches the smallest residual.
+int swm_helm_autotune(swm_helm *h, const double *rhs, double omega_lo, double omega_hi, int ngrid,
+                      int trial_sweeps, double *omega, int *block_x, int *block_y) {
+  SWM_REQUIRE(h && rhs && ngrid >= 1 && trial_sweeps > 0 && omega_lo > 0 && omega_hi < 2 && omega_lo <= omega_hi,
+              "swm_helm_autotune: bad arguments");
+  SWM_CK(cudaMemcpyAsync(h->rhs, rhs, h->n * 8, cudaMemcpyHostToDevice, h->stream));
+  double bn;
+  HTRY(rhs_norm(h, &bn));
+  const unsigned nb = (unsigned)((h->n + 255) / 256);
+  k_h_to32<<<nb, 256, 0, h->stream>>>(h->rhs, h->r32, h->e32, h->n, bn > 0 ? 1. / bn : 1.);
+  h->launches++;
+  // block shape
+  const dim3 shapes[4] = {dim3(32, 8), dim3(64, 4), dim3(128, 2), dim3(256, 1)};
+  cudaEvent_t a, b;
+  SWM_CK(cudaEventCreate(&a));
+  SWM_CK(cudaEventCreate(&b));
+  float tbest = 1e30f;
+  for (const dim3 &shp : shapes) {
+    sweep<float>(h, h->hinv32, h->r32, h->e32, 1.f, shp);
+    SWM_CK(cudaEventRecord(a, h->stream));
+    for (int q = 0; q < 4; q++) sweep<float>(h, h->hinv32, h->r32, h->e32, 1.f, shp);
+    SWM_CK(cudaEventRecord(b, h->stream));
+    SWM_CK(cudaEventSynchronize(b));
+    float ms;
+    SWM_CK(cudaEventElapsedTime(&ms, a, b));
+    if (ms < tbest) { tbest = ms; h->blk = shp; }
+  }
+  cudaEventDestroy(a);
+  cudaEventDestroy(b);
+  // relaxation factor
+  double best = omega_lo, rbest = 1e300;
+  for (int q = 0; q < ngrid; q++) {
+    const double om = ngrid == 1 ? omega_lo : omega_lo + (omega_hi - omega_lo) * q / (ngrid - 1);
+    k_h_to32<<<nb, 256, 0, h->stream>>>(h->rhs, h->r32, h->e32, h->n, bn > 0 ? 1. / bn : 1.);
+    h->launches++;
+    for (int s = 0; s < trial_sweeps; s++) sweep<float>(h, h->hinv32, h->r32, h->e32, (float)om, h->blk);
+    double e2;
+    HTRY(resid2<float>(h, h->hinv32, h->r32, h->e32, nullptr, &e2));
+    if (e2 < rbest) { rbest = e2; best = om; }
+  }
+  if (omega) *omega = best;
+  if (block_x) *block_x = (int)h->blk.x;
+  if (block_y) *block_y = (int)h->blk.y;
+  return SWM_GPU_OK;
+}
+
+}  // extern "C"

@@ -149,7 +149,7 @@ def _grf(ny, nx, slope, rng):
     return f - f.mean()
 
 
-def tracer_flow(cells=2048, dx=2.5e3, seed_index=3, nsteps=5000, depth=100.0, peak_speed=0.5, n_tracers=2,
+def tracer_flow(cells=2048, dx=2.5e3, seed_index=2, nsteps=5000, depth=100.0, peak_speed=0.5, n_tracers=2,
                 kappa=50.0, relax_days=30.0, dt=60.0, flux=1):
     """Two passive tracers in a steady nondivergent flow (prescribed: the SWM
     state is frozen), closed box with a one-cell land rim, uniform depth.
@@ -187,3 +187,39 @@ def tracer_flow(cells=2048, dx=2.5e3, seed_index=3, nsteps=5000, depth=100.0, pe
         case['tracers'].append(dict(varid='C%d' % t, kappa_h=kappa, cons=0.0, gamma_c=1.0 / (relax_days * DAY),
                                     field_C=c, field_C0=c.copy(), field_gamma_C=None, field_cons=None))
     return case
+
+
+def _smooth_field(ny, nx, corr_cells, rng):
+    """Unit-variance Gaussian random field with a Gaussian correlation of
+    corr_cells grid cells (white noise filtered in Fourier space)."""
+    fy = np.fft.fftfreq(ny)[:, None]
+    fx = np.fft.fftfreq(nx)[None, :]
+    filt = np.exp(-2.0 * (np.pi * corr_cells) ** 2 * (fx ** 2 + fy ** 2))
+    f = np.fft.ifft2(np.fft.fft2(rng.standard_normal((ny, nx))) * filt).real
+    return (f - f.mean()) / f.std()
+
+
+HELMHOLTZ_LAMBDA = 1.6e-12
+
+
+def helmholtz_case(cells=4096, dx=5e3, seed_index=3, lam=HELMHOLTZ_LAMBDA):
+    """Barotropic streamfunction problem div(H^-1 grad psi) - lam psi = rhs.
+
+    Depth: exp(log(1000 m) + g) with g a unit Gaussian random field of 200 km
+    correlation, clipped to 50-5000 m.  Coast: land where a second random
+    field (400 km correlation) exceeds its 85th percentile, plus the outer
+    frame (psi = 0 on land).  rhs: wind-curl-like random field of 500 km
+    correlation with standard deviation 1e-10, 0 on land.  lam = 1.6e-12 (per
+    m^3) keeps the Jacobi spectral radius near 0.9995 where H is shallowest,
+    so the best relaxation factor lies inside 1.8-1.99.
+    Returns dict(H, ocean (int8), rhs, dx, dy, lam)."""
+    rng = np.random.Generator(np.random.PCG64(20260 + seed_index))
+    n = cells
+    g = _smooth_field(n, n, 200e3 / dx, rng)
+    H = np.clip(np.exp(np.log(1000.0) + g), 50.0, 5000.0)
+    land = _smooth_field(n, n, 400e3 / dx, rng)
+    ocean = (land <= np.quantile(land, 0.85)).astype(np.int8)
+    ocean[0, :] = ocean[-1, :] = 0
+    ocean[:, 0] = ocean[:, -1] = 0
+    rhs = 1e-10 * _smooth_field(n, n, 500e3 / dx, rng) * ocean
+    return dict(H=H, ocean=ocean, rhs=rhs, dx=dx, dy=dx, lam=lam)

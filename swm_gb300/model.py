@@ -219,3 +219,61 @@ class GpuEnsemble:
 
     def rows(self):
         return self.L.swm_gpu_ensemble_rows(self.ens)
+
+
+class GpuHelmholtz:
+    """div(H^-1 grad psi) - lam psi = rhs solved by red-black SOR on the GPU
+    (swm_helm_*): FP64 sweeps or FP32 sweeps with FP64 refinement."""
+
+    def __init__(self, H, ocean, dx, dy, lam):
+        self.L = lib()
+        self.shape = H.shape
+        ny, nx = H.shape
+        h = _f64(H)
+        m = np.ascontiguousarray(ocean, dtype=np.int8)
+        out = C.c_void_p()
+        check(self.L.swm_helm_create(nx, ny, dx, dy, lam, _p(h), _p(m), C.byref(out)))
+        self.h = out
+
+    def close(self):
+        if self.h:
+            self.L.swm_helm_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def apply(self, psi):
+        out = np.zeros(self.shape)
+        check(self.L.swm_helm_apply(self.h, _p(_f64(psi)), _p(out)))
+        return out
+
+    def solve(self, rhs, psi0=None, omega=1.9, rtol=1e-10, max_sweeps=100000, mixed=False, inner_tol=1e-4,
+              raise_on_fail=True):
+        psi = np.zeros(self.shape) if psi0 is None else np.array(psi0, dtype=np.float64)
+        b = _f64(rhs)
+        sw, outer, rel = C.c_int(), C.c_int(), C.c_double()
+        if mixed:
+            rc = self.L.swm_helm_solve_mixed(self.h, _p(b), _p(psi), omega, rtol, inner_tol, max_sweeps,
+                                             C.byref(sw), C.byref(outer), C.byref(rel))
+        else:
+            rc = self.L.swm_helm_solve_fp64(self.h, _p(b), _p(psi), omega, rtol, max_sweeps, C.byref(sw),
+                                            C.byref(rel))
+        if raise_on_fail or rc not in (0, 4):
+            check(rc)
+        return psi, sw.value, outer.value, rel.value, rc
+
+    def autotune(self, rhs, lo=1.8, hi=1.99, ngrid=12, trial_sweeps=64):
+        om, bx, by = C.c_double(), C.c_int(), C.c_int()
+        check(self.L.swm_helm_autotune(self.h, _p(_f64(rhs)), lo, hi, ngrid, trial_sweeps, C.byref(om),
+                                       C.byref(bx), C.byref(by)))
+        return om.value, (bx.value, by.value)
+
+    def stream(self):
+        return self.L.swm_helm_stream(self.h)
+
+    def launch_count(self):
+        return self.L.swm_helm_launch_count(self.h)
