@@ -203,7 +203,7 @@ def ours(args, rank, ws):
     line['roofline'] = {'bound': 'hbm', 'achieved': achieved, 'peak': peak, 'unit': 'GB/s',
                         'frac': achieved / peak, 'traffic': traffic, 'peak_kind': kind,
                         'algorithmic_bytes_per_launch': alg,
-                        'kernel': 'k_march<2,16>' if args.path == 'fused_fp32c' else args.path}
+                        'kernel': 'k_march<2>' if args.path == 'fused_fp32c' else args.path}
     if args.device_only:
         g.close()
         return line
@@ -319,7 +319,7 @@ def ensemble_measurement(args, n_members=256, steps=200, one_by_one=True):
     peak, kind = peaks()
     ach = 89 * pts / (ms_step * 1e-3) / 1e9
     out['roofline'] = {'bound': 'hbm', 'achieved': ach, 'peak': peak, 'unit': 'GB/s', 'frac': ach / peak,
-                       'peak_kind': kind, 'kernel': 'k_march_ens<1,%d>' % ens.rows(), 'bytes_per_point': 89}
+                       'peak_kind': kind, 'kernel': 'k_march_ens<1>', 'bytes_per_point': 89}
     ens.close()
     for g in ms:
         g.close()

@@ -26,6 +26,8 @@ def nvcc():
 
 def _compile(src, extra):
     obj = os.path.join(BUILD, src.replace('.cu', '.o'))
+    # SWM_GB300_NVCC_FLAGS: extra nvcc flags (e.g. -D tuning macros)
+    extra = list(extra) + os.environ.get('SWM_GB300_NVCC_FLAGS', '').split()
     cmd = [nvcc(), *ARCH, '-O3', '-lineinfo', '-std=c++17', '-Xcompiler', '-fPIC,-ffp-contract=off', '-Xptxas', '-v',
            '--expt-relaxed-constexpr', *extra, '-c', os.path.join(CSRC, src), '-o', obj]
     r = subprocess.run(cmd, capture_output=True, text=True)

@@ -63,11 +63,6 @@ __global__ void k_ens_integrals(const EnsInt *__restrict__ d, double *__restrict
   if (threadIdx.x < 3) out[3 * (size_t)blockIdx.x + threadIdx.x] = red[threadIdx.x][0];
 }
 
-static int rows_index(int r) {
-  for (int i = 0; i < 3; i++)
-    if (MARCH_ROWS[i] == r) return i;
-  return 1;
-}
 
 }  // namespace swm
 
@@ -78,8 +73,14 @@ struct swm_gpu_ensemble {
   cudaEvent_t done = nullptr;
   std::vector<cudaEvent_t> ev;
   P32 *tab = nullptr;  // [ENS_PHASES][n]
-  int2 *tiles[3] = {};
-  int ntiles[3] = {};
+  std::vector<int> cand;     // candidate rows per strip
+  std::vector<int2 *> tiles;  // tile list per candidate
+  std::vector<int> ntiles;
+  int rows_index(int r) const {
+    for (size_t i = 0; i < cand.size(); i++)
+      if (cand[i] == r) return (int)i;
+    return 0;
+  }
   int *next = nullptr;  // queue heads, one per phase
   cudaGraphExec_t graph = nullptr;
   int64_t launches = 0, graph_launches = 0;
@@ -121,7 +122,7 @@ int rotate_members(swm_gpu_ensemble *e, int64_t itt) {
 
 int ens_step(swm_gpu_ensemble *e, int64_t itt) {
   const size_t n = e->m.size();
-  const int ri = rows_index(e->rows);
+  const int ri = e->rows_index(e->rows);
   SWM_CK(cudaMemsetAsync(e->next + e->phase, 0, sizeof(int), e->stream));
   int rc = march_ens_launch(e->mix, e->rows, e->tab + (size_t)e->phase * n, e->tiles[ri], e->ntiles[ri],
                             e->next + e->phase, e->stream);
@@ -225,8 +226,12 @@ int swm_gpu_ensemble_create(swm_gpu_ctx *const *members, int n, swm_gpu_ensemble
   for (int i = 0; i < n; i++) fused_set_indices(members[i], n0, g0);
   // tiles for each candidate strip length
   const int ti = march_tile_cols(mix);
-  for (int r = 0; r < 3; r++) {
-    const int S = MARCH_ROWS[r];
+  e->cand.assign(MARCH_ROWS, MARCH_ROWS + MARCH_NROWS);
+  if (march_rows_override()) e->cand.assign(1, march_rows_override());
+  e->tiles.assign(e->cand.size(), nullptr);
+  e->ntiles.assign(e->cand.size(), 0);
+  for (size_t r = 0; r < e->cand.size(); r++) {
+    const int S = e->cand[r];
     std::vector<int2> t;
     for (int i = 0; i < n; i++) {
       const int nbx = (members[i]->nx + ti - 1) / ti, nrg = (members[i]->ny + S - 1) / S;
@@ -252,8 +257,8 @@ int swm_gpu_ensemble_create(swm_gpu_ctx *const *members, int n, swm_gpu_ensemble
   // rewrites level N0p1 and slot 3 only, which the first real step rewrites)
   if (join_members(e) != SWM_GPU_OK) return fail(SWM_GPU_ECUDA);
   int best = 16;
-  int rc = march_pick_rows(e->stream, 3, [&](int r) {
-    const int ri = rows_index(r);
+  int rc = march_pick_rows(e->stream, 3, e->cand, [&](int r) {
+    const int ri = e->rows_index(r);
     cudaMemsetAsync(e->next, 0, sizeof(int), e->stream);
     march_ens_launch(mix, r, e->tab, e->tiles[ri], e->ntiles[ri], e->next, e->stream);
   }, &best);

@@ -30,14 +30,17 @@ struct P32 {
 };
 
 // candidate rows per warp strip of the step kernel
-constexpr int MARCH_ROWS[3] = {8, 16, 32};
+constexpr int MARCH_NROWS = 4;
+constexpr int MARCH_ROWS[MARCH_NROWS] = {8, 16, 24, 32};
 
 std::vector<double> fp32c_rows(const swm_gpu_ctx *c);
 void make_p32(const swm_gpu_ctx *c, int64_t itt, P32 &p);
 void march_launch(swm_gpu_ctx *c, const P32 &p);
 int march_tile_cols(int mix);          // columns a warp strip updates
 int march_rows_override();             // SWM_GB300_MARCH_S, 0 when unset
-int march_pick_rows(cudaStream_t st, int reps, const std::function<void(int)> &launch, int *best);
+std::vector<int> march_row_candidates(int mix, int nx, int ny);
+int march_pick_rows(cudaStream_t st, int reps, const std::vector<int> &cands, const std::function<void(int)> &launch,
+                    int *best);
 int march_autotune(swm_gpu_ctx *c, const P32 &p);
 void fused_indices(const swm_gpu_ctx *c, int *n0, int *g0);
 void fused_set_indices(swm_gpu_ctx *c, int n0, int g0);

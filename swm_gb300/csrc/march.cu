@@ -20,10 +20,17 @@
 // tendencies), swm_lateralmixing_module.f90:66-240 (stress tensor),
 // time_integration_module.f90:74-112 (Adams-Bashforth).
 #include <cmath>
+#include <algorithm>
 #include <cstdlib>
 #include <type_traits>
 #include <vector>
 #include "fused32.h"
+
+// minimum resident blocks per SM asked of the register allocator, and the
+// unroll factor of the row loop (tuning knobs, set with -D)
+#ifndef MARCH_MINB
+#define MARCH_MINB 4
+#endif
 
 namespace swm {
 
@@ -61,8 +68,8 @@ __device__ __forceinline__ void comp_damp(float hi, float lo, float inc, float d
 
 // One warp updates rows ry0 .. ry0+S-1 of strip bx (columns bx*TI ..
 // bx*TI+TI-1) of the basin p describes.
-template <int MIX, int S>
-__device__ __forceinline__ void march_strip(const P32 &p, const int bx, const int ry0, const int lane) {
+template <int MIX>
+__device__ __forceinline__ void march_strip(const P32 &p, const int bx, const int ry0, const int lane, const int S) {
   constexpr int H = MIX == 2 ? 2 : 1;
   constexpr int TI = 32 - 2 * H;
   const int nx = p.nx, ny = p.ny;
@@ -353,6 +360,11 @@ __device__ __forceinline__ void march_strip(const P32 &p, const int bx, const in
 #undef HALF2
   };
 
+#ifdef MARCH_UNROLL
+#define MARCH_PRAGMA_(x) _Pragma(#x)
+#define MARCH_PRAGMA(x) MARCH_PRAGMA_(x)
+  MARCH_PRAGMA(unroll MARCH_UNROLL)
+#endif
   for (; J < jend; J++) {
 #pragma unroll
     for (int a = 3; a > 0; a--) {
@@ -380,27 +392,34 @@ __device__ __forceinline__ void march_strip(const P32 &p, const int bx, const in
       n_uh = p.uh0[kn]; n_ul = p.ul0[kn]; n_vh = p.vh0[kn]; n_vl = p.vl0[kn];
       n_eh = p.eh0[kn]; n_el = p.el0[kn]; n_he = p.He[kn];
     }
+    // rows ry0-3 and ry0-2 only fill the windows: nothing computed from them
+    // reaches an output row (the first, ry0, needs first-pass stresses from
+    // row ry0-2 on, formed once row ry0-1 is in)
+    if (J < ry0 - 1) continue;
     const bool interior = __all_sync(FULL, (m[0] & m[1] & m[2] & m[3] & 0xFFFu) == 0xFFFu);
     if (interior) body(std::true_type{});
     else body(std::false_type{});
   }
 }
 
-template <int MIX, int S>
-__global__ void __launch_bounds__(128) k_march(P32 p) {
-  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-  const int ry0 = (blockIdx.y * 4 + warp) * S;
+// block b takes strip b % nstrips; its four warps take four consecutive row
+// groups of that strip (their look-ahead rows overlap and meet in L1)
+template <int MIX>
+__global__ void __launch_bounds__(128, MARCH_MINB) k_march(P32 p, int S, int nstrips) {
+  const int lane = threadIdx.x & 31;
+  const int ry0 = ((blockIdx.x / nstrips) * 4 + (threadIdx.x >> 5)) * S;
   if (ry0 >= p.ny) return;  // whole warp leaves together
-  march_strip<MIX, S>(p, blockIdx.x, ry0, lane);
+  march_strip<MIX>(p, blockIdx.x % nstrips, ry0, lane, S);
 }
 
 // Ensemble of basins in one persistent launch: every warp takes (member,
 // strip, row group) tiles from the queue until it is empty.  A tile is
 // int2 {member, strip << 16 | row group}; the member's parameter block is
 // copied into the warp's slice of shared memory first.
-template <int MIX, int S>
-__global__ void __launch_bounds__(128) k_march_ens(const P32 *__restrict__ tab, const int2 *__restrict__ tiles,
-                                                   int ntiles, int *__restrict__ next) {
+template <int MIX>
+__global__ void __launch_bounds__(128, MARCH_MINB) k_march_ens(const P32 *__restrict__ tab,
+                                                               const int2 *__restrict__ tiles, int ntiles,
+                                                               int *__restrict__ next, int S) {
   __shared__ P32 sp[4];
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
   for (;;) {
@@ -413,7 +432,7 @@ __global__ void __launch_bounds__(128) k_march_ens(const P32 *__restrict__ tab, 
     int *dst = reinterpret_cast<int *>(&sp[warp]);
     for (int k = lane; k < (int)(sizeof(P32) / sizeof(int)); k += 32) dst[k] = src[k];
     __syncwarp();
-    march_strip<MIX, S>(sp[warp], d.y >> 16, (d.y & 0xffff) * S, lane);
+    march_strip<MIX>(sp[warp], d.y >> 16, (d.y & 0xffff) * S, lane, S);
     __syncwarp();
   }
 }
@@ -451,36 +470,54 @@ std::vector<double> fp32c_rows(const swm_gpu_ctx *c) {
 
 int march_tile_cols(int mix) { return 32 - 2 * (mix == 2 ? 2 : 1); }
 
-// rows per warp strip: longer strips recompute fewer look-ahead rows, shorter
-// ones give more warps.  One of MARCH_ROWS, picked by timing (march_autotune)
-// unless SWM_GB300_MARCH_S names one.
-template <int MIX, int S>
-static void launch_s(const P32 &p, cudaStream_t st) {
-  const int ti = march_tile_cols(MIX);
-  dim3 grid((p.nx + ti - 1) / ti, (p.ny + 4 * S - 1) / (4 * S));
-  k_march<MIX, S><<<grid, 128, 0, st>>>(p);
-}
-
 template <int MIX>
-static void launch_mix(const P32 &p, int s, cudaStream_t st) {
-  if (s == 8) launch_s<MIX, 8>(p, st);
-  else if (s == 32) launch_s<MIX, 32>(p, st);
-  else launch_s<MIX, 16>(p, st);
+static int resident_blocks_of() {  // blocks of k_march resident on the whole GPU at once
+  static int b = 0;
+  if (!b) {
+    int per_sm = 0, sms = 0, dev = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_march<MIX>, 128, 0);
+    b = sms * (per_sm > 0 ? per_sm : 1);
+  }
+  return b;
 }
 
-static void launch_any(const P32 &p, int s, cudaStream_t st) {
-  if (p.mix == 2) launch_mix<2>(p, s, st);
-  else if (p.mix == 1) launch_mix<1>(p, s, st);
-  else launch_mix<0>(p, s, st);
+static int resident_blocks(int mix) {
+  return mix == 2 ? resident_blocks_of<2>() : (mix == 1 ? resident_blocks_of<1>() : resident_blocks_of<0>());
+}
+
+// Candidate rows per warp strip: the fixed MARCH_ROWS and the lengths that
+// make the grid exactly one, two or three waves of resident blocks (a grid
+// slightly over a whole number of waves costs a whole extra wave).
+std::vector<int> march_row_candidates(int mix, int nx, int ny) {
+  std::vector<int> c(MARCH_ROWS, MARCH_ROWS + MARCH_NROWS);
+  const int nstrips = (nx + march_tile_cols(mix) - 1) / march_tile_cols(mix);
+  const int rb = resident_blocks(mix);
+  for (int waves = 1; waves <= 3; waves++) {
+    const int per_strip = waves * rb / nstrips;  // blocks of 4 row groups per strip
+    if (per_strip < 1) continue;
+    const int S = (ny + 4 * per_strip - 1) / (4 * per_strip);
+    if (S >= 4 && S <= 256) c.push_back(S);
+  }
+  std::sort(c.begin(), c.end());
+  c.erase(std::unique(c.begin(), c.end()), c.end());
+  return c;
+}
+
+static void launch_any(const P32 &p, int S, cudaStream_t st) {
+  const int nstrips = (p.nx + march_tile_cols(p.mix) - 1) / march_tile_cols(p.mix);
+  const unsigned blocks = (unsigned)(nstrips * ((p.ny + 4 * S - 1) / (4 * S)));
+  if (p.mix == 2) k_march<2><<<blocks, 128, 0, st>>>(p, S, nstrips);
+  else if (p.mix == 1) k_march<1><<<blocks, 128, 0, st>>>(p, S, nstrips);
+  else k_march<0><<<blocks, 128, 0, st>>>(p, S, nstrips);
 }
 
 int march_rows_override() {
   const char *e = getenv("SWM_GB300_MARCH_S");
   if (!e) return 0;
   int s = atoi(e);
-  for (int r : MARCH_ROWS)
-    if (r == s) return s;
-  return 0;
+  return s >= 4 && s <= 256 ? s : 0;
 }
 
 void march_launch(swm_gpu_ctx *c, const P32 &p) {
@@ -491,7 +528,8 @@ void march_launch(swm_gpu_ctx *c, const P32 &p) {
 // Mean time of `reps` launches per candidate; the step reads level n0 and
 // slots 1-2 and writes level n0p1 and slot 3 only, so repeating it leaves
 // the model state as one launch leaves it.
-int march_pick_rows(cudaStream_t st, int reps, const std::function<void(int)> &launch, int *best) {
+int march_pick_rows(cudaStream_t st, int reps, const std::vector<int> &cands, const std::function<void(int)> &launch,
+                    int *best) {
   int s = march_rows_override();
   if (s) {
     *best = s;
@@ -502,7 +540,7 @@ int march_pick_rows(cudaStream_t st, int reps, const std::function<void(int)> &l
   SWM_CK(cudaEventCreate(&b));
   float tbest = 1e30f;
   *best = 16;
-  for (int r : MARCH_ROWS) {
+  for (int r : cands) {
     launch(r);  // warm-up
     SWM_CK(cudaEventRecord(a, st));
     for (int k = 0; k < reps; k++) launch(r);
@@ -523,39 +561,33 @@ int march_pick_rows(cudaStream_t st, int reps, const std::function<void(int)> &l
 
 int march_autotune(swm_gpu_ctx *c, const P32 &p) {
   int s = 16;
-  int rc = march_pick_rows(c->stream, 5, [&](int r) { launch_any(p, r, c->stream); }, &s);
+  int rc = march_pick_rows(c->stream, 5, march_row_candidates(p.mix, p.nx, p.ny),
+                           [&](int r) { launch_any(p, r, c->stream); }, &s);
   if (rc != SWM_GPU_OK) return rc;
   c->march_rows = s;
   return SWM_GPU_OK;
 }
 
 // ---- ensemble launch ------------------------------------------------------
-template <int MIX, int S>
-static int ens_launch_s(const P32 *tab, const int2 *tiles, int ntiles, int *next, cudaStream_t st) {
+template <int MIX>
+static int ens_launch_m(const P32 *tab, const int2 *tiles, int ntiles, int *next, int S, cudaStream_t st) {
   static int blocks = 0;
   if (!blocks) {
     int per_sm = 0, sms = 0, dev = 0;
     SWM_CK(cudaGetDevice(&dev));
     SWM_CK(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
-    SWM_CK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_march_ens<MIX, S>, 128, 0));
+    SWM_CK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_march_ens<MIX>, 128, 0));
     blocks = sms * (per_sm > 0 ? per_sm : 1);
   }
   int need = (ntiles + 3) / 4;
-  k_march_ens<MIX, S><<<need < blocks ? need : blocks, 128, 0, st>>>(tab, tiles, ntiles, next);
+  k_march_ens<MIX><<<need < blocks ? need : blocks, 128, 0, st>>>(tab, tiles, ntiles, next, S);
   return SWM_GPU_OK;
 }
 
-template <int MIX>
-static int ens_launch_mix(int s, const P32 *tab, const int2 *tiles, int ntiles, int *next, cudaStream_t st) {
-  if (s == 8) return ens_launch_s<MIX, 8>(tab, tiles, ntiles, next, st);
-  if (s == 32) return ens_launch_s<MIX, 32>(tab, tiles, ntiles, next, st);
-  return ens_launch_s<MIX, 16>(tab, tiles, ntiles, next, st);
-}
-
 int march_ens_launch(int mix, int s, const P32 *tab, const int2 *tiles, int ntiles, int *next, cudaStream_t st) {
-  if (mix == 2) return ens_launch_mix<2>(s, tab, tiles, ntiles, next, st);
-  if (mix == 1) return ens_launch_mix<1>(s, tab, tiles, ntiles, next, st);
-  return ens_launch_mix<0>(s, tab, tiles, ntiles, next, st);
+  if (mix == 2) return ens_launch_m<2>(tab, tiles, ntiles, next, s, st);
+  if (mix == 1) return ens_launch_m<1>(tab, tiles, ntiles, next, s, st);
+  return ens_launch_m<0>(tab, tiles, ntiles, next, s, st);
 }
 
 }  // namespace swm

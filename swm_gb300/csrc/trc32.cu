@@ -72,20 +72,21 @@ __device__ __forceinline__ void comp_update(float hi, float lo, float inc, float
 }
 
 constexpr unsigned FULLM = 0xffffffffu;
-constexpr int TRC_ROWS = 16;  // output rows per warp
+constexpr int TRC_ROWS = 16;  // output rows per warp (before fitting the grid to whole waves)
 
 // One warp owns a strip of 32 columns (lane = column; 2 halo lanes per side,
 // as the upwind-biased faces reach two cells) and TRC_ROWS output rows; it
 // walks up the strip keeping the last five rows of CH (hi + lo), thickness
 // and masks in registers, and updates row J-2 once row J is in.
 template <int NT, int FLUX>
-__global__ void __launch_bounds__(128) k_trc32(TrcP p) {
+__global__ void __launch_bounds__(128, NT <= 2 ? 4 : 3) k_trc32(TrcP p, int S, int nstrips) {
   constexpr int H = 2, TI = 32 - 2 * H;
-  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  const int lane = threadIdx.x & 31;
+  // block b: strip b % nstrips, its four warps four consecutive row groups
   const int nx = p.nx, ny = p.ny;
-  const int ry0 = (blockIdx.y * 4 + warp) * TRC_ROWS;
+  const int ry0 = ((blockIdx.x / nstrips) * 4 + (threadIdx.x >> 5)) * S;
   if (ry0 >= ny) return;  // whole warp leaves together
-  const int gx = blockIdx.x * TI - H + lane;
+  const int gx = (blockIdx.x % nstrips) * TI - H + lane;
   const int gi = wr(gx, nx);
   const bool store_lane = lane >= H && lane < 32 - H && gx < nx;
 
@@ -96,7 +97,7 @@ __global__ void __launch_bounds__(128) k_trc32(TrcP p) {
   const float *rr[3] = {};
 
   int J = ry0 - 2;
-  const int ylast = min(ry0 + TRC_ROWS, ny);  // one past the last output row
+  const int ylast = min(ry0 + S, ny);  // one past the last output row
   const int jend = ylast + 2;
   // row loads run two rows ahead of the window; the update inputs (increments
   // 1-2, C0) one output row ahead
@@ -233,11 +234,36 @@ __global__ void __launch_bounds__(128) k_trc32(TrcP p) {
   }
 }
 
+// rows per warp: TRC_ROWS, lengthened so the grid ends on a whole wave of
+// resident warps (a grid just over a whole number of waves costs one more)
+template <int NT, int FLUX>
+static int trc_rows(int nstrips, int ny) {
+  static int resident = 0;
+  if (!resident) {
+    int per_sm = 0, sms = 0, dev = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_trc32<NT, FLUX>, 128, 0);
+    resident = sms * (per_sm > 0 ? per_sm : 1);  // blocks
+  }
+  const long blocks = (long)nstrips * ((ny + 4 * TRC_ROWS - 1) / (4 * TRC_ROWS));
+  const long waves = (blocks + resident - 1) / resident;
+  const long per_strip = waves * resident / nstrips;
+  return per_strip > 0 ? (int)((ny + 4 * per_strip - 1) / (4 * per_strip)) : TRC_ROWS;
+}
+
+template <int NT, int FLUX>
+static void trc_launch_f(const TrcP &p, cudaStream_t st) {
+  const int nstrips = (p.nx + 27) / 28;
+  const int S = trc_rows<NT, FLUX>(nstrips, p.ny);
+  const unsigned blocks = (unsigned)((long)nstrips * ((p.ny + 4 * S - 1) / (4 * S)));
+  k_trc32<NT, FLUX><<<blocks, 128, 0, st>>>(p, S, nstrips);
+}
+
 template <int NT>
 static void trc_launch_nt(const TrcP &p, cudaStream_t st) {
-  dim3 grid((p.nx + 27) / 28, (p.ny + 4 * TRC_ROWS - 1) / (4 * TRC_ROWS));
-  if (p.flux == 1) k_trc32<NT, 1><<<grid, 128, 0, st>>>(p);
-  else k_trc32<NT, 0><<<grid, 128, 0, st>>>(p);
+  if (p.flux == 1) trc_launch_f<NT, 1>(p, st);
+  else trc_launch_f<NT, 0>(p, st);
 }
 
 static void trc_launch(const TrcP &p, cudaStream_t st) {
