@@ -87,6 +87,7 @@ enum {
   SWM_F_U_BS, SWM_F_V_BS, SWM_F_ZETA_BS,
   SWM_F_LATMIX_U, SWM_F_LATMIX_V,
   SWM_F_GU, SWM_F_GV, SWM_F_GETA,  /* newest increment G(:,:,NG0) */
+  SWM_F_PSI,          /* computeStreamfunction (calc_lib.f90:727-780), formed on the device */
   SWM_F_NFIELDS
 };
 
@@ -157,8 +158,16 @@ int swm_gpu_set_field(swm_gpu_ctx *ctx, int field, const double *host_in);
 /* 1-D metric: which = 0 lat, 1 cos, 2 tan, 3 f; grid = 0 H, 1 u, 2 v, 3 eta */
 int swm_gpu_get_metric(swm_gpu_ctx *ctx, int which, int grid, double *host_out);
 int swm_gpu_get_mask(swm_gpu_ctx *ctx, int grid, int8_t *host_out);
-/* computeStreamfunction (calc_lib.f90:727-780) of the current u, v */
+/* computeStreamfunction (calc_lib.f90:727-780) of the current u, v, formed
+   on the device in the reference's summation order */
 int swm_gpu_streamfunction(swm_gpu_ctx *ctx, double *psi_out);
+/* Time averaging of diagTask (diagTask.f90:266-338) on the device: add
+   weight * field (square = 1: field^2) to the FP64 buffer of slot and weight
+   to its count; swm_gpu_diag_mean returns buffer / count (and the count),
+   then clears the slot.  One device field read per call, no host copy until
+   the mean. */
+int swm_gpu_diag_accumulate(swm_gpu_ctx *ctx, int slot, int field, int square, double weight);
+int swm_gpu_diag_mean(swm_gpu_ctx *ctx, int slot, double *host_out, double *count_out);
 /* Domain integrals of the current state, summed in FP64 on the device over
    ocean points with the cell area A^2 cos(lat) dLambda dTheta:
    out[0] = volume anomaly sum(eta * area), out[1] = sum(0.5 G eta^2 area),

@@ -24,7 +24,7 @@ class Config(C.Structure):
 FIELDS = ['u', 'v', 'eta', 'D', 'Dh', 'Du', 'Dv', 'edens', 'pot', 'zeta', 'mu', 'mv', 'H', 'H_u', 'H_v',
           'H_eta', 'impl_u', 'impl_v', 'impl_eta', 'gamma_lin_u', 'gamma_lin_v', 'gamma_lin_eta',
           'gamma_sq_u', 'gamma_sq_v', 'F_x', 'F_y', 'F_eta', 'u_bs', 'v_bs', 'zeta_bs', 'latmix_u',
-          'latmix_v', 'G_u', 'G_v', 'G_eta']
+          'latmix_v', 'G_u', 'G_v', 'G_eta', 'psi']
 FIELD_ID = {n: i for i, n in enumerate(FIELDS)}
 PATHS = {'plain_fp64': 0, 'fused_fp64': 1, 'fused_fp32c': 2}
 
@@ -51,6 +51,8 @@ def _sigs():
         'swm_gpu_get_field': (I, [P, I, P]), 'swm_gpu_set_field': (I, [P, I, P]),
         'swm_gpu_get_metric': (I, [P, I, I, P]), 'swm_gpu_get_mask': (I, [P, I, P]),
         'swm_gpu_streamfunction': (I, [P, P]),
+        'swm_gpu_diag_accumulate': (I, [P, I, I, I, D]),
+        'swm_gpu_diag_mean': (I, [P, I, P, C.POINTER(C.c_double)]),
         'trc_gpu_add': (I, [P, D, D, D, P, P, P, P, C.POINTER(C.c_int)]), 'trc_gpu_init': (I, [P]),
         'trc_gpu_get_field': (I, [P, I, I, P]),
         'swm_gpu_ensemble_create': (I, [P, I, PP]), 'swm_gpu_ensemble_destroy': (I, [P]),

@@ -15,7 +15,7 @@ LIB = os.path.join(HERE, 'libswm_gb300.so')
 ARCH = ['-gencode', 'arch=compute_103a,code=sm_103a']
 UNITS = {
     'api.cu': [], 'setup.cu': [], 'plain.cu': ['-fmad=false'], 'tracer.cu': ['-fmad=false'],
-    'sor.cu': ['-fmad=false'], 'fused.cu': [], 'march.cu': [], 'ensemble.cu': [], 'trc32.cu': [], 'helm.cu': ['-fmad=false'],
+    'sor.cu': ['-fmad=false'], 'fused.cu': [], 'march.cu': [], 'ensemble.cu': [], 'trc32.cu': [], 'helm.cu': ['-fmad=false'], 'diag.cu': ['-fmad=false'],
 }
 
 

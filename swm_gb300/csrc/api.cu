@@ -163,6 +163,7 @@ int swm_gpu_destroy(swm_gpu_ctx *c) {
   sor_free(c);
   integrals_free(c);
   trc32_free(c);
+  diag_free(c);
   auto F = [](void *p) { if (p) cudaFree(p); };
   for (int q = 0; q < 4; q++) {
     F(c->d_ocean[q]); F(c->d_cos[q]); F(c->d_tan[q]); F(c->d_f[q]); F(c->d_lat[q]); F(c->d_H[q]);
@@ -509,16 +510,48 @@ static const double *field_ptr(swm_gpu_ctx *c, int f, double **wptr) {
   return p;
 }
 
-int swm_gpu_get_field(swm_gpu_ctx *c, int f, double *out) {
-  SWM_REQUIRE(c && c->stage >= 1 && out, "swm_gpu_get_field: bad arguments");
+// device copy of a field as of the current state (fused paths: the FP64
+// state and the diagnostics are formed from the FP32 pair state first)
+static int field_device(swm_gpu_ctx *c, int f, const double **out) {
   if (c->cfg.path != SWM_PATH_PLAIN_FP64 && c->stage >= 5 && c->fused) {
     TRY(fused_sync_state(c));
     if (f >= SWM_F_D && f <= SWM_F_MV) TRY(plain_diagnostics(c, 1));
     if (f >= SWM_F_FX && f <= SWM_F_FETA) TRY(plain_forcing_update(c, 1, 0));
   }
+  if (f == SWM_F_PSI) {
+    SWM_REQUIRE(c->stage >= 5, "streamfunction: model not initialised");
+    TRY(device_streamfunction(c));
+    *out = c->psi;
+    return SWM_GPU_OK;
+  }
   const double *p = field_ptr(c, f, nullptr);
-  SWM_REQUIRE(p, "swm_gpu_get_field: unknown field or not allocated");
+  SWM_REQUIRE(p, "unknown field or not allocated");
+  *out = p;
+  return SWM_GPU_OK;
+}
+
+int swm_gpu_get_field(swm_gpu_ctx *c, int f, double *out) {
+  SWM_REQUIRE(c && c->stage >= 1 && out, "swm_gpu_get_field: bad arguments");
+  const double *p = nullptr;
+  TRY(field_device(c, f, &p));
   return d2h(c, out, p, c->n);
+}
+
+int swm_gpu_diag_accumulate(swm_gpu_ctx *c, int slot, int f, int square, double weight) {
+  SWM_REQUIRE(c && c->stage >= 5 && slot >= 0 && slot < 4096, "swm_gpu_diag_accumulate: bad arguments");
+  const double *p = nullptr;
+  TRY(field_device(c, f, &p));
+  return diag_accumulate(c, slot, p, square, weight);
+}
+
+int swm_gpu_diag_mean(swm_gpu_ctx *c, int slot, double *out, double *count) {
+  SWM_REQUIRE(c && out, "swm_gpu_diag_mean: bad arguments");
+  if (!c->psi_tmp) {  // the zonal-sum scratch doubles as the staging buffer
+    SWM_CK(cudaMalloc((void **)&c->psi, c->n * 8));
+    SWM_CK(cudaMalloc((void **)&c->psi_tmp, c->n * 8));
+  }
+  TRY(diag_mean(c, slot, c->psi_tmp, count));
+  return d2h(c, out, c->psi_tmp, c->n);
 }
 
 int swm_gpu_set_field(swm_gpu_ctx *c, int f, const double *in) {
@@ -549,13 +582,7 @@ int swm_gpu_get_mask(swm_gpu_ctx *c, int grid, int8_t *out) {
 
 int swm_gpu_streamfunction(swm_gpu_ctx *c, double *psi) {
   SWM_REQUIRE(c && c->stage >= 5 && psi, "swm_gpu_streamfunction: bad arguments");
-  std::vector<double> u(c->n), v(c->n), hu(c->n), hv(c->n);
-  TRY(swm_gpu_get_field(c, SWM_F_U, u.data()));
-  TRY(swm_gpu_get_field(c, SWM_F_V, v.data()));
-  TRY(d2h(c, hu.data(), c->d_H[GU], c->n));
-  TRY(d2h(c, hv.data(), c->d_H[GV], c->n));
-  host_streamfunction(c, u.data(), v.data(), hu.data(), hv.data(), psi);
-  return SWM_GPU_OK;
+  return swm_gpu_get_field(c, SWM_F_PSI, psi);
 }
 
 }  // extern "C"

@@ -55,6 +55,11 @@ struct Stream {
   double *d1 = nullptr, *d2 = nullptr;  // device records
 };
 
+struct DiagAcc {  // one time-averaging buffer (diagTask)
+  double *buf = nullptr;
+  double count = 0.;
+};
+
 struct Tracer {
   double kappa_h;
   double *CH[2] = {nullptr, nullptr};   // TRC_N0, TRC_N0p1 (rotated)
@@ -121,6 +126,8 @@ struct swm_gpu_ctx {
   SorState *sor = nullptr;
   IntegralScratch *integrals = nullptr;
   Trc32State *trc32 = nullptr;      // tracers of the FP32 compensated path
+  std::vector<swm::DiagAcc> diag;   // averaging buffers by slot
+  double *psi = nullptr, *psi_tmp = nullptr;  // streamfunction and its zonal sums
   int64_t advances = 0;             // swm_gpu_advance calls (the rotation phase is advances mod 6)
   int march_rows = 0;                // rows per warp strip of the FP32 step kernel (0: not tuned yet)
   cudaGraphExec_t graph = nullptr;  // GRAPH_STEPS captured steps (swm_gpu_run)
@@ -136,8 +143,7 @@ void host_basic_state(swm_gpu_ctx *c, const double *psi);
 void host_damping_add(swm_gpu_ctx *c, int term, int type, double value, double sl_length,
                       double sl_cutoff, int loc, const double *file_data);
 void host_damping_finish(swm_gpu_ctx *c);
-void host_streamfunction(const swm_gpu_ctx *c, const double *u, const double *v, const double *Hu,
-                         const double *Hv, double *psi);
+
 // plain.cu
 int plain_diagnostics(swm_gpu_ctx *c, int64_t itt);
 int plain_step(swm_gpu_ctx *c, int64_t itt);
@@ -156,6 +162,11 @@ void fused_free(swm_gpu_ctx *c);
 void integrals_free(swm_gpu_ctx *c);
 // sor.cu
 void sor_free(swm_gpu_ctx *c);
+// diag.cu
+int device_streamfunction(swm_gpu_ctx *c);
+int diag_accumulate(swm_gpu_ctx *c, int slot, const double *f, int square, double w);
+int diag_mean(swm_gpu_ctx *c, int slot, double *dev_out, double *count);
+void diag_free(swm_gpu_ctx *c);
 // trc32.cu
 bool trc32_active(const swm_gpu_ctx *c);
 int trc32_add(swm_gpu_ctx *c, const std::vector<double> &CH, const std::vector<double> &C0,

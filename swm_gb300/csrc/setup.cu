@@ -255,46 +255,5 @@ void host_damping_finish(swm_gpu_ctx *c) {
 
 // computeStreamfunction (calc_lib.f90:727-780) without an elliptic solver
 // configured (u_nd = u).  Row/column prefix sums in the reference's order.
-void host_streamfunction(const swm_gpu_ctx *c, const double *u, const double *v, const double *Hu,
-                         const double *Hv, double *psi) {
-  const HostGrid &g = c->hg;
-  int nx = g.nx, ny = g.ny;
-  double A = c->cfg.A, dL = g.dLambda, dT = g.dTheta;
-  int bt = c->cfg.barotropic;
-  const std::vector<int8_t> &oU = g.ocean[GU], &oV = g.ocean[GV];
-  const std::vector<double> &cV = g.cosl[GV];
-  for (size_t k = 0; k < (size_t)nx * ny; k++) psi[k] = 0.;
-  for (int i = 0; i < nx - 1; i++) {
-    double s = 0.;
-    for (int q = i; q <= nx - 2; q++) s = s + (bt ? Hv[q] * oV[q] * v[q] : oV[q] * v[q]);
-    psi[i] = (-1) * s * A * cV[0] * dL;
-  }
-  for (int j = 1; j < ny; j++) {
-    double s = 0.;
-    for (int q = 0; q <= j - 1; q++) {
-      size_t k = (nx - 1) + (size_t)nx * q;
-      s = s + (bt ? Hu[k] * oU[k] * u[k] : oU[k] * u[k]);
-    }
-    psi[(nx - 1) + (size_t)nx * j] = (-1) * s * A * dT;
-  }
-  // the interior sums are suffix sums along rows and prefix sums along
-  // columns; accumulate them in the same order as the reference's SUM
-  std::vector<double> s2(nx, 0.);
-  for (int j = 1; j < ny; j++) {
-    for (int i = 0; i < nx - 1; i++) {
-      size_t kq = i + (size_t)nx * (j - 1);
-      s2[i] = s2[i] + (bt ? Hu[kq] * u[kq] : u[kq]);
-    }
-    for (int i = 0; i < nx - 1; i++) {
-      double s1 = 0.;
-      for (int q = i; q <= nx - 2; q++) {
-        size_t k = q + (size_t)nx * j;
-        s1 = s1 + (bt ? Hv[k] * v[k] : v[k]);
-      }
-      psi[i + (size_t)nx * j] = ((-1) * s1 * A * cV[j] * dL + psi[(nx - 1) + (size_t)nx * j] -
-                                 s2[i] * A * dT + psi[i]) / 2.;
-    }
-  }
-}
 
 }  // namespace swm

@@ -51,7 +51,28 @@ class DiagTask:
         self.buffer = self.buffer + dT * d
         self.count = self.count + dT
 
-    def process(self, itt, fetch):
+    def process(self, itt, fetch, device=None, slot=None):
+        """device: a backend with diag_accumulate/diag_mean (the averaging
+        buffer then lives on the GPU and one field crosses per period)."""
+        if device is not None and self.type == 'A':
+            return self._process_device(itt, device, slot)
+        return self._process_host(itt, fetch)
+
+    def _process_device(self, itt, dev, slot):
+        k = itt - self.dsi
+        if math.fmod(k, self.nstep) != 0:
+            return
+        per = self.period if self.period != 2.628e6 else self.meant_out
+        dT = min(math.fmod(self.dt * k, per), self.dt)
+        field = DIAG_VARS[self.name][0]
+        if dT < self.dt and k != 0:
+            dev.diag_accumulate(slot, field, self.square, self.dt - dT)
+            mean, _ = dev.diag_mean(slot)
+            self.times.append(self.dt * itt - dT)
+            self.records.append(mean)
+        dev.diag_accumulate(slot, field, self.square, dT)
+
+    def _process_host(self, itt, fetch):
         k = itt - self.dsi
         if math.fmod(k, self.nstep) != 0:
             return
@@ -77,8 +98,9 @@ class DiagTask:
 
 
 class Driver:
-    def __init__(self, case, backend):
+    def __init__(self, case, backend, device_averages=True):
         self.case, self.b = case, backend
+        self.device_averages = device_averages
         self.cfg = case['config']
         self.itt = 0
         self.tasks = []
@@ -132,8 +154,9 @@ class Driver:
         if self.itt < self.cfg['diag_start_ind']:
             return
         self._psi_cache = None
-        for t in self.tasks:
-            t.process(self.itt, self.fetch)
+        dev = self.b if self.device_averages and hasattr(self.b, 'diag_accumulate') else None
+        for slot, t in enumerate(self.tasks):
+            t.process(self.itt, self.fetch, dev, slot)
 
     # -- time loop: model.f90 timestepModel :153-197 ---------------------
     def run(self, nsteps=None, with_diag=True):

@@ -153,6 +153,17 @@ class GpuModel:
         check(self.L.swm_gpu_get_mask(self.ctx, ['H', 'u', 'v', 'eta'].index(grid), _p(out)))
         return out
 
+    def diag_accumulate(self, slot, name, square, weight):
+        """Device time-averaging buffer (swm_gpu_diag_accumulate)."""
+        fid = FIELD_ID[self._ALIAS.get(name, name)]
+        check(self.L.swm_gpu_diag_accumulate(self.ctx, slot, fid, int(bool(square)), float(weight)))
+
+    def diag_mean(self, slot):
+        out = np.empty((self.ny, self.nx))
+        cnt = C.c_double()
+        check(self.L.swm_gpu_diag_mean(self.ctx, slot, _p(out), C.byref(cnt)))
+        return out, cnt.value
+
     def streamfunction(self):
         out = np.empty((self.ny, self.nx))
         check(self.L.swm_gpu_streamfunction(self.ctx, _p(out)))

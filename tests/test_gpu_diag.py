@@ -1,0 +1,64 @@
+"""Diagnostics formed on the device: the streamfunction (computeStreamfunction,
+summed in the reference's order) bit for bit against the FP64 oracle, and the
+device averaging buffers against the host averaging of the same snapshots."""
+import numpy as np
+import pytest
+
+from harness import golden_case, run_case
+from oracle import OracleBackend
+from swm_gb300.host import synthetic
+from swm_gb300.host.driver import Driver
+from swm_gb300.model import GpuModel
+
+pytestmark = pytest.mark.gpu
+
+
+@pytest.mark.parametrize('barotropic', [0, 1])
+@pytest.mark.parametrize('path', ['plain_fp64', 'fused_fp32c'])
+def test_streamfunction_bit_exact(barotropic, path):
+    case = synthetic.double_gyre((48, 40), biharmonic=False, nsteps=100)
+    case['config'].update(barotropic=barotropic)
+    o, g = OracleBackend(), GpuModel(path)
+    run_case(case, o, nsteps=100, with_diag=False)
+    run_case(case, g, nsteps=100, with_diag=False)
+    # the oracle's streamfunction of the GPU's own state: the same sums
+    psi_g = g.streamfunction()
+    psi_o = o.streamfunction(g.field('u'), g.field('v'))
+    assert np.array_equal(psi_g, psi_o)
+    assert np.abs(psi_g).max() > 0
+
+
+def test_device_averages_equal_host_averages():
+    case, _ = golden_case('test_fixed_length_output')
+    outs = []
+    for dev in (True, False):
+        g = GpuModel('plain_fp64')
+        d = Driver(case, g, device_averages=dev)
+        d.init(with_diag=True)
+        d.run(with_diag=True)
+        outs.append(d.outputs())
+    assert outs[0].keys() == outs[1].keys()
+    n = 0
+    for fn in outs[0]:
+        ta, ra, _ = outs[0][fn]
+        tb, rb, _ = outs[1][fn]
+        assert np.array_equal(ta, tb), fn
+        assert np.array_equal(ra, rb), fn
+        n += len(ra)
+    assert n > 0
+
+
+def test_psi_average_on_device():
+    case = synthetic.double_gyre((40, 32), biharmonic=False, nsteps=40)
+    g = GpuModel('fused_fp32c')
+    d = Driver(case, g)
+    d.init(with_diag=False)
+    acc = np.zeros((case['config']['ny'], case['config']['nx']))
+    for s in range(1, 11):
+        d.run(1, with_diag=False)
+        g.diag_accumulate(3, 'psi', True, 2.0)
+        p = g.streamfunction()
+        acc = acc + 2.0 * (p * p)
+    mean, cnt = g.diag_mean(3)
+    assert cnt == 20.0
+    assert np.array_equal(mean, acc / 20.0)
