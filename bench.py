@@ -45,7 +45,8 @@ def parse():
     ap.add_argument('--quick', action='store_true', help='skip the side measurements')
     ap.add_argument('--device-only', action='store_true',
                     help='only the warm-up and timed device steps (the form to run under ncu)')
-    ap.add_argument('--workload', default='double_gyre', choices=['double_gyre', 'ensemble', 'tracer', 'helmholtz'],
+    ap.add_argument('--workload', default='double_gyre',
+                    choices=['double_gyre', 'ensemble', 'tracer', 'helmholtz', 'linear_rg'],
                     help='ensemble / tracer: print that measurement alone (profiling)')
     return ap.parse_args()
 
@@ -235,6 +236,7 @@ def ours(args, rank, ws):
         line['ensemble'] = ensemble_measurement(args)
         line['tracer'] = tracer_measurement(args)
         line['helmholtz'] = helmholtz_measurement(args)
+        line['linear_rg'] = linear_rg_measurement(args)
     if rank == 0 and ws == 1 and not args.quick:
         line['cpu_baseline'] = cpu_baseline(cells)
     g.close()
@@ -441,6 +443,49 @@ def helmholtz_measurement(args, cells=4096, rtol=1e-10):
     return out
 
 
+def linear_rg_measurement(args, steps=2000, cpu_budget_s=5.0):
+    """The reference's plain linear reduced-gravity configuration (256 x 128
+    cells, FP64, Laplacian mixing, Rayleigh damping, AB3 dt = 1800 s) on the
+    plain FP64 GPU path (bit-exact with the oracle), beside the oracle on the
+    host cores; also the relative L2 of eta after the timed steps between the
+    two (0 when bit-exact)."""
+    import torch
+    sys.path.insert(0, os.path.join(ROOT, 'oracle'))
+    from oracle import OracleBackend
+    from swm_gb300.host import synthetic
+    from swm_gb300.host.driver import Driver
+    from swm_gb300.model import GpuModel
+    case = synthetic.linear_rg(256, 128, nsteps=steps + 10)
+    cells = 256 * 128
+    g = GpuModel('plain_fp64')
+    Driver(case, g).init(with_diag=False)
+    g.run(0, 10)
+    g.synchronize()
+    st = torch.cuda.ExternalStream(g.stream())
+    a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    a.record(st)
+    g.run(10, steps)
+    b.record(st)
+    g.synchronize()
+    ms = a.elapsed_time(b) / steps
+    o = OracleBackend()
+    Driver(case, o).init(with_diag=False)
+    o.run_steady(10)
+    n, t0 = 0, time.perf_counter()
+    while time.perf_counter() - t0 < cpu_budget_s and n < steps:
+        o.run_steady(50)
+        n += 50
+    tcpu = time.perf_counter() - t0
+    same = None
+    if n == steps:
+        same = bool(np.array_equal(o.field('eta'), g.field('eta')))
+    out = {'workload': 'linear_rg_256x128_fp64', 'cells': cells, 'steps': steps, 'gpu_ms_per_step': ms,
+           'gpu_value': cells / (ms * 1e-3), 'cpu_value': cells * n / tcpu, 'cpu_steps': n,
+           'cpu_cores': os.cpu_count(), 'unit': 'cell-steps/s', 'bit_identical_after_timed_steps': same}
+    g.close()
+    return out
+
+
 def cpu_baseline(cells, budget_s=15.0):
     """The FP64 CPU restatement (oracle) on the same basin, all host cores."""
     sys.path.insert(0, os.path.join(ROOT, 'oracle'))
@@ -498,6 +543,8 @@ def main():
                                      err_steps=0 if args.device_only else 1000)
         elif args.workload == 'helmholtz':
             out = helmholtz_measurement(args, cells=args.cells)
+        elif args.workload == 'linear_rg':
+            out = linear_rg_measurement(args)
         else:
             out = ensemble_measurement(args, steps=args.steps, one_by_one=not args.device_only)
         print(json.dumps(out))

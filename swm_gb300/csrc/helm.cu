@@ -16,6 +16,8 @@
 // the relaxation factor in a given range from short trial solves and the
 // thread-block shape of the sweep kernel from timings.
 #include <cmath>
+#include <algorithm>
+#include <cstdlib>
 #include <cstring>
 #include <string>
 #include <vector>
@@ -25,6 +27,19 @@ namespace swm {
 
 constexpr int HELM_CHECK = 16;  // sweeps between residual checks
 constexpr int HELM_RED = 1024;  // reduction blocks
+
+// One FP32 SOR point update, shared by the global and the tiled kernels so
+// both round alike: explicit fused multiply-adds, the diagonal applied as its
+// reciprocal (formed once per cell)
+__device__ __forceinline__ float sor32_update(float p, float r, float cxw, float cxe, float cys, float cyn, float rcc,
+                                              float w, float e, float s, float n, float omega) {
+  const float off = fmaf(cyn, n, fmaf(cys, s, fmaf(cxe, e, cxw * w)));
+  const float gs = (r - off) * rcc;
+  return fmaf(omega, gs - p, p);
+}
+
+__device__ __forceinline__ float face32(float a, float b, float rd2) { return (0.5f * (a + b)) * rd2; }
+
 
 // FP64 coefficients formed once: west and south face coefficients and the
 // reciprocal of the diagonal (the sweeps would otherwise be bound by the
@@ -60,25 +75,115 @@ __global__ void k_h_sweep64(int nx, int ny, const double *__restrict__ cx, const
   psi[k] = psi[k] + omega * (gs - psi[k]);
 }
 
-template <typename T>
-__global__ void k_h_sweep(int nx, int ny, const T *__restrict__ h, const int8_t *__restrict__ mask,
-                          const T *__restrict__ rhs, T *psi, T rdx2, T rdy2, T lambda, T omega, int colour) {
+// one colour of an FP32 sweep over the whole grid (the arithmetic of k_h_tb32)
+__global__ void k_h_sweep32(int nx, int ny, const float *__restrict__ h, const int8_t *__restrict__ mask,
+                            const float *__restrict__ rhs, float *psi, float rdx2, float rdy2, float lambda,
+                            float omega, int colour) {
   const int j = blockIdx.y * blockDim.y + threadIdx.y;
   const int i = 2 * (blockIdx.x * blockDim.x + threadIdx.x) + ((j + colour) & 1);
   if (i >= nx || j >= ny) return;
   const size_t k = (size_t)i + (size_t)nx * j;
   if (!mask[k]) return;
-  const T hk = h[k];
-  const T cxw = i > 0 ? (T(0.5) * (hk + h[k - 1])) * rdx2 : T(0);
-  const T cxe = i < nx - 1 ? (T(0.5) * (h[k + 1] + hk)) * rdx2 : T(0);
-  const T cys = j > 0 ? (T(0.5) * (hk + h[k - nx])) * rdy2 : T(0);
-  const T cyn = j < ny - 1 ? (T(0.5) * (h[k + nx] + hk)) * rdy2 : T(0);
-  const T cc = -(((cxw + cxe) + cys) + cyn) - lambda;
-  const T w = i > 0 ? psi[k - 1] : T(0), e = i < nx - 1 ? psi[k + 1] : T(0);
-  const T s = j > 0 ? psi[k - nx] : T(0), n = j < ny - 1 ? psi[k + nx] : T(0);
-  const T off = cxw * w + cxe * e + cys * s + cyn * n;
-  const T gs = (rhs[k] - off) / cc;
-  psi[k] = psi[k] + omega * (gs - psi[k]);
+  const float hk = h[k];
+  const float cxw = i > 0 ? face32(hk, h[k - 1], rdx2) : 0.f;
+  const float cxe = i < nx - 1 ? face32(h[k + 1], hk, rdx2) : 0.f;
+  const float cys = j > 0 ? face32(hk, h[k - nx], rdy2) : 0.f;
+  const float cyn = j < ny - 1 ? face32(h[k + nx], hk, rdy2) : 0.f;
+  // the tiled kernel forms the next cell's west face as face32(h[k+1], h[k]),
+  // this kernel forms this cell's east face the same way: same operand order
+  const float rcc = 1.f / (-(((cxw + cxe) + cys) + cyn) - lambda);
+  const float w = i > 0 ? psi[k - 1] : 0.f, e = i < nx - 1 ? psi[k + 1] : 0.f;
+  const float s = j > 0 ? psi[k - nx] : 0.f, n = j < ny - 1 ? psi[k + nx] : 0.f;
+  psi[k] = sor32_update(psi[k], rhs[k], cxw, cxe, cys, cyn, rcc, w, e, s, n, omega);
+}
+
+// K red-black sweeps of FP32 SOR on one TX x TY tile in shared memory.  The
+// tile is loaded with a halo of 2K cells (each colour pass needs the
+// previous pass's neighbours, so the valid region shrinks by one cell per
+// pass); halo cells are updated too, with the same arithmetic as their owning
+// tile, so after 2K passes the interior equals K global sweeps bit for bit.
+// Coefficients are formed from 1/H in shared memory at each update (13 bytes
+// of shared memory per cell keep five blocks resident per SM; a variant that
+// stored the coefficients ran slower at two blocks per SM).  Reads pin,
+// writes the interior to pout (ping-pong: other tiles still read pin's halo
+// cells).  Cells outside the grid hold psi = 0, mask = 0.
+template <int TX, int TY, int K>
+__global__ void __launch_bounds__(256) k_h_tb32(int nx, int ny, const float *__restrict__ hin,
+                                                const int8_t *__restrict__ mask, const float *__restrict__ rhs,
+                                                const float *__restrict__ pin, float *__restrict__ pout, float rdx2,
+                                                float rdy2, float lambda, float omega) {
+  constexpr int W = 2 * K, RX = TX + 2 * W, RY = TY + 2 * W, PX = RX + 1;
+  __shared__ float sp[RY * PX], sh[RY * PX], sr[RY * PX];
+  __shared__ int8_t sm[RY * PX];
+  const int x0 = blockIdx.x * TX - W, y0 = blockIdx.y * TY - W;
+  const int tid = threadIdx.y * blockDim.x + threadIdx.x, nt = blockDim.x * blockDim.y;
+  for (int q = tid; q < RX * RY; q += nt) {
+    const int ly = q / RX, lx = q - ly * RX, gx = x0 + lx, gy = y0 + ly;
+    const bool in = gx >= 0 && gx < nx && gy >= 0 && gy < ny;
+    const size_t g = in ? (size_t)gx + (size_t)nx * gy : 0;
+    const int l = ly * PX + lx;
+    sp[l] = in ? pin[g] : 0.f;
+    sh[l] = in ? hin[g] : 1.f;
+    sr[l] = in ? rhs[g] : 0.f;
+    sm[l] = in ? mask[g] : (int8_t)0;
+  }
+  __syncthreads();
+  for (int pass = 0; pass < 2 * K; pass++) {
+    const int c = pass & 1, lo = pass + 1, hx = RX - pass - 1, hy = RY - pass - 1;
+    for (int ly = lo + threadIdx.y; ly < hy; ly += blockDim.y) {
+      const int gy = y0 + ly;
+      const int lxs = lo + ((c - x0 - gy - lo) & 1);  // first column with (gx + gy) & 1 == c
+      for (int lx = lxs + 2 * threadIdx.x; lx < hx; lx += 2 * blockDim.x) {
+        const int l = ly * PX + lx;
+        if (!sm[l]) continue;
+        const int gx = x0 + lx;
+        const float hk = sh[l];
+        const float cxw = gx > 0 ? face32(hk, sh[l - 1], rdx2) : 0.f;
+        const float cxe = gx < nx - 1 ? face32(sh[l + 1], hk, rdx2) : 0.f;
+        const float cys = gy > 0 ? face32(hk, sh[l - PX], rdy2) : 0.f;
+        const float cyn = gy < ny - 1 ? face32(sh[l + PX], hk, rdy2) : 0.f;
+        const float rcc = 1.f / (-(((cxw + cxe) + cys) + cyn) - lambda);
+        sp[l] = sor32_update(sp[l], sr[l], cxw, cxe, cys, cyn, rcc, sp[l - 1], sp[l + 1], sp[l - PX], sp[l + PX],
+                             omega);
+      }
+    }
+    __syncthreads();
+  }
+  for (int q = tid; q < TX * TY; q += nt) {
+    const int ly = q / TX, lx = q - ly * TX, gx = x0 + W + lx, gy = y0 + W + ly;
+    if (gx < nx && gy < ny) pout[(size_t)gx + (size_t)nx * gy] = sp[(ly + W) * PX + lx + W];
+  }
+}
+
+// r = rhs - A psi on ocean cells (0 elsewhere) from the FP64 face
+// coefficients, for an FP64 or FP32 iterate; per-block partial sums of r^2
+template <typename T>
+__global__ void k_h_resid_c(int nx, int ny, const double *__restrict__ cx, const double *__restrict__ cy,
+                            double lambda, const int8_t *__restrict__ mask, const T *__restrict__ rhs,
+                            const T *__restrict__ psi, double *r, double *partial) {
+  __shared__ double red[256];
+  double acc = 0.;
+  const size_t n = (size_t)nx * ny;
+  for (size_t k = (size_t)blockIdx.x * blockDim.x + threadIdx.x; k < n; k += (size_t)gridDim.x * blockDim.x) {
+    const int i = (int)(k % nx), j = (int)(k / nx);
+    double rr = 0.;
+    if (mask[k]) {
+      const double cxw = cx[k], cxe = i < nx - 1 ? cx[k + 1] : 0., cys = cy[k], cyn = j < ny - 1 ? cy[k + nx] : 0.;
+      const double cc = -(((cxw + cxe) + cys) + cyn) - lambda;
+      const double w = i > 0 ? (double)psi[k - 1] : 0., e = i < nx - 1 ? (double)psi[k + 1] : 0.;
+      const double s = j > 0 ? (double)psi[k - nx] : 0., nn = j < ny - 1 ? (double)psi[k + nx] : 0.;
+      rr = (double)rhs[k] - (cxw * w + cxe * e + cys * s + cyn * nn + cc * (double)psi[k]);
+    }
+    if (r) r[k] = rr;
+    acc += rr * rr;
+  }
+  red[threadIdx.x] = acc;
+  __syncthreads();
+  for (int w = blockDim.x / 2; w > 0; w >>= 1) {
+    if (threadIdx.x < w) red[threadIdx.x] += red[threadIdx.x + w];
+    __syncthreads();
+  }
+  if (threadIdx.x == 0) partial[blockIdx.x] = red[0];
 }
 
 // r = rhs - A psi on ocean cells (0 elsewhere); per-block partial sums of r^2
@@ -168,7 +273,8 @@ struct swm_helm {
   cudaStream_t stream = nullptr;
   double *hinv = nullptr, *psi = nullptr, *rhs = nullptr, *r = nullptr, *partial = nullptr, *out = nullptr;
   double *host = nullptr;  // pinned, 1 double
-  float *hinv32 = nullptr, *e32 = nullptr, *r32 = nullptr;
+  float *hinv32 = nullptr, *e32 = nullptr, *r32 = nullptr, *e32b = nullptr;  // e32b: ping-pong of e32
+  int tbk = 4;  // sweeps per temporally blocked FP32 launch
   int8_t *mask = nullptr;
   dim3 blk = dim3(64, 4);
   int64_t launches = 0;
@@ -194,21 +300,48 @@ void sweep64(swm_helm *h, double omega, dim3 b) {
   h->launches += 2;
 }
 
-template <typename T>
-void sweep(swm_helm *h, const T *hh, const T *rhs, T *psi, T omega, dim3 b) {
+void sweep32(swm_helm *h, float omega, dim3 b) {
   const dim3 g = sweep_grid(h, b);
-  const T rdx2 = T(1. / (h->dx * h->dx)), rdy2 = T(1. / (h->dy * h->dy)), lam = T(h->lambda);
+  const float rdx2 = (float)(1. / (h->dx * h->dx)), rdy2 = (float)(1. / (h->dy * h->dy)), lam = (float)h->lambda;
   for (int colour = 0; colour < 2; colour++)
-    k_h_sweep<T><<<g, b, 0, h->stream>>>(h->nx, h->ny, hh, h->mask, rhs, psi, rdx2, rdy2, lam, omega, colour);
+    k_h_sweep32<<<g, b, 0, h->stream>>>(h->nx, h->ny, h->hinv32, h->mask, h->r32, h->e32, rdx2, rdy2, lam, omega,
+                                        colour);
   h->launches += 2;
+}
+
+// tile of the temporally blocked kernel: 64 columns, rows so that the
+// shared arrays (13 bytes per cell with the 2K halo) stay within 48 KB
+constexpr int TB_X = 64;
+template <int K>
+constexpr int tb_rows() { return K == 4 ? 24 : 32; }
+
+template <int K>
+void launch_tb32(swm_helm *h, float omega) {
+  constexpr int TY = tb_rows<K>();
+  const dim3 g((h->nx + TB_X - 1) / TB_X, (h->ny + TY - 1) / TY), b(32, 8);
+  const float rdx2 = (float)(1. / (h->dx * h->dx)), rdy2 = (float)(1. / (h->dy * h->dy)), lam = (float)h->lambda;
+  k_h_tb32<TB_X, TY, K><<<g, b, 0, h->stream>>>(h->nx, h->ny, h->hinv32, h->mask, h->r32, h->e32, h->e32b, rdx2,
+                                                rdy2, lam, omega);
+}
+
+// n FP32 sweeps (a multiple of h->tbk) on A e = r32, ping-ponging e32/e32b;
+// the result ends in h->e32
+void sweeps_tb32(swm_helm *h, float omega, int n) {
+  for (int s = 0; s < n; s += h->tbk) {
+    if (h->tbk == 4) launch_tb32<4>(h, omega);
+    else if (h->tbk == 2) launch_tb32<2>(h, omega);
+    else launch_tb32<1>(h, omega);
+    std::swap(h->e32, h->e32b);
+    h->launches++;
+  }
 }
 
 // ||rhs - A psi||^2 (FP64 accumulation); r written when wanted
 template <typename T>
 int resid2(swm_helm *h, const T *hh, const T *rhs, const T *psi, double *r, double *out) {
-  const T rdx2 = T(1. / (h->dx * h->dx)), rdy2 = T(1. / (h->dy * h->dy)), lam = T(h->lambda);
-  k_h_resid<T><<<HELM_RED, 256, 0, h->stream>>>(h->nx, h->ny, hh, h->mask, rhs, psi, rdx2, rdy2, lam, r,
-                                                h->partial);
+  (void)hh;
+  k_h_resid_c<T><<<HELM_RED, 256, 0, h->stream>>>(h->nx, h->ny, h->cx, h->cy, h->lambda, h->mask, rhs, psi, r,
+                                                  h->partial);
   k_h_final<<<1, 256, 0, h->stream>>>(h->partial, HELM_RED, h->out);
   h->launches += 2;
   SWM_CK(cudaGetLastError());
@@ -242,8 +375,11 @@ int inner32(swm_helm *h, float omega, double tol, int max_sweeps, int *sweeps, d
   int s = 0, checks = 0;
   double rr = 1., prev = 1.;
   while (s < max_sweeps) {
-    int blk = std::min(HELM_CHECK, max_sweeps - s);
-    for (int q = 0; q < blk; q++) sweep<float>(h, h->hinv32, h->r32, h->e32, omega, h->blk);
+    // 2 * HELM_CHECK sweeps between checks of the correction equation
+    int blk = std::min(2 * HELM_CHECK, max_sweeps - s);
+    const int tb = blk - blk % h->tbk;
+    sweeps_tb32(h, omega, tb);
+    for (int q = tb; q < blk; q++) sweep32(h, omega, h->blk);
     s += blk;
     double e2 = 0.;
     HTRY(resid2<float>(h, h->hinv32, h->r32, h->e32, nullptr, &e2));
@@ -261,7 +397,7 @@ void helm_free(swm_helm *h) {
   if (h->stream) cudaStreamSynchronize(h->stream);
   cudaFree(h->hinv); cudaFree(h->psi); cudaFree(h->rhs); cudaFree(h->r); cudaFree(h->partial); cudaFree(h->out);
   cudaFreeHost(h->host);
-  cudaFree(h->hinv32); cudaFree(h->e32); cudaFree(h->r32); cudaFree(h->mask);
+  cudaFree(h->hinv32); cudaFree(h->e32); cudaFree(h->r32); cudaFree(h->mask); cudaFree(h->e32b);
   cudaFree(h->cx); cudaFree(h->cy); cudaFree(h->rcc);
   if (h->stream) cudaStreamDestroy(h->stream);
   delete h;
@@ -296,6 +432,7 @@ int swm_helm_create(int nx, int ny, double dx, double dy, double lambda, const d
             cudaMalloc((void **)&h->out, 8) == cudaSuccess && cudaMallocHost((void **)&h->host, 8) == cudaSuccess &&
             cudaMalloc((void **)&h->hinv32, n * 4) == cudaSuccess && cudaMalloc((void **)&h->e32, n * 4) == cudaSuccess &&
             cudaMalloc((void **)&h->r32, n * 4) == cudaSuccess && cudaMalloc((void **)&h->mask, n) == cudaSuccess &&
+            cudaMalloc((void **)&h->e32b, n * 4) == cudaSuccess &&
             cudaMalloc((void **)&h->cx, n * 8) == cudaSuccess && cudaMalloc((void **)&h->cy, n * 8) == cudaSuccess &&
             cudaMalloc((void **)&h->rcc, n * 8) == cudaSuccess;
   if (!ok) {
@@ -421,13 +558,14 @@ int swm_helm_autotune(swm_helm *h, const double *rhs, double omega_lo, double om
   // block shape
   const dim3 shapes[4] = {dim3(32, 8), dim3(64, 4), dim3(128, 2), dim3(256, 1)};
   cudaEvent_t a, b;
+  int best_k = 4;
   SWM_CK(cudaEventCreate(&a));
   SWM_CK(cudaEventCreate(&b));
   float tbest = 1e30f;
   for (const dim3 &shp : shapes) {
-    sweep<float>(h, h->hinv32, h->r32, h->e32, 1.f, shp);
+    sweep32(h, 1.f, shp);
     SWM_CK(cudaEventRecord(a, h->stream));
-    for (int q = 0; q < 4; q++) sweep<float>(h, h->hinv32, h->r32, h->e32, 1.f, shp);
+    for (int q = 0; q < 4; q++) sweep32(h, 1.f, shp);
     SWM_CK(cudaEventRecord(b, h->stream));
     SWM_CK(cudaEventSynchronize(b));
     float ms;
@@ -436,13 +574,38 @@ int swm_helm_autotune(swm_helm *h, const double *rhs, double omega_lo, double om
   }
   cudaEventDestroy(a);
   cudaEventDestroy(b);
+  // sweeps per temporally blocked launch (SWM_GB300_HELM_K overrides)
+  const char *ek = getenv("SWM_GB300_HELM_K");
+  if (ek && (atoi(ek) == 1 || atoi(ek) == 2 || atoi(ek) == 4)) {
+    h->tbk = atoi(ek);
+  } else {
+    SWM_CK(cudaEventCreate(&a));
+    SWM_CK(cudaEventCreate(&b));
+    float kbest = 1e30f;
+    for (int kk : {1, 2, 4}) {
+      h->tbk = kk;
+      sweeps_tb32(h, 1.f, 4);
+      SWM_CK(cudaEventRecord(a, h->stream));
+      sweeps_tb32(h, 1.f, 8);
+      SWM_CK(cudaEventRecord(b, h->stream));
+      SWM_CK(cudaEventSynchronize(b));
+      float ms;
+      SWM_CK(cudaEventElapsedTime(&ms, a, b));
+      if (ms < kbest) { kbest = ms; best_k = kk; }
+    }
+    h->tbk = best_k;
+    cudaEventDestroy(a);
+    cudaEventDestroy(b);
+  }
   // relaxation factor
   double best = omega_lo, rbest = 1e300;
   for (int q = 0; q < ngrid; q++) {
     const double om = ngrid == 1 ? omega_lo : omega_lo + (omega_hi - omega_lo) * q / (ngrid - 1);
     k_h_to32<<<nb, 256, 0, h->stream>>>(h->rhs, h->r32, h->e32, h->n, bn > 0 ? 1. / bn : 1.);
     h->launches++;
-    for (int s = 0; s < trial_sweeps; s++) sweep<float>(h, h->hinv32, h->r32, h->e32, (float)om, h->blk);
+    const int tb = trial_sweeps - trial_sweeps % h->tbk;
+    sweeps_tb32(h, (float)om, tb);
+    for (int s = tb; s < trial_sweeps; s++) sweep32(h, (float)om, h->blk);
     double e2;
     HTRY(resid2<float>(h, h->hinv32, h->r32, h->e32, nullptr, &e2));
     if (e2 < rbest) { rbest = e2; best = om; }

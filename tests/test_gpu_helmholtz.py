@@ -70,3 +70,19 @@ def test_autotune_choices(case):
     for w in (1.8, om, 1.99):
         counts[w] = g.solve(case['rhs'], omega=w, rtol=1e-10, max_sweeps=20000)[1]
     assert counts[om] <= max(counts[1.8], counts[1.99])
+
+
+def test_temporal_blocking_does_not_change_results(case, monkeypatch):
+    """K sweeps per launch on shared-memory tiles with a 2K halo give the
+    same iterates as K global sweeps: the mixed solve is identical for K = 1,
+    2, 4."""
+    res = []
+    for k in ('1', '2', '4'):
+        monkeypatch.setenv('SWM_GB300_HELM_K', k)
+        g = GpuHelmholtz(case['H'], case['ocean'], case['dx'], case['dy'], case['lam'])
+        g.autotune(case['rhs'], 1.9, 1.9, 1, 16)
+        res.append(g.solve(case['rhs'], omega=1.9, rtol=1e-10, mixed=True))
+        g.close()
+    for r in res[1:]:
+        assert r[1] == res[0][1] and r[2] == res[0][2]
+        assert np.array_equal(r[0], res[0][0])
