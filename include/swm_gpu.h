@@ -224,6 +224,14 @@ int elsolv_sor_gpu_init(swm_gpu_ctx *ctx);   /* init_ElSolv_SOR (:44-66) */
    sweeps did not bring the correction norm below eps */
 int elsolv_sor_gpu_solve(swm_gpu_ctx *ctx, const double *B, double *chi, double eps, int first_guess,
                          int *iterations, double *anorm);
+/* computeNonDivergentFlowField (calc_lib.f90:548-590) of the current model
+   velocities on the device: computeDivergence (:607-622), main_ElSolv_SOR
+   for chi (kept on the device between calls, like calc_lib::chi;
+   first_guess = itt == 1; eps = EPS of calc_lib.h, 1e-4), computeGradient
+   (:638-648); u_nd = u - d chi / (A cos dLambda), v_nd = v - d chi / (A
+   dTheta).  Outputs may be NULL. */
+int swm_gpu_nondivergent(swm_gpu_ctx *ctx, int first_guess, double eps, double *u_nd, double *v_nd, double *chi,
+                         int *iterations);
 
 /* ---- variable-coefficient Helmholtz solver (extension of ElSolv_SOR) ----
    div(H^-1 grad psi) - lambda psi = rhs on an (nx, ny) grid of spacing dx,

@@ -67,6 +67,7 @@ def lib():
             'orc_helmholtz_sor': (I, [I, I, P, P, P, P, P, P, D, D, I, P]),
             'orc_helmholtz_apply': (V, [I, I, P, P, P, P, P, P]),
             'orc_helmholtz_coeffs': (V, [I, I, P, D, D, D, P, P, P]),
+            'orc_nondivergent_from_chi': (V, [P, P, P, P, P, P]),
         }
         for name, (res, args) in sig.items():
             f = getattr(L, name)
@@ -200,6 +201,16 @@ class OracleBackend:
         out = np.zeros((self.ny, self.nx))
         self.L.orc_divergence(self.m, ptr(uu), ptr(vv), ptr(out))
         return out
+
+    def nondivergent(self, u, v, chi0, first_guess, eps=1e-4):
+        """computeNonDivergentFlowField: divergence, SOR for chi from chi0,
+        gradient subtracted; returns (u_nd, v_nd, chi, iterations)."""
+        div = self.divergence(u, v)
+        chi, it, _ = self.sor_solve(div, chi0, eps, first_guess)
+        uu, vv, cc = f64(u), f64(v), f64(chi)
+        und, vnd = np.zeros_like(uu), np.zeros_like(vv)
+        self.L.orc_nondivergent_from_chi(self.m, ptr(cc), ptr(uu), ptr(vv), ptr(und), ptr(vnd))
+        return und, vnd, chi, it
 
     def sor_init(self):
         self.L.orc_sor_init(self.m)

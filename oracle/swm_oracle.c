@@ -962,6 +962,25 @@ void orc_divergence(orc_model *m, const double *u, const double *v, double *div)
     }
 }
 
+/* computeGradient (calc_lib.f90:638-648) of chi on the eta grid, pder_zonal3D
+   onto u (ind0 = ip0, indm1 = im1) and pder_meridional3D onto v (jp0, jm1),
+   subtracted from (u, v) as computeNonDivergentFlowField does (:567-571) */
+void orc_nondivergent_from_chi(orc_model *m, const double *chi, const double *u, const double *v, double *u_nd,
+                               double *v_nd) {
+  int nx = m->nx, ny = m->ny;
+  double A = m->c.A, dL = m->dLambda, dT = m->dTheta;
+  const int8_t *oE = m->ocean[ORC_OCEAN_ETA];
+  const double *bcU = m->f[ORC_BC_U], *bcV = m->f[ORC_BC_V], *cU = m->lat[ORC_COS_U];
+  for (int j = 0; j < ny; j++)
+    for (int i = 0; i < nx; i++) {
+      int k = IDX(i, j), ki = IDX(m->im1[i], j), kj = IDX(i, m->jm1[j]);
+      double uc = (oE[ki] + oE[k] == 0) ? 0. : bcU[k] / (A * cU[j] * dL) * (chi[k] - chi[ki]);
+      double vc = (oE[kj] + oE[k] == 0) ? 0. : bcV[k] * (chi[k] - chi[kj]) / (A * dT);
+      u_nd[k] = u[k] - uc;
+      v_nd[k] = v[k] - vc;
+    }
+}
+
 /* ------------------------------------------------------------------------ */
 /* Tracer: tracer_vars.f90:124-185, tracer_module.f90:109-342               */
 /* ------------------------------------------------------------------------ */

@@ -119,6 +119,8 @@ void orc_run(orc_model *m, int64_t nsteps); /* itt+1 .. itt+nsteps with steady f
 /* ---- diagnostics helpers (calc_lib) ---- */
 void orc_streamfunction(orc_model *m, const double *u, const double *v, double *psi);
 void orc_divergence(orc_model *m, const double *u, const double *v, double *div);
+void orc_nondivergent_from_chi(orc_model *m, const double *chi, const double *u, const double *v, double *u_nd,
+                               double *v_nd);
 
 /* ---- tracer (tracer_module / tracer_vars) ---- */
 int orc_tracer_add(orc_model *m, double kappa_h, double cons, double gamma_c,

@@ -66,6 +66,7 @@ def _sigs():
                                      C.POINTER(C.c_double)]),
         'swm_helm_autotune': (I, [P, P, D, D, I, I, C.POINTER(C.c_double), C.POINTER(C.c_int),
                                   C.POINTER(C.c_int)]),
+        'swm_gpu_nondivergent': (I, [P, I, D, P, P, P, C.POINTER(C.c_int)]),
         'elsolv_sor_gpu_init': (I, [P]),
         'elsolv_sor_gpu_solve': (I, [P, P, P, D, I, C.POINTER(C.c_int), C.POINTER(C.c_double)]),
     }

@@ -20,6 +20,7 @@ struct SorState {
   double *anorm2 = nullptr;    // running sum for the current iteration
   int *done = nullptr;         // [0] converged flag, [1] iteration at convergence
   double *anorm_hist = nullptr;
+  double *und = nullptr, *vnd = nullptr;  // non-divergent flow
   int nblocks = 0;
 };
 
@@ -95,11 +96,47 @@ __global__ void k_sor_check(SorState s, int nparts, int l, double eps) {
   }
 }
 
+// computeDivergence (calc_lib.f90:607-622) of (u, v) onto the eta grid:
+// pder_zonal(u, u_grid) + pder_meridional(cos_v v, v_grid) / cos_eta, with
+// the mask tests of pder_zonal3D / pder_meridional3D (:892-998)
+__global__ void k_sor_divergence(Dev d, const double *u, const double *v, double *div) {
+  int i = blockIdx.x * blockDim.x + threadIdx.x, j = blockIdx.y * blockDim.y + threadIdx.y;
+  if (i >= d.nx || j >= d.ny) return;
+  size_t k = i + (size_t)d.nx * j;
+  int ip = i + 1 == d.nx ? 0 : i + 1, jp = j + 1 == d.ny ? 0 : j + 1;
+  size_t ki = ip + (size_t)d.nx * j, kj = i + (size_t)d.nx * jp;
+  const int8_t *oU = d.ocean[GU], *oV = d.ocean[GV];
+  const double bcE = d.ocean[GE][k] == 1 ? 1. : d.lbc;
+  const double *cE = d.cosl[GE], *cV = d.cosl[GV];
+  double dx = (oU[k] + oU[ki] == 0) ? 0. : bcE / (d.A * cE[j] * d.dLambda) * (u[ki] - u[k]);
+  double dy = (oV[kj] + oV[k] == 0) ? 0. : bcE * (cV[jp] * v[kj] - cV[j] * v[k]) / (d.A * d.dTheta);
+  div[k] = dx + dy / cE[j];
+}
+
+// computeGradient (:638-648) of chi on the eta grid (zonal part onto u,
+// meridional onto v) subtracted from (u, v): computeNonDivergentFlowField
+// (:548-590), u_nd = u - u_corr, v_nd = v - v_corr
+__global__ void k_sor_nondiv(Dev d, const double *chi, const double *u, const double *v, double *u_nd,
+                             double *v_nd) {
+  int i = blockIdx.x * blockDim.x + threadIdx.x, j = blockIdx.y * blockDim.y + threadIdx.y;
+  if (i >= d.nx || j >= d.ny) return;
+  size_t k = i + (size_t)d.nx * j;
+  int im = i == 0 ? d.nx - 1 : i - 1, jm = j == 0 ? d.ny - 1 : j - 1;
+  size_t ki = im + (size_t)d.nx * j, kj = i + (size_t)d.nx * jm;
+  const int8_t *oE = d.ocean[GE];
+  const double bcU = d.ocean[GU][k] == 1 ? 1. : d.lbc, bcV = d.ocean[GV][k] == 1 ? 1. : d.lbc;
+  double uc = (oE[ki] + oE[k] == 0) ? 0. : bcU / (d.A * d.cosl[GU][j] * d.dLambda) * (chi[k] - chi[ki]);
+  double vc = (oE[kj] + oE[k] == 0) ? 0. : bcV * (chi[k] - chi[kj]) / (d.A * d.dTheta);
+  u_nd[k] = u[k] - uc;
+  v_nd[k] = v[k] - vc;
+}
+
 void sor_free(swm_gpu_ctx *c) {
   if (!c->sor) return;
   SorState *s = c->sor;
   for (int q = 0; q < 5; q++) cudaFree(s->c[q]);
   cudaFree(s->chi); cudaFree(s->B); cudaFree(s->partial); cudaFree(s->done); cudaFree(s->anorm_hist);
+  cudaFree(s->und); cudaFree(s->vnd);
   delete s;
   c->sor = nullptr;
 }
@@ -124,6 +161,7 @@ int elsolv_sor_gpu_init(swm_gpu_ctx *c) {
   SWM_CK(cudaMalloc((void **)&s->partial, 2 * (size_t)s->nblocks * 8));
   SWM_CK(cudaMalloc((void **)&s->done, 2 * sizeof(int)));
   SWM_CK(cudaMalloc((void **)&s->anorm_hist, 8));
+  SWM_CK(cudaMemsetAsync(s->chi, 0, n * 8, c->stream));  // calc_lib::chi starts at 0
   k_sor_coeff<<<g, b, 0, c->stream>>>(c->dev(), *s);
   c->launches++;
   SWM_CK(cudaGetLastError());
@@ -131,16 +169,16 @@ int elsolv_sor_gpu_init(swm_gpu_ctx *c) {
   return SWM_GPU_OK;
 }
 
-int elsolv_sor_gpu_solve(swm_gpu_ctx *c, const double *B, double *chi, double eps, int first_guess, int *iters,
-                         double *anorm) {
-  SWM_REQUIRE(c && c->sor && B && chi, "elsolv_sor_gpu_solve: call elsolv_sor_gpu_init first");
+}  // extern "C"
+
+// main_ElSolv_SOR on the device arrays s->B (right-hand side) and s->chi
+// (first guess in, solution out); returns SWM_GPU_ENOT_CONVERGED after
+// max_count iterations
+static int sor_solve_device(swm_gpu_ctx *c, double eps, int first_guess, int *iters, double *anorm) {
   SorState *s = c->sor;
-  size_t n = c->n;
   int mx = c->nx > c->ny ? c->nx : c->ny;
   int max_count = first_guess ? (int)lround(1000. * mx) : (int)lround(10. * mx);
   const double rJ = (double)(float)9.9999178e-1;
-  SWM_CK(cudaMemcpyAsync(s->B, B, n * 8, cudaMemcpyHostToDevice, c->stream));
-  SWM_CK(cudaMemcpyAsync(s->chi, chi, n * 8, cudaMemcpyHostToDevice, c->stream));
   SWM_CK(cudaMemsetAsync(s->done, 0, 2 * sizeof(int), c->stream));
   dim3 b(32, 8), g((c->nx + 31) / 32, (c->ny + 7) / 8);
   Dev d = c->dev();
@@ -168,7 +206,6 @@ int elsolv_sor_gpu_solve(swm_gpu_ctx *c, const double *B, double *chi, double ep
   }
   double an = 0.;
   SWM_CK(cudaMemcpyAsync(&an, s->anorm_hist, 8, cudaMemcpyDeviceToHost, c->stream));
-  SWM_CK(cudaMemcpyAsync(chi, s->chi, n * 8, cudaMemcpyDeviceToHost, c->stream));
   SWM_CK(cudaStreamSynchronize(c->stream));
   if (anorm) *anorm = an;
   if (done[0]) {
@@ -178,6 +215,57 @@ int elsolv_sor_gpu_solve(swm_gpu_ctx *c, const double *B, double *chi, double ep
   if (iters) *iters = max_count;
   set_error("elsolv_sor_gpu_solve: not converged after max_count iterations");
   return SWM_GPU_ENOT_CONVERGED;
+}
+
+extern "C" {
+
+int elsolv_sor_gpu_solve(swm_gpu_ctx *c, const double *B, double *chi, double eps, int first_guess, int *iters,
+                         double *anorm) {
+  SWM_REQUIRE(c && c->sor && B && chi, "elsolv_sor_gpu_solve: call elsolv_sor_gpu_init first");
+  SorState *s = c->sor;
+  size_t n = c->n;
+  SWM_CK(cudaMemcpyAsync(s->B, B, n * 8, cudaMemcpyHostToDevice, c->stream));
+  SWM_CK(cudaMemcpyAsync(s->chi, chi, n * 8, cudaMemcpyHostToDevice, c->stream));
+  int rc = sor_solve_device(c, eps, first_guess, iters, anorm);
+  SWM_CK(cudaMemcpyAsync(chi, s->chi, n * 8, cudaMemcpyDeviceToHost, c->stream));
+  SWM_CK(cudaStreamSynchronize(c->stream));
+  return rc;
+}
+
+// computeNonDivergentFlowField (calc_lib.f90:548-590) of the model's current
+// (u, v): divergence, SOR for chi (chi kept on the device between calls as
+// the reference keeps calc_lib::chi; first_guess as itt == 1), gradient,
+// u_nd = u - grad_lambda chi, v_nd = v - grad_theta chi.  Outputs may be
+// NULL.  SOR non-convergence is reported as by elsolv_sor_gpu_solve, with
+// the non-divergent flow still formed.
+int swm_gpu_nondivergent(swm_gpu_ctx *c, int first_guess, double eps, double *u_nd, double *v_nd, double *chi,
+                         int *iters) {
+  SWM_REQUIRE(c && c->stage >= 5 && c->sor, "swm_gpu_nondivergent: call elsolv_sor_gpu_init first");
+  SorState *s = c->sor;
+  const size_t n = c->n;
+  if (!s->und) {
+    SWM_CK(cudaMalloc((void **)&s->und, n * 8));
+    SWM_CK(cudaMalloc((void **)&s->vnd, n * 8));
+  }
+  if (c->cfg.path != SWM_PATH_PLAIN_FP64 && c->fused) {
+    int rc0 = fused_sync_state(c);
+    if (rc0 != SWM_GPU_OK) return rc0;
+  }
+  Dev d = c->dev();
+  dim3 b(32, 8), g((c->nx + 31) / 32, (c->ny + 7) / 8);
+  k_sor_divergence<<<g, b, 0, c->stream>>>(d, d.u0, d.v0, s->B);
+  c->launches++;
+  SWM_CK(cudaGetLastError());
+  int rc = sor_solve_device(c, eps, first_guess, iters, nullptr);
+  if (rc != SWM_GPU_OK && rc != SWM_GPU_ENOT_CONVERGED) return rc;
+  k_sor_nondiv<<<g, b, 0, c->stream>>>(d, s->chi, d.u0, d.v0, s->und, s->vnd);
+  c->launches++;
+  SWM_CK(cudaGetLastError());
+  if (u_nd) SWM_CK(cudaMemcpyAsync(u_nd, s->und, n * 8, cudaMemcpyDeviceToHost, c->stream));
+  if (v_nd) SWM_CK(cudaMemcpyAsync(v_nd, s->vnd, n * 8, cudaMemcpyDeviceToHost, c->stream));
+  if (chi) SWM_CK(cudaMemcpyAsync(chi, s->chi, n * 8, cudaMemcpyDeviceToHost, c->stream));
+  SWM_CK(cudaStreamSynchronize(c->stream));
+  return rc;
 }
 
 }  // extern "C"

@@ -174,6 +174,17 @@ class GpuModel:
         check(self.L.trc_gpu_get_field(self.ctx, t, TRC_FIELD[name], _p(out)))
         return out
 
+    def nondivergent(self, first_guess, eps=1e-4):
+        """computeNonDivergentFlowField of the current state: (u_nd, v_nd,
+        chi, SOR iterations, status)."""
+        u, v, chi = (np.empty((self.ny, self.nx)) for _ in range(3))
+        it = C.c_int()
+        rc = self.L.swm_gpu_nondivergent(self.ctx, int(bool(first_guess)), eps, _p(u), _p(v), _p(chi),
+                                         C.byref(it))
+        if rc not in (0, 4):
+            check(rc)
+        return u, v, chi, it.value, rc
+
     # -- SOR -----------------------------------------------------------
     def sor_init(self):
         check(self.L.elsolv_sor_gpu_init(self.ctx))

@@ -109,3 +109,42 @@ def test_sor_matches_oracle():
     # a non-converging call (max_count = 10*max(Nx,Ny)) reports it
     xg2, ig2, _ = g.sor_solve(B, chi0, 1e-40, False)
     assert ig2 < 0
+
+
+def test_nondivergent_flow_matches_oracle():
+    """computeNonDivergentFlowField on the GPU (divergence, SOR, gradient on
+    the device) against the oracle pipeline from the same state, for a first
+    call (first_guess) and a second one starting from the kept chi."""
+    case = synthetic.double_gyre((40, 32), biharmonic=False, nsteps=60)
+    o, g = _pair(case, 60)
+    o.sor_init()
+    g.sor_init()
+    chi = np.zeros((case['config']['ny'], case['config']['nx']))
+    for first in (True, False):
+        uo, vo, chi, io = o.nondivergent(o.field('u'), o.field('v'), chi, first)
+        ug, vg, cg, ig, rc = g.nondivergent(first)
+        if io < 0:
+            # max_count (10 max(Nx, Ny) after the first call) reached
+            # unconverged, as the reference allows with a warning
+            assert rc == 4 and ig == -io, (io, ig)
+            io = -io
+        else:
+            assert rc == 0 and abs(ig - io) <= 1, (io, ig)
+        if ig == io:
+            assert np.array_equal(cg, chi)
+            assert np.array_equal(ug, uo) and np.array_equal(vg, vo)
+        assert np.abs(ug - uo).max() <= 1e-6 * np.abs(uo).max()
+        chi = cg
+        o.run_steady(5)
+        g.run(60 + (0 if first else 5), 5)
+    # a converged correction (the first-call iteration budget) removes the
+    # divergence of cells away from the coast (next to it the reference's
+    # gradient, masked with the eta masks and the land boundary factor, puts
+    # velocity on land faces, which the divergence then reads)
+    oe, ou, ov = g.ocean('eta'), g.ocean('u'), g.ocean('v')
+    inner = (oe == 1) & (ou == 1) & (np.roll(ou, -1, 1) == 1) & (ov == 1) & (np.roll(ov, -1, 0) == 1)
+    inner &= (np.roll(oe, 1, 1) == 1) & (np.roll(oe, -1, 1) == 1) & (np.roll(oe, 1, 0) == 1) & (np.roll(oe, -1, 0) == 1)
+    d0 = np.abs(o.divergence(g.field('u'), g.field('v'))[inner]).sum()
+    ug, vg, _, _, rc = g.nondivergent(True)
+    assert rc == 0
+    assert np.abs(o.divergence(ug, vg)[inner]).sum() < 0.5 * d0
