@@ -134,6 +134,14 @@ int swm_gpu_set_stream_data(swm_gpu_ctx *ctx, int id, const double *d1, const do
 /* same for a stream whose data is constant along each row: Ny values per
    part (one H2D copy of Ny doubles); d2 may be NULL */
 int swm_gpu_set_stream_rows(swm_gpu_ctx *ctx, int id, const double *rows1, const double *rows2);
+/* All records of part 1 or 2 (nrec x Nx x Ny) of a time-dependent stream,
+   kept on the device; each step swm_gpu_stream_interp then forms the record
+   in use on the device from the memchunk bracket the host computes (record
+   indices r0, r1 and their times t0, t1; r1 < 0: exactly record r0) as
+   getChunkData (memchunk_module.f90:214-246) does, instead of one H2D copy
+   of the whole field per step and stream */
+int swm_gpu_stream_records(swm_gpu_ctx *ctx, int id, int part, int nrec, const double *records);
+int swm_gpu_stream_interp(swm_gpu_ctx *ctx, int id, int part, int r0, int r1, double t, double t0, double t1);
 /* SWM_forcing_init (swm_forcing_module.f90:78-127) */
 int swm_gpu_forcing_init(swm_gpu_ctx *ctx);
 /* SWM_initialConditions (swm_module.f90:156-181) */

@@ -44,6 +44,8 @@ def _sigs():
         'swm_gpu_add_damping': (I, [P, I, I, D, D, D, I, P]), 'swm_gpu_finish_damping': (I, [P]),
         'swm_gpu_add_stream': (I, [P, I, I, D, I, P, P, C.POINTER(C.c_int)]),
         'swm_gpu_set_stream_data': (I, [P, I, P, P]), 'swm_gpu_forcing_init': (I, [P]),
+        'swm_gpu_stream_records': (I, [P, I, I, I, P]),
+        'swm_gpu_stream_interp': (I, [P, I, I, I, I, D, D, D]),
         'swm_gpu_set_stream_rows': (I, [P, I, P, P]), 'swm_gpu_integrals': (I, [P, P]),
         'swm_gpu_integrals_noalloc': (I, [P, P]),
         'swm_gpu_initial_conditions': (I, [P, P, P, P]), 'swm_gpu_step': (I, [P, I64]),

@@ -173,7 +173,7 @@ int swm_gpu_destroy(swm_gpu_ctx *c) {
   for (int q = 0; q < 3; q++) { F(c->Gu[q]); F(c->Gv[q]); F(c->Ge[q]); F(c->impl[q]); F(c->glin[q]); F(c->F[q]); F(c->Fc[q]); }
   F(c->edens); F(c->pot); F(c->zeta); F(c->mu); F(c->mv); F(c->pll); F(c->plt); F(c->lmu); F(c->lmv);
   F(c->ones); F(c->ubs); F(c->vbs); F(c->zbs); F(c->trc_coeff);
-  for (auto &s : c->streams) { F(s.d1); F(s.d2); }
+  for (auto &s : c->streams) { F(s.d1); F(s.d2); F(s.rec[0]); F(s.rec[1]); }
   for (auto &t : c->tracers) {
     F(t.CH[0]); F(t.CH[1]); F(t.G[0]); F(t.G[1]); F(t.G[2]); F(t.C); F(t.C0); F(t.gamma); F(t.impl);
     F(t.uhc); F(t.vhc); F(t.diff);
@@ -310,6 +310,32 @@ int swm_gpu_set_stream_data(swm_gpu_ctx *c, int id, const double *d1, const doub
   SWM_REQUIRE(c && id >= 0 && id < (int)c->streams.size(), "swm_gpu_set_stream_data: bad stream id");
   if (d1) TRY(h2d(c, c->streams[id].d1, d1, c->n));
   if (d2) TRY(h2d(c, c->streams[id].d2, d2, c->n));
+  if (d1) TRY(fused_refresh_wind(c, id));
+  return SWM_GPU_OK;
+}
+
+int swm_gpu_stream_records(swm_gpu_ctx *c, int id, int part, int nrec, const double *records) {
+  SWM_REQUIRE(c && id >= 0 && id < (int)c->streams.size() && (part == 1 || part == 2) && nrec > 0 && records,
+              "swm_gpu_stream_records: bad arguments");
+  Stream &s = c->streams[id];
+  double *&r = s.rec[part - 1];
+  if (r) cudaFree(r);
+  r = nullptr;
+  SWM_CK(cudaMalloc((void **)&r, (size_t)nrec * c->n * 8));
+  s.nrec[part - 1] = nrec;
+  SWM_CK(cudaMemcpyAsync(r, records, (size_t)nrec * c->n * 8, cudaMemcpyHostToDevice, c->stream));
+  SWM_CK(cudaStreamSynchronize(c->stream));
+  return SWM_GPU_OK;
+}
+
+int swm_gpu_stream_interp(swm_gpu_ctx *c, int id, int part, int r0, int r1, double t, double t0, double t1) {
+  SWM_REQUIRE(c && id >= 0 && id < (int)c->streams.size() && (part == 1 || part == 2),
+              "swm_gpu_stream_interp: bad arguments");
+  Stream &s = c->streams[id];
+  const int nr = s.nrec[part - 1];
+  SWM_REQUIRE(s.rec[part - 1] && r0 >= 0 && r0 < nr && r1 < nr, "swm_gpu_stream_interp: records not set or bad index");
+  TRY(stream_interp(c, s.rec[part - 1], part == 1 ? s.d1 : s.d2, r0, r1, t, t0, t1));
+  if (part == 1) TRY(fused_refresh_wind(c, id));
   return SWM_GPU_OK;
 }
 

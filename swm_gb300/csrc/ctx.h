@@ -52,7 +52,9 @@ struct HostGrid {
 struct Stream {
   int type, comp, is_const;
   double omega;
-  double *d1 = nullptr, *d2 = nullptr;  // device records
+  double *d1 = nullptr, *d2 = nullptr;      // the record in use (device)
+  double *rec[2] = {nullptr, nullptr};      // all records of parts 1 and 2 (device, optional)
+  int nrec[2] = {0, 0};
 };
 
 struct DiagAcc {  // one time-averaging buffer (diagTask)
@@ -158,6 +160,7 @@ int fused_prepare(swm_gpu_ctx *c);
 int fused_step(swm_gpu_ctx *c, int64_t itt);
 int fused_sync_state(swm_gpu_ctx *c);    // FP32 pair state -> FP64 buffers
 int fused_load_state(swm_gpu_ctx *c);    // FP64 buffers -> FP32 pair state
+int fused_refresh_wind(swm_gpu_ctx *c, int id);  // stream id's record changed
 void fused_free(swm_gpu_ctx *c);
 void integrals_free(swm_gpu_ctx *c);
 // sor.cu
@@ -167,6 +170,7 @@ int device_streamfunction(swm_gpu_ctx *c);
 int diag_accumulate(swm_gpu_ctx *c, int slot, const double *f, int square, double w);
 int diag_mean(swm_gpu_ctx *c, int slot, double *dev_out, double *count);
 void diag_free(swm_gpu_ctx *c);
+int stream_interp(swm_gpu_ctx *c, const double *rec, double *dst, int r0, int r1, double t, double t0, double t1);
 // trc32.cu
 bool trc32_active(const swm_gpu_ctx *c);
 int trc32_add(swm_gpu_ctx *c, const std::vector<double> &CH, const std::vector<double> &C0,

@@ -136,6 +136,29 @@ int diag_mean(swm_gpu_ctx *c, int slot, double *dev_out, double *count) {
   return SWM_GPU_OK;
 }
 
+// getChunkData (memchunk_module.f90:214-246) on the device: the record at
+// the bracket's lower end, or y0 + (t - t0) (y1 - y0) / (t1 - t0) between two
+// records (r1 < 0: exactly record r0), in the restatement's operation order
+__global__ void k_stream_interp(const double *rec, double *dst, size_t n, int r0, int r1, double t, double t0,
+                                double t1) {
+  const size_t k = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (k >= n) return;
+  const double y0 = rec[(size_t)r0 * n + k];
+  if (r1 < 0) {
+    dst[k] = y0;
+    return;
+  }
+  const double y1 = rec[(size_t)r1 * n + k];
+  dst[k] = y0 + (t - t0) * (y1 - y0) / (t1 - t0);
+}
+
+int stream_interp(swm_gpu_ctx *c, const double *rec, double *dst, int r0, int r1, double t, double t0, double t1) {
+  k_stream_interp<<<(unsigned)((c->n + 255) / 256), 256, 0, c->stream>>>(rec, dst, c->n, r0, r1, t, t0, t1);
+  c->launches++;
+  SWM_CK(cudaGetLastError());
+  return SWM_GPU_OK;
+}
+
 void diag_free(swm_gpu_ctx *c) {
   for (auto &a : c->diag) cudaFree(a.buf);
   c->diag.clear();

@@ -702,6 +702,37 @@ void fused_set_indices(swm_gpu_ctx *c, int n0, int g0) {
   c->fused->n0 = n0;
   c->fused->g0 = g0;
 }
+template <typename T>
+__global__ void k_field_col0(const double *field, T *dst, int nx, int ny) {
+  int j = blockIdx.x * blockDim.x + threadIdx.x;
+  if (j < ny) dst[j] = (T)field[(size_t)nx * j];
+}
+
+// after a time-dependent wind-stress stream's device record changed: the
+// fused kernels read their own copy (row profile or field, in the path's
+// precision), refreshed here from the stream's FP64 record
+int fused_refresh_wind(swm_gpu_ctx *c, int id) {
+  FusedState *f = c->fused;
+  if (!f || !f->ready) return SWM_GPU_OK;
+  const Stream &s = c->streams[id];
+  if (s.is_const || s.type != SWM_FRC_WIND || c->cfg.mode != SWM_MODE_NONLINEAR) return SWM_GPU_OK;
+  if (s.comp != SWM_CMP_ZONAL && s.comp != SWM_CMP_MERID) return SWM_GPU_OK;
+  void *dst = s.comp == SWM_CMP_ZONAL ? f->wx : f->wy;
+  if (!dst) return SWM_GPU_OK;
+  if (f->wind_rows) {
+    unsigned nb = (unsigned)((c->ny + 255) / 256);
+    if (f->comp) k_field_col0<float><<<nb, 256, 0, c->stream>>>(s.d1, (float *)dst, c->nx, c->ny);
+    else k_field_col0<double><<<nb, 256, 0, c->stream>>>(s.d1, (double *)dst, c->nx, c->ny);
+  } else {
+    unsigned nb = (unsigned)((c->n + 255) / 256);
+    if (f->comp) k_to_f32<<<nb, 256, 0, c->stream>>>(s.d1, (float *)dst, c->n);
+    else SWM_CK(cudaMemcpyAsync(dst, s.d1, c->n * 8, cudaMemcpyDeviceToDevice, c->stream));
+  }
+  c->launches++;
+  SWM_CK(cudaGetLastError());
+  return SWM_GPU_OK;
+}
+
 void fused_static(const swm_gpu_ctx *c, const float **He, const uint16_t **mask16, const float **Fe) {
   const FusedState *f = c->fused;
   *He = (const float *)f->He;

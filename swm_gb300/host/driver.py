@@ -98,9 +98,11 @@ class DiagTask:
 
 
 class Driver:
-    def __init__(self, case, backend, device_averages=True):
+    def __init__(self, case, backend, device_averages=True, device_streams=True):
         self.case, self.b = case, backend
         self.device_averages = device_averages
+        # time-dependent forcing records kept on the device, interpolated there
+        self.device_streams = device_streams and hasattr(backend, 'stream_interp')
         self.cfg = case['config']
         self.itt = 0
         self.tasks = []
@@ -122,7 +124,11 @@ class Driver:
             self.chunks.append((mc1, mc2, tdf))
             d1 = mc1.get(0.0) if not tdf else np.zeros_like(mc1.rec[0])
             d2 = (mc2.get(0.0) if (mc2 is not None and not tdf) else None)
-            b.add_stream(s, not tdf, d1, d2)
+            sid = b.add_stream(s, not tdf, d1, d2)
+            if tdf and self.device_streams:
+                b.stream_records(sid, 1, mc1.rec)
+                if mc2 is not None:
+                    b.stream_records(sid, 2, mc2.rec)
         self._feed_streams(0)
         b.forcing_init()
         self._feed_streams(0)
@@ -140,7 +146,13 @@ class Driver:
     def _feed_streams(self, itt):
         t = itt * self.cfg['dt']
         for sid, (mc1, mc2, tdf) in enumerate(self.chunks):
-            if tdf:
+            if not tdf:
+                continue
+            if self.device_streams:
+                self.b.stream_interp(sid, 1, mc1.bracket(t))
+                if mc2 is not None:
+                    self.b.stream_interp(sid, 2, mc2.bracket(t))
+            else:
                 self.b.set_stream_data(sid, mc1.get(t), mc2.get(t) if mc2 is not None else None)
 
     def fetch(self, name):

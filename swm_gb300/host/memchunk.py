@@ -35,13 +35,14 @@ class MemChunk:
         self.file_rec = 1
         self.nfpc = 1
         self.var = np.zeros((self.chunksize,) + rec.shape[1:])
+        self.idx = np.zeros(self.chunksize, dtype=np.int64)  # record index held by each chunk slot
         self.time = np.zeros(self.chunksize)
         self.initialised = False
         self._get_chunk_from_disk()
         self.nfpc = max(int(np.floor(float(np.float32(self.chunksize)) / nrec)), 1)
         self.initialised = True
 
-    def _read(self, out, nstart, length):
+    def _read(self, out, nstart, length, off=0):
         # getVarChunkFromDisk; returns the (possibly rewound) nstart
         nrec = self.nrec
         if nstart > nrec:
@@ -51,8 +52,9 @@ class MemChunk:
         nend = min(nstart + length - 1, nrec)
         len2 = max(nend - nstart, 0) + 1
         out[:len2] = self.rec[nstart - 1:nstart - 1 + len2]
+        self.idx[off:off + len2] = np.arange(nstart - 1, nstart - 1 + len2)
         if len2 < length:
-            self._read(out[len2:], 1, length - len2)
+            self._read(out[len2:], 1, length - len2, off + len2)
         return nstart
 
     def _get_chunk_from_disk(self):
@@ -67,10 +69,12 @@ class MemChunk:
                 self.t_offset = self.t_offset + self.dt
         self.counter = 1
 
-    def get(self, t):
-        """getChunkData(memChunk, time) -> (ny, nx) float64."""
+    def bracket(self, t):
+        """The records getChunkData interpolates between at time t:
+        (r0, r1, t, t0, t1) with record indices of the dataset; r1 = -1 when
+        the value is exactly record r0.  Advances the chunk state as get."""
         if self.is_constant:
-            return self.var[0].copy()
+            return int(self.idx[0]), -1, t, 0.0, 0.0
         if self.counter >= self.chunksize:
             self._get_chunk_from_disk()
         while self.time[self.counter] < t:       # time(counter+1), 1-based
@@ -79,7 +83,13 @@ class MemChunk:
                 self._get_chunk_from_disk()
         c = self.counter - 1
         if t == self.time[c]:
-            return self.var[c].copy()
-        y0, y1 = self.var[c], self.var[c + 1]
-        x0, x1 = self.time[c], self.time[c + 1]
+            return int(self.idx[c]), -1, t, float(self.time[c]), float(self.time[c])
+        return int(self.idx[c]), int(self.idx[c + 1]), t, float(self.time[c]), float(self.time[c + 1])
+
+    def get(self, t):
+        """getChunkData(memChunk, time) -> (ny, nx) float64."""
+        r0, r1, t, x0, x1 = self.bracket(t)
+        if r1 < 0:
+            return self.rec[r0].copy()
+        y0, y1 = self.rec[r0], self.rec[r1]
         return y0 + (t - x0) * (y1 - y0) / (x1 - x0)

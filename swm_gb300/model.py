@@ -82,6 +82,14 @@ class GpuModel:
         a, b = _f64(d1), _f64(d2)
         check(self.L.swm_gpu_set_stream_data(self.ctx, sid, _p(a), _p(b)))
 
+    def stream_records(self, sid, part, records):
+        r = np.ascontiguousarray(records, dtype=np.float64)
+        check(self.L.swm_gpu_stream_records(self.ctx, sid, part, r.shape[0], _p(r)))
+
+    def stream_interp(self, sid, part, bracket):
+        r0, r1, t, t0, t1 = bracket
+        check(self.L.swm_gpu_stream_interp(self.ctx, sid, part, r0, r1, t, t0, t1))
+
     def set_stream_rows(self, sid, r1, r2=None):
         a, b = _f64(r1), _f64(r2)
         check(self.L.swm_gpu_set_stream_rows(self.ctx, sid, _p(a), _p(b)))
