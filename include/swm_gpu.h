@@ -163,6 +163,16 @@ int swm_gpu_run(swm_gpu_ctx *ctx, int64_t itt0, int64_t nsteps);
 /* ---- host access (the registry pointers the diagnostics read) ---- */
 int swm_gpu_get_field(swm_gpu_ctx *ctx, int field, double *host_out);
 int swm_gpu_set_field(swm_gpu_ctx *ctx, int field, const double *host_in);
+/* Output without stalling the time loop (for a writer thread; the reference
+   writes its diagnostics synchronously, io_module.f90:504-529): the copy of
+   the field as of this point of the stream goes into host_out (pinned memory
+   lets it overlap the following steps), and *ticket names it.  The buffer
+   must stay valid until swm_gpu_wait(ticket) returns; swm_gpu_ready returns
+   1 when done, 0 when not yet, -1 on error.  Tickets older than the last 64
+   wait for a later copy. */
+int swm_gpu_get_field_async(swm_gpu_ctx *ctx, int field, double *host_out, int64_t *ticket);
+int swm_gpu_wait(swm_gpu_ctx *ctx, int64_t ticket);
+int swm_gpu_ready(swm_gpu_ctx *ctx, int64_t ticket);
 /* 1-D metric: which = 0 lat, 1 cos, 2 tan, 3 f; grid = 0 H, 1 u, 2 v, 3 eta */
 int swm_gpu_get_metric(swm_gpu_ctx *ctx, int which, int grid, double *host_out);
 int swm_gpu_get_mask(swm_gpu_ctx *ctx, int grid, int8_t *host_out);

@@ -51,6 +51,8 @@ def _sigs():
         'swm_gpu_initial_conditions': (I, [P, P, P, P]), 'swm_gpu_step': (I, [P, I64]),
         'swm_gpu_advance': (I, [P, I64]), 'swm_gpu_run': (I, [P, I64, I64]),
         'swm_gpu_get_field': (I, [P, I, P]), 'swm_gpu_set_field': (I, [P, I, P]),
+        'swm_gpu_get_field_async': (I, [P, I, P, C.POINTER(C.c_int64)]), 'swm_gpu_wait': (I, [P, I64]),
+        'swm_gpu_ready': (I, [P, I64]),
         'swm_gpu_get_metric': (I, [P, I, I, P]), 'swm_gpu_get_mask': (I, [P, I, P]),
         'swm_gpu_streamfunction': (I, [P, P]),
         'swm_gpu_diag_accumulate': (I, [P, I, I, I, D]),

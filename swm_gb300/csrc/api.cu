@@ -178,6 +178,7 @@ int swm_gpu_destroy(swm_gpu_ctx *c) {
     F(t.CH[0]); F(t.CH[1]); F(t.G[0]); F(t.G[1]); F(t.G[2]); F(t.C); F(t.C0); F(t.gamma); F(t.impl);
     F(t.uhc); F(t.vhc); F(t.diff);
   }
+  for (auto e : c->async_ev) cudaEventDestroy(e);
   cudaStreamDestroy(c->stream);
   delete c;
   return SWM_GPU_OK;
@@ -561,6 +562,38 @@ int swm_gpu_get_field(swm_gpu_ctx *c, int f, double *out) {
   const double *p = nullptr;
   TRY(field_device(c, f, &p));
   return d2h(c, out, p, c->n);
+}
+
+constexpr int ASYNC_RING = 64;
+
+int swm_gpu_get_field_async(swm_gpu_ctx *c, int f, double *out, int64_t *ticket) {
+  SWM_REQUIRE(c && c->stage >= 1 && out && ticket, "swm_gpu_get_field_async: bad arguments");
+  if (c->async_ev.empty()) {
+    c->async_ev.resize(ASYNC_RING);
+    for (auto &e : c->async_ev) SWM_CK(cudaEventCreateWithFlags(&e, cudaEventDisableTiming));
+  }
+  const double *p = nullptr;
+  TRY(field_device(c, f, &p));
+  SWM_CK(cudaMemcpyAsync(out, p, c->n * 8, cudaMemcpyDeviceToHost, c->stream));
+  const int64_t t = c->async_next++;
+  SWM_CK(cudaEventRecord(c->async_ev[t % ASYNC_RING], c->stream));
+  *ticket = t;
+  return SWM_GPU_OK;
+}
+
+int swm_gpu_wait(swm_gpu_ctx *c, int64_t ticket) {
+  SWM_REQUIRE(c && ticket >= 0 && ticket < c->async_next, "swm_gpu_wait: unknown ticket");
+  SWM_CK(cudaEventSynchronize(c->async_ev[ticket % ASYNC_RING]));
+  return SWM_GPU_OK;
+}
+
+int swm_gpu_ready(swm_gpu_ctx *c, int64_t ticket) {
+  if (!c || ticket < 0 || ticket >= c->async_next) return -1;
+  cudaError_t e = cudaEventQuery(c->async_ev[ticket % ASYNC_RING]);
+  if (e == cudaSuccess) return 1;
+  if (e == cudaErrorNotReady) return 0;
+  set_error(std::string("swm_gpu_ready: ") + cudaGetErrorString(e));
+  return -1;
 }
 
 int swm_gpu_diag_accumulate(swm_gpu_ctx *c, int slot, int f, int square, double weight) {

@@ -129,6 +129,8 @@ struct swm_gpu_ctx {
   IntegralScratch *integrals = nullptr;
   Trc32State *trc32 = nullptr;      // tracers of the FP32 compensated path
   std::vector<swm::DiagAcc> diag;   // averaging buffers by slot
+  std::vector<cudaEvent_t> async_ev;  // ring of events for swm_gpu_get_field_async
+  int64_t async_next = 0;             // next ticket
   double *psi = nullptr, *psi_tmp = nullptr;  // streamfunction and its zonal sums
   int64_t advances = 0;             // swm_gpu_advance calls (the rotation phase is advances mod 6)
   int march_rows = 0;                // rows per warp strip of the FP32 step kernel (0: not tuned yet)

@@ -145,6 +145,21 @@ class GpuModel:
         check(self.L.swm_gpu_get_field(self.ctx, FIELD_ID[name], _p(out)))
         return out
 
+    def field_async(self, name, out):
+        """Start the copy of a field into out (a C-contiguous float64 array,
+        ideally in pinned memory); returns a ticket for wait()/ready()."""
+        name = self._ALIAS.get(name, name)
+        assert out.flags.c_contiguous and out.dtype == np.float64 and out.size == self.nx * self.ny
+        t = C.c_int64()
+        check(self.L.swm_gpu_get_field_async(self.ctx, FIELD_ID[name], _p(out), C.byref(t)))
+        return t.value
+
+    def wait(self, ticket):
+        check(self.L.swm_gpu_wait(self.ctx, ticket))
+
+    def ready(self, ticket):
+        return self.L.swm_gpu_ready(self.ctx, ticket)
+
     def set_field(self, name, arr):
         a = _f64(arr)
         check(self.L.swm_gpu_set_field(self.ctx, FIELD_ID[self._ALIAS.get(name, name)], _p(a)))
