@@ -12,6 +12,7 @@
 // (swm_gpu_config.tracer_flux = 1) with the reference's mask-weighted mean
 // next to land.
 #include <cmath>
+#include <cstdlib>
 #include <cstring>
 #include <string>
 #include <vector>
@@ -72,7 +73,7 @@ __device__ __forceinline__ void comp_update(float hi, float lo, float inc, float
 }
 
 constexpr unsigned FULLM = 0xffffffffu;
-constexpr int TRC_ROWS = 16;  // output rows per warp (before fitting the grid to whole waves)
+constexpr int TRC_ROWS = 16;  // output rows per warp
 
 // One warp owns a strip of 32 columns (lane = column; 2 halo lanes per side,
 // as the upwind-biased faces reach two cells) and TRC_ROWS output rows; it
@@ -234,28 +235,19 @@ __global__ void __launch_bounds__(128, NT <= 2 ? 4 : 3) k_trc32(TrcP p, int S, i
   }
 }
 
-// rows per warp: TRC_ROWS, lengthened so the grid ends on a whole wave of
-// resident warps (a grid just over a whole number of waves costs one more)
-template <int NT, int FLUX>
-static int trc_rows(int nstrips, int ny) {
-  static int resident = 0;
-  if (!resident) {
-    int per_sm = 0, sms = 0, dev = 0;
-    cudaGetDevice(&dev);
-    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_trc32<NT, FLUX>, 128, 0);
-    resident = sms * (per_sm > 0 ? per_sm : 1);  // blocks
-  }
-  const long blocks = (long)nstrips * ((ny + 4 * TRC_ROWS - 1) / (4 * TRC_ROWS));
-  const long waves = (blocks + resident - 1) / resident;
-  const long per_strip = waves * resident / nstrips;
-  return per_strip > 0 ? (int)((ny + 4 * per_strip - 1) / (4 * per_strip)) : TRC_ROWS;
+// rows per warp: TRC_ROWS (SWM_GB300_TRC_ROWS overrides).  Lengths fitted
+// to whole waves of resident blocks were tried and ran slower (more
+// look-ahead rows per output row outweighed the shorter tail).
+static int trc_rows() {
+  const char *e = getenv("SWM_GB300_TRC_ROWS");
+  if (e && atoi(e) >= 4 && atoi(e) <= 256) return atoi(e);
+  return TRC_ROWS;
 }
 
 template <int NT, int FLUX>
 static void trc_launch_f(const TrcP &p, cudaStream_t st) {
   const int nstrips = (p.nx + 27) / 28;
-  const int S = trc_rows<NT, FLUX>(nstrips, p.ny);
+  const int S = trc_rows();
   const unsigned blocks = (unsigned)((long)nstrips * ((p.ny + 4 * S - 1) / (4 * S)));
   k_trc32<NT, FLUX><<<blocks, 128, 0, st>>>(p, S, nstrips);
 }

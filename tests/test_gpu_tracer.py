@@ -82,3 +82,21 @@ def test_fp32_tracers_graph_replay_and_launches():
         b.advance(s)
     for t in range(2):
         assert np.array_equal(a.tracer_field(t, 'CH'), b.tracer_field(t, 'CH')), t
+
+
+@pytest.mark.parametrize('flux', [0, 1])
+def test_fp32_tracer_rows_per_warp_do_not_change_results(flux, monkeypatch):
+    """Each tracer point is computed from the same inputs whatever the rows
+    per warp strip: the results agree bit for bit."""
+    case = synthetic.tracer_flow(72, nsteps=30, flux=flux)
+    out = []
+    for rows in ('5', '16', '23'):
+        monkeypatch.setenv('SWM_GB300_TRC_ROWS', rows)
+        g = GpuModel('fused_fp32c', tracer_nan_guard=True)
+        Driver(case, g).init(with_diag=False)
+        g.run(0, 25)
+        out.append([g.tracer_field(t, 'CH') for t in range(2)])
+        g.close()
+    for other in out[1:]:
+        for a, b in zip(out[0], other):
+            assert np.array_equal(a, b)
