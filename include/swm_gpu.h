@@ -160,6 +160,16 @@ int swm_gpu_advance(swm_gpu_ctx *ctx, int64_t itt);
    (bit-identical to single steps) */
 int swm_gpu_run(swm_gpu_ctx *ctx, int64_t itt0, int64_t nsteps);
 
+/* nsteps monitored steps (itt0+1 .. itt0+nsteps) issued without a host wait
+   per step: before step s the row profile rows1 + s*Ny (and rows2 + s*Ny for
+   a second component, may be NULL) of stream stream_id goes to the device
+   as swm_gpu_set_stream_rows does (rows1 NULL: no upload); after it the
+   three domain integrals of swm_gpu_integrals go to out3 + 3*s.  Returns
+   when the last copy has landed.  Inputs and outputs in pinned memory let
+   the copies overlap the steps. */
+int swm_gpu_run_monitor(swm_gpu_ctx *ctx, int64_t itt0, int64_t nsteps, int stream_id, const double *rows1,
+                        const double *rows2, double *out3);
+
 /* ---- host access (the registry pointers the diagnostics read) ---- */
 int swm_gpu_get_field(swm_gpu_ctx *ctx, int field, double *host_out);
 int swm_gpu_set_field(swm_gpu_ctx *ctx, int field, const double *host_in);
@@ -193,6 +203,10 @@ int swm_gpu_diag_mean(swm_gpu_ctx *ctx, int slot, double *host_out, double *coun
    No counterpart in the reference (its diagnostics write fields only); this
    is the per-step scalar a monitoring loop reads back (16-24 bytes D2H). */
 int swm_gpu_integrals(swm_gpu_ctx *ctx, double *out3);
+/* The same sums copied into out3 (pinned host memory, valid until the
+   ticket is waited on) without waiting: collect with swm_gpu_wait(ticket),
+   so a monitoring loop can issue the next step first */
+int swm_gpu_integrals_async(swm_gpu_ctx *ctx, double *out3, int64_t *ticket);
 /* The same three integrals, bit for bit, computed without allocating any
    memory (no device, pinned or library allocation): all scratch is one fixed
    array inside the library, for hosts that cannot allocate inside their time

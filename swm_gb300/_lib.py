@@ -48,8 +48,10 @@ def _sigs():
         'swm_gpu_stream_interp': (I, [P, I, I, I, I, D, D, D]),
         'swm_gpu_set_stream_rows': (I, [P, I, P, P]), 'swm_gpu_integrals': (I, [P, P]),
         'swm_gpu_integrals_noalloc': (I, [P, P]),
+        'swm_gpu_integrals_async': (I, [P, P, C.POINTER(C.c_int64)]),
         'swm_gpu_initial_conditions': (I, [P, P, P, P]), 'swm_gpu_step': (I, [P, I64]),
         'swm_gpu_advance': (I, [P, I64]), 'swm_gpu_run': (I, [P, I64, I64]),
+        'swm_gpu_run_monitor': (I, [P, I64, I64, I, P, P, P]),
         'swm_gpu_get_field': (I, [P, I, P]), 'swm_gpu_set_field': (I, [P, I, P]),
         'swm_gpu_get_field_async': (I, [P, I, P, C.POINTER(C.c_int64)]), 'swm_gpu_wait': (I, [P, I64]),
         'swm_gpu_ready': (I, [P, I64]),

@@ -492,6 +492,29 @@ int swm_gpu_run(swm_gpu_ctx *c, int64_t itt0, int64_t nsteps) {
   return SWM_GPU_OK;
 }
 
+// A monitored run issued from C with no host wait per step: for each step,
+// the step's wind-stress row profile goes up, the step and advance run, and
+// the domain integrals of the new state come down into out3 + 3 s; one wait
+// at the end.  Host and device work overlap, so a host loop of small API
+// calls does not set the pace.
+int swm_gpu_run_monitor(swm_gpu_ctx *c, int64_t itt0, int64_t nsteps, int stream_id, const double *rows1,
+                        const double *rows2, double *out3) {
+  SWM_REQUIRE(c && c->stage >= 5 && nsteps > 0 && out3, "swm_gpu_run_monitor: bad arguments");
+  SWM_REQUIRE(!rows1 || (stream_id >= 0 && stream_id < (int)c->streams.size()),
+              "swm_gpu_run_monitor: bad stream id");
+  const size_t ny = (size_t)c->ny;
+  for (int64_t s = 0; s < nsteps; s++) {
+    const int64_t itt = itt0 + s + 1;
+    if (rows1) TRY(swm_gpu_set_stream_rows(c, stream_id, rows1 + s * ny, rows2 ? rows2 + s * ny : nullptr));
+    TRY(swm_step_impl(c, itt));
+    TRY(swm_advance_impl(c, itt));
+    int64_t ticket;
+    TRY(swm_gpu_integrals_async(c, out3 + 3 * s, &ticket));
+  }
+  SWM_CK(cudaStreamSynchronize(c->stream));
+  return SWM_GPU_OK;
+}
+
 static const double *field_ptr(swm_gpu_ctx *c, int f, double **wptr) {
   Dev d = c->dev();
   double *p = nullptr;
@@ -564,21 +587,30 @@ int swm_gpu_get_field(swm_gpu_ctx *c, int f, double *out) {
   return d2h(c, out, p, c->n);
 }
 
+}  // extern "C"
+
 constexpr int ASYNC_RING = 64;
 
-int swm_gpu_get_field_async(swm_gpu_ctx *c, int f, double *out, int64_t *ticket) {
-  SWM_REQUIRE(c && c->stage >= 1 && out && ticket, "swm_gpu_get_field_async: bad arguments");
+// marks the work queued so far on the context's stream with a new ticket
+int swm::async_record(swm_gpu_ctx *c, int64_t *ticket) {
   if (c->async_ev.empty()) {
     c->async_ev.resize(ASYNC_RING);
     for (auto &e : c->async_ev) SWM_CK(cudaEventCreateWithFlags(&e, cudaEventDisableTiming));
   }
-  const double *p = nullptr;
-  TRY(field_device(c, f, &p));
-  SWM_CK(cudaMemcpyAsync(out, p, c->n * 8, cudaMemcpyDeviceToHost, c->stream));
   const int64_t t = c->async_next++;
   SWM_CK(cudaEventRecord(c->async_ev[t % ASYNC_RING], c->stream));
   *ticket = t;
   return SWM_GPU_OK;
+}
+
+extern "C" {
+
+int swm_gpu_get_field_async(swm_gpu_ctx *c, int f, double *out, int64_t *ticket) {
+  SWM_REQUIRE(c && c->stage >= 1 && out && ticket, "swm_gpu_get_field_async: bad arguments");
+  const double *p = nullptr;
+  TRY(field_device(c, f, &p));
+  SWM_CK(cudaMemcpyAsync(out, p, c->n * 8, cudaMemcpyDeviceToHost, c->stream));
+  return async_record(c, ticket);
 }
 
 int swm_gpu_wait(swm_gpu_ctx *c, int64_t ticket) {

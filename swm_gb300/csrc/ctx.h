@@ -167,6 +167,8 @@ void fused_free(swm_gpu_ctx *c);
 void integrals_free(swm_gpu_ctx *c);
 // sor.cu
 void sor_free(swm_gpu_ctx *c);
+// api.cu
+int async_record(swm_gpu_ctx *c, int64_t *ticket);  // ticket for the work queued so far
 // diag.cu
 int device_streamfunction(swm_gpu_ctx *c);
 int diag_accumulate(swm_gpu_ctx *c, int slot, const double *f, int square, double w);

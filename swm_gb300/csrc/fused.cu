@@ -796,52 +796,122 @@ void fused_free(swm_gpu_ctx *c) {
 // ---------------------------------------------------------------------------
 namespace swm {
 
-template <typename T, bool COMP>
-__global__ void k_integrals(int nx, int ny, const int8_t *oU, const int8_t *oV, const int8_t *oE,
-                            const double *area_u, const double *area_e, const T *u, const float *ul,
-                            const T *v, const float *vl, const T *e, const float *el, double G,
-                            double *partial) {
-  __shared__ double red[3][256];
-  double s0 = 0., s1 = 0., s2 = 0.;
-  size_t n = (size_t)nx * ny;
-  for (size_t k = (size_t)blockIdx.x * blockDim.x + threadIdx.x; k < n; k += (size_t)gridDim.x * blockDim.x) {
-    int j = (int)(k / nx);
-    double ee = (double)e[k] + (COMP ? (double)el[k] : 0.);
-    double uu = (double)u[k] + (COMP ? (double)ul[k] : 0.);
-    double vv = (double)v[k] + (COMP ? (double)vl[k] : 0.);
-    if (oE[k]) {
-      s0 += ee * area_e[j];
-      s1 += 0.5 * G * ee * ee * area_e[j];
-    }
-    if (oU[k]) s2 += 0.5 * uu * uu * area_u[j];
-    if (oV[k]) s2 += 0.5 * vv * vv * area_e[j];
+// (hi, lo) binary32 accumulator: TwoSum keeps the rounding error of every
+// addition, so a row sum carries about 46 bits; used for the pair state,
+// where FP64 arithmetic per point would tie the kernel to the FP64 pipe
+struct F2 {
+  float h = 0.f, l = 0.f;
+  __device__ __forceinline__ void add(float a, float b) {  // += a + b, |b| << |a|
+    const float s = h + a, bb = s - h;
+    l += ((h - (s - bb)) + (a - bb)) + b;
+    h = s;
   }
-  red[0][threadIdx.x] = s0;
-  red[1][threadIdx.x] = s1;
-  red[2][threadIdx.x] = s2;
-  __syncthreads();
-  for (int w = 128; w > 0; w >>= 1) {
-    if (threadIdx.x < w)
-      for (int q = 0; q < 3; q++) red[q][threadIdx.x] += red[q][threadIdx.x + w];
-    __syncthreads();
-  }
-  if (threadIdx.x == 0)
-    for (int q = 0; q < 3; q++) partial[(size_t)q * gridDim.x + blockIdx.x] = red[q][0];
+  __device__ __forceinline__ double value() const { return (double)h + (double)l; }
+};
+
+// the square of the pair (x, xl) as a pair: TwoProd of the high parts plus
+// the cross term (xl^2 is below the pair's precision)
+__device__ __forceinline__ void sq_pair(float x, float xl, float &p, float &e) {
+  p = x * x;
+  e = fmaf(x, x, -p) + 2.f * x * xl;
 }
 
-__global__ void k_integrals_final(const double *partial, int nb, double *out) {
-  __shared__ double red[256];
-  for (int q = 0; q < 3; q++) {
-    double a = 0.;
-    for (int b = threadIdx.x; b < nb; b += blockDim.x) a += partial[(size_t)q * nb + b];
-    red[threadIdx.x] = a;
-    __syncthreads();
-    for (int w = 128; w > 0; w >>= 1) {
-      if (threadIdx.x < w) red[threadIdx.x] += red[threadIdx.x + w];
-      __syncthreads();
+// Domain sums over ocean points, one grid row at a time: row sums of eta,
+// eta^2, u^2 and v^2 (FP64 state: in FP64; pair state: in (hi, lo) binary32
+// pairs), then times the row's cell area in FP64.  Per-block partials in a
+// fixed order (deterministic).
+template <typename T, bool COMP>
+__global__ void __launch_bounds__(256) k_integrals(int nx, int ny, const int8_t *oU, const int8_t *oV,
+                                                   const int8_t *oE, const double *area_u, const double *area_e,
+                                                   const T *u, const float *ul, const T *v, const float *vl,
+                                                   const T *e, const float *el, double G, double *partial) {
+  __shared__ double red[3][8];
+  double s0 = 0., s1 = 0., s2 = 0.;
+  for (int j = blockIdx.x; j < ny; j += gridDim.x) {
+    double r0 = 0., r1 = 0., ru = 0., rv = 0.;
+    const size_t row = (size_t)nx * j;
+    if (COMP) {
+      F2 a0, a1, au2, av2;
+      for (int i = threadIdx.x; i < nx; i += blockDim.x) {
+        const size_t k = row + i;
+        float p, q;
+        if (oE[k]) {
+          const float x = (float)e[k], xl = el[k];
+          a0.add(x, xl);
+          sq_pair(x, xl, p, q);
+          a1.add(p, q);
+        }
+        if (oU[k]) {
+          sq_pair((float)u[k], ul[k], p, q);
+          au2.add(p, q);
+        }
+        if (oV[k]) {
+          sq_pair((float)v[k], vl[k], p, q);
+          av2.add(p, q);
+        }
+      }
+      r0 = a0.value();
+      r1 = a1.value();
+      ru = au2.value();
+      rv = av2.value();
+    } else {
+      for (int i = threadIdx.x; i < nx; i += blockDim.x) {
+        const size_t k = row + i;
+        if (oE[k]) {
+          const double ee = (double)e[k];
+          r0 += ee;
+          r1 += ee * ee;
+        }
+        if (oU[k]) {
+          const double uu = (double)u[k];
+          ru += uu * uu;
+        }
+        if (oV[k]) {
+          const double vv = (double)v[k];
+          rv += vv * vv;
+        }
+      }
     }
-    if (threadIdx.x == 0) out[q] = red[0];
-    __syncthreads();
+    const double ae = area_e[j], au = area_u[j];
+    s0 += r0 * ae;
+    s1 += 0.5 * G * r1 * ae;
+    s2 += 0.5 * (ru * au + rv * ae);
+  }
+  for (int o = 16; o > 0; o >>= 1) {
+    s0 += __shfl_down_sync(0xffffffffu, s0, o);
+    s1 += __shfl_down_sync(0xffffffffu, s1, o);
+    s2 += __shfl_down_sync(0xffffffffu, s2, o);
+  }
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  if (lane == 0) {
+    red[0][warp] = s0;
+    red[1][warp] = s1;
+    red[2][warp] = s2;
+  }
+  __syncthreads();
+  if (threadIdx.x < 3) {
+    double a = 0.;
+    for (int w = 0; w < (int)(blockDim.x >> 5); w++) a += red[threadIdx.x][w];
+    partial[(size_t)threadIdx.x * gridDim.x + blockIdx.x] = a;
+  }
+}
+
+// sum of the per-block partials (one block of 256 threads, fixed order)
+__global__ void k_integrals_final(const double *partial, int nb, double *out) {
+  __shared__ double red[3][8];
+  double a[3] = {0., 0., 0.};
+  for (int b = threadIdx.x; b < nb; b += blockDim.x)
+    for (int q = 0; q < 3; q++) a[q] += partial[(size_t)q * nb + b];
+  for (int o = 16; o > 0; o >>= 1)
+    for (int q = 0; q < 3; q++) a[q] += __shfl_down_sync(0xffffffffu, a[q], o);
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  if (lane == 0)
+    for (int q = 0; q < 3; q++) red[q][warp] = a[q];
+  __syncthreads();
+  if (threadIdx.x < 3) {
+    double t = 0.;
+    for (int w = 0; w < (int)(blockDim.x >> 5); w++) t += red[threadIdx.x][w];
+    out[threadIdx.x] = t;
   }
 }
 
@@ -912,8 +982,11 @@ int swm_gpu_set_stream_rows(swm_gpu_ctx *c, int id, const double *r1, const doub
   return SWM_GPU_OK;
 }
 
-int swm_gpu_integrals(swm_gpu_ctx *c, double *out3) {
-  SWM_REQUIRE(c && c->stage >= 5 && out3, "swm_gpu_integrals: bad arguments");
+}  // extern "C"
+
+// the three sums of the current state into the context's device scratch
+// S->out (allocated on the first call)
+static int integrals_launch(swm_gpu_ctx *c) {
   IntegralScratch *S = c->integrals;
   if (!S) {
     S = c->integrals = new IntegralScratch();
@@ -947,10 +1020,27 @@ int swm_gpu_integrals(swm_gpu_ctx *c, double *out3) {
   }
   k_integrals_final<<<1, 256, 0, c->stream>>>(S->partial, S->nb, S->out);
   c->launches += 2;
+  SWM_CK(cudaGetLastError());
+  return SWM_GPU_OK;
+}
+
+extern "C" {
+
+int swm_gpu_integrals(swm_gpu_ctx *c, double *out3) {
+  SWM_REQUIRE(c && c->stage >= 5 && out3, "swm_gpu_integrals: bad arguments");
+  FTRY(integrals_launch(c));
+  IntegralScratch *S = c->integrals;
   SWM_CK(cudaMemcpyAsync(S->host, S->out, 3 * 8, cudaMemcpyDeviceToHost, c->stream));
   SWM_CK(cudaStreamSynchronize(c->stream));
   for (int q = 0; q < 3; q++) out3[q] = S->host[q];
   return SWM_GPU_OK;
+}
+
+int swm_gpu_integrals_async(swm_gpu_ctx *c, double *out3, int64_t *ticket) {
+  SWM_REQUIRE(c && c->stage >= 5 && out3 && ticket, "swm_gpu_integrals_async: bad arguments");
+  FTRY(integrals_launch(c));
+  SWM_CK(cudaMemcpyAsync(out3, c->integrals->out, 3 * 8, cudaMemcpyDeviceToHost, c->stream));
+  return async_record(c, ticket);
 }
 
 }  // extern "C"

@@ -99,6 +99,13 @@ class GpuModel:
         check(self.L.swm_gpu_integrals(self.ctx, _p(out)))
         return out
 
+    def integrals_async(self, out3):
+        """Start the domain integrals into out3 (3 float64, ideally pinned);
+        returns a ticket for wait()."""
+        t = C.c_int64()
+        check(self.L.swm_gpu_integrals_async(self.ctx, _p(out3), C.byref(t)))
+        return t.value
+
     def forcing_init(self):
         check(self.L.swm_gpu_forcing_init(self.ctx))
 
@@ -126,6 +133,14 @@ class GpuModel:
 
     def run(self, itt0, nsteps):
         check(self.L.swm_gpu_run(self.ctx, itt0, nsteps))
+
+    def run_monitor(self, itt0, nsteps, sid, rows1, out3, rows2=None):
+        """swm_gpu_run_monitor: rows1 (nsteps, Ny) per-step row profiles of
+        stream sid (or None), out3 (nsteps, 3) receives each step's integrals."""
+        assert out3.shape == (nsteps, 3) and out3.flags.c_contiguous and out3.dtype == np.float64
+        for r in (rows1, rows2):
+            assert r is None or (r.shape == (nsteps, self.ny) and r.flags.c_contiguous and r.dtype == np.float64)
+        check(self.L.swm_gpu_run_monitor(self.ctx, itt0, nsteps, sid, _p(rows1), _p(rows2), _p(out3)))
 
     def synchronize(self):
         check(self.L.swm_gpu_synchronize(self.ctx))
