@@ -11,8 +11,8 @@ compensated path) with the state resident in HBM; the L2 cache (129 MB; the
 per-step working set is ~85 MB) is flushed by a 512 MB device write before
 every timed step, and each step is timed with CUDA events on the library's
 stream.  e2e: the same metric through the C ABI with host buffers: every step
-uploads that step's wind-stress rows (H2D) and reads back the FP64 domain
-integrals (D2H), wall clock.  --impl reference times the CPU restatement of
+takes that step's wind-stress rows from host memory (H2D) and returns the
+FP64 domain integrals of its result to host memory (D2H), wall clock.  --impl reference times the CPU restatement of
 the reference's loops (the Fortran reference cannot be built here: no Fortran
 compiler) on the host cores.
 """
@@ -212,9 +212,9 @@ def ours(args, rank, ws):
     ms_nf = timed_steps(g, itt, 200, None, stream)
     itt += 200
     line['no_flush'] = {'ms_per_step': float(ms_nf.mean()), 'value': ncell / (ms_nf.mean() * 1e-3)}
-    # e2e through the C ABI with host buffers
-    # e2e: every step uploads its wind-stress row profile and reads back the
-    # FP64 domain integrals of its result, both in pinned host memory, through
+    # e2e through the C ABI with host buffers: every step takes its own
+    # wind-stress row profile from pinned host memory and returns the FP64
+    # domain integrals of its result into pinned host memory, through
     # swm_gpu_run_monitor (one C call issues all steps; no host wait per step)
     k_e2e = min(args.steps, 1000)
     ny = case['config']['ny']
@@ -230,9 +230,10 @@ def ours(args, rank, ws):
     assert np.isfinite(outs).all()
     line['e2e'] = {'value': ncell * k_e2e / e2e_s, 'unit': 'cell-steps/s', 'h2d_bytes_per_step': ny * 8,
                    'd2h_bytes_per_step': 3 * 8, 'steps': k_e2e,
-                   'per_step': "H2D of the step's wind-stress row profile (pinned), swm_gpu_step + "
-                               'swm_gpu_advance, D2H of the FP64 domain integrals (pinned), all steps issued by '
-                               'swm_gpu_run_monitor; wall clock including the final wait'}
+                   'per_step': "H2D: the step's wind-stress row profile, read from pinned host memory by the "
+                               'step kernel before the step; swm_gpu_step + swm_gpu_advance; D2H: the FP64 '
+                               'domain integrals of the new state, written into pinned host memory; all steps '
+                               'issued by swm_gpu_run_monitor; wall clock including the final wait; no L2 flush'}
     if rank == 0 and not args.quick:
         line.update(side_measurements(args, case, g, stream, flush, ncell))
         line['speedup_vs_fp64_plain'] = line['plain_fp64']['ms_per_step'] / step_ms

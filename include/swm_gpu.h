@@ -196,8 +196,11 @@ int swm_gpu_streamfunction(swm_gpu_ctx *ctx, double *psi_out);
    the mean. */
 int swm_gpu_diag_accumulate(swm_gpu_ctx *ctx, int slot, int field, int square, double weight);
 int swm_gpu_diag_mean(swm_gpu_ctx *ctx, int slot, double *host_out, double *count_out);
-/* Domain integrals of the current state, summed in FP64 on the device over
-   ocean points with the cell area A^2 cos(lat) dLambda dTheta:
+/* Domain integrals of the current state over ocean points, each point
+   weighted by the cell area A^2 cos(lat) dLambda dTheta at its own latitude
+   (eta and u points: the eta rows; v points: the v rows).  FP64 state:
+   summed in FP64; FP32 pair state: summed in (hi, lo) binary32 pairs (about
+   46 bits) and combined in FP64:
    out[0] = volume anomaly sum(eta * area), out[1] = sum(0.5 G eta^2 area),
    out[2] = sum(0.5 u^2 area) over u points + sum(0.5 v^2 area) over v points.
    No counterpart in the reference (its diagnostics write fields only); this

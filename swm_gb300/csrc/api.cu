@@ -4,6 +4,7 @@
 #include <cstring>
 #include <mutex>
 #include "ctx.h"
+#include "fused32.h"
 
 namespace swm {
 static thread_local std::string g_last_error;
@@ -172,7 +173,7 @@ int swm_gpu_destroy(swm_gpu_ctx *c) {
   for (int q = 0; q < 2; q++) { F(c->u[q]); F(c->v[q]); F(c->eta[q]); F(c->gsq[q]); }
   for (int q = 0; q < 3; q++) { F(c->Gu[q]); F(c->Gv[q]); F(c->Ge[q]); F(c->impl[q]); F(c->glin[q]); F(c->F[q]); F(c->Fc[q]); }
   F(c->edens); F(c->pot); F(c->zeta); F(c->mu); F(c->mv); F(c->pll); F(c->plt); F(c->lmu); F(c->lmv);
-  F(c->ones); F(c->ubs); F(c->vbs); F(c->zbs); F(c->trc_coeff);
+  F(c->ones); F(c->ubs); F(c->vbs); F(c->zbs); F(c->trc_coeff); F(c->rows_buf);
   for (auto &s : c->streams) { F(s.d1); F(s.d2); F(s.rec[0]); F(s.rec[1]); }
   for (auto &t : c->tracers) {
     F(t.CH[0]); F(t.CH[1]); F(t.G[0]); F(t.G[1]); F(t.G[2]); F(t.C); F(t.C0); F(t.gamma); F(t.impl);
@@ -492,24 +493,93 @@ int swm_gpu_run(swm_gpu_ctx *c, int64_t itt0, int64_t nsteps) {
   return SWM_GPU_OK;
 }
 
+// device address of a host array the device may read and write in place
+// (pinned, mapped into the device's address space), else null
+static double *mapped_view(const double *h) {
+  if (!h) return nullptr;
+  cudaPointerAttributes a;
+  if (cudaPointerGetAttributes(&a, h) != cudaSuccess) {
+    cudaGetLastError();
+    return nullptr;
+  }
+  return a.type == cudaMemoryTypeHost && a.devicePointer ? (double *)a.devicePointer : nullptr;
+}
+
 // A monitored run issued from C with no host wait per step: for each step,
 // the step's wind-stress row profile goes up, the step and advance run, and
 // the domain integrals of the new state come down into out3 + 3 s; one wait
-// at the end.  Host and device work overlap, so a host loop of small API
-// calls does not set the pace.
+// at the end.
+//
+// On the FP32 pair path each step is one kernel launch: the step kernel sums
+// the state it writes per block, and its extra block 0 converts the next
+// step's rows (read in place from pinned host memory, into the other half of
+// a double buffer) and finishes the previous step's integrals, written in
+// place into pinned host memory.  Other paths, and arrays that are not
+// pinned, take the general route: staged rows, the reduction kernel after the
+// advance, and copies.
 int swm_gpu_run_monitor(swm_gpu_ctx *c, int64_t itt0, int64_t nsteps, int stream_id, const double *rows1,
                         const double *rows2, double *out3) {
   SWM_REQUIRE(c && c->stage >= 5 && nsteps > 0 && out3, "swm_gpu_run_monitor: bad arguments");
   SWM_REQUIRE(!rows1 || (stream_id >= 0 && stream_id < (int)c->streams.size()),
               "swm_gpu_run_monitor: bad stream id");
   const size_t ny = (size_t)c->ny;
-  for (int64_t s = 0; s < nsteps; s++) {
+  const double *rows_dev = mapped_view(rows1);
+  double *out_dev = mapped_view(out3);
+  auto set_rows = [&](int64_t s) -> int {
+    if (!rows1) return SWM_GPU_OK;
+    return stream_rows(c, stream_id, rows1 + s * ny, rows2 ? rows2 + s * ny : nullptr,
+                       rows_dev ? rows_dev + s * ny : nullptr);
+  };
+  int64_t s = 0;
+  // the general route, until the pair path is ready (its first step prepares it)
+  for (; s < nsteps && !monitor_fast(c); s++) {
     const int64_t itt = itt0 + s + 1;
-    if (rows1) TRY(swm_gpu_set_stream_rows(c, stream_id, rows1 + s * ny, rows2 ? rows2 + s * ny : nullptr));
+    TRY(set_rows(s));
     TRY(swm_step_impl(c, itt));
     TRY(swm_advance_impl(c, itt));
-    int64_t ticket;
-    TRY(swm_gpu_integrals_async(c, out3 + 3 * s, &ticket));
+    double *where = nullptr;
+    TRY(integrals_to(c, out_dev ? out_dev + 3 * s : nullptr, &where));
+    if (!out_dev) SWM_CK(cudaMemcpyAsync(out3 + 3 * s, where, 3 * sizeof(double), cudaMemcpyDeviceToHost, c->stream));
+  }
+  if (s < nsteps) {
+    const int64_t s0 = s;
+    const bool rows_job = rows1 && rows_dev && monitor_rows_fast(c, stream_id);
+    MonitorBufs b;
+    TRY(monitor_buffers(c, nsteps, stream_id, rows_job, !out_dev, &b));
+    double *res = out_dev ? out_dev : b.res;  // step s's integrals at res + 3 s
+    if (rows_job) TRY(monitor_rows_first(c, rows_dev + s0 * ny, b.w[0]));
+    for (; s < nsteps; s++) {
+      const int64_t k = s - s0, itt = itt0 + s + 1;
+      MonitorStep m = {};
+      if (rows_job) {
+        m.w_now = b.w[k & 1];
+        m.w_merid = b.w_merid;
+        if (s + 1 < nsteps) {
+          m.next_rows = rows_dev + (s + 1) * ny;
+          m.next_w = b.w[(k + 1) & 1];
+        }
+      } else {
+        TRY(set_rows(s));
+      }
+      m.partial = b.partial[k & 1];
+      if (k > 0) {
+        m.prev_partial = b.partial[(k - 1) & 1];
+        m.prev_out = res + 3 * (s - 1);
+      }
+      c->mon = &m;
+      const int rc = swm_step_impl(c, itt);
+      const bool taken = c->mon == nullptr;
+      c->mon = nullptr;
+      TRY(rc);
+      SWM_REQUIRE(taken, "swm_gpu_run_monitor: the step did not run the monitored step kernel");
+      TRY(swm_advance_impl(c, itt));
+    }
+    const int last = (int)((nsteps - 1 - s0) & 1);
+    TRY(monitor_finish(c, b, b.partial[last], res + 3 * (nsteps - 1)));
+    if (rows_job) TRY(monitor_keep_rows(c, b, last));
+    if (!out_dev)
+      SWM_CK(cudaMemcpyAsync(out3 + 3 * s0, b.res + 3 * s0, 3 * sizeof(double) * (size_t)(nsteps - s0),
+                             cudaMemcpyDeviceToHost, c->stream));
   }
   SWM_CK(cudaStreamSynchronize(c->stream));
   return SWM_GPU_OK;

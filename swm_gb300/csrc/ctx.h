@@ -15,6 +15,8 @@
 
 namespace swm {
 
+struct MonitorStep;
+
 enum { GH = 0, GU = 1, GV = 2, GE = 3 };  // grid ids: H (corner), u, v, eta
 
 void set_error(const std::string &msg);
@@ -127,11 +129,14 @@ struct swm_gpu_ctx {
   FusedState *fused = nullptr;
   SorState *sor = nullptr;
   IntegralScratch *integrals = nullptr;
+  int integrals_shape[3] = {-1, 0, 0};  // k_integrals: kernel (0 FP64, 1 pair), threads, blocks
   Trc32State *trc32 = nullptr;      // tracers of the FP32 compensated path
   std::vector<swm::DiagAcc> diag;   // averaging buffers by slot
   std::vector<cudaEvent_t> async_ev;  // ring of events for swm_gpu_get_field_async
   int64_t async_next = 0;             // next ticket
   double *psi = nullptr, *psi_tmp = nullptr;  // streamfunction and its zonal sums
+  double *rows_buf = nullptr;       // 2 x Ny staging rows of swm_gpu_set_stream_rows
+  const swm::MonitorStep *mon = nullptr;  // the next FP32 pair step is a monitored step
   int64_t advances = 0;             // swm_gpu_advance calls (the rotation phase is advances mod 6)
   int march_rows = 0;                // rows per warp strip of the FP32 step kernel (0: not tuned yet)
   cudaGraphExec_t graph = nullptr;  // GRAPH_STEPS captured steps (swm_gpu_run)
@@ -163,6 +168,22 @@ int fused_step(swm_gpu_ctx *c, int64_t itt);
 int fused_sync_state(swm_gpu_ctx *c);    // FP32 pair state -> FP64 buffers
 int fused_load_state(swm_gpu_ctx *c);    // FP64 buffers -> FP32 pair state
 int fused_refresh_wind(swm_gpu_ctx *c, int id);  // stream id's record changed
+int stream_rows(swm_gpu_ctx *c, int id, const double *r1, const double *r2, const double *d1);
+int integrals_to(swm_gpu_ctx *c, double *dst, double **where);  // dst: device or host-mapped
+// swm_gpu_run_monitor on the FP32 pair path (one step kernel per step)
+struct MonitorBufs {
+  float *w[2];         // wind rows: the fused state's own, and the alternate
+  int w_merid;         // the rows are the meridional ones
+  double *partial[2];  // per-block sums of even and odd steps
+  int nb;              // strip blocks of one step
+  double *res;         // 3 x nsteps results when the caller's array is not mapped
+};
+bool monitor_fast(const swm_gpu_ctx *c);                 // the pair path is ready for it
+bool monitor_rows_fast(const swm_gpu_ctx *c, int sid);   // stream sid's rows are converted in the step kernel
+int monitor_buffers(swm_gpu_ctx *c, int64_t nsteps, int sid, bool rows, bool res, MonitorBufs *b);
+int monitor_rows_first(swm_gpu_ctx *c, const double *rows_dev, float *w);
+int monitor_finish(swm_gpu_ctx *c, const MonitorBufs &b, const double *partial, double *out);
+int monitor_keep_rows(swm_gpu_ctx *c, const MonitorBufs &b, int last);
 void fused_free(swm_gpu_ctx *c);
 void integrals_free(swm_gpu_ctx *c);
 // sor.cu

@@ -26,7 +26,7 @@ constexpr int ENS_PHASES = 6;  // lcm of the 2 levels and 3 increment slots
 struct EnsInt {
   const float *uh, *ul, *vh, *vl, *eh, *el;
   const int8_t *oU, *oV, *oE;
-  const double *cU, *cE;
+  const double *cU, *cV, *cE;
   int nx, ny;
   double A2dLdT, G;
 };
@@ -40,7 +40,7 @@ __global__ void k_ens_integrals(const EnsInt *__restrict__ d, double *__restrict
   const int n = q.nx * q.ny;
   for (int k = threadIdx.x; k < n; k += blockDim.x) {
     const int j = k / q.nx;
-    const double ae = q.A2dLdT * q.cE[j], au = q.A2dLdT * q.cU[j];
+    const double ae = q.A2dLdT * q.cE[j], au = q.A2dLdT * q.cU[j], av = q.A2dLdT * q.cV[j];
     const double ee = (double)q.eh[k] + (double)q.el[k];
     const double uu = (double)q.uh[k] + (double)q.ul[k];
     const double vv = (double)q.vh[k] + (double)q.vl[k];
@@ -49,7 +49,7 @@ __global__ void k_ens_integrals(const EnsInt *__restrict__ d, double *__restrict
       s1 += 0.5 * q.G * ee * ee * ae;
     }
     if (q.oU[k]) s2 += 0.5 * uu * uu * au;
-    if (q.oV[k]) s2 += 0.5 * vv * vv * ae;
+    if (q.oV[k]) s2 += 0.5 * vv * vv * av;
   }
   red[0][threadIdx.x] = s0;
   red[1][threadIdx.x] = s1;
@@ -324,7 +324,7 @@ int swm_gpu_ensemble_integrals(swm_gpu_ensemble *e, double *out) {
     EnsInt &q = d[i];
     q.uh = lv[0]; q.ul = lv[1]; q.vh = lv[2]; q.vl = lv[3]; q.eh = lv[4]; q.el = lv[5];
     q.oU = c->d_ocean[GU]; q.oV = c->d_ocean[GV]; q.oE = c->d_ocean[GE];
-    q.cU = c->d_cos[GU]; q.cE = c->d_cos[GE];
+    q.cU = c->d_cos[GU]; q.cV = c->d_cos[GV]; q.cE = c->d_cos[GE];
     q.nx = c->nx; q.ny = c->ny;
     q.A2dLdT = c->cfg.A * c->cfg.A * c->hg.dLambda * c->hg.dTheta;
     q.G = c->cfg.G;

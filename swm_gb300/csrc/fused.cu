@@ -745,10 +745,20 @@ void fused_pair_level(const swm_gpu_ctx *c, const float *out[6]) {
   out[0] = f->uh[a]; out[1] = f->ul[a]; out[2] = f->vh[a]; out[3] = f->vl[a]; out[4] = f->eh[a]; out[5] = f->el[a];
 }
 
-static void launch_fp32c(swm_gpu_ctx *c, int64_t itt) {
+int monitor_march(swm_gpu_ctx *c, P32 &p, const MonitorStep &m);
+
+// one step of the pair state; a monitored step (c->mon, taken here) runs the
+// step kernel with its monitoring jobs
+static int launch_fp32c(swm_gpu_ctx *c, int64_t itt) {
   P32 p;
   make_p32(c, itt, p);
+  if (c->mon) {
+    const MonitorStep *m = c->mon;
+    c->mon = nullptr;
+    return monitor_march(c, p, *m);
+  }
   march_launch(c, p);
+  return SWM_GPU_OK;
 }
 
 int fused_step(swm_gpu_ctx *c, int64_t itt) {
@@ -766,7 +776,7 @@ int fused_step(swm_gpu_ctx *c, int64_t itt) {
     p.Ge1 = d.Ge[0]; p.Ge2 = d.Ge[1]; p.Ge3 = d.Ge[2];
     launch_fused<double, false>(c, p);
   } else {
-    launch_fp32c(c, itt);
+    FTRY(launch_fp32c(c, itt));
     // the pair state advances here; the host-side advance only rotates the
     // FP64 level and ring indices
     f->n0 = 1 - f->n0;
@@ -796,112 +806,13 @@ void fused_free(swm_gpu_ctx *c) {
 // ---------------------------------------------------------------------------
 namespace swm {
 
-// (hi, lo) binary32 accumulator: TwoSum keeps the rounding error of every
-// addition, so a row sum carries about 46 bits; used for the pair state,
-// where FP64 arithmetic per point would tie the kernel to the FP64 pipe
-struct F2 {
-  float h = 0.f, l = 0.f;
-  __device__ __forceinline__ void add(float a, float b) {  // += a + b, |b| << |a|
-    const float s = h + a, bb = s - h;
-    l += ((h - (s - bb)) + (a - bb)) + b;
-    h = s;
-  }
-  __device__ __forceinline__ double value() const { return (double)h + (double)l; }
-};
-
-// the square of the pair (x, xl) as a pair: TwoProd of the high parts plus
-// the cross term (xl^2 is below the pair's precision)
-__device__ __forceinline__ void sq_pair(float x, float xl, float &p, float &e) {
-  p = x * x;
-  e = fmaf(x, x, -p) + 2.f * x * xl;
-}
-
-// Domain sums over ocean points, one grid row at a time: row sums of eta,
-// eta^2, u^2 and v^2 (FP64 state: in FP64; pair state: in (hi, lo) binary32
-// pairs), then times the row's cell area in FP64.  Per-block partials in a
-// fixed order (deterministic).
-template <typename T, bool COMP>
-__global__ void __launch_bounds__(256) k_integrals(int nx, int ny, const int8_t *oU, const int8_t *oV,
-                                                   const int8_t *oE, const double *area_u, const double *area_e,
-                                                   const T *u, const float *ul, const T *v, const float *vl,
-                                                   const T *e, const float *el, double G, double *partial) {
-  __shared__ double red[3][8];
-  double s0 = 0., s1 = 0., s2 = 0.;
-  for (int j = blockIdx.x; j < ny; j += gridDim.x) {
-    double r0 = 0., r1 = 0., ru = 0., rv = 0.;
-    const size_t row = (size_t)nx * j;
-    if (COMP) {
-      F2 a0, a1, au2, av2;
-      for (int i = threadIdx.x; i < nx; i += blockDim.x) {
-        const size_t k = row + i;
-        float p, q;
-        if (oE[k]) {
-          const float x = (float)e[k], xl = el[k];
-          a0.add(x, xl);
-          sq_pair(x, xl, p, q);
-          a1.add(p, q);
-        }
-        if (oU[k]) {
-          sq_pair((float)u[k], ul[k], p, q);
-          au2.add(p, q);
-        }
-        if (oV[k]) {
-          sq_pair((float)v[k], vl[k], p, q);
-          av2.add(p, q);
-        }
-      }
-      r0 = a0.value();
-      r1 = a1.value();
-      ru = au2.value();
-      rv = av2.value();
-    } else {
-      for (int i = threadIdx.x; i < nx; i += blockDim.x) {
-        const size_t k = row + i;
-        if (oE[k]) {
-          const double ee = (double)e[k];
-          r0 += ee;
-          r1 += ee * ee;
-        }
-        if (oU[k]) {
-          const double uu = (double)u[k];
-          ru += uu * uu;
-        }
-        if (oV[k]) {
-          const double vv = (double)v[k];
-          rv += vv * vv;
-        }
-      }
-    }
-    const double ae = area_e[j], au = area_u[j];
-    s0 += r0 * ae;
-    s1 += 0.5 * G * r1 * ae;
-    s2 += 0.5 * (ru * au + rv * ae);
-  }
-  for (int o = 16; o > 0; o >>= 1) {
-    s0 += __shfl_down_sync(0xffffffffu, s0, o);
-    s1 += __shfl_down_sync(0xffffffffu, s1, o);
-    s2 += __shfl_down_sync(0xffffffffu, s2, o);
-  }
-  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-  if (lane == 0) {
-    red[0][warp] = s0;
-    red[1][warp] = s1;
-    red[2][warp] = s2;
-  }
-  __syncthreads();
-  if (threadIdx.x < 3) {
-    double a = 0.;
-    for (int w = 0; w < (int)(blockDim.x >> 5); w++) a += red[threadIdx.x][w];
-    partial[(size_t)threadIdx.x * gridDim.x + blockIdx.x] = a;
-  }
-}
-
-// sum of the per-block partials (one block of 256 threads, fixed order)
-__global__ void k_integrals_final(const double *partial, int nb, double *out) {
-  __shared__ double red[3][8];
+// sum of the per-block partials, 3 x nb, by one block in a fixed order (the
+// result does not depend on which block runs it)
+__device__ __forceinline__ void integrals_final(const double *partial, int nb, double *out) {
+  __shared__ double red[3][32];
   double a[3] = {0., 0., 0.};
   for (int b = threadIdx.x; b < nb; b += blockDim.x)
-    for (int q = 0; q < 3; q++) a[q] += partial[(size_t)q * nb + b];
+    for (int q = 0; q < 3; q++) a[q] += __ldcg(partial + (size_t)q * nb + b);
   for (int o = 16; o > 0; o >>= 1)
     for (int q = 0; q < 3; q++) a[q] += __shfl_down_sync(0xffffffffu, a[q], o);
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
@@ -915,12 +826,236 @@ __global__ void k_integrals_final(const double *partial, int nb, double *out) {
   }
 }
 
+constexpr int INTEGRALS_IL = 4;             // columns per thread in one row chunk
+constexpr int INTEGRALS_MAX_THREADS = 512;  // threads per block
+constexpr int INTEGRALS_MAX_BLOCKS = 1024;
+
+// cell areas of one row: FP64, and as (hi, lo) binary32 pairs
+struct RowAreas {
+  const double *u, *v, *e;
+  const float2 *pu, *pv, *pe;
+};
+
+// one thread's share of one (row, chunk) item: IL columns, their masks and
+// the row's areas
+template <typename T>
+struct IntChunk {
+  int8_t mE[INTEGRALS_IL], mU[INTEGRALS_IL], mV[INTEGRALS_IL];
+  T xe[INTEGRALS_IL], xu[INTEGRALS_IL], xv[INTEGRALS_IL];
+  float le[INTEGRALS_IL], lu[INTEGRALS_IL], lv[INTEGRALS_IL];
+  float2 pu, pv, pe;
+  double du, dv, de;
+};
+
+// Domain sums over ocean points.  The work is a row-major list of (row,
+// chunk) items; a chunk is IL * blockDim.x columns, thread t holding columns
+// t, t + blockDim.x, ...  Blocks stride through the list.  A thread issues
+// all loads of an item (masks, values, areas; clamped in-row indices, no
+// branch) before it adds any of them, so an item costs one memory round trip
+// and the launch keeps a whole wave of items in flight.  Per item a thread sums eta, eta^2,
+// u^2, v^2 of its columns and adds them times the row's cell area to its
+// running totals: for the pair state all of it in (hi, lo) binary32 pairs
+// (about 46 bits; FP64 arithmetic per row would make the kernel FP64-pipe
+// bound on this part), for the FP64 state in FP64.  Each block leaves its
+// three sums in `partial`; the block that finishes last (counted in *done,
+// which it resets to 0) adds the partials in block order into out[3].  Every
+// order is fixed by the launch shape: the result is deterministic.
+template <typename T, bool COMP>
+__global__ void __launch_bounds__(INTEGRALS_MAX_THREADS)
+    k_integrals(int nx, int ny, const int8_t *oU, const int8_t *oV, const int8_t *oE, RowAreas ar,
+                const T *u, const float *ul, const T *v, const float *vl, const T *e, const float *el,
+                double G, double *partial, unsigned *done, double *out) {
+  constexpr int IL = INTEGRALS_IL;
+  __shared__ double red[4][INTEGRALS_MAX_THREADS / 32];
+  __shared__ bool last;
+  const int B = blockDim.x, W = IL * B;
+  const int C = (nx + W - 1) / W;  // chunks per row
+  const long long items = (long long)ny * C;
+  auto load = [&](IntChunk<T> &c, long long t) {
+    const int j = (int)(t / C);
+    const int i0 = (int)(t - (long long)j * C) * W + (int)threadIdx.x;
+    const size_t row = (size_t)nx * j;
+#pragma unroll
+    for (int q = 0; q < IL; q++) {
+      const int i = i0 + q * B;
+      const bool in = i < nx;
+      const size_t k = row + (in ? i : 0);
+      c.mE[q] = in ? oE[k] : (int8_t)0;
+      c.mU[q] = in ? oU[k] : (int8_t)0;
+      c.mV[q] = in ? oV[k] : (int8_t)0;
+      c.xe[q] = e[k];
+      c.xu[q] = u[k];
+      c.xv[q] = v[k];
+      if (COMP) {
+        c.le[q] = el[k];
+        c.lu[q] = ul[k];
+        c.lv[q] = vl[k];
+      }
+    }
+    if (COMP) {
+      c.pu = ar.pu[j];
+      c.pv = ar.pv[j];
+      c.pe = ar.pe[j];
+    } else {
+      c.du = ar.u[j];
+      c.dv = ar.v[j];
+      c.de = ar.e[j];
+    }
+  };
+  F2 P0, P1, PU, PV;                    // pair state totals
+  double D0 = 0., D1 = 0., DU = 0., DV = 0.;  // FP64 state totals
+  for (long long t = blockIdx.x; t < items; t += gridDim.x) {
+    IntChunk<T> cur;
+    load(cur, t);
+    if (COMP) {
+      // land points add the pair (0, 0), an exact identity of F2::add: a
+      // select instead of a branch, so every load stays ahead of its use
+      F2 a0, a1, au2, av2;
+#pragma unroll
+      for (int q = 0; q < IL; q++) {
+        float p, r;
+        const float x = cur.mE[q] ? (float)cur.xe[q] : 0.f, xl = cur.mE[q] ? cur.le[q] : 0.f;
+        a0.add(x, xl);
+        sq_pair(x, xl, p, r);
+        a1.add(p, r);
+        sq_pair(cur.mU[q] ? (float)cur.xu[q] : 0.f, cur.mU[q] ? cur.lu[q] : 0.f, p, r);
+        au2.add(p, r);
+        sq_pair(cur.mV[q] ? (float)cur.xv[q] : 0.f, cur.mV[q] ? cur.lv[q] : 0.f, p, r);
+        av2.add(p, r);
+      }
+      P0.add_prod(cur.pe, a0);
+      P1.add_prod(cur.pe, a1);
+      PU.add_prod(cur.pu, au2);
+      PV.add_prod(cur.pv, av2);
+    } else {
+      double r0 = 0., r1 = 0., ru = 0., rv = 0.;
+#pragma unroll
+      for (int q = 0; q < IL; q++) {
+        const double ee = cur.mE[q] ? (double)cur.xe[q] : 0.;
+        const double uu = cur.mU[q] ? (double)cur.xu[q] : 0.;
+        const double vv = cur.mV[q] ? (double)cur.xv[q] : 0.;
+        r0 += ee;
+        r1 += ee * ee;
+        ru += uu * uu;
+        rv += vv * vv;
+      }
+      D0 += r0 * cur.de;
+      D1 += r1 * cur.de;
+      DU += ru * cur.du;
+      DV += rv * cur.dv;
+    }
+  }
+  double s[4];
+  if (COMP) {
+    s[0] = P0.value();
+    s[1] = P1.value();
+    s[2] = PU.value();
+    s[3] = PV.value();
+  } else {
+    s[0] = D0;
+    s[1] = D1;
+    s[2] = DU;
+    s[3] = DV;
+  }
+  for (int o = 16; o > 0; o >>= 1)
+    for (int q = 0; q < 4; q++) s[q] += __shfl_down_sync(0xffffffffu, s[q], o);
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  if (lane == 0)
+    for (int q = 0; q < 4; q++) red[q][warp] = s[q];
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    double a[4] = {0., 0., 0., 0.};
+    for (int w = 0; w < B / 32; w++)
+      for (int q = 0; q < 4; q++) a[q] += red[q][w];
+    partial[blockIdx.x] = a[0];
+    partial[(size_t)gridDim.x + blockIdx.x] = 0.5 * G * a[1];
+    partial[2 * (size_t)gridDim.x + blockIdx.x] = 0.5 * (a[2] + a[3]);
+    __threadfence();
+    last = atomicAdd(done, 1u) == gridDim.x - 1;
+  }
+  __syncthreads();
+  if (!last) return;
+  __threadfence();
+  integrals_final(partial, gridDim.x, out);
+  if (threadIdx.x == 0) *done = 0u;
+}
+
+// launch shape of k_integrals for an nx x ny grid: the fewest threads (a
+// multiple of 32, at most INTEGRALS_MAX_THREADS) that cover a row in equal
+// chunks of IL columns each, and one wave of blocks (at most one per item)
+template <typename T, bool COMP>
+static int integrals_shape_t(int nx, int ny, int *threads, int *blocks) {
+  const int need = (nx + INTEGRALS_IL - 1) / INTEGRALS_IL;
+  const int chunks = (need + INTEGRALS_MAX_THREADS - 1) / INTEGRALS_MAX_THREADS;
+  const int thr = std::min(INTEGRALS_MAX_THREADS, ((need + chunks - 1) / chunks + 31) / 32 * 32);
+  const int W = INTEGRALS_IL * thr;
+  const long long items = (long long)ny * ((nx + W - 1) / W);
+  int dev = 0, sms = 0, per_sm = 0;
+  SWM_CK(cudaGetDevice(&dev));
+  SWM_CK(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
+  SWM_CK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_integrals<T, COMP>, thr, 0));
+  const long long wave = (long long)std::max(per_sm, 1) * std::max(sms, 1);
+  *threads = thr;
+  *blocks = (int)std::max(1LL, std::min(items, std::min<long long>(wave, INTEGRALS_MAX_BLOCKS)));
+  return SWM_GPU_OK;
+}
+
+// the state k_integrals reads (pair state of the fused paths once it is
+// ready, else the FP64 state) and its cached launch shape
+struct IntegralsInput {
+  bool comp;
+  const void *u, *v, *e;
+  const float *ul, *vl, *el;
+};
+
+static IntegralsInput integrals_input(swm_gpu_ctx *c) {
+  FusedState *f = c->fused;
+  if (f && f->ready && f->comp) {
+    const int a = f->n0;
+    return {true, f->uh[a], f->vh[a], f->eh[a], f->ul[a], f->vl[a], f->el[a]};
+  }
+  return {false, c->u[c->n0], c->v[c->n0], c->eta[c->n0], nullptr, nullptr, nullptr};
+}
+
+static int integrals_run(swm_gpu_ctx *c, const RowAreas &ar, double *partial, unsigned *done, double *out) {
+  const IntegralsInput in = integrals_input(c);
+  int *sh = c->integrals_shape;  // {kernel (0 FP64, 1 pair), threads, blocks}
+  if (sh[0] != (int)in.comp) {
+    const int rc = in.comp ? integrals_shape_t<float, true>(c->nx, c->ny, &sh[1], &sh[2])
+                           : integrals_shape_t<double, false>(c->nx, c->ny, &sh[1], &sh[2]);
+    if (rc != SWM_GPU_OK) return rc;
+    sh[0] = (int)in.comp;
+  }
+  const int8_t *oU = c->d_ocean[GU], *oV = c->d_ocean[GV], *oE = c->d_ocean[GE];
+  if (in.comp)
+    k_integrals<float, true><<<sh[2], sh[1], 0, c->stream>>>(
+        c->nx, c->ny, oU, oV, oE, ar, (const float *)in.u, in.ul, (const float *)in.v, in.vl,
+        (const float *)in.e, in.el, c->cfg.G, partial, done, out);
+  else
+    k_integrals<double, false><<<sh[2], sh[1], 0, c->stream>>>(
+        c->nx, c->ny, oU, oV, oE, ar, (const double *)in.u, nullptr, (const double *)in.v, nullptr,
+        (const double *)in.e, nullptr, c->cfg.G, partial, done, out);
+  c->launches++;
+  SWM_CK(cudaGetLastError());
+  return SWM_GPU_OK;
+}
+
+// (hi, lo) binary32 split of an FP64 area, the same on the host and the device
+__host__ __device__ inline float2 area_pair(double a) {
+  const float h = (float)a;
+  return make_float2(h, (float)(a - (double)h));
+}
+
 __global__ void k_expand_rows(const double *rows, double *field, int nx, int ny) {
   size_t k = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (k < (size_t)nx * ny) field[k] = rows[k / nx];
 }
 
+// the wind rows in binary32; waits for the previous kernel on the stream
+// (which may read dst) when launched as its programmatic dependent
 __global__ void k_rows_f32(const double *rows, float *dst, int ny) {
+  grid_dep_wait();
+  grid_dep_trigger();
   int j = blockIdx.x * blockDim.x + threadIdx.x;
   if (j < ny) dst[j] = (float)rows[j];
 }
@@ -930,19 +1065,31 @@ __global__ void k_rows_f32(const double *rows, float *dst, int ny) {
 // scratch of swm_gpu_integrals, owned by its context (allocated on the first
 // call, freed with the context)
 struct IntegralScratch {
-  double *area_u = nullptr, *area_e = nullptr, *partial = nullptr, *out = nullptr;
-  double *host = nullptr;  // pinned
-  int nb = 0;
+  double *area = nullptr;     // FP64 cell areas of the u, v, eta rows, 3 x Ny
+  float2 *pairs = nullptr;    // the same as (hi, lo) binary32 pairs, 3 x Ny
+  double *partial = nullptr;  // 3 x INTEGRALS_MAX_BLOCKS
+  double *out = nullptr;      // 3
+  unsigned *done = nullptr;   // blocks finished in the running reduction (0 between calls)
+  double *host = nullptr;     // pinned
+  double *mpartial = nullptr;  // per-block sums of monitored steps, two steps' worth
+  size_t mpartial_n = 0;
+  float *w_alt = nullptr;      // alternate wind rows of monitored steps (Ny)
+  double *res = nullptr;       // results of monitored steps for unmapped host arrays
+  size_t res_n = 0;
 };
 
 namespace swm {
 void integrals_free(swm_gpu_ctx *c) {
   IntegralScratch *S = c->integrals;
   if (!S) return;
-  cudaFree(S->area_u);
-  cudaFree(S->area_e);
+  cudaFree(S->area);
+  cudaFree(S->pairs);
   cudaFree(S->partial);
   cudaFree(S->out);
+  cudaFree(S->done);
+  cudaFree(S->mpartial);
+  cudaFree(S->w_alt);
+  cudaFree(S->res);
   cudaFreeHost(S->host);
   delete S;
   c->integrals = nullptr;
@@ -952,19 +1099,33 @@ void integrals_free(swm_gpu_ctx *c) {
 extern "C" {
 
 int swm_gpu_set_stream_rows(swm_gpu_ctx *c, int id, const double *r1, const double *r2) {
+  return swm::stream_rows(c, id, r1, r2, nullptr);
+}
+
+}  // extern "C"
+
+namespace swm {
+// rows r1 (and r2) of stream id into the stream's device record, or into the
+// fused path's row copy.  d1: r1 as the device may read it in place (r1 in
+// host-mapped pinned memory), or null; it is used where the rows go through
+// one small conversion kernel, which then reads the host array directly
+// instead of a staged copy.
+int stream_rows(swm_gpu_ctx *c, int id, const double *r1, const double *r2, const double *d1) {
   SWM_REQUIRE(c && id >= 0 && id < (int)c->streams.size() && r1, "swm_gpu_set_stream_rows: bad arguments");
-  static thread_local double *d_rows = nullptr;
-  static thread_local int d_rows_n = 0;
-  if (d_rows_n < 2 * c->ny) {
-    if (d_rows) cudaFree(d_rows);
-    SWM_CK(cudaMalloc((void **)&d_rows, 2 * (size_t)c->ny * 8));
-    d_rows_n = 2 * c->ny;
-  }
   const Stream &s = c->streams[id];
-  SWM_CK(cudaMemcpyAsync(d_rows, r1, c->ny * 8, cudaMemcpyHostToDevice, c->stream));
-  if (r2) SWM_CK(cudaMemcpyAsync(d_rows + c->ny, r2, c->ny * 8, cudaMemcpyHostToDevice, c->stream));
   FusedState *f = c->fused;
   bool fused_rows = f && f->ready && f->wind_rows && !s.is_const && s.type == SWM_FRC_WIND;
+  if (fused_rows && f->comp && d1) {
+    float *dst = (float *)(s.comp == SWM_CMP_ZONAL ? f->wx : f->wy);
+    SWM_CK(launch_programmatic(k_rows_f32, dim3((c->ny + 255) / 256), dim3(256), c->stream, d1, dst, c->ny));
+    c->launches++;
+    SWM_CK(cudaGetLastError());
+    return SWM_GPU_OK;
+  }
+  if (!c->rows_buf) SWM_CK(cudaMalloc((void **)&c->rows_buf, 2 * (size_t)c->ny * 8));
+  double *d_rows = c->rows_buf;
+  SWM_CK(cudaMemcpyAsync(d_rows, r1, c->ny * 8, cudaMemcpyHostToDevice, c->stream));
+  if (r2) SWM_CK(cudaMemcpyAsync(d_rows + c->ny, r2, c->ny * 8, cudaMemcpyHostToDevice, c->stream));
   if (fused_rows) {
     void *dst = s.comp == SWM_CMP_ZONAL ? f->wx : f->wy;
     if (f->comp) {
@@ -982,47 +1143,145 @@ int swm_gpu_set_stream_rows(swm_gpu_ctx *c, int id, const double *r1, const doub
   return SWM_GPU_OK;
 }
 
-}  // extern "C"
+}  // namespace swm
 
-// the three sums of the current state into the context's device scratch
-// S->out (allocated on the first call)
-static int integrals_launch(swm_gpu_ctx *c) {
+// the context's integrals scratch (allocated on the first call)
+static int integrals_scratch(swm_gpu_ctx *c, IntegralScratch **out) {
   IntegralScratch *S = c->integrals;
+  const size_t ny = (size_t)c->ny;
   if (!S) {
     S = c->integrals = new IntegralScratch();
     const HostGrid &g = c->hg;
-    std::vector<double> au(c->ny), ae(c->ny);
-    double A = c->cfg.A;
-    for (int j = 0; j < c->ny; j++) {
-      au[j] = A * A * g.cosl[GU][j] * g.dLambda * g.dTheta;
-      ae[j] = A * A * g.cosl[GE][j] * g.dLambda * g.dTheta;
-    }
-    S->nb = 2 * 152;
-    SWM_CK(cudaMalloc((void **)&S->area_u, c->ny * 8));
-    SWM_CK(cudaMalloc((void **)&S->area_e, c->ny * 8));
-    SWM_CK(cudaMalloc((void **)&S->partial, 3 * (size_t)S->nb * 8));
-    SWM_CK(cudaMalloc((void **)&S->out, 3 * 8));
-    SWM_CK(cudaMallocHost((void **)&S->host, 3 * 8));
-    SWM_CK(cudaMemcpy(S->area_u, au.data(), c->ny * 8, cudaMemcpyHostToDevice));
-    SWM_CK(cudaMemcpy(S->area_e, ae.data(), c->ny * 8, cudaMemcpyHostToDevice));
+    std::vector<double> area(3 * ny);
+    std::vector<float2> pairs(3 * ny);
+    const double A = c->cfg.A;
+    const int grids[3] = {GU, GV, GE};
+    for (int q = 0; q < 3; q++)
+      for (size_t j = 0; j < ny; j++) {
+        area[q * ny + j] = A * A * g.cosl[grids[q]][j] * g.dLambda * g.dTheta;
+        pairs[q * ny + j] = area_pair(area[q * ny + j]);
+      }
+    SWM_CK(cudaMalloc((void **)&S->area, 3 * ny * sizeof(double)));
+    SWM_CK(cudaMalloc((void **)&S->pairs, 3 * ny * sizeof(float2)));
+    SWM_CK(cudaMalloc((void **)&S->partial, 3 * (size_t)INTEGRALS_MAX_BLOCKS * sizeof(double)));
+    SWM_CK(cudaMalloc((void **)&S->out, 3 * sizeof(double)));
+    SWM_CK(cudaMalloc((void **)&S->done, sizeof(unsigned)));
+    SWM_CK(cudaMemset(S->done, 0, sizeof(unsigned)));
+    SWM_CK(cudaMallocHost((void **)&S->host, 3 * sizeof(double)));
+    SWM_CK(cudaMemcpy(S->area, area.data(), 3 * ny * sizeof(double), cudaMemcpyHostToDevice));
+    SWM_CK(cudaMemcpy(S->pairs, pairs.data(), 3 * ny * sizeof(float2), cudaMemcpyHostToDevice));
   }
-  FusedState *f = c->fused;
-  const int8_t *oU = c->d_ocean[GU], *oV = c->d_ocean[GV], *oE = c->d_ocean[GE];
-  if (f && f->ready && f->comp) {
-    int a = f->n0;
-    k_integrals<float, true><<<S->nb, 256, 0, c->stream>>>(c->nx, c->ny, oU, oV, oE, S->area_u, S->area_e,
-                                                            f->uh[a], f->ul[a], f->vh[a], f->vl[a], f->eh[a],
-                                                            f->el[a], c->cfg.G, S->partial);
-  } else {
-    k_integrals<double, false><<<S->nb, 256, 0, c->stream>>>(c->nx, c->ny, oU, oV, oE, S->area_u, S->area_e,
-                                                              c->u[c->n0], nullptr, c->v[c->n0], nullptr,
-                                                              c->eta[c->n0], nullptr, c->cfg.G, S->partial);
+  *out = S;
+  return SWM_GPU_OK;
+}
+
+// the three sums of the current state into the context's device scratch S->out
+static int integrals_launch(swm_gpu_ctx *c) {
+  IntegralScratch *S = nullptr;
+  FTRY(integrals_scratch(c, &S));
+  const size_t ny = (size_t)c->ny;
+  const RowAreas ar{S->area, S->area + ny, S->area + 2 * ny, S->pairs, S->pairs + ny, S->pairs + 2 * ny};
+  return integrals_run(c, ar, S->partial, S->done, S->out);
+}
+
+namespace swm {
+// the integrals of the current state into dst[3] (device or host-mapped
+// memory; null: the context's device result slot); *where gets the address
+// written
+int integrals_to(swm_gpu_ctx *c, double *dst, double **where) {
+  IntegralScratch *S = nullptr;
+  FTRY(integrals_scratch(c, &S));
+  const size_t ny = (size_t)c->ny;
+  if (!dst) dst = S->out;
+  if (where) *where = dst;
+  const RowAreas ar{S->area, S->area + ny, S->area + 2 * ny, S->pairs, S->pairs + ny, S->pairs + 2 * ny};
+  return integrals_run(c, ar, S->partial, S->done, dst);
+}
+
+// ---- swm_gpu_run_monitor on the FP32 pair path ----------------------------
+
+bool monitor_fast(const swm_gpu_ctx *c) {
+  const FusedState *f = c->fused;
+  return c->cfg.path == SWM_PATH_FUSED_FP32C && f && f->ready && f->comp && !c->cfg.frozen_flow;
+}
+
+bool monitor_rows_fast(const swm_gpu_ctx *c, int sid) {
+  const FusedState *f = c->fused;
+  if (!monitor_fast(c) || sid < 0 || sid >= (int)c->streams.size() || !f->wind_rows) return false;
+  const Stream &s = c->streams[sid];
+  return !s.is_const && s.type == SWM_FRC_WIND && (s.comp == SWM_CMP_ZONAL ? f->wx : f->wy) != nullptr;
+}
+
+static int grow(double **p, size_t *have, size_t need) {
+  if (*have >= need) return SWM_GPU_OK;
+  if (*p) SWM_CK(cudaFree(*p));
+  *p = nullptr;
+  *have = 0;
+  SWM_CK(cudaMalloc((void **)p, need * sizeof(double)));
+  *have = need;
+  return SWM_GPU_OK;
+}
+
+int monitor_buffers(swm_gpu_ctx *c, int64_t nsteps, int sid, bool rows, bool res, MonitorBufs *b) {
+  IntegralScratch *S = nullptr;
+  FTRY(integrals_scratch(c, &S));
+  const FusedState *f = c->fused;
+  const swm_gpu_config &cf = c->cfg;
+  const int mix = cf.lateral_mixing ? (cf.mixing_kind == SWM_MIX_BIHARMONIC ? 2 : 1) : 0;
+  b->nb = march_blocks(mix, c->nx, c->ny, c->march_rows ? c->march_rows : 16);
+  FTRY(grow(&S->mpartial, &S->mpartial_n, 2 * 4 * (size_t)b->nb));
+  b->partial[0] = S->mpartial;
+  b->partial[1] = S->mpartial + 4 * (size_t)b->nb;
+  b->w[0] = b->w[1] = nullptr;
+  b->w_merid = 0;
+  if (rows) {
+    if (!S->w_alt) SWM_CK(cudaMalloc((void **)&S->w_alt, (size_t)c->ny * sizeof(float)));
+    b->w_merid = c->streams[sid].comp != SWM_CMP_ZONAL;
+    b->w[0] = (float *)(b->w_merid ? f->wy : f->wx);
+    b->w[1] = S->w_alt;
   }
-  k_integrals_final<<<1, 256, 0, c->stream>>>(S->partial, S->nb, S->out);
-  c->launches += 2;
+  b->res = nullptr;
+  if (res) {
+    FTRY(grow(&S->res, &S->res_n, 3 * (size_t)nsteps));
+    b->res = S->res;
+  }
+  return SWM_GPU_OK;
+}
+
+// the first monitored step's wind rows, converted before its step kernel
+int monitor_rows_first(swm_gpu_ctx *c, const double *rows_dev, float *w) {
+  SWM_CK(launch_programmatic(k_rows_f32, dim3((c->ny + 255) / 256), dim3(256), c->stream, rows_dev, w, c->ny));
+  c->launches++;
+  return SWM_GPU_OK;
+}
+
+// the step kernel of a monitored step
+int monitor_march(swm_gpu_ctx *c, P32 &p, const MonitorStep &m) {
+  IntegralScratch *S = nullptr;
+  FTRY(integrals_scratch(c, &S));
+  if (m.w_now) (m.w_merid ? p.wy : p.wx) = m.w_now;
+  const MarchInteg mi{S->pairs, m.partial, m.prev_partial, m.prev_out, m.next_rows, m.next_w, c->cfg.G, c->ny, 1};
+  march_launch(c, p, &mi);
   SWM_CK(cudaGetLastError());
   return SWM_GPU_OK;
 }
+
+// the last monitored step's integrals
+int monitor_finish(swm_gpu_ctx *c, const MonitorBufs &b, const double *partial, double *out) {
+  march_integrals_final(partial, b.nb, c->cfg.G, out, c->stream);
+  c->launches++;
+  SWM_CK(cudaGetLastError());
+  return SWM_GPU_OK;
+}
+
+// after a monitored run whose last step read the alternate rows: the fused
+// state's own rows take them, so later steps see the last rows set
+int monitor_keep_rows(swm_gpu_ctx *c, const MonitorBufs &b, int last) {
+  if (b.w[0] && last == 1)
+    SWM_CK(cudaMemcpyAsync(b.w[0], b.w[1], (size_t)c->ny * sizeof(float), cudaMemcpyDeviceToDevice, c->stream));
+  return SWM_GPU_OK;
+}
+}  // namespace swm
 
 extern "C" {
 
@@ -1062,22 +1321,28 @@ int swm_gpu_integrals_async(swm_gpu_ctx *c, double *out3, int64_t *ticket) {
 // ---------------------------------------------------------------------------
 namespace swm {
 
-constexpr int NOALLOC_NB = 2 * 152;  // partial-sum blocks, as in swm_gpu_integrals
-constexpr size_t NOALLOC_DOUBLES = 2 * (size_t)SWM_NOALLOC_MAX_NY + 3 * NOALLOC_NB + 3;
-// area_u[MAX_NY] | area_e[MAX_NY] | partial[3 * NB] | out[3]  (138 KB per device)
+constexpr size_t NOALLOC_MAX_NY = SWM_NOALLOC_MAX_NY;
+// area[3 * MAX_NY] | pairs[3 * MAX_NY] (float2, one double slot each) |
+// partial[3 * INTEGRALS_MAX_BLOCKS] | out[3] | block counter (one 8-byte slot,
+// zero at load, left at zero by every call): 418 KB per device
+constexpr size_t NOALLOC_DOUBLES = 6 * NOALLOC_MAX_NY + 3 * (size_t)INTEGRALS_MAX_BLOCKS + 4;
 static __device__ __align__(256) double g_noalloc_scratch[NOALLOC_DOUBLES];
 // device address of the scratch per device ordinal, looked up on first use
 constexpr int NOALLOC_MAX_DEVICES = 64;
 static std::atomic<double *> g_noalloc_ptr[NOALLOC_MAX_DEVICES];
 
-// cell areas per row, A^2 cos(lat) dLambda dTheta, the product in the order
-// swm_gpu_integrals forms it on the host
-__global__ void k_area_rows(const double *cos_u, const double *cos_e, double A, double dL, double dT, int ny,
-                            double *area_u, double *area_e) {
-  int j = blockIdx.x * blockDim.x + threadIdx.x;
-  if (j < ny) {
-    area_u[j] = A * A * cos_u[j] * dL * dT;
-    area_e[j] = A * A * cos_e[j] * dL * dT;
+// cell areas per row, A^2 cos(lat) dLambda dTheta, for the u, v and eta rows,
+// the product in the order swm_gpu_integrals forms it on the host, and their
+// binary32 pairs
+__global__ void k_area_rows(const double *cos_u, const double *cos_v, const double *cos_e, double A, double dL,
+                            double dT, int ny, double *area, float2 *pairs) {
+  const int j = blockIdx.x * blockDim.x + threadIdx.x;
+  if (j >= ny) return;
+  const double *cs[3] = {cos_u, cos_v, cos_e};
+  for (int q = 0; q < 3; q++) {
+    const double a = A * A * cs[q][j] * dL * dT;
+    area[(size_t)q * ny + j] = a;
+    pairs[(size_t)q * ny + j] = area_pair(a);
   }
 }
 
@@ -1100,27 +1365,20 @@ extern "C" int swm_gpu_integrals_noalloc(swm_gpu_ctx *c, double *out3) {
     SWM_CK(cudaGetSymbolAddress((void **)&scr, g_noalloc_scratch));
     g_noalloc_ptr[dev].store(scr, std::memory_order_release);
   }
-  // every slot below is written before it is read, so nothing needs clearing
-  double *area_u = scr, *area_e = scr + SWM_NOALLOC_MAX_NY;
-  double *partial = scr + 2 * (size_t)SWM_NOALLOC_MAX_NY, *out = partial + 3 * NOALLOC_NB;
+  // every slot below but the counter is written before it is read; the
+  // counter starts at zero with the module and each reduction resets it
+  const size_t ny = (size_t)c->ny;
+  double *area = scr;
+  float2 *pairs = reinterpret_cast<float2 *>(scr + 3 * NOALLOC_MAX_NY);
+  double *partial = scr + 6 * NOALLOC_MAX_NY, *out = partial + 3 * (size_t)INTEGRALS_MAX_BLOCKS;
+  unsigned *done = reinterpret_cast<unsigned *>(out + 3);
   const HostGrid &g = c->hg;
-  k_area_rows<<<(c->ny + 127) / 128, 128, 0, c->stream>>>(c->d_cos[GU], c->d_cos[GE], c->cfg.A, g.dLambda,
-                                                          g.dTheta, c->ny, area_u, area_e);
-  FusedState *f = c->fused;
-  const int8_t *oU = c->d_ocean[GU], *oV = c->d_ocean[GV], *oE = c->d_ocean[GE];
-  if (f && f->ready && f->comp) {
-    int a = f->n0;
-    k_integrals<float, true><<<NOALLOC_NB, 256, 0, c->stream>>>(c->nx, c->ny, oU, oV, oE, area_u, area_e,
-                                                                f->uh[a], f->ul[a], f->vh[a], f->vl[a],
-                                                                f->eh[a], f->el[a], c->cfg.G, partial);
-  } else {
-    k_integrals<double, false><<<NOALLOC_NB, 256, 0, c->stream>>>(c->nx, c->ny, oU, oV, oE, area_u, area_e,
-                                                                  c->u[c->n0], nullptr, c->v[c->n0], nullptr,
-                                                                  c->eta[c->n0], nullptr, c->cfg.G, partial);
-  }
-  k_integrals_final<<<1, 256, 0, c->stream>>>(partial, NOALLOC_NB, out);
-  c->launches += 3;
+  k_area_rows<<<(c->ny + 127) / 128, 128, 0, c->stream>>>(c->d_cos[GU], c->d_cos[GV], c->d_cos[GE], c->cfg.A,
+                                                          g.dLambda, g.dTheta, c->ny, area, pairs);
+  c->launches++;
   SWM_CK(cudaGetLastError());
+  const RowAreas ar{area, area + ny, area + 2 * ny, pairs, pairs + ny, pairs + 2 * ny};
+  FTRY(integrals_run(c, ar, partial, done, out));
   SWM_CK(cudaMemcpyAsync(out3, out, 3 * sizeof(double), cudaMemcpyDeviceToHost, c->stream));
   SWM_CK(cudaStreamSynchronize(c->stream));
   return SWM_GPU_OK;

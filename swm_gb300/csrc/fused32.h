@@ -29,13 +29,104 @@ struct P32 {
   float *Gu3, *Gv3, *Ge3;
 };
 
+#ifdef __CUDACC__
+// (hi, lo) binary32 accumulator: TwoSum keeps the rounding error of every
+// addition, so a sum carries about 46 bits.  Used for domain sums of the
+// pair state, where FP64 arithmetic per point would tie a kernel to the
+// FP64 pipe.
+struct F2 {
+  float h = 0.f, l = 0.f;
+  __device__ __forceinline__ void add(float a, float b) {  // += a + b, |b| << |a|
+    const float s = h + a, bb = s - h;
+    l += ((h - (s - bb)) + (a - bb)) + b;
+    h = s;
+  }
+  // += (a.x + a.y) * (r.h + r.l): TwoProd of the high parts plus the cross
+  // terms (the low-low product is below the pair's precision)
+  __device__ __forceinline__ void add_prod(float2 a, const F2 &r) {
+    const float p = a.x * r.h;
+    add(p, fmaf(a.x, r.h, -p) + fmaf(a.x, r.l, a.y * r.h));
+  }
+  __device__ __forceinline__ double value() const { return (double)h + (double)l; }
+};
+
+// Programmatic dependent launch: a kernel launched with
+// cudaLaunchAttributeProgrammaticStreamSerialization may start before its
+// predecessor on the stream has finished; grid_dep_wait() returns once the
+// predecessor has completed and its writes are visible (at once for a kernel
+// launched the ordinary way).  grid_dep_trigger() lets the successor launch.
+__device__ __forceinline__ void grid_dep_wait() { asm volatile("griddepcontrol.wait;" ::: "memory"); }
+__device__ __forceinline__ void grid_dep_trigger() { asm volatile("griddepcontrol.launch_dependents;" ::: "memory"); }
+
+// the square of the pair (x, xl) as a pair: TwoProd of the high parts plus
+// the cross term (xl^2 is below the pair's precision)
+__device__ __forceinline__ void sq_pair(float x, float xl, float &p, float &e) {
+  p = x * x;
+  e = fmaf(x, x, -p) + 2.f * x * xl;
+}
+#endif
+
+// Monitored steps of the pair state (k_march<MIX, true>).  The strip blocks
+// (blockIdx.x >= 1) also sum the new state of their ocean points times the
+// cell areas: per block eta*area, eta^2*area, u^2*area_u, v^2*area_v into
+// partial[q * nb + b] (nb strip blocks).  Block 0 does the step's side jobs
+// while they run: it converts the next step's wind rows (host-mapped FP64)
+// into next_w, and it finishes the previous step's sums (prev_partial) into
+// prev_out[3] = {sum eta*area, 0.5 G sum eta^2*area, 0.5 (sum u^2*area_u +
+// sum v^2*area_v)}, in the order k_march_integrals_final uses.  prev_out may
+// be host-mapped memory.
+struct MarchInteg {
+  const float2 *area;  // (hi, lo) cell areas of the u, v, eta rows, 3 x ny
+  double *partial;
+  const double *prev_partial;  // null: nothing to finish
+  double *prev_out;
+  const double *next_rows;  // null: no rows to convert
+  float *next_w;
+  double G;
+  int ny;
+  int programmatic;  // launch as a programmatic dependent of the stream's previous kernel
+};
+
+// one monitored step as swm_gpu_run_monitor sets it up for the step kernel
+struct MonitorStep {
+  float *w_now;   // wind rows the step reads (null: the fused state's own)
+  int w_merid;    // w_now replaces the meridional rows (else the zonal)
+  double *partial;
+  const double *prev_partial;
+  double *prev_out;
+  const double *next_rows;
+  float *next_w;
+};
+
+// the integrals of one monitored step from its per-block sums (nb strip
+// blocks) into out[3]
+void march_integrals_final(const double *partial, int nb, double G, double *out, cudaStream_t st);
+
+// cudaLaunchKernelEx with programmatic stream serialisation (see grid_dep_wait)
+template <typename... KArgs, typename... Args>
+cudaError_t launch_programmatic(void (*kernel)(KArgs...), dim3 grid, dim3 block, cudaStream_t st, Args... args) {
+  cudaLaunchConfig_t cfg = {};
+  cfg.gridDim = grid;
+  cfg.blockDim = block;
+  cfg.dynamicSmemBytes = 0;
+  cfg.stream = st;
+  cudaLaunchAttribute at[1];
+  at[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+  at[0].val.programmaticStreamSerializationAllowed = 1;
+  cfg.attrs = at;
+  cfg.numAttrs = 1;
+  return cudaLaunchKernelEx(&cfg, kernel, args...);
+}
+// blocks of one k_march launch with S rows per strip
+int march_blocks(int mix, int nx, int ny, int S);
+
 // candidate rows per warp strip of the step kernel
 constexpr int MARCH_NROWS = 4;
 constexpr int MARCH_ROWS[MARCH_NROWS] = {8, 16, 24, 32};
 
 std::vector<double> fp32c_rows(const swm_gpu_ctx *c);
 void make_p32(const swm_gpu_ctx *c, int64_t itt, P32 &p);
-void march_launch(swm_gpu_ctx *c, const P32 &p);
+void march_launch(swm_gpu_ctx *c, const P32 &p, const MarchInteg *mi = nullptr);
 int march_tile_cols(int mix);          // columns a warp strip updates
 int march_rows_override();             // SWM_GB300_MARCH_S, 0 when unset
 std::vector<int> march_row_candidates(int mix, int nx, int ny);

@@ -31,6 +31,16 @@
 #ifndef MARCH_MINB
 #define MARCH_MINB 4
 #endif
+// integrals formed by the step kernel: 1 = (hi, lo) pair sums of exact
+// products; 0 = binary32 sums per lane (a lane holds at most S + 4 rows),
+// FP64 across lanes
+#ifndef MARCH_INTEG_PAIRS
+#define MARCH_INTEG_PAIRS 1
+#endif
+// 1: the row's cell areas are loaded at the start of the row update
+#ifndef MARCH_INTEG_HOIST
+#define MARCH_INTEG_HOIST 1
+#endif
 
 namespace swm {
 
@@ -67,9 +77,13 @@ __device__ __forceinline__ void comp_damp(float hi, float lo, float inc, float d
 }
 
 // One warp updates rows ry0 .. ry0+S-1 of strip bx (columns bx*TI ..
-// bx*TI+TI-1) of the basin p describes.
-template <int MIX>
-__device__ __forceinline__ void march_strip(const P32 &p, const int bx, const int ry0, const int lane, const int S) {
+// bx*TI+TI-1) of the basin p describes.  INTEG: each updating lane also adds
+// the new state of its ocean points, times the cell area of the point's row
+// (area: 3 x ny (hi, lo) pairs, u, v, eta rows), into acc[4]: eta, eta^2,
+// u^2, v^2.
+template <int MIX, bool INTEG = false>
+__device__ __forceinline__ void march_strip(const P32 &p, const int bx, const int ry0, const int lane, const int S,
+                                            const float2 *area = nullptr, F2 *acc = nullptr) {
   constexpr int H = MIX == 2 ? 2 : 1;
   constexpr int TI = 32 - 2 * H;
   const int nx = p.nx, ny = p.ny;
@@ -274,6 +288,14 @@ __device__ __forceinline__ void march_strip(const P32 &p, const int bx, const in
     if (upd) {
       const unsigned mm = m[2];
       float ge = 0.f, gu = 0.f, gv = 0.f;
+      // INTEG: the row's cell areas, loaded here so that their latency
+      // overlaps the tendencies
+      float2 aru, arv, are;
+      if (INTEG && MARCH_INTEG_HOIST) {
+        aru = area[o];
+        arv = area[ny + o];
+        are = area[2 * ny + o];
+      }
       if (XE(mm)) {
         float dmv = r1[Q_CV] * ((mvh[1] - mvh[2]) + (mvl[1] - mvl[2])) + r1[Q_DCV] * mvh[2];
         ge = -((muh2_r - muh[2]) + (mul2_r - mul[2])) * r2[Q_RE_DL] - dmv * r2[Q_RE_DT];
@@ -344,10 +366,46 @@ __device__ __forceinline__ void march_strip(const P32 &p, const int bx, const in
         if (nh < lim) { nh = lim; nlo = 0.f; }
       }
       p.eh1[ko] = nh; p.el1[ko] = nlo;
+      if (INTEG && !MARCH_INTEG_HOIST) {
+        aru = area[o];
+        arv = area[ny + o];
+        are = area[2 * ny + o];
+      }
+      F2 sq;
+      if (INTEG && XE(mm)) {
+        if (MARCH_INTEG_PAIRS) {
+          F2 x;
+          x.h = nh;
+          x.l = nlo;
+          acc[0].add_prod(are, x);
+          sq_pair(nh, nlo, sq.h, sq.l);
+          acc[1].add_prod(are, sq);
+        } else {
+          const float x = nh + nlo;
+          acc[0].h = fmaf(are.x, x, acc[0].h);
+          acc[1].h = fmaf(are.x, x * x, acc[1].h);
+        }
+      }
       comp_damp(uh[2], ul[2], incu, dpu, nh, nlo);
       p.uh1[ko] = nh; p.ul1[ko] = nlo;
+      if (INTEG && XU(mm)) {
+        if (MARCH_INTEG_PAIRS) {
+          sq_pair(nh, nlo, sq.h, sq.l);
+          acc[2].add_prod(aru, sq);
+        } else {
+          acc[2].h = fmaf(aru.x, nh * nh, acc[2].h);
+        }
+      }
       comp_damp(vh[2], vl[2], incv, dpv, nh, nlo);
       p.vh1[ko] = nh; p.vl1[ko] = nlo;
+      if (INTEG && XV(mm)) {
+        if (MARCH_INTEG_PAIRS) {
+          sq_pair(nh, nlo, sq.h, sq.l);
+          acc[3].add_prod(arv, sq);
+        } else {
+          acc[3].h = fmaf(arv.x, nh * nh, acc[3].h);
+        }
+      }
     }
 #undef XH
 #undef XU
@@ -402,14 +460,108 @@ __device__ __forceinline__ void march_strip(const P32 &p, const int bx, const in
   }
 }
 
+// End of a strip block of k_march<MIX, true>: each warp reduces its lanes'
+// pair sums (shuffle tree), then thread 0 adds the four warps in order in
+// FP64 and stores the block's sums as block b of nb.
+__device__ __forceinline__ void march_integrals_block(const MarchInteg &mi, F2 *acc, int b, int nb) {
+  __shared__ double red[4][4];
+  for (int o = 16; o > 0; o >>= 1)
+#pragma unroll
+    for (int q = 0; q < 4; q++) {
+      const float h = __shfl_down_sync(FULL, acc[q].h, o), l = __shfl_down_sync(FULL, acc[q].l, o);
+      acc[q].add(h, l);
+    }
+  const int warp = threadIdx.x >> 5;
+  if ((threadIdx.x & 31) == 0)
+#pragma unroll
+    for (int q = 0; q < 4; q++) red[q][warp] = acc[q].value();
+  __syncthreads();
+  if (threadIdx.x == 0)
+#pragma unroll
+    for (int q = 0; q < 4; q++) mi.partial[(size_t)q * nb + b] = ((red[q][0] + red[q][1]) + red[q][2]) + red[q][3];
+}
+
+// The three integrals from nb per-block sums, by one block of 128 threads:
+// thread t adds blocks t, t + 128, ... (BATCH loads at a time), then the
+// shuffle tree, then the four warps in order.
+__device__ __forceinline__ void integrals_from_blocks(const double *partial, int nb, double G, double *out) {
+  __shared__ double red[4][4];
+  constexpr int BATCH = 8;
+  double t[4] = {0., 0., 0., 0.};
+  for (int b0 = threadIdx.x; b0 < nb; b0 += BATCH * 128) {
+    double v[4][BATCH];
+#pragma unroll
+    for (int k = 0; k < BATCH; k++) {
+      const int b = b0 + k * 128;
+#pragma unroll
+      for (int q = 0; q < 4; q++) v[q][k] = b < nb ? partial[(size_t)q * nb + b] : 0.;
+    }
+#pragma unroll
+    for (int k = 0; k < BATCH; k++)
+#pragma unroll
+      for (int q = 0; q < 4; q++) t[q] += v[q][k];
+  }
+  for (int o = 16; o > 0; o >>= 1)
+#pragma unroll
+    for (int q = 0; q < 4; q++) t[q] += __shfl_down_sync(FULL, t[q], o);
+  const int warp = threadIdx.x >> 5;
+  if ((threadIdx.x & 31) == 0)
+#pragma unroll
+    for (int q = 0; q < 4; q++) red[q][warp] = t[q];
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    double a[4];
+#pragma unroll
+    for (int q = 0; q < 4; q++) a[q] = ((red[q][0] + red[q][1]) + red[q][2]) + red[q][3];
+    out[0] = a[0];
+    out[1] = 0.5 * G * a[1];
+    out[2] = 0.5 * (a[2] + a[3]);
+  }
+}
+
+// block 0 of a monitored step: the next step's wind rows, then the previous
+// step's integrals
+__device__ __forceinline__ void march_monitor_jobs(const MarchInteg &mi, int nb) {
+  if (mi.next_rows)
+    for (int j = threadIdx.x; j < mi.ny; j += blockDim.x) mi.next_w[j] = (float)mi.next_rows[j];
+  if (mi.prev_partial) integrals_from_blocks(mi.prev_partial, nb, mi.G, mi.prev_out);
+}
+
+// the last monitored step's integrals (launched after its step kernel, as its
+// programmatic dependent)
+__global__ void __launch_bounds__(128) k_march_integrals_final(const double *__restrict__ partial, int nb, double G,
+                                                                double *out) {
+  grid_dep_wait();
+  integrals_from_blocks(partial, nb, G, out);
+}
+
+void march_integrals_final(const double *partial, int nb, double G, double *out, cudaStream_t st) {
+  launch_programmatic(k_march_integrals_final, dim3(1), dim3(128), st, partial, nb, G, out);
+}
+
 // block b takes strip b % nstrips; its four warps take four consecutive row
-// groups of that strip (their look-ahead rows overlap and meet in L1)
-template <int MIX>
-__global__ void __launch_bounds__(128, MARCH_MINB) k_march(P32 p, int S, int nstrips) {
+// groups of that strip (their look-ahead rows overlap and meet in L1).
+// INTEG (a monitored step, MarchInteg): block 0 does the side jobs and the
+// strip blocks are blockIdx.x - 1; they sum the new state as well.
+template <int MIX, bool INTEG>
+__global__ void __launch_bounds__(128, MARCH_MINB) k_march(P32 p, int S, int nstrips, MarchInteg mi) {
   const int lane = threadIdx.x & 31;
-  const int ry0 = ((blockIdx.x / nstrips) * 4 + (threadIdx.x >> 5)) * S;
-  if (ry0 >= p.ny) return;  // whole warp leaves together
-  march_strip<MIX>(p, blockIdx.x % nstrips, ry0, lane, S);
+  int b = blockIdx.x;
+  if (INTEG) {
+    grid_dep_wait();
+    if (b == 0) {
+      march_monitor_jobs(mi, gridDim.x - 1);
+      return;
+    }
+    b -= 1;
+  }
+  const int ry0 = ((b / nstrips) * 4 + (threadIdx.x >> 5)) * S;
+  F2 acc[4];
+  if (ry0 < p.ny) march_strip<MIX, INTEG>(p, b % nstrips, ry0, lane, S, mi.area, acc);
+  if (INTEG) {
+    grid_dep_trigger();
+    march_integrals_block(mi, acc, b, gridDim.x - 1);
+  }
 }
 
 // Ensemble of basins in one persistent launch: every warp takes (member,
@@ -477,7 +629,7 @@ static int resident_blocks_of() {  // blocks of k_march resident on the whole GP
     int per_sm = 0, sms = 0, dev = 0;
     cudaGetDevice(&dev);
     cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_march<MIX>, 128, 0);
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_march<MIX, false>, 128, 0);
     b = sms * (per_sm > 0 ? per_sm : 1);
   }
   return b;
@@ -505,12 +657,28 @@ std::vector<int> march_row_candidates(int mix, int nx, int ny) {
   return c;
 }
 
-static void launch_any(const P32 &p, int S, cudaStream_t st) {
+int march_blocks(int mix, int nx, int ny, int S) {
+  const int nstrips = (nx + march_tile_cols(mix) - 1) / march_tile_cols(mix);
+  return nstrips * ((ny + 4 * S - 1) / (4 * S));
+}
+
+template <int MIX>
+static void launch_mix(const P32 &p, int S, int nstrips, unsigned blocks, cudaStream_t st, const MarchInteg *mi) {
+  if (!mi) {
+    k_march<MIX, false><<<blocks, 128, 0, st>>>(p, S, nstrips, MarchInteg{});
+    return;
+  }
+  // one more block for the side jobs
+  if (mi->programmatic) launch_programmatic(k_march<MIX, true>, dim3(blocks + 1), dim3(128), st, p, S, nstrips, *mi);
+  else k_march<MIX, true><<<blocks + 1, 128, 0, st>>>(p, S, nstrips, *mi);
+}
+
+static void launch_any(const P32 &p, int S, cudaStream_t st, const MarchInteg *mi = nullptr) {
   const int nstrips = (p.nx + march_tile_cols(p.mix) - 1) / march_tile_cols(p.mix);
-  const unsigned blocks = (unsigned)(nstrips * ((p.ny + 4 * S - 1) / (4 * S)));
-  if (p.mix == 2) k_march<2><<<blocks, 128, 0, st>>>(p, S, nstrips);
-  else if (p.mix == 1) k_march<1><<<blocks, 128, 0, st>>>(p, S, nstrips);
-  else k_march<0><<<blocks, 128, 0, st>>>(p, S, nstrips);
+  const unsigned blocks = (unsigned)march_blocks(p.mix, p.nx, p.ny, S);
+  if (p.mix == 2) launch_mix<2>(p, S, nstrips, blocks, st, mi);
+  else if (p.mix == 1) launch_mix<1>(p, S, nstrips, blocks, st, mi);
+  else launch_mix<0>(p, S, nstrips, blocks, st, mi);
 }
 
 int march_rows_override() {
@@ -520,8 +688,8 @@ int march_rows_override() {
   return s >= 4 && s <= 256 ? s : 0;
 }
 
-void march_launch(swm_gpu_ctx *c, const P32 &p) {
-  launch_any(p, c->march_rows ? c->march_rows : 16, c->stream);
+void march_launch(swm_gpu_ctx *c, const P32 &p, const MarchInteg *mi) {
+  launch_any(p, c->march_rows ? c->march_rows : 16, c->stream, mi);
   c->launches++;
 }
 

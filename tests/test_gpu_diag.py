@@ -110,27 +110,97 @@ def test_async_integrals_match_sync():
         assert np.array_equal(buf, r)
 
 
-def test_run_monitor_matches_step_by_step():
+@pytest.mark.parametrize('start', [0, 5])
+@pytest.mark.parametrize('pinned', [True, False])
+@pytest.mark.parametrize('path', ['fused_fp32c', 'plain_fp64'])
+def test_run_monitor_matches_step_by_step(path, pinned, start):
     """swm_gpu_run_monitor (per-step row uploads and integrals, no host wait
-    per step) gives the state and per-step integrals of the same steps made
-    one call at a time."""
+    per step) gives the state of the same steps made one call at a time, bit
+    for bit, and their integrals.  Pinned arrays are read and written in
+    place by the kernels, pageable ones through staged copies.  On the FP32
+    pair path the step kernel forms the integrals itself, in its own order:
+    1e-12 of the sum's scale; elsewhere (and for a first step that prepares
+    the pair path) they come from the same reduction as swm_gpu_integrals:
+    bit for bit.  The rows change every step, so a step that read another
+    step's rows would leave a different state."""
     import torch
     case = synthetic.double_gyre((40, 32), biharmonic=True, nsteps=60)
-    a, b = GpuModel('fused_fp32c'), GpuModel('fused_fp32c')
+    a, b = GpuModel(path), GpuModel(path)
     for g in (a, b):
         Driver(case, g).init(with_diag=False)
     ny, n = case['config']['ny'], 20
     prof = case['streams'][0]['rec1'][0][:, 0]
-    rows = torch.empty((n, ny), dtype=torch.float64).pin_memory().numpy()
+    if pinned:
+        rows = torch.empty((n, ny), dtype=torch.float64).pin_memory().numpy()
+        out = torch.empty((n, 3), dtype=torch.float64).pin_memory().numpy()
+    else:
+        rows, out = np.empty((n, ny)), np.empty((n, 3))
     rows[:] = prof[None, :] * (1.0 + 0.1 * np.arange(n))[:, None]
-    out = torch.empty((n, 3), dtype=torch.float64).pin_memory().numpy()
-    a.run(0, 5)
-    b.run(0, 5)
-    a.run_monitor(5, n, 0, rows, out)
+    if start:
+        a.run(0, start)
+        b.run(0, start)
+    a.run_monitor(start, n, 0, rows, out)
     for s in range(n):
         b.set_stream_rows(0, np.ascontiguousarray(rows[s]))
-        b.step(6 + s)
-        b.advance(6 + s)
-        assert np.array_equal(out[s], b.integrals()), s
+        b.step(start + 1 + s)
+        b.advance(start + 1 + s)
+        ref = b.integrals()
+        if path == 'fused_fp32c' and start + s > 0:
+            _, scale = _numpy_integrals(case, b)
+            assert np.all(np.abs(out[s] - ref) <= 1e-12 * scale), (s, out[s], ref)
+        else:
+            assert np.array_equal(out[s], ref), s
     for f in ('u', 'v', 'eta'):
         assert np.array_equal(a.field(f), b.field(f))
+
+
+def _numpy_integrals(case, g):
+    """FP64 numpy sums of the three integrals of g's current fields, with the
+    oracle's grid (cos of each point's latitude, ocean masks, dLambda,
+    dTheta), and the scale of each sum's rounding error (the volume sum
+    cancels: sum |eta| area)."""
+    o = OracleBackend()
+    Driver(case, o).init(with_diag=False)
+    dl, dt = o.scalars()
+    A, G = case['config']['A'], case['config']['G']
+    area = {k: (A * A * o.lat('cos_' + k) * dl * dt)[:, None] for k in ('u', 'v', 'eta')}
+    m = {k: o.ocean(k) == 1 for k in ('u', 'v', 'eta')}
+    u, v, e = g.field('u'), g.field('v'), g.field('eta')
+    vol = e * area['eta'] * m['eta']
+    want = np.array([vol.sum(), (0.5 * G * e * e * area['eta'] * m['eta']).sum(),
+                     (0.5 * u * u * area['u'] * m['u']).sum() + (0.5 * v * v * area['v'] * m['v']).sum()])
+    return want, np.array([np.abs(vol).sum(), want[1], want[2]])
+
+
+@pytest.mark.parametrize('path,cells', [('plain_fp64', (48, 40)), ('fused_fp64', (48, 40)),
+                                        ('fused_fp32c', (48, 40)), ('fused_fp32c', (2100, 10)),
+                                        ('plain_fp64', (2100, 10)), ('fused_fp32c', (1024, 24)),
+                                        ('fused_fp32c', (5, 300))])
+def test_integrals_against_numpy_sums(path, cells):
+    """swm_gpu_integrals against FP64 numpy sums of the fields the library
+    returns.  Rows of 2101 points take two chunks of the reduction; 6-point
+    rows leave most of a warp idle."""
+    case = synthetic.double_gyre(cells, biharmonic=True, nsteps=40)
+    g = GpuModel(path)
+    Driver(case, g).init(with_diag=False)
+    g.run(0, 30)
+    got = g.integrals()
+    want, scale = _numpy_integrals(case, g)
+    assert np.all(want[1:] > 0) and scale[0] > 0
+    tol = 1e-13 if path != 'fused_fp32c' else 1e-12
+    assert np.all(np.abs(got - want) <= tol * scale), (got, want, (got - want) / scale)
+
+
+@pytest.mark.parametrize('cells', [(48, 40), (300, 17)])
+def test_step_kernel_integrals_against_numpy_sums(cells):
+    """The integrals the FP32 step kernel forms of the state it writes
+    (swm_gpu_run_monitor) against FP64 numpy sums of that state."""
+    import torch
+    case = synthetic.double_gyre(cells, biharmonic=True, nsteps=40)
+    g = GpuModel('fused_fp32c')
+    Driver(case, g).init(with_diag=False)
+    g.run(0, 10)
+    out = torch.empty((3, 3), dtype=torch.float64).pin_memory().numpy()
+    g.run_monitor(10, 3, 0, None, out)
+    want, scale = _numpy_integrals(case, g)
+    assert np.all(np.abs(out[-1] - want) <= 1e-12 * scale), (out[-1], want, (out[-1] - want) / scale)
