@@ -165,8 +165,12 @@ int swm_gpu_run(swm_gpu_ctx *ctx, int64_t itt0, int64_t nsteps);
    a second component, may be NULL) of stream stream_id goes to the device
    as swm_gpu_set_stream_rows does (rows1 NULL: no upload); after it the
    three domain integrals of swm_gpu_integrals go to out3 + 3*s.  Returns
-   when the last copy has landed.  Inputs and outputs in pinned memory let
-   the copies overlap the steps. */
+   when the last result has landed; the arrays must stay untouched until
+   then.  On the FP32 pair path with pinned (mapped) arrays each step is one
+   kernel launch that reads its rows and writes its integrals in place; the
+   integrals are then summed inside the step kernel, in another order than
+   swm_gpu_integrals (agreement about 1e-13 relative).  Other paths and
+   arrays take staged copies and the reduction of swm_gpu_integrals. */
 int swm_gpu_run_monitor(swm_gpu_ctx *ctx, int64_t itt0, int64_t nsteps, int stream_id, const double *rows1,
                         const double *rows2, double *out3);
 
