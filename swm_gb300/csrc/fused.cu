@@ -343,6 +343,7 @@ struct FusedState {
   void *impl[3] = {}, *gsq[2] = {}, *F[3] = {}, *wx = nullptr, *wy = nullptr;
   void *rows32c = nullptr;
   uint16_t *mask16 = nullptr;
+  std::vector<uint16_t> m16h;  // host copy of mask16 (the step kernel's tiles are cut from it)
   void *dp[3] = {};
   double dp_s[3] = {0, 0, 0};
   bool impl_uniform = true, gsq_uniform = true, has_F = false, wind_rows = false;
@@ -501,6 +502,7 @@ int fused_prepare(swm_gpu_ctx *c) {
       }
     FTRY(dmalloc((void **)&f->mask16, n * 2));
     SWM_CK(cudaMemcpy(f->mask16, m16.data(), n * 2, cudaMemcpyHostToDevice));
+    f->m16h = std::move(m16);
     // implicit damping as the removed fraction dt*gamma/(1 + dt*gamma)
     for (int q = 0; q < 3; q++) f->dp_s[q] = (f->impl_s[q] - 1.) / f->impl_s[q];
     if (!f->impl_uniform)
@@ -527,7 +529,7 @@ int fused_prepare(swm_gpu_ctx *c) {
     // rewrites again)
     P32 p;
     make_p32(c, 3, p);
-    FTRY(march_autotune(c, p));
+    FTRY(march_autotune(c, p, f->m16h.data()));
   }
   return SWM_GPU_OK;
 }
@@ -747,6 +749,14 @@ void fused_pair_level(const swm_gpu_ctx *c, const float *out[6]) {
 
 int monitor_march(swm_gpu_ctx *c, P32 &p, const MonitorStep &m);
 
+// the step kernel's tiles (cut with S rows per warp now if the autotuner has
+// not run: contexts the ensemble prepares)
+static int march_grid(swm_gpu_ctx *c, const P32 &p, MarchGrid *g) {
+  if (!c->march_tiles) FTRY(march_default_tiles(c, p, c->fused->m16h.data(), c->march_rows ? c->march_rows : 16));
+  *g = MarchGrid{c->march_tiles, c->march_blocks};
+  return SWM_GPU_OK;
+}
+
 // one step of the pair state; a monitored step (c->mon, taken here) runs the
 // step kernel with its monitoring jobs
 static int launch_fp32c(swm_gpu_ctx *c, int64_t itt) {
@@ -757,7 +767,9 @@ static int launch_fp32c(swm_gpu_ctx *c, int64_t itt) {
     c->mon = nullptr;
     return monitor_march(c, p, *m);
   }
-  march_launch(c, p);
+  MarchGrid g;
+  FTRY(march_grid(c, p, &g));
+  march_launch(c, p, g);
   return SWM_GPU_OK;
 }
 
@@ -1226,9 +1238,11 @@ int monitor_buffers(swm_gpu_ctx *c, int64_t nsteps, int sid, bool rows, bool res
   IntegralScratch *S = nullptr;
   FTRY(integrals_scratch(c, &S));
   const FusedState *f = c->fused;
-  const swm_gpu_config &cf = c->cfg;
-  const int mix = cf.lateral_mixing ? (cf.mixing_kind == SWM_MIX_BIHARMONIC ? 2 : 1) : 0;
-  b->nb = march_blocks(mix, c->nx, c->ny, c->march_rows ? c->march_rows : 16);
+  P32 p;
+  make_p32(c, 3, p);
+  MarchGrid g;
+  FTRY(march_grid(c, p, &g));
+  b->nb = g.blocks;
   FTRY(grow(&S->mpartial, &S->mpartial_n, 2 * 4 * (size_t)b->nb));
   b->partial[0] = S->mpartial;
   b->partial[1] = S->mpartial + 4 * (size_t)b->nb;
@@ -1261,7 +1275,9 @@ int monitor_march(swm_gpu_ctx *c, P32 &p, const MonitorStep &m) {
   FTRY(integrals_scratch(c, &S));
   if (m.w_now) (m.w_merid ? p.wy : p.wx) = m.w_now;
   const MarchInteg mi{S->pairs, m.partial, m.prev_partial, m.prev_out, m.next_rows, m.next_w, c->cfg.G, c->ny, 1};
-  march_launch(c, p, &mi);
+  MarchGrid g;
+  FTRY(march_grid(c, p, &g));
+  march_launch(c, p, g, &mi);
   SWM_CK(cudaGetLastError());
   return SWM_GPU_OK;
 }

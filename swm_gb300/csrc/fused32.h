@@ -117,8 +117,13 @@ cudaError_t launch_programmatic(void (*kernel)(KArgs...), dim3 grid, dim3 block,
   cfg.numAttrs = 1;
   return cudaLaunchKernelEx(&cfg, kernel, args...);
 }
-// blocks of one k_march launch with S rows per strip
-int march_blocks(int mix, int nx, int ny, int S);
+// the step kernel's tiles (device) and blocks
+struct MarchGrid {
+  const int2 *tiles;
+  int blocks;
+};
+std::vector<int2> march_tiles(int mix, int nx, int ny, const uint16_t *m16, double S, double slow);
+int march_default_tiles(swm_gpu_ctx *c, const P32 &p, const uint16_t *m16, int S);
 
 // candidate rows per warp strip of the step kernel
 constexpr int MARCH_NROWS = 4;
@@ -126,13 +131,12 @@ constexpr int MARCH_ROWS[MARCH_NROWS] = {8, 16, 24, 32};
 
 std::vector<double> fp32c_rows(const swm_gpu_ctx *c);
 void make_p32(const swm_gpu_ctx *c, int64_t itt, P32 &p);
-void march_launch(swm_gpu_ctx *c, const P32 &p, const MarchInteg *mi = nullptr);
+void march_launch(swm_gpu_ctx *c, const P32 &p, const MarchGrid &g, const MarchInteg *mi = nullptr);
 int march_tile_cols(int mix);          // columns a warp strip updates
 int march_rows_override();             // SWM_GB300_MARCH_S, 0 when unset
-std::vector<int> march_row_candidates(int mix, int nx, int ny);
 int march_pick_rows(cudaStream_t st, int reps, const std::vector<int> &cands, const std::function<void(int)> &launch,
                     int *best);
-int march_autotune(swm_gpu_ctx *c, const P32 &p);
+int march_autotune(swm_gpu_ctx *c, const P32 &p, const uint16_t *m16);
 void fused_indices(const swm_gpu_ctx *c, int *n0, int *g0);
 void fused_set_indices(swm_gpu_ctx *c, int n0, int g0);
 void fused_pair_level(const swm_gpu_ctx *c, const float *out[6]);

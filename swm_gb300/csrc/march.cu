@@ -539,12 +539,13 @@ void march_integrals_final(const double *partial, int nb, double G, double *out,
   launch_programmatic(k_march_integrals_final, dim3(1), dim3(128), st, partial, nb, G, out);
 }
 
-// block b takes strip b % nstrips; its four warps take four consecutive row
-// groups of that strip (their look-ahead rows overlap and meet in L1).
+// Warp w of block b takes tile 4 b + w of `tiles`: {strip, first row << 8 |
+// rows} (rows 0: nothing to do).  A block's four tiles are consecutive row
+// groups of one strip, so their look-ahead rows overlap and meet in L1.
 // INTEG (a monitored step, MarchInteg): block 0 does the side jobs and the
 // strip blocks are blockIdx.x - 1; they sum the new state as well.
 template <int MIX, bool INTEG>
-__global__ void __launch_bounds__(128, MARCH_MINB) k_march(P32 p, int S, int nstrips, MarchInteg mi) {
+__global__ void __launch_bounds__(128, MARCH_MINB) k_march(P32 p, const int2 *__restrict__ tiles, MarchInteg mi) {
   const int lane = threadIdx.x & 31;
   int b = blockIdx.x;
   if (INTEG) {
@@ -555,9 +556,10 @@ __global__ void __launch_bounds__(128, MARCH_MINB) k_march(P32 p, int S, int nst
     }
     b -= 1;
   }
-  const int ry0 = ((b / nstrips) * 4 + (threadIdx.x >> 5)) * S;
+  const int2 t = tiles[4 * b + (threadIdx.x >> 5)];
+  const int S = t.y & 255;
   F2 acc[4];
-  if (ry0 < p.ny) march_strip<MIX, INTEG>(p, b % nstrips, ry0, lane, S, mi.area, acc);
+  if (S > 0) march_strip<MIX, INTEG>(p, t.x, t.y >> 8, lane, S, mi.area, acc);
   if (INTEG) {
     grid_dep_trigger();
     march_integrals_block(mi, acc, b, gridDim.x - 1);
@@ -622,75 +624,121 @@ std::vector<double> fp32c_rows(const swm_gpu_ctx *c) {
 
 int march_tile_cols(int mix) { return 32 - 2 * (mix == 2 ? 2 : 1); }
 
-template <int MIX>
-static int resident_blocks_of() {  // blocks of k_march resident on the whole GPU at once
-  static int b = 0;
-  if (!b) {
-    int per_sm = 0, sms = 0, dev = 0;
-    cudaGetDevice(&dev);
-    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_march<MIX, false>, 128, 0);
-    b = sms * (per_sm > 0 ? per_sm : 1);
+// ---- tiles of the step kernel ---------------------------------------------
+//
+// A warp's time grows with its rows, and a row whose 4-row window holds a
+// land point (every row of a strip that contains a coast) takes the masked
+// body, about 1.3 times the all-ocean one.  With equal rows per warp the
+// strips along a coast finish last and set the kernel's duration.  So each
+// strip is cut into row groups of equal estimated cost: a body iteration
+// counts 1 when the kernel's vote will pick the all-ocean body (the same
+// test on the same mask words) and `slow` otherwise; a group with k rows runs
+// the iterations of rows ry0 - 1 .. ry0 + k + 1 (the look-ahead rows), and
+// a group takes rows while it stays within the cost of S all-ocean rows.
+// per strip and row: does the kernel's vote pick the all-ocean body there
+std::vector<uint8_t> march_fast_rows(int mix, int nx, int ny, const uint16_t *m16) {
+  const int H = mix == 2 ? 2 : 1, TI = march_tile_cols(mix);
+  const int nstrips = (nx + TI - 1) / TI;
+  auto wrap = [](int g, int n) { return ((g % n) + n) % n; };
+  std::vector<uint8_t> fast((size_t)nstrips * ny), ocean(ny);
+  for (int s = 0; s < nstrips; s++) {
+    for (int j = 0; j < ny; j++) {
+      bool all = true;
+      for (int lane = 0; lane < 32 && all; lane++) {
+        const int gi = wrap(s * TI - H + lane, nx);
+        all = (m16[gi + (size_t)nx * j] & 0xFFFu) == 0xFFFu;
+      }
+      ocean[j] = all;
+    }
+    for (int j = 0; j < ny; j++)
+      fast[(size_t)s * ny + j] = ocean[j] && ocean[wrap(j - 1, ny)] && ocean[wrap(j - 2, ny)] && ocean[wrap(j - 3, ny)];
   }
-  return b;
+  return fast;
 }
 
-static int resident_blocks(int mix) {
-  return mix == 2 ? resident_blocks_of<2>() : (mix == 1 ? resident_blocks_of<1>() : resident_blocks_of<0>());
-}
-
-// Candidate rows per warp strip: the fixed MARCH_ROWS and the lengths that
-// make the grid exactly one, two or three waves of resident blocks (a grid
-// slightly over a whole number of waves costs a whole extra wave).
-std::vector<int> march_row_candidates(int mix, int nx, int ny) {
-  std::vector<int> c(MARCH_ROWS, MARCH_ROWS + MARCH_NROWS);
-  const int nstrips = (nx + march_tile_cols(mix) - 1) / march_tile_cols(mix);
-  const int rb = resident_blocks(mix);
-  for (int waves = 1; waves <= 3; waves++) {
-    const int per_strip = waves * rb / nstrips;  // blocks of 4 row groups per strip
-    if (per_strip < 1) continue;
-    const int S = (ny + 4 * per_strip - 1) / (4 * per_strip);
-    if (S >= 4 && S <= 256) c.push_back(S);
+std::vector<int2> march_tiles_cut(const std::vector<uint8_t> &fast, int ny, double S, double slow) {
+  const int nstrips = (int)(fast.size() / ny);
+  auto wrap = [ny](int g) { return ((g % ny) + ny) % ny; };
+  const double target = S + 3.0;
+  std::vector<int2> tiles;
+  for (int s = 0; s < nstrips; s++) {
+    const uint8_t *f = &fast[(size_t)s * ny];
+    auto cost = [&](int j) { return f[wrap(j)] ? 1.0 : slow; };
+    for (int ry0 = 0; ry0 < ny;) {
+      // iterations of k rows: ry0 - 1 .. min(ry0 + k, ny) + 1
+      double c = cost(ry0 - 1) + cost(ry0) + cost(ry0 + 1) + cost(ry0 + 2);
+      int k = 1;
+      while (k < 255 && ry0 + k < ny) {
+        const double next = c + cost(ry0 + k + 2);
+        if (next > target) break;
+        c = next;
+        k++;
+      }
+      tiles.push_back(make_int2(s, (ry0 << 8) | k));
+      ry0 += k;
+    }
   }
-  std::sort(c.begin(), c.end());
-  c.erase(std::unique(c.begin(), c.end()), c.end());
-  return c;
+  // the groups strip after strip, four to a block (a block may take the end
+  // of one strip and the start of the next); idle tiles pad the last block
+  while (tiles.size() % 4) tiles.push_back(make_int2(0, 0));
+  return tiles;
 }
 
-int march_blocks(int mix, int nx, int ny, int S) {
-  const int nstrips = (nx + march_tile_cols(mix) - 1) / march_tile_cols(mix);
-  return nstrips * ((ny + 4 * S - 1) / (4 * S));
+std::vector<int2> march_tiles(int mix, int nx, int ny, const uint16_t *m16, double S, double slow) {
+  return march_tiles_cut(march_fast_rows(mix, nx, ny, m16), ny, S, slow);
 }
 
 template <int MIX>
-static void launch_mix(const P32 &p, int S, int nstrips, unsigned blocks, cudaStream_t st, const MarchInteg *mi) {
+static void launch_mix(const P32 &p, const MarchGrid &g, cudaStream_t st, const MarchInteg *mi) {
   if (!mi) {
-    k_march<MIX, false><<<blocks, 128, 0, st>>>(p, S, nstrips, MarchInteg{});
+    k_march<MIX, false><<<g.blocks, 128, 0, st>>>(p, g.tiles, MarchInteg{});
     return;
   }
   // one more block for the side jobs
-  if (mi->programmatic) launch_programmatic(k_march<MIX, true>, dim3(blocks + 1), dim3(128), st, p, S, nstrips, *mi);
-  else k_march<MIX, true><<<blocks + 1, 128, 0, st>>>(p, S, nstrips, *mi);
+  if (mi->programmatic) launch_programmatic(k_march<MIX, true>, dim3(g.blocks + 1), dim3(128), st, p, g.tiles, *mi);
+  else k_march<MIX, true><<<g.blocks + 1, 128, 0, st>>>(p, g.tiles, *mi);
 }
 
-static void launch_any(const P32 &p, int S, cudaStream_t st, const MarchInteg *mi = nullptr) {
-  const int nstrips = (p.nx + march_tile_cols(p.mix) - 1) / march_tile_cols(p.mix);
-  const unsigned blocks = (unsigned)march_blocks(p.mix, p.nx, p.ny, S);
-  if (p.mix == 2) launch_mix<2>(p, S, nstrips, blocks, st, mi);
-  else if (p.mix == 1) launch_mix<1>(p, S, nstrips, blocks, st, mi);
-  else launch_mix<0>(p, S, nstrips, blocks, st, mi);
+static void launch_any(const P32 &p, const MarchGrid &g, cudaStream_t st, const MarchInteg *mi = nullptr) {
+  if (p.mix == 2) launch_mix<2>(p, g, st, mi);
+  else if (p.mix == 1) launch_mix<1>(p, g, st, mi);
+  else launch_mix<0>(p, g, st, mi);
 }
 
 int march_rows_override() {
   const char *e = getenv("SWM_GB300_MARCH_S");
   if (!e) return 0;
   int s = atoi(e);
-  return s >= 4 && s <= 256 ? s : 0;
+  return s >= 4 && s <= 250 ? s : 0;
 }
 
-void march_launch(swm_gpu_ctx *c, const P32 &p, const MarchInteg *mi) {
-  launch_any(p, c->march_rows ? c->march_rows : 16, c->stream, mi);
+// SWM_GB300_MARCH_SLOW: the masked-row cost factor, 0 when unset
+static double march_slow_override() {
+  const char *e = getenv("SWM_GB300_MARCH_SLOW");
+  if (!e) return 0.;
+  double v = atof(e);
+  return v >= 1. && v <= 4. ? v : 0.;
+}
+
+void march_launch(swm_gpu_ctx *c, const P32 &p, const MarchGrid &g, const MarchInteg *mi) {
+  launch_any(p, g, c->stream, mi);
   c->launches++;
+}
+
+static int upload_tiles(swm_gpu_ctx *c, const std::vector<int2> &t) {
+  if (c->march_tiles) SWM_CK(cudaFree(c->march_tiles));
+  c->march_tiles = nullptr;
+  c->march_blocks = 0;
+  SWM_CK(cudaMalloc((void **)&c->march_tiles, t.size() * sizeof(int2)));
+  SWM_CK(cudaMemcpy(c->march_tiles, t.data(), t.size() * sizeof(int2), cudaMemcpyHostToDevice));
+  c->march_blocks = (int)(t.size() / 4);
+  return SWM_GPU_OK;
+}
+
+// tiles of S rows per warp, without tuning
+int march_default_tiles(swm_gpu_ctx *c, const P32 &p, const uint16_t *m16, int S) {
+  const double slow = march_slow_override();
+  return upload_tiles(c, march_tiles(p.mix, p.nx, p.ny, m16, S, slow > 0. ? slow : 1.));
 }
 
 // Mean time of `reps` launches per candidate; the step reads level n0 and
@@ -707,8 +755,9 @@ int march_pick_rows(cudaStream_t st, int reps, const std::vector<int> &cands, co
   SWM_CK(cudaEventCreate(&a));
   SWM_CK(cudaEventCreate(&b));
   float tbest = 1e30f;
-  *best = 16;
-  for (int r : cands) {
+  *best = cands.empty() ? 16 : cands[0];
+  for (size_t i = 0; i < cands.size(); i++) {
+    const int r = cands[i];
     launch(r);  // warm-up
     SWM_CK(cudaEventRecord(a, st));
     for (int k = 0; k < reps; k++) launch(r);
@@ -727,13 +776,87 @@ int march_pick_rows(cudaStream_t st, int reps, const std::vector<int> &cands, co
   return SWM_GPU_OK;
 }
 
-int march_autotune(swm_gpu_ctx *c, const P32 &p) {
-  int s = 16;
-  int rc = march_pick_rows(c->stream, 5, march_row_candidates(p.mix, p.nx, p.ny),
-                           [&](int r) { launch_any(p, r, c->stream); }, &s);
-  if (rc != SWM_GPU_OK) return rc;
-  c->march_rows = s;
-  return SWM_GPU_OK;
+template <int MIX>
+static int resident_blocks_of() {  // blocks of k_march resident on the whole GPU at once
+  static int b = 0;
+  if (!b) {
+    int per_sm = 0, sms = 0, dev = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_march<MIX, false>, 128, 0);
+    b = sms * (per_sm > 0 ? per_sm : 1);
+  }
+  return b;
+}
+
+static int resident_blocks(int mix) {
+  return mix == 2 ? resident_blocks_of<2>() : (mix == 1 ? resident_blocks_of<1>() : resident_blocks_of<0>());
+}
+
+// Tiles of the step kernel, by timing the step on this basin.  A kernel is
+// fastest when all its warps are resident at once (one wave) and finish
+// together, with as few rows each as that allows.  So for each masked-row
+// cost in MARCH_TUNE_SLOW the candidate is the fewest rows per warp (in
+// steps of 1/4) whose tiles fit one wave, and the same for two waves; plus
+// equal groups of 16 rows.
+constexpr double MARCH_TUNE_SLOW[] = {1.0, 1.2, 1.3, 1.4, 1.5, 1.7};
+
+int march_autotune(swm_gpu_ctx *c, const P32 &p, const uint16_t *m16) {
+  std::vector<std::vector<int2>> tabs;
+  std::vector<std::pair<double, double>> params;
+  const int s_env = march_rows_override();
+  const double w_env = march_slow_override();
+  const std::vector<uint8_t> fast = march_fast_rows(p.mix, p.nx, p.ny, m16);
+  auto add = [&](double S, double w) {
+    for (auto &q : params)
+      if (q.first == S && q.second == w) return;
+    params.push_back({S, w});
+    tabs.push_back(march_tiles_cut(fast, p.ny, S, w));
+  };
+  if (s_env) {
+    add(s_env, w_env > 0. ? w_env : 1.);
+  } else {
+    const int R = resident_blocks(p.mix);
+    add(16., 1.);
+    for (double w : MARCH_TUNE_SLOW) {
+      if (w_env > 0. && w != MARCH_TUNE_SLOW[0]) continue;
+      const double wu = w_env > 0. ? w_env : w;
+      for (int waves = 1; waves <= 2; waves++) {
+        // the fewest rows (quarters) that fit: the block count falls as S grows
+        int lo = 16, hi = 4 * 250;  // S = q / 4
+        if (march_tiles_cut(fast, p.ny, hi / 4., wu).size() / 4 > (size_t)(waves * R)) continue;
+        while (lo < hi) {
+          const int mid = (lo + hi) / 2;
+          if (march_tiles_cut(fast, p.ny, mid / 4., wu).size() / 4 > (size_t)(waves * R)) lo = mid + 1;
+          else hi = mid;
+        }
+        add(lo / 4., wu);
+      }
+    }
+  }
+  int best = 0;
+  if (tabs.size() > 1) {
+    size_t maxn = 0;
+    for (auto &t : tabs) maxn = std::max(maxn, t.size());
+    int2 *d = nullptr;
+    SWM_CK(cudaMalloc((void **)&d, maxn * sizeof(int2)));
+    std::vector<int> idx(tabs.size());
+    for (size_t i = 0; i < idx.size(); i++) idx[i] = (int)i;
+    int uploaded = -1;
+    const int rc = march_pick_rows(c->stream, 5, idx, [&](int i) {
+      if (uploaded != i) {
+        cudaMemcpyAsync(d, tabs[i].data(), tabs[i].size() * sizeof(int2), cudaMemcpyHostToDevice, c->stream);
+        uploaded = i;
+      }
+      launch_any(p, MarchGrid{d, (int)(tabs[i].size() / 4)}, c->stream);
+    }, &best);
+    cudaStreamSynchronize(c->stream);
+    cudaFree(d);
+    if (rc != SWM_GPU_OK) return rc;
+  }
+  c->march_rows = (int)params[best].first;
+  c->march_slow = params[best].second;
+  return upload_tiles(c, tabs[best]);
 }
 
 // ---- ensemble launch ------------------------------------------------------
