@@ -196,6 +196,9 @@ def ours(args, rank, ws):
                        'l2': 'flushed (512 MB write) before every timed step',
                        'parallelism': 'replicas x%d' % ws if ws > 1 else 'single GPU'},
             'gpu_launches': int(launches), 'wall_s_timed_region': wall}
+    if args.path == 'fused_fp32c':
+        rows, cost, blocks = g.step_shape()
+        line['config']['step_kernel_tiles'] = {'rows_per_warp': rows, 'masked_row_cost': cost, 'blocks': blocks}
     line['clocks'] = clk.summary()
     peak, kind = peaks()
     alg = BYTES_PER_POINT[args.path] * npts

@@ -110,6 +110,11 @@ int swm_gpu_synchronize(swm_gpu_ctx *ctx);
 void *swm_gpu_stream(swm_gpu_ctx *ctx);
 /* number of kernels this context has launched so far */
 int64_t swm_gpu_launch_count(swm_gpu_ctx *ctx);
+/* Launch shape of the FP32 pair step kernel, as its autotuner picked it on
+   the first step: rows per warp strip (the cost target of a row group), the
+   cost of a row whose window holds land, and the blocks per launch; zeros
+   before the first step or on other paths.  No reference counterpart. */
+int swm_gpu_step_shape(swm_gpu_ctx *ctx, double *rows, double *masked_cost, int *blocks);
 
 /* ---- SWM_initSWM pieces (swm_module.f90:37-48) ---- */
 /* initDomain (domain_module.f90:49-207): grids, masks, depth on all grids,

@@ -194,6 +194,14 @@ int swm_gpu_synchronize(swm_gpu_ctx *c) {
 void *swm_gpu_stream(swm_gpu_ctx *c) { return c ? (void *)c->stream : nullptr; }
 int64_t swm_gpu_launch_count(swm_gpu_ctx *c) { return c ? c->launches : -1; }
 
+int swm_gpu_step_shape(swm_gpu_ctx *c, double *rows, double *masked_cost, int *blocks) {
+  SWM_REQUIRE(c && rows && masked_cost && blocks, "swm_gpu_step_shape: bad arguments");
+  *rows = c->march_tiles ? c->march_S : 0.;
+  *masked_cost = c->march_tiles ? c->march_slow : 0.;
+  *blocks = c->march_tiles ? c->march_blocks : 0;
+  return SWM_GPU_OK;
+}
+
 int swm_gpu_domain(swm_gpu_ctx *c, const double *H, const int8_t *Hmiss) {
   SWM_REQUIRE(c && c->stage == 0, "swm_gpu_domain: call once, first");
   TRY(host_domain(c, H, Hmiss));

@@ -139,6 +139,7 @@ struct swm_gpu_ctx {
   const swm::MonitorStep *mon = nullptr;  // the next FP32 pair step is a monitored step
   int64_t advances = 0;             // swm_gpu_advance calls (the rotation phase is advances mod 6)
   int march_rows = 0;                // rows per warp strip of the FP32 step kernel (0: not tuned yet)
+  double march_S = 0.;               // rows per warp its tiles were cut for (cost target)
   double march_slow = 1.;            // masked-row cost its tiles were cut with
   int2 *march_tiles = nullptr;       // its tiles, one per warp (device)
   int march_blocks = 0;              // its blocks (tiles / 4)

@@ -134,6 +134,8 @@ void make_p32(const swm_gpu_ctx *c, int64_t itt, P32 &p);
 void march_launch(swm_gpu_ctx *c, const P32 &p, const MarchGrid &g, const MarchInteg *mi = nullptr);
 int march_tile_cols(int mix);          // columns a warp strip updates
 int march_rows_override();             // SWM_GB300_MARCH_S, 0 when unset
+double march_rows_override_f();        // the same, quarters allowed
+double march_slow_override();         // SWM_GB300_MARCH_SLOW, 0 when unset
 int march_pick_rows(cudaStream_t st, int reps, const std::vector<int> &cands, const std::function<void(int)> &launch,
                     int *best);
 int march_autotune(swm_gpu_ctx *c, const P32 &p, const uint16_t *m16);

@@ -705,15 +705,21 @@ static void launch_any(const P32 &p, const MarchGrid &g, cudaStream_t st, const 
   else launch_mix<0>(p, g, st, mi);
 }
 
-int march_rows_override() {
+// SWM_GB300_MARCH_S: rows per warp (quarters allowed), 0 when unset
+double march_rows_override_f() {
   const char *e = getenv("SWM_GB300_MARCH_S");
-  if (!e) return 0;
-  int s = atoi(e);
-  return s >= 4 && s <= 250 ? s : 0;
+  if (!e) return 0.;
+  const double s = atof(e);
+  return s >= 4. && s <= 250. ? s : 0.;
+}
+
+int march_rows_override() {
+  const double s = march_rows_override_f();
+  return s > 0. ? (int)s : 0;
 }
 
 // SWM_GB300_MARCH_SLOW: the masked-row cost factor, 0 when unset
-static double march_slow_override() {
+double march_slow_override() {
   const char *e = getenv("SWM_GB300_MARCH_SLOW");
   if (!e) return 0.;
   double v = atof(e);
@@ -738,7 +744,9 @@ static int upload_tiles(swm_gpu_ctx *c, const std::vector<int2> &t) {
 // tiles of S rows per warp, without tuning
 int march_default_tiles(swm_gpu_ctx *c, const P32 &p, const uint16_t *m16, int S) {
   const double slow = march_slow_override();
-  return upload_tiles(c, march_tiles(p.mix, p.nx, p.ny, m16, S, slow > 0. ? slow : 1.));
+  c->march_S = S;
+  c->march_slow = slow > 0. ? slow : 1.;
+  return upload_tiles(c, march_tiles(p.mix, p.nx, p.ny, m16, S, c->march_slow));
 }
 
 // Mean time of `reps` launches per candidate; the step reads level n0 and
@@ -804,7 +812,7 @@ constexpr double MARCH_TUNE_SLOW[] = {1.0, 1.2, 1.3, 1.4, 1.5, 1.7};
 int march_autotune(swm_gpu_ctx *c, const P32 &p, const uint16_t *m16) {
   std::vector<std::vector<int2>> tabs;
   std::vector<std::pair<double, double>> params;
-  const int s_env = march_rows_override();
+  const double s_env = march_rows_override_f();
   const double w_env = march_slow_override();
   const std::vector<uint8_t> fast = march_fast_rows(p.mix, p.nx, p.ny, m16);
   auto add = [&](double S, double w) {
@@ -813,7 +821,7 @@ int march_autotune(swm_gpu_ctx *c, const P32 &p, const uint16_t *m16) {
     params.push_back({S, w});
     tabs.push_back(march_tiles_cut(fast, p.ny, S, w));
   };
-  if (s_env) {
+  if (s_env > 0.) {
     add(s_env, w_env > 0. ? w_env : 1.);
   } else {
     const int R = resident_blocks(p.mix);
@@ -855,6 +863,7 @@ int march_autotune(swm_gpu_ctx *c, const P32 &p, const uint16_t *m16) {
     if (rc != SWM_GPU_OK) return rc;
   }
   c->march_rows = (int)params[best].first;
+  c->march_S = params[best].first;
   c->march_slow = params[best].second;
   return upload_tiles(c, tabs[best]);
 }

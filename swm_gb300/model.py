@@ -148,6 +148,13 @@ class GpuModel:
     def launch_count(self):
         return self.L.swm_gpu_launch_count(self.ctx)
 
+    def step_shape(self):
+        """(rows per warp strip, masked-row cost, blocks) of the FP32 step
+        kernel's tiles, zeros before the first step."""
+        rows, cost, blocks = C.c_double(), C.c_double(), C.c_int()
+        check(self.L.swm_gpu_step_shape(self.ctx, C.byref(rows), C.byref(cost), C.byref(blocks)))
+        return rows.value, cost.value, blocks.value
+
     def stream(self):
         return self.L.swm_gpu_stream(self.ctx)
 
