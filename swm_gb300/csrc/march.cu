@@ -807,7 +807,7 @@ static int resident_blocks(int mix) {
 // cost in MARCH_TUNE_SLOW the candidate is the fewest rows per warp (in
 // steps of 1/4) whose tiles fit one wave, and the same for two waves; plus
 // equal groups of 16 rows.
-constexpr double MARCH_TUNE_SLOW[] = {1.0, 1.2, 1.3, 1.4, 1.5, 1.7};
+constexpr double MARCH_TUNE_SLOW[] = {1.0, 1.2, 1.4, 1.6, 1.8, 2.0, 2.3, 2.6};
 
 int march_autotune(swm_gpu_ctx *c, const P32 &p, const uint16_t *m16) {
   std::vector<std::vector<int2>> tabs;
