@@ -115,6 +115,15 @@ int64_t swm_gpu_launch_count(swm_gpu_ctx *ctx);
    cost of a row whose window holds land, and the blocks per launch; zeros
    before the first step or on other paths.  No reference counterpart. */
 int swm_gpu_step_shape(swm_gpu_ctx *ctx, double *rows, double *masked_cost, int *blocks);
+/* Host-only planner behind that shape: the tiles of the FP32 step kernel for
+   an nx x ny basin (mixing 0 none, 1 Laplacian, 2 biharmonic) from its packed
+   mask words (per point: bits 0-3 ocean at H, u, v, eta; bits 4-7 the same
+   at i-1, bits 8-11 at i+1), cut for `rows` rows per warp with a masked row
+   counted masked_cost.  Writes up to `capacity` tiles as (strip, first row,
+   rows) triples, four per block, rows 0 for padding; returns the number of
+   tiles, or -1 for bad arguments.  Runs no GPU code. */
+int swm_gpu_plan_step_tiles(int mixing, int nx, int ny, const uint16_t *mask_words, double rows,
+                            double masked_cost, int32_t *tiles, int capacity);
 
 /* ---- SWM_initSWM pieces (swm_module.f90:37-48) ---- */
 /* initDomain (domain_module.f90:49-207): grids, masks, depth on all grids,

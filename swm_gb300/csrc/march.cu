@@ -688,6 +688,24 @@ std::vector<int2> march_tiles(int mix, int nx, int ny, const uint16_t *m16, doub
   return march_tiles_cut(march_fast_rows(mix, nx, ny, m16), ny, S, slow);
 }
 
+}  // namespace swm
+
+extern "C" int swm_gpu_plan_step_tiles(int mixing, int nx, int ny, const uint16_t *mask_words, double rows,
+                                       double masked_cost, int32_t *tiles, int capacity) {
+  if (nx < 1 || ny < 1 || !mask_words || rows < 1. || rows > 250. || masked_cost < 1. || capacity < 0 ||
+      (capacity > 0 && !tiles))
+    return -1;
+  const std::vector<int2> t = swm::march_tiles(mixing, nx, ny, mask_words, rows, masked_cost);
+  for (size_t k = 0; k < t.size() && (int)k < capacity; k++) {
+    tiles[3 * k] = t[k].x;
+    tiles[3 * k + 1] = t[k].y >> 8;
+    tiles[3 * k + 2] = t[k].y & 255;
+  }
+  return (int)t.size();
+}
+
+namespace swm {
+
 template <int MIX>
 static void launch_mix(const P32 &p, const MarchGrid &g, cudaStream_t st, const MarchInteg *mi) {
   if (!mi) {
