@@ -11,6 +11,7 @@
 // for each of the six phases of that rotation, and blocks of six steps replay
 // one captured CUDA graph.  Per-member volume and energy sums are taken in
 // FP64.
+#include <algorithm>
 #include <cstring>
 #include <string>
 #include <vector>
@@ -22,6 +23,9 @@ using swm::P32;
 namespace swm {
 
 constexpr int ENS_PHASES = 6;  // lcm of the 2 levels and 3 increment slots
+// tile candidates: rows per warp x masked-row cost
+constexpr int ENS_TUNE_ROWS[] = {16, 24, 32, 48};
+constexpr double ENS_TUNE_SLOW[] = {1.0, 1.7};
 
 struct EnsInt {
   const float *uh, *ul, *vh, *vl, *eh, *el;
@@ -69,18 +73,13 @@ __global__ void k_ens_integrals(const EnsInt *__restrict__ d, double *__restrict
 struct swm_gpu_ensemble {
   std::vector<swm_gpu_ctx *> m;
   int mix = 0, rows = 16, phase = 0, graph_phase = -1;
+  double slow = 1.;  // masked-row cost the tiles were cut with
   cudaStream_t stream = nullptr;
   cudaEvent_t done = nullptr;
   std::vector<cudaEvent_t> ev;
   P32 *tab = nullptr;  // [ENS_PHASES][n]
-  std::vector<int> cand;     // candidate rows per strip
-  std::vector<int2 *> tiles;  // tile list per candidate
-  std::vector<int> ntiles;
-  int rows_index(int r) const {
-    for (size_t i = 0; i < cand.size(); i++)
-      if (cand[i] == r) return (int)i;
-    return 0;
-  }
+  int4 *tiles = nullptr;  // {member, strip, first row, rows}, costliest first
+  int ntiles = 0;
   int *next = nullptr;  // queue heads, one per phase
   cudaGraphExec_t graph = nullptr;
   int64_t launches = 0, graph_launches = 0;
@@ -122,10 +121,9 @@ int rotate_members(swm_gpu_ensemble *e, int64_t itt) {
 
 int ens_step(swm_gpu_ensemble *e, int64_t itt) {
   const size_t n = e->m.size();
-  const int ri = e->rows_index(e->rows);
   SWM_CK(cudaMemsetAsync(e->next + e->phase, 0, sizeof(int), e->stream));
-  int rc = march_ens_launch(e->mix, e->rows, e->tab + (size_t)e->phase * n, e->tiles[ri], e->ntiles[ri],
-                            e->next + e->phase, e->stream);
+  int rc = march_ens_launch(e->mix, e->tab + (size_t)e->phase * n, e->tiles, e->ntiles, e->next + e->phase,
+                            e->stream);
   if (rc != SWM_GPU_OK) return rc;
   e->launches++;
   return rotate_members(e, itt);
@@ -167,7 +165,7 @@ void ens_free(swm_gpu_ensemble *e) {
   if (e->stream) cudaStreamSynchronize(e->stream);
   if (e->graph) cudaGraphExecDestroy(e->graph);
   cudaFree(e->tab);
-  for (auto *t : e->tiles) cudaFree(t);
+  cudaFree(e->tiles);
   cudaFree(e->next);
   cudaFree(e->d_int);
   cudaFree(e->d_out);
@@ -190,7 +188,7 @@ int swm_gpu_ensemble_create(swm_gpu_ctx *const *members, int n, swm_gpu_ensemble
     SWM_REQUIRE(c && c->stage >= 5, "swm_gpu_ensemble_create: members must be initialised");
     SWM_REQUIRE(c->cfg.path == SWM_PATH_FUSED_FP32C, "swm_gpu_ensemble_create: members must use SWM_PATH_FUSED_FP32C");
     SWM_REQUIRE(c->tracers.empty(), "swm_gpu_ensemble_create: members with tracers are not batched");
-    SWM_REQUIRE(c->nx <= 65535 * 28 && c->ny <= 65535 * 8, "swm_gpu_ensemble_create: member too large for a tile index");
+    SWM_REQUIRE(c->ny < (1 << 23), "swm_gpu_ensemble_create: member too large for a tile index");
     if (!c->march_rows) c->march_rows = 16;  // the ensemble tunes its own strip rows
     int rc = fused_prepare(c);
     if (rc != SWM_GPU_OK) return rc;
@@ -224,26 +222,39 @@ int swm_gpu_ensemble_create(swm_gpu_ctx *const *members, int n, swm_gpu_ensemble
       make_p32(members[i], 3, tab[(size_t)k * n + i]);
     }
   for (int i = 0; i < n; i++) fused_set_indices(members[i], n0, g0);
-  // tiles for each candidate strip length
-  const int ti = march_tile_cols(mix);
-  e->cand.assign(MARCH_ROWS, MARCH_ROWS + MARCH_NROWS);
-  if (march_rows_override()) e->cand.assign(1, march_rows_override());
-  e->tiles.assign(e->cand.size(), nullptr);
-  e->ntiles.assign(e->cand.size(), 0);
-  for (size_t r = 0; r < e->cand.size(); r++) {
-    const int S = e->cand[r];
-    std::vector<int2> t;
+  // Tiles: every member's strips cut into row groups of equal estimated
+  // cost (as the single-basin step kernel's tiles), all members' tiles in
+  // one queue, costliest first, so the queue ends on small tiles and the
+  // warps finish close together.  Candidates: rows per warp x masked-row
+  // cost, timed below.
+  std::vector<std::vector<uint8_t>> fast(n);
+  for (int i = 0; i < n; i++) {
+    const uint16_t *m16 = fused_mask_words(members[i]);
+    SWM_REQUIRE(m16, "swm_gpu_ensemble_create: member has no FP32 pair state");
+    fast[i] = march_fast_rows(mix, members[i]->nx, members[i]->ny, m16);
+  }
+  std::vector<std::pair<double, double>> cand;
+  const double s_env = march_rows_override_f(), w_env = march_slow_override();
+  for (int S : ENS_TUNE_ROWS)
+    for (double w : ENS_TUNE_SLOW) {
+      const std::pair<double, double> q(s_env > 0. ? s_env : S, w_env > 0. ? w_env : w);
+      if (std::find(cand.begin(), cand.end(), q) == cand.end()) cand.push_back(q);
+    }
+  std::vector<std::vector<int4>> lists(cand.size());
+  size_t maxn = 0;
+  for (size_t r = 0; r < cand.size(); r++) {
+    std::vector<std::pair<double, int4>> t;
     for (int i = 0; i < n; i++) {
-      const int nbx = (members[i]->nx + ti - 1) / ti, nrg = (members[i]->ny + S - 1) / S;
-      for (int rg = 0; rg < nrg; rg++)
-        for (int bx = 0; bx < nbx; bx++) t.push_back(make_int2(i, (bx << 16) | rg));
+      const int ny = members[i]->ny;
+      for (const int2 g : march_tiles_cut(fast[i], ny, cand[r].first, cand[r].second))
+        if (g.y & 255)
+          t.push_back({march_tile_cost(fast[i], ny, g, cand[r].second), make_int4(i, g.x, g.y >> 8, g.y & 255)});
     }
-    e->ntiles[r] = (int)t.size();
-    if (cudaMalloc((void **)&e->tiles[r], t.size() * sizeof(int2)) != cudaSuccess ||
-        cudaMemcpy(e->tiles[r], t.data(), t.size() * sizeof(int2), cudaMemcpyHostToDevice) != cudaSuccess) {
-      set_error("swm_gpu_ensemble_create: tile list upload failed");
-      return fail(SWM_GPU_ENOMEM);
-    }
+    std::stable_sort(t.begin(), t.end(), [](const std::pair<double, int4> &a, const std::pair<double, int4> &b) {
+      return a.first > b.first;
+    });
+    for (auto &q : t) lists[r].push_back(q.second);
+    maxn = std::max(maxn, lists[r].size());
   }
   if (cudaMalloc((void **)&e->tab, tab.size() * sizeof(P32)) != cudaSuccess ||
       cudaMemcpy(e->tab, tab.data(), tab.size() * sizeof(P32), cudaMemcpyHostToDevice) != cudaSuccess ||
@@ -253,17 +264,37 @@ int swm_gpu_ensemble_create(swm_gpu_ctx *const *members, int n, swm_gpu_ensemble
     set_error("swm_gpu_ensemble_create: device allocation failed");
     return fail(SWM_GPU_ENOMEM);
   }
-  // strip rows by timing the ensemble step at the current phase (the step
+  // tiles by timing the ensemble step at the current phase (the step
   // rewrites level N0p1 and slot 3 only, which the first real step rewrites)
+  if (cudaMalloc((void **)&e->tiles, maxn * sizeof(int4)) != cudaSuccess) {
+    set_error("swm_gpu_ensemble_create: tile list allocation failed");
+    return fail(SWM_GPU_ENOMEM);
+  }
   if (join_members(e) != SWM_GPU_OK) return fail(SWM_GPU_ECUDA);
-  int best = 16;
-  int rc = march_pick_rows(e->stream, 3, e->cand, [&](int r) {
-    const int ri = e->rows_index(r);
-    cudaMemsetAsync(e->next, 0, sizeof(int), e->stream);
-    march_ens_launch(mix, r, e->tab, e->tiles[ri], e->ntiles[ri], e->next, e->stream);
-  }, &best);
+  int best = 0, uploaded = -1;
+  std::vector<int> idx(cand.size());
+  for (size_t r = 0; r < idx.size(); r++) idx[r] = (int)r;
+  int rc = SWM_GPU_OK;
+  if (cand.size() > 1)
+    rc = march_pick_rows(e->stream, 3, idx, [&](int r) {
+      if (uploaded != r) {
+        cudaMemcpyAsync(e->tiles, lists[r].data(), lists[r].size() * sizeof(int4), cudaMemcpyHostToDevice,
+                        e->stream);
+        uploaded = r;
+      }
+      cudaMemsetAsync(e->next, 0, sizeof(int), e->stream);
+      march_ens_launch(mix, e->tab, e->tiles, (int)lists[r].size(), e->next, e->stream);
+    }, &best);
   if (rc != SWM_GPU_OK) return fail(rc);
-  e->rows = best;
+  if (cudaMemcpyAsync(e->tiles, lists[best].data(), lists[best].size() * sizeof(int4), cudaMemcpyHostToDevice,
+                      e->stream) != cudaSuccess ||
+      cudaStreamSynchronize(e->stream) != cudaSuccess) {
+    set_error("swm_gpu_ensemble_create: tile list upload failed");
+    return fail(SWM_GPU_ECUDA);
+  }
+  e->ntiles = (int)lists[best].size();
+  e->rows = (int)cand[best].first;
+  e->slow = cand[best].second;
   if (release_members(e) != SWM_GPU_OK) return fail(SWM_GPU_ECUDA);
   *out = e;
   return SWM_GPU_OK;

@@ -741,6 +741,9 @@ void fused_static(const swm_gpu_ctx *c, const float **He, const uint16_t **mask1
   *mask16 = f->mask16;
   *Fe = f->has_F ? (const float *)f->F[2] : nullptr;
 }
+const uint16_t *fused_mask_words(const swm_gpu_ctx *c) {
+  return c->fused && !c->fused->m16h.empty() ? c->fused->m16h.data() : nullptr;
+}
 void fused_pair_level(const swm_gpu_ctx *c, const float *out[6]) {
   const FusedState *f = c->fused;
   int a = f->n0;

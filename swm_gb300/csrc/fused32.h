@@ -123,6 +123,10 @@ struct MarchGrid {
   int blocks;
 };
 std::vector<int2> march_tiles(int mix, int nx, int ny, const uint16_t *m16, double S, double slow);
+std::vector<uint8_t> march_fast_rows(int mix, int nx, int ny, const uint16_t *m16);
+std::vector<int2> march_tiles_cut(const std::vector<uint8_t> &fast, int ny, double S, double slow);
+double march_tile_cost(const std::vector<uint8_t> &fast, int ny, int2 t, double slow);
+const uint16_t *fused_mask_words(const swm_gpu_ctx *c);  // host copy, FP32 pair path
 int march_default_tiles(swm_gpu_ctx *c, const P32 &p, const uint16_t *m16, int S);
 
 // candidate rows per warp strip of the step kernel
@@ -143,8 +147,7 @@ void fused_indices(const swm_gpu_ctx *c, int *n0, int *g0);
 void fused_set_indices(swm_gpu_ctx *c, int n0, int g0);
 void fused_pair_level(const swm_gpu_ctx *c, const float *out[6]);
 void fused_static(const swm_gpu_ctx *c, const float **He, const uint16_t **mask16, const float **Fe);
-// one launch of the ensemble step: tiles {member, strip << 16 | row group}
-int march_ens_launch(int mix, int rows, const P32 *tab, const int2 *tiles, int ntiles, int *next,
-                     cudaStream_t st);
+// one launch of the ensemble step: tiles {member, strip, first row, rows}
+int march_ens_launch(int mix, const P32 *tab, const int4 *tiles, int ntiles, int *next, cudaStream_t st);
 
 }  // namespace swm

@@ -566,14 +566,14 @@ __global__ void __launch_bounds__(128, MARCH_MINB) k_march(P32 p, const int2 *__
   }
 }
 
-// Ensemble of basins in one persistent launch: every warp takes (member,
-// strip, row group) tiles from the queue until it is empty.  A tile is
-// int2 {member, strip << 16 | row group}; the member's parameter block is
-// copied into the warp's slice of shared memory first.
+// Ensemble of basins in one persistent launch: every warp takes tiles from
+// the queue until it is empty.  A tile is int4 {member, strip, first row,
+// rows}; the member's parameter block is copied into the warp's slice of
+// shared memory first.
 template <int MIX>
 __global__ void __launch_bounds__(128, MARCH_MINB) k_march_ens(const P32 *__restrict__ tab,
-                                                               const int2 *__restrict__ tiles, int ntiles,
-                                                               int *__restrict__ next, int S) {
+                                                               const int4 *__restrict__ tiles, int ntiles,
+                                                               int *__restrict__ next) {
   __shared__ P32 sp[4];
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
   for (;;) {
@@ -581,12 +581,12 @@ __global__ void __launch_bounds__(128, MARCH_MINB) k_march_ens(const P32 *__rest
     if (lane == 0) t = atomicAdd(next, 1);
     t = __shfl_sync(FULL, t, 0);
     if (t >= ntiles) return;
-    const int2 d = tiles[t];
+    const int4 d = tiles[t];
     const int *src = reinterpret_cast<const int *>(tab + d.x);
     int *dst = reinterpret_cast<int *>(&sp[warp]);
     for (int k = lane; k < (int)(sizeof(P32) / sizeof(int)); k += 32) dst[k] = src[k];
     __syncwarp();
-    march_strip<MIX>(sp[warp], d.y >> 16, (d.y & 0xffff) * S, lane, S);
+    march_strip<MIX>(sp[warp], d.y, d.z, lane, d.w);
     __syncwarp();
   }
 }
@@ -686,6 +686,15 @@ std::vector<int2> march_tiles_cut(const std::vector<uint8_t> &fast, int ny, doub
 
 std::vector<int2> march_tiles(int mix, int nx, int ny, const uint16_t *m16, double S, double slow) {
   return march_tiles_cut(march_fast_rows(mix, nx, ny, m16), ny, S, slow);
+}
+
+// estimated cost of a tile {strip, first row << 8 | rows} as march_tiles_cut counts it
+double march_tile_cost(const std::vector<uint8_t> &fast, int ny, int2 t, double slow) {
+  const int k = t.y & 255, ry0 = t.y >> 8;
+  const uint8_t *f = &fast[(size_t)t.x * ny];
+  double c = 0.;
+  for (int j = ry0 - 1; j <= std::min(ry0 + k, ny) + 1; j++) c += f[((j % ny) + ny) % ny] ? 1.0 : slow;
+  return k > 0 ? c : 0.;
 }
 
 }  // namespace swm
@@ -888,7 +897,7 @@ int march_autotune(swm_gpu_ctx *c, const P32 &p, const uint16_t *m16) {
 
 // ---- ensemble launch ------------------------------------------------------
 template <int MIX>
-static int ens_launch_m(const P32 *tab, const int2 *tiles, int ntiles, int *next, int S, cudaStream_t st) {
+static int ens_launch_m(const P32 *tab, const int4 *tiles, int ntiles, int *next, cudaStream_t st) {
   static int blocks = 0;
   if (!blocks) {
     int per_sm = 0, sms = 0, dev = 0;
@@ -898,14 +907,14 @@ static int ens_launch_m(const P32 *tab, const int2 *tiles, int ntiles, int *next
     blocks = sms * (per_sm > 0 ? per_sm : 1);
   }
   int need = (ntiles + 3) / 4;
-  k_march_ens<MIX><<<need < blocks ? need : blocks, 128, 0, st>>>(tab, tiles, ntiles, next, S);
+  k_march_ens<MIX><<<need < blocks ? need : blocks, 128, 0, st>>>(tab, tiles, ntiles, next);
   return SWM_GPU_OK;
 }
 
-int march_ens_launch(int mix, int s, const P32 *tab, const int2 *tiles, int ntiles, int *next, cudaStream_t st) {
-  if (mix == 2) return ens_launch_m<2>(tab, tiles, ntiles, next, s, st);
-  if (mix == 1) return ens_launch_m<1>(tab, tiles, ntiles, next, s, st);
-  return ens_launch_m<0>(tab, tiles, ntiles, next, s, st);
+int march_ens_launch(int mix, const P32 *tab, const int4 *tiles, int ntiles, int *next, cudaStream_t st) {
+  if (mix == 2) return ens_launch_m<2>(tab, tiles, ntiles, next, st);
+  if (mix == 1) return ens_launch_m<1>(tab, tiles, ntiles, next, st);
+  return ens_launch_m<0>(tab, tiles, ntiles, next, st);
 }
 
 }  // namespace swm
