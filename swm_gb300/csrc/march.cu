@@ -781,11 +781,6 @@ int march_default_tiles(swm_gpu_ctx *c, const P32 &p, const uint16_t *m16, int S
 // the model state as one launch leaves it.
 int march_pick_rows(cudaStream_t st, int reps, const std::vector<int> &cands, const std::function<void(int)> &launch,
                     int *best) {
-  int s = march_rows_override();
-  if (s) {
-    *best = s;
-    return SWM_GPU_OK;
-  }
   cudaEvent_t a, b;
   SWM_CK(cudaEventCreate(&a));
   SWM_CK(cudaEventCreate(&b));

@@ -11,6 +11,7 @@
 // binary32.  Extension: third-order upwind-biased face values
 // (swm_gpu_config.tracer_flux = 1) with the reference's mask-weighted mean
 // next to land.
+#include <algorithm>
 #include <cmath>
 #include <cstdlib>
 #include <cstring>
@@ -235,36 +236,80 @@ __global__ void __launch_bounds__(128, NT <= 2 ? 4 : 3) k_trc32(TrcP p, int S, i
   }
 }
 
-// rows per warp: TRC_ROWS (SWM_GB300_TRC_ROWS overrides).  Lengths fitted
-// to whole waves of resident blocks were tried and ran slower (more
-// look-ahead rows per output row outweighed the shorter tail).
-static int trc_rows() {
+// rows per warp set by SWM_GB300_TRC_ROWS, 0 when unset
+static int trc_rows_override() {
   const char *e = getenv("SWM_GB300_TRC_ROWS");
   if (e && atoi(e) >= 4 && atoi(e) <= 256) return atoi(e);
-  return TRC_ROWS;
+  return 0;
 }
 
 template <int NT, int FLUX>
-static void trc_launch_f(const TrcP &p, cudaStream_t st) {
+static void trc_launch_f(const TrcP &p, int S, cudaStream_t st) {
   const int nstrips = (p.nx + 27) / 28;
-  const int S = trc_rows();
   const unsigned blocks = (unsigned)((long)nstrips * ((p.ny + 4 * S - 1) / (4 * S)));
   k_trc32<NT, FLUX><<<blocks, 128, 0, st>>>(p, S, nstrips);
 }
 
-template <int NT>
-static void trc_launch_nt(const TrcP &p, cudaStream_t st) {
-  if (p.flux == 1) trc_launch_f<NT, 1>(p, st);
-  else trc_launch_f<NT, 0>(p, st);
+template <int NT, int FLUX>
+static int trc_resident_f() {
+  int per_sm = 0, sms = 0, dev = 0;
+  cudaGetDevice(&dev);
+  cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_trc32<NT, FLUX>, 128, 0);
+  return sms * (per_sm > 0 ? per_sm : 1);
 }
 
-static void trc_launch(const TrcP &p, cudaStream_t st) {
+template <int NT>
+static void trc_launch_nt(const TrcP &p, int S, cudaStream_t st) {
+  if (p.flux == 1) trc_launch_f<NT, 1>(p, S, st);
+  else trc_launch_f<NT, 0>(p, S, st);
+}
+
+template <int NT>
+static int trc_resident_nt(const TrcP &p) {
+  return p.flux == 1 ? trc_resident_f<NT, 1>() : trc_resident_f<NT, 0>();
+}
+
+static void trc_launch(const TrcP &p, int S, cudaStream_t st) {
   switch (p.ntr) {
-    case 1: trc_launch_nt<1>(p, st); break;
-    case 2: trc_launch_nt<2>(p, st); break;
-    case 3: trc_launch_nt<3>(p, st); break;
-    default: trc_launch_nt<4>(p, st); break;
+    case 1: trc_launch_nt<1>(p, S, st); break;
+    case 2: trc_launch_nt<2>(p, S, st); break;
+    case 3: trc_launch_nt<3>(p, S, st); break;
+    default: trc_launch_nt<4>(p, S, st); break;
   }
+}
+
+// blocks of the tracer kernel resident on the whole GPU at once
+static int trc_resident(const TrcP &p) {
+  switch (p.ntr) {
+    case 1: return trc_resident_nt<1>(p);
+    case 2: return trc_resident_nt<2>(p);
+    case 3: return trc_resident_nt<3>(p);
+    default: return trc_resident_nt<4>(p);
+  }
+}
+
+// Rows per warp, by timing the tracer step on this basin (the repeated step
+// rewrites the next level and the newest increment only): TRC_ROWS, 32, 64
+// and the lengths that make the grid one and two waves of resident blocks
+// (the look-ahead costs 4 rows per warp, so longer warps do less of it, and
+// a grid of whole waves has no partial last wave).
+static int trc_tune_rows(swm_gpu_ctx *c, const TrcP &p) {
+  const int env = trc_rows_override();
+  if (env) return env;
+  std::vector<int> cand = {TRC_ROWS, 32, 64};
+  const int nstrips = (p.nx + 27) / 28, R = trc_resident(p);
+  for (int waves = 1; waves <= 2; waves++) {
+    const int per_strip = waves * R / nstrips;  // blocks of four row groups per strip
+    if (per_strip < 1) continue;
+    const int S = (p.ny + 4 * per_strip - 1) / (4 * per_strip);
+    if (S >= 4 && S <= 256) cand.push_back(S);
+  }
+  std::sort(cand.begin(), cand.end());
+  cand.erase(std::unique(cand.begin(), cand.end()), cand.end());
+  int best = TRC_ROWS;
+  const int rc = march_pick_rows(c->stream, 3, cand, [&](int S) { trc_launch(p, S, c->stream); }, &best);
+  return rc == SWM_GPU_OK ? best : TRC_ROWS;
 }
 
 __global__ void k_trc32_export(const float *ch, const float *cl, const double *D, double *out, size_t n, int conc) {
@@ -283,6 +328,7 @@ __global__ void k_f64_to_f32(const double *a, float *b, size_t n) {
 
 struct Trc32State {
   std::vector<swm::Tracer32> t;
+  int warp_rows = 0;  // rows per warp of the tracer kernel (0: not tuned yet)
   float *rows = nullptr;
   float *u = nullptr, *v = nullptr, *eta = nullptr;  // frozen-flow copies
   bool ready = false;
@@ -425,7 +471,8 @@ int trc32_step(swm_gpu_ctx *c, int64_t itt) {
       d.C0 = T.C0; d.gamma = T.gamma; d.dp = T.dp;
       d.gamma_s = T.gamma_s; d.dp_s = T.dp_s; d.kappa = T.kappa;
     }
-    trc_launch(p, c->stream);
+    if (!s->warp_rows) s->warp_rows = trc_tune_rows(c, p);
+    trc_launch(p, s->warp_rows, c->stream);
     c->launches++;
   }
   SWM_CK(cudaGetLastError());
