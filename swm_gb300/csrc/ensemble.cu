@@ -224,9 +224,9 @@ int swm_gpu_ensemble_create(swm_gpu_ctx *const *members, int n, swm_gpu_ensemble
   for (int i = 0; i < n; i++) fused_set_indices(members[i], n0, g0);
   // Tiles: every member's strips cut into row groups of equal estimated
   // cost (as the single-basin step kernel's tiles), all members' tiles in
-  // one queue, costliest first, so the queue ends on small tiles and the
-  // warps finish close together.  Candidates: rows per warp x masked-row
-  // cost, timed below.
+  // one queue with the short remainder groups last, so the queue ends on
+  // small tiles and the warps finish close together.  Candidates: rows per
+  // warp x masked-row cost, timed below.
   std::vector<std::vector<uint8_t>> fast(n);
   for (int i = 0; i < n; i++) {
     const uint16_t *m16 = fused_mask_words(members[i]);
@@ -250,8 +250,15 @@ int swm_gpu_ensemble_create(swm_gpu_ctx *const *members, int n, swm_gpu_ensemble
         if (g.y & 255)
           t.push_back({march_tile_cost(fast[i], ny, g, cand[r].second), make_int4(i, g.x, g.y >> 8, g.y & 255)});
     }
-    std::stable_sort(t.begin(), t.end(), [](const std::pair<double, int4> &a, const std::pair<double, int4> &b) {
-      return a.first > b.first;
+    // full groups (cost within 3/4 of the target) first, in their natural
+    // order: vertically adjacent groups of a strip go to warps at about the
+    // same time and share their look-ahead rows in L2; the short remainders
+    // after them, costliest first
+    const double full = 0.75 * (cand[r].first + 3.0);
+    std::stable_sort(t.begin(), t.end(), [full](const std::pair<double, int4> &a, const std::pair<double, int4> &b) {
+      const bool fa = a.first >= full, fb = b.first >= full;
+      if (fa != fb) return fa;
+      return !fa && a.first > b.first;
     });
     for (auto &q : t) lists[r].push_back(q.second);
     maxn = std::max(maxn, lists[r].size());
