@@ -191,7 +191,7 @@ def test_integrals_against_numpy_sums(path, cells):
     assert np.all(np.abs(got - want) <= tol * scale), (got, want, (got - want) / scale)
 
 
-@pytest.mark.parametrize('cells', [(48, 40), (300, 17)])
+@pytest.mark.parametrize('cells', [(48, 40), (300, 17), (5, 300), (2100, 10)])
 def test_step_kernel_integrals_against_numpy_sums(cells):
     """The integrals the FP32 step kernel forms of the state it writes
     (swm_gpu_run_monitor) against FP64 numpy sums of that state."""
@@ -247,3 +247,42 @@ def test_run_monitor_variants(variant):
         assert np.array_equal(a.field(f), b.field(f)), f
     want, scale = _numpy_integrals(case, b)
     assert np.all(np.abs(out[-1] - want) <= 1e-12 * np.maximum(scale, 1e-300)), (out[-1], want)
+
+
+@pytest.mark.parametrize('nsteps', [1, 2, 3])
+def test_run_monitor_short_runs(nsteps):
+    """Monitored runs of one to three steps: the first step of a run has no
+    previous step for the side-job block to finish and the last is finished
+    by its own kernel; state and integrals as the same steps one at a time,
+    and a second run continues from the first."""
+    import torch
+    case = synthetic.double_gyre((40, 32), biharmonic=True, nsteps=60)
+    a, b = GpuModel('fused_fp32c'), GpuModel('fused_fp32c')
+    for g in (a, b):
+        Driver(case, g).init(with_diag=False)
+    ny = case['config']['ny']
+    prof = case['streams'][0]['rec1'][0][:, 0]
+    a.run(0, 5)
+    b.run(0, 5)
+    itt = 5
+    for rep in range(2):
+        rows = torch.empty((nsteps, ny), dtype=torch.float64).pin_memory().numpy()
+        rows[:] = prof[None, :] * (1.0 + 0.2 * (rep + 1) + 0.1 * np.arange(nsteps))[:, None]
+        out = torch.empty((nsteps, 3), dtype=torch.float64).pin_memory().numpy()
+        out[:] = np.nan
+        a.run_monitor(itt, nsteps, 0, rows, out)
+        for s in range(nsteps):
+            b.set_stream_rows(0, np.ascontiguousarray(rows[s]))
+            b.step(itt + 1 + s)
+            b.advance(itt + 1 + s)
+            _, scale = _numpy_integrals(case, b)
+            ref = b.integrals()
+            assert np.all(np.abs(out[s] - ref) <= 1e-12 * scale), (rep, s, out[s], ref)
+        itt += nsteps
+        for f in ('u', 'v', 'eta'):
+            assert np.array_equal(a.field(f), b.field(f)), (rep, f)
+    # plain steps after the monitored runs read the last rows set
+    a.run(itt, 3)
+    b.run(itt, 3)
+    for f in ('u', 'v', 'eta'):
+        assert np.array_equal(a.field(f), b.field(f)), f
