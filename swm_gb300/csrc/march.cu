@@ -701,8 +701,8 @@ double march_tile_cost(const std::vector<uint8_t> &fast, int ny, int2 t, double 
 
 extern "C" int swm_gpu_plan_step_tiles(int mixing, int nx, int ny, const uint16_t *mask_words, double rows,
                                        double masked_cost, int32_t *tiles, int capacity) {
-  if (nx < 1 || ny < 1 || !mask_words || rows < 1. || rows > 250. || masked_cost < 1. || capacity < 0 ||
-      (capacity > 0 && !tiles))
+  if (nx < 1 || ny < 1 || ny >= (1 << 23) || !mask_words || rows < 1. || rows > 250. || masked_cost < 1. ||
+      capacity < 0 || (capacity > 0 && !tiles))
     return -1;
   const std::vector<int2> t = swm::march_tiles(mixing, nx, ny, mask_words, rows, masked_cost);
   for (size_t k = 0; k < t.size() && (int)k < capacity; k++) {
@@ -759,6 +759,7 @@ void march_launch(swm_gpu_ctx *c, const P32 &p, const MarchGrid &g, const MarchI
 }
 
 static int upload_tiles(swm_gpu_ctx *c, const std::vector<int2> &t) {
+  SWM_REQUIRE(c->ny < (1 << 23), "FP32 step kernel: at most 2^23 - 1 rows (tile row index)");
   if (c->march_tiles) SWM_CK(cudaFree(c->march_tiles));
   c->march_tiles = nullptr;
   c->march_blocks = 0;

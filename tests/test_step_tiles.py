@@ -105,6 +105,18 @@ def test_coastal_strips_get_shorter_groups_as_their_cost_rises(L):
     assert groups[1.0][interior] == groups[2.5][interior]
 
 
+@pytest.mark.parametrize('ny', [1, 2, 3, 4])
+def test_basins_of_a_few_rows(L, ny):
+    m16 = mask_words(np.ones((ny, 40), bool))
+    for rows, cost in ((4, 1.0), (16, 2.6)):
+        t = plan(L, 2, m16, rows, cost)
+        t = t[t[:, 2] > 0]
+        cover = np.zeros((strips_of(2, 40), ny), int)
+        for s, r0, k in t:
+            cover[s, r0:r0 + k] += 1
+        assert (cover == 1).all()
+
+
 def test_bad_arguments_are_refused(L):
     m16 = mask_words(basins()['ocean'])
     p = m16.ctypes.data_as(ctypes.c_void_p)
@@ -113,3 +125,4 @@ def test_bad_arguments_are_refused(L):
     assert L.swm_gpu_plan_step_tiles(2, 61, 40, p, 0.5, 1.0, None, 0) == -1
     assert L.swm_gpu_plan_step_tiles(2, 61, 40, p, 16, 0.5, None, 0) == -1
     assert L.swm_gpu_plan_step_tiles(2, 61, 40, p, 16, 1.0, None, 4) == -1
+    assert L.swm_gpu_plan_step_tiles(2, 1, 1 << 23, p, 16, 1.0, None, 0) == -1
