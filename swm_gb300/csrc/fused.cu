@@ -489,8 +489,9 @@ int fused_prepare(swm_gpu_ctx *c) {
   if (f->has_F)
     for (int q = 0; q < 3; q++) FTRY(upload_t(c, f32, Fh[q].data(), n, &f->F[q]));
   if (f32) {
-    std::vector<double> r32 = fp32c_rows(c);
-    FTRY(upload_t(c, true, r32.data(), r32.size(), &f->rows32c));
+    const std::vector<float> rec = fp32c_records(c);
+    FTRY(dmalloc(&f->rows32c, rec.size() * sizeof(float)));
+    SWM_CK(cudaMemcpy(f->rows32c, rec.data(), rec.size() * sizeof(float), cudaMemcpyHostToDevice));
     // mask word with the x-neighbours' bits (bits 4-7: i-1, 8-11: i+1)
     std::vector<uint16_t> m16(n);
     int nx = c->nx;
@@ -676,7 +677,7 @@ void make_p32(const swm_gpu_ctx *c, int64_t itt, P32 &p) {
   for (int q = 0; q < 2; q++) p.gsq_s[q] = (float)f->gsq_s[q];
   p.mask16 = f->mask16;
   p.He = (const float *)f->He;
-  p.rows = (const float *)f->rows32c;
+  p.rec = (const float4 *)f->rows32c;
   p.Hu = (const float *)f->Hu;
   p.Hv = (const float *)f->Hv;
   for (int q = 0; q < 3; q++) p.impl[q] = (const float *)f->impl[q];

@@ -12,6 +12,20 @@ enum {
   Q_PC0, Q_HC0, Q_TE, Q_TH, Q_TU, Q_TV, Q_NR
 };
 
+// The step kernel reads the factors of rows J, J-1 and J-2 in the iteration
+// that loads row J.  Record J holds exactly those, as float4 groups in the
+// order of the code that uses them, so an iteration issues a few vector
+// loads of one warp-uniform address instead of a load per factor:
+//   A {RH_DL, CU, DCU, INV_CH} (J)          relative vorticity and PV
+//   G {FH (J), 0, 0, 0}                     PV
+//   B {TE, PC0 (J-1), TH, HC0 (J)}          first stress pass
+//   C {TU, RU_DL, TV, RV_DL} (J-1)          lu1, lv1
+//   D {TE, PC0 (J-2), TH, HC0 (J-1)}        second (or the only) stress pass
+//   E {CV, DCV (J-1), RE_DL, RE_DT (J-2)}   eta tendency
+//   F {RU_DL, TU, TV, RV_DL} (J-2)          u and v tendencies
+enum { REC_A, REC_G, REC_B, REC_C, REC_D, REC_E, REC_F, REC_N };
+std::vector<float> fp32c_records(const swm_gpu_ctx *c);  // REC_N * 4 floats per row
+
 struct P32 {
   int nx, ny, nl, mix, qbf, barotropic, has_F, impl_uniform, gsq_uniform, wind_x, wind_y, wind_rows, has_mode;
   float dt, G, minD, lbc, q1, ts_rho, Ah, bih;
@@ -19,7 +33,8 @@ struct P32 {
   float impl_s[3], dp_s[3], gsq_s[2];
   const uint16_t *mask16;
   const float *dp[3];
-  const float *He, *rows, *Hu, *Hv;
+  const float *He, *Hu, *Hv;
+  const float4 *rec;  // per-iteration factor records, REC_N per row
   const float *impl[3], *gsq[2];
   const float *Fx, *Fy, *Fe;
   const float *wx, *wy;

@@ -99,12 +99,10 @@ __device__ __forceinline__ void march_strip(const P32 &p, const int bx, const in
   float pll1[2] = {}, plt1[2] = {}, lu1[2] = {}, lv1[2] = {}, pll2[2] = {}, plt2[2] = {};
   float muh[4] = {}, mul[4] = {}, mvh[3] = {}, mvl[3] = {}, pot[3] = {}, ke[3] = {};
   int off[3] = {};            // row offsets nx * j of rows J, J-1, J-2
-  const float *rr[3] = {};    // per-row factors of rows J, J-1, J-2
 
   int J = ry0 - 3;
   const int jend = min(ry0 + S, ny) + 2;
   int noff = nx * wrapm(J, ny);
-  const float *nrow = p.rows + (size_t)wrapm(J, ny) * Q_NR;
   unsigned n_m = p.mask16[gi + noff];
   float n_uh = p.uh0[gi + noff], n_ul = p.ul0[gi + noff], n_vh = p.vh0[gi + noff], n_vl = p.vl0[gi + noff];
   float n_eh = p.eh0[gi + noff], n_el = p.el0[gi + noff], n_he = p.He[gi + noff];
@@ -123,7 +121,11 @@ __device__ __forceinline__ void march_strip(const P32 &p, const int bx, const in
 #define W4(a_, b_, c_, d_) (FAST ? 0.25f : rcnt((a_) + (b_) + (c_) + (d_)))
 #define HALF2(a_, b_) (FAST ? 0.5f : ((a_) + (b_) > 1 ? 0.5f : 1.f))
     auto dval = [&](int a) { return nl ? (XE(m[a]) ? he[a] + eh[a] : 1.f) : he[a]; };
-    const float *r0 = rr[0], *r1 = rr[1], *r2 = rr[2];
+    const float4 *rec = p.rec + (size_t)wrapm(J, ny) * REC_N;  // factors of rows J, J-1, J-2
+    // all record loads issued first, so their latency overlaps the fluxes
+    const float4 fa = rec[REC_A], fb = rec[REC_B], fc = rec[REC_C], fd = rec[REC_D], fe = rec[REC_E],
+                 ff = rec[REC_F];
+    const float fh = reinterpret_cast<const float *>(rec + REC_G)[0];
     const int o = J - 2;
     const bool upd = o >= ry0 && o < ry0 + S && o < ny && store_lane;
     const int ko = gi + off[2];
@@ -165,15 +167,15 @@ __device__ __forceinline__ void march_strip(const P32 &p, const int bx, const in
         float zeta = 0.f;
         if (nl) {
           float bc = XH(mm) ? 1.f : p.lbc;
-          float dvdx = (XLV(mm) + XV(mm) == 0) ? 0.f : bc * r0[Q_RH_DL] * ((vh[0] - vh0_l) + (vl[0] - vl0_l));
+          float dvdx = (XLV(mm) + XV(mm) == 0) ? 0.f : bc * fa.x * ((vh[0] - vh0_l) + (vl[0] - vl0_l));
           float dudy = (XU(mm) + XU(m[1]) == 0)
                            ? 0.f
-                           : bc * q1 * (r0[Q_CU] * ((uh[0] - uh[1]) + (ul[0] - ul[1])) + r0[Q_DCU] * uh[1]);
-          zeta = dvdx - dudy * r0[Q_INV_CH];
+                           : bc * q1 * (fa.y * ((uh[0] - uh[1]) + (ul[0] - ul[1])) + fa.z * uh[1]);
+          zeta = dvdx - dudy * fa.w;
         }
         unsigned a = XE(mm), b = XLE(m[1]), c = XLE(mm), d = XE(m[1]);
         float dh = ((a ? d0 : 0.f) + (b ? dl1 : 0.f) + (c ? dl0 : 0.f) + (d ? d1 : 0.f)) * W4(a, b, c, d);
-        pv = __fdividef(r0[Q_FH] + zeta, fmaxf(dh, 2.220446e-16f));
+        pv = __fdividef(fh + zeta, fmaxf(dh, 2.220446e-16f));
       }
       pot[0] = pv;
       float k1 = 0.f;
@@ -192,17 +194,17 @@ __device__ __forceinline__ void march_strip(const P32 &p, const int bx, const in
         float pl = 0.f, pt = 0.f;
         if (XE(m1)) {
           unsigned ov = XV(m1), ovp = XV(m0);
-          float tE = r1[Q_TE] * HALF2(ov, ovp);
+          float tE = fb.x * HALF2(ov, ovp);
           float du = (uh1_r - uh[1]) + (ul1_r - ul[1]);
           float dv = (vh[0] - vh[1]) + (vl[0] - vl[1]);
-          pl = r1[Q_PC0] * du + q1 * dv + tE * ((ovp ? vh[0] : 0.f) + (ov ? vh[1] : 0.f));
+          pl = fb.y * du + q1 * dv + tE * ((ovp ? vh[0] : 0.f) + (ov ? vh[1] : 0.f));
         }
         if (XH(m0)) {
           unsigned ou = XU(m0), oum = XU(m1);
-          float tH = r0[Q_TH] * HALF2(ou, oum);
+          float tH = fb.z * HALF2(ou, oum);
           float dv = (vh[0] - vh0_l) + (vl[0] - vl0_l);
           float du = (uh[0] - uh[1]) + (ul[0] - ul[1]);
-          pt = r0[Q_HC0] * dv - q1 * du - tH * ((ou ? uh[0] : 0.f) + (oum ? uh[1] : 0.f));
+          pt = fb.w * dv - q1 * du - tH * ((ou ? uh[0] : 0.f) + (oum ? uh[1] : 0.f));
         }
         pll1[0] = pl;
         plt1[0] = pt;
@@ -212,12 +214,12 @@ __device__ __forceinline__ void march_strip(const P32 &p, const int bx, const in
         const unsigned m1 = m[1];
         float a = 0.f, b = 0.f;
         if (XU(m1)) {
-          float t2 = 2.f * r1[Q_TU] * HALF2(XH(m1), XH(m[0]));
-          a = -r1[Q_RU_DL] * (pll1[0] - pll1_l) + q1 * (plt1[1] - plt1[0]) + t2 * (plt1[0] + plt1[1]);
+          float t2 = 2.f * fc.x * HALF2(XH(m1), XH(m[0]));
+          a = -fc.y * (pll1[0] - pll1_l) + q1 * (plt1[1] - plt1[0]) + t2 * (plt1[0] + plt1[1]);
         }
         if (XV(m1)) {
-          float t2 = 2.f * r1[Q_TV] * HALF2(XE(m1), XE(m[2]));
-          b = -r1[Q_RV_DL] * (plt1_r - plt1[1]) + q1 * (pll1[0] - pll1[1]) - t2 * (pll1[0] + pll1[1]);
+          float t2 = 2.f * fc.z * HALF2(XE(m1), XE(m[2]));
+          b = -fc.w * (plt1_r - plt1[1]) + q1 * (pll1[0] - pll1[1]) - t2 * (pll1[0] + pll1[1]);
         }
         lu1[0] = a;
         lv1[0] = b;
@@ -228,15 +230,15 @@ __device__ __forceinline__ void march_strip(const P32 &p, const int bx, const in
         float pl = 0.f, pt = 0.f;
         if (XE(m2)) {
           unsigned ov = XV(m2), ovp = XV(m1);
-          float tE = r2[Q_TE] * HALF2(ov, ovp);
-          float s = r2[Q_PC0] * (lu1_r - lu1[1]) + q1 * (lv1[0] - lv1[1]) +
+          float tE = fd.x * HALF2(ov, ovp);
+          float s = fd.y * (lu1_r - lu1[1]) + q1 * (lv1[0] - lv1[1]) +
                     tE * ((ovp ? lv1[0] : 0.f) + (ov ? lv1[1] : 0.f));
           pl = -p.bih * d2 * s;
         }
         if (XH(m1)) {
           unsigned ou = XU(m1), oum = XU(m2);
-          float tH = r1[Q_TH] * HALF2(ou, oum);
-          float s = r1[Q_HC0] * (lv1[0] - lv1_l) - q1 * (lu1[0] - lu1[1]) -
+          float tH = fd.z * HALF2(ou, oum);
+          float s = fd.w * (lv1[0] - lv1_l) - q1 * (lu1[0] - lu1[1]) -
                     tH * ((ou ? lu1[0] : 0.f) + (oum ? lu1[1] : 0.f));
           unsigned a = XE(m1), b = XLE(m2), c = XLE(m1), d = XE(m2);
           float dh = ((a ? d1 : 0.f) + (b ? dl2 : 0.f) + (c ? dl1 : 0.f) + (d ? d2 : 0.f)) * W4(a, b, c, d);
@@ -252,18 +254,18 @@ __device__ __forceinline__ void march_strip(const P32 &p, const int bx, const in
       float pl = 0.f, pt = 0.f;
       if (XE(m2)) {
         unsigned ov = XV(m2), ovp = XV(m1);
-        float tE = r2[Q_TE] * HALF2(ov, ovp);
+        float tE = fd.x * HALF2(ov, ovp);
         float du = (uh2_r - uh[2]) + (ul2_r - ul[2]);
         float dv = (vh[1] - vh[2]) + (vl[1] - vl[2]);
-        float s = r2[Q_PC0] * du + q1 * dv + tE * ((ovp ? vh[1] : 0.f) + (ov ? vh[2] : 0.f));
+        float s = fd.y * du + q1 * dv + tE * ((ovp ? vh[1] : 0.f) + (ov ? vh[2] : 0.f));
         pl = p.Ah * d2 * s;
       }
       if (XH(m1)) {
         unsigned ou = XU(m1), oum = XU(m2);
-        float tH = r1[Q_TH] * HALF2(ou, oum);
+        float tH = fd.z * HALF2(ou, oum);
         float dv = (vh[1] - vh1_l) + (vl[1] - vl1_l);
         float du = (uh[1] - uh[2]) + (ul[1] - ul[2]);
-        float s = r1[Q_HC0] * dv - q1 * du - tH * ((ou ? uh[1] : 0.f) + (oum ? uh[2] : 0.f));
+        float s = fd.w * dv - q1 * du - tH * ((ou ? uh[1] : 0.f) + (oum ? uh[2] : 0.f));
         unsigned a = XE(m1), b = XLE(m2), c = XLE(m1), d = XE(m2);
         float dh = ((a ? d1 : 0.f) + (b ? dl2 : 0.f) + (c ? dl1 : 0.f) + (d ? d2 : 0.f)) * W4(a, b, c, d);
         pt = p.Ah * dh * s;
@@ -297,15 +299,15 @@ __device__ __forceinline__ void march_strip(const P32 &p, const int bx, const in
         are = area[2 * ny + o];
       }
       if (XE(mm)) {
-        float dmv = r1[Q_CV] * ((mvh[1] - mvh[2]) + (mvl[1] - mvl[2])) + r1[Q_DCV] * mvh[2];
-        ge = -((muh2_r - muh[2]) + (mul2_r - mul[2])) * r2[Q_RE_DL] - dmv * r2[Q_RE_DT];
+        float dmv = fe.x * ((mvh[1] - mvh[2]) + (mvl[1] - mvl[2])) + fe.y * mvh[2];
+        ge = -((muh2_r - muh[2]) + (mul2_r - mul[2])) * fe.z - dmv * fe.w;
         if (p.has_F) ge += p.Fe[ko];
       }
       if (XU(mm)) {
         float pv = 0.5f * (pot[1] + pot[2]);
         float mv = 0.25f * ((mvs1 + mvs2_l) + (mvs1_l + mvs2));
         float dE = G * ((eh[2] - eh2_l) + (el[2] - el2_l)) + (ke[1] - ke1_l);
-        float g = pv * mv - dE * r2[Q_RU_DL];
+        float g = pv * mv - dE * ff.x;
         unsigned a = XE(mm), b = XLE(mm);
         float du = ((a ? d2 : 0.f) + (b ? dl2 : 0.f)) * W2(a, b);
         if (p.qbf) {
@@ -316,8 +318,8 @@ __device__ __forceinline__ void march_strip(const P32 &p, const int bx, const in
           g -= f;
         }
         if (MIX) {
-          float t2 = 2.f * r2[Q_TU] * HALF2(XH(mm), XH(m[1]));
-          float lat = -r2[Q_RU_DL] * (pll2[0] - pll2_l) + q1 * (plt2[1] - plt2[0]) + t2 * (plt2[0] + plt2[1]);
+          float t2 = 2.f * ff.y * HALF2(XH(mm), XH(m[1]));
+          float lat = -ff.x * (pll2[0] - pll2_l) + q1 * (plt2[1] - plt2[0]) + t2 * (plt2[0] + plt2[1]);
           g += __fdividef(lat, du);
         }
         if (p.has_F) g += p.Fx[ko];
@@ -339,8 +341,8 @@ __device__ __forceinline__ void march_strip(const P32 &p, const int bx, const in
           g -= f;
         }
         if (MIX) {
-          float t2 = 2.f * r2[Q_TV] * HALF2(XE(mm), XE(m[3]));
-          float lat = -r2[Q_RV_DL] * (plt2_r - plt2[1]) + q1 * (pll2[0] - pll2[1]) - t2 * (pll2[0] + pll2[1]);
+          float t2 = 2.f * ff.z * HALF2(XE(mm), XE(m[3]));
+          float lat = -ff.w * (plt2_r - plt2[1]) + q1 * (pll2[0] - pll2[1]) - t2 * (pll2[0] + pll2[1]);
           g += __fdividef(lat, dv);
         }
         if (p.has_F) g += p.Fy[ko];
@@ -433,18 +435,16 @@ __device__ __forceinline__ void march_strip(const P32 &p, const int bx, const in
 #pragma unroll
     for (int a = 2; a > 0; a--) {
       mvh[a] = mvh[a - 1]; mvl[a] = mvl[a - 1]; pot[a] = pot[a - 1]; ke[a] = ke[a - 1];
-      off[a] = off[a - 1]; rr[a] = rr[a - 1];
+      off[a] = off[a - 1];
     }
     pll1[1] = pll1[0]; plt1[1] = plt1[0]; lu1[1] = lu1[0]; lv1[1] = lv1[0];
     pll2[1] = pll2[0]; plt2[1] = plt2[0];
     m[0] = n_m; uh[0] = n_uh; ul[0] = n_ul; vh[0] = n_vh; vl[0] = n_vl;
     eh[0] = n_eh; el[0] = n_el; he[0] = n_he;
     off[0] = noff;
-    rr[0] = nrow;
     if (J + 1 < jend) {  // prefetch row J+1
       int jw = wrapm(J + 1, ny);
       noff = nx * jw;
-      nrow = p.rows + (size_t)jw * Q_NR;
       const int kn = gi + noff;
       n_m = p.mask16[kn];
       n_uh = p.uh0[kn]; n_ul = p.ul0[kn]; n_vh = p.vh0[kn]; n_vl = p.vl0[kn];
@@ -620,6 +620,29 @@ std::vector<double> fp32c_rows(const swm_gpu_ctx *c) {
     r[Q_TV] = g.tanl[GV][j] / A;
   }
   return rows;
+}
+
+// the per-iteration records of the step kernel (fused32.h): record J holds
+// the factors iteration J reads from rows J, J-1 and J-2 (periodic in j)
+std::vector<float> fp32c_records(const swm_gpu_ctx *c) {
+  const int ny = c->ny;
+  const std::vector<double> r = fp32c_rows(c);
+  std::vector<float> rec((size_t)ny * REC_N * 4, 0.f);
+  auto q = [&](int j, int k) { return (float)r[(size_t)(((j % ny) + ny) % ny) * Q_NR + k]; };
+  for (int J = 0; J < ny; J++) {
+    float *o = &rec[(size_t)J * REC_N * 4];
+    const float a[REC_N][4] = {
+        {q(J, Q_RH_DL), q(J, Q_CU), q(J, Q_DCU), q(J, Q_INV_CH)},
+        {q(J, Q_FH), 0.f, 0.f, 0.f},
+        {q(J - 1, Q_TE), q(J - 1, Q_PC0), q(J, Q_TH), q(J, Q_HC0)},
+        {q(J - 1, Q_TU), q(J - 1, Q_RU_DL), q(J - 1, Q_TV), q(J - 1, Q_RV_DL)},
+        {q(J - 2, Q_TE), q(J - 2, Q_PC0), q(J - 1, Q_TH), q(J - 1, Q_HC0)},
+        {q(J - 1, Q_CV), q(J - 1, Q_DCV), q(J - 2, Q_RE_DL), q(J - 2, Q_RE_DT)},
+        {q(J - 2, Q_RU_DL), q(J - 2, Q_TU), q(J - 2, Q_TV), q(J - 2, Q_RV_DL)}};
+    for (int g = 0; g < REC_N; g++)
+      for (int k = 0; k < 4; k++) o[4 * g + k] = a[g][k];
+  }
+  return rec;
 }
 
 int march_tile_cols(int mix) { return 32 - 2 * (mix == 2 ? 2 : 1); }
