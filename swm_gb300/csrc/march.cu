@@ -81,7 +81,7 @@ __device__ __forceinline__ void comp_damp(float hi, float lo, float inc, float d
 // the new state of its ocean points, times the cell area of the point's row
 // (area: 3 x ny (hi, lo) pairs, u, v, eta rows), into acc[4]: eta, eta^2,
 // u^2, v^2.
-template <int MIX, bool INTEG = false>
+template <int MIX, bool INTEG = false, bool STD = false>
 __device__ __forceinline__ void march_strip(const P32 &p, const int bx, const int ry0, const int lane, const int S,
                                             const float2 *area = nullptr, F2 *acc = nullptr) {
   constexpr int H = MIX == 2 ? 2 : 1;
@@ -89,7 +89,9 @@ __device__ __forceinline__ void march_strip(const P32 &p, const int bx, const in
   const int nx = p.nx, ny = p.ny;
   const int gx = bx * TI - H + lane;
   const int gi = wrapm(gx, nx);
-  const bool nl = p.nl;
+  // STD: the configuration flags of march_std() hold, as compile-time constants
+  const bool nl = STD || p.nl, has_mode = STD || p.has_mode, qbf = !STD && p.qbf, has_F = !STD && p.has_F;
+  const bool impl_uniform = STD || p.impl_uniform, wind_rows = STD || p.wind_rows;
   const bool store_lane = lane >= H && lane < 32 - H && gx < nx;
   const float q1 = p.q1, G = p.G;
 
@@ -163,7 +165,7 @@ __device__ __forceinline__ void march_strip(const P32 &p, const int bx, const in
       }
       mvh[0] = b_h; mvl[0] = b_l;
       float pv = 0.f;
-      if (p.has_mode) {
+      if (has_mode) {
         float zeta = 0.f;
         if (nl) {
           float bc = XH(mm) ? 1.f : p.lbc;
@@ -301,7 +303,7 @@ __device__ __forceinline__ void march_strip(const P32 &p, const int bx, const in
       if (XE(mm)) {
         float dmv = fe.x * ((mvh[1] - mvh[2]) + (mvl[1] - mvl[2])) + fe.y * mvh[2];
         ge = -((muh2_r - muh[2]) + (mul2_r - mul[2])) * fe.z - dmv * fe.w;
-        if (p.has_F) ge += p.Fe[ko];
+        if (has_F) ge += p.Fe[ko];
       }
       if (XU(mm)) {
         float pv = 0.5f * (pot[1] + pot[2]);
@@ -310,7 +312,7 @@ __device__ __forceinline__ void march_strip(const P32 &p, const int bx, const in
         float g = pv * mv - dE * ff.x;
         unsigned a = XE(mm), b = XLE(mm);
         float du = ((a ? d2 : 0.f) + (b ? dl2 : 0.f)) * W2(a, b);
-        if (p.qbf) {
+        if (qbf) {
           float vb = 0.25f * ((vh[1] + vh2_l) + (vh1_lo + vh[2]));
           float gs = p.gsq_uniform ? p.gsq_s[0] : p.gsq[0][ko];
           float f = gs * sqrtf(uh[2] * uh[2] + vb * vb) * uh[2];
@@ -322,8 +324,8 @@ __device__ __forceinline__ void march_strip(const P32 &p, const int bx, const in
           float lat = -ff.x * (pll2[0] - pll2_l) + q1 * (plt2[1] - plt2[0]) + t2 * (plt2[0] + plt2[1]);
           g += __fdividef(lat, du);
         }
-        if (p.has_F) g += p.Fx[ko];
-        if (p.wind_x) g += __fdividef(p.ts_rho * (p.wind_rows ? p.wx[o] : p.wx[ko]), nl ? du : 1.f);
+        if (has_F) g += p.Fx[ko];
+        if (p.wind_x) g += __fdividef(p.ts_rho * (wind_rows ? p.wx[o] : p.wx[ko]), nl ? du : 1.f);
         gu = g;
       }
       if (XV(mm)) {
@@ -333,7 +335,7 @@ __device__ __forceinline__ void march_strip(const P32 &p, const int bx, const in
         float g = -pv * mu - dE * q1;
         unsigned a = XE(mm), b = XE(m[3]);
         float dv = ((a ? d2 : 0.f) + (b ? d3 : 0.f)) * W2(a, b);
-        if (p.qbf) {
+        if (qbf) {
           float ub = 0.25f * ((uh2_r + uh[3]) + (uh[2] + uh3_r));
           float gs = p.gsq_uniform ? p.gsq_s[1] : p.gsq[1][ko];
           float f = gs * sqrtf(vh[2] * vh[2] + ub * ub) * vh[2];
@@ -345,15 +347,15 @@ __device__ __forceinline__ void march_strip(const P32 &p, const int bx, const in
           float lat = -ff.w * (plt2_r - plt2[1]) + q1 * (pll2[0] - pll2[1]) - t2 * (pll2[0] + pll2[1]);
           g += __fdividef(lat, dv);
         }
-        if (p.has_F) g += p.Fy[ko];
-        if (p.wind_y) g += __fdividef(p.ts_rho * (p.wind_rows ? p.wy[o] : p.wy[ko]), nl ? dv : 1.f);
+        if (has_F) g += p.Fy[ko];
+        if (p.wind_y) g += __fdividef(p.ts_rho * (wind_rows ? p.wy[o] : p.wy[ko]), nl ? dv : 1.f);
         gv = g;
       }
       p.Ge3[ko] = ge;
       p.Gu3[ko] = gu;
       p.Gv3[ko] = gv;
       float dpu, dpv, dpe;
-      if (p.impl_uniform) {
+      if (impl_uniform) {
         dpu = p.dp_s[0]; dpv = p.dp_s[1]; dpe = p.dp_s[2];
       } else {
         dpu = p.dp[0][ko]; dpv = p.dp[1][ko]; dpe = p.dp[2][ko];
@@ -544,7 +546,7 @@ void march_integrals_final(const double *partial, int nb, double G, double *out,
 // groups of one strip, so their look-ahead rows overlap and meet in L1.
 // INTEG (a monitored step, MarchInteg): block 0 does the side jobs and the
 // strip blocks are blockIdx.x - 1; they sum the new state as well.
-template <int MIX, bool INTEG>
+template <int MIX, bool INTEG, bool STD>
 __global__ void __launch_bounds__(128, MARCH_MINB) k_march(P32 p, const int2 *__restrict__ tiles, MarchInteg mi) {
   const int lane = threadIdx.x & 31;
   int b = blockIdx.x;
@@ -559,7 +561,7 @@ __global__ void __launch_bounds__(128, MARCH_MINB) k_march(P32 p, const int2 *__
   const int2 t = tiles[4 * b + (threadIdx.x >> 5)];
   const int S = t.y & 255;
   F2 acc[4];
-  if (S > 0) march_strip<MIX, INTEG>(p, t.x, t.y >> 8, lane, S, mi.area, acc);
+  if (S > 0) march_strip<MIX, INTEG, STD>(p, t.x, t.y >> 8, lane, S, mi.area, acc);
   if (INTEG) {
     grid_dep_trigger();
     march_integrals_block(mi, acc, b, gridDim.x - 1);
@@ -738,15 +740,30 @@ extern "C" int swm_gpu_plan_step_tiles(int mixing, int nx, int ny, const uint16_
 
 namespace swm {
 
-template <int MIX>
-static void launch_mix(const P32 &p, const MarchGrid &g, cudaStream_t st, const MarchInteg *mi) {
+// the common configuration the STD variant of the step kernel serves:
+// nonlinear with a linearisation, no quadratic drag, no extra forcing field,
+// uniform damping, wind (if any) as row profiles
+static bool march_std(const P32 &p) {
+  return p.nl && p.has_mode && !p.qbf && !p.has_F && p.impl_uniform && (p.wind_rows || (!p.wind_x && !p.wind_y));
+}
+
+template <int MIX, bool STD>
+static void launch_mix_s(const P32 &p, const MarchGrid &g, cudaStream_t st, const MarchInteg *mi) {
   if (!mi) {
-    k_march<MIX, false><<<g.blocks, 128, 0, st>>>(p, g.tiles, MarchInteg{});
+    k_march<MIX, false, STD><<<g.blocks, 128, 0, st>>>(p, g.tiles, MarchInteg{});
     return;
   }
   // one more block for the side jobs
-  if (mi->programmatic) launch_programmatic(k_march<MIX, true>, dim3(g.blocks + 1), dim3(128), st, p, g.tiles, *mi);
-  else k_march<MIX, true><<<g.blocks + 1, 128, 0, st>>>(p, g.tiles, *mi);
+  if (mi->programmatic)
+    launch_programmatic(k_march<MIX, true, STD>, dim3(g.blocks + 1), dim3(128), st, p, g.tiles, *mi);
+  else
+    k_march<MIX, true, STD><<<g.blocks + 1, 128, 0, st>>>(p, g.tiles, *mi);
+}
+
+template <int MIX>
+static void launch_mix(const P32 &p, const MarchGrid &g, cudaStream_t st, const MarchInteg *mi) {
+  if (march_std(p)) launch_mix_s<MIX, true>(p, g, st, mi);
+  else launch_mix_s<MIX, false>(p, g, st, mi);
 }
 
 static void launch_any(const P32 &p, const MarchGrid &g, cudaStream_t st, const MarchInteg *mi = nullptr) {
@@ -830,21 +847,24 @@ int march_pick_rows(cudaStream_t st, int reps, const std::vector<int> &cands, co
   return SWM_GPU_OK;
 }
 
-template <int MIX>
+template <int MIX, bool STD>
 static int resident_blocks_of() {  // blocks of k_march resident on the whole GPU at once
   static int b = 0;
   if (!b) {
     int per_sm = 0, sms = 0, dev = 0;
     cudaGetDevice(&dev);
     cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_march<MIX, false>, 128, 0);
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_march<MIX, false, STD>, 128, 0);
     b = sms * (per_sm > 0 ? per_sm : 1);
   }
   return b;
 }
 
-static int resident_blocks(int mix) {
-  return mix == 2 ? resident_blocks_of<2>() : (mix == 1 ? resident_blocks_of<1>() : resident_blocks_of<0>());
+static int resident_blocks(const P32 &p) {
+  const bool s = march_std(p);
+  if (p.mix == 2) return s ? resident_blocks_of<2, true>() : resident_blocks_of<2, false>();
+  if (p.mix == 1) return s ? resident_blocks_of<1, true>() : resident_blocks_of<1, false>();
+  return s ? resident_blocks_of<0, true>() : resident_blocks_of<0, false>();
 }
 
 // Tiles of the step kernel, by timing the step on this basin.  A kernel is
@@ -870,7 +890,7 @@ int march_autotune(swm_gpu_ctx *c, const P32 &p, const uint16_t *m16) {
   if (s_env > 0.) {
     add(s_env, w_env > 0. ? w_env : 1.);
   } else {
-    const int R = resident_blocks(p.mix);
+    const int R = resident_blocks(p);
     add(16., 1.);
     for (double w : MARCH_TUNE_SLOW) {
       if (w_env > 0. && w != MARCH_TUNE_SLOW[0]) continue;
