@@ -74,6 +74,7 @@ struct swm_gpu_ensemble {
   std::vector<swm_gpu_ctx *> m;
   int mix = 0, rows = 16, phase = 0, graph_phase = -1;
   double slow = 1.;  // masked-row cost the tiles were cut with
+  bool std_cfg = false;  // all members in the step kernel's common configuration
   cudaStream_t stream = nullptr;
   cudaEvent_t done = nullptr;
   std::vector<cudaEvent_t> ev;
@@ -122,8 +123,8 @@ int rotate_members(swm_gpu_ensemble *e, int64_t itt) {
 int ens_step(swm_gpu_ensemble *e, int64_t itt) {
   const size_t n = e->m.size();
   SWM_CK(cudaMemsetAsync(e->next + e->phase, 0, sizeof(int), e->stream));
-  int rc = march_ens_launch(e->mix, e->tab + (size_t)e->phase * n, e->tiles, e->ntiles, e->next + e->phase,
-                            e->stream);
+  int rc = march_ens_launch(e->mix, e->std_cfg, e->tab + (size_t)e->phase * n, e->tiles, e->ntiles,
+                            e->next + e->phase, e->stream);
   if (rc != SWM_GPU_OK) return rc;
   e->launches++;
   return rotate_members(e, itt);
@@ -222,6 +223,8 @@ int swm_gpu_ensemble_create(swm_gpu_ctx *const *members, int n, swm_gpu_ensemble
       make_p32(members[i], 3, tab[(size_t)k * n + i]);
     }
   for (int i = 0; i < n; i++) fused_set_indices(members[i], n0, g0);
+  e->std_cfg = true;
+  for (const P32 &q : tab) e->std_cfg = e->std_cfg && march_std_params(q);
   // Tiles: every member's strips cut into row groups of equal estimated
   // cost (as the single-basin step kernel's tiles), all members' tiles in
   // one queue with the short remainder groups last, so the queue ends on
@@ -290,7 +293,7 @@ int swm_gpu_ensemble_create(swm_gpu_ctx *const *members, int n, swm_gpu_ensemble
         uploaded = r;
       }
       cudaMemsetAsync(e->next, 0, sizeof(int), e->stream);
-      march_ens_launch(mix, e->tab, e->tiles, (int)lists[r].size(), e->next, e->stream);
+      march_ens_launch(mix, e->std_cfg, e->tab, e->tiles, (int)lists[r].size(), e->next, e->stream);
     }, &best);
   if (rc != SWM_GPU_OK) return fail(rc);
   if (cudaMemcpyAsync(e->tiles, lists[best].data(), lists[best].size() * sizeof(int4), cudaMemcpyHostToDevice,

@@ -163,6 +163,10 @@ void fused_set_indices(swm_gpu_ctx *c, int n0, int g0);
 void fused_pair_level(const swm_gpu_ctx *c, const float *out[6]);
 void fused_static(const swm_gpu_ctx *c, const float **He, const uint16_t **mask16, const float **Fe);
 // one launch of the ensemble step: tiles {member, strip, first row, rows}
-int march_ens_launch(int mix, const P32 *tab, const int4 *tiles, int ntiles, int *next, cudaStream_t st);
+// std_cfg: every member's parameter block is of the common configuration
+// (march_std_params), so the kernel's specialised instance serves them
+int march_ens_launch(int mix, bool std_cfg, const P32 *tab, const int4 *tiles, int ntiles, int *next,
+                     cudaStream_t st);
+bool march_std_params(const P32 &p);
 
 }  // namespace swm

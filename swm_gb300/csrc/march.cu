@@ -572,7 +572,7 @@ __global__ void __launch_bounds__(128, MARCH_MINB) k_march(P32 p, const int2 *__
 // the queue until it is empty.  A tile is int4 {member, strip, first row,
 // rows}; the member's parameter block is copied into the warp's slice of
 // shared memory first.
-template <int MIX>
+template <int MIX, bool STD>
 __global__ void __launch_bounds__(128, MARCH_MINB) k_march_ens(const P32 *__restrict__ tab,
                                                                const int4 *__restrict__ tiles, int ntiles,
                                                                int *__restrict__ next) {
@@ -588,7 +588,7 @@ __global__ void __launch_bounds__(128, MARCH_MINB) k_march_ens(const P32 *__rest
     int *dst = reinterpret_cast<int *>(&sp[warp]);
     for (int k = lane; k < (int)(sizeof(P32) / sizeof(int)); k += 32) dst[k] = src[k];
     __syncwarp();
-    march_strip<MIX>(sp[warp], d.y, d.z, lane, d.w);
+    march_strip<MIX, false, STD>(sp[warp], d.y, d.z, lane, d.w);
     __syncwarp();
   }
 }
@@ -935,25 +935,33 @@ int march_autotune(swm_gpu_ctx *c, const P32 &p, const uint16_t *m16) {
 }
 
 // ---- ensemble launch ------------------------------------------------------
-template <int MIX>
+template <int MIX, bool STD>
 static int ens_launch_m(const P32 *tab, const int4 *tiles, int ntiles, int *next, cudaStream_t st) {
   static int blocks = 0;
   if (!blocks) {
     int per_sm = 0, sms = 0, dev = 0;
     SWM_CK(cudaGetDevice(&dev));
     SWM_CK(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
-    SWM_CK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_march_ens<MIX>, 128, 0));
+    SWM_CK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_march_ens<MIX, STD>, 128, 0));
     blocks = sms * (per_sm > 0 ? per_sm : 1);
   }
   int need = (ntiles + 3) / 4;
-  k_march_ens<MIX><<<need < blocks ? need : blocks, 128, 0, st>>>(tab, tiles, ntiles, next);
+  k_march_ens<MIX, STD><<<need < blocks ? need : blocks, 128, 0, st>>>(tab, tiles, ntiles, next);
   return SWM_GPU_OK;
 }
 
-int march_ens_launch(int mix, const P32 *tab, const int4 *tiles, int ntiles, int *next, cudaStream_t st) {
-  if (mix == 2) return ens_launch_m<2>(tab, tiles, ntiles, next, st);
-  if (mix == 1) return ens_launch_m<1>(tab, tiles, ntiles, next, st);
-  return ens_launch_m<0>(tab, tiles, ntiles, next, st);
+bool march_std_params(const P32 &p) { return march_std(p); }
+
+int march_ens_launch(int mix, bool std_cfg, const P32 *tab, const int4 *tiles, int ntiles, int *next,
+                     cudaStream_t st) {
+  if (mix == 2)
+    return std_cfg ? ens_launch_m<2, true>(tab, tiles, ntiles, next, st)
+                   : ens_launch_m<2, false>(tab, tiles, ntiles, next, st);
+  if (mix == 1)
+    return std_cfg ? ens_launch_m<1, true>(tab, tiles, ntiles, next, st)
+                   : ens_launch_m<1, false>(tab, tiles, ntiles, next, st);
+  return std_cfg ? ens_launch_m<0, true>(tab, tiles, ntiles, next, st)
+                 : ens_launch_m<0, false>(tab, tiles, ntiles, next, st);
 }
 
 }  // namespace swm
