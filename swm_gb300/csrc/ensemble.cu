@@ -75,6 +75,7 @@ struct swm_gpu_ensemble {
   int mix = 0, rows = 16, phase = 0, graph_phase = -1;
   double slow = 1.;  // masked-row cost the tiles were cut with
   bool std_cfg = false;  // all members in the step kernel's common configuration
+  bool pf = false;       // the members' state is larger than L2: prefetch rows
   cudaStream_t stream = nullptr;
   cudaEvent_t done = nullptr;
   std::vector<cudaEvent_t> ev;
@@ -123,7 +124,7 @@ int rotate_members(swm_gpu_ensemble *e, int64_t itt) {
 int ens_step(swm_gpu_ensemble *e, int64_t itt) {
   const size_t n = e->m.size();
   SWM_CK(cudaMemsetAsync(e->next + e->phase, 0, sizeof(int), e->stream));
-  int rc = march_ens_launch(e->mix, e->std_cfg, e->tab + (size_t)e->phase * n, e->tiles, e->ntiles,
+  int rc = march_ens_launch(e->mix, e->std_cfg, e->pf, e->tab + (size_t)e->phase * n, e->tiles, e->ntiles,
                             e->next + e->phase, e->stream);
   if (rc != SWM_GPU_OK) return rc;
   e->launches++;
@@ -225,6 +226,9 @@ int swm_gpu_ensemble_create(swm_gpu_ctx *const *members, int n, swm_gpu_ensemble
   for (int i = 0; i < n; i++) fused_set_indices(members[i], n0, g0);
   e->std_cfg = true;
   for (const P32 &q : tab) e->std_cfg = e->std_cfg && march_std_params(q);
+  size_t points = 0;
+  for (int i = 0; i < n; i++) points += (size_t)members[i]->nx * members[i]->ny;
+  e->pf = march_prefetch(points);
   // Tiles: every member's strips cut into row groups of equal estimated
   // cost (as the single-basin step kernel's tiles), all members' tiles in
   // one queue with the short remainder groups last, so the queue ends on
@@ -293,7 +297,7 @@ int swm_gpu_ensemble_create(swm_gpu_ctx *const *members, int n, swm_gpu_ensemble
         uploaded = r;
       }
       cudaMemsetAsync(e->next, 0, sizeof(int), e->stream);
-      march_ens_launch(mix, e->std_cfg, e->tab, e->tiles, (int)lists[r].size(), e->next, e->stream);
+      march_ens_launch(mix, e->std_cfg, e->pf, e->tab, e->tiles, (int)lists[r].size(), e->next, e->stream);
     }, &best);
   if (rc != SWM_GPU_OK) return fail(rc);
   if (cudaMemcpyAsync(e->tiles, lists[best].data(), lists[best].size() * sizeof(int4), cudaMemcpyHostToDevice,

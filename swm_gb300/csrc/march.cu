@@ -42,11 +42,14 @@
 #define MARCH_INTEG_HOIST 1
 #endif
 
+
 namespace swm {
 
 constexpr unsigned FULL = 0xffffffffu;
 __device__ __forceinline__ float shl(float x) { return __shfl_up_sync(FULL, x, 1); }    // lane - 1
 __device__ __forceinline__ float shr(float x) { return __shfl_down_sync(FULL, x, 1); }  // lane + 1
+
+__device__ __forceinline__ void prefetch_l2(const void *a) { asm volatile("prefetch.global.L2 [%0];" ::"l"(a)); }
 
 __device__ __forceinline__ int wrapm(int g, int n) {
   g = g < 0 ? g + n : g;
@@ -81,7 +84,10 @@ __device__ __forceinline__ void comp_damp(float hi, float lo, float inc, float d
 // the new state of its ocean points, times the cell area of the point's row
 // (area: 3 x ny (hi, lo) pairs, u, v, eta rows), into acc[4]: eta, eta^2,
 // u^2, v^2.
-template <int MIX, bool INTEG = false, bool STD = false>
+// PF: each iteration also asks L2 for the input rows two ahead and for the
+// next output row's increments (prefetch.global.L2, no registers), for a
+// state larger than L2, which every step reads from DRAM (march_prefetch).
+template <int MIX, bool INTEG = false, bool STD = false, bool PF = false>
 __device__ __forceinline__ void march_strip(const P32 &p, const int bx, const int ry0, const int lane, const int S,
                                             const float2 *area = nullptr, F2 *acc = nullptr) {
   constexpr int H = MIX == 2 ? 2 : 1;
@@ -452,6 +458,19 @@ __device__ __forceinline__ void march_strip(const P32 &p, const int bx, const in
       n_uh = p.uh0[kn]; n_ul = p.ul0[kn]; n_vh = p.vh0[kn]; n_vl = p.vl0[kn];
       n_eh = p.eh0[kn]; n_el = p.el0[kn]; n_he = p.He[kn];
     }
+    if (PF) {
+      if (J + 2 < jend) {  // the input rows two ahead
+        const int k2 = gi + nx * wrapm(J + 2, ny);
+        prefetch_l2(p.mask16 + k2);
+        prefetch_l2(p.uh0 + k2); prefetch_l2(p.ul0 + k2); prefetch_l2(p.vh0 + k2); prefetch_l2(p.vl0 + k2);
+        prefetch_l2(p.eh0 + k2); prefetch_l2(p.el0 + k2); prefetch_l2(p.He + k2);
+      }
+      if (store_lane && J - 1 >= ry0 && J - 1 < ry0 + S && J - 1 < ny) {  // the next output row's increments
+        const int k1 = gi + off[1];
+        prefetch_l2(p.Ge1 + k1); prefetch_l2(p.Ge2 + k1); prefetch_l2(p.Gu1 + k1);
+        prefetch_l2(p.Gu2 + k1); prefetch_l2(p.Gv1 + k1); prefetch_l2(p.Gv2 + k1);
+      }
+    }
     // rows ry0-3 and ry0-2 only fill the windows: nothing computed from them
     // reaches an output row (the first, ry0, needs first-pass stresses from
     // row ry0-2 on, formed once row ry0-1 is in)
@@ -546,7 +565,7 @@ void march_integrals_final(const double *partial, int nb, double G, double *out,
 // groups of one strip, so their look-ahead rows overlap and meet in L1.
 // INTEG (a monitored step, MarchInteg): block 0 does the side jobs and the
 // strip blocks are blockIdx.x - 1; they sum the new state as well.
-template <int MIX, bool INTEG, bool STD>
+template <int MIX, bool INTEG, bool STD, bool PF>
 __global__ void __launch_bounds__(128, MARCH_MINB) k_march(P32 p, const int2 *__restrict__ tiles, MarchInteg mi) {
   const int lane = threadIdx.x & 31;
   int b = blockIdx.x;
@@ -561,7 +580,7 @@ __global__ void __launch_bounds__(128, MARCH_MINB) k_march(P32 p, const int2 *__
   const int2 t = tiles[4 * b + (threadIdx.x >> 5)];
   const int S = t.y & 255;
   F2 acc[4];
-  if (S > 0) march_strip<MIX, INTEG, STD>(p, t.x, t.y >> 8, lane, S, mi.area, acc);
+  if (S > 0) march_strip<MIX, INTEG, STD, PF>(p, t.x, t.y >> 8, lane, S, mi.area, acc);
   if (INTEG) {
     grid_dep_trigger();
     march_integrals_block(mi, acc, b, gridDim.x - 1);
@@ -572,7 +591,7 @@ __global__ void __launch_bounds__(128, MARCH_MINB) k_march(P32 p, const int2 *__
 // the queue until it is empty.  A tile is int4 {member, strip, first row,
 // rows}; the member's parameter block is copied into the warp's slice of
 // shared memory first.
-template <int MIX, bool STD>
+template <int MIX, bool STD, bool PF>
 __global__ void __launch_bounds__(128, MARCH_MINB) k_march_ens(const P32 *__restrict__ tab,
                                                                const int4 *__restrict__ tiles, int ntiles,
                                                                int *__restrict__ next) {
@@ -588,7 +607,7 @@ __global__ void __launch_bounds__(128, MARCH_MINB) k_march_ens(const P32 *__rest
     int *dst = reinterpret_cast<int *>(&sp[warp]);
     for (int k = lane; k < (int)(sizeof(P32) / sizeof(int)); k += 32) dst[k] = src[k];
     __syncwarp();
-    march_strip<MIX, false, STD>(sp[warp], d.y, d.z, lane, d.w);
+    march_strip<MIX, false, STD, PF>(sp[warp], d.y, d.z, lane, d.w);
     __syncwarp();
   }
 }
@@ -747,23 +766,43 @@ static bool march_std(const P32 &p) {
   return p.nl && p.has_mode && !p.qbf && !p.has_F && p.impl_uniform && (p.wind_rows || (!p.wind_x && !p.wind_y));
 }
 
-template <int MIX, bool STD>
+// Is a state of `points` array points larger than L2, so that the step
+// kernel should prefetch its rows (89 bytes move per point and step)?
+bool march_prefetch(size_t points) {
+  const char *e = getenv("SWM_GB300_MARCH_PREFETCH");  // 0 or 1 forces the choice
+  if (e && (e[0] == '0' || e[0] == '1') && e[1] == 0) return e[0] == '1';
+  static long long l2 = -1;
+  if (l2 < 0) {
+    int dev = 0, v = 0;
+    cudaGetDevice(&dev);
+    l2 = cudaDeviceGetAttribute(&v, cudaDevAttrL2CacheSize, dev) == cudaSuccess ? v : 0;
+  }
+  return 89.0 * (double)points > (double)l2;
+}
+
+template <int MIX, bool STD, bool PF>
 static void launch_mix_s(const P32 &p, const MarchGrid &g, cudaStream_t st, const MarchInteg *mi) {
   if (!mi) {
-    k_march<MIX, false, STD><<<g.blocks, 128, 0, st>>>(p, g.tiles, MarchInteg{});
+    k_march<MIX, false, STD, PF><<<g.blocks, 128, 0, st>>>(p, g.tiles, MarchInteg{});
     return;
   }
   // one more block for the side jobs
   if (mi->programmatic)
-    launch_programmatic(k_march<MIX, true, STD>, dim3(g.blocks + 1), dim3(128), st, p, g.tiles, *mi);
+    launch_programmatic(k_march<MIX, true, STD, PF>, dim3(g.blocks + 1), dim3(128), st, p, g.tiles, *mi);
   else
-    k_march<MIX, true, STD><<<g.blocks + 1, 128, 0, st>>>(p, g.tiles, *mi);
+    k_march<MIX, true, STD, PF><<<g.blocks + 1, 128, 0, st>>>(p, g.tiles, *mi);
 }
 
 template <int MIX>
 static void launch_mix(const P32 &p, const MarchGrid &g, cudaStream_t st, const MarchInteg *mi) {
-  if (march_std(p)) launch_mix_s<MIX, true>(p, g, st, mi);
-  else launch_mix_s<MIX, false>(p, g, st, mi);
+  const bool pf = march_prefetch((size_t)p.nx * p.ny);
+  if (march_std(p)) {
+    if (pf) launch_mix_s<MIX, true, true>(p, g, st, mi);
+    else launch_mix_s<MIX, true, false>(p, g, st, mi);
+  } else {
+    if (pf) launch_mix_s<MIX, false, true>(p, g, st, mi);
+    else launch_mix_s<MIX, false, false>(p, g, st, mi);
+  }
 }
 
 static void launch_any(const P32 &p, const MarchGrid &g, cudaStream_t st, const MarchInteg *mi = nullptr) {
@@ -847,24 +886,30 @@ int march_pick_rows(cudaStream_t st, int reps, const std::vector<int> &cands, co
   return SWM_GPU_OK;
 }
 
-template <int MIX, bool STD>
+template <int MIX, bool STD, bool PF>
 static int resident_blocks_of() {  // blocks of k_march resident on the whole GPU at once
   static int b = 0;
   if (!b) {
     int per_sm = 0, sms = 0, dev = 0;
     cudaGetDevice(&dev);
     cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_march<MIX, false, STD>, 128, 0);
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_march<MIX, false, STD, PF>, 128, 0);
     b = sms * (per_sm > 0 ? per_sm : 1);
   }
   return b;
 }
 
+template <int MIX>
+static int resident_blocks_m(bool s, bool pf) {
+  if (s) return pf ? resident_blocks_of<MIX, true, true>() : resident_blocks_of<MIX, true, false>();
+  return pf ? resident_blocks_of<MIX, false, true>() : resident_blocks_of<MIX, false, false>();
+}
+
 static int resident_blocks(const P32 &p) {
-  const bool s = march_std(p);
-  if (p.mix == 2) return s ? resident_blocks_of<2, true>() : resident_blocks_of<2, false>();
-  if (p.mix == 1) return s ? resident_blocks_of<1, true>() : resident_blocks_of<1, false>();
-  return s ? resident_blocks_of<0, true>() : resident_blocks_of<0, false>();
+  const bool s = march_std(p), pf = march_prefetch((size_t)p.nx * p.ny);
+  if (p.mix == 2) return resident_blocks_m<2>(s, pf);
+  if (p.mix == 1) return resident_blocks_m<1>(s, pf);
+  return resident_blocks_m<0>(s, pf);
 }
 
 // Tiles of the step kernel, by timing the step on this basin.  A kernel is
@@ -935,33 +980,38 @@ int march_autotune(swm_gpu_ctx *c, const P32 &p, const uint16_t *m16) {
 }
 
 // ---- ensemble launch ------------------------------------------------------
-template <int MIX, bool STD>
+template <int MIX, bool STD, bool PF>
 static int ens_launch_m(const P32 *tab, const int4 *tiles, int ntiles, int *next, cudaStream_t st) {
   static int blocks = 0;
   if (!blocks) {
     int per_sm = 0, sms = 0, dev = 0;
     SWM_CK(cudaGetDevice(&dev));
     SWM_CK(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
-    SWM_CK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_march_ens<MIX, STD>, 128, 0));
+    SWM_CK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_march_ens<MIX, STD, PF>, 128, 0));
     blocks = sms * (per_sm > 0 ? per_sm : 1);
   }
   int need = (ntiles + 3) / 4;
-  k_march_ens<MIX, STD><<<need < blocks ? need : blocks, 128, 0, st>>>(tab, tiles, ntiles, next);
+  k_march_ens<MIX, STD, PF><<<need < blocks ? need : blocks, 128, 0, st>>>(tab, tiles, ntiles, next);
   return SWM_GPU_OK;
+}
+
+template <int MIX>
+static int ens_launch_mix(bool std_cfg, bool pf, const P32 *tab, const int4 *tiles, int ntiles, int *next,
+                          cudaStream_t st) {
+  if (std_cfg)
+    return pf ? ens_launch_m<MIX, true, true>(tab, tiles, ntiles, next, st)
+              : ens_launch_m<MIX, true, false>(tab, tiles, ntiles, next, st);
+  return pf ? ens_launch_m<MIX, false, true>(tab, tiles, ntiles, next, st)
+            : ens_launch_m<MIX, false, false>(tab, tiles, ntiles, next, st);
 }
 
 bool march_std_params(const P32 &p) { return march_std(p); }
 
-int march_ens_launch(int mix, bool std_cfg, const P32 *tab, const int4 *tiles, int ntiles, int *next,
+int march_ens_launch(int mix, bool std_cfg, bool pf, const P32 *tab, const int4 *tiles, int ntiles, int *next,
                      cudaStream_t st) {
-  if (mix == 2)
-    return std_cfg ? ens_launch_m<2, true>(tab, tiles, ntiles, next, st)
-                   : ens_launch_m<2, false>(tab, tiles, ntiles, next, st);
-  if (mix == 1)
-    return std_cfg ? ens_launch_m<1, true>(tab, tiles, ntiles, next, st)
-                   : ens_launch_m<1, false>(tab, tiles, ntiles, next, st);
-  return std_cfg ? ens_launch_m<0, true>(tab, tiles, ntiles, next, st)
-                 : ens_launch_m<0, false>(tab, tiles, ntiles, next, st);
+  if (mix == 2) return ens_launch_mix<2>(std_cfg, pf, tab, tiles, ntiles, next, st);
+  if (mix == 1) return ens_launch_mix<1>(std_cfg, pf, tab, tiles, ntiles, next, st);
+  return ens_launch_mix<0>(std_cfg, pf, tab, tiles, ntiles, next, st);
 }
 
 }  // namespace swm

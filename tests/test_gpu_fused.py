@@ -119,3 +119,32 @@ def test_strip_rows_do_not_change_results(variant, monkeypatch):
     for other in fields[1:]:
         for a, b in zip(fields[0], other):
             assert np.array_equal(a, b)
+
+
+@pytest.mark.parametrize('variant', ['biharmonic', 'laplace_qbf'])
+def test_l2_prefetch_does_not_change_results(variant, monkeypatch):
+    """The step kernel's L2 prefetch of rows ahead (chosen for states larger
+    than L2; forced here on a small basin) changes no result: the same
+    steps, plain and monitored, give the same state bit for bit with and
+    without it.  The monitored integrals come from separately compiled
+    instances, whose pair sums may round differently: within 1e-12 of each
+    sum's scale."""
+    from test_gpu_diag import _numpy_integrals
+    import torch
+    from swm_gb300.host.driver import Driver
+    case = _case(variant, 60)
+    ny = case['config']['ny']
+    fields = []
+    for pf in ('0', '1'):
+        monkeypatch.setenv('SWM_GB300_MARCH_PREFETCH', pf)
+        g = GpuModel('fused_fp32c')
+        Driver(case, g).init(with_diag=False)
+        g.run(0, 30)
+        out = torch.empty((10, 3), dtype=torch.float64).pin_memory().numpy()
+        g.run_monitor(30, 10, 0, None, out)
+        fields.append([g.field(f) for f in ('u', 'v', 'eta')] + [out.copy()])
+        _, scale = _numpy_integrals(case, g)
+        g.close()
+    for a, b in zip(fields[0][:3], fields[1][:3]):
+        assert np.array_equal(a, b)
+    assert np.all(np.abs(fields[0][3] - fields[1][3]) <= 1e-12 * scale)
