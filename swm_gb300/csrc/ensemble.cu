@@ -75,7 +75,7 @@ struct swm_gpu_ensemble {
   int mix = 0, rows = 16, phase = 0, graph_phase = -1;
   double slow = 1.;  // masked-row cost the tiles were cut with
   bool std_cfg = false;  // all members in the step kernel's common configuration
-  bool pf = false;       // the members' state is larger than L2: prefetch rows
+  int pf = 1;            // the step kernel's prefetch level for the members' state
   cudaStream_t stream = nullptr;
   cudaEvent_t done = nullptr;
   std::vector<cudaEvent_t> ev;
@@ -228,7 +228,7 @@ int swm_gpu_ensemble_create(swm_gpu_ctx *const *members, int n, swm_gpu_ensemble
   for (const P32 &q : tab) e->std_cfg = e->std_cfg && march_std_params(q);
   size_t points = 0;
   for (int i = 0; i < n; i++) points += (size_t)members[i]->nx * members[i]->ny;
-  e->pf = march_prefetch(points);
+  e->pf = march_prefetch_level(points, false);
   // Tiles: every member's strips cut into row groups of equal estimated
   // cost (as the single-basin step kernel's tiles), all members' tiles in
   // one queue with the short remainder groups last, so the queue ends on

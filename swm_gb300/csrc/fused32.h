@@ -165,10 +165,10 @@ void fused_static(const swm_gpu_ctx *c, const float **He, const uint16_t **mask1
 // one launch of the ensemble step: tiles {member, strip, first row, rows}
 // std_cfg: every member's parameter block is of the common configuration
 // (march_std_params), so the kernel's specialised instance serves them
-// pf: the members' state together is larger than L2 (march_prefetch)
-int march_ens_launch(int mix, bool std_cfg, bool pf, const P32 *tab, const int4 *tiles, int ntiles, int *next,
+// pf: the step kernel's prefetch level (march_prefetch_level)
+int march_ens_launch(int mix, bool std_cfg, int pf, const P32 *tab, const int4 *tiles, int ntiles, int *next,
                      cudaStream_t st);
 bool march_std_params(const P32 &p);
-bool march_prefetch(size_t points);
+int march_prefetch_level(size_t points, bool integ);
 
 }  // namespace swm

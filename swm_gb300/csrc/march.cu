@@ -84,10 +84,11 @@ __device__ __forceinline__ void comp_damp(float hi, float lo, float inc, float d
 // the new state of its ocean points, times the cell area of the point's row
 // (area: 3 x ny (hi, lo) pairs, u, v, eta rows), into acc[4]: eta, eta^2,
 // u^2, v^2.
-// PF: each iteration also asks L2 for the input rows two ahead and for the
-// next output row's increments (prefetch.global.L2, no registers), for a
-// state larger than L2, which every step reads from DRAM (march_prefetch).
-template <int MIX, bool INTEG = false, bool STD = false, bool PF = false>
+// PF: each iteration also asks L2 (prefetch.global.L2, no registers) for the
+// next output row's increments (PF >= 1), which it would otherwise load in
+// the iteration that uses them, and for the input rows two ahead (PF = 2),
+// so that rows not in L2 do not wait on DRAM (march_prefetch_level).
+template <int MIX, bool INTEG = false, bool STD = false, int PF = 0>
 __device__ __forceinline__ void march_strip(const P32 &p, const int bx, const int ry0, const int lane, const int S,
                                             const float2 *area = nullptr, F2 *acc = nullptr) {
   constexpr int H = MIX == 2 ? 2 : 1;
@@ -458,8 +459,8 @@ __device__ __forceinline__ void march_strip(const P32 &p, const int bx, const in
       n_uh = p.uh0[kn]; n_ul = p.ul0[kn]; n_vh = p.vh0[kn]; n_vl = p.vl0[kn];
       n_eh = p.eh0[kn]; n_el = p.el0[kn]; n_he = p.He[kn];
     }
-    if (PF) {
-      if (J + 2 < jend) {  // the input rows two ahead
+    if (PF >= 1) {
+      if (PF == 2 && J + 2 < jend) {  // the input rows two ahead
         const int k2 = gi + nx * wrapm(J + 2, ny);
         prefetch_l2(p.mask16 + k2);
         prefetch_l2(p.uh0 + k2); prefetch_l2(p.ul0 + k2); prefetch_l2(p.vh0 + k2); prefetch_l2(p.vl0 + k2);
@@ -565,7 +566,7 @@ void march_integrals_final(const double *partial, int nb, double G, double *out,
 // groups of one strip, so their look-ahead rows overlap and meet in L1.
 // INTEG (a monitored step, MarchInteg): block 0 does the side jobs and the
 // strip blocks are blockIdx.x - 1; they sum the new state as well.
-template <int MIX, bool INTEG, bool STD, bool PF>
+template <int MIX, bool INTEG, bool STD, int PF>
 __global__ void __launch_bounds__(128, MARCH_MINB) k_march(P32 p, const int2 *__restrict__ tiles, MarchInteg mi) {
   const int lane = threadIdx.x & 31;
   int b = blockIdx.x;
@@ -591,7 +592,7 @@ __global__ void __launch_bounds__(128, MARCH_MINB) k_march(P32 p, const int2 *__
 // the queue until it is empty.  A tile is int4 {member, strip, first row,
 // rows}; the member's parameter block is copied into the warp's slice of
 // shared memory first.
-template <int MIX, bool STD, bool PF>
+template <int MIX, bool STD, int PF>
 __global__ void __launch_bounds__(128, MARCH_MINB) k_march_ens(const P32 *__restrict__ tab,
                                                                const int4 *__restrict__ tiles, int ntiles,
                                                                int *__restrict__ next) {
@@ -766,11 +767,9 @@ static bool march_std(const P32 &p) {
   return p.nl && p.has_mode && !p.qbf && !p.has_F && p.impl_uniform && (p.wind_rows || (!p.wind_x && !p.wind_y));
 }
 
-// Is a state of `points` array points larger than L2, so that the step
-// kernel should prefetch its rows (89 bytes move per point and step)?
-bool march_prefetch(size_t points) {
-  const char *e = getenv("SWM_GB300_MARCH_PREFETCH");  // 0 or 1 forces the choice
-  if (e && (e[0] == '0' || e[0] == '1') && e[1] == 0) return e[0] == '1';
+// Is a state of `points` array points larger than L2 (89 bytes move per
+// point and step)?
+bool march_state_exceeds_l2(size_t points) {
   static long long l2 = -1;
   if (l2 < 0) {
     int dev = 0, v = 0;
@@ -780,7 +779,20 @@ bool march_prefetch(size_t points) {
   return 89.0 * (double)points > (double)l2;
 }
 
-template <int MIX, bool STD, bool PF>
+// Prefetch level of the step kernel (march_strip's PF).  A state larger than
+// L2 is read from DRAM every step: 2.  Otherwise the rows are in L2 when
+// steps follow one another, as in a monitored run (integ): 0; a single step
+// may follow other work that evicted them, and the increments it loads last
+// then wait on DRAM: 1 (measured on the 1025^2 basin: 5 % faster from a cold
+// L2, 1 % slower from a warm one).  SWM_GB300_MARCH_PREFETCH=0/1/2 forces it.
+int march_prefetch_level(size_t points, bool integ) {
+  const char *e = getenv("SWM_GB300_MARCH_PREFETCH");
+  if (e && e[0] >= '0' && e[0] <= '2' && e[1] == 0) return e[0] - '0';
+  if (march_state_exceeds_l2(points)) return 2;
+  return integ ? 0 : 1;
+}
+
+template <int MIX, bool STD, int PF>
 static void launch_mix_s(const P32 &p, const MarchGrid &g, cudaStream_t st, const MarchInteg *mi) {
   if (!mi) {
     k_march<MIX, false, STD, PF><<<g.blocks, 128, 0, st>>>(p, g.tiles, MarchInteg{});
@@ -793,16 +805,18 @@ static void launch_mix_s(const P32 &p, const MarchGrid &g, cudaStream_t st, cons
     k_march<MIX, true, STD, PF><<<g.blocks + 1, 128, 0, st>>>(p, g.tiles, *mi);
 }
 
+template <int MIX, bool STD>
+static void launch_mix_p(const P32 &p, const MarchGrid &g, cudaStream_t st, const MarchInteg *mi) {
+  const int pf = march_prefetch_level((size_t)p.nx * p.ny, mi != nullptr);
+  if (pf == 2) launch_mix_s<MIX, STD, 2>(p, g, st, mi);
+  else if (pf == 1) launch_mix_s<MIX, STD, 1>(p, g, st, mi);
+  else launch_mix_s<MIX, STD, 0>(p, g, st, mi);
+}
+
 template <int MIX>
 static void launch_mix(const P32 &p, const MarchGrid &g, cudaStream_t st, const MarchInteg *mi) {
-  const bool pf = march_prefetch((size_t)p.nx * p.ny);
-  if (march_std(p)) {
-    if (pf) launch_mix_s<MIX, true, true>(p, g, st, mi);
-    else launch_mix_s<MIX, true, false>(p, g, st, mi);
-  } else {
-    if (pf) launch_mix_s<MIX, false, true>(p, g, st, mi);
-    else launch_mix_s<MIX, false, false>(p, g, st, mi);
-  }
+  if (march_std(p)) launch_mix_p<MIX, true>(p, g, st, mi);
+  else launch_mix_p<MIX, false>(p, g, st, mi);
 }
 
 static void launch_any(const P32 &p, const MarchGrid &g, cudaStream_t st, const MarchInteg *mi = nullptr) {
@@ -886,7 +900,7 @@ int march_pick_rows(cudaStream_t st, int reps, const std::vector<int> &cands, co
   return SWM_GPU_OK;
 }
 
-template <int MIX, bool STD, bool PF>
+template <int MIX, bool STD, int PF>
 static int resident_blocks_of() {  // blocks of k_march resident on the whole GPU at once
   static int b = 0;
   if (!b) {
@@ -899,14 +913,20 @@ static int resident_blocks_of() {  // blocks of k_march resident on the whole GP
   return b;
 }
 
+template <int MIX, bool STD>
+static int resident_blocks_p(int pf) {
+  return pf == 2 ? resident_blocks_of<MIX, STD, 2>()
+                 : (pf == 1 ? resident_blocks_of<MIX, STD, 1>() : resident_blocks_of<MIX, STD, 0>());
+}
+
 template <int MIX>
-static int resident_blocks_m(bool s, bool pf) {
-  if (s) return pf ? resident_blocks_of<MIX, true, true>() : resident_blocks_of<MIX, true, false>();
-  return pf ? resident_blocks_of<MIX, false, true>() : resident_blocks_of<MIX, false, false>();
+static int resident_blocks_m(bool s, int pf) {
+  return s ? resident_blocks_p<MIX, true>(pf) : resident_blocks_p<MIX, false>(pf);
 }
 
 static int resident_blocks(const P32 &p) {
-  const bool s = march_std(p), pf = march_prefetch((size_t)p.nx * p.ny);
+  const bool s = march_std(p);
+  const int pf = march_prefetch_level((size_t)p.nx * p.ny, false);
   if (p.mix == 2) return resident_blocks_m<2>(s, pf);
   if (p.mix == 1) return resident_blocks_m<1>(s, pf);
   return resident_blocks_m<0>(s, pf);
@@ -980,7 +1000,7 @@ int march_autotune(swm_gpu_ctx *c, const P32 &p, const uint16_t *m16) {
 }
 
 // ---- ensemble launch ------------------------------------------------------
-template <int MIX, bool STD, bool PF>
+template <int MIX, bool STD, int PF>
 static int ens_launch_m(const P32 *tab, const int4 *tiles, int ntiles, int *next, cudaStream_t st) {
   static int blocks = 0;
   if (!blocks) {
@@ -995,19 +1015,23 @@ static int ens_launch_m(const P32 *tab, const int4 *tiles, int ntiles, int *next
   return SWM_GPU_OK;
 }
 
+template <int MIX, bool STD>
+static int ens_launch_p(int pf, const P32 *tab, const int4 *tiles, int ntiles, int *next, cudaStream_t st) {
+  if (pf == 2) return ens_launch_m<MIX, STD, 2>(tab, tiles, ntiles, next, st);
+  if (pf == 1) return ens_launch_m<MIX, STD, 1>(tab, tiles, ntiles, next, st);
+  return ens_launch_m<MIX, STD, 0>(tab, tiles, ntiles, next, st);
+}
+
 template <int MIX>
-static int ens_launch_mix(bool std_cfg, bool pf, const P32 *tab, const int4 *tiles, int ntiles, int *next,
+static int ens_launch_mix(bool std_cfg, int pf, const P32 *tab, const int4 *tiles, int ntiles, int *next,
                           cudaStream_t st) {
-  if (std_cfg)
-    return pf ? ens_launch_m<MIX, true, true>(tab, tiles, ntiles, next, st)
-              : ens_launch_m<MIX, true, false>(tab, tiles, ntiles, next, st);
-  return pf ? ens_launch_m<MIX, false, true>(tab, tiles, ntiles, next, st)
-            : ens_launch_m<MIX, false, false>(tab, tiles, ntiles, next, st);
+  return std_cfg ? ens_launch_p<MIX, true>(pf, tab, tiles, ntiles, next, st)
+                 : ens_launch_p<MIX, false>(pf, tab, tiles, ntiles, next, st);
 }
 
 bool march_std_params(const P32 &p) { return march_std(p); }
 
-int march_ens_launch(int mix, bool std_cfg, bool pf, const P32 *tab, const int4 *tiles, int ntiles, int *next,
+int march_ens_launch(int mix, bool std_cfg, int pf, const P32 *tab, const int4 *tiles, int ntiles, int *next,
                      cudaStream_t st) {
   if (mix == 2) return ens_launch_mix<2>(std_cfg, pf, tab, tiles, ntiles, next, st);
   if (mix == 1) return ens_launch_mix<1>(std_cfg, pf, tab, tiles, ntiles, next, st);

@@ -123,8 +123,8 @@ def test_strip_rows_do_not_change_results(variant, monkeypatch):
 
 @pytest.mark.parametrize('variant', ['biharmonic', 'laplace_qbf'])
 def test_l2_prefetch_does_not_change_results(variant, monkeypatch):
-    """The step kernel's L2 prefetch of rows ahead (chosen for states larger
-    than L2; forced here on a small basin) changes no result: the same
+    """The step kernel's L2 prefetch levels (none, the next row's increments,
+    also the input rows two ahead; forced here) change no result: the same
     steps, plain and monitored, give the same state bit for bit with and
     without it.  The monitored integrals come from separately compiled
     instances, whose pair sums may round differently: within 1e-12 of each
@@ -135,7 +135,7 @@ def test_l2_prefetch_does_not_change_results(variant, monkeypatch):
     case = _case(variant, 60)
     ny = case['config']['ny']
     fields = []
-    for pf in ('0', '1'):
+    for pf in ('0', '1', '2'):
         monkeypatch.setenv('SWM_GB300_MARCH_PREFETCH', pf)
         g = GpuModel('fused_fp32c')
         Driver(case, g).init(with_diag=False)
@@ -145,6 +145,7 @@ def test_l2_prefetch_does_not_change_results(variant, monkeypatch):
         fields.append([g.field(f) for f in ('u', 'v', 'eta')] + [out.copy()])
         _, scale = _numpy_integrals(case, g)
         g.close()
-    for a, b in zip(fields[0][:3], fields[1][:3]):
-        assert np.array_equal(a, b)
-    assert np.all(np.abs(fields[0][3] - fields[1][3]) <= 1e-12 * scale)
+    for other in fields[1:]:
+        for a, b in zip(fields[0][:3], other[:3]):
+            assert np.array_equal(a, b)
+        assert np.all(np.abs(fields[0][3] - other[3]) <= 1e-12 * scale)
