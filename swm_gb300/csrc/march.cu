@@ -139,8 +139,15 @@ __device__ __forceinline__ void march_strip(const P32 &p, const int bx, const in
     const bool upd = o >= ry0 && o < ry0 + S && o < ny && store_lane;
     const int ko = gi + off[2];
     float g1e = 0, g2e = 0, g1u = 0, g2u = 0, g1v = 0, g2v = 0;
+    // row-profile wind of row o, loaded with the increments (not in the
+    // monitored instances, whose sums leave no register for it)
+    float wxo = 0.f, wyo = 0.f;
     if (upd) {
       g1e = p.Ge1[ko]; g2e = p.Ge2[ko]; g1u = p.Gu1[ko]; g2u = p.Gu2[ko]; g1v = p.Gv1[ko]; g2v = p.Gv2[ko];
+      if (!INTEG && wind_rows) {
+        if (p.wind_x) wxo = p.wx[o];
+        if (p.wind_y) wyo = p.wy[o];
+      }
     }
 
     // ---- row J: mass fluxes and PV; row J-1: kinetic energy ----------
@@ -332,7 +339,7 @@ __device__ __forceinline__ void march_strip(const P32 &p, const int bx, const in
           g += __fdividef(lat, du);
         }
         if (has_F) g += p.Fx[ko];
-        if (p.wind_x) g += __fdividef(p.ts_rho * (wind_rows ? p.wx[o] : p.wx[ko]), nl ? du : 1.f);
+        if (p.wind_x) g += __fdividef(p.ts_rho * (wind_rows ? (INTEG ? p.wx[o] : wxo) : p.wx[ko]), nl ? du : 1.f);
         gu = g;
       }
       if (XV(mm)) {
@@ -355,7 +362,7 @@ __device__ __forceinline__ void march_strip(const P32 &p, const int bx, const in
           g += __fdividef(lat, dv);
         }
         if (has_F) g += p.Fy[ko];
-        if (p.wind_y) g += __fdividef(p.ts_rho * (wind_rows ? p.wy[o] : p.wy[ko]), nl ? dv : 1.f);
+        if (p.wind_y) g += __fdividef(p.ts_rho * (wind_rows ? (INTEG ? p.wy[o] : wyo) : p.wy[ko]), nl ? dv : 1.f);
         gv = g;
       }
       p.Ge3[ko] = ge;
