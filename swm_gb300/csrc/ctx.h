@@ -129,7 +129,7 @@ struct swm_gpu_ctx {
   FusedState *fused = nullptr;
   SorState *sor = nullptr;
   IntegralScratch *integrals = nullptr;
-  int integrals_shape[3] = {-1, 0, 0};  // k_integrals: kernel (0 FP64, 1 pair), threads, blocks
+  int integrals_shape[3] = {-1, 0, 0};  // k_integrals (FP64 state): tuned (0) or not (-1), threads, blocks
   Trc32State *trc32 = nullptr;      // tracers of the FP32 compensated path
   std::vector<swm::DiagAcc> diag;   // averaging buffers by slot
   std::vector<cudaEvent_t> async_ev;  // ring of events for swm_gpu_get_field_async

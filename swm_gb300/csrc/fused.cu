@@ -854,40 +854,34 @@ struct RowAreas {
 
 // one thread's share of one (row, chunk) item: IL columns, their masks and
 // the row's areas
-template <typename T>
 struct IntChunk {
   int8_t mE[INTEGRALS_IL], mU[INTEGRALS_IL], mV[INTEGRALS_IL];
-  T xe[INTEGRALS_IL], xu[INTEGRALS_IL], xv[INTEGRALS_IL];
-  float le[INTEGRALS_IL], lu[INTEGRALS_IL], lv[INTEGRALS_IL];
-  float2 pu, pv, pe;
+  double xe[INTEGRALS_IL], xu[INTEGRALS_IL], xv[INTEGRALS_IL];
   double du, dv, de;
 };
 
-// Domain sums over ocean points.  The work is a row-major list of (row,
-// chunk) items; a chunk is IL * blockDim.x columns, thread t holding columns
-// t, t + blockDim.x, ...  Blocks stride through the list.  A thread issues
-// all loads of an item (masks, values, areas; clamped in-row indices, no
-// branch) before it adds any of them, so an item costs one memory round trip
-// and the launch keeps a whole wave of items in flight.  Per item a thread sums eta, eta^2,
-// u^2, v^2 of its columns and adds them times the row's cell area to its
-// running totals: for the pair state all of it in (hi, lo) binary32 pairs
-// (about 46 bits; FP64 arithmetic per row would make the kernel FP64-pipe
-// bound on this part), for the FP64 state in FP64.  Each block leaves its
-// three sums in `partial`; the block that finishes last (counted in *done,
-// which it resets to 0) adds the partials in block order into out[3].  Every
-// order is fixed by the launch shape: the result is deterministic.
-template <typename T, bool COMP>
+// Domain sums of the FP64 state over ocean points.  The work is a row-major
+// list of (row, chunk) items; a chunk is IL * blockDim.x columns, thread t
+// holding columns t, t + blockDim.x, ...  Blocks stride through the list.  A
+// thread issues all loads of an item (masks, values, areas; clamped in-row
+// indices, no branch) before it adds any of them, so an item costs one
+// memory round trip and the launch keeps a whole wave of items in flight.
+// Per item a thread sums eta, eta^2, u^2, v^2 of its columns in FP64 and adds
+// them times the row's cell area to its running totals.  Each block leaves
+// its three sums in `partial`; the block that finishes last (counted in
+// *done, which it resets to 0) adds the partials in block order into out[3].
+// Every order is fixed by the launch shape: the result is deterministic.
 __global__ void __launch_bounds__(INTEGRALS_MAX_THREADS)
     k_integrals(int nx, int ny, const int8_t *oU, const int8_t *oV, const int8_t *oE, RowAreas ar,
-                const T *u, const float *ul, const T *v, const float *vl, const T *e, const float *el,
-                double G, double *partial, unsigned *done, double *out) {
+                const double *u, const double *v, const double *e, double G, double *partial, unsigned *done,
+                double *out) {
   constexpr int IL = INTEGRALS_IL;
   __shared__ double red[4][INTEGRALS_MAX_THREADS / 32];
   __shared__ bool last;
   const int B = blockDim.x, W = IL * B;
   const int C = (nx + W - 1) / W;  // chunks per row
   const long long items = (long long)ny * C;
-  auto load = [&](IntChunk<T> &c, long long t) {
+  auto load = [&](IntChunk &c, long long t) {
     const int j = (int)(t / C);
     const int i0 = (int)(t - (long long)j * C) * W + (int)threadIdx.x;
     const size_t row = (size_t)nx * j;
@@ -902,76 +896,30 @@ __global__ void __launch_bounds__(INTEGRALS_MAX_THREADS)
       c.xe[q] = e[k];
       c.xu[q] = u[k];
       c.xv[q] = v[k];
-      if (COMP) {
-        c.le[q] = el[k];
-        c.lu[q] = ul[k];
-        c.lv[q] = vl[k];
-      }
     }
-    if (COMP) {
-      c.pu = ar.pu[j];
-      c.pv = ar.pv[j];
-      c.pe = ar.pe[j];
-    } else {
-      c.du = ar.u[j];
-      c.dv = ar.v[j];
-      c.de = ar.e[j];
-    }
+    c.du = ar.u[j];
+    c.dv = ar.v[j];
+    c.de = ar.e[j];
   };
-  F2 P0, P1, PU, PV;                    // pair state totals
-  double D0 = 0., D1 = 0., DU = 0., DV = 0.;  // FP64 state totals
+  double s[4] = {0., 0., 0., 0.};
   for (long long t = blockIdx.x; t < items; t += gridDim.x) {
-    IntChunk<T> cur;
+    IntChunk cur;
     load(cur, t);
-    if (COMP) {
-      // land points add the pair (0, 0), an exact identity of F2::add: a
-      // select instead of a branch, so every load stays ahead of its use
-      F2 a0, a1, au2, av2;
+    double r0 = 0., r1 = 0., ru = 0., rv = 0.;
 #pragma unroll
-      for (int q = 0; q < IL; q++) {
-        float p, r;
-        const float x = cur.mE[q] ? (float)cur.xe[q] : 0.f, xl = cur.mE[q] ? cur.le[q] : 0.f;
-        a0.add(x, xl);
-        sq_pair(x, xl, p, r);
-        a1.add(p, r);
-        sq_pair(cur.mU[q] ? (float)cur.xu[q] : 0.f, cur.mU[q] ? cur.lu[q] : 0.f, p, r);
-        au2.add(p, r);
-        sq_pair(cur.mV[q] ? (float)cur.xv[q] : 0.f, cur.mV[q] ? cur.lv[q] : 0.f, p, r);
-        av2.add(p, r);
-      }
-      P0.add_prod(cur.pe, a0);
-      P1.add_prod(cur.pe, a1);
-      PU.add_prod(cur.pu, au2);
-      PV.add_prod(cur.pv, av2);
-    } else {
-      double r0 = 0., r1 = 0., ru = 0., rv = 0.;
-#pragma unroll
-      for (int q = 0; q < IL; q++) {
-        const double ee = cur.mE[q] ? (double)cur.xe[q] : 0.;
-        const double uu = cur.mU[q] ? (double)cur.xu[q] : 0.;
-        const double vv = cur.mV[q] ? (double)cur.xv[q] : 0.;
-        r0 += ee;
-        r1 += ee * ee;
-        ru += uu * uu;
-        rv += vv * vv;
-      }
-      D0 += r0 * cur.de;
-      D1 += r1 * cur.de;
-      DU += ru * cur.du;
-      DV += rv * cur.dv;
+    for (int q = 0; q < IL; q++) {
+      const double ee = cur.mE[q] ? cur.xe[q] : 0.;
+      const double uu = cur.mU[q] ? cur.xu[q] : 0.;
+      const double vv = cur.mV[q] ? cur.xv[q] : 0.;
+      r0 += ee;
+      r1 += ee * ee;
+      ru += uu * uu;
+      rv += vv * vv;
     }
-  }
-  double s[4];
-  if (COMP) {
-    s[0] = P0.value();
-    s[1] = P1.value();
-    s[2] = PU.value();
-    s[3] = PV.value();
-  } else {
-    s[0] = D0;
-    s[1] = D1;
-    s[2] = DU;
-    s[3] = DV;
+    s[0] += r0 * cur.de;
+    s[1] += r1 * cur.de;
+    s[2] += ru * cur.du;
+    s[3] += rv * cur.dv;
   }
   for (int o = 16; o > 0; o >>= 1)
     for (int q = 0; q < 4; q++) s[q] += __shfl_down_sync(0xffffffffu, s[q], o);
@@ -996,11 +944,110 @@ __global__ void __launch_bounds__(INTEGRALS_MAX_THREADS)
   if (threadIdx.x == 0) *done = 0u;
 }
 
+// Domain sums of the pair state, marching as the step kernel does: warp
+// task t covers columns 32 s .. 32 s + 31 (s = t % strips, lane = column) and
+// rows IP_ROWS g .. IP_ROWS g + IP_ROWS - 1 (g = t / strips).  Each row's
+// values, packed mask word and cell areas are loaded one row ahead into
+// registers; each lane adds its ocean points times the row's areas into
+// (hi, lo) pair sums (the monitored step kernel's arithmetic).  The warps of
+// a block are added in order in FP64, and the blocks as in k_integrals: the
+// last block to finish adds their partials in block order into out[3] and
+// resets *done.  Fixed order throughout.
+#ifndef IP_ROWS_N
+#define IP_ROWS_N 16
+#endif
+constexpr int IP_ROWS = IP_ROWS_N;  // rows of one warp task
+constexpr int IP_WARPS = 8;         // warps per block
+
+__global__ void __launch_bounds__(32 * IP_WARPS)
+    k_integrals_pair(int nx, int ny, const uint16_t *__restrict__ m16, RowAreas ar, const float *__restrict__ uh,
+                     const float *__restrict__ ul, const float *__restrict__ vh, const float *__restrict__ vl,
+                     const float *__restrict__ eh, const float *__restrict__ el, double G, double *partial,
+                     unsigned *done, double *out) {
+  __shared__ double red[4][IP_WARPS];
+  __shared__ bool last;
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  const int strips = (nx + 31) / 32, groups = (ny + IP_ROWS - 1) / IP_ROWS;
+  const long long tasks = (long long)strips * groups;
+  F2 acc[4];
+  for (long long t = (long long)blockIdx.x * IP_WARPS + warp; t < tasks; t += (long long)gridDim.x * IP_WARPS) {
+    const int st = (int)(t % strips), g = (int)(t / strips);
+    const int i = 32 * st + lane;
+    const bool col = i < nx;
+    const int ic = col ? i : nx - 1;
+    const int j0 = g * IP_ROWS, j1 = min(j0 + IP_ROWS, ny);
+    unsigned nm;
+    float nuh, nul, nvh, nvl, neh, nel;
+    float2 npu, npv, npe;
+    auto load = [&](int j) {
+      const size_t k = (size_t)nx * j + ic;
+      nm = col ? m16[k] : 0u;
+      nuh = uh[k]; nul = ul[k]; nvh = vh[k]; nvl = vl[k]; neh = eh[k]; nel = el[k];
+      npu = ar.pu[j]; npv = ar.pv[j]; npe = ar.pe[j];
+    };
+    load(j0);
+    for (int j = j0; j < j1; j++) {
+      const unsigned m = nm;
+      const float xuh = nuh, xul = nul, xvh = nvh, xvl = nvl, xeh = neh, xel = nel;
+      const float2 apu = npu, apv = npv, ape = npe;
+      if (j + 1 < j1) load(j + 1);
+      F2 sq;
+      if ((m >> 3) & 1u) {
+        F2 x;
+        x.h = xeh;
+        x.l = xel;
+        acc[0].add_prod(ape, x);
+        sq_pair(xeh, xel, sq.h, sq.l);
+        acc[1].add_prod(ape, sq);
+      }
+      if ((m >> 1) & 1u) {
+        sq_pair(xuh, xul, sq.h, sq.l);
+        acc[2].add_prod(apu, sq);
+      }
+      if ((m >> 2) & 1u) {
+        sq_pair(xvh, xvl, sq.h, sq.l);
+        acc[3].add_prod(apv, sq);
+      }
+    }
+  }
+  for (int o = 16; o > 0; o >>= 1)
+#pragma unroll
+    for (int q = 0; q < 4; q++) {
+      const float h = __shfl_down_sync(0xffffffffu, acc[q].h, o), l = __shfl_down_sync(0xffffffffu, acc[q].l, o);
+      acc[q].add(h, l);
+    }
+  if (lane == 0)
+#pragma unroll
+    for (int q = 0; q < 4; q++) red[q][warp] = acc[q].value();
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    double a[4] = {0., 0., 0., 0.};
+    for (int w = 0; w < IP_WARPS; w++)
+      for (int q = 0; q < 4; q++) a[q] += red[q][w];
+    partial[blockIdx.x] = a[0];
+    partial[(size_t)gridDim.x + blockIdx.x] = 0.5 * G * a[1];
+    partial[2 * (size_t)gridDim.x + blockIdx.x] = 0.5 * (a[2] + a[3]);
+    __threadfence();
+    last = atomicAdd(done, 1u) == gridDim.x - 1;
+  }
+  __syncthreads();
+  if (!last) return;
+  __threadfence();
+  integrals_final(partial, gridDim.x, out);
+  if (threadIdx.x == 0) *done = 0u;
+}
+
+// blocks of k_integrals_pair: a block per IP_WARPS tasks, at most
+// INTEGRALS_MAX_BLOCKS (the warps then take several tasks each)
+static int integrals_pair_blocks(int nx, int ny) {
+  const long long tasks = (long long)((nx + 31) / 32) * ((ny + IP_ROWS - 1) / IP_ROWS);
+  return (int)std::max(1LL, std::min<long long>((tasks + IP_WARPS - 1) / IP_WARPS, INTEGRALS_MAX_BLOCKS));
+}
+
 // launch shape of k_integrals for an nx x ny grid: the fewest threads (a
 // multiple of 32, at most INTEGRALS_MAX_THREADS) that cover a row in equal
 // chunks of IL columns each, and one wave of blocks (at most one per item)
-template <typename T, bool COMP>
-static int integrals_shape_t(int nx, int ny, int *threads, int *blocks) {
+static int integrals_shape_fp64(int nx, int ny, int *threads, int *blocks) {
   const int need = (nx + INTEGRALS_IL - 1) / INTEGRALS_IL;
   const int chunks = (need + INTEGRALS_MAX_THREADS - 1) / INTEGRALS_MAX_THREADS;
   const int thr = std::min(INTEGRALS_MAX_THREADS, ((need + chunks - 1) / chunks + 31) / 32 * 32);
@@ -1009,7 +1056,7 @@ static int integrals_shape_t(int nx, int ny, int *threads, int *blocks) {
   int dev = 0, sms = 0, per_sm = 0;
   SWM_CK(cudaGetDevice(&dev));
   SWM_CK(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
-  SWM_CK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_integrals<T, COMP>, thr, 0));
+  SWM_CK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_integrals, thr, 0));
   const long long wave = (long long)std::max(per_sm, 1) * std::max(sms, 1);
   *threads = thr;
   *blocks = (int)std::max(1LL, std::min(items, std::min<long long>(wave, INTEGRALS_MAX_BLOCKS)));
@@ -1035,22 +1082,21 @@ static IntegralsInput integrals_input(swm_gpu_ctx *c) {
 
 static int integrals_run(swm_gpu_ctx *c, const RowAreas &ar, double *partial, unsigned *done, double *out) {
   const IntegralsInput in = integrals_input(c);
-  int *sh = c->integrals_shape;  // {kernel (0 FP64, 1 pair), threads, blocks}
-  if (sh[0] != (int)in.comp) {
-    const int rc = in.comp ? integrals_shape_t<float, true>(c->nx, c->ny, &sh[1], &sh[2])
-                           : integrals_shape_t<double, false>(c->nx, c->ny, &sh[1], &sh[2]);
+  int *sh = c->integrals_shape;  // {tuned, threads, blocks} of k_integrals
+  if (!in.comp && sh[0] != 0) {
+    const int rc = integrals_shape_fp64(c->nx, c->ny, &sh[1], &sh[2]);
     if (rc != SWM_GPU_OK) return rc;
-    sh[0] = (int)in.comp;
+    sh[0] = 0;
   }
   const int8_t *oU = c->d_ocean[GU], *oV = c->d_ocean[GV], *oE = c->d_ocean[GE];
   if (in.comp)
-    k_integrals<float, true><<<sh[2], sh[1], 0, c->stream>>>(
-        c->nx, c->ny, oU, oV, oE, ar, (const float *)in.u, in.ul, (const float *)in.v, in.vl,
+    k_integrals_pair<<<integrals_pair_blocks(c->nx, c->ny), 32 * IP_WARPS, 0, c->stream>>>(
+        c->nx, c->ny, c->fused->mask16, ar, (const float *)in.u, in.ul, (const float *)in.v, in.vl,
         (const float *)in.e, in.el, c->cfg.G, partial, done, out);
   else
-    k_integrals<double, false><<<sh[2], sh[1], 0, c->stream>>>(
-        c->nx, c->ny, oU, oV, oE, ar, (const double *)in.u, nullptr, (const double *)in.v, nullptr,
-        (const double *)in.e, nullptr, c->cfg.G, partial, done, out);
+    k_integrals<<<sh[2], sh[1], 0, c->stream>>>(c->nx, c->ny, oU, oV, oE, ar, (const double *)in.u,
+                                                 (const double *)in.v, (const double *)in.e, c->cfg.G, partial,
+                                                 done, out);
   c->launches++;
   SWM_CK(cudaGetLastError());
   return SWM_GPU_OK;
