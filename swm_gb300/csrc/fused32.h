@@ -73,6 +73,9 @@ struct F2 {
 __device__ __forceinline__ void grid_dep_wait() { asm volatile("griddepcontrol.wait;" ::: "memory"); }
 __device__ __forceinline__ void grid_dep_trigger() { asm volatile("griddepcontrol.launch_dependents;" ::: "memory"); }
 
+// ask L2 for the line holding a (no register is written, nothing waits)
+__device__ __forceinline__ void prefetch_l2(const void *a) { asm volatile("prefetch.global.L2 [%0];" ::"l"(a)); }
+
 // the square of the pair (x, xl) as a pair: TwoProd of the high parts plus
 // the cross term (xl^2 is below the pair's precision)
 __device__ __forceinline__ void sq_pair(float x, float xl, float &p, float &e) {
@@ -170,5 +173,7 @@ int march_ens_launch(int mix, bool std_cfg, int pf, const P32 *tab, const int4 *
                      cudaStream_t st);
 bool march_std_params(const P32 &p);
 int march_prefetch_level(size_t points, bool integ);
+// more bytes than the device's L2 holds
+bool exceeds_l2(double bytes);
 
 }  // namespace swm

@@ -49,8 +49,6 @@ constexpr unsigned FULL = 0xffffffffu;
 __device__ __forceinline__ float shl(float x) { return __shfl_up_sync(FULL, x, 1); }    // lane - 1
 __device__ __forceinline__ float shr(float x) { return __shfl_down_sync(FULL, x, 1); }  // lane + 1
 
-__device__ __forceinline__ void prefetch_l2(const void *a) { asm volatile("prefetch.global.L2 [%0];" ::"l"(a)); }
-
 __device__ __forceinline__ int wrapm(int g, int n) {
   g = g < 0 ? g + n : g;
   return g >= n ? g - n : g;
@@ -776,14 +774,16 @@ static bool march_std(const P32 &p) {
 
 // Is a state of `points` array points larger than L2 (89 bytes move per
 // point and step)?
-bool march_state_exceeds_l2(size_t points) {
+bool march_state_exceeds_l2(size_t points) { return exceeds_l2(89.0 * (double)points); }
+
+bool exceeds_l2(double bytes) {
   static long long l2 = -1;
   if (l2 < 0) {
     int dev = 0, v = 0;
     cudaGetDevice(&dev);
     l2 = cudaDeviceGetAttribute(&v, cudaDevAttrL2CacheSize, dev) == cudaSuccess ? v : 0;
   }
-  return 89.0 * (double)points > (double)l2;
+  return bytes > (double)l2;
 }
 
 // Prefetch level of the step kernel (march_strip's PF).  A state larger than

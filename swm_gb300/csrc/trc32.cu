@@ -34,7 +34,7 @@ struct Tracer32 {
 };
 
 struct TrcP {
-  int nx, ny, nl, flux, ntr;
+  int nx, ny, nl, flux, ntr, pf;
   float dt, ab0, ab1, ab2;
   const float *u, *v, *eta, *He, *Fe, *rows;
   const uint16_t *mask16;
@@ -80,7 +80,10 @@ constexpr int TRC_ROWS = 16;  // output rows per warp
 // as the upwind-biased faces reach two cells) and TRC_ROWS output rows; it
 // walks up the strip keeping the last five rows of CH (hi + lo), thickness
 // and masks in registers, and updates row J-2 once row J is in.
-template <int NT, int FLUX>
+// PF 1: each iteration also asks L2 for the input rows two beyond those it
+// loads and for the update inputs of the output row after next, so that a
+// state larger than L2 does not make the warp wait on DRAM (trc_prefetch).
+template <int NT, int FLUX, int PF>
 __global__ void __launch_bounds__(128, NT <= 2 ? 4 : 3) k_trc32(TrcP p, int S, int nstrips) {
   constexpr int H = 2, TI = 32 - 2 * H;
   const int lane = threadIdx.x & 31;
@@ -159,6 +162,30 @@ __global__ void __launch_bounds__(128, NT <= 2 ? 4 : 3) k_trc32(TrcP p, int S, i
     }
     n1 = n2;
     if (J + 2 < jend) load(J + 2, n2);
+    if (PF) {
+      if (J + 4 < jend) {  // rows two beyond the one just loaded
+        const int k4 = gi + nx * wr(J + 4, ny);
+        prefetch_l2(p.mask16 + k4);
+        prefetch_l2(p.He + k4);
+        if (p.nl) prefetch_l2(p.eta + k4);
+        prefetch_l2(p.u + k4);
+        prefetch_l2(p.v + k4);
+#pragma unroll
+        for (int q = 0; q < NT; q++) {
+          prefetch_l2(p.t[q].ch + k4);
+          prefetch_l2(p.t[q].cl + k4);
+        }
+      }
+      if (store_lane && J >= ry0 && J < ylast) {  // update inputs of output row J (loaded at J + 1)
+        const int k0 = gi + off[0];
+#pragma unroll
+        for (int q = 0; q < NT; q++) {
+          prefetch_l2(p.t[q].G1 + k0);
+          prefetch_l2(p.t[q].G2 + k0);
+          prefetch_l2(p.t[q].C0 + k0);
+        }
+      }
+    }
 
     const int o = J - 2;
     if (o >= ry0) {  // uniform across the warp
@@ -243,19 +270,31 @@ static int trc_rows_override() {
   return 0;
 }
 
+// Prefetch level of the tracer kernel (k_trc32's PF): 1 when the bytes one
+// step moves (u, v, H, mask and eta 18 B per point, 32 B per tracer) exceed
+// L2, so that every step reads its rows from DRAM.  SWM_GB300_TRC_PREFETCH=0/1
+// forces it.
+static int trc_prefetch(size_t points, int ntr) {
+  const char *e = getenv("SWM_GB300_TRC_PREFETCH");
+  if (e && (e[0] == '0' || e[0] == '1') && e[1] == 0) return e[0] - '0';
+  return exceeds_l2((18.0 + 32.0 * ntr) * (double)points) ? 1 : 0;
+}
+
 template <int NT, int FLUX>
 static void trc_launch_f(const TrcP &p, int S, cudaStream_t st) {
   const int nstrips = (p.nx + 27) / 28;
   const unsigned blocks = (unsigned)((long)nstrips * ((p.ny + 4 * S - 1) / (4 * S)));
-  k_trc32<NT, FLUX><<<blocks, 128, 0, st>>>(p, S, nstrips);
+  if (p.pf) k_trc32<NT, FLUX, 1><<<blocks, 128, 0, st>>>(p, S, nstrips);
+  else k_trc32<NT, FLUX, 0><<<blocks, 128, 0, st>>>(p, S, nstrips);
 }
 
 template <int NT, int FLUX>
-static int trc_resident_f() {
+static int trc_resident_f(int pf) {
   int per_sm = 0, sms = 0, dev = 0;
   cudaGetDevice(&dev);
   cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_trc32<NT, FLUX>, 128, 0);
+  if (pf) cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_trc32<NT, FLUX, 1>, 128, 0);
+  else cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_trc32<NT, FLUX, 0>, 128, 0);
   return sms * (per_sm > 0 ? per_sm : 1);
 }
 
@@ -267,7 +306,7 @@ static void trc_launch_nt(const TrcP &p, int S, cudaStream_t st) {
 
 template <int NT>
 static int trc_resident_nt(const TrcP &p) {
-  return p.flux == 1 ? trc_resident_f<NT, 1>() : trc_resident_f<NT, 0>();
+  return p.flux == 1 ? trc_resident_f<NT, 1>(p.pf) : trc_resident_f<NT, 0>(p.pf);
 }
 
 static void trc_launch(const TrcP &p, int S, cudaStream_t st) {
@@ -463,6 +502,7 @@ int trc32_step(swm_gpu_ctx *c, int64_t itt) {
   p.rows = s->rows;
   for (size_t t0 = 0; t0 < s->t.size(); t0 += TRC32_MAX) {
     p.ntr = (int)std::min(s->t.size() - t0, (size_t)TRC32_MAX);
+    p.pf = trc_prefetch(c->n, p.ntr);
     for (int q = 0; q < p.ntr; q++) {
       const Tracer32 &T = s->t[t0 + q];
       auto &d = p.t[q];

@@ -100,3 +100,21 @@ def test_fp32_tracer_rows_per_warp_do_not_change_results(flux, monkeypatch):
     for other in out[1:]:
         for a, b in zip(out[0], other):
             assert np.array_equal(a, b)
+
+
+@pytest.mark.parametrize('flux', [0, 1])
+def test_fp32_tracer_prefetch_level_does_not_change_results(flux, monkeypatch):
+    """The L2 prefetches of the tracer kernel write no register: both levels
+    give the same fields bit for bit."""
+    case = synthetic.tracer_flow(72, nsteps=30, flux=flux)
+    out = []
+    for pf in ('0', '1'):
+        monkeypatch.setenv('SWM_GB300_TRC_PREFETCH', pf)
+        monkeypatch.setenv('SWM_GB300_TRC_ROWS', '7')
+        g = GpuModel('fused_fp32c', tracer_nan_guard=True)
+        Driver(case, g).init(with_diag=False)
+        g.run(0, 25)
+        out.append([g.tracer_field(t, 'CH') for t in range(2)])
+        g.close()
+    for a, b in zip(out[0], out[1]):
+        assert np.array_equal(a, b)
