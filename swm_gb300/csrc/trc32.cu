@@ -131,6 +131,7 @@ __global__ void __launch_bounds__(128, NT <= 2 ? 4 : 3) k_trc32(TrcP p, int S, i
   load(J, n1);
   load(J + 1, n2);
   float pg1[NT] = {}, pg2[NT] = {}, pc0[NT] = {};
+  float fyp[NT] = {};  // flux through the north faces of the previous output row
 
   for (; J < jend; J++) {
 #pragma unroll
@@ -188,56 +189,65 @@ __global__ void __launch_bounds__(128, NT <= 2 ? 4 : 3) k_trc32(TrcP p, int S, i
     }
 
     const int o = J - 2;
-    if (o >= ry0) {  // uniform across the warp
-      const bool upd = store_lane && o < ny;
+    // row ry0 - 1 only forms its north faces (the south faces of row ry0)
+    if (o >= ry0 - 1) {  // uniform across the warp
+      const bool upd = store_lane && o >= ry0 && o < ny;
       // masks of row o and its neighbours
       const unsigned mo = m[2];
       const unsigned oE = (mo >> 3) & 1, oEim = (mo >> 7) & 1, oEip = (mo >> 11) & 1;
-      const unsigned oU = (mo >> 1) & 1, oUip = (mo >> 9) & 1, oV = (mo >> 2) & 1;
+      const unsigned oUip = (mo >> 9) & 1, oV = (mo >> 2) & 1;
       const unsigned oVjp = (m[1] >> 2) & 1, oEjp = (m[1] >> 3) & 1, oEjm = (m[3] >> 3) & 1;
-      const unsigned mr = __shfl_down_sync(FULLM, mo, 1), ml = __shfl_up_sync(FULLM, mo, 1);
-      const unsigned oEipp = (mr >> 11) & 1, oEimm = (ml >> 7) & 1;
-      const unsigned oEjpp = (m[0] >> 3) & 1, oEjmm = (m[4] >> 3) & 1;
-      const float Do = D[2], Dip = __shfl_down_sync(FULLM, Do, 1), Dim = __shfl_up_sync(FULLM, Do, 1);
+      const unsigned oEipp = (__shfl_down_sync(FULLM, mo, 1) >> 11) & 1;
+      const unsigned oEjpp = (m[0] >> 3) & 1;
+      const float Do = D[2], Dip = __shfl_down_sync(FULLM, Do, 1);
       const float Djp = D[1], Djm = D[3];
-      const float ro = rD[2], rip = __shfl_down_sync(FULLM, ro, 1), rim = __shfl_up_sync(FULLM, ro, 1);
+      const float ro = rD[2], rip = __shfl_down_sync(FULLM, ro, 1);
       const float rjp = rD[1], rjm = rD[3];
-      const float uo = u[2], uip = __shfl_down_sync(FULLM, uo, 1), vo = v[2], vjp = v[1];
-      float ch_r[NT], ch_l[NT], ch_rr[NT], ch_ll[NT];
+      const float uip = __shfl_down_sync(FULLM, u[2], 1), vjp = v[1];
+      const float *r = rr[2], *rp = rr[1];
+      const float cv = r[RT_CV], cvp = rp[RT_CV];
+      auto avg2 = [](float a, unsigned oa, float b, unsigned ob) {
+        unsigned c = oa + ob;
+        return c == 0 ? 0.f : ((oa ? a : 0.f) + (ob ? b : 0.f)) * (c == 2 ? 0.5f : 1.f);
+      };
+      const float huip = avg2(Dip, oEip, Do, oE);
+      const float c8 = oUip * r[RT_D8];
+      // Advective fluxes through the east and north faces of every lane's
+      // cell, and the diffusive flux through the east face.  The west face
+      // of a cell is the east face of the lane below it, the south face the
+      // north face of the previous output row: the same operands in the same
+      // order, so the same bits as forming them again (and one call site, so
+      // one rounding of the contracted arithmetic).
+      float fxe[NT], fxw[NT], fyn[NT], fys[NT], dxe[NT], dxw[NT];
 #pragma unroll
       for (int q = 0; q < NT; q++) {
-        ch_r[q] = __shfl_down_sync(FULLM, chs[q][2], 1);
-        ch_l[q] = __shfl_up_sync(FULLM, chs[q][2], 1);
-        ch_rr[q] = FLUX ? __shfl_down_sync(FULLM, chs[q][2], 2) : 0.f;
-        ch_ll[q] = FLUX ? __shfl_up_sync(FULLM, chs[q][2], 2) : 0.f;
+        const float ch = chs[q][2], chip = __shfl_down_sync(FULLM, ch, 1), chim = __shfl_up_sync(FULLM, ch, 1);
+        const float chrr = FLUX ? __shfl_down_sync(FULLM, ch, 2) : 0.f;
+        const float chjp = chs[q][1], chjm = chs[q][3];
+        fxe[q] = oUip * uip * face(FLUX, uip, chim, ch, chip, chrr, oEim, oE, oEip, oEipp);
+        fyn[q] = oVjp * cvp * vjp * face(FLUX, vjp, chjm, ch, chjp, chs[q][0], oEjm, oE, oEjp, oEjpp);
+        fys[q] = fyp[q];
+        fyp[q] = fyn[q];
+        dxe[q] = huip * (chip * rip - ch * ro) * c8;
+        fxw[q] = __shfl_up_sync(FULLM, fxe[q], 1);
+        dxw[q] = -__shfl_up_sync(FULLM, dxe[q], 1);
       }
       if (upd) {
         const int ko = gi + off[2];
-        const float *r = rr[2], *rp = rr[1];
-        const float rdl = r[RT_RDL], rdt = r[RT_RDT], cv = r[RT_CV], cvp = rp[RT_CV];
-        auto avg2 = [](float a, unsigned oa, float b, unsigned ob) {
-          unsigned c = oa + ob;
-          return c == 0 ? 0.f : ((oa ? a : 0.f) + (ob ? b : 0.f)) * (c == 2 ? 0.5f : 1.f);
-        };
-        const float hu = avg2(Do, oE, Dim, oEim), huip = avg2(Dip, oEip, Do, oE);
+        const float rdl = r[RT_RDL], rdt = r[RT_RDT];
         const float hv = avg2(Do, oE, Djm, oEjm), hvjp = avg2(Djp, oEjp, Do, oE);
         const float Fe = p.Fe ? p.Fe[ko] : 0.f;
-        const float c8 = oUip * r[RT_D8], c9 = -(float)oU * r[RT_D8];
         const float c10 = oVjp * cvp * r[RT_D10], c11 = -(float)oV * cv * r[RT_D10];
 #pragma unroll
         for (int q = 0; q < NT; q++) {
           const auto &t = p.t[q];
-          const float ch = chs[q][2], chip = ch_r[q], chim = ch_l[q], chjp = chs[q][1], chjm = chs[q][3];
-          const float fe = face(FLUX, uip, chim, ch, chip, ch_rr[q], oEim, oE, oEip, oEipp);
-          const float fw = face(FLUX, uo, ch_ll[q], chim, ch, chip, oEimm, oEim, oE, oEip);
-          const float fn = face(FLUX, vjp, chjm, ch, chjp, chs[q][0], oEjm, oE, oEjp, oEjpp);
-          const float fs = face(FLUX, vo, chs[q][4], chjm, ch, chjp, oEjmm, oEjm, oE, oEjp);
-          float g = rdl * (oU * uo * fw - oUip * uip * fe) + rdt * (oV * cv * vo * fs - oVjp * cvp * vjp * fn);
+          const float ch = chs[q][2], chjp = chs[q][1], chjm = chs[q][3];
+          float g = rdl * (fxw[q] - fxe[q]) + rdt * (fys[q] - fyn[q]);
           if (FLUX == 1 && !oE) g = 0.f;
           if (oE) {
             const float C = ch * ro;
-            const float diff = t.kappa * (huip * (chip * rip - C) * c8 + hu * (C - chim * rim) * c9 +
-                                          hvjp * (chjp * rjp - C) * c10 + hv * (C - chjm * rjm) * c11);
+            const float diff =
+                t.kappa * (dxe[q] + dxw[q] + hvjp * (chjp * rjp - C) * c10 + hv * (C - chjm * rjm) * c11);
             const float gam = t.gamma ? t.gamma[ko] : t.gamma_s;
             g += diff - gam * Do * (C - pc0[q]) + C * Fe;
           }
