@@ -75,7 +75,7 @@ __global__ void k_h_sweep64(int nx, int ny, const double *__restrict__ cx, const
   psi[k] = psi[k] + omega * (gs - psi[k]);
 }
 
-// one colour of an FP32 sweep over the whole grid (the arithmetic of k_h_tb32)
+// one colour of an FP32 sweep over the whole grid (the arithmetic of k_h_tbr)
 __global__ void k_h_sweep32(int nx, int ny, const float *__restrict__ h, const int8_t *__restrict__ mask,
                             const float *__restrict__ rhs, float *psi, float rdx2, float rdy2, float lambda,
                             float omega, int colour) {
@@ -97,62 +97,115 @@ __global__ void k_h_sweep32(int nx, int ny, const float *__restrict__ h, const i
   psi[k] = sor32_update(psi[k], rhs[k], cxw, cxe, cys, cyn, rcc, w, e, s, n, omega);
 }
 
-// K red-black sweeps of FP32 SOR on one TX x TY tile in shared memory.  The
-// tile is loaded with a halo of 2K cells (each colour pass needs the
-// previous pass's neighbours, so the valid region shrinks by one cell per
-// pass); halo cells are updated too, with the same arithmetic as their owning
-// tile, so after 2K passes the interior equals K global sweeps bit for bit.
-// Coefficients are formed from 1/H in shared memory at each update (13 bytes
-// of shared memory per cell keep five blocks resident per SM; a variant that
-// stored the coefficients ran slower at two blocks per SM).  Reads pin,
-// writes the interior to pout (ping-pong: other tiles still read pin's halo
-// cells).  Cells outside the grid hold psi = 0, mask = 0.
-template <int TX, int TY, int K>
-__global__ void __launch_bounds__(256) k_h_tb32(int nx, int ny, const float *__restrict__ hin,
-                                                const int8_t *__restrict__ mask, const float *__restrict__ rhs,
-                                                const float *__restrict__ pin, float *__restrict__ pout, float rdx2,
-                                                float rdy2, float lambda, float omega) {
-  constexpr int W = 2 * K, RX = TX + 2 * W, RY = TY + 2 * W, PX = RX + 1;
-  __shared__ float sp[RY * PX], sh[RY * PX], sr[RY * PX];
-  __shared__ int8_t sm[RY * PX];
+// K red-black sweeps of FP32 SOR on a region of 64 columns by 8M rows
+// (interior 64 - 4K by 8M - 4K, halo 2K), each thread owning, for the whole
+// launch, the cell pair of region columns 2tx (cell a) and 2tx + 1 (cell b)
+// in rows ty + 8m.  A pair's face coefficients, reciprocal diagonals and rhs
+// are formed once per launch and kept in registers (the pair shares its
+// inner face).  psi is kept in shared memory split by column parity, so a
+// warp's accesses are contiguous, and each cell's inner neighbour is the
+// thread's own register.  Every neighbour of a cell has the other colour, so
+// a pass reads only what the previous passes wrote.  Halo cells are relaxed
+// with the arithmetic of the global sweep (sor32_update, same coefficients),
+// so after 2K passes the interior equals K global sweeps bit for bit; rows
+// that can no longer reach the interior are skipped.  Cells outside the grid
+// hold psi = 0 and are never relaxed.
+constexpr int TBR_M = 5;  // rows per thread
+template <int K>
+__global__ void __launch_bounds__(256, 2) k_h_tbr(int nx, int ny, const float *__restrict__ hin,
+                                                  const int8_t *__restrict__ mask, const float *__restrict__ rhs,
+                                                  const float *__restrict__ pin, float *__restrict__ pout, float rdx2,
+                                                  float rdy2, float lambda, float omega) {
+  constexpr int M = TBR_M, W = 2 * K, RY = 8 * M, TX = 64 - 2 * W, TY = RY - 2 * W;
+  __shared__ float sa[RY][32], sb[RY][32];  // psi of the even / odd region columns
+  __shared__ float ha[RY][32], hb[RY][32];  // 1/H, read while forming the coefficients
+  const int tx = threadIdx.x, ty = threadIdx.y;
   const int x0 = blockIdx.x * TX - W, y0 = blockIdx.y * TY - W;
-  const int tid = threadIdx.y * blockDim.x + threadIdx.x, nt = blockDim.x * blockDim.y;
-  for (int q = tid; q < RX * RY; q += nt) {
-    const int ly = q / RX, lx = q - ly * RX, gx = x0 + lx, gy = y0 + ly;
-    const bool in = gx >= 0 && gx < nx && gy >= 0 && gy < ny;
-    const size_t g = in ? (size_t)gx + (size_t)nx * gy : 0;
-    const int l = ly * PX + lx;
-    sp[l] = in ? pin[g] : 0.f;
-    sh[l] = in ? hin[g] : 1.f;
-    sr[l] = in ? rhs[g] : 0.f;
-    sm[l] = in ? mask[g] : (int8_t)0;
+  const int gxa = x0 + 2 * tx, gxb = gxa + 1;
+  float pa[M], pb[M], ra[M], rb[M];                       // psi and rhs of cells a and b
+  float cwa[M], cm[M], ceb[M], csa[M], cna[M], csb[M], cnb[M];  // face coefficients (cm: a's east = b's west)
+  float qa[M], qb[M];                                     // reciprocal diagonals
+  unsigned relax = 0;                                     // bit 2m: cell a of row m is relaxed, 2m + 1: cell b
+#pragma unroll
+  for (int m = 0; m < M; m++) {
+    const int ly = ty + 8 * m, gy = y0 + ly;
+    const bool iny = gy >= 0 && gy < ny;
+    const bool ina = iny && gxa >= 0 && gxa < nx, inb = iny && gxb >= 0 && gxb < nx;
+    const size_t ka = ina ? (size_t)gxa + (size_t)nx * gy : 0, kb = inb ? (size_t)gxb + (size_t)nx * gy : 0;
+    pa[m] = ina ? pin[ka] : 0.f;
+    pb[m] = inb ? pin[kb] : 0.f;
+    ra[m] = ina ? rhs[ka] : 0.f;
+    rb[m] = inb ? rhs[kb] : 0.f;
+    ha[ly][tx] = ina ? hin[ka] : 1.f;
+    hb[ly][tx] = inb ? hin[kb] : 1.f;
+    sa[ly][tx] = pa[m];
+    sb[ly][tx] = pb[m];
+    // the region's outer ring is never relaxed (its neighbours lie outside)
+    const bool inner = ly >= 1 && ly < RY - 1;
+    if (inner && ina && tx > 0 && mask[ka]) relax |= 1u << (2 * m);
+    if (inner && inb && tx < 31 && mask[kb]) relax |= 2u << (2 * m);
   }
   __syncthreads();
+#pragma unroll
+  for (int m = 0; m < M; m++) {
+    const int ly = ty + 8 * m, gy = y0 + ly;
+    cwa[m] = cm[m] = ceb[m] = csa[m] = cna[m] = csb[m] = cnb[m] = qa[m] = qb[m] = 0.f;
+    const bool da = (relax >> (2 * m)) & 1, db = (relax >> (2 * m + 1)) & 1;
+    const float hka = ha[ly][tx], hkb = hb[ly][tx];
+    if (da || db) cm[m] = gxa < nx - 1 && gxb > 0 ? face32(hkb, hka, rdx2) : 0.f;
+    if (da) {
+      cwa[m] = gxa > 0 ? face32(hka, hb[ly][tx - 1], rdx2) : 0.f;
+      csa[m] = gy > 0 ? face32(hka, ha[ly - 1][tx], rdy2) : 0.f;
+      cna[m] = gy < ny - 1 ? face32(ha[ly + 1][tx], hka, rdy2) : 0.f;
+      qa[m] = 1.f / (-(((cwa[m] + cm[m]) + csa[m]) + cna[m]) - lambda);
+    }
+    if (db) {
+      ceb[m] = gxb < nx - 1 ? face32(ha[ly][tx + 1], hkb, rdx2) : 0.f;
+      csb[m] = gy > 0 ? face32(hkb, hb[ly - 1][tx], rdy2) : 0.f;
+      cnb[m] = gy < ny - 1 ? face32(hb[ly + 1][tx], hkb, rdy2) : 0.f;
+      qb[m] = 1.f / (-(((cm[m] + ceb[m]) + csb[m]) + cnb[m]) - lambda);
+    }
+  }
+  // colour of this thread's cells a ((gx + gy) & 1, the same in all its rows)
+  const int ca = (x0 + y0 + ty) & 1;
+  // flat views: the ring columns' outer neighbours (never used: those cells
+  // are not relaxed) then stay inside the arrays
+  const float *fa = &sa[0][0], *fb = &sb[0][0];
+#pragma unroll
   for (int pass = 0; pass < 2 * K; pass++) {
-    const int c = pass & 1, lo = pass + 1, hx = RX - pass - 1, hy = RY - pass - 1;
-    for (int ly = lo + threadIdx.y; ly < hy; ly += blockDim.y) {
-      const int gy = y0 + ly;
-      const int lxs = lo + ((c - x0 - gy - lo) & 1);  // first column with (gx + gy) & 1 == c
-      for (int lx = lxs + 2 * threadIdx.x; lx < hx; lx += 2 * blockDim.x) {
-        const int l = ly * PX + lx;
-        if (!sm[l]) continue;
-        const int gx = x0 + lx;
-        const float hk = sh[l];
-        const float cxw = gx > 0 ? face32(hk, sh[l - 1], rdx2) : 0.f;
-        const float cxe = gx < nx - 1 ? face32(sh[l + 1], hk, rdx2) : 0.f;
-        const float cys = gy > 0 ? face32(hk, sh[l - PX], rdy2) : 0.f;
-        const float cyn = gy < ny - 1 ? face32(sh[l + PX], hk, rdy2) : 0.f;
-        const float rcc = 1.f / (-(((cxw + cxe) + cys) + cyn) - lambda);
-        sp[l] = sor32_update(sp[l], sr[l], cxw, cxe, cys, cyn, rcc, sp[l - 1], sp[l + 1], sp[l - PX], sp[l + PX],
-                             omega);
+    const int lo = pass + 1, hi = RY - pass - 1;  // rows that still reach the interior
+    const bool do_a = ca == (pass & 1);           // warp-uniform
+#pragma unroll
+    for (int m = 0; m < M; m++) {
+      const int ly = ty + 8 * m, l = ly * 32 + tx;
+      // rows 8m .. 8m + 7 lie in [lo, hi) in every pass unless m is the first
+      // or last row group: only those test the row (warp-uniform)
+      const bool mid = 8 * m >= 2 * K && 8 * m + 8 <= RY - 2 * K;
+      if (!mid && (ly < lo || ly >= hi)) continue;
+      // relaxed as in the global sweep; cells not relaxed (land, outside the
+      // grid, the region's ring) store their value back unchanged
+      if (do_a) {
+        const float v = sor32_update(pa[m], ra[m], cwa[m], cm[m], csa[m], cna[m], qa[m], fb[l - 1], pb[m],
+                                     fa[l - 32], fa[l + 32], omega);
+        pa[m] = ((relax >> (2 * m)) & 1) ? v : pa[m];
+        sa[ly][tx] = pa[m];
+      } else {
+        const float v = sor32_update(pb[m], rb[m], cm[m], ceb[m], csb[m], cnb[m], qb[m], pa[m], fa[l + 1],
+                                     fb[l - 32], fb[l + 32], omega);
+        pb[m] = ((relax >> (2 * m + 1)) & 1) ? v : pb[m];
+        sb[ly][tx] = pb[m];
       }
     }
     __syncthreads();
   }
-  for (int q = tid; q < TX * TY; q += nt) {
-    const int ly = q / TX, lx = q - ly * TX, gx = x0 + W + lx, gy = y0 + W + ly;
-    if (gx < nx && gy < ny) pout[(size_t)gx + (size_t)nx * gy] = sp[(ly + W) * PX + lx + W];
+#pragma unroll
+  for (int m = 0; m < M; m++) {
+    const int ly = ty + 8 * m, gy = y0 + ly;
+    if (ly < W || ly >= RY - W || gy >= ny) continue;
+    if (2 * tx >= W && 2 * tx < 64 - W && gxa < nx) pout[(size_t)gxa + (size_t)nx * gy] = pa[m];
+    if (2 * tx + 1 >= W && 2 * tx + 1 < 64 - W && gxb < nx) pout[(size_t)gxb + (size_t)nx * gy] = pb[m];
   }
+  (void)TY;
 }
 
 // r = rhs - A psi on ocean cells (0 elsewhere) from the FP64 face
@@ -309,25 +362,23 @@ void sweep32(swm_helm *h, float omega, dim3 b) {
   h->launches += 2;
 }
 
-// tile of the temporally blocked kernel: 64 columns, rows so that the
-// shared arrays (13 bytes per cell with the 2K halo) stay within 48 KB
-constexpr int TB_X = 64;
-template <int K>
-constexpr int tb_rows() { return K == 4 ? 24 : 32; }
-
 template <int K>
 void launch_tb32(swm_helm *h, float omega) {
-  constexpr int TY = tb_rows<K>();
-  const dim3 g((h->nx + TB_X - 1) / TB_X, (h->ny + TY - 1) / TY), b(32, 8);
+  constexpr int TX = 64 - 4 * K, TY = 8 * TBR_M - 4 * K;
+  const dim3 g((h->nx + TX - 1) / TX, (h->ny + TY - 1) / TY), b(32, 8);
   const float rdx2 = (float)(1. / (h->dx * h->dx)), rdy2 = (float)(1. / (h->dy * h->dy)), lam = (float)h->lambda;
-  k_h_tb32<TB_X, TY, K><<<g, b, 0, h->stream>>>(h->nx, h->ny, h->hinv32, h->mask, h->r32, h->e32, h->e32b, rdx2,
-                                                rdy2, lam, omega);
+  k_h_tbr<K><<<g, b, 0, h->stream>>>(h->nx, h->ny, h->hinv32, h->mask, h->r32, h->e32, h->e32b, rdx2, rdy2, lam,
+                                     omega);
 }
+
+// whole temporally blocked launches in n sweeps (none when tbk is 0: global
+// sweeps only)
+int tb_part(const swm_helm *h, int n) { return h->tbk > 0 ? n - n % h->tbk : 0; }
 
 // n FP32 sweeps (a multiple of h->tbk) on A e = r32, ping-ponging e32/e32b;
 // the result ends in h->e32
 void sweeps_tb32(swm_helm *h, float omega, int n) {
-  for (int s = 0; s < n; s += h->tbk) {
+  for (int s = 0; s < n && h->tbk > 0; s += h->tbk) {
     if (h->tbk == 4) launch_tb32<4>(h, omega);
     else if (h->tbk == 2) launch_tb32<2>(h, omega);
     else launch_tb32<1>(h, omega);
@@ -377,7 +428,7 @@ int inner32(swm_helm *h, float omega, double tol, int max_sweeps, int *sweeps, d
   while (s < max_sweeps) {
     // 2 * HELM_CHECK sweeps between checks of the correction equation
     int blk = std::min(2 * HELM_CHECK, max_sweeps - s);
-    const int tb = blk - blk % h->tbk;
+    const int tb = tb_part(h, blk);
     sweeps_tb32(h, omega, tb);
     for (int q = tb; q < blk; q++) sweep32(h, omega, h->blk);
     s += blk;
@@ -574,9 +625,10 @@ int swm_helm_autotune(swm_helm *h, const double *rhs, double omega_lo, double om
   }
   cudaEventDestroy(a);
   cudaEventDestroy(b);
-  // sweeps per temporally blocked launch (SWM_GB300_HELM_K overrides)
+  // sweeps per temporally blocked launch (SWM_GB300_HELM_K overrides; 0:
+  // global sweeps only)
   const char *ek = getenv("SWM_GB300_HELM_K");
-  if (ek && (atoi(ek) == 1 || atoi(ek) == 2 || atoi(ek) == 4)) {
+  if (ek && (atoi(ek) == 0 || atoi(ek) == 1 || atoi(ek) == 2 || atoi(ek) == 4) && ek[0] >= '0' && ek[0] <= '9') {
     h->tbk = atoi(ek);
   } else {
     SWM_CK(cudaEventCreate(&a));
@@ -603,7 +655,7 @@ int swm_helm_autotune(swm_helm *h, const double *rhs, double omega_lo, double om
     const double om = ngrid == 1 ? omega_lo : omega_lo + (omega_hi - omega_lo) * q / (ngrid - 1);
     k_h_to32<<<nb, 256, 0, h->stream>>>(h->rhs, h->r32, h->e32, h->n, bn > 0 ? 1. / bn : 1.);
     h->launches++;
-    const int tb = trial_sweeps - trial_sweeps % h->tbk;
+    const int tb = tb_part(h, trial_sweeps);
     sweeps_tb32(h, (float)om, tb);
     for (int s = tb; s < trial_sweeps; s++) sweep32(h, (float)om, h->blk);
     double e2;
