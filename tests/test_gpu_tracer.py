@@ -118,3 +118,43 @@ def test_fp32_tracer_prefetch_level_does_not_change_results(flux, monkeypatch):
         g.close()
     for a, b in zip(out[0], out[1]):
         assert np.array_equal(a, b)
+
+
+def _gyre_with_n_tracers(n, flux, nsteps):
+    """The gyre with n tracers of different diffusivities; the odd ones relax
+    with a per-cell rate field and the last decays with a per-cell rate."""
+    case = synthetic.double_gyre((48, 40), biharmonic=False, nsteps=nsteps)
+    case['config'].update(tracer_flux=flux)
+    rng = np.random.default_rng(11)
+    ny, nx = case['config']['ny'], case['config']['nx']
+    for q in range(n):
+        gam = rng.uniform(0.5, 2.0, (ny, nx)) / (30 * 86400.0) if q % 2 else None
+        cons = rng.uniform(0.5, 2.0, (ny, nx)) * 1e-7 if q == n - 1 and n > 1 else None
+        case['tracers'].append(dict(varid='C', kappa_h=(50.0, 5e3, 500.0, 20.0, 1e3)[q % 5], cons=1e-7,
+                                    gamma_c=1.0 / (30 * 86400.0), field_C=rng.uniform(0, 1, (ny, nx)),
+                                    field_C0=rng.uniform(0, 1, (ny, nx)), field_gamma_C=gam, field_cons=cons))
+    return case
+
+
+@pytest.mark.parametrize('n', [1, 3, 5])
+def test_fp32_tracer_counts_against_oracle(n):
+    """The tracer kernel's instances for 1 to 4 tracers per launch, and more
+    tracers than one launch takes (5 = 4 + 1), with per-cell relaxation and
+    decay fields, against the oracle."""
+    nsteps = 150
+    case = _gyre_with_n_tracers(n, 1, nsteps)
+    o, g = _pair(case, nsteps, 'fused_fp32c')
+    m = o.ocean('eta').astype(bool)
+    for t in range(n):
+        a, b = g.tracer_field(t, 'CH'), o.tracer_field(t, 'CH0')
+        assert np.isfinite(a[m]).all()
+        assert rel_l2(a, b, m) <= 1e-5, (t, rel_l2(a, b, m))
+
+
+def test_plain_tracer_fields_bit_exact():
+    """Three tracers with per-cell relaxation and decay fields on the FP64
+    tracer kernels: bit for bit with the oracle."""
+    case = _gyre_with_n_tracers(3, 1, 80)
+    o, g = _pair(case, 80, 'plain_fp64')
+    for t in range(3):
+        assert np.array_equal(o.tracer_field(t, 'CH0'), g.tracer_field(t, 'CH'), equal_nan=True), t
