@@ -83,8 +83,11 @@ constexpr int TRC_ROWS = 16;  // output rows per warp
 // PF 1: each iteration also asks L2 for the input rows two beyond those it
 // loads and for the update inputs of the output row after next, so that a
 // state larger than L2 does not make the warp wait on DRAM (trc_prefetch).
+// Resident blocks per SM asked of the register allocator: one tracer fits 6
+// (80 registers, no spill; 2049^2 step 76.0 us against 83.8 at 4), two
+// tracers 4 (at 5 they spill and run slower), more 3.
 template <int NT, int FLUX, int PF>
-__global__ void __launch_bounds__(128, NT <= 2 ? 4 : 3) k_trc32(TrcP p, int S, int nstrips) {
+__global__ void __launch_bounds__(128, NT == 1 ? 6 : (NT == 2 ? 4 : 3)) k_trc32(TrcP p, int S, int nstrips) {
   constexpr int H = 2, TI = 32 - 2 * H;
   const int lane = threadIdx.x & 31;
   // block b: strip b % nstrips, its four warps four consecutive row groups
