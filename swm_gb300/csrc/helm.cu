@@ -97,10 +97,10 @@ __global__ void k_h_sweep32(int nx, int ny, const float *__restrict__ h, const i
   psi[k] = sor32_update(psi[k], rhs[k], cxw, cxe, cys, cyn, rcc, w, e, s, n, omega);
 }
 
-// K red-black sweeps of FP32 SOR on a region of 64 columns by 8M rows
-// (interior 64 - 4K by 8M - 4K, halo 2K), each thread owning, for the whole
+// K red-black sweeps of FP32 SOR on a region of 64 columns by YM rows
+// (interior 64 - 4K by YM - 4K, halo 2K), each thread owning, for the whole
 // launch, the cell pair of region columns 2tx (cell a) and 2tx + 1 (cell b)
-// in rows ty + 8m.  A pair's face coefficients, reciprocal diagonals and rhs
+// in rows ty + Ym.  A pair's face coefficients, reciprocal diagonals and rhs
 // are formed once per launch and kept in registers (the pair shares its
 // inner face).  psi is kept in shared memory split by column parity, so a
 // warp's accesses are contiguous, and each cell's inner neighbour is the
@@ -110,13 +110,16 @@ __global__ void k_h_sweep32(int nx, int ny, const float *__restrict__ h, const i
 // so after 2K passes the interior equals K global sweeps bit for bit; rows
 // that can no longer reach the interior are skipped.  Cells outside the grid
 // hold psi = 0 and are never relaxed.
-constexpr int TBR_M = 5;  // rows per thread
+// TBR_Y x 32 threads per block, TBR_M rows per thread (64 registers: 2
+// blocks, 32 warps per SM); TBR_Y even, so a thread's cells a share one
+// colour
+constexpr int TBR_Y = 16, TBR_M = 3;
 template <int K>
-__global__ void __launch_bounds__(256, 2) k_h_tbr(int nx, int ny, const float *__restrict__ hin,
+__global__ void __launch_bounds__(32 * TBR_Y, 2) k_h_tbr(int nx, int ny, const float *__restrict__ hin,
                                                   const int8_t *__restrict__ mask, const float *__restrict__ rhs,
                                                   const float *__restrict__ pin, float *__restrict__ pout, float rdx2,
                                                   float rdy2, float lambda, float omega) {
-  constexpr int M = TBR_M, W = 2 * K, RY = 8 * M, TX = 64 - 2 * W, TY = RY - 2 * W;
+  constexpr int M = TBR_M, Y = TBR_Y, W = 2 * K, RY = Y * M, TX = 64 - 2 * W, TY = RY - 2 * W;
   __shared__ float sa[RY][32], sb[RY][32];  // psi of the even / odd region columns
   __shared__ float ha[RY][32], hb[RY][32];  // 1/H, read while forming the coefficients
   const int tx = threadIdx.x, ty = threadIdx.y;
@@ -128,7 +131,7 @@ __global__ void __launch_bounds__(256, 2) k_h_tbr(int nx, int ny, const float *_
   unsigned relax = 0;                                     // bit 2m: cell a of row m is relaxed, 2m + 1: cell b
 #pragma unroll
   for (int m = 0; m < M; m++) {
-    const int ly = ty + 8 * m, gy = y0 + ly;
+    const int ly = ty + Y * m, gy = y0 + ly;
     const bool iny = gy >= 0 && gy < ny;
     const bool ina = iny && gxa >= 0 && gxa < nx, inb = iny && gxb >= 0 && gxb < nx;
     const size_t ka = ina ? (size_t)gxa + (size_t)nx * gy : 0, kb = inb ? (size_t)gxb + (size_t)nx * gy : 0;
@@ -148,7 +151,7 @@ __global__ void __launch_bounds__(256, 2) k_h_tbr(int nx, int ny, const float *_
   __syncthreads();
 #pragma unroll
   for (int m = 0; m < M; m++) {
-    const int ly = ty + 8 * m, gy = y0 + ly;
+    const int ly = ty + Y * m, gy = y0 + ly;
     cwa[m] = cm[m] = ceb[m] = csa[m] = cna[m] = csb[m] = cnb[m] = qa[m] = qb[m] = 0.f;
     const bool da = (relax >> (2 * m)) & 1, db = (relax >> (2 * m + 1)) & 1;
     const float hka = ha[ly][tx], hkb = hb[ly][tx];
@@ -177,10 +180,10 @@ __global__ void __launch_bounds__(256, 2) k_h_tbr(int nx, int ny, const float *_
     const bool do_a = ca == (pass & 1);           // warp-uniform
 #pragma unroll
     for (int m = 0; m < M; m++) {
-      const int ly = ty + 8 * m, l = ly * 32 + tx;
-      // rows 8m .. 8m + 7 lie in [lo, hi) in every pass unless m is the first
-      // or last row group: only those test the row (warp-uniform)
-      const bool mid = 8 * m >= 2 * K && 8 * m + 8 <= RY - 2 * K;
+      const int ly = ty + Y * m, l = ly * 32 + tx;
+      // rows Ym .. Ym + Y - 1 lie in [lo, hi) in every pass unless m is the
+      // first or last row group: only those test the row (warp-uniform)
+      const bool mid = Y * m >= 2 * K && Y * m + Y <= RY - 2 * K;
       if (!mid && (ly < lo || ly >= hi)) continue;
       // relaxed as in the global sweep; cells not relaxed (land, outside the
       // grid, the region's ring) store their value back unchanged
@@ -200,7 +203,7 @@ __global__ void __launch_bounds__(256, 2) k_h_tbr(int nx, int ny, const float *_
   }
 #pragma unroll
   for (int m = 0; m < M; m++) {
-    const int ly = ty + 8 * m, gy = y0 + ly;
+    const int ly = ty + Y * m, gy = y0 + ly;
     if (ly < W || ly >= RY - W || gy >= ny) continue;
     if (2 * tx >= W && 2 * tx < 64 - W && gxa < nx) pout[(size_t)gxa + (size_t)nx * gy] = pa[m];
     if (2 * tx + 1 >= W && 2 * tx + 1 < 64 - W && gxb < nx) pout[(size_t)gxb + (size_t)nx * gy] = pb[m];
@@ -364,8 +367,8 @@ void sweep32(swm_helm *h, float omega, dim3 b) {
 
 template <int K>
 void launch_tb32(swm_helm *h, float omega) {
-  constexpr int TX = 64 - 4 * K, TY = 8 * TBR_M - 4 * K;
-  const dim3 g((h->nx + TX - 1) / TX, (h->ny + TY - 1) / TY), b(32, 8);
+  constexpr int TX = 64 - 4 * K, TY = TBR_Y * TBR_M - 4 * K;
+  const dim3 g((h->nx + TX - 1) / TX, (h->ny + TY - 1) / TY), b(32, TBR_Y);
   const float rdx2 = (float)(1. / (h->dx * h->dx)), rdy2 = (float)(1. / (h->dy * h->dy)), lam = (float)h->lambda;
   k_h_tbr<K><<<g, b, 0, h->stream>>>(h->nx, h->ny, h->hinv32, h->mask, h->r32, h->e32, h->e32b, rdx2, rdy2, lam,
                                      omega);
