@@ -383,6 +383,7 @@ int tb_part(const swm_helm *h, int n) { return h->tbk > 0 ? n - n % h->tbk : 0; 
 void sweeps_tb32(swm_helm *h, float omega, int n) {
   for (int s = 0; s < n && h->tbk > 0; s += h->tbk) {
     if (h->tbk == 4) launch_tb32<4>(h, omega);
+    else if (h->tbk == 3) launch_tb32<3>(h, omega);
     else if (h->tbk == 2) launch_tb32<2>(h, omega);
     else launch_tb32<1>(h, omega);
     std::swap(h->e32, h->e32b);
@@ -631,13 +632,13 @@ int swm_helm_autotune(swm_helm *h, const double *rhs, double omega_lo, double om
   // sweeps per temporally blocked launch (SWM_GB300_HELM_K overrides; 0:
   // global sweeps only)
   const char *ek = getenv("SWM_GB300_HELM_K");
-  if (ek && (atoi(ek) == 0 || atoi(ek) == 1 || atoi(ek) == 2 || atoi(ek) == 4) && ek[0] >= '0' && ek[0] <= '9') {
+  if (ek && atoi(ek) >= 0 && atoi(ek) <= 4 && ek[0] >= '0' && ek[0] <= '9') {
     h->tbk = atoi(ek);
   } else {
     SWM_CK(cudaEventCreate(&a));
     SWM_CK(cudaEventCreate(&b));
     float kbest = 1e30f;
-    for (int kk : {1, 2, 4}) {
+    for (int kk : {1, 2, 3, 4}) {
       h->tbk = kk;
       sweeps_tb32(h, 1.f, 4);
       SWM_CK(cudaEventRecord(a, h->stream));
