@@ -291,15 +291,18 @@ def side_measurements(args, case, g32, stream, flush, ncell):
     return out
 
 
-def ensemble_measurement(args, n_members=256, steps=200, one_by_one=True):
+def ensemble_measurement(args, n_members=256, steps=200, one_by_one=True, err_members=8):
     """The batched FP32 path on 256 basins of uneven sizes (Nx, Ny
     log-uniform in 64-512, Laplacian Ah = 500), against the same members
-    stepped one by one on the FP64 plain path."""
+    stepped one by one on the FP64 plain path; with one_by_one, also the
+    batched members' error against the FP64 plain path after
+    args.error_steps steps, on err_members members spread over the sizes."""
     import torch
     from swm_gb300.host import synthetic
     from swm_gb300.host.driver import Driver
     from swm_gb300.model import GpuEnsemble, GpuModel
-    cases = synthetic.ensemble_members(n=n_members, nsteps=steps + 100)
+    err_steps = max(getattr(args, 'error_steps', 0), 12 + steps) if one_by_one else 0
+    cases = synthetic.ensemble_members(n=n_members, nsteps=max(steps + 100, err_steps + 10))
     cells = sum((c['config']['nx'] - 1) * (c['config']['ny'] - 1) for c in cases)
     pts = sum(c['config']['nx'] * c['config']['ny'] for c in cases)
     ms = []
@@ -320,11 +323,37 @@ def ensemble_measurement(args, n_members=256, steps=200, one_by_one=True):
     launches = ens.launch_count() - l0
     ms_step = a.elapsed_time(b) / steps
     ints = ens.integrals()
+    err = None
+    if one_by_one:
+        # continue the batched run to err_steps, then compare members spread
+        # over the sizes with the FP64 plain path from the same start
+        ens.run(12 + steps, err_steps - 12 - steps)
+        ens.synchronize()
+        order = sorted(range(n_members), key=lambda i: cases[i]['config']['nx'] * cases[i]['config']['ny'])
+        pick = [order[round(q * (n_members - 1) / (err_members - 1))] for q in range(err_members)]
+        worst = {f: {'rel_l2': 0.0, 'rel_max': 0.0} for f in ('u', 'v', 'eta')}
+        for i in pick:
+            ref = GpuModel('plain_fp64')
+            Driver(cases[i], ref).init(with_diag=False)
+            ref.run(0, err_steps)
+            for f in ('u', 'v', 'eta'):
+                m = ref.ocean(f).astype(bool)
+                a, b = ms[i].field(f)[m], ref.field(f)[m]
+                den = max(float(np.linalg.norm(b)), 1e-300)
+                worst[f]['rel_l2'] = max(worst[f]['rel_l2'], float(np.linalg.norm(a - b)) / den)
+                worst[f]['rel_max'] = max(worst[f]['rel_max'],
+                                          float(np.abs(a - b).max() / max(np.abs(b).max(), 1e-300)))
+            ref.close()
+        err = {'steps': err_steps, 'members': len(pick),
+               'sizes': [[cases[i]['config']['nx'], cases[i]['config']['ny']] for i in pick],
+               'worst_over_members': worst}
     out = {'members': n_members, 'cells': cells, 'array_points': pts, 'steps': steps,
            'ms_per_step': ms_step, 'value': cells / (ms_step * 1e-3), 'unit': 'cell-steps/s',
            'rows_per_strip': ens.rows(), 'gpu_launches': launches,
            'l2': 'not flushed: the ensemble state (%.2f GB) is larger than L2' % (89 * pts / 1e9),
            'finite_integrals': bool(np.isfinite(ints).all())}
+    if err is not None:
+        out['fp32c_error_vs_fp64'] = err
     peak, kind = peaks()
     ach = 89 * pts / (ms_step * 1e-3) / 1e9
     out['roofline'] = {'bound': 'hbm', 'achieved': ach, 'peak': peak, 'unit': 'GB/s', 'frac': ach / peak,
