@@ -87,3 +87,41 @@ def test_temporal_blocking_does_not_change_results(case, monkeypatch):
     for r in res[1:]:
         assert r[1] == res[0][1] and r[2] == res[0][2]
         assert np.array_equal(r[0], res[0][0])
+
+
+@pytest.fixture(scope='module')
+def edge_case(case):
+    """A 13 x 21 slice of the basin whose edge cells are ocean (the other
+    cases have a land frame), so the zero face coefficients at the grid's
+    edge are exercised; smaller than one tiled region in both directions."""
+    sl = (slice(30, 43), slice(40, 61))
+    ocean = np.ones((13, 21), dtype=np.int8)
+    ocean[5:7, 8:11] = 0
+    rhs = 1e-10 * np.random.default_rng(4).standard_normal((13, 21)) * ocean
+    return dict(H=case['H'][sl].copy(), ocean=ocean, rhs=rhs, dx=case['dx'], dy=case['dy'], lam=case['lam'])
+
+
+def test_edge_ocean_fp64_solve_bit_exact(edge_case):
+    c = edge_case
+    g = GpuHelmholtz(c['H'], c['ocean'], c['dx'], c['dy'], c['lam'])
+    cx, cy, cc = _oracle(c)
+    po, so, ro = helmholtz_sor(cx, cy, cc, c['ocean'], c['rhs'], np.zeros_like(c['H']), 1.5, 1e-10, 5000)
+    pg, sg, _, rg, rc = g.solve(c['rhs'], omega=1.5, rtol=1e-10, max_sweeps=5000)
+    assert rc == 0 and sg == so and np.array_equal(pg, po)
+
+
+def test_edge_ocean_tiles_equal_global_sweeps(edge_case, monkeypatch):
+    """Mixed solves with global sweeps only and with K = 1 .. 4 sweeps per
+    tiled launch agree bit for bit on the small edge-ocean grid."""
+    c = edge_case
+    res = []
+    for k in ('0', '1', '2', '3', '4'):
+        monkeypatch.setenv('SWM_GB300_HELM_K', k)
+        g = GpuHelmholtz(c['H'], c['ocean'], c['dx'], c['dy'], c['lam'])
+        g.autotune(c['rhs'], 1.5, 1.5, 1, 16)
+        res.append(g.solve(c['rhs'], omega=1.5, rtol=1e-10, mixed=True))
+        g.close()
+    assert res[0][4] == 0
+    for r in res[1:]:
+        assert r[1] == res[0][1] and r[2] == res[0][2]
+        assert np.array_equal(r[0], res[0][0])
