@@ -272,20 +272,26 @@ def side_measurements(args, case, g32, stream, flush, ncell):
         ms = timed_steps(g, 3, k, flush, __import__('torch').cuda.ExternalStream(g.stream()))
         out[path] = {'ms_per_step': float(ms.mean()), 'value': ncell / (ms.mean() * 1e-3), 'steps': k}
         g.close()
-    # FP32C against the bit-exact FP64 plain path from the same start
+    # FP32C against the bit-exact FP64 plain path from the same start, with
+    # the relative L2 errors along the way (error against time)
     e = args.error_steps
     _, gp, _ = build_model('plain_fp64', args.cells, e)
     _, gc, _ = build_model('fused_fp32c', args.cells, e)
-    gp.run(0, e)
-    gc.run(0, e)
-    errs = {}
-    for f, grid in (('u', 'u'), ('v', 'v'), ('eta', 'eta')):
-        m = gp.ocean(grid).astype(bool)
-        a, b = gc.field(f), gp.field(f)
-        den = np.linalg.norm(b[m])
-        errs[f] = {'rel_l2': float(np.linalg.norm((a - b)[m]) / den) if den > 0 else None,
-                   'rel_max': float(np.abs(a - b)[m].max() / max(np.abs(b[m]).max(), 1e-300))}
-    out['fp32c_error_vs_fp64'] = {'steps': e, 'fields': errs}
+    masks = {grid: gp.ocean(grid).astype(bool) for grid in ('u', 'v', 'eta')}
+    curve, done = [], 0
+    for c in sorted({c for c in (1000, 2000, 5000, 10000, 20000) if c < e} | {e}):
+        gp.run(done, c - done)
+        gc.run(done, c - done)
+        done = c
+        errs = {}
+        for f in ('u', 'v', 'eta'):
+            m = masks[f]
+            a, b = gc.field(f), gp.field(f)
+            den = np.linalg.norm(b[m])
+            errs[f] = {'rel_l2': float(np.linalg.norm((a - b)[m]) / den) if den > 0 else None,
+                       'rel_max': float(np.abs(a - b)[m].max() / max(np.abs(b[m]).max(), 1e-300))}
+        curve.append({'steps': c, **{f: errs[f]['rel_l2'] for f in errs}})
+    out['fp32c_error_vs_fp64'] = {'steps': e, 'fields': errs, 'rel_l2_curve': curve}
     gp.close()
     gc.close()
     return out
