@@ -85,9 +85,12 @@ constexpr int TRC_ROWS = 16;  // output rows per warp
 // state larger than L2 does not make the warp wait on DRAM (trc_prefetch).
 // Resident blocks per SM asked of the register allocator: one tracer fits 6
 // (80 registers, no spill; 2049^2 step 76.0 us against 83.8 at 4), two
-// tracers 4 (at 5 they spill and run slower), more 3.
+// tracers 4 (at 5 they spill and run slower), three 4 with the updated row's
+// CH pair reloaded instead of carried (RELOAD; 2049^2 step 169 us against
+// 176 at 3 blocks), four 3.
 template <int NT, int FLUX, int PF>
-__global__ void __launch_bounds__(128, NT == 1 ? 6 : (NT == 2 ? 4 : 3)) k_trc32(TrcP p, int S, int nstrips) {
+__global__ void __launch_bounds__(128, NT == 1 ? 6 : (NT <= 3 ? 4 : 3)) k_trc32(TrcP p, int S, int nstrips) {
+  constexpr bool RELOAD = NT == 3;
   constexpr int H = 2, TI = 32 - 2 * H;
   const int lane = threadIdx.x & 31;
   // block b: strip b % nstrips, its four warps four consecutive row groups
@@ -153,15 +156,19 @@ __global__ void __launch_bounds__(128, NT == 1 ? 6 : (NT == 2 ? 4 : 3)) k_trc32(
       rr[a] = rr[a - 1];
 #pragma unroll
       for (int q = 0; q < NT; q++) {
-        chh[q][a] = chh[q][a - 1];
-        chl[q][a] = chl[q][a - 1];
+        if (!RELOAD) {
+          chh[q][a] = chh[q][a - 1];
+          chl[q][a] = chl[q][a - 1];
+        }
       }
     }
     m[0] = n1.m; D[0] = n1.D; rD[0] = rthick(n1.D); u[0] = n1.u; v[0] = n1.v; off[0] = n1.off; rr[0] = n1.rows;
 #pragma unroll
     for (int q = 0; q < NT; q++) {
-      chh[q][0] = n1.h[q];
-      chl[q][0] = n1.l[q];
+      if (!RELOAD) {
+        chh[q][0] = n1.h[q];
+        chl[q][0] = n1.l[q];
+      }
       chs[q][0] = n1.h[q] + n1.l[q];
     }
     n1 = n2;
@@ -257,7 +264,8 @@ __global__ void __launch_bounds__(128, NT == 1 ? 6 : (NT == 2 ? 4 : 3)) k_trc32(
           t.G3[ko] = g;
           const float inc = p.dt * (p.ab0 * pg1[q] + p.ab1 * pg2[q] + p.ab2 * g);
           float nh, nl;
-          comp_update(chh[q][2], chl[q][2], inc, t.dp ? t.dp[ko] : t.dp_s, nh, nl);
+          comp_update(RELOAD ? t.ch[ko] : chh[q][2], RELOAD ? t.cl[ko] : chl[q][2], inc, t.dp ? t.dp[ko] : t.dp_s,
+                      nh, nl);
           t.chn[ko] = nh;
           t.cln[ko] = nl;
         }
