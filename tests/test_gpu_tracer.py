@@ -84,18 +84,21 @@ def test_fp32_tracers_graph_replay_and_launches():
         assert np.array_equal(a.tracer_field(t, 'CH'), b.tracer_field(t, 'CH')), t
 
 
-@pytest.mark.parametrize('flux', [0, 1])
-def test_fp32_tracer_rows_per_warp_do_not_change_results(flux, monkeypatch):
+@pytest.mark.parametrize('flux,ntr', [(0, 2), (1, 2), (1, 3)])
+def test_fp32_tracer_rows_per_warp_do_not_change_results(flux, ntr, monkeypatch):
     """Each tracer point is computed from the same inputs whatever the rows
-    per warp strip: the results agree bit for bit."""
+    per warp strip: the results agree bit for bit (three tracers: the
+    instance that reloads the updated row's CH pair)."""
     case = synthetic.tracer_flow(72, nsteps=30, flux=flux)
+    while len(case['tracers']) < ntr:
+        case['tracers'].append(dict(case['tracers'][0], kappa_h=500.0))
     out = []
     for rows in ('5', '16', '23'):
         monkeypatch.setenv('SWM_GB300_TRC_ROWS', rows)
         g = GpuModel('fused_fp32c', tracer_nan_guard=True)
         Driver(case, g).init(with_diag=False)
         g.run(0, 25)
-        out.append([g.tracer_field(t, 'CH') for t in range(2)])
+        out.append([g.tracer_field(t, 'CH') for t in range(ntr)])
         g.close()
     for other in out[1:]:
         for a, b in zip(out[0], other):
