@@ -208,7 +208,6 @@ __global__ void __launch_bounds__(32 * TBR_Y, 2) k_h_tbr(int nx, int ny, const f
     if (2 * tx >= W && 2 * tx < 64 - W && gxa < nx) pout[(size_t)gxa + (size_t)nx * gy] = pa[m];
     if (2 * tx + 1 >= W && 2 * tx + 1 < 64 - W && gxb < nx) pout[(size_t)gxb + (size_t)nx * gy] = pb[m];
   }
-  (void)TY;
 }
 
 // r = rhs - A psi on ocean cells (0 elsewhere) from the FP64 face
