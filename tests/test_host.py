@@ -1,7 +1,12 @@
 """Host-side logic that needs no GPU: namelist and model.h readers, the
-memchunk time interpolation, case files, the synthetic workloads."""
+memchunk time interpolation, case files, the synthetic workloads, and
+bench.py's reading of the committed step-kernel profile."""
+import os
+
 import numpy as np
 import pytest
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
 
 from swm_gb300.host import caseio, memchunk, modelh, namelist, synthetic
 
@@ -87,3 +92,17 @@ def test_perturbed_basin_is_closed_with_bounded_inset():
     H = synthetic.perturbed_basin(40, 30, 500.0, np.random.default_rng(1), max_inset=3)
     assert (H[0] == 0).all() and (H[-1] == 0).all() and (H[:, 0] == 0).all() and (H[:, -1] == 0).all()
     assert (H[4:-4, 4:-4] == 500.0).all()
+
+
+def test_bench_reads_the_step_kernel_traffic_from_its_profile():
+    """bench.py's roofline.traffic for the default workload comes from the
+    committed ncu summary of the step kernel: it must be there and parse, and
+    lie between the kernel's written bytes and twice its algorithmic bytes
+    (89 B per point of the 1025^2 basin)."""
+    import importlib.util
+    spec = importlib.util.spec_from_file_location('bench_mod', os.path.join(ROOT, 'bench.py'))
+    bench = importlib.util.module_from_spec(spec)
+    spec.loader.exec_module(bench)
+    t = bench.profiled_traffic('fused_fp32c', 1024)
+    assert t is not None
+    assert 20e6 < t < 2 * 89 * 1025 * 1025
