@@ -236,7 +236,9 @@ int swm_gpu_integrals_async(swm_gpu_ctx *ctx, double *out3, int64_t *ticket);
    stall).  No counterpart in the reference.  Grids of at most
    SWM_NOALLOC_MAX_NY rows (SWM_GPU_EINVAL beyond).  The first call on a
    device looks up the array's device address; make that first call before
-   any stream capture.  The array is shared by all contexts on a device:
+   any stream capture.  Every call waits on the context's stream for its
+   result, so it is never valid on a stream under capture: it returns
+   SWM_GPU_EINVAL there.  The array is shared by all contexts on a device:
    calls that overlap in time on one device race and must be serialised. */
 #define SWM_NOALLOC_MAX_NY 8192
 int swm_gpu_integrals_noalloc(swm_gpu_ctx *ctx, double *out3);

@@ -1422,6 +1422,12 @@ extern "C" int swm_gpu_integrals_noalloc(swm_gpu_ctx *c, double *out3) {
               " rows; the fixed scratch serves at most " + std::to_string(SWM_NOALLOC_MAX_NY));
     return SWM_GPU_EINVAL;
   }
+  // the call ends by waiting for its result, which a stream under capture
+  // cannot do (the wait would invalidate the capture)
+  cudaStreamCaptureStatus cap = cudaStreamCaptureStatusNone;
+  SWM_CK(cudaStreamIsCapturing(c->stream, &cap));
+  SWM_REQUIRE(cap == cudaStreamCaptureStatusNone,
+              "swm_gpu_integrals_noalloc: the context's stream is being captured; this call waits for its result");
   int dev = -1;
   SWM_CK(cudaGetDevice(&dev));
   SWM_REQUIRE(dev >= 0 && dev < NOALLOC_MAX_DEVICES, "swm_gpu_integrals_noalloc: device ordinal out of range");

@@ -313,7 +313,10 @@ __device__ __forceinline__ void march_strip(const P32 &p, const int bx, const in
         are = area[2 * ny + o];
       }
       if (XE(mm)) {
-        float dmv = fe.x * ((mvh[1] - mvh[2]) + (mvl[1] - mvl[2])) + fe.y * mvh[2];
+        // cos_{o+1} MV_{o+1} - cos_o MV_o as cos_{o+1} (MV_{o+1} - MV_o) +
+        // (cos_{o+1} - cos_o) MV_o; the second product takes the whole MV_o,
+        // hi + lo, because lo holds the free-surface part eta * v
+        float dmv = fe.x * ((mvh[1] - mvh[2]) + (mvl[1] - mvl[2])) + fe.y * mvs2;
         ge = -((muh2_r - muh[2]) + (mul2_r - mul[2])) * fe.z - dmv * fe.w;
         if (has_F) ge += p.Fe[ko];
       }

@@ -3,8 +3,17 @@
 Reads <reference>/selfcheck/<case>/{model.h, model.namelist, input/*.nc,
 output/reference_*.nc} and writes tests/golden/<case>.npz with the resolved
 configuration, the input fields and the reference's FP64 output records
-(the goldens the oracle is pinned against).  Run once where the reference
-tree is mounted:  python tests/golden/make_golden.py /path/to/reference
+(the goldens the oracle is pinned against).
+
+selfcheck/test_nonlinear and selfcheck/test_nl_tracer ship their
+configuration and inputs but not their outputs (the reference tree lists
+those as missing large files), so they are packed as inputs only: they are
+the reference's own configurations of the nonlinear and tracer paths on the
+real sphere (A = 6371 km, 25S-25N), which the GPU paths are checked on
+against the oracle.
+
+Run once where the reference tree is mounted:
+    python tests/golden/make_golden.py <path of the swm source tree>
 """
 import os
 import sys
@@ -21,6 +30,9 @@ CASES = {
     'test_diaglist': ['u_out.nc', 'v_out.nc', 'eta_out.nc', 'psi_out.nc', 'u_mean_out.nc', 'eta2_mean_out.nc',
                       'H_out.nc', 'impl_u.nc', 'impl_v.nc', 'impl_n.nc', 'gamma_u.nc', 'gamma_v.nc', 'gamma_n.nc',
                       'edens.nc', 'potvort.nc', 'relvort.nc', 'mu.nc', 'mv.nc', 'd.nc'],
+    # inputs only: the outputs of these two runs are not in the source tree
+    'test_nonlinear': [],
+    'test_nl_tracer': [],
 }
 
 
@@ -50,4 +62,6 @@ def main(ref):
 
 
 if __name__ == '__main__':
-    main(sys.argv[1] if len(sys.argv) > 1 else '/root/reference')
+    if len(sys.argv) != 2:
+        sys.exit('usage: make_golden.py <path of the swm source tree>')
+    main(sys.argv[1])
