@@ -1,20 +1,29 @@
 """Benchmark of the SWM time step on GB300 (one JSON line on stdout).
 
-Workload: the nonlinear wind-driven double gyre on 1024 x 1024 cells
-(dx = 5 km, beta-plane f0 = 1e-4, beta = 2e-11, H = 500 m, tau = 0.1 cos(2 pi
-y/L), biharmonic viscosity 1e10 m^4/s, bottom drag 1e-7 /s, seeded coastline,
-rest start), synthetic seeded inputs.  One bench step = one model time step
-(swm_gpu_step + swm_gpu_advance) of the whole basin.
+Headline workload (the metric's "FP32 batched"): an ensemble of 256
+nonlinear wind-driven basins of uneven sizes (Nx, Ny log-uniform in 64-512,
+dx 5-20 km, wind amplitude 0.05-0.2 N/m^2, seeded coastline, Laplacian Ah =
+500 m^2/s, rest start), synthetic seeded inputs, FP32 compensated state,
+stepped by one persistent launch per step.  One bench step = one model time
+step (SWM_timestep + model_advance) of every member.
 
-value: cell-steps/s of the selected path (default fused_fp32c, the FP32
-compensated path) with the state resident in HBM; the L2 cache (129 MB; the
-per-step working set is ~85 MB) is flushed by a 512 MB device write before
-every timed step, and each step is timed with CUDA events on the library's
-stream.  e2e: the same metric through the C ABI with host buffers: every step
-takes that step's wind-stress rows from host memory (H2D) and returns the
-FP64 domain integrals of its result to host memory (D2H), wall clock.  --impl reference times the CPU restatement of
-the reference's loops (the Fortran reference cannot be built here: no Fortran
-compiler) on the host cores.
+value: cell-steps/s of the batched path with the state resident in HBM;
+the state (1.07 GB) is larger than the 129 MB L2, so no flush is needed
+between steps; the K steps are timed with CUDA events on the ensemble's
+stream.  e2e: the same metric through the C ABI with host buffers: every
+step takes every member's wind-stress rows from pinned host memory (H2D)
+and returns every member's FP64 domain integrals to pinned host memory
+(D2H), swm_gpu_ensemble_run_monitor, wall clock.  Under torchrun the
+members of an N x 256-member ensemble are split across the ranks by cell
+count (weak scaling, no collective on the data path).
+
+Side measurements (rank 0): the same members one by one on the FP64 plain
+path (the metric's "FP64 plain"), the batched members' error against FP64
+after --error-steps, the single 1024^2 double gyre, the tracer, Helmholtz,
+SOR and linear reduced-gravity workloads, and the CPU restatement of the
+reference's loops on a sample of the ensemble.  --impl reference times that
+CPU restatement (the Fortran reference cannot be built: no Fortran compiler)
+on the host cores, on the headline ensemble.
 """
 import argparse
 import json
@@ -30,24 +39,33 @@ ROOT = os.path.dirname(os.path.abspath(__file__))
 sys.path.insert(0, ROOT)
 
 METRIC = 'grid-cell-steps/s on 1 GB300, FP32 batched vs FP64 plain, at stated L2 error'
+_T0 = time.time()
+
+
+def note(msg):
+    """Progress of the run on stderr (stdout carries the one JSON line)."""
+    print('[bench %7.1f s] %s' % (time.time() - _T0, msg), file=sys.stderr, flush=True)
 BYTES_PER_POINT = {'fused_fp32c': 89, 'fused_fp64': 129, 'plain_fp64': 129}
 
 
 def parse():
     ap = argparse.ArgumentParser()
     ap.add_argument('--gpus', type=int, default=1)
-    ap.add_argument('--steps', type=int, default=2000)
+    ap.add_argument('--steps', type=int, default=1000)
     ap.add_argument('--warmup', type=int, default=20)
     ap.add_argument('--impl', default='ours', choices=['ours', 'reference'])
-    ap.add_argument('--path', default='fused_fp32c', choices=['fused_fp32c', 'fused_fp64', 'plain_fp64'])
-    ap.add_argument('--cells', type=int, default=1024)
-    ap.add_argument('--error-steps', type=int, default=1000)
+    ap.add_argument('--members', type=int, default=256, help='ensemble members per GPU')
+    ap.add_argument('--path', default='fused_fp32c', choices=['fused_fp32c', 'fused_fp64', 'plain_fp64'],
+                    help='path of the single-basin double gyre (--workload double_gyre)')
+    ap.add_argument('--cells', type=int, default=1024, help='cells per side of the single-basin double gyre')
+    ap.add_argument('--error-steps', type=int, default=10000)
+    ap.add_argument('--e2e-steps', type=int, default=1000)
     ap.add_argument('--quick', action='store_true', help='skip the side measurements')
     ap.add_argument('--device-only', action='store_true',
                     help='only the warm-up and timed device steps (the form to run under ncu)')
-    ap.add_argument('--workload', default='double_gyre',
-                    choices=['double_gyre', 'ensemble', 'tracer', 'helmholtz', 'linear_rg'],
-                    help='ensemble / tracer: print that measurement alone (profiling)')
+    ap.add_argument('--workload', default='ensemble',
+                    choices=['ensemble', 'double_gyre', 'tracer', 'helmholtz', 'linear_rg', 'sor'],
+                    help='ensemble: the headline line; the others print that measurement alone')
     return ap.parse_args()
 
 
@@ -73,6 +91,16 @@ def allmax(ws, x):
     import torch.distributed as dist
     t = torch.tensor([x], dtype=torch.float64)
     dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def allsum(ws, x):
+    if ws == 1:
+        return x
+    import torch
+    import torch.distributed as dist
+    t = torch.tensor([x], dtype=torch.float64)
+    dist.all_reduce(t, op=dist.ReduceOp.SUM)
     return float(t.item())
 
 
@@ -162,33 +190,36 @@ def timed_steps(g, itt0, k, flush=None, stream=None):
     return np.array([a.elapsed_time(b) for a, b in ev])
 
 
-def ours(args, rank, ws):
+def double_gyre_line(args, rank, ws, steps, warmup, side=True):
+    """The single-basin double gyre (args.cells^2, biharmonic) on args.path:
+    device steps with the L2 flushed before each, back-to-back steps, the
+    monitored end-to-end run, and (side) the FP64 paths and the FP32 error
+    against FP64 after args.error_steps."""
     import torch
-    torch.cuda.set_device(int(os.environ.get('LOCAL_RANK', '0')))
     cells = args.cells
     npts = (cells + 1) * (cells + 1)  # array points (Nx, Ny) = cells + 1: the bytes moved
     ncell = cells * cells              # cells: the unit of the metric
-    case, g, drv = build_model(args.path, cells, args.warmup + args.steps)
+    case, g, drv = build_model(args.path, cells, warmup + steps)
     stream = torch.cuda.ExternalStream(g.stream())
     flush = torch.empty(512 * 1024 * 1024 // 4, dtype=torch.float32, device='cuda')
     itt = 0
-    g.run(itt, args.warmup)
-    itt += args.warmup
+    g.run(itt, warmup)
+    itt += warmup
     g.synchronize()
     barrier(ws)
     torch.cuda.synchronize()
     l0 = g.launch_count()
     t0 = time.perf_counter()
     with ClockSampler(int(os.environ.get('LOCAL_RANK', '0'))) as clk:
-        ms = timed_steps(g, itt, args.steps, flush, stream)
+        ms = timed_steps(g, itt, steps, flush, stream)
     wall = time.perf_counter() - t0
     launches = g.launch_count() - l0
-    itt += args.steps
+    itt += steps
     barrier(ws)
     step_ms = allmax(ws, float(ms.mean()))
     value = ncell * ws / (step_ms * 1e-3)
-    line = {'metric': METRIC, 'value': value, 'unit': 'cell-steps/s', 'n_gpus': ws, 'steps': args.steps,
-            'warmup': args.warmup, 'ms_per_step': step_ms, 'higher_is_better': True, 'scaling': 'weak',
+    line = {'metric': METRIC, 'value': value, 'unit': 'cell-steps/s', 'n_gpus': ws, 'steps': steps,
+            'warmup': warmup, 'ms_per_step': step_ms, 'higher_is_better': True, 'scaling': 'weak',
             'vs_baseline': None, 'dtype': 'f32' if args.path == 'fused_fp32c' else 'f64',
             'data': 'synthetic (seeded double-gyre basin, rest start)',
             'config': {'workload': 'double_gyre_%dx%d_biharmonic' % (cells, cells), 'cells': cells * cells,
@@ -203,7 +234,8 @@ def ours(args, rank, ws):
     peak, kind = peaks()
     alg = BYTES_PER_POINT[args.path] * npts
     achieved = alg / (step_ms * 1e-3) / 1e9
-    traffic = profiled_traffic(args.path, cells)
+    kname = {'fused_fp32c': 'k_march', 'fused_fp64': 'k_fused'}.get(args.path)
+    traffic = profiled_traffic('%s_double_gyre_%d.md' % (kname, cells)) if kname else None
     line['roofline'] = {'bound': 'hbm', 'achieved': achieved, 'peak': peak, 'unit': 'GB/s',
                         'frac': achieved / peak, 'traffic': traffic, 'peak_kind': kind,
                         'algorithmic_bytes_per_launch': alg,
@@ -219,7 +251,7 @@ def ours(args, rank, ws):
     # wind-stress row profile from pinned host memory and returns the FP64
     # domain integrals of its result into pinned host memory, through
     # swm_gpu_run_monitor (one C call issues all steps; no host wait per step)
-    k_e2e = min(args.steps, 1000)
+    k_e2e = args.e2e_steps
     ny = case['config']['ny']
     rows_pin = torch.empty((k_e2e, ny), dtype=torch.float64).pin_memory().numpy()
     prof = case['streams'][0]['rec1'][0][:, 0]
@@ -237,24 +269,17 @@ def ours(args, rank, ws):
                                'step kernel before the step; swm_gpu_step + swm_gpu_advance; D2H: the FP64 '
                                'domain integrals of the new state, written into pinned host memory; all steps '
                                'issued by swm_gpu_run_monitor; wall clock including the final wait; no L2 flush'}
-    if rank == 0 and not args.quick:
+    if rank == 0 and side:
         line.update(side_measurements(args, case, g, stream, flush, ncell))
         line['speedup_vs_fp64_plain'] = line['plain_fp64']['ms_per_step'] / step_ms
-        line['ensemble'] = ensemble_measurement(args)
-        line['tracer'] = tracer_measurement(args)
-        line['helmholtz'] = helmholtz_measurement(args)
-        line['linear_rg'] = linear_rg_measurement(args)
-    if rank == 0 and ws == 1 and not args.quick:
-        line['cpu_baseline'] = cpu_baseline(cells)
     g.close()
     return line
 
 
-def profiled_traffic(path, cells):
-    """DRAM bytes per launch of the step kernel from the committed ncu summary."""
-    name = {'fused_fp32c': 'k_march', 'fused_fp64': 'k_fused'}.get(path)
-    f = os.path.join(ROOT, 'profiles', '%s_double_gyre_%d.md' % (name, cells))
-    if name is None or not os.path.exists(f):
+def profiled_traffic(fname):
+    """DRAM bytes per launch of a kernel from its committed ncu summary."""
+    f = os.path.join(ROOT, 'profiles', fname)
+    if not os.path.exists(f):
         return None
     with open(f) as fh:
         for l in fh:
@@ -297,79 +322,143 @@ def side_measurements(args, case, g32, stream, flush, ncell):
     return out
 
 
-def ensemble_measurement(args, n_members=256, steps=200, one_by_one=True, err_members=8):
-    """The batched FP32 path on 256 basins of uneven sizes (Nx, Ny
-    log-uniform in 64-512, Laplacian Ah = 500), against the same members
-    stepped one by one on the FP64 plain path; with one_by_one, also the
-    batched members' error against the FP64 plain path after
-    args.error_steps steps, on err_members members spread over the sizes."""
-    import torch
+def ensemble_cases(n, nsteps):
     from swm_gb300.host import synthetic
+    return synthetic.ensemble_members(n=n, nsteps=nsteps)
+
+
+def ensemble_models(cases):
     from swm_gb300.host.driver import Driver
     from swm_gb300.model import GpuEnsemble, GpuModel
-    err_steps = max(getattr(args, 'error_steps', 0), 12 + steps) if one_by_one else 0
-    cases = synthetic.ensemble_members(n=n_members, nsteps=max(steps + 100, err_steps + 10))
-    cells = sum((c['config']['nx'] - 1) * (c['config']['ny'] - 1) for c in cases)
-    pts = sum(c['config']['nx'] * c['config']['ny'] for c in cases)
     ms = []
     for c in cases:
         g = GpuModel('fused_fp32c')
         Driver(c, g).init(with_diag=False)
         ms.append(g)
-    ens = GpuEnsemble(ms)
+    return ms, GpuEnsemble(ms)
+
+
+def ensemble_line(args, rank, ws):
+    """The headline: this rank's share of an (args.members x ws)-member
+    ensemble stepped by the batched path (K device-timed steps, then
+    args.e2e_steps monitored steps through the C ABI with host buffers)."""
+    import torch
+    from swm_gb300.host.partition import member_cells, partition_members
+    torch.cuda.set_device(int(os.environ.get('LOCAL_RANK', '0')))
+    W, K = args.warmup, args.steps
+    all_cases = ensemble_cases(args.members * ws, W + K + args.e2e_steps + 10)
+    share = partition_members([member_cells(c) for c in all_cases], ws)[rank]
+    cases = [all_cases[i] for i in share]
+    cells = sum(member_cells(c) for c in cases)
+    pts = sum(c['config']['nx'] * c['config']['ny'] for c in cases)
+    note('ensemble: %d members, set-up' % len(cases))
+    ms, ens = ensemble_models(cases)
+    note('ensemble: warm-up and timed steps')
     st = torch.cuda.ExternalStream(ens.stream())
-    ens.run(0, 12)
+    ens.run(0, W)
     ens.synchronize()
+    itt = W
+    barrier(ws)
+    torch.cuda.synchronize()
     a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
     l0 = ens.launch_count()
-    a.record(st)
-    ens.run(12, steps)
-    b.record(st)
-    ens.synchronize()
-    launches = ens.launch_count() - l0
-    ms_step = a.elapsed_time(b) / steps
-    ints = ens.integrals()
-    err = None
-    if one_by_one:
-        # continue the batched run to err_steps, then compare members spread
-        # over the sizes with the FP64 plain path from the same start
-        ens.run(12 + steps, err_steps - 12 - steps)
+    t0 = time.perf_counter()
+    with ClockSampler(int(os.environ.get('LOCAL_RANK', '0'))) as clk:
+        with torch.cuda.stream(st):
+            a.record(st)
+            ens.run(itt, K)
+            b.record(st)
         ens.synchronize()
-        order = sorted(range(n_members), key=lambda i: cases[i]['config']['nx'] * cases[i]['config']['ny'])
-        pick = [order[round(q * (n_members - 1) / (err_members - 1))] for q in range(err_members)]
-        worst = {f: {'rel_l2': 0.0, 'rel_max': 0.0} for f in ('u', 'v', 'eta')}
-        for i in pick:
-            ref = GpuModel('plain_fp64')
-            Driver(cases[i], ref).init(with_diag=False)
-            ref.run(0, err_steps)
-            for f in ('u', 'v', 'eta'):
-                m = ref.ocean(f).astype(bool)
-                a, b = ms[i].field(f)[m], ref.field(f)[m]
-                den = max(float(np.linalg.norm(b)), 1e-300)
-                worst[f]['rel_l2'] = max(worst[f]['rel_l2'], float(np.linalg.norm(a - b)) / den)
-                worst[f]['rel_max'] = max(worst[f]['rel_max'],
-                                          float(np.abs(a - b).max() / max(np.abs(b).max(), 1e-300)))
-            ref.close()
-        err = {'steps': err_steps, 'members': len(pick),
-               'sizes': [[cases[i]['config']['nx'], cases[i]['config']['ny']] for i in pick],
-               'worst_over_members': worst}
-    out = {'members': n_members, 'cells': cells, 'array_points': pts, 'steps': steps,
-           'ms_per_step': ms_step, 'value': cells / (ms_step * 1e-3), 'unit': 'cell-steps/s',
-           'rows_per_strip': ens.rows(), 'gpu_launches': launches,
-           'l2': 'not flushed: the ensemble state (%.2f GB) is larger than L2' % (89 * pts / 1e9),
-           'finite_integrals': bool(np.isfinite(ints).all())}
-    if err is not None:
-        out['fp32c_error_vs_fp64'] = err
+        torch.cuda.synchronize()
+    wall = time.perf_counter() - t0
+    launches = ens.launch_count() - l0
+    itt += K
+    ms_step = allmax(ws, a.elapsed_time(b) / K)
+    barrier(ws)
+    cells_all = allsum(ws, float(cells))
     peak, kind = peaks()
     ach = 89 * pts / (ms_step * 1e-3) / 1e9
-    out['roofline'] = {'bound': 'hbm', 'achieved': ach, 'peak': peak, 'unit': 'GB/s', 'frac': ach / peak,
-                       'peak_kind': kind, 'kernel': 'k_march_ens<1>', 'bytes_per_point': 89}
+    traffic = profiled_traffic('k_march_ens_ensemble_256.md')
+    if traffic is not None:
+        traffic *= pts / ENSEMBLE_256_POINTS
+    line = {'metric': METRIC, 'value': cells_all / (ms_step * 1e-3), 'unit': 'cell-steps/s', 'n_gpus': ws,
+            'steps': K, 'warmup': W, 'ms_per_step': ms_step, 'higher_is_better': True, 'scaling': 'weak',
+            'vs_baseline': None, 'dtype': 'f32',
+            'data': 'synthetic (seeded basins of uneven sizes, rest start)',
+            'config': {'workload': 'ensemble_%d_uneven_basins_laplacian' % args.members,
+                       'members_per_gpu': args.members, 'members': len(cases), 'cells': cells,
+                       'array_points': pts, 'path': 'fused_fp32c batched (one persistent launch per step)',
+                       'rows_per_strip': ens.rows(),
+                       'l2': 'not flushed: the state (%.2f GB) is larger than the 129 MB L2' % (89 * pts / 1e9),
+                       'parallelism': ('members split across %d ranks by cell count, no collective' % ws
+                                       if ws > 1 else 'single GPU')},
+            'gpu_launches': int(launches), 'wall_s_timed_region': wall,
+            'roofline': {'bound': 'hbm', 'achieved': ach, 'peak': peak, 'unit': 'GB/s', 'frac': ach / peak,
+                         'traffic': traffic, 'peak_kind': kind, 'algorithmic_bytes_per_launch': 89 * pts,
+                         'kernel': 'k_march_ens<1>', 'bytes_per_point': 89},
+            'clocks': clk.summary()}
+    # e2e: every step takes every member's wind rows from pinned host memory
+    # and returns every member's integrals into pinned host memory
+    k_e2e = args.e2e_steps
+    ny = [c['config']['ny'] for c in cases]
+    off = np.concatenate([[0], np.cumsum(ny)]).astype(int)
+    rows = torch.empty((k_e2e, int(off[-1])), dtype=torch.float64).pin_memory().numpy()
+    mod = 1.0 + 1e-3 * np.cos(np.arange(k_e2e) * 2e-3)
+    for i, c in enumerate(cases):
+        rows[:, off[i]:off[i + 1]] = c['streams'][0]['rec1'][0][:, 0][None, :] * mod[:, None]
+    outs = torch.empty((k_e2e, len(cases), 3), dtype=torch.float64).pin_memory().numpy()
+    ens.synchronize()
+    barrier(ws)
+    note('ensemble: end-to-end steps')
+    t0 = time.perf_counter()
+    ens.run_monitor(itt, k_e2e, rows, outs)
+    e2e_s = allmax(ws, time.perf_counter() - t0)
+    itt += k_e2e
+    assert np.isfinite(outs).all()
+    line['e2e'] = {'value': cells_all * k_e2e / e2e_s, 'unit': 'cell-steps/s',
+                   'h2d_bytes_per_step': int(off[-1]) * 8, 'd2h_bytes_per_step': 3 * len(cases) * 8,
+                   'steps': k_e2e,
+                   'per_step': "H2D: every member's wind-stress row profile for the step (one copy from pinned "
+                               'host memory); the batched step; D2H: every member\'s FP64 domain integrals '
+                               '(volume, potential and kinetic energy) of the new state into pinned host memory; '
+                               'all steps issued by swm_gpu_ensemble_run_monitor; wall clock including the final '
+                               'wait'}
     ens.close()
     for g in ms:
         g.close()
-    if not one_by_one:
-        return out
-    # the same members one by one on the FP64 plain path (3 steps each, after start-up)
+    if rank == 0 and not args.quick:
+        note('members one by one on the FP64 plain path')
+        one = plain_one_by_one(cases)
+        line['plain_fp64_one_by_one'] = one
+        line['speedup_vs_plain_fp64_one_by_one'] = one['ms_per_step'] / ms_step
+        note('batched error against FP64 after %d steps' % args.error_steps)
+        line['fp32c_error_vs_fp64'] = ensemble_error(cases, args.error_steps)
+        note('single basin')
+        line['single_basin'] = double_gyre_line(args, 0, 1, 200, 5, side=True)
+        note('tracer')
+        line['tracer'] = tracer_measurement(args)
+        note('helmholtz')
+        line['helmholtz'] = helmholtz_measurement(args)
+        note('sor')
+        line['sor'] = sor_measurement(args)
+        note('linear reduced gravity')
+        line['linear_rg'] = linear_rg_measurement(args)
+    if rank == 0 and ws == 1 and not args.quick:
+        note('cpu baseline')
+        line['cpu_baseline'] = cpu_baseline(cases)
+    note('done')
+    return line
+
+
+# array points of the 256-member ensemble the committed ncu summary covers
+ENSEMBLE_256_POINTS = 12043762
+
+
+def plain_one_by_one(cases):
+    """The same members one by one on the FP64 plain path (3 steps each after
+    the start-up, wall clock per member, summed)."""
+    from swm_gb300.host.driver import Driver
+    from swm_gb300.model import GpuModel
     tot = 0.0
     for c in cases:
         g = GpuModel('plain_fp64')
@@ -381,10 +470,60 @@ def ensemble_measurement(args, n_members=256, steps=200, one_by_one=True, err_me
         g.synchronize()
         tot += (time.perf_counter() - t0) / 3
         g.close()
-    out['plain_fp64_one_by_one'] = {'ms_per_step': tot * 1e3, 'value': cells / tot, 'unit': 'cell-steps/s',
-                                    'timing': 'wall clock per member, summed'}
-    out['speedup_vs_plain_fp64_one_by_one'] = tot * 1e3 / ms_step
-    return out
+    cells = sum((c['config']['nx'] - 1) * (c['config']['ny'] - 1) for c in cases)
+    return {'ms_per_step': tot * 1e3, 'value': cells / tot, 'unit': 'cell-steps/s',
+            'timing': 'wall clock per member, summed'}
+
+
+def ensemble_error(cases, steps, picks=8):
+    """The batched path's error against the FP64 plain path from the same
+    start after `steps` steps: a fresh ensemble of the same members runs
+    `steps` steps; picks members spread over the sizes are compared."""
+    from swm_gb300.host.driver import Driver
+    from swm_gb300.model import GpuModel
+    ms, ens = ensemble_models(cases)
+    ens.run(0, steps)
+    ens.synchronize()
+    n = len(cases)
+    order = sorted(range(n), key=lambda i: cases[i]['config']['nx'] * cases[i]['config']['ny'])
+    pick = sorted({order[round(q * (n - 1) / max(picks - 1, 1))] for q in range(min(picks, n))})
+    worst = {f: {'rel_l2': 0.0, 'rel_max': 0.0} for f in ('u', 'v', 'eta')}
+    for i in pick:
+        ref = GpuModel('plain_fp64')
+        Driver(cases[i], ref).init(with_diag=False)
+        ref.run(0, steps)
+        for f in ('u', 'v', 'eta'):
+            m = ref.ocean(f).astype(bool)
+            x, y = ms[i].field(f)[m], ref.field(f)[m]
+            den = max(float(np.linalg.norm(y)), 1e-300)
+            worst[f]['rel_l2'] = max(worst[f]['rel_l2'], float(np.linalg.norm(x - y)) / den)
+            worst[f]['rel_max'] = max(worst[f]['rel_max'], float(np.abs(x - y).max() / max(np.abs(y).max(), 1e-300)))
+        ref.close()
+    ens.close()
+    for g in ms:
+        g.close()
+    return {'steps': steps, 'members': len(pick),
+            'sizes': [[cases[i]['config']['nx'], cases[i]['config']['ny']] for i in pick],
+            'worst_over_members': worst}
+
+
+def ensemble_device_only(args):
+    """Warm-up and K timed ensemble steps only (the form to run under ncu)."""
+    import torch
+    cases = ensemble_cases(args.members, args.warmup + args.steps + 10)
+    ms, ens = ensemble_models(cases)
+    st = torch.cuda.ExternalStream(ens.stream())
+    ens.run(0, args.warmup)
+    ens.synchronize()
+    a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    a.record(st)
+    ens.run(args.warmup, args.steps)
+    b.record(st)
+    ens.synchronize()
+    ms_step = a.elapsed_time(b) / args.steps
+    pts = sum(c['config']['nx'] * c['config']['ny'] for c in cases)
+    return {'workload': 'ensemble_%d' % args.members, 'ms_per_step': ms_step, 'rows_per_strip': ens.rows(),
+            'array_points': pts, 'achieved_GBps': 89 * pts / (ms_step * 1e-3) / 1e9}
 
 
 def tracer_measurement(args, cells=2048, steps=200, err_steps=1000):
@@ -528,71 +667,180 @@ def linear_rg_measurement(args, steps=2000, cpu_budget_s=5.0):
     return out
 
 
-def cpu_baseline(cells, budget_s=15.0):
-    """The FP64 CPU restatement (oracle) on the same basin, all host cores."""
+def oracle_ensemble(cases, warmup, steps, budget_s, threads=None):
+    """The FP64 CPU restatement of the reference (oracle) stepping ensemble
+    members on the host cores: a pool of `threads` host threads, each
+    stepping one member at a time with OpenMP off inside the member (the
+    members are independent, as the reference's one-basin-per-process runs
+    are).  A bench step advances every member by one model step; when that
+    would take the whole run past budget_s, each bench step advances a
+    round-robin share of the members instead.  Returns (cell-steps/s, ms per
+    bench step, sample description, threads)."""
+    import concurrent.futures as cf
+    import ctypes
+    import math
     sys.path.insert(0, os.path.join(ROOT, 'oracle'))
     from oracle import OracleBackend
-    from swm_gb300.host import synthetic
     from swm_gb300.host.driver import Driver
-    case = synthetic.double_gyre(cells, biharmonic=True, nsteps=100)
-    o = OracleBackend()
-    Driver(case, o).init(with_diag=False)
-    o.run_steady(2)
-    n, t = 0, 0.0
-    t0 = time.perf_counter()
-    while t < budget_s and n < 200:
-        o.run_steady(1)
-        n += 1
-        t = time.perf_counter() - t0
-    return {'value': cells * cells * n / t, 'unit': 'cell-steps/s', 'cores': os.cpu_count(), 'kind': 'port',
-            'sample': '%d model steps of the %dx%d basin (FP64 C restatement, OpenMP)' % (n, cells, cells)}
+    from swm_gb300.host.partition import member_cells
+    threads = threads or os.cpu_count() or 1
+    try:
+        gomp = ctypes.CDLL('libgomp.so.1')
+        init = lambda: gomp.omp_set_num_threads(1)  # noqa: E731
+    except OSError:
+        init = None
+    n = len(cases)
+    cells = [member_cells(c) for c in cases]
+    order = sorted(range(n), key=lambda i: -cells[i])  # largest first keeps the pool busy to the end
+    with cf.ThreadPoolExecutor(threads, initializer=init) as pool:
+        def make(c):
+            o = OracleBackend()
+            Driver(c, o).init(with_diag=False)
+            o.run_steady(2)  # Adams-Bashforth start-up (untimed)
+            return o
+        models = list(pool.map(make, cases))
+
+        def advance(idx):
+            list(pool.map(lambda i: models[i].run_steady(1), idx))
+
+        t0 = time.perf_counter()
+        advance(order)  # first warm-up step, also the calibration
+        t_full = time.perf_counter() - t0
+        per = n
+        if t_full * (warmup + steps) > budget_s:
+            per = min(n, max(threads, int(math.ceil(n * budget_s / (t_full * (warmup + steps))))))
+        pos = 0
+
+        def share():
+            nonlocal pos
+            idx = [order[(pos + k) % n] for k in range(per)]
+            pos = (pos + per) % n
+            return sorted(idx, key=lambda i: -cells[i])
+
+        for _ in range(max(warmup - 1, 0)):
+            advance(share())
+        done, t = 0, 0.0
+        for _ in range(steps):
+            idx = share()
+            t0 = time.perf_counter()
+            advance(idx)
+            t += time.perf_counter() - t0
+            done += sum(cells[i] for i in idx)
+    sample = ('%d members, one model step of every member per bench step' % n if per == n else
+              '%d members; each bench step advances a round-robin share of %d members by one model step '
+              '(bounded run time); value = member-cells advanced / time' % (n, per))
+    return done / t, t / steps * 1e3, sample, threads
+
+
+def cpu_baseline(cases, budget_s=20.0, sample=32):
+    """The oracle on a sample of the ensemble's members (spread over the
+    sizes), all host cores, member-parallel."""
+    n = len(cases)
+    order = sorted(range(n), key=lambda i: cases[i]['config']['nx'] * cases[i]['config']['ny'])
+    pick = sorted({order[round(q * (n - 1) / max(sample - 1, 1))] for q in range(min(sample, n))})
+    v, _, desc, threads = oracle_ensemble([cases[i] for i in pick], 2, 3, budget_s)
+    return {'value': v, 'unit': 'cell-steps/s', 'cores': threads, 'kind': 'port',
+            'sample': '%d of the %d ensemble members spread over the sizes, 3 timed steps (%s); FP64 C '
+                      'restatement of the reference loops' % (len(pick), n, desc)}
 
 
 def reference(args, rank, ws):
-    """CPU restatement of the reference loops, timed on the host cores."""
+    """The CPU restatement of the reference's loops on the headline ensemble,
+    timed on the host cores (rank 0 alone; the other ranks exit)."""
     if rank != 0:
         return None
-    sys.path.insert(0, os.path.join(ROOT, 'oracle'))
-    from oracle import OracleBackend
-    from swm_gb300.host import synthetic
-    from swm_gb300.host.driver import Driver
-    strip = 64
-    case = synthetic.double_gyre((args.cells, strip), biharmonic=True, nsteps=args.warmup + args.steps)
-    o = OracleBackend()
-    Driver(case, o).init(with_diag=False)
-    o.run_steady(args.warmup)
-    t0 = time.perf_counter()
-    o.run_steady(args.steps)
-    t = time.perf_counter() - t0
-    v = args.cells * strip * args.steps / t
-    sample = 'one model step per bench step on a %dx%d-cell strip of the basin (same physics)' % (args.cells, strip)
+    cases = ensemble_cases(args.members, args.warmup + args.steps + 10)
+    v, ms, sample, threads = oracle_ensemble(cases, args.warmup, args.steps, budget_s=90.0)
     return {'metric': METRIC, 'value': v, 'unit': 'cell-steps/s', 'n_gpus': ws, 'steps': args.steps,
-            'warmup': args.warmup, 'ms_per_step': t / args.steps * 1e3, 'higher_is_better': True,
+            'warmup': args.warmup, 'ms_per_step': ms, 'higher_is_better': True,
             'scaling': 'weak', 'vs_baseline': None, 'dtype': 'f64', 'data': 'synthetic', 'impl': 'reference',
-            'config': {'workload': 'double_gyre_%dx%d_biharmonic' % (args.cells, args.cells)},
-            'cpu_baseline': {'value': v, 'unit': 'cell-steps/s', 'cores': os.cpu_count(), 'kind': 'port',
+            'config': {'workload': 'ensemble_%d_uneven_basins_laplacian' % args.members},
+            'cpu_baseline': {'value': v, 'unit': 'cell-steps/s', 'cores': threads, 'kind': 'port',
                              'sample': sample},
             'e2e': {'value': v, 'unit': 'cell-steps/s', 'h2d_bytes_per_step': 0, 'd2h_bytes_per_step': 0}}
 
 
+def sor_measurement(args, cells=2048, eps=1e-4):
+    """The reference's own solver (main_ElSolv_SOR: masked spherical
+    Laplacian, fixed Chebyshev relaxation schedule, absolute stop on the
+    correction norm, eps = 1e-4 as calc_lib.h) on the 2048^2 basin (chi, B
+    and the five coefficients, 270 MB, exceed L2).  The right-hand side is a
+    smooth random field of the size of a flow divergence (1e-9 /s), as
+    computeVelocityPotential passes one.  A call after the first (first_guess
+    false, as every call but the first from the diagnostics) is capped by the
+    reference at max_count = 10 max(Nx, Ny) iterations; from chi = 0 it may
+    end there unconverged, which is reported.  Roofline: 9 words per point and iteration (chi read
+    and written, B, the five coefficients)."""
+    import torch
+    from swm_gb300.host import synthetic
+    from swm_gb300.host.driver import Driver
+    from swm_gb300.model import GpuModel
+    case = synthetic.double_gyre(cells, biharmonic=False, nsteps=10, ah=500.0)
+    g = GpuModel('plain_fp64')
+    Driver(case, g).init(with_diag=False)
+    g.sor_init()
+    ny, nx = case['config']['ny'], case['config']['nx']
+    rng = np.random.default_rng(7)
+    # a smooth random field (scales of a few hundred km) of divergence size
+    k = np.fft.fftfreq(nx)[None, :] ** 2 + np.fft.fftfreq(ny)[:, None] ** 2
+    B = np.fft.ifft2(np.fft.fft2(rng.standard_normal((ny, nx))) * np.exp(-k * (nx / 16.0) ** 2)).real
+    B *= 1e-9 / max(np.abs(B).max(), 1e-300) * g.ocean('eta')
+    chi0 = np.zeros_like(B)
+    g.sor_solve(B, chi0, 1e30, False)  # set-up and one iteration
+    st = torch.cuda.ExternalStream(g.stream())
+    a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    l0 = g.launch_count()
+    t0 = time.perf_counter()
+    a.record(st)
+    chi, iters, anorm = g.sor_solve(B, chi0, eps, False)
+    b.record(st)
+    g.synchronize()
+    wall = time.perf_counter() - t0
+    dev = a.elapsed_time(b) * 1e-3
+    launches = g.launch_count() - l0
+    it = abs(iters)
+    pts = nx * ny
+    peak, kind = peaks()
+    ach = 9 * 8 * pts * it / dev / 1e9
+    g.close()
+    return {'workload': 'elsolv_sor_%dx%d' % (cells, cells), 'points': pts, 'eps': eps,
+            'iterations': it, 'converged': iters > 0, 'anorm': anorm, 'max_count': 10 * max(nx, ny),
+            'time_s': wall, 'device_s': dev, 'ms_per_iteration': dev / max(it, 1) * 1e3,
+            'gpu_launches': launches,
+            'roofline': {'bound': 'hbm', 'achieved': ach, 'peak': peak, 'unit': 'GB/s', 'frac': ach / peak,
+                         'peak_kind': kind, 'bytes_per_point_iteration': 72,
+                         'note': 'one iteration = a red and a black half-sweep over all points'}}
+
+
 def main():
     args = parse()
-    if args.workload != 'double_gyre':
+    if args.impl == 'ours' and args.workload not in ('ensemble', 'double_gyre'):
         import torch
         torch.cuda.set_device(0)
         if args.workload == 'tracer':
-            out = tracer_measurement(args, cells=args.cells, steps=args.steps,
+            out = tracer_measurement(args, cells=args.cells if args.cells != 1024 else 2048, steps=args.steps,
                                      err_steps=0 if args.device_only else 1000)
         elif args.workload == 'helmholtz':
-            out = helmholtz_measurement(args, cells=args.cells)
-        elif args.workload == 'linear_rg':
-            out = linear_rg_measurement(args)
+            out = helmholtz_measurement(args, cells=args.cells if args.cells != 1024 else 4096)
+        elif args.workload == 'sor':
+            out = sor_measurement(args, cells=args.cells if args.cells != 1024 else 2048)
         else:
-            out = ensemble_measurement(args, steps=args.steps, one_by_one=not args.device_only)
+            out = linear_rg_measurement(args)
         print(json.dumps(out))
         return
     rank, ws = dist_setup(args)
-    line = reference(args, rank, ws) if args.impl == 'reference' else ours(args, rank, ws)
+    if args.impl == 'reference':
+        line = reference(args, rank, ws)
+    elif args.workload == 'double_gyre':
+        import torch
+        torch.cuda.set_device(int(os.environ.get('LOCAL_RANK', '0')))
+        line = double_gyre_line(args, rank, ws, args.steps, args.warmup, side=not args.quick and not args.device_only)
+    elif args.device_only:
+        import torch
+        torch.cuda.set_device(0)
+        line = ensemble_device_only(args)
+    else:
+        line = ensemble_line(args, rank, ws)
     if rank == 0 and line is not None:
         print(json.dumps(line))
 

@@ -260,6 +260,21 @@ int swm_gpu_ensemble_destroy(swm_gpu_ensemble *ens);
 int swm_gpu_ensemble_run(swm_gpu_ensemble *ens, int64_t itt0, int64_t nsteps);
 /* FP64 domain integrals of every member, 3 per member as swm_gpu_integrals */
 int swm_gpu_ensemble_integrals(swm_gpu_ensemble *ens, double *out);
+/* nsteps monitored steps of every member (itt0+1 .. itt0+nsteps) issued
+   without a host wait per step, the batched form of swm_gpu_run_monitor:
+   before step s, the row profiles rows + s*R (R = the sum of the members'
+   Ny; member i's Ny rows follow those of members 0 .. i-1) become the
+   members' zonal wind-stress rows (one H2D copy; rows may be NULL: no
+   update; otherwise every member needs a time-dependent row-profile zonal
+   wind stream); after it, the three integrals of swm_gpu_integrals of every
+   member go to out + 3*n*s + 3*i (one D2H copy).  From itt = 3 on the step
+   kernel forms the sums itself, in (hi, lo) binary32 pairs per tile added
+   in FP64 in a fixed order (agreement with swm_gpu_ensemble_integrals about
+   1e-13 relative); the start-up steps use swm_gpu_ensemble_integrals.
+   Returns when the last result has landed; pinned arrays let the copies
+   run asynchronously, and they must stay untouched until then. */
+int swm_gpu_ensemble_run_monitor(swm_gpu_ensemble *ens, int64_t itt0, int64_t nsteps, const double *rows,
+                                 double *out);
 int swm_gpu_ensemble_synchronize(swm_gpu_ensemble *ens);
 void *swm_gpu_ensemble_stream(swm_gpu_ensemble *ens);
 int64_t swm_gpu_ensemble_launch_count(swm_gpu_ensemble *ens);

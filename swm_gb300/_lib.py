@@ -64,6 +64,7 @@ def _sigs():
         'trc_gpu_get_field': (I, [P, I, I, P]),
         'swm_gpu_ensemble_create': (I, [P, I, PP]), 'swm_gpu_ensemble_destroy': (I, [P]),
         'swm_gpu_ensemble_run': (I, [P, I64, I64]), 'swm_gpu_ensemble_integrals': (I, [P, P]),
+        'swm_gpu_ensemble_run_monitor': (I, [P, I64, I64, P, P]),
         'swm_gpu_ensemble_synchronize': (I, [P]), 'swm_gpu_ensemble_stream': (P, [P]),
         'swm_gpu_ensemble_launch_count': (I64, [P]), 'swm_gpu_ensemble_rows': (I, [P]),
         'swm_helm_create': (I, [I, I, D, D, D, P, P, PP]), 'swm_helm_destroy': (I, [P]),

@@ -67,6 +67,51 @@ __global__ void k_ens_integrals(const EnsInt *__restrict__ d, double *__restrict
   if (threadIdx.x < 3) out[3 * (size_t)blockIdx.x + threadIdx.x] = red[threadIdx.x][0];
 }
 
+// monitored steps: one step's wind rows of every member (FP64, staged on the
+// device) into each member's FP32 row profile
+__global__ void k_ens_rows(const double *__restrict__ rows, const int *__restrict__ row_member,
+                           const int *__restrict__ row_off, float *const *__restrict__ w, int nrows) {
+  const int r = blockIdx.x * blockDim.x + threadIdx.x;
+  if (r >= nrows) return;
+  const int i = row_member[r];
+  w[i][r - row_off[i]] = (float)rows[r];
+}
+
+// monitored steps: the integrals of every member from its tiles' sums, added
+// in the member's tile order (tiles_of[tile_off[i] .. tile_off[i + 1]))
+__global__ void k_ens_tile_sums(const double *__restrict__ partial, const int *__restrict__ tile_off,
+                                const int *__restrict__ tiles_of, const double *__restrict__ G, int n,
+                                double *__restrict__ out) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  double s[4] = {0., 0., 0., 0.};
+  for (int k = tile_off[i]; k < tile_off[i + 1]; k++) {
+    const double *q = partial + 4 * (size_t)tiles_of[k];
+    s[0] += q[0];
+    s[1] += q[1];
+    s[2] += q[2];
+    s[3] += q[3];
+  }
+  out[3 * (size_t)i] = s[0];
+  out[3 * (size_t)i + 1] = 0.5 * G[i] * s[1];
+  out[3 * (size_t)i + 2] = 0.5 * (s[2] + s[3]);
+}
+
+// device tables of the monitored steps, built on their first use
+struct EnsMonitor {
+  int nrows = 0;                 // rows of all members: the doubles of one step's wind rows
+  std::vector<int> row_off;      // first row of each member in a step's rows
+  std::vector<int> wind_sid;     // each member's row-profile wind stream
+  double *rows[2] = {nullptr, nullptr};  // one step's rows, alternating
+  int *row_member = nullptr, *d_row_off = nullptr;
+  float **w = nullptr;           // each member's FP32 wind rows
+  const float2 **areas = nullptr;
+  double *partial = nullptr;     // 4 per tile
+  int *tile_off = nullptr, *tiles_of = nullptr;
+  double *G = nullptr;
+  double *res = nullptr;         // 3 per member
+  bool has_rows = false;         // every member has a row-profile zonal wind stream
+};
 
 }  // namespace swm
 
@@ -87,6 +132,8 @@ struct swm_gpu_ensemble {
   int64_t launches = 0, graph_launches = 0;
   swm::EnsInt *d_int = nullptr;
   double *d_out = nullptr;
+  std::vector<int4> htiles;  // host copy of the tiles in queue order
+  swm::EnsMonitor *mon = nullptr;
 };
 
 namespace {
@@ -121,11 +168,11 @@ int rotate_members(swm_gpu_ensemble *e, int64_t itt) {
   return SWM_GPU_OK;
 }
 
-int ens_step(swm_gpu_ensemble *e, int64_t itt) {
+int ens_step(swm_gpu_ensemble *e, int64_t itt, const EnsInteg *mi = nullptr) {
   const size_t n = e->m.size();
   SWM_CK(cudaMemsetAsync(e->next + e->phase, 0, sizeof(int), e->stream));
   int rc = march_ens_launch(e->mix, e->std_cfg, e->pf, e->tab + (size_t)e->phase * n, e->tiles, e->ntiles,
-                            e->next + e->phase, e->stream);
+                            e->next + e->phase, e->stream, mi);
   if (rc != SWM_GPU_OK) return rc;
   e->launches++;
   return rotate_members(e, itt);
@@ -163,6 +210,62 @@ int ens_capture(swm_gpu_ensemble *e, int64_t itt0) {
   return SWM_GPU_OK;
 }
 
+// the monitored steps' device tables (first use)
+int ens_monitor_setup(swm_gpu_ensemble *e) {
+  if (e->mon) return SWM_GPU_OK;
+  const int n = (int)e->m.size();
+  EnsMonitor *M = new EnsMonitor();
+  e->mon = M;
+  std::vector<float *> w(n);
+  std::vector<const float2 *> areas(n);
+  std::vector<double> G(n);
+  std::vector<int> row_member;
+  M->has_rows = true;
+  M->row_off.resize(n);
+  M->wind_sid.assign(n, -1);
+  for (int i = 0; i < n; i++) {
+    swm_gpu_ctx *c = e->m[i];
+    int rc = fused_monitor_inputs(c, SWM_CMP_ZONAL, &w[i], &areas[i]);
+    if (rc != SWM_GPU_OK) return rc;
+    for (size_t k = 0; k < c->streams.size(); k++) {
+      const Stream &st = c->streams[k];
+      if (st.type == SWM_FRC_WIND && st.comp == SWM_CMP_ZONAL && !st.is_const) {
+        M->wind_sid[i] = (int)k;
+        break;
+      }
+    }
+    M->has_rows = M->has_rows && w[i] && M->wind_sid[i] >= 0;
+    G[i] = c->cfg.G;
+    M->row_off[i] = M->nrows;
+    row_member.insert(row_member.end(), c->ny, i);
+    M->nrows += c->ny;
+  }
+  // each member's tiles in queue order (the order its sums are added in)
+  std::vector<int> tile_off(n + 1, 0), tiles_of(e->ntiles);
+  for (const int4 &t : e->htiles) tile_off[t.x + 1]++;
+  for (int i = 0; i < n; i++) tile_off[i + 1] += tile_off[i];
+  std::vector<int> fill(tile_off.begin(), tile_off.end() - 1);
+  for (int t = 0; t < e->ntiles; t++) tiles_of[fill[e->htiles[t].x]++] = t;
+  auto up = [&](void **dst, const void *src, size_t bytes) {
+    if (cudaMalloc(dst, bytes) != cudaSuccess) return SWM_GPU_ENOMEM;
+    if (src && cudaMemcpy(*dst, src, bytes, cudaMemcpyHostToDevice) != cudaSuccess) return SWM_GPU_ECUDA;
+    return SWM_GPU_OK;
+  };
+  int rc = SWM_GPU_OK;
+  for (int b = 0; b < 2 && rc == SWM_GPU_OK; b++) rc = up((void **)&M->rows[b], nullptr, M->nrows * sizeof(double));
+  if (rc == SWM_GPU_OK) rc = up((void **)&M->row_member, row_member.data(), M->nrows * sizeof(int));
+  if (rc == SWM_GPU_OK) rc = up((void **)&M->d_row_off, M->row_off.data(), n * sizeof(int));
+  if (rc == SWM_GPU_OK) rc = up((void **)&M->w, w.data(), n * sizeof(float *));
+  if (rc == SWM_GPU_OK) rc = up((void **)&M->areas, areas.data(), n * sizeof(float2 *));
+  if (rc == SWM_GPU_OK) rc = up((void **)&M->partial, nullptr, 4 * (size_t)e->ntiles * sizeof(double));
+  if (rc == SWM_GPU_OK) rc = up((void **)&M->tile_off, tile_off.data(), (n + 1) * sizeof(int));
+  if (rc == SWM_GPU_OK) rc = up((void **)&M->tiles_of, tiles_of.data(), e->ntiles * sizeof(int));
+  if (rc == SWM_GPU_OK) rc = up((void **)&M->G, G.data(), n * sizeof(double));
+  if (rc == SWM_GPU_OK) rc = up((void **)&M->res, nullptr, 3 * (size_t)n * sizeof(double));
+  if (rc != SWM_GPU_OK) set_error("swm_gpu_ensemble_run_monitor: device tables could not be set up");
+  return rc;
+}
+
 void ens_free(swm_gpu_ensemble *e) {
   if (e->stream) cudaStreamSynchronize(e->stream);
   if (e->graph) cudaGraphExecDestroy(e->graph);
@@ -171,6 +274,20 @@ void ens_free(swm_gpu_ensemble *e) {
   cudaFree(e->next);
   cudaFree(e->d_int);
   cudaFree(e->d_out);
+  if (EnsMonitor *m = e->mon) {
+    cudaFree(m->rows[0]);
+    cudaFree(m->rows[1]);
+    cudaFree(m->row_member);
+    cudaFree(m->d_row_off);
+    cudaFree(m->w);
+    cudaFree(m->areas);
+    cudaFree(m->partial);
+    cudaFree(m->tile_off);
+    cudaFree(m->tiles_of);
+    cudaFree(m->G);
+    cudaFree(m->res);
+    delete m;
+  }
   for (auto ev : e->ev) cudaEventDestroy(ev);
   if (e->done) cudaEventDestroy(e->done);
   if (e->stream) cudaStreamDestroy(e->stream);
@@ -307,6 +424,7 @@ int swm_gpu_ensemble_create(swm_gpu_ctx *const *members, int n, swm_gpu_ensemble
     return fail(SWM_GPU_ECUDA);
   }
   e->ntiles = (int)lists[best].size();
+  e->htiles = lists[best];
   e->rows = (int)cand[best].first;
   e->slow = cand[best].second;
   if (release_members(e) != SWM_GPU_OK) return fail(SWM_GPU_ECUDA);
@@ -355,6 +473,63 @@ int swm_gpu_ensemble_run(swm_gpu_ensemble *e, int64_t itt0, int64_t nsteps) {
   rc = release_members(e);
   if (rc != SWM_GPU_OK) return rc;
   SWM_CK(cudaGetLastError());
+  return SWM_GPU_OK;
+}
+
+int swm_gpu_ensemble_run_monitor(swm_gpu_ensemble *e, int64_t itt0, int64_t nsteps, const double *rows,
+                                 double *out) {
+  SWM_REQUIRE(e && nsteps >= 0 && out, "swm_gpu_ensemble_run_monitor: bad arguments");
+  int rc = ens_monitor_setup(e);
+  if (rc != SWM_GPU_OK) return rc;
+  EnsMonitor *M = e->mon;
+  SWM_REQUIRE(!rows || M->has_rows,
+              "swm_gpu_ensemble_run_monitor: rows need a time-dependent row-profile zonal wind stress in every member");
+  const size_t n = e->m.size();
+  bool joined = false;
+  for (int64_t s = 0; s < nsteps; s++) {
+    const int64_t itt = itt0 + s + 1;
+    const double *rs = rows ? rows + (size_t)s * M->nrows : nullptr;
+    double *os = out + 3 * n * (size_t)s;
+    if (itt < 3) {
+      // Adams-Bashforth start-up: each member on its own stream, as
+      // swm_gpu_ensemble_run does, then swm_gpu_ensemble_integrals
+      for (size_t i = 0; i < n; i++) {
+        swm_gpu_ctx *c = e->m[i];
+        if (rs) rc = swm_gpu_set_stream_rows(c, M->wind_sid[i], rs + M->row_off[i], nullptr);
+        if (rc == SWM_GPU_OK) rc = swm_gpu_step(c, itt);
+        if (rc == SWM_GPU_OK) rc = swm_gpu_advance(c, itt);
+        if (rc != SWM_GPU_OK) return rc;
+      }
+      e->phase = (e->phase + 1) % ENS_PHASES;
+      rc = swm_gpu_ensemble_integrals(e, os);
+      if (rc != SWM_GPU_OK) return rc;
+      continue;
+    }
+    if (!joined) {
+      rc = join_members(e);
+      if (rc != SWM_GPU_OK) return rc;
+      joined = true;
+    }
+    if (rs) {
+      double *d = M->rows[s & 1];
+      SWM_CK(cudaMemcpyAsync(d, rs, M->nrows * sizeof(double), cudaMemcpyHostToDevice, e->stream));
+      k_ens_rows<<<(M->nrows + 255) / 256, 256, 0, e->stream>>>(d, M->row_member, M->d_row_off, M->w, M->nrows);
+      e->launches++;
+    }
+    const EnsInteg mi{M->areas, M->partial};
+    rc = ens_step(e, itt, &mi);
+    if (rc != SWM_GPU_OK) return rc;
+    k_ens_tile_sums<<<(unsigned)((n + 127) / 128), 128, 0, e->stream>>>(M->partial, M->tile_off, M->tiles_of, M->G,
+                                                                      (int)n, M->res);
+    e->launches++;
+    SWM_CK(cudaMemcpyAsync(os, M->res, 3 * n * sizeof(double), cudaMemcpyDeviceToHost, e->stream));
+  }
+  if (joined) {
+    rc = release_members(e);
+    if (rc != SWM_GPU_OK) return rc;
+  }
+  SWM_CK(cudaGetLastError());
+  SWM_CK(cudaStreamSynchronize(e->stream));
   return SWM_GPU_OK;
 }
 

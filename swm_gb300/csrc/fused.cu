@@ -1284,6 +1284,18 @@ static int grow(double **p, size_t *have, size_t need) {
   return SWM_GPU_OK;
 }
 
+int fused_monitor_inputs(swm_gpu_ctx *c, int comp, float **wind_rows, const float2 **area_pairs) {
+  const FusedState *f = c->fused;
+  SWM_REQUIRE(f && f->ready && f->comp, "monitored ensemble steps: member has no FP32 pair state");
+  IntegralScratch *S = nullptr;
+  FTRY(integrals_scratch(c, &S));
+  *area_pairs = S->pairs;
+  *wind_rows = nullptr;
+  if (f->wind_rows) *wind_rows = (float *)(comp == SWM_CMP_ZONAL ? (f->wind_x ? f->wx : nullptr)
+                                                                 : (f->wind_y ? f->wy : nullptr));
+  return SWM_GPU_OK;
+}
+
 int monitor_buffers(swm_gpu_ctx *c, int64_t nsteps, int sid, bool rows, bool res, MonitorBufs *b) {
   IntegralScratch *S = nullptr;
   FTRY(integrals_scratch(c, &S));

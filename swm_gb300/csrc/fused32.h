@@ -169,8 +169,17 @@ void fused_static(const swm_gpu_ctx *c, const float **He, const uint16_t **mask1
 // std_cfg: every member's parameter block is of the common configuration
 // (march_std_params), so the kernel's specialised instance serves them
 // pf: the step kernel's prefetch level (march_prefetch_level)
+// mi: a monitored step (the sums of k_march_ens's INTEG instance), or null
+struct EnsInteg {
+  const float2 *const *areas;  // per member: (hi, lo) cell areas of the u, v, eta rows, 3 x ny
+  double *partial;             // 4 sums per tile
+};
 int march_ens_launch(int mix, bool std_cfg, int pf, const P32 *tab, const int4 *tiles, int ntiles, int *next,
-                     cudaStream_t st);
+                     cudaStream_t st, const EnsInteg *mi = nullptr);
+// the FP32 pair path's row-profile wind of one component (SWM_CMP_ZONAL or
+// SWM_CMP_MERID; null when the wind is not a row profile) and the context's
+// (hi, lo) cell-area pairs (3 x ny), for the ensemble's monitored steps
+int fused_monitor_inputs(swm_gpu_ctx *c, int comp, float **wind_rows, const float2 **area_pairs);
 bool march_std_params(const P32 &p);
 int march_prefetch_level(size_t points, bool integ);
 // more bytes than the device's L2 holds

@@ -600,10 +600,16 @@ __global__ void __launch_bounds__(128, MARCH_MINB) k_march(P32 p, const int2 *__
 // the queue until it is empty.  A tile is int4 {member, strip, first row,
 // rows}; the member's parameter block is copied into the warp's slice of
 // shared memory first.
-template <int MIX, bool STD, int PF>
+// INTEG (monitored ensemble steps): each warp also sums the new state of its
+// tile's ocean points times the member's cell areas (areas[member], 3 x ny
+// (hi, lo) pairs) and writes the tile's four sums, eta, eta^2, u^2 and v^2
+// times area, to partial[4 * tile + q]; k_ens_tile_sums adds them per member.
+template <int MIX, bool STD, int PF, bool INTEG>
 __global__ void __launch_bounds__(128, MARCH_MINB) k_march_ens(const P32 *__restrict__ tab,
                                                                const int4 *__restrict__ tiles, int ntiles,
-                                                               int *__restrict__ next) {
+                                                               int *__restrict__ next,
+                                                               const float2 *const *__restrict__ areas,
+                                                               double *__restrict__ partial) {
   __shared__ P32 sp[4];
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
   for (;;) {
@@ -616,7 +622,21 @@ __global__ void __launch_bounds__(128, MARCH_MINB) k_march_ens(const P32 *__rest
     int *dst = reinterpret_cast<int *>(&sp[warp]);
     for (int k = lane; k < (int)(sizeof(P32) / sizeof(int)); k += 32) dst[k] = src[k];
     __syncwarp();
-    march_strip<MIX, false, STD, PF>(sp[warp], d.y, d.z, lane, d.w);
+    if (INTEG) {
+      F2 acc[4];
+      march_strip<MIX, true, STD, PF>(sp[warp], d.y, d.z, lane, d.w, areas[d.x], acc);
+      for (int o = 16; o > 0; o >>= 1)
+#pragma unroll
+        for (int q = 0; q < 4; q++) {
+          const float h = __shfl_down_sync(FULL, acc[q].h, o), l = __shfl_down_sync(FULL, acc[q].l, o);
+          acc[q].add(h, l);
+        }
+      if (lane == 0)
+#pragma unroll
+        for (int q = 0; q < 4; q++) partial[4 * (size_t)t + q] = acc[q].value();
+    } else {
+      march_strip<MIX, false, STD, PF>(sp[warp], d.y, d.z, lane, d.w);
+    }
     __syncwarp();
   }
 }
@@ -1010,42 +1030,52 @@ int march_autotune(swm_gpu_ctx *c, const P32 &p, const uint16_t *m16) {
 }
 
 // ---- ensemble launch ------------------------------------------------------
-template <int MIX, bool STD, int PF>
-static int ens_launch_m(const P32 *tab, const int4 *tiles, int ntiles, int *next, cudaStream_t st) {
+template <int MIX, bool STD, int PF, bool INTEG>
+static int ens_launch_m(const P32 *tab, const int4 *tiles, int ntiles, int *next, const EnsInteg *mi,
+                        cudaStream_t st) {
   static int blocks = 0;
   if (!blocks) {
     int per_sm = 0, sms = 0, dev = 0;
     SWM_CK(cudaGetDevice(&dev));
     SWM_CK(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
-    SWM_CK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_march_ens<MIX, STD, PF>, 128, 0));
+    SWM_CK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_march_ens<MIX, STD, PF, INTEG>, 128, 0));
     blocks = sms * (per_sm > 0 ? per_sm : 1);
   }
   int need = (ntiles + 3) / 4;
-  k_march_ens<MIX, STD, PF><<<need < blocks ? need : blocks, 128, 0, st>>>(tab, tiles, ntiles, next);
+  k_march_ens<MIX, STD, PF, INTEG><<<need < blocks ? need : blocks, 128, 0, st>>>(
+      tab, tiles, ntiles, next, mi ? mi->areas : nullptr, mi ? mi->partial : nullptr);
   return SWM_GPU_OK;
 }
 
+template <int MIX, bool STD, int PF>
+static int ens_launch_i(const P32 *tab, const int4 *tiles, int ntiles, int *next, const EnsInteg *mi,
+                        cudaStream_t st) {
+  return mi ? ens_launch_m<MIX, STD, PF, true>(tab, tiles, ntiles, next, mi, st)
+            : ens_launch_m<MIX, STD, PF, false>(tab, tiles, ntiles, next, mi, st);
+}
+
 template <int MIX, bool STD>
-static int ens_launch_p(int pf, const P32 *tab, const int4 *tiles, int ntiles, int *next, cudaStream_t st) {
-  if (pf == 2) return ens_launch_m<MIX, STD, 2>(tab, tiles, ntiles, next, st);
-  if (pf == 1) return ens_launch_m<MIX, STD, 1>(tab, tiles, ntiles, next, st);
-  return ens_launch_m<MIX, STD, 0>(tab, tiles, ntiles, next, st);
+static int ens_launch_p(int pf, const P32 *tab, const int4 *tiles, int ntiles, int *next, const EnsInteg *mi,
+                        cudaStream_t st) {
+  if (pf == 2) return ens_launch_i<MIX, STD, 2>(tab, tiles, ntiles, next, mi, st);
+  if (pf == 1) return ens_launch_i<MIX, STD, 1>(tab, tiles, ntiles, next, mi, st);
+  return ens_launch_i<MIX, STD, 0>(tab, tiles, ntiles, next, mi, st);
 }
 
 template <int MIX>
 static int ens_launch_mix(bool std_cfg, int pf, const P32 *tab, const int4 *tiles, int ntiles, int *next,
-                          cudaStream_t st) {
-  return std_cfg ? ens_launch_p<MIX, true>(pf, tab, tiles, ntiles, next, st)
-                 : ens_launch_p<MIX, false>(pf, tab, tiles, ntiles, next, st);
+                          const EnsInteg *mi, cudaStream_t st) {
+  return std_cfg ? ens_launch_p<MIX, true>(pf, tab, tiles, ntiles, next, mi, st)
+                 : ens_launch_p<MIX, false>(pf, tab, tiles, ntiles, next, mi, st);
 }
 
 bool march_std_params(const P32 &p) { return march_std(p); }
 
 int march_ens_launch(int mix, bool std_cfg, int pf, const P32 *tab, const int4 *tiles, int ntiles, int *next,
-                     cudaStream_t st) {
-  if (mix == 2) return ens_launch_mix<2>(std_cfg, pf, tab, tiles, ntiles, next, st);
-  if (mix == 1) return ens_launch_mix<1>(std_cfg, pf, tab, tiles, ntiles, next, st);
-  return ens_launch_mix<0>(std_cfg, pf, tab, tiles, ntiles, next, st);
+                     cudaStream_t st, const EnsInteg *mi) {
+  if (mix == 2) return ens_launch_mix<2>(std_cfg, pf, tab, tiles, ntiles, next, mi, st);
+  if (mix == 1) return ens_launch_mix<1>(std_cfg, pf, tab, tiles, ntiles, next, mi, st);
+  return ens_launch_mix<0>(std_cfg, pf, tab, tiles, ntiles, next, mi, st);
 }
 
 }  // namespace swm

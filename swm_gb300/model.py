@@ -275,6 +275,17 @@ class GpuEnsemble:
         check(self.L.swm_gpu_ensemble_integrals(self.ens, _p(out)))
         return out
 
+    def run_monitor(self, itt0, nsteps, rows, out):
+        """nsteps monitored steps: rows (nsteps x sum of the members' Ny,
+        float64, C order; None: no wind update) feed each step's zonal wind
+        rows, out (nsteps x members x 3, float64) receives each step's
+        integrals.  Pinned arrays keep the copies asynchronous."""
+        assert out.dtype == np.float64 and out.flags.c_contiguous and out.shape == (nsteps, len(self.members), 3)
+        if rows is not None:
+            assert rows.dtype == np.float64 and rows.flags.c_contiguous and rows.shape[0] == nsteps
+        check(self.L.swm_gpu_ensemble_run_monitor(self.ens, itt0, nsteps, None if rows is None else _p(rows),
+                                                   _p(out)))
+
     def synchronize(self):
         check(self.L.swm_gpu_ensemble_synchronize(self.ens))
 

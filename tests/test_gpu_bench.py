@@ -23,7 +23,7 @@ def run_bench(*args):
 
 
 def test_bench_line_carries_the_contract_keys():
-    d = run_bench('--quick', '--steps', '5', '--warmup', '3')
+    d = run_bench('--quick', '--steps', '5', '--warmup', '3', '--members', '16', '--e2e-steps', '20')
     assert d['metric'] and d['unit'] == 'cell-steps/s'
     assert d['value'] > 0 and d['ms_per_step'] > 0
     assert d['n_gpus'] == 1 and d['steps'] == 5 and d['warmup'] == 3
@@ -39,12 +39,20 @@ def test_bench_line_carries_the_contract_keys():
     assert d['gpu_launches'] == 5
     clk = d['clocks']
     assert 'sm_mhz' in clk and 'sm_max_mhz' in clk and isinstance(clk['reasons'], list)
+    assert d['config']['members'] == 16 and d['config']['rows_per_strip'] >= 16
+    assert d['e2e']['steps'] == 20 and d['e2e']['d2h_bytes_per_step'] == 16 * 3 * 8
+
+
+def test_single_basin_line():
+    d = run_bench('--workload', 'double_gyre', '--quick', '--steps', '5', '--warmup', '3', '--cells', '256',
+                  '--e2e-steps', '20')
+    assert d['value'] > 0 and d['gpu_launches'] == 5 and d['roofline']['achieved'] > 0
     tiles = d['config']['step_kernel_tiles']
     assert tiles['rows_per_warp'] >= 4 and tiles['blocks'] > 0
 
 
 def test_reference_arm_line():
-    d = run_bench('--impl', 'reference', '--steps', '2', '--warmup', '1')
+    d = run_bench('--impl', 'reference', '--steps', '2', '--warmup', '1', '--members', '12')
     assert d['impl'] == 'reference' and d['value'] > 0 and d['unit'] == 'cell-steps/s'
     assert d['cpu_baseline']['kind'] in ('port', 'reference') and d['cpu_baseline']['cores'] >= 1
     assert d['e2e']['h2d_bytes_per_step'] == 0 and d['e2e']['d2h_bytes_per_step'] == 0

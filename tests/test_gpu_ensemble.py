@@ -121,3 +121,54 @@ def test_ensemble_rejects_other_paths():
     ms = _models(cases[:1]) + _models(cases[1:], path='plain_fp64')
     with pytest.raises(SwmGpuError):
         GpuEnsemble(ms)
+
+
+@pytest.mark.parametrize('biharmonic', [False, True])
+def test_ensemble_monitor_matches_steps_and_integrals(biharmonic):
+    """swm_gpu_ensemble_run_monitor (each step: every member's wind rows in,
+    every member's integrals out, no host wait) against FP64 numpy sums of
+    the fields it leaves (1e-11 of each sum's scale, after two calls that
+    split the run), and against the same members given the same rows
+    through swm_gpu_set_stream_rows and stepped one step at a time by
+    swm_gpu_ensemble_run.  The monitored steps run a separately compiled
+    instance of the step kernel, so the two runs agree to binary32 rounding
+    (1e-6), not bit for bit."""
+    import torch
+    from test_gpu_diag import _numpy_integrals
+    cases = _cases(6, biharmonic=biharmonic, seed=21)
+    ma, mb = _models(cases), _models(cases)
+    ea, eb = GpuEnsemble(ma), GpuEnsemble(mb)
+    ny = [c['config']['ny'] for c in cases]
+    off = np.concatenate([[0], np.cumsum(ny)])
+    nsteps = 17
+    rows = torch.empty((nsteps, off[-1]), dtype=torch.float64).pin_memory().numpy()
+    for i, c in enumerate(cases):
+        prof = c['streams'][0]['rec1'][0][:, 0]
+        rows[:, off[i]:off[i + 1]] = prof[None, :] * (1.0 + 0.05 * np.cos(0.7 * np.arange(nsteps) + i))[:, None]
+    out = torch.empty((nsteps, len(cases), 3), dtype=torch.float64).pin_memory().numpy()
+    for s0, s1 in ((0, 9), (9, nsteps)):
+        part = torch.empty((s1 - s0, len(cases), 3), dtype=torch.float64).pin_memory().numpy()
+        ea.run_monitor(s0, s1 - s0, np.ascontiguousarray(rows[s0:s1]), part)
+        out[s0:s1] = part
+        for k, (c, a) in enumerate(zip(cases, ma)):
+            want, scale = _numpy_integrals(c, a)
+            assert np.all(want[1:] > 0)
+            assert np.all(np.abs(out[s1 - 1][k] - want) <= 1e-11 * scale), (s1, k, out[s1 - 1][k], want)
+    for s in range(nsteps):
+        for i, g in enumerate(mb):
+            g.set_stream_rows(0, np.ascontiguousarray(rows[s, off[i]:off[i + 1]]))
+        eb.run(s, 1)
+        ref = eb.integrals()
+        assert np.isfinite(out[s]).all()
+        np.testing.assert_allclose(out[s][:, 1:], ref[:, 1:], rtol=1e-6, atol=0, err_msg='step %d' % s)
+    for a, b in zip(ma, mb):
+        for f in ('u', 'v', 'eta'):
+            x, y = a.field(f), b.field(f)
+            assert np.abs(x - y).max() <= 1e-6 * np.abs(y).max(), f
+    # rows=None: no wind update, the steps go on with the last rows
+    out2 = torch.empty((3, len(cases), 3), dtype=torch.float64).pin_memory().numpy()
+    ea.run_monitor(nsteps, 3, None, out2)
+    eb.run(nsteps, 3)
+    np.testing.assert_allclose(out2[-1][:, 1:], eb.integrals()[:, 1:], rtol=1e-6, atol=0)
+    ea.close()
+    eb.close()

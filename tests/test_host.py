@@ -94,15 +94,19 @@ def test_perturbed_basin_is_closed_with_bounded_inset():
     assert (H[4:-4, 4:-4] == 500.0).all()
 
 
-def test_bench_reads_the_step_kernel_traffic_from_its_profile():
-    """bench.py's roofline.traffic for the default workload comes from the
-    committed ncu summary of the step kernel: it must be there and parse, and
-    lie between the kernel's written bytes and twice its algorithmic bytes
-    (89 B per point of the 1025^2 basin)."""
+def test_bench_reads_the_step_kernels_traffic_from_their_profiles():
+    """bench.py's roofline.traffic comes from the committed ncu summaries of
+    the step kernels: the batched ensemble kernel (the headline) and the
+    single-basin kernel; each must be there and parse, and lie between the
+    kernel's written bytes and twice its algorithmic bytes (89 B per
+    point)."""
     import importlib.util
     spec = importlib.util.spec_from_file_location('bench_mod', os.path.join(ROOT, 'bench.py'))
     bench = importlib.util.module_from_spec(spec)
     spec.loader.exec_module(bench)
-    t = bench.profiled_traffic('fused_fp32c', 1024)
+    t = bench.profiled_traffic('k_march_double_gyre_1024.md')
     assert t is not None
     assert 20e6 < t < 2 * 89 * 1025 * 1025
+    t = bench.profiled_traffic('k_march_ens_ensemble_256.md')
+    assert t is not None
+    assert 0.3 * 89 * bench.ENSEMBLE_256_POINTS < t < 2 * 89 * bench.ENSEMBLE_256_POINTS
