@@ -124,6 +124,10 @@ int swm_gpu_step_shape(swm_gpu_ctx *ctx, double *rows, double *masked_cost, int 
    tiles, or -1 for bad arguments.  Runs no GPU code. */
 int swm_gpu_plan_step_tiles(int mixing, int nx, int ny, const uint16_t *mask_words, double rows,
                             double masked_cost, int32_t *tiles, int capacity);
+/* Columns of the basin one warp strip of the FP32 step kernel updates, for
+   the mixing kind (0 none, 1 Laplacian, 2 biharmonic): the width the tiles
+   of swm_gpu_plan_step_tiles are strips of.  No reference counterpart. */
+int swm_gpu_step_strip_columns(int mixing);
 
 /* ---- SWM_initSWM pieces (swm_module.f90:37-48) ---- */
 /* initDomain (domain_module.f90:49-207): grids, masks, depth on all grids,

@@ -40,7 +40,7 @@ def _sigs():
         'swm_gpu_last_error': (C.c_char_p, []),
         'swm_gpu_create': (I, [P, PP]), 'swm_gpu_destroy': (I, [P]), 'swm_gpu_synchronize': (I, [P]),
         'swm_gpu_stream': (P, [P]), 'swm_gpu_launch_count': (I64, [P]), 'swm_gpu_step_shape': (I, [P, C.POINTER(C.c_double), C.POINTER(C.c_double), C.POINTER(C.c_int)]),
-        'swm_gpu_plan_step_tiles': (I, [I, I, I, P, D, D, P, I]),
+        'swm_gpu_plan_step_tiles': (I, [I, I, I, P, D, D, P, I]), 'swm_gpu_step_strip_columns': (I, [I]),
         'swm_gpu_domain': (I, [P, P, P]), 'swm_gpu_timestep_init': (I, [P, P]),
         'swm_gpu_add_damping': (I, [P, I, I, D, D, D, I, P]), 'swm_gpu_finish_damping': (I, [P]),
         'swm_gpu_add_stream': (I, [P, I, I, D, I, P, P, C.POINTER(C.c_int)]),

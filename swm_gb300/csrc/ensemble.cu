@@ -346,6 +346,7 @@ int swm_gpu_ensemble_create(swm_gpu_ctx *const *members, int n, swm_gpu_ensemble
   size_t points = 0;
   for (int i = 0; i < n; i++) points += (size_t)members[i]->nx * members[i]->ny;
   e->pf = march_prefetch_level(points, false);
+  for (P32 &q : tab) q.pf = e->pf;
   // Tiles: every member's strips cut into row groups of equal estimated
   // cost (as the single-basin step kernel's tiles), all members' tiles in
   // one queue with the short remainder groups last, so the queue ends on

@@ -28,6 +28,7 @@ std::vector<float> fp32c_records(const swm_gpu_ctx *c);  // REC_N * 4 floats per
 
 struct P32 {
   int nx, ny, nl, mix, qbf, barotropic, has_F, impl_uniform, gsq_uniform, wind_x, wind_y, wind_rows, has_mode;
+  int pf;  // L2 prefetch level of the two-column step kernel (march_prefetch_level), set at launch
   float dt, G, minD, lbc, q1, ts_rho, Ah, bih;
   float ab0, ab1, ab2;
   float impl_s[3], dp_s[3], gsq_s[2];

@@ -26,10 +26,15 @@
 #include <vector>
 #include "fused32.h"
 
+// columns per lane of the step kernels (2: march_strip2, packed FP32x2
+// arithmetic on 64-column strips; 1: march_strip, 32-column strips), the
 // minimum resident blocks per SM asked of the register allocator, and the
 // unroll factor of the row loop (tuning knobs, set with -D)
+#ifndef MARCH_COLS
+#define MARCH_COLS 1
+#endif
 #ifndef MARCH_MINB
-#define MARCH_MINB 4
+#define MARCH_MINB (MARCH_COLS == 2 ? 2 : 4)
 #endif
 // integrals formed by the step kernel: 1 = (hi, lo) pair sums of exact
 // products; 0 = binary32 sums per lane (a lane holds at most S + 4 rows),
@@ -93,7 +98,7 @@ __device__ __forceinline__ void march_strip(const P32 &p, const int bx, const in
   constexpr int TI = 32 - 2 * H;
   const int nx = p.nx, ny = p.ny;
   const int gx = bx * TI - H + lane;
-  const int gi = wrapm(gx, nx);
+  const int gi = ((gx % nx) + nx) % nx;  // periodic in i; narrow basins stay in bounds
   // STD: the configuration flags of march_std() hold, as compile-time constants
   const bool nl = STD || p.nl, has_mode = STD || p.has_mode, qbf = !STD && p.qbf, has_F = !STD && p.has_F;
   const bool impl_uniform = STD || p.impl_uniform, wind_rows = STD || p.wind_rows;
@@ -490,6 +495,13 @@ __device__ __forceinline__ void march_strip(const P32 &p, const int bx, const in
   }
 }
 
+#if MARCH_COLS == 2
+#include "march2.cuh"
+#define MARCH_STRIP march_strip2
+#else
+#define MARCH_STRIP march_strip
+#endif
+
 // End of a strip block of k_march<MIX, true>: each warp reduces its lanes'
 // pair sums (shuffle tree), then thread 0 adds the four warps in order in
 // FP64 and stores the block's sums as block b of nb.
@@ -589,7 +601,7 @@ __global__ void __launch_bounds__(128, MARCH_MINB) k_march(P32 p, const int2 *__
   const int2 t = tiles[4 * b + (threadIdx.x >> 5)];
   const int S = t.y & 255;
   F2 acc[4];
-  if (S > 0) march_strip<MIX, INTEG, STD, PF>(p, t.x, t.y >> 8, lane, S, mi.area, acc);
+  if (S > 0) MARCH_STRIP<MIX, INTEG, STD, PF>(p, t.x, t.y >> 8, lane, S, mi.area, acc);
   if (INTEG) {
     grid_dep_trigger();
     march_integrals_block(mi, acc, b, gridDim.x - 1);
@@ -624,7 +636,7 @@ __global__ void __launch_bounds__(128, MARCH_MINB) k_march_ens(const P32 *__rest
     __syncwarp();
     if (INTEG) {
       F2 acc[4];
-      march_strip<MIX, true, STD, PF>(sp[warp], d.y, d.z, lane, d.w, areas[d.x], acc);
+      MARCH_STRIP<MIX, true, STD, PF>(sp[warp], d.y, d.z, lane, d.w, areas[d.x], acc);
       for (int o = 16; o > 0; o >>= 1)
 #pragma unroll
         for (int q = 0; q < 4; q++) {
@@ -635,7 +647,7 @@ __global__ void __launch_bounds__(128, MARCH_MINB) k_march_ens(const P32 *__rest
 #pragma unroll
         for (int q = 0; q < 4; q++) partial[4 * (size_t)t + q] = acc[q].value();
     } else {
-      march_strip<MIX, false, STD, PF>(sp[warp], d.y, d.z, lane, d.w);
+      MARCH_STRIP<MIX, false, STD, PF>(sp[warp], d.y, d.z, lane, d.w);
     }
     __syncwarp();
   }
@@ -695,7 +707,7 @@ std::vector<float> fp32c_records(const swm_gpu_ctx *c) {
   return rec;
 }
 
-int march_tile_cols(int mix) { return 32 - 2 * (mix == 2 ? 2 : 1); }
+int march_tile_cols(int mix) { return 32 * MARCH_COLS - 2 * (mix == 2 ? 2 : 1); }
 
 // ---- tiles of the step kernel ---------------------------------------------
 //
@@ -717,8 +729,8 @@ std::vector<uint8_t> march_fast_rows(int mix, int nx, int ny, const uint16_t *m1
   for (int s = 0; s < nstrips; s++) {
     for (int j = 0; j < ny; j++) {
       bool all = true;
-      for (int lane = 0; lane < 32 && all; lane++) {
-        const int gi = wrap(s * TI - H + lane, nx);
+      for (int col = 0; col < 32 * MARCH_COLS && all; col++) {
+        const int gi = wrap(s * TI - H + col, nx);
         all = (m16[gi + (size_t)nx * j] & 0xFFFu) == 0xFFFu;
       }
       ocean[j] = all;
@@ -771,6 +783,8 @@ double march_tile_cost(const std::vector<uint8_t> &fast, int ny, int2 t, double 
 }
 
 }  // namespace swm
+
+extern "C" int swm_gpu_step_strip_columns(int mixing) { return swm::march_tile_cols(mixing); }
 
 extern "C" int swm_gpu_plan_step_tiles(int mixing, int nx, int ny, const uint16_t *mask_words, double rows,
                                        double masked_cost, int32_t *tiles, int capacity) {
@@ -838,9 +852,15 @@ static void launch_mix_s(const P32 &p, const MarchGrid &g, cudaStream_t st, cons
 template <int MIX, bool STD>
 static void launch_mix_p(const P32 &p, const MarchGrid &g, cudaStream_t st, const MarchInteg *mi) {
   const int pf = march_prefetch_level((size_t)p.nx * p.ny, mi != nullptr);
+#if MARCH_COLS == 2
+  P32 q = p;  // the two-column kernel takes the level at run time
+  q.pf = pf;
+  launch_mix_s<MIX, STD, 0>(q, g, st, mi);
+#else
   if (pf == 2) launch_mix_s<MIX, STD, 2>(p, g, st, mi);
   else if (pf == 1) launch_mix_s<MIX, STD, 1>(p, g, st, mi);
   else launch_mix_s<MIX, STD, 0>(p, g, st, mi);
+#endif
 }
 
 template <int MIX>
@@ -945,8 +965,13 @@ static int resident_blocks_of() {  // blocks of k_march resident on the whole GP
 
 template <int MIX, bool STD>
 static int resident_blocks_p(int pf) {
+#if MARCH_COLS == 2
+  (void)pf;  // one instance serves every level
+  return resident_blocks_of<MIX, STD, 0>();
+#else
   return pf == 2 ? resident_blocks_of<MIX, STD, 2>()
                  : (pf == 1 ? resident_blocks_of<MIX, STD, 1>() : resident_blocks_of<MIX, STD, 0>());
+#endif
 }
 
 template <int MIX>
@@ -1057,9 +1082,14 @@ static int ens_launch_i(const P32 *tab, const int4 *tiles, int ntiles, int *next
 template <int MIX, bool STD>
 static int ens_launch_p(int pf, const P32 *tab, const int4 *tiles, int ntiles, int *next, const EnsInteg *mi,
                         cudaStream_t st) {
+#if MARCH_COLS == 2
+  (void)pf;  // the level is in the parameter blocks
+  return ens_launch_i<MIX, STD, 0>(tab, tiles, ntiles, next, mi, st);
+#else
   if (pf == 2) return ens_launch_i<MIX, STD, 2>(tab, tiles, ntiles, next, mi, st);
   if (pf == 1) return ens_launch_i<MIX, STD, 1>(tab, tiles, ntiles, next, mi, st);
   return ens_launch_i<MIX, STD, 0>(tab, tiles, ntiles, next, mi, st);
+#endif
 }
 
 template <int MIX>

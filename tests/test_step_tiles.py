@@ -50,7 +50,9 @@ def plan(L, mix, m16, rows, cost):
 
 
 def strips_of(mix, nx):
-    cols = 32 - 2 * (2 if mix == 2 else 1)
+    from swm_gb300 import _lib
+    cols = _lib.lib().swm_gpu_step_strip_columns(mix)
+    assert cols in (32 - 2 * (2 if mix == 2 else 1), 64 - 2 * (2 if mix == 2 else 1))
     return (nx + cols - 1) // cols
 
 
