@@ -4,25 +4,60 @@
 // (init_ElSolv_SOR :54-62), colour 1 = i+j even (1-based) then colour 2,
 // fixed Chebyshev relaxation schedule from rJacobi = 0.99999178 (binary32
 // literal, :175, :206-210), stop on the first iteration whose correction norm
-// sqrt(sum res^2) drops below eps (:213-218).  Each colour is one kernel; a
-// finished solve turns the remaining kernels of a batch into no-ops through a
-// device flag, so the host reads back once per batch instead of once per
-// iteration.  The per-iteration norm is summed in a fixed order (per-block
-// partials, then one block), so it is deterministic.
+// sqrt(sum res^2) drops below eps (:213-218), max_count = 1000 max(Nx, Ny)
+// on a first call and 10 max(Nx, Ny) after it (:166-176).
+//
+// Layout: the coefficients, the right-hand side and chi are kept split by
+// colour, row by row: cell (i, j) of colour (i + j) % 2 sits at j * W + i / 2
+// of its colour's arrays (W = ceil(Nx / 2)).  A half-sweep then reads only
+// its own colour's coefficients, right-hand side and chi (and the other
+// colour's chi as neighbours): 9 words per point and iteration, one thread
+// per cell of the colour, coalesced.  Each cell's update is the reference's
+// expression in the reference's order (this file is compiled without FMA
+// contraction), so chi is bit for bit the restatement's when the iteration
+// counts agree; within a colour no cell reads another of its own colour
+// (the periodic wrap only pairs land cells, which stay fixed).
+//
+// Control: the relaxation factor, the iteration counter and the stop flag
+// live on the device.  Each half-sweep kernel sums res^2 per warp with
+// shuffles and per block; the last block to finish (fence and counter) adds
+// the blocks in a fixed order, advances the relaxation schedule, and after
+// the second colour applies the stop test.  The kernels take no per-
+// iteration arguments, so a batch of iterations is one CUDA graph, replayed
+// until the flag is set; kernels after convergence (or max_count) return at
+// once.  The host reads the flag once per batch.
 #include <cmath>
+#include <string>
 #include <vector>
 #include "ctx.h"
 
-struct SorState {
-  double *c[5] = {};       // ElSolvSOR_c(:,:,1..5)
-  double *chi = nullptr, *B = nullptr;
-  double *partial = nullptr;   // per-block partial sums of res^2
-  double *anorm2 = nullptr;    // running sum for the current iteration
-  int *done = nullptr;         // [0] converged flag, [1] iteration at convergence
-  double *anorm_hist = nullptr;
-  double *und = nullptr, *vnd = nullptr;  // non-divergent flow
-  int nblocks = 0;
+// device control block of a solve
+struct SorCtl {
+  double relax;      // relaxation factor of the next half-sweep
+  double sum0;       // sum of res^2 of the current iteration's first colour
+  double anorm;      // correction norm of the last finished iteration
+  double eps;        // stop when the correction norm falls below it
+  int l;             // the iteration the next half-sweep belongs to (1-based)
+  int max_count;
+  int done;          // 1: converged (at iteration iters)
+  int iters;
+  unsigned count;    // blocks finished in the running half-sweep
 };
+
+struct SorState {
+  double *c[5] = {};       // ElSolvSOR_c(:,:,1..5), natural layout (set-up only)
+  double *chi = nullptr, *B = nullptr;   // natural layout
+  double *cs[2][5] = {};   // coefficients split by colour
+  double *Bs[2] = {}, *chis[2] = {};     // right-hand side and chi split by colour
+  double *partial = nullptr;   // per-block sums of res^2 of a half-sweep
+  SorCtl *ctl = nullptr;
+  double *und = nullptr, *vnd = nullptr;  // non-divergent flow
+  int W = 0, nblocks = 0;      // split row length; blocks of a half-sweep
+  cudaGraphExec_t graph = nullptr;  // SOR_BATCH iterations
+};
+
+constexpr int SOR_THREADS = 256;
+constexpr int SOR_BATCH = 32;  // iterations per graph replay (one host read of the flag)
 
 namespace swm {
 
@@ -44,55 +79,87 @@ __global__ void k_sor_coeff(Dev d, SorState s) {
   s.c[4][k] = (-oU[ki] - oU[k]) / ax + (-cV[jp] * oV[kj] - cV[j] * oV[k]) / ay;
 }
 
-// one colour of one SOR iteration; colour 0 <-> (i+j) even in 0-based indices
-__global__ void k_sor_colour(Dev d, SorState s, int colour, double relax) {
-  __shared__ double red[256];
-  int tid = threadIdx.y * blockDim.x + threadIdx.x;
-  double r2 = 0.;
-  if (!s.done[0]) {
-    int i = blockIdx.x * blockDim.x + threadIdx.x, j = blockIdx.y * blockDim.y + threadIdx.y;
-    if (i < d.nx && j < d.ny && ((i + j) & 1) == colour) {
-      size_t k = i + (size_t)d.nx * j;
-      if (d.ocean[GE][k] != 0) {
-        int ip = i + 1 == d.nx ? 0 : i + 1, im = i == 0 ? d.nx - 1 : i - 1;
-        int jp = j + 1 == d.ny ? 0 : j + 1, jm = j == 0 ? d.ny - 1 : j - 1;
-        double *chi = s.chi;
-        double res = relax * (s.c[0][k] * chi[ip + (size_t)d.nx * j] + s.c[1][k] * chi[im + (size_t)d.nx * j] +
-                              s.c[2][k] * chi[i + (size_t)d.nx * jp] + s.c[3][k] * chi[i + (size_t)d.nx * jm] +
-                              s.c[4][k] * chi[k] - s.B[k]) / s.c[4][k];
-        chi[k] = chi[k] - res;
-        r2 = res * res;
-      }
-    }
-  }
-  red[tid] = r2;
-  __syncthreads();
-  for (int w = 128; w > 0; w >>= 1) {
-    if (tid < w) red[tid] += red[tid + w];
-    __syncthreads();
-  }
-  if (tid == 0) s.partial[(size_t)colour * gridDim.x * gridDim.y + blockIdx.y * gridDim.x + blockIdx.x] = red[0];
+// natural <-> colour-split layout (join 0: natural -> split, 1: split -> natural)
+__global__ void k_sor_split(double *nat, double *s0, double *s1, int nx, int ny, int W, int join) {
+  const size_t k = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (k >= (size_t)nx * ny) return;
+  const int i = (int)(k % nx), j = (int)(k / nx);
+  double *sp = ((i + j) & 1) ? s1 : s0;
+  const size_t q = (size_t)j * W + (i >> 1);
+  if (join) nat[k] = sp[q];
+  else sp[q] = nat[k];
 }
 
-// sums both colours' partials in a fixed order and applies the stop test
-__global__ void k_sor_check(SorState s, int nparts, int l, double eps) {
-  __shared__ double red[256];
-  if (s.done[0]) return;
-  double acc = 0.;
-  for (int q = threadIdx.x; q < 2 * nparts; q += blockDim.x) acc += s.partial[q];
-  red[threadIdx.x] = acc;
-  __syncthreads();
-  for (int w = 128; w > 0; w >>= 1) {
-    if (threadIdx.x < w) red[threadIdx.x] += red[threadIdx.x + w];
-    __syncthreads();
-  }
-  if (threadIdx.x == 0) {
-    double an = sqrt(red[0]);
-    s.anorm_hist[0] = an;
-    if (an < eps) {
-      s.done[0] = 1;
-      s.done[1] = l;
+// One half-sweep of colour col (0: (i+j) even in 0-based indices, the
+// reference's colour 1) over the colour-split arrays; then the block sums of
+// res^2 and, in the last block, the iteration's bookkeeping.
+__global__ void __launch_bounds__(SOR_THREADS) k_sor_half(const int8_t *__restrict__ ocean, SorState s, int nx,
+                                                          int ny, int col, double rJ) {
+  SorCtl *ctl = s.ctl;
+  if (ctl->done || ctl->l > ctl->max_count) return;  // converged, or max_count reached
+  const double relax = ctl->relax;
+  const int W = s.W;
+  const size_t q = (size_t)blockIdx.x * SOR_THREADS + threadIdx.x;
+  double r2 = 0.;
+  if (q < (size_t)W * ny) {
+    const int j = (int)(q / W), t = (int)(q % W);
+    const int i = 2 * t + ((col + j) & 1);
+    if (i < nx && ocean[i + (size_t)nx * j] != 0) {
+      const int ip = i + 1 == nx ? 0 : i + 1, im = i == 0 ? nx - 1 : i - 1;
+      const int jp = j + 1 == ny ? 0 : j + 1, jm = j == 0 ? ny - 1 : j - 1;
+      // neighbours are of the other colour except across an odd periodic wrap
+      auto at = [&](int a, int b) { return s.chis[(a + b) & 1][(size_t)b * W + (a >> 1)]; };
+      double *x = s.chis[col];
+      const double res = relax * (s.cs[col][0][q] * at(ip, j) + s.cs[col][1][q] * at(im, j) +
+                                  s.cs[col][2][q] * at(i, jp) + s.cs[col][3][q] * at(i, jm) +
+                                  s.cs[col][4][q] * x[q] - s.Bs[col][q]) / s.cs[col][4][q];
+      x[q] = x[q] - res;
+      r2 = res * res;
     }
+  }
+  // block sum: shuffles within warps, then the warps in order
+  __shared__ double wsum[SOR_THREADS / 32];
+  __shared__ bool last;
+  for (int o = 16; o > 0; o >>= 1) r2 += __shfl_down_sync(0xffffffffu, r2, o);
+  if ((threadIdx.x & 31) == 0) wsum[threadIdx.x >> 5] = r2;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    double b = 0.;
+    for (int w = 0; w < SOR_THREADS / 32; w++) b += wsum[w];
+    s.partial[blockIdx.x] = b;
+    __threadfence();
+    last = atomicAdd(&ctl->count, 1u) == gridDim.x - 1;
+  }
+  __syncthreads();
+  if (!last) return;
+  // last block: the blocks' sums in block order (thread t adds blocks t,
+  // t + 256, ..., then the warps' shuffle trees, then the warps in order)
+  __threadfence();
+  double v = 0.;
+  for (int b = threadIdx.x; b < (int)gridDim.x; b += SOR_THREADS) v += ((volatile double *)s.partial)[b];
+  for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
+  if ((threadIdx.x & 31) == 0) wsum[threadIdx.x >> 5] = v;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    double tot = 0.;
+    for (int w = 0; w < SOR_THREADS / 32; w++) tot += wsum[w];
+    const int l = ctl->l;
+    // the schedule of main_ElSolv_SOR (:206-210): after the first colour of
+    // the first iteration 1 / (1 - rJ^2 / 2), else 1 / (1 - rJ^2 relax / 4)
+    if (col == 0 && l == 1) ctl->relax = 1. / (1. - .5 * rJ * rJ);
+    else ctl->relax = 1. / (1. - .25 * rJ * rJ * relax);
+    if (col == 0) {
+      ctl->sum0 = tot;
+    } else {
+      const double an = sqrt(ctl->sum0 + tot);
+      ctl->anorm = an;
+      if (an < ctl->eps) {
+        ctl->done = 1;
+        ctl->iters = l;
+      }
+      ctl->l = l + 1;
+    }
+    ctl->count = 0;
   }
 }
 
@@ -134,8 +201,14 @@ __global__ void k_sor_nondiv(Dev d, const double *chi, const double *u, const do
 void sor_free(swm_gpu_ctx *c) {
   if (!c->sor) return;
   SorState *s = c->sor;
+  if (s->graph) cudaGraphExecDestroy(s->graph);
   for (int q = 0; q < 5; q++) cudaFree(s->c[q]);
-  cudaFree(s->chi); cudaFree(s->B); cudaFree(s->partial); cudaFree(s->done); cudaFree(s->anorm_hist);
+  for (int col = 0; col < 2; col++) {
+    for (int q = 0; q < 5; q++) cudaFree(s->cs[col][q]);
+    cudaFree(s->Bs[col]);
+    cudaFree(s->chis[col]);
+  }
+  cudaFree(s->chi); cudaFree(s->B); cudaFree(s->partial); cudaFree(s->ctl);
   cudaFree(s->und); cudaFree(s->vnd);
   delete s;
   c->sor = nullptr;
@@ -152,18 +225,28 @@ int elsolv_sor_gpu_init(swm_gpu_ctx *c) {
   sor_free(c);
   SorState *s = new SorState();
   c->sor = s;
-  size_t n = c->n;
+  const size_t n = c->n;
+  s->W = (c->nx + 1) / 2;
+  const size_t ns = (size_t)s->W * c->ny;
+  s->nblocks = (int)((ns + SOR_THREADS - 1) / SOR_THREADS);
   for (int q = 0; q < 5; q++) SWM_CK(cudaMalloc((void **)&s->c[q], n * 8));
+  for (int col = 0; col < 2; col++) {
+    for (int q = 0; q < 5; q++) SWM_CK(cudaMalloc((void **)&s->cs[col][q], ns * 8));
+    SWM_CK(cudaMalloc((void **)&s->Bs[col], ns * 8));
+    SWM_CK(cudaMalloc((void **)&s->chis[col], ns * 8));
+  }
   SWM_CK(cudaMalloc((void **)&s->chi, n * 8));
   SWM_CK(cudaMalloc((void **)&s->B, n * 8));
-  dim3 b(32, 8), g((c->nx + 31) / 32, (c->ny + 7) / 8);
-  s->nblocks = g.x * g.y;
-  SWM_CK(cudaMalloc((void **)&s->partial, 2 * (size_t)s->nblocks * 8));
-  SWM_CK(cudaMalloc((void **)&s->done, 2 * sizeof(int)));
-  SWM_CK(cudaMalloc((void **)&s->anorm_hist, 8));
+  SWM_CK(cudaMalloc((void **)&s->partial, (size_t)s->nblocks * 8));
+  SWM_CK(cudaMalloc((void **)&s->ctl, sizeof(SorCtl)));
+  SWM_CK(cudaMemsetAsync(s->ctl, 0, sizeof(SorCtl), c->stream));
   SWM_CK(cudaMemsetAsync(s->chi, 0, n * 8, c->stream));  // calc_lib::chi starts at 0
+  dim3 b(32, 8), g((c->nx + 31) / 32, (c->ny + 7) / 8);
   k_sor_coeff<<<g, b, 0, c->stream>>>(c->dev(), *s);
-  c->launches++;
+  const unsigned nb = (unsigned)((n + 255) / 256);
+  for (int q = 0; q < 5; q++)
+    k_sor_split<<<nb, 256, 0, c->stream>>>(s->c[q], s->cs[0][q], s->cs[1][q], c->nx, c->ny, s->W, 0);
+  c->launches += 6;
   SWM_CK(cudaGetLastError());
   SWM_CK(cudaStreamSynchronize(c->stream));
   return SWM_GPU_OK;
@@ -171,45 +254,68 @@ int elsolv_sor_gpu_init(swm_gpu_ctx *c) {
 
 }  // extern "C"
 
+namespace {
+
+// the two half-sweeps of one iteration
+void sor_iteration(swm_gpu_ctx *c, SorState *s) {
+  const double rJ = (double)(float)9.9999178e-1;  // default-real literal (ElSolv_SOR.f90:175)
+  for (int col = 0; col < 2; col++)
+    k_sor_half<<<s->nblocks, SOR_THREADS, 0, c->stream>>>(c->d_ocean[GE], *s, c->nx, c->ny, col, rJ);
+}
+
+// SOR_BATCH iterations as one graph, captured once per set-up (the kernels
+// read their iteration state and eps from the control block, so one capture
+// serves every batch and every call)
+int sor_graph(swm_gpu_ctx *c, SorState *s) {
+  if (s->graph) return SWM_GPU_OK;
+  SWM_CK(cudaStreamBeginCapture(c->stream, cudaStreamCaptureModeThreadLocal));
+  for (int l = 0; l < SOR_BATCH; l++) sor_iteration(c, s);
+  cudaGraph_t g = nullptr;
+  SWM_CK(cudaStreamEndCapture(c->stream, &g));
+  cudaError_t e = cudaGraphInstantiate(&s->graph, g, 0);
+  cudaGraphDestroy(g);
+  if (e != cudaSuccess) {
+    s->graph = nullptr;
+    set_error(std::string("elsolv_sor_gpu_solve: cudaGraphInstantiate: ") + cudaGetErrorString(e));
+    return SWM_GPU_ECUDA;
+  }
+  return SWM_GPU_OK;
+}
+
+}  // namespace
+
 // main_ElSolv_SOR on the device arrays s->B (right-hand side) and s->chi
-// (first guess in, solution out); returns SWM_GPU_ENOT_CONVERGED after
-// max_count iterations
+// (first guess in, solution out), natural layout; returns
+// SWM_GPU_ENOT_CONVERGED after max_count iterations
 static int sor_solve_device(swm_gpu_ctx *c, double eps, int first_guess, int *iters, double *anorm) {
   SorState *s = c->sor;
-  int mx = c->nx > c->ny ? c->nx : c->ny;
-  int max_count = first_guess ? (int)lround(1000. * mx) : (int)lround(10. * mx);
-  const double rJ = (double)(float)9.9999178e-1;
-  SWM_CK(cudaMemsetAsync(s->done, 0, 2 * sizeof(int), c->stream));
-  dim3 b(32, 8), g((c->nx + 31) / 32, (c->ny + 7) / 8);
-  Dev d = c->dev();
-  double relax = 1.;
-  int done[2] = {0, 0};
-  const int batch = 64;
-  int l = 1;
-  while (l <= max_count) {
-    int lend = l + batch - 1 < max_count ? l + batch - 1 : max_count;
-    for (; l <= lend; l++) {
-      for (int oe = 1; oe <= 2; oe++) {
-        // oe = 1: (i+j) even with 1-based indices = (i+j) even with 0-based
-        k_sor_colour<<<g, b, 0, c->stream>>>(d, *s, oe == 1 ? 0 : 1, relax);
-        c->launches++;
-        if (oe == 1 && l == 1) relax = 1. / (1. - .5 * rJ * rJ);
-        else relax = 1. / (1. - .25 * rJ * rJ * relax);
-      }
-      k_sor_check<<<1, 256, 0, c->stream>>>(*s, s->nblocks, l, eps);
-      c->launches++;
-    }
-    SWM_CK(cudaGetLastError());
-    SWM_CK(cudaMemcpyAsync(done, s->done, 2 * sizeof(int), cudaMemcpyDeviceToHost, c->stream));
+  const int mx = c->nx > c->ny ? c->nx : c->ny;
+  const int max_count = first_guess ? (int)lround(1000. * mx) : (int)lround(10. * mx);
+  const unsigned nb = (unsigned)((c->n + 255) / 256);
+  k_sor_split<<<nb, 256, 0, c->stream>>>(s->B, s->Bs[0], s->Bs[1], c->nx, c->ny, s->W, 0);
+  k_sor_split<<<nb, 256, 0, c->stream>>>(s->chi, s->chis[0], s->chis[1], c->nx, c->ny, s->W, 0);
+  c->launches += 2;
+  SorCtl ctl = {};
+  ctl.relax = 1.;
+  ctl.l = 1;
+  ctl.max_count = max_count;
+  ctl.eps = eps;
+  SWM_CK(cudaMemcpyAsync(s->ctl, &ctl, sizeof(SorCtl), cudaMemcpyHostToDevice, c->stream));
+  int rc = sor_graph(c, s);
+  if (rc != SWM_GPU_OK) return rc;
+  for (int l = 1; l <= max_count; l += SOR_BATCH) {
+    SWM_CK(cudaGraphLaunch(s->graph, c->stream));
+    c->launches += 2 * SOR_BATCH;
+    SWM_CK(cudaMemcpyAsync(&ctl, s->ctl, sizeof(SorCtl), cudaMemcpyDeviceToHost, c->stream));
     SWM_CK(cudaStreamSynchronize(c->stream));
-    if (done[0]) break;
+    if (ctl.done) break;
   }
-  double an = 0.;
-  SWM_CK(cudaMemcpyAsync(&an, s->anorm_hist, 8, cudaMemcpyDeviceToHost, c->stream));
-  SWM_CK(cudaStreamSynchronize(c->stream));
-  if (anorm) *anorm = an;
-  if (done[0]) {
-    if (iters) *iters = done[1];
+  k_sor_split<<<nb, 256, 0, c->stream>>>(s->chi, s->chis[0], s->chis[1], c->nx, c->ny, s->W, 1);
+  c->launches++;
+  SWM_CK(cudaGetLastError());
+  if (anorm) *anorm = ctl.anorm;
+  if (ctl.done) {
+    if (iters) *iters = ctl.iters;
     return SWM_GPU_OK;
   }
   if (iters) *iters = max_count;
