@@ -143,6 +143,7 @@ int swm_gpu_create(const swm_gpu_config *cfg, swm_gpu_ctx **out) {
   }
   swm_gpu_ctx *c = new swm_gpu_ctx();
   c->cfg = *cfg;
+  if (cudaGetDevice(&c->device) != cudaSuccess) c->device = -1;
   c->nx = cfg->nx;
   c->ny = cfg->ny;
   c->n = (size_t)cfg->nx * cfg->ny;
@@ -157,6 +158,7 @@ int swm_gpu_create(const swm_gpu_config *cfg, swm_gpu_ctx **out) {
 }
 
 int swm_gpu_destroy(swm_gpu_ctx *c) {
+  SWM_ON_DEVICE(c ? c->device : -1);
   if (!c) return SWM_GPU_OK;
   cudaStreamSynchronize(c->stream);
   invalidate_graph(c);
@@ -186,15 +188,18 @@ int swm_gpu_destroy(swm_gpu_ctx *c) {
 }
 
 int swm_gpu_synchronize(swm_gpu_ctx *c) {
+  SWM_ON_DEVICE(c ? c->device : -1);
   SWM_REQUIRE(c, "null context");
   SWM_CK(cudaStreamSynchronize(c->stream));
   return SWM_GPU_OK;
 }
 
 void *swm_gpu_stream(swm_gpu_ctx *c) { return c ? (void *)c->stream : nullptr; }
-int64_t swm_gpu_launch_count(swm_gpu_ctx *c) { return c ? c->launches : -1; }
+int64_t swm_gpu_launch_count(swm_gpu_ctx *c) {
+  SWM_ON_DEVICE(c ? c->device : -1); return c ? c->launches : -1; }
 
 int swm_gpu_step_shape(swm_gpu_ctx *c, double *rows, double *masked_cost, int *blocks) {
+  SWM_ON_DEVICE(c ? c->device : -1);
   SWM_REQUIRE(c && rows && masked_cost && blocks, "swm_gpu_step_shape: bad arguments");
   *rows = c->march_tiles ? c->march_S : 0.;
   *masked_cost = c->march_tiles ? c->march_slow : 0.;
@@ -203,6 +208,7 @@ int swm_gpu_step_shape(swm_gpu_ctx *c, double *rows, double *masked_cost, int *b
 }
 
 int swm_gpu_domain(swm_gpu_ctx *c, const double *H, const int8_t *Hmiss) {
+  SWM_ON_DEVICE(c ? c->device : -1);
   SWM_REQUIRE(c && c->stage == 0, "swm_gpu_domain: call once, first");
   TRY(host_domain(c, H, Hmiss));
   g_alloc_stream = c->stream;
@@ -254,6 +260,7 @@ int swm_gpu_domain(swm_gpu_ctx *c, const double *H, const int8_t *Hmiss) {
 // SWM_timestep_init: basic state, then computeD/RelVort/PotVort/EDens/
 // MassFluxes at itt = 0 (which overwrites the grid depths in linear modes).
 int swm_gpu_timestep_init(swm_gpu_ctx *c, const double *psi_bs) {
+  SWM_ON_DEVICE(c ? c->device : -1);
   SWM_REQUIRE(c && c->stage == 1, "swm_gpu_timestep_init: call after swm_gpu_domain");
   if (c->cfg.mode == SWM_MODE_LIN_MEAN) {
     SWM_REQUIRE(psi_bs, "swm_gpu_timestep_init: LINEARISED_MEAN_STATE needs psi_bs");
@@ -270,6 +277,7 @@ int swm_gpu_timestep_init(swm_gpu_ctx *c, const double *psi_bs) {
 
 int swm_gpu_add_damping(swm_gpu_ctx *c, int term, int type, double value, double sl_length,
                         double sl_cutoff, int loc, const double *file_data) {
+  SWM_ON_DEVICE(c ? c->device : -1);
   SWM_REQUIRE(c && c->stage == 2, "swm_gpu_add_damping: call after swm_gpu_timestep_init");
   SWM_REQUIRE(term >= 0 && term <= 4, "swm_gpu_add_damping: unknown term");
   SWM_REQUIRE(type >= 0 && type <= 2, "swm_gpu_add_damping: unknown type");
@@ -280,6 +288,7 @@ int swm_gpu_add_damping(swm_gpu_ctx *c, int term, int type, double value, double
 }
 
 int swm_gpu_finish_damping(swm_gpu_ctx *c) {
+  SWM_ON_DEVICE(c ? c->device : -1);
   SWM_REQUIRE(c && c->stage == 2, "swm_gpu_finish_damping: call after swm_gpu_timestep_init");
   host_damping_finish(c);
   const HostGrid &g = c->hg;
@@ -295,6 +304,7 @@ int swm_gpu_finish_damping(swm_gpu_ctx *c) {
 
 int swm_gpu_add_stream(swm_gpu_ctx *c, int type, int comp, double omega, int is_const, const double *d1,
                        const double *d2, int *id) {
+  SWM_ON_DEVICE(c ? c->device : -1);
   SWM_REQUIRE(c && c->stage == 3, "swm_gpu_add_stream: call after swm_gpu_finish_damping");
   SWM_REQUIRE(type >= 0 && type <= 4, "swm_gpu_add_stream: unknown forcing type");
   SWM_REQUIRE(c->streams.size() < 64, "swm_gpu_add_stream: too many streams");
@@ -317,6 +327,7 @@ int swm_gpu_add_stream(swm_gpu_ctx *c, int type, int comp, double omega, int is_
 }
 
 int swm_gpu_set_stream_data(swm_gpu_ctx *c, int id, const double *d1, const double *d2) {
+  SWM_ON_DEVICE(c ? c->device : -1);
   SWM_REQUIRE(c && id >= 0 && id < (int)c->streams.size(), "swm_gpu_set_stream_data: bad stream id");
   if (d1) TRY(h2d(c, c->streams[id].d1, d1, c->n));
   if (d2) TRY(h2d(c, c->streams[id].d2, d2, c->n));
@@ -325,6 +336,7 @@ int swm_gpu_set_stream_data(swm_gpu_ctx *c, int id, const double *d1, const doub
 }
 
 int swm_gpu_stream_records(swm_gpu_ctx *c, int id, int part, int nrec, const double *records) {
+  SWM_ON_DEVICE(c ? c->device : -1);
   SWM_REQUIRE(c && id >= 0 && id < (int)c->streams.size() && (part == 1 || part == 2) && nrec > 0 && records,
               "swm_gpu_stream_records: bad arguments");
   Stream &s = c->streams[id];
@@ -339,6 +351,7 @@ int swm_gpu_stream_records(swm_gpu_ctx *c, int id, int part, int nrec, const dou
 }
 
 int swm_gpu_stream_interp(swm_gpu_ctx *c, int id, int part, int r0, int r1, double t, double t0, double t1) {
+  SWM_ON_DEVICE(c ? c->device : -1);
   SWM_REQUIRE(c && id >= 0 && id < (int)c->streams.size() && (part == 1 || part == 2),
               "swm_gpu_stream_interp: bad arguments");
   Stream &s = c->streams[id];
@@ -350,6 +363,7 @@ int swm_gpu_stream_interp(swm_gpu_ctx *c, int id, int part, int r0, int r1, doub
 }
 
 int swm_gpu_forcing_init(swm_gpu_ctx *c) {
+  SWM_ON_DEVICE(c ? c->device : -1);
   SWM_REQUIRE(c && c->stage == 3, "swm_gpu_forcing_init: call after swm_gpu_finish_damping");
   TRY(plain_forcing_update(c, 0, 1));
   TRY(plain_forcing_update(c, 0, 0));
@@ -360,6 +374,7 @@ int swm_gpu_forcing_init(swm_gpu_ctx *c) {
 static int swm_advance_impl(swm_gpu_ctx *c, int64_t itt);
 
 int swm_gpu_initial_conditions(swm_gpu_ctx *c, const double *eta, const double *u, const double *v) {
+  SWM_ON_DEVICE(c ? c->device : -1);
   SWM_REQUIRE(c && c->stage == 4, "swm_gpu_initial_conditions: call after swm_gpu_forcing_init");
   size_t n = c->n;
   std::vector<double> buf(n);
@@ -419,12 +434,14 @@ static int swm_advance_impl(swm_gpu_ctx *c, int64_t itt) {
 }
 
 int swm_gpu_step(swm_gpu_ctx *c, int64_t itt) {
+  SWM_ON_DEVICE(c ? c->device : -1);
   SWM_REQUIRE(c && c->stage >= 5, "swm_gpu_step: model not initialised");
   SWM_REQUIRE(itt >= 1, "swm_gpu_step: itt starts at 1");
   return swm_step_impl(c, itt);
 }
 
 int swm_gpu_advance(swm_gpu_ctx *c, int64_t itt) {
+  SWM_ON_DEVICE(c ? c->device : -1);
   SWM_REQUIRE(c && c->stage >= 5, "swm_gpu_advance: model not initialised");
   return swm_advance_impl(c, itt);
 }
@@ -479,6 +496,7 @@ static int graph_capture(swm_gpu_ctx *c, int64_t itt0) {
 }
 
 int swm_gpu_run(swm_gpu_ctx *c, int64_t itt0, int64_t nsteps) {
+  SWM_ON_DEVICE(c ? c->device : -1);
   SWM_REQUIRE(c && c->stage >= 5, "swm_gpu_run: model not initialised");
   const bool graphs = graph_eligible(c) && nsteps >= 2 * GRAPH_STEPS;
   int64_t s = 1;
@@ -527,6 +545,7 @@ static double *mapped_view(const double *h) {
 // advance, and copies.
 int swm_gpu_run_monitor(swm_gpu_ctx *c, int64_t itt0, int64_t nsteps, int stream_id, const double *rows1,
                         const double *rows2, double *out3) {
+  SWM_ON_DEVICE(c ? c->device : -1);
   SWM_REQUIRE(c && c->stage >= 5 && nsteps > 0 && out3, "swm_gpu_run_monitor: bad arguments");
   SWM_REQUIRE(!rows1 || (stream_id >= 0 && stream_id < (int)c->streams.size()),
               "swm_gpu_run_monitor: bad stream id");
@@ -659,6 +678,7 @@ static int field_device(swm_gpu_ctx *c, int f, const double **out) {
 }
 
 int swm_gpu_get_field(swm_gpu_ctx *c, int f, double *out) {
+  SWM_ON_DEVICE(c ? c->device : -1);
   SWM_REQUIRE(c && c->stage >= 1 && out, "swm_gpu_get_field: bad arguments");
   const double *p = nullptr;
   TRY(field_device(c, f, &p));
@@ -684,6 +704,7 @@ int swm::async_record(swm_gpu_ctx *c, int64_t *ticket) {
 extern "C" {
 
 int swm_gpu_get_field_async(swm_gpu_ctx *c, int f, double *out, int64_t *ticket) {
+  SWM_ON_DEVICE(c ? c->device : -1);
   SWM_REQUIRE(c && c->stage >= 1 && out && ticket, "swm_gpu_get_field_async: bad arguments");
   const double *p = nullptr;
   TRY(field_device(c, f, &p));
@@ -692,12 +713,14 @@ int swm_gpu_get_field_async(swm_gpu_ctx *c, int f, double *out, int64_t *ticket)
 }
 
 int swm_gpu_wait(swm_gpu_ctx *c, int64_t ticket) {
+  SWM_ON_DEVICE(c ? c->device : -1);
   SWM_REQUIRE(c && ticket >= 0 && ticket < c->async_next, "swm_gpu_wait: unknown ticket");
   SWM_CK(cudaEventSynchronize(c->async_ev[ticket % ASYNC_RING]));
   return SWM_GPU_OK;
 }
 
 int swm_gpu_ready(swm_gpu_ctx *c, int64_t ticket) {
+  SWM_ON_DEVICE(c ? c->device : -1);
   if (!c || ticket < 0 || ticket >= c->async_next) return -1;
   cudaError_t e = cudaEventQuery(c->async_ev[ticket % ASYNC_RING]);
   if (e == cudaSuccess) return 1;
@@ -707,6 +730,7 @@ int swm_gpu_ready(swm_gpu_ctx *c, int64_t ticket) {
 }
 
 int swm_gpu_diag_accumulate(swm_gpu_ctx *c, int slot, int f, int square, double weight) {
+  SWM_ON_DEVICE(c ? c->device : -1);
   SWM_REQUIRE(c && c->stage >= 5 && slot >= 0 && slot < 4096, "swm_gpu_diag_accumulate: bad arguments");
   const double *p = nullptr;
   TRY(field_device(c, f, &p));
@@ -714,6 +738,7 @@ int swm_gpu_diag_accumulate(swm_gpu_ctx *c, int slot, int f, int square, double 
 }
 
 int swm_gpu_diag_mean(swm_gpu_ctx *c, int slot, double *out, double *count) {
+  SWM_ON_DEVICE(c ? c->device : -1);
   SWM_REQUIRE(c && out, "swm_gpu_diag_mean: bad arguments");
   if (!c->psi_tmp) {  // the zonal-sum scratch doubles as the staging buffer
     SWM_CK(cudaMalloc((void **)&c->psi, c->n * 8));
@@ -724,6 +749,7 @@ int swm_gpu_diag_mean(swm_gpu_ctx *c, int slot, double *out, double *count) {
 }
 
 int swm_gpu_set_field(swm_gpu_ctx *c, int f, const double *in) {
+  SWM_ON_DEVICE(c ? c->device : -1);
   SWM_REQUIRE(c && c->stage >= 1 && in, "swm_gpu_set_field: bad arguments");
   double *p = nullptr;
   field_ptr(c, f, &p);
@@ -735,6 +761,7 @@ int swm_gpu_set_field(swm_gpu_ctx *c, int f, const double *in) {
 }
 
 int swm_gpu_get_metric(swm_gpu_ctx *c, int which, int grid, double *out) {
+  SWM_ON_DEVICE(c ? c->device : -1);
   SWM_REQUIRE(c && c->stage >= 1 && out && which >= 0 && which <= 3 && grid >= 0 && grid <= 3,
               "swm_gpu_get_metric: bad arguments");
   const HostGrid &g = c->hg;
@@ -744,12 +771,14 @@ int swm_gpu_get_metric(swm_gpu_ctx *c, int which, int grid, double *out) {
 }
 
 int swm_gpu_get_mask(swm_gpu_ctx *c, int grid, int8_t *out) {
+  SWM_ON_DEVICE(c ? c->device : -1);
   SWM_REQUIRE(c && c->stage >= 1 && out && grid >= 0 && grid <= 3, "swm_gpu_get_mask: bad arguments");
   memcpy(out, c->hg.ocean[grid].data(), c->n);
   return SWM_GPU_OK;
 }
 
 int swm_gpu_streamfunction(swm_gpu_ctx *c, double *psi) {
+  SWM_ON_DEVICE(c ? c->device : -1);
   SWM_REQUIRE(c && c->stage >= 5 && psi, "swm_gpu_streamfunction: bad arguments");
   return swm_gpu_get_field(c, SWM_F_PSI, psi);
 }

@@ -30,6 +30,23 @@ void set_error(const std::string &msg);
     }                                                                             \
   } while (0)
 
+// Every entry point runs on the device its context was created on: the guard
+// makes that device current for the call and restores the caller's device
+// when it returns (nothing happens when it is already current).
+struct DeviceGuard {
+  int prev = -1;
+  explicit DeviceGuard(int dev) {
+    int cur = -1;
+    if (dev >= 0 && cudaGetDevice(&cur) == cudaSuccess && cur != dev && cudaSetDevice(dev) == cudaSuccess) prev = cur;
+  }
+  ~DeviceGuard() {
+    if (prev >= 0) cudaSetDevice(prev);
+  }
+  DeviceGuard(const DeviceGuard &) = delete;
+  DeviceGuard &operator=(const DeviceGuard &) = delete;
+};
+#define SWM_ON_DEVICE(dev) ::swm::DeviceGuard swm_device_guard_(dev)
+
 #define SWM_REQUIRE(cond, msg)                                                    \
   do {                                                                            \
     if (!(cond)) {                                                                \
@@ -101,6 +118,7 @@ struct Trc32State;
 
 struct swm_gpu_ctx {
   swm_gpu_config cfg;
+  int device = -1;  // the CUDA device the context was created on
   int nx = 0, ny = 0;
   size_t n = 0;
   cudaStream_t stream = nullptr;

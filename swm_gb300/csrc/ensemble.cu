@@ -117,6 +117,7 @@ struct EnsMonitor {
 
 struct swm_gpu_ensemble {
   std::vector<swm_gpu_ctx *> m;
+  int device = -1;  // the members' device
   int mix = 0, rows = 16, phase = 0, graph_phase = -1;
   double slow = 1.;  // masked-row cost the tiles were cut with
   bool std_cfg = false;  // all members in the step kernel's common configuration
@@ -301,12 +302,22 @@ extern "C" {
 int swm_gpu_ensemble_create(swm_gpu_ctx *const *members, int n, swm_gpu_ensemble **out) {
   SWM_REQUIRE(members && n > 0 && out, "swm_gpu_ensemble_create: bad arguments");
   *out = nullptr;
+  SWM_REQUIRE(members[0], "swm_gpu_ensemble_create: members must be initialised");
+  for (int i = 1; i < n; i++)
+    SWM_REQUIRE(members[i] && members[i]->device == members[0]->device,
+                "swm_gpu_ensemble_create: members must live on one device");
+  SWM_ON_DEVICE(members[0]->device);
   int n0 = -1, g0 = -1, mix = -1;
   for (int i = 0; i < n; i++) {
     swm_gpu_ctx *c = members[i];
     SWM_REQUIRE(c && c->stage >= 5, "swm_gpu_ensemble_create: members must be initialised");
     SWM_REQUIRE(c->cfg.path == SWM_PATH_FUSED_FP32C, "swm_gpu_ensemble_create: members must use SWM_PATH_FUSED_FP32C");
     SWM_REQUIRE(c->tracers.empty(), "swm_gpu_ensemble_create: members with tracers are not batched");
+    SWM_REQUIRE(c->cfg.mode != SWM_MODE_LIN_MEAN,
+                "swm_gpu_ensemble_create: LINEARISED_MEAN_STATE members are stepped on their own");
+    for (const Stream &st : c->streams)
+      SWM_REQUIRE(st.type != SWM_FRC_OSC, "swm_gpu_ensemble_create: members with oscillating forcing are stepped "
+                                          "on their own");
     SWM_REQUIRE(c->ny < (1 << 23), "swm_gpu_ensemble_create: member too large for a tile index");
     if (!c->march_rows) c->march_rows = 16;  // the ensemble tunes its own strip rows
     int rc = fused_prepare(c);
@@ -320,6 +331,7 @@ int swm_gpu_ensemble_create(swm_gpu_ctx *const *members, int n, swm_gpu_ensemble
   }
   swm_gpu_ensemble *e = new swm_gpu_ensemble();
   e->m.assign(members, members + n);
+  e->device = members[0]->device;
   e->mix = mix;
   auto fail = [&](int rc) { ens_free(e); return rc; };
   if (cudaStreamCreateWithFlags(&e->stream, cudaStreamNonBlocking) != cudaSuccess ||
@@ -434,11 +446,13 @@ int swm_gpu_ensemble_create(swm_gpu_ctx *const *members, int n, swm_gpu_ensemble
 }
 
 int swm_gpu_ensemble_destroy(swm_gpu_ensemble *e) {
+  SWM_ON_DEVICE(e ? e->device : -1);
   if (e) ens_free(e);
   return SWM_GPU_OK;
 }
 
 int swm_gpu_ensemble_run(swm_gpu_ensemble *e, int64_t itt0, int64_t nsteps) {
+  SWM_ON_DEVICE(e ? e->device : -1);
   SWM_REQUIRE(e && nsteps >= 0, "swm_gpu_ensemble_run: bad arguments");
   int64_t s = 1;
   // Adams-Bashforth start-up steps (itt 1, 2): each member on its own stream
@@ -479,6 +493,7 @@ int swm_gpu_ensemble_run(swm_gpu_ensemble *e, int64_t itt0, int64_t nsteps) {
 
 int swm_gpu_ensemble_run_monitor(swm_gpu_ensemble *e, int64_t itt0, int64_t nsteps, const double *rows,
                                  double *out) {
+  SWM_ON_DEVICE(e ? e->device : -1);
   SWM_REQUIRE(e && nsteps >= 0 && out, "swm_gpu_ensemble_run_monitor: bad arguments");
   int rc = ens_monitor_setup(e);
   if (rc != SWM_GPU_OK) return rc;
@@ -535,6 +550,7 @@ int swm_gpu_ensemble_run_monitor(swm_gpu_ensemble *e, int64_t itt0, int64_t nste
 }
 
 int swm_gpu_ensemble_integrals(swm_gpu_ensemble *e, double *out) {
+  SWM_ON_DEVICE(e ? e->device : -1);
   SWM_REQUIRE(e && out, "swm_gpu_ensemble_integrals: bad arguments");
   const size_t n = e->m.size();
   std::vector<EnsInt> d(n);
@@ -562,6 +578,7 @@ int swm_gpu_ensemble_integrals(swm_gpu_ensemble *e, double *out) {
 }
 
 int swm_gpu_ensemble_synchronize(swm_gpu_ensemble *e) {
+  SWM_ON_DEVICE(e ? e->device : -1);
   SWM_REQUIRE(e, "swm_gpu_ensemble_synchronize: null ensemble");
   SWM_CK(cudaStreamSynchronize(e->stream));
   return SWM_GPU_OK;

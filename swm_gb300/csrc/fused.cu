@@ -350,6 +350,12 @@ struct FusedState {
   int wind_x = 0, wind_y = 0;
   double impl_s[3] = {1, 1, 1}, gsq_s[2] = {0, 0};
   int n0 = 0, g0 = 0;  // FP32C level / ring indices
+  // forcing that changes every step (LINEARISED_MEAN_STATE terms, oscillating
+  // streams): F = Fc + this step's part, written before the step kernel;
+  // the per-step relative vorticity and energy term of the mean state
+  bool lin_mean = false, dyn_F = false;
+  void *Fc[3] = {};
+  double *ms_zeta = nullptr, *ms_ex = nullptr;
 };
 
 namespace swm {
@@ -401,8 +407,8 @@ int fused_prepare(swm_gpu_ctx *c) {
   FusedState *f = c->fused;
   if (f && f->ready) return SWM_GPU_OK;
   const swm_gpu_config &cf = c->cfg;
-  SWM_REQUIRE(cf.mode != SWM_MODE_LIN_MEAN, "fused paths: LINEARISED_MEAN_STATE runs on the plain path");
   if (!f) f = c->fused = new FusedState();
+  f->lin_mean = cf.mode == SWM_MODE_LIN_MEAN;
   bool f32 = cf.path == SWM_PATH_FUSED_FP32C;
   f->comp = f32;
   size_t n = c->n;
@@ -465,7 +471,11 @@ int fused_prepare(swm_gpu_ctx *c) {
     if (s.is_const) continue;
     bool nl_wind = s.type == SWM_FRC_WIND && cf.mode == SWM_MODE_NONLINEAR &&
                    (s.comp == SWM_CMP_ZONAL || s.comp == SWM_CMP_MERID);
-    SWM_REQUIRE(nl_wind, "fused paths: time-dependent forcing other than FULLY_NONLINEAR wind stress runs on the plain path");
+    if (!nl_wind) {  // added to the forcing fields every step (dyn_forcing)
+      SWM_REQUIRE(s.type != SWM_FRC_EMF, "fused paths: time-dependent eddy momentum flux forcing runs on the plain path");
+      f->dyn_F = true;
+      continue;
+    }
     std::vector<double> d;
     download(c, s.d1, d);
     bool rowwise = true;
@@ -486,6 +496,16 @@ int fused_prepare(swm_gpu_ctx *c) {
     f->wind_rows = rowwise;
   }
   if (f->wind_x && f->wind_y) SWM_REQUIRE(f->wind_rows, "fused paths: two wind components must both be row profiles");
+  f->dyn_F = f->dyn_F || f->lin_mean;
+  if (f->dyn_F) {
+    // every step writes F = Fc + its own part (dyn_forcing)
+    f->has_F = true;
+    for (int q = 0; q < 3; q++) FTRY(upload_t(c, f32, Fh[q].data(), n, &f->Fc[q]));
+  }
+  if (f->lin_mean) {
+    FTRY(dmalloc((void **)&f->ms_zeta, n * 8));
+    FTRY(dmalloc((void **)&f->ms_ex, n * 8));
+  }
   if (f->has_F)
     for (int q = 0; q < 3; q++) FTRY(upload_t(c, f32, Fh[q].data(), n, &f->F[q]));
   if (f32) {
@@ -763,6 +783,179 @@ static int march_grid(swm_gpu_ctx *c, const P32 &p, MarchGrid *g) {
 
 // one step of the pair state; a monitored step (c->mon, taken here) runs the
 // step kernel with its monitoring jobs
+// ---- LINEARISED_MEAN_STATE on the fused paths ------------------------------
+// The mean-state terms of the step -- the eta flux by the basic flow (with
+// the reference's ip1(j) zonal index, Q3; swm_nonlinear_timestep_module.f90:
+// 353-365), the relative vorticity times the basic flow (:385-388, :419-422),
+// the basic-state vorticity part of the potential vorticity ((f + zeta_bs) /
+// Dh, :230-257) and the basic-state part of the energy density (u U + v V,
+// :259-310) -- are linear in the perturbation with static coefficients.  Two
+// small kernels form them from the state the step reads and write F = Fc +
+// terms into the forcing fields the fused kernels add, so the kernels keep
+// the state-of-rest arithmetic (f / Dh, G eta).  FP64 arithmetic on either
+// path; the FP32 pair state is read as hi + lo.
+struct MSIn {
+  const double *u, *v, *e;                              // FP64 state, or
+  const float *uh, *ul, *vh, *vl, *eh, *el;             // the FP32 pair state
+  __device__ __forceinline__ double U(size_t k) const { return u ? u[k] : (double)uh[k] + (double)ul[k]; }
+  __device__ __forceinline__ double V(size_t k) const { return v ? v[k] : (double)vh[k] + (double)vl[k]; }
+  __device__ __forceinline__ double E(size_t k) const { return e ? e[k] : (double)eh[k] + (double)el[k]; }
+};
+
+// relative vorticity at H points (vorticityFromVelocities2D, calc_lib.f90:
+// 663-678) and u U + v V interpolated to eta points
+__global__ void k_ms_diag(Dev d, MSIn s, const double *ubs, const double *vbs, double *zeta, double *ex) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x, j = blockIdx.y * blockDim.y + threadIdx.y;
+  if (i >= d.nx || j >= d.ny) return;
+  const size_t k = i + (size_t)d.nx * j;
+  const int im = i == 0 ? d.nx - 1 : i - 1, jm = j == 0 ? d.ny - 1 : j - 1;
+  const int ip = i + 1 == d.nx ? 0 : i + 1, jp = j + 1 == d.ny ? 0 : j + 1;
+  const size_t ki = im + (size_t)d.nx * j, kj = i + (size_t)d.nx * jm;
+  const int8_t *oU = d.ocean[GU], *oV = d.ocean[GV];
+  const double bcH = d.ocean[GH][k] == 1 ? 1. : d.lbc;
+  const double *cH = d.cosl[GH], *cU = d.cosl[GU];
+  const double dvdx = (oV[ki] + oV[k] == 0) ? 0. : bcH / (d.A * cH[j] * d.dLambda) * (s.V(k) - s.V(ki));
+  const double dudy = (oU[k] + oU[kj] == 0) ? 0. : bcH * (cU[j] * s.U(k) - cU[jm] * s.U(kj)) / (d.A * d.dTheta);
+  zeta[k] = dvdx - dudy / cH[j];
+  const size_t kip = ip + (size_t)d.nx * j, kjp = i + (size_t)d.nx * jp;
+  ex[k] = d.ocean[GE][k] == 1 ? (.5 * (s.U(kip) * ubs[kip]) + .5 * (s.U(k) * ubs[k])) +
+                                   (.5 * (s.V(kjp) * vbs[kjp]) + .5 * (s.V(k) * vbs[k]))
+                              : 0.;
+}
+
+template <typename T>
+__global__ void k_ms_terms(Dev d, MSIn s, const double *ubs, const double *vbs, const double *zbs,
+                           const double *zeta, const double *ex, const T *Fcx, const T *Fcy, const T *Fce, T *Fx,
+                           T *Fy, T *Fe) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x, j = blockIdx.y * blockDim.y + threadIdx.y;
+  if (i >= d.nx || j >= d.ny) return;
+  const int nx = d.nx, ny = d.ny;
+  auto K = [nx](int a, int b) { return a + (size_t)nx * b; };
+  const size_t k = K(i, j);
+  const int im = i == 0 ? nx - 1 : i - 1, jm = j == 0 ? ny - 1 : j - 1;
+  const int ip = i + 1 == nx ? 0 : i + 1, jp = j + 1 == ny ? 0 : j + 1;
+  const int8_t *oE = d.ocean[GE], *oU = d.ocean[GU], *oV = d.ocean[GV];
+  const double A = d.A, dL = d.dLambda, dT = d.dTheta;
+  const double *cE = d.cosl[GE], *cU = d.cosl[GU], *cV = d.cosl[GV];
+  const double *Dh = d.Hg[GH], *Du = d.Hg[GU], *Dv = d.Hg[GV];
+  auto e2 = [&](size_t a, size_t b) {  // mask-normalised two-point mean of eta
+    const double w = 1. / fmax((double)(oE[a] + oE[b]), 1.);
+    return ((double)oE[a] * w) * s.E(a) + ((double)oE[b] * w) * s.E(b);
+  };
+  auto potx = [&](size_t a) { return zbs[a] / fmax(Dh[a], 2.220446049250313e-16); };
+  double te = 0., tu = 0., tv = 0.;
+  if (oE[k] == 1) {
+    const int qi = j % nx == nx - 1 ? 0 : j % nx + 1;  // ip1(j) (Q3)
+    const int qim = qi == 0 ? nx - 1 : qi - 1;
+    const int jpm = jp == 0 ? ny - 1 : jp - 1;
+    const double ea = e2(K(qi, j), K(qim, j)), eb = e2(k, K(im, j));
+    const double ec = e2(K(i, jp), K(i, jpm)), ed = e2(k, K(i, jm));
+    const double t = -(ea * ubs[K(ip, j)] - eb * ubs[k]) / dL - (cV[jp] * ec * vbs[K(i, jp)] - cV[j] * ed * vbs[k]) / dT;
+    te = t / (A * cE[j]);
+  }
+  if (oU[k] == 1) {
+    const size_t a1 = K(i, jp), a2 = K(im, j), a3 = K(im, jp);
+    auto mv = [&](size_t a) { return oV[a] == 1 ? Dv[a] * s.V(a) : 0.; };
+    tu = (.5 * zeta[a1] + .5 * zeta[k]) * (.25 * vbs[a1] + .25 * vbs[a2] + .25 * vbs[a3] + .25 * vbs[k]) +
+         (.5 * potx(a1) + .5 * potx(k)) * (.25 * mv(a1) + .25 * mv(a2) + .25 * mv(a3) + .25 * mv(k)) -
+         (ex[k] - ex[a2]) / (A * cU[j] * dL);
+  }
+  if (oV[k] == 1) {
+    const size_t a1 = K(ip, j), a2 = K(i, jm), a4 = K(ip, jm);
+    auto mu = [&](size_t a) { return oU[a] == 1 ? Du[a] * s.U(a) : 0.; };
+    tv = -(.5 * zeta[a1] + .5 * zeta[k]) * (.25 * ubs[a1] + .25 * ubs[a2] + .25 * ubs[k] + .25 * ubs[a4]) -
+         (.5 * potx(a1) + .5 * potx(k)) * (.25 * mu(a1) + .25 * mu(a2) + .25 * mu(k) + .25 * mu(a4)) -
+         (ex[k] - ex[a2]) / (A * dT);
+  }
+  Fe[k] = (T)((double)Fce[k] + te);
+  Fx[k] = (T)((double)Fcx[k] + tu);
+  Fy[k] = (T)((double)Fcy[k] + tv);
+}
+
+// a time-dependent stream's part of the step's forcing, on the component's
+// ocean points (swm_forcing_module.f90): oscillating (processOscillation
+// :326-374) F += 2 (Re cos(omega t) - Im sin(omega t)); wind stress in the
+// linear modes (processWindstress :274-324) F += scale d / (RHO0 [D]);
+// custom and heating (:396-434, :539-552) F += d
+template <typename T>
+__global__ void k_stream_add(int n, int type, const double *d1, const double *d2, const int8_t *msk,
+                             const double *D, double scale, double rho0, double r_iot, double i_iot, T *F) {
+  const size_t k = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (k >= (size_t)n) return;
+  double a;
+  if (type == SWM_FRC_OSC) {
+    a = (2. * (d1[k] * r_iot - d2[k] * i_iot)) * msk[k];
+  } else {
+    if (msk[k] != 1) return;
+    a = type == SWM_FRC_WIND ? scale * d1[k] / (D ? rho0 * D[k] : rho0) : d1[k];
+  }
+  F[k] = (T)((double)F[k] + a);
+}
+
+// the mean-state terms of the coming step into the forcing fields
+static int ms_terms(swm_gpu_ctx *c) {
+  FusedState *f = c->fused;
+  Dev d = c->dev();
+  MSIn s = {};
+  if (f->comp) {
+    const int a = f->n0;
+    s.uh = f->uh[a]; s.ul = f->ul[a]; s.vh = f->vh[a]; s.vl = f->vl[a]; s.eh = f->eh[a]; s.el = f->el[a];
+  } else {
+    s.u = d.u0; s.v = d.v0; s.e = d.eta0;
+  }
+  dim3 b(32, 8), g((c->nx + 31) / 32, (c->ny + 7) / 8);
+  k_ms_diag<<<g, b, 0, c->stream>>>(d, s, c->ubs, c->vbs, f->ms_zeta, f->ms_ex);
+  if (f->comp)
+    k_ms_terms<float><<<g, b, 0, c->stream>>>(d, s, c->ubs, c->vbs, c->zbs, f->ms_zeta, f->ms_ex,
+                                              (const float *)f->Fc[0], (const float *)f->Fc[1],
+                                              (const float *)f->Fc[2], (float *)f->F[0], (float *)f->F[1],
+                                              (float *)f->F[2]);
+  else
+    k_ms_terms<double><<<g, b, 0, c->stream>>>(d, s, c->ubs, c->vbs, c->zbs, f->ms_zeta, f->ms_ex,
+                                               (const double *)f->Fc[0], (const double *)f->Fc[1],
+                                               (const double *)f->Fc[2], (double *)f->F[0], (double *)f->F[1],
+                                               (double *)f->F[2]);
+  c->launches += 2;
+  SWM_CK(cudaGetLastError());
+  return SWM_GPU_OK;
+}
+
+// forcing of step itt: F = Fc (+ the mean-state terms) + the oscillating
+// streams at the time the reference's forcing holds during step itt (set by
+// the advance after step itt - 1: t = (itt - 1) dt)
+static int dyn_forcing(swm_gpu_ctx *c, int64_t itt) {
+  FusedState *f = c->fused;
+  const size_t es = f->comp ? 4 : 8;
+  if (f->lin_mean) FTRY(ms_terms(c));
+  else
+    for (int q = 0; q < 3; q++) SWM_CK(cudaMemcpyAsync(f->F[q], f->Fc[q], c->n * es, cudaMemcpyDeviceToDevice, c->stream));
+  const double t = (double)(itt - 1) * c->cfg.dt;
+  const int ns = (int)c->streams.size();
+  std::vector<int> order;  // the reference's stream order: head, then reverse insertion
+  if (ns > 0) order.push_back(0);
+  for (int q = ns - 1; q >= 1; q--) order.push_back(q);
+  const bool nonlin = c->cfg.mode == SWM_MODE_NONLINEAR;
+  for (int q : order) {
+    const Stream &st = c->streams[q];
+    if (st.is_const) continue;
+    if (st.type == SWM_FRC_WIND && nonlin) continue;  // recomputed by the step kernel
+    const int k = st.type == SWM_FRC_HEAT ? 2 : (st.comp == SWM_CMP_ZONAL ? 0 : (st.comp == SWM_CMP_MERID ? 1 : 2));
+    const int g = k == 0 ? GU : (k == 1 ? GV : GE);
+    const double *D = (st.type == SWM_FRC_WIND && c->cfg.barotropic) ? c->d_H[g] : nullptr;
+    const double r = cos(st.omega * t), im = sin(st.omega * t);
+    const unsigned nb = (unsigned)((c->n + 255) / 256);
+    if (f->comp)
+      k_stream_add<float><<<nb, 256, 0, c->stream>>>((int)c->n, st.type, st.d1, st.d2, c->d_ocean[g], D,
+                                                     c->cfg.tau_scale, c->cfg.RHO0, r, im, (float *)f->F[k]);
+    else
+      k_stream_add<double><<<nb, 256, 0, c->stream>>>((int)c->n, st.type, st.d1, st.d2, c->d_ocean[g], D,
+                                                      c->cfg.tau_scale, c->cfg.RHO0, r, im, (double *)f->F[k]);
+    c->launches++;
+  }
+  SWM_CK(cudaGetLastError());
+  return SWM_GPU_OK;
+}
+
 static int launch_fp32c(swm_gpu_ctx *c, int64_t itt) {
   P32 p;
   make_p32(c, itt, p);
@@ -780,6 +973,7 @@ static int launch_fp32c(swm_gpu_ctx *c, int64_t itt) {
 int fused_step(swm_gpu_ctx *c, int64_t itt) {
   FTRY(fused_prepare(c));
   FusedState *f = c->fused;
+  if (f->dyn_F) FTRY(dyn_forcing(c, itt));
   if (!f->comp) {
     FP<double> p;
     memset(&p, 0, sizeof(p));
@@ -810,7 +1004,8 @@ void fused_free(swm_gpu_ctx *c) {
   for (int q = 0; q < 3; q++) { F(f->Gu[q]); F(f->Gv[q]); F(f->Ge[q]); F(f->impl[q]); F(f->F[q]); }
   for (int q = 0; q < 2; q++) F(f->gsq[q]);
   F(f->mc); F(f->He); F(f->rows); F(f->Hu); F(f->Hv); F(f->wx); F(f->wy); F(f->rows32c); F(f->mask16);
-  for (int q = 0; q < 3; q++) F(f->dp[q]);
+  for (int q = 0; q < 3; q++) { F(f->dp[q]); F(f->Fc[q]); }
+  F(f->ms_zeta); F(f->ms_ex);
   delete f;
   c->fused = nullptr;
 }
@@ -1161,6 +1356,7 @@ void integrals_free(swm_gpu_ctx *c) {
 extern "C" {
 
 int swm_gpu_set_stream_rows(swm_gpu_ctx *c, int id, const double *r1, const double *r2) {
+  SWM_ON_DEVICE(c ? c->device : -1);
   return swm::stream_rows(c, id, r1, r2, nullptr);
 }
 
@@ -1264,7 +1460,7 @@ int integrals_to(swm_gpu_ctx *c, double *dst, double **where) {
 
 bool monitor_fast(const swm_gpu_ctx *c) {
   const FusedState *f = c->fused;
-  return c->cfg.path == SWM_PATH_FUSED_FP32C && f && f->ready && f->comp && !c->cfg.frozen_flow;
+  return c->cfg.path == SWM_PATH_FUSED_FP32C && f && f->ready && f->comp && !c->cfg.frozen_flow && !f->dyn_F;
 }
 
 bool monitor_rows_fast(const swm_gpu_ctx *c, int sid) {
@@ -1364,6 +1560,7 @@ int monitor_keep_rows(swm_gpu_ctx *c, const MonitorBufs &b, int last) {
 extern "C" {
 
 int swm_gpu_integrals(swm_gpu_ctx *c, double *out3) {
+  SWM_ON_DEVICE(c ? c->device : -1);
   SWM_REQUIRE(c && c->stage >= 5 && out3, "swm_gpu_integrals: bad arguments");
   FTRY(integrals_launch(c));
   IntegralScratch *S = c->integrals;
@@ -1374,6 +1571,7 @@ int swm_gpu_integrals(swm_gpu_ctx *c, double *out3) {
 }
 
 int swm_gpu_integrals_async(swm_gpu_ctx *c, double *out3, int64_t *ticket) {
+  SWM_ON_DEVICE(c ? c->device : -1);
   SWM_REQUIRE(c && c->stage >= 5 && out3 && ticket, "swm_gpu_integrals_async: bad arguments");
   FTRY(integrals_launch(c));
   SWM_CK(cudaMemcpyAsync(out3, c->integrals->out, 3 * 8, cudaMemcpyDeviceToHost, c->stream));
@@ -1427,6 +1625,7 @@ __global__ void k_area_rows(const double *cos_u, const double *cos_v, const doub
 }  // namespace swm
 
 extern "C" int swm_gpu_integrals_noalloc(swm_gpu_ctx *c, double *out3) {
+  SWM_ON_DEVICE(c ? c->device : -1);
   using namespace swm;
   SWM_REQUIRE(c && c->stage >= 5 && out3, "swm_gpu_integrals_noalloc: bad arguments");
   if (c->ny > SWM_NOALLOC_MAX_NY) {

@@ -321,6 +321,7 @@ __global__ void k_h_axpy(double *psi, const float *e32, size_t n, double scale) 
 }  // namespace swm
 
 struct swm_helm {
+  int device = -1;  // the CUDA device the solver was created on
   double *cx = nullptr, *cy = nullptr, *rcc = nullptr;  // FP64 coefficients
   int nx = 0, ny = 0;
   size_t n = 0;
@@ -466,6 +467,7 @@ int swm_helm_create(int nx, int ny, double dx, double dy, double lambda, const d
   SWM_REQUIRE(nx >= 3 && ny >= 3 && dx > 0 && dy > 0 && H && ocean && out, "swm_helm_create: bad arguments");
   *out = nullptr;
   swm_helm *h = new swm_helm();
+  if (cudaGetDevice(&h->device) != cudaSuccess) h->device = -1;
   h->nx = nx; h->ny = ny; h->n = (size_t)nx * ny; h->dx = dx; h->dy = dy; h->lambda = lambda;
   const size_t n = h->n;
   std::vector<double> hinv(n);
@@ -507,6 +509,7 @@ int swm_helm_create(int nx, int ny, double dx, double dy, double lambda, const d
 }
 
 int swm_helm_destroy(swm_helm *h) {
+  SWM_ON_DEVICE(h ? h->device : -1);
   helm_free(h);
   return SWM_GPU_OK;
 }
@@ -516,6 +519,7 @@ int64_t swm_helm_launch_count(swm_helm *h) { return h ? h->launches : -1; }
 
 // out = A psi (ocean cells; 0 elsewhere), FP64
 int swm_helm_apply(swm_helm *h, const double *psi, double *out) {
+  SWM_ON_DEVICE(h ? h->device : -1);
   SWM_REQUIRE(h && psi && out, "swm_helm_apply: bad arguments");
   SWM_CK(cudaMemcpyAsync(h->psi, psi, h->n * 8, cudaMemcpyHostToDevice, h->stream));
   SWM_CK(cudaMemsetAsync(h->rhs, 0, h->n * 8, h->stream));
@@ -531,6 +535,7 @@ int swm_helm_apply(swm_helm *h, const double *psi, double *out) {
 // (checked every 16 sweeps) or max_sweeps.
 int swm_helm_solve_fp64(swm_helm *h, const double *rhs, double *psi, double omega, double rtol, int max_sweeps,
                         int *sweeps, double *relres) {
+  SWM_ON_DEVICE(h ? h->device : -1);
   SWM_REQUIRE(h && rhs && psi && max_sweeps > 0, "swm_helm_solve_fp64: bad arguments");
   SWM_CK(cudaMemcpyAsync(h->rhs, rhs, h->n * 8, cudaMemcpyHostToDevice, h->stream));
   SWM_CK(cudaMemcpyAsync(h->psi, psi, h->n * 8, cudaMemcpyHostToDevice, h->stream));
@@ -561,6 +566,7 @@ int swm_helm_solve_fp64(swm_helm *h, const double *rhs, double *psi, double omeg
 // FP64; repeated until the FP64 relative residual is below rtol.
 int swm_helm_solve_mixed(swm_helm *h, const double *rhs, double *psi, double omega, double rtol, double inner_tol,
                          int max_sweeps, int *sweeps, int *outer, double *relres) {
+  SWM_ON_DEVICE(h ? h->device : -1);
   SWM_REQUIRE(h && rhs && psi && max_sweeps > 0 && inner_tol > 0, "swm_helm_solve_mixed: bad arguments");
   SWM_CK(cudaMemcpyAsync(h->rhs, rhs, h->n * 8, cudaMemcpyHostToDevice, h->stream));
   SWM_CK(cudaMemcpyAsync(h->psi, psi, h->n * 8, cudaMemcpyHostToDevice, h->stream));
@@ -601,6 +607,7 @@ int swm_helm_solve_mixed(swm_helm *h, const double *rhs, double *psi, double ome
 // reaches the smallest residual.
 int swm_helm_autotune(swm_helm *h, const double *rhs, double omega_lo, double omega_hi, int ngrid,
                       int trial_sweeps, double *omega, int *block_x, int *block_y) {
+  SWM_ON_DEVICE(h ? h->device : -1);
   SWM_REQUIRE(h && rhs && ngrid >= 1 && trial_sweeps > 0 && omega_lo > 0 && omega_hi < 2 && omega_lo <= omega_hi,
               "swm_helm_autotune: bad arguments");
   SWM_CK(cudaMemcpyAsync(h->rhs, rhs, h->n * 8, cudaMemcpyHostToDevice, h->stream));

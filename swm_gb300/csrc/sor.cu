@@ -221,6 +221,7 @@ using namespace swm;
 extern "C" {
 
 int elsolv_sor_gpu_init(swm_gpu_ctx *c) {
+  SWM_ON_DEVICE(c ? c->device : -1);
   SWM_REQUIRE(c && c->stage >= 1, "elsolv_sor_gpu_init: call after swm_gpu_domain");
   sor_free(c);
   SorState *s = new SorState();
@@ -327,6 +328,7 @@ extern "C" {
 
 int elsolv_sor_gpu_solve(swm_gpu_ctx *c, const double *B, double *chi, double eps, int first_guess, int *iters,
                          double *anorm) {
+  SWM_ON_DEVICE(c ? c->device : -1);
   SWM_REQUIRE(c && c->sor && B && chi, "elsolv_sor_gpu_solve: call elsolv_sor_gpu_init first");
   SorState *s = c->sor;
   size_t n = c->n;
@@ -346,6 +348,7 @@ int elsolv_sor_gpu_solve(swm_gpu_ctx *c, const double *B, double *chi, double ep
 // the non-divergent flow still formed.
 int swm_gpu_nondivergent(swm_gpu_ctx *c, int first_guess, double eps, double *u_nd, double *v_nd, double *chi,
                          int *iters) {
+  SWM_ON_DEVICE(c ? c->device : -1);
   SWM_REQUIRE(c && c->stage >= 5 && c->sor, "swm_gpu_nondivergent: call elsolv_sor_gpu_init first");
   SorState *s = c->sor;
   const size_t n = c->n;

@@ -203,6 +203,7 @@ extern "C" {
 
 int trc_gpu_add(swm_gpu_ctx *c, double kappa_h, double cons, double gamma_c, const double *C, const double *C0,
                 const double *gfield, const double *cfield, int *id) {
+  SWM_ON_DEVICE(c ? c->device : -1);
   SWM_REQUIRE(c && c->stage >= 5, "trc_gpu_add: call after swm_gpu_initial_conditions");
   SWM_REQUIRE(c->tracers.size() < 16, "trc_gpu_add: too many tracers");
   size_t n = c->n;
@@ -241,12 +242,14 @@ int trc_gpu_add(swm_gpu_ctx *c, double kappa_h, double cons, double gamma_c, con
 }
 
 int trc_gpu_init(swm_gpu_ctx *c) {
+  SWM_ON_DEVICE(c ? c->device : -1);
   SWM_REQUIRE(c && !c->tracers.empty(), "trc_gpu_init: no tracer added");
   if (trc32_active(c)) return trc32_init(c);
   return tracer_init_coeffs(c);
 }
 
 int trc_gpu_get_field(swm_gpu_ctx *c, int t, int f, double *out) {
+  SWM_ON_DEVICE(c ? c->device : -1);
   SWM_REQUIRE(c && t >= 0 && t < (int)c->tracers.size() && out, "trc_gpu_get_field: bad arguments");
   const Tracer &T = c->tracers[t];
   if (trc32_active(c)) {

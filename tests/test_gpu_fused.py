@@ -69,13 +69,42 @@ def test_fused_fp32c_launches_one_kernel_per_step():
     assert g.launch_count() - l0 == 40
 
 
-def test_fused_rejects_mean_state():
+def _mean_state_case(nsteps):
+    """LINEARISED_MEAN_STATE about a basin-scale gyre of about 0.13 m/s (the
+    test_diaglist basic state is under 1e-6 m/s, too weak to exercise the
+    mean-state terms)."""
+    case = synthetic.double_gyre((64, 48), biharmonic=False, nsteps=nsteps)
+    ny, nx = case['config']['ny'], case['config']['nx']
+    y = np.linspace(0.0, np.pi, ny)[:, None]
+    x = np.linspace(0.0, np.pi, nx)[None, :]
+    case['psi_bs'] = 5e6 * np.sin(x) * np.sin(y) * (1.0 + 0.3 * np.sin(2.0 * x))
+    case['config'].update(mode=3, barotropic=1)
+    return case
+
+
+@pytest.mark.parametrize('path', ['plain_fp64', 'fused_fp64', 'fused_fp32c'])
+@pytest.mark.parametrize('which', ['gyre', 'test_diaglist'])
+def test_mean_state_vs_oracle(path, which):
+    """LINEARISED_MEAN_STATE (the eta flux by the basic flow with the
+    reference's ip1(j) index, vorticity times basic flow, (f + zeta_bs)/Dh,
+    u U + v V in the energy density) on every path: the plain path bit for
+    bit, the fused paths to their tolerances after 300 steps."""
     from harness import golden_case
-    from swm_gb300 import SwmGpuError
-    case, _ = golden_case('test_diaglist')
-    g = GpuModel('fused_fp64')
-    with pytest.raises(SwmGpuError):
-        run_case(case, g, nsteps=2, with_diag=False)
+    nsteps = 300
+    case = _mean_state_case(nsteps) if which == 'gyre' else golden_case('test_diaglist')[0]
+    o, g = OracleBackend(), GpuModel(path)
+    run_case(case, o, nsteps=nsteps, with_diag=False)
+    run_case(case, g, nsteps=nsteps, with_diag=False)
+    if which == 'gyre':
+        assert np.abs(o.field('u_bs')).max() > 0.05
+    for f in ('u', 'v', 'eta'):
+        a, b = g.field(f), o.field(f)
+        assert np.isfinite(a).all(), f
+        if path == 'plain_fp64':
+            assert np.array_equal(a, b), f
+        else:
+            err = rel_l2(a, b, o.ocean(f).astype(bool))
+            assert err <= TOL[path], (f, err)
 
 
 @pytest.mark.parametrize('path', ['plain_fp64', 'fused_fp64', 'fused_fp32c'])

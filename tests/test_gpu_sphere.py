@@ -79,8 +79,11 @@ def test_plain_bit_exact_on_sphere(name, guard):
 
 @pytest.mark.parametrize('path', ['fused_fp64', 'fused_fp32c'])
 @pytest.mark.parametrize('name,biharmonic', [('test_nonlinear', False), ('test_nonlinear', True),
-                                             ('test_nl_tracer', False)])
+                                             ('test_nl_tracer', False), ('test_fixed_length_output', False)])
 def test_fused_paths_on_sphere(path, name, biharmonic):
+    """test_fixed_length_output is the reference's linear state-of-rest case
+    with oscillating forcing (added to the forcing fields every step on the
+    fused paths) and a bathymetry file, 61 x 41 points on the sphere."""
     case = _case(name, biharmonic)
     guard = bool(case['tracers'])
     o = _oracle(case, guard)
