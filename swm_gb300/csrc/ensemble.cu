@@ -67,34 +67,43 @@ __global__ void k_ens_integrals(const EnsInt *__restrict__ d, double *__restrict
   if (threadIdx.x < 3) out[3 * (size_t)blockIdx.x + threadIdx.x] = red[threadIdx.x][0];
 }
 
-// monitored steps: one step's wind rows of every member (FP64, staged on the
-// device) into each member's FP32 row profile
+// monitored steps: one step's wind rows of every member (FP64: a staged copy,
+// or the caller's pinned host array read in place) into each member's FP32
+// row profile; the first thread also resets the step's queue head
 __global__ void k_ens_rows(const double *__restrict__ rows, const int *__restrict__ row_member,
-                           const int *__restrict__ row_off, float *const *__restrict__ w, int nrows) {
+                           const int *__restrict__ row_off, float *const *__restrict__ w, int nrows,
+                           int *__restrict__ queue_head) {
   const int r = blockIdx.x * blockDim.x + threadIdx.x;
-  if (r >= nrows) return;
+  if (r == 0) *queue_head = 0;
+  if (r >= nrows || !rows) return;
   const int i = row_member[r];
   w[i][r - row_off[i]] = (float)rows[r];
 }
 
-// monitored steps: the integrals of every member from its tiles' sums, added
-// in the member's tile order (tiles_of[tile_off[i] .. tile_off[i + 1]))
+// monitored steps: the integrals of every member from its tiles' sums, one
+// warp per member: lane l adds the member's tiles l, l + 32, ... (in queue
+// order), then a shuffle tree in fixed order; out may be pinned host memory
 __global__ void k_ens_tile_sums(const double *__restrict__ partial, const int *__restrict__ tile_off,
                                 const int *__restrict__ tiles_of, const double *__restrict__ G, int n,
                                 double *__restrict__ out) {
-  const int i = blockIdx.x * blockDim.x + threadIdx.x;
-  if (i >= n) return;
+  const int i = (int)((blockIdx.x * blockDim.x + threadIdx.x) >> 5), lane = threadIdx.x & 31;
+  if (i >= n) return;  // whole warps leave together
   double s[4] = {0., 0., 0., 0.};
-  for (int k = tile_off[i]; k < tile_off[i + 1]; k++) {
+  for (int k = tile_off[i] + lane; k < tile_off[i + 1]; k += 32) {
     const double *q = partial + 4 * (size_t)tiles_of[k];
     s[0] += q[0];
     s[1] += q[1];
     s[2] += q[2];
     s[3] += q[3];
   }
-  out[3 * (size_t)i] = s[0];
-  out[3 * (size_t)i + 1] = 0.5 * G[i] * s[1];
-  out[3 * (size_t)i + 2] = 0.5 * (s[2] + s[3]);
+  for (int o = 16; o > 0; o >>= 1)
+#pragma unroll
+    for (int c = 0; c < 4; c++) s[c] += __shfl_down_sync(0xffffffffu, s[c], o);
+  if (lane == 0) {
+    out[3 * (size_t)i] = s[0];
+    out[3 * (size_t)i + 1] = 0.5 * G[i] * s[1];
+    out[3 * (size_t)i + 2] = 0.5 * (s[2] + s[3]);
+  }
 }
 
 // device tables of the monitored steps, built on their first use
@@ -169,9 +178,20 @@ int rotate_members(swm_gpu_ensemble *e, int64_t itt) {
   return SWM_GPU_OK;
 }
 
-int ens_step(swm_gpu_ensemble *e, int64_t itt, const EnsInteg *mi = nullptr) {
+// the device address of host memory the GPU can read in place (pinned and
+// mapped), or null
+const void *mapped_device_pointer(const void *host) {
+  cudaPointerAttributes a;
+  if (cudaPointerGetAttributes(&a, host) != cudaSuccess) {
+    cudaGetLastError();  // clear the error of an unregistered pointer
+    return nullptr;
+  }
+  return a.type == cudaMemoryTypeHost ? a.devicePointer : nullptr;
+}
+
+int ens_step(swm_gpu_ensemble *e, int64_t itt, const EnsInteg *mi = nullptr, bool reset_head = true) {
   const size_t n = e->m.size();
-  SWM_CK(cudaMemsetAsync(e->next + e->phase, 0, sizeof(int), e->stream));
+  if (reset_head) SWM_CK(cudaMemsetAsync(e->next + e->phase, 0, sizeof(int), e->stream));
   int rc = march_ens_launch(e->mix, e->std_cfg, e->pf, e->tab + (size_t)e->phase * n, e->tiles, e->ntiles,
                             e->next + e->phase, e->stream, mi);
   if (rc != SWM_GPU_OK) return rc;
@@ -501,6 +521,9 @@ int swm_gpu_ensemble_run_monitor(swm_gpu_ensemble *e, int64_t itt0, int64_t nste
   SWM_REQUIRE(!rows || M->has_rows,
               "swm_gpu_ensemble_run_monitor: rows need a time-dependent row-profile zonal wind stress in every member");
   const size_t n = e->m.size();
+  // pinned (host-mapped) arrays are read and written in place by the kernels
+  const double *rows_dev = rows ? static_cast<const double *>(mapped_device_pointer(rows)) : nullptr;
+  double *out_dev = static_cast<double *>(const_cast<void *>(mapped_device_pointer(out)));
   bool joined = false;
   for (int64_t s = 0; s < nsteps; s++) {
     const int64_t itt = itt0 + s + 1;
@@ -526,19 +549,27 @@ int swm_gpu_ensemble_run_monitor(swm_gpu_ensemble *e, int64_t itt0, int64_t nste
       if (rc != SWM_GPU_OK) return rc;
       joined = true;
     }
+    const double *rd = nullptr;  // the rows as the device reads them
     if (rs) {
-      double *d = M->rows[s & 1];
-      SWM_CK(cudaMemcpyAsync(d, rs, M->nrows * sizeof(double), cudaMemcpyHostToDevice, e->stream));
-      k_ens_rows<<<(M->nrows + 255) / 256, 256, 0, e->stream>>>(d, M->row_member, M->d_row_off, M->w, M->nrows);
-      e->launches++;
+      if (rows_dev) {
+        rd = rows_dev + (size_t)s * M->nrows;
+      } else {
+        double *d = M->rows[s & 1];
+        SWM_CK(cudaMemcpyAsync(d, rs, M->nrows * sizeof(double), cudaMemcpyHostToDevice, e->stream));
+        rd = d;
+      }
     }
-    const EnsInteg mi{M->areas, M->partial};
-    rc = ens_step(e, itt, &mi);
-    if (rc != SWM_GPU_OK) return rc;
-    k_ens_tile_sums<<<(unsigned)((n + 127) / 128), 128, 0, e->stream>>>(M->partial, M->tile_off, M->tiles_of, M->G,
-                                                                      (int)n, M->res);
+    k_ens_rows<<<rd ? (M->nrows + 255) / 256 : 1, 256, 0, e->stream>>>(rd, M->row_member, M->d_row_off, M->w,
+                                                                     M->nrows, e->next + e->phase);
     e->launches++;
-    SWM_CK(cudaMemcpyAsync(os, M->res, 3 * n * sizeof(double), cudaMemcpyDeviceToHost, e->stream));
+    const EnsInteg mi{M->areas, M->partial};
+    rc = ens_step(e, itt, &mi, false);
+    if (rc != SWM_GPU_OK) return rc;
+    double *od = out_dev ? out_dev + 3 * n * (size_t)s : M->res;
+    k_ens_tile_sums<<<(unsigned)((32 * n + 127) / 128), 128, 0, e->stream>>>(M->partial, M->tile_off, M->tiles_of,
+                                                                           M->G, (int)n, od);
+    e->launches++;
+    if (!out_dev) SWM_CK(cudaMemcpyAsync(os, M->res, 3 * n * sizeof(double), cudaMemcpyDeviceToHost, e->stream));
   }
   if (joined) {
     rc = release_members(e);
