@@ -809,7 +809,9 @@ def sor_measurement(args, cells=2048, eps=1e-4):
             'gpu_launches': launches,
             'roofline': {'bound': 'hbm', 'achieved': ach, 'peak': peak, 'unit': 'GB/s', 'frac': ach / peak,
                          'peak_kind': kind, 'bytes_per_point_iteration': 72,
-                         'note': 'one iteration = a red and a black half-sweep over all points'}}
+                         'note': 'one iteration = a red and a black half-sweep over all points; the half-sweep '
+                                 'is bound by the FP64 pipe (83 % busy in ncu), which the FP64 division of the '
+                                 "reference's update requires"}}
 
 
 def main():
