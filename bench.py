@@ -769,8 +769,8 @@ def sor_measurement(args, cells=2048, eps=1e-4):
     computeVelocityPotential passes one.  A call after the first (first_guess
     false, as every call but the first from the diagnostics) is capped by the
     reference at max_count = 10 max(Nx, Ny) iterations; from chi = 0 it may
-    end there unconverged, which is reported.  Roofline: 9 words per point and iteration (chi read
-    and written, B, the five coefficients)."""
+    end there unconverged, which is reported.  Roofline: 10 words per point and iteration (chi read
+    and written, B, the five coefficients, the reciprocal diagonal)."""
     import torch
     from swm_gb300.host import synthetic
     from swm_gb300.host.driver import Driver
@@ -801,17 +801,17 @@ def sor_measurement(args, cells=2048, eps=1e-4):
     it = abs(iters)
     pts = nx * ny
     peak, kind = peaks()
-    ach = 9 * 8 * pts * it / dev / 1e9
+    ach = 10 * 8 * pts * it / dev / 1e9
     g.close()
     return {'workload': 'elsolv_sor_%dx%d' % (cells, cells), 'points': pts, 'eps': eps,
             'iterations': it, 'converged': iters > 0, 'anorm': anorm, 'max_count': 10 * max(nx, ny),
             'time_s': wall, 'device_s': dev, 'ms_per_iteration': dev / max(it, 1) * 1e3,
             'gpu_launches': launches,
             'roofline': {'bound': 'hbm', 'achieved': ach, 'peak': peak, 'unit': 'GB/s', 'frac': ach / peak,
-                         'peak_kind': kind, 'bytes_per_point_iteration': 72,
+                         'peak_kind': kind, 'bytes_per_point_iteration': 80,
                          'note': 'one iteration = a red and a black half-sweep over all points; the half-sweep '
-                                 'is bound by the FP64 pipe (83 % busy in ncu), which the FP64 division of the '
-                                 "reference's update requires"}}
+                                 "is bound by GB300's FP64 pipe: the reference's update is FP64 arithmetic, "
+                                 'its division formed from the reciprocal diagonal by Markstein corrections'}}
 
 
 def main():

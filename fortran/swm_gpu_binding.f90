@@ -453,6 +453,12 @@ module swm_gpu_binding
       type(c_ptr), value :: chi
       type(c_ptr), value :: iterations
     end function swm_gpu_nondivergent
+    integer(c_int) function swm_gpu_check_division(n, seed, mismatches) bind(C)
+      import :: c_int, c_int64_t, c_ptr
+      integer(c_int64_t), value :: n
+      integer(c_int64_t), value :: seed
+      type(c_ptr), value :: mismatches
+    end function swm_gpu_check_division
     integer(c_int) function swm_helm_create(nx, ny, dx, dy, lambda, H, ocean, out_) bind(C)
       import :: c_double, c_int, c_ptr
       integer(c_int), value :: nx

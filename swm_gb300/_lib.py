@@ -77,6 +77,7 @@ def _sigs():
         'swm_gpu_nondivergent': (I, [P, I, D, P, P, P, C.POINTER(C.c_int)]),
         'elsolv_sor_gpu_init': (I, [P]),
         'elsolv_sor_gpu_solve': (I, [P, P, P, D, I, C.POINTER(C.c_int), C.POINTER(C.c_double)]),
+        'swm_gpu_check_division': (I, [I64, I64, C.POINTER(C.c_int64)]),
     }
 
 

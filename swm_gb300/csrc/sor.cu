@@ -7,16 +7,23 @@
 // sqrt(sum res^2) drops below eps (:213-218), max_count = 1000 max(Nx, Ny)
 // on a first call and 10 max(Nx, Ny) after it (:166-176).
 //
-// Layout: the coefficients, the right-hand side and chi are kept split by
-// colour, row by row: cell (i, j) of colour (i + j) % 2 sits at j * W + i / 2
-// of its colour's arrays (W = ceil(Nx / 2)).  A half-sweep then reads only
-// its own colour's coefficients, right-hand side and chi (and the other
-// colour's chi as neighbours): 9 words per point and iteration, one thread
-// per cell of the colour, coalesced.  Each cell's update is the reference's
-// expression in the reference's order (this file is compiled without FMA
-// contraction), so chi is bit for bit the restatement's when the iteration
-// counts agree; within a colour no cell reads another of its own colour
-// (the periodic wrap only pairs land cells, which stay fixed).
+// Layout: the coefficients, the right-hand side, chi and the ocean mask are
+// kept split by colour, row by row: cell (i, j) of colour (i + j) % 2 sits at
+// j * W + i / 2 of its colour's arrays (W = ceil(Nx / 2)).  A half-sweep then
+// reads only its own colour's coefficients, right-hand side, reciprocal
+// diagonal and chi (and the other colour's chi as neighbours): 10 words per
+// point and iteration, SOR_CELLS consecutive cells of the colour per thread,
+// coalesced.  Each cell's update is the reference's expression in the
+// reference's order (this file is compiled without FMA contraction), so chi
+// is bit for bit the restatement's when the iteration counts agree; within a
+// colour no cell reads another of its own colour (the periodic wrap only
+// pairs land cells, which stay fixed).
+//
+// Division: GB300's FP64 rate is low and the half-sweep is bound by it, so
+// the update's division by the diagonal coefficient is formed from that
+// coefficient's reciprocal, set up once, by Markstein's correction
+// (div_rn below): the same correctly rounded quotient with five FP64
+// operations.
 //
 // Control: the relaxation factor, the iteration counter and the stop flag
 // live on the device.  Each half-sweep kernel sums res^2 per warp with
@@ -48,6 +55,10 @@ struct SorState {
   double *c[5] = {};       // ElSolvSOR_c(:,:,1..5), natural layout (set-up only)
   double *chi = nullptr, *B = nullptr;   // natural layout
   double *cs[2][5] = {};   // coefficients split by colour
+  double *rc4[2] = {};     // 1 / ElSolvSOR_c(:,:,5), split by colour
+  uint8_t *ms[2] = {};     // ocean mask split by colour (0 also on the padding of odd rows)
+  int *bad = nullptr;      // set-up: 1 when an ocean cell's diagonal is outside div_rn's range
+  bool fast = true;        // every ocean diagonal inside div_rn's range
   double *Bs[2] = {}, *chis[2] = {};     // right-hand side and chi split by colour
   double *partial = nullptr;   // per-block sums of res^2 of a half-sweep
   SorCtl *ctl = nullptr;
@@ -57,6 +68,7 @@ struct SorState {
 };
 
 constexpr int SOR_THREADS = 256;
+constexpr int SOR_CELLS = 4;  // consecutive cells of the colour per thread (one 32-bit word of mask bytes)
 constexpr int SOR_BATCH = 32;  // iterations per graph replay (one host read of the flag)
 
 namespace swm {
@@ -90,31 +102,81 @@ __global__ void k_sor_split(double *nat, double *s0, double *s1, int nx, int ny,
   else sp[q] = nat[k];
 }
 
+// a / b rounded to nearest from y = 1/b rounded to nearest, by Markstein's
+// theorem (P. Markstein, "Computation of elementary functions on the IBM
+// RISC System/6000 processor", IBM J. Res. Dev. 34, 1990; also Muller et
+// al., Handbook of Floating-Point Arithmetic, the FMA-based division
+// section): if y is within half an ulp of 1/b and q within one ulp of a/b,
+// then q + (a - b q) y, each operation rounded to nearest and the remainder
+// taken with one FMA, is a/b rounded to nearest.  q = a y can be up to 1.5
+// ulp off, so a first correction brings it within an ulp and the second
+// gives the rounded quotient.  Valid while no step underflows or overflows:
+// for a and b with binary exponents in [-500, 500] (div_rn_range).
+__device__ __forceinline__ double div_rn(double a, double b, double y) {
+  double q = __dmul_rn(a, y);
+  double r = __fma_rn(-q, b, a);
+  q = __fma_rn(r, y, q);
+  r = __fma_rn(-q, b, a);
+  return __fma_rn(r, y, q);
+}
+
+// x is finite, nonzero, normal and of binary exponent in [-500, 500]
+__device__ __forceinline__ bool div_rn_range(double x) {
+  const unsigned e = ((unsigned)__double2hiint(x) >> 20) & 0x7ffu;
+  return e - 523u <= 1000u;
+}
+
+// set-up: the reciprocal diagonal and the split ocean mask of colour col;
+// *bad = 1 when an ocean cell's diagonal is outside div_rn's range
+__global__ void k_sor_recip(const int8_t *__restrict__ ocean, const double *__restrict__ c4, double *__restrict__ rc4,
+                            uint8_t *__restrict__ ms, int nx, int ny, int W, int col, int *bad) {
+  const size_t q = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (q >= (size_t)W * ny) return;
+  const int j = (int)(q / W), i = 2 * (int)(q % W) + ((col + j) & 1);
+  const bool o = i < nx && ocean[i + (size_t)nx * j] != 0;
+  ms[q] = o;
+  rc4[q] = 1. / c4[q];
+  if (o && !div_rn_range(c4[q])) atomicOr(bad, 1);
+}
+
 // One half-sweep of colour col (0: (i+j) even in 0-based indices, the
-// reference's colour 1) over the colour-split arrays; then the block sums of
-// res^2 and, in the last block, the iteration's bookkeeping.
-__global__ void __launch_bounds__(SOR_THREADS) k_sor_half(const int8_t *__restrict__ ocean, SorState s, int nx,
-                                                          int ny, int col, double rJ) {
+// reference's colour 1) over the colour-split arrays, SOR_CELLS cells per
+// thread; then the block sums of res^2 and, in the last block, the
+// iteration's bookkeeping.  FAST: the division by div_rn (every ocean
+// diagonal in its range; a numerator outside it still divides).
+template <bool FAST>
+__global__ void __launch_bounds__(SOR_THREADS) k_sor_half(SorState s, int nx, int ny, int col, double rJ) {
   SorCtl *ctl = s.ctl;
   if (ctl->done || ctl->l > ctl->max_count) return;  // converged, or max_count reached
   const double relax = ctl->relax;
   const int W = s.W;
-  const size_t q = (size_t)blockIdx.x * SOR_THREADS + threadIdx.x;
+  const size_t ns = (size_t)W * ny;
+  const size_t q0 = ((size_t)blockIdx.x * SOR_THREADS + threadIdx.x) * SOR_CELLS;
+  const double *const *cs = s.cs[col];
+  double *x = s.chis[col];
   double r2 = 0.;
-  if (q < (size_t)W * ny) {
-    const int j = (int)(q / W), t = (int)(q % W);
-    const int i = 2 * t + ((col + j) & 1);
-    if (i < nx && ocean[i + (size_t)nx * j] != 0) {
+  if (q0 < ns) {
+    uint32_t m4 = 0;  // the cells' mask bytes
+    if (q0 + SOR_CELLS <= ns) {
+      m4 = *reinterpret_cast<const uint32_t *>(s.ms[col] + q0);
+    } else {
+      for (int k = 0; k < SOR_CELLS && q0 + k < ns; k++) m4 |= (uint32_t)s.ms[col][q0 + k] << (8 * k);
+    }
+#pragma unroll
+    for (int k = 0; k < SOR_CELLS; k++) {
+      if (!((m4 >> (8 * k)) & 0xffu)) continue;
+      const size_t q = q0 + k;
+      const int j = (int)(q / W), i = 2 * (int)(q - (size_t)j * W) + ((col + j) & 1);
       const int ip = i + 1 == nx ? 0 : i + 1, im = i == 0 ? nx - 1 : i - 1;
       const int jp = j + 1 == ny ? 0 : j + 1, jm = j == 0 ? ny - 1 : j - 1;
       // neighbours are of the other colour except across an odd periodic wrap
       auto at = [&](int a, int b) { return s.chis[(a + b) & 1][(size_t)b * W + (a >> 1)]; };
-      double *x = s.chis[col];
-      const double res = relax * (s.cs[col][0][q] * at(ip, j) + s.cs[col][1][q] * at(im, j) +
-                                  s.cs[col][2][q] * at(i, jp) + s.cs[col][3][q] * at(i, jm) +
-                                  s.cs[col][4][q] * x[q] - s.Bs[col][q]) / s.cs[col][4][q];
+      const double c4 = cs[4][q];
+      const double num = relax * (cs[0][q] * at(ip, j) + cs[1][q] * at(im, j) + cs[2][q] * at(i, jp) +
+                                  cs[3][q] * at(i, jm) + c4 * x[q] - s.Bs[col][q]);
+      const double res = FAST && div_rn_range(num) ? div_rn(num, c4, s.rc4[col][q]) : num / c4;
       x[q] = x[q] - res;
-      r2 = res * res;
+      r2 = r2 + res * res;
     }
   }
   // block sum: shuffles within warps, then the warps in order
@@ -198,6 +260,42 @@ __global__ void k_sor_nondiv(Dev d, const double *chi, const double *u, const do
   v_nd[k] = v[k] - vc;
 }
 
+// the pair of k_div_check's sample k: splitmix64 bits; one pair in four
+// takes a special significand (all ones, all zeros, or one of them with the
+// lowest bits flipped) for a, b or both
+__device__ uint64_t mix64(uint64_t z) {
+  z += 0x9e3779b97f4a7c15ull;
+  z = (z ^ (z >> 30)) * 0xbf58476d1ce4e5b9ull;
+  z = (z ^ (z >> 27)) * 0x94d049bb133111ebull;
+  return z ^ (z >> 31);
+}
+
+__device__ double sample_operand(uint64_t r, uint64_t r2, bool special) {
+  uint64_t man = r & 0xfffffffffffffull;
+  if (special) {
+    const uint64_t pat[4] = {0xfffffffffffffull, 0ull, 0xffffffffffff0ull ^ (r2 & 15), r2 & 15};
+    man = pat[(r2 >> 8) & 3];
+  }
+  const uint64_t e = 523 + (r2 >> 16) % 1001;  // binary exponent -500 .. 500
+  const uint64_t sign = (r2 >> 40) & 1;
+  return __longlong_as_double((long long)((sign << 63) | (e << 52) | man));
+}
+
+__global__ void k_div_check(int64_t n, uint64_t seed, unsigned long long *bad) {
+  unsigned long long mism = 0;
+  for (int64_t k = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; k < n; k += (int64_t)gridDim.x * blockDim.x) {
+    const uint64_t h = mix64(seed ^ mix64((uint64_t)k));
+    const uint64_t r[4] = {mix64(h + 1), mix64(h + 2), mix64(h + 3), mix64(h + 4)};
+    const int sp = (int)(h & 15);  // 0, 1, 2: special a, b, both
+    const double a = sample_operand(r[0], r[1], sp == 0 || sp == 2);
+    const double b = sample_operand(r[2], r[3], sp == 1 || sp == 2);
+    const double q = __ddiv_rn(a, b), y = __ddiv_rn(1., b);
+    mism += __double_as_longlong(div_rn(a, b, y)) != __double_as_longlong(q);
+  }
+  for (int o = 16; o > 0; o >>= 1) mism += __shfl_down_sync(0xffffffffu, mism, o);
+  if ((threadIdx.x & 31) == 0 && mism) atomicAdd(bad, mism);
+}
+
 void sor_free(swm_gpu_ctx *c) {
   if (!c->sor) return;
   SorState *s = c->sor;
@@ -207,7 +305,10 @@ void sor_free(swm_gpu_ctx *c) {
     for (int q = 0; q < 5; q++) cudaFree(s->cs[col][q]);
     cudaFree(s->Bs[col]);
     cudaFree(s->chis[col]);
+    cudaFree(s->rc4[col]);
+    cudaFree(s->ms[col]);
   }
+  cudaFree(s->bad);
   cudaFree(s->chi); cudaFree(s->B); cudaFree(s->partial); cudaFree(s->ctl);
   cudaFree(s->und); cudaFree(s->vnd);
   delete s;
@@ -229,13 +330,17 @@ int elsolv_sor_gpu_init(swm_gpu_ctx *c) {
   const size_t n = c->n;
   s->W = (c->nx + 1) / 2;
   const size_t ns = (size_t)s->W * c->ny;
-  s->nblocks = (int)((ns + SOR_THREADS - 1) / SOR_THREADS);
+  s->nblocks = (int)((ns + (size_t)SOR_THREADS * SOR_CELLS - 1) / ((size_t)SOR_THREADS * SOR_CELLS));
   for (int q = 0; q < 5; q++) SWM_CK(cudaMalloc((void **)&s->c[q], n * 8));
   for (int col = 0; col < 2; col++) {
     for (int q = 0; q < 5; q++) SWM_CK(cudaMalloc((void **)&s->cs[col][q], ns * 8));
     SWM_CK(cudaMalloc((void **)&s->Bs[col], ns * 8));
     SWM_CK(cudaMalloc((void **)&s->chis[col], ns * 8));
+    SWM_CK(cudaMalloc((void **)&s->rc4[col], ns * 8));
+    SWM_CK(cudaMalloc((void **)&s->ms[col], ns + SOR_CELLS));
   }
+  SWM_CK(cudaMalloc((void **)&s->bad, sizeof(int)));
+  SWM_CK(cudaMemsetAsync(s->bad, 0, sizeof(int), c->stream));
   SWM_CK(cudaMalloc((void **)&s->chi, n * 8));
   SWM_CK(cudaMalloc((void **)&s->B, n * 8));
   SWM_CK(cudaMalloc((void **)&s->partial, (size_t)s->nblocks * 8));
@@ -247,9 +352,16 @@ int elsolv_sor_gpu_init(swm_gpu_ctx *c) {
   const unsigned nb = (unsigned)((n + 255) / 256);
   for (int q = 0; q < 5; q++)
     k_sor_split<<<nb, 256, 0, c->stream>>>(s->c[q], s->cs[0][q], s->cs[1][q], c->nx, c->ny, s->W, 0);
-  c->launches += 6;
+  const unsigned nbs = (unsigned)((ns + 255) / 256);
+  for (int col = 0; col < 2; col++)
+    k_sor_recip<<<nbs, 256, 0, c->stream>>>(c->d_ocean[GE], s->cs[col][4], s->rc4[col], s->ms[col], c->nx, c->ny,
+                                            s->W, col, s->bad);
+  c->launches += 8;
   SWM_CK(cudaGetLastError());
+  int bad = 0;
+  SWM_CK(cudaMemcpyAsync(&bad, s->bad, sizeof(int), cudaMemcpyDeviceToHost, c->stream));
   SWM_CK(cudaStreamSynchronize(c->stream));
+  s->fast = bad == 0;
   return SWM_GPU_OK;
 }
 
@@ -260,8 +372,10 @@ namespace {
 // the two half-sweeps of one iteration
 void sor_iteration(swm_gpu_ctx *c, SorState *s) {
   const double rJ = (double)(float)9.9999178e-1;  // default-real literal (ElSolv_SOR.f90:175)
-  for (int col = 0; col < 2; col++)
-    k_sor_half<<<s->nblocks, SOR_THREADS, 0, c->stream>>>(c->d_ocean[GE], *s, c->nx, c->ny, col, rJ);
+  for (int col = 0; col < 2; col++) {
+    if (s->fast) k_sor_half<true><<<s->nblocks, SOR_THREADS, 0, c->stream>>>(*s, c->nx, c->ny, col, rJ);
+    else k_sor_half<false><<<s->nblocks, SOR_THREADS, 0, c->stream>>>(*s, c->nx, c->ny, col, rJ);
+  }
 }
 
 // SOR_BATCH iterations as one graph, captured once per set-up (the kernels
@@ -338,6 +452,26 @@ int elsolv_sor_gpu_solve(swm_gpu_ctx *c, const double *B, double *chi, double ep
   SWM_CK(cudaMemcpyAsync(chi, s->chi, n * 8, cudaMemcpyDeviceToHost, c->stream));
   SWM_CK(cudaStreamSynchronize(c->stream));
   return rc;
+}
+
+int swm_gpu_check_division(int64_t n, int64_t seed, int64_t *mismatches) {
+  SWM_REQUIRE(n >= 0 && mismatches, "swm_gpu_check_division: bad arguments");
+  unsigned long long *d = nullptr;
+  SWM_CK(cudaMalloc((void **)&d, sizeof(*d)));
+  cudaError_t e = cudaMemset(d, 0, sizeof(*d));
+  if (e == cudaSuccess) {
+    k_div_check<<<4 * 152, 256>>>(n, (uint64_t)seed, d);
+    e = cudaGetLastError();
+  }
+  unsigned long long h = 0;
+  if (e == cudaSuccess) e = cudaMemcpy(&h, d, sizeof(h), cudaMemcpyDeviceToHost);
+  cudaFree(d);
+  if (e != cudaSuccess) {
+    set_error(std::string("swm_gpu_check_division: ") + cudaGetErrorString(e));
+    return SWM_GPU_ECUDA;
+  }
+  *mismatches = (int64_t)h;
+  return SWM_GPU_OK;
 }
 
 // computeNonDivergentFlowField (calc_lib.f90:548-590) of the model's current

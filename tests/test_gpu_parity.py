@@ -87,8 +87,10 @@ def test_tracer_bit_exact(nan_guard):
         assert np.isfinite(g.tracer_field(0, 'CH')).all()
 
 
-def test_sor_matches_oracle():
-    case = synthetic.double_gyre((40, 32), biharmonic=False, nsteps=10)
+@pytest.mark.parametrize('shape', [(40, 32), (41, 33)])
+def test_sor_matches_oracle(shape):
+    """Odd Nx pads one colour's rows in the colour-split layout."""
+    case = synthetic.double_gyre(shape, biharmonic=False, nsteps=10)
     o, g = _pair(case, 10)
     o.sor_init()
     g.sor_init()
@@ -109,6 +111,20 @@ def test_sor_matches_oracle():
     # a non-converging call (max_count = 10*max(Nx,Ny)) reports it
     xg2, ig2, _ = g.sor_solve(B, chi0, 1e-40, False)
     assert ig2 < 0
+
+
+def test_sor_division_is_correctly_rounded():
+    """The half-sweep divides by the diagonal through its reciprocal and two
+    Markstein corrections; on 2^26 pairs over the exponent range it serves
+    (all-ones and power-of-two significands among them) the quotient equals
+    the division operator's in every bit."""
+    from swm_gb300 import _lib
+    import ctypes
+    lib = _lib.lib()
+    for seed in (1, 2):
+        bad = ctypes.c_int64(-1)
+        assert lib.swm_gpu_check_division(1 << 26, seed, ctypes.byref(bad)) == 0
+        assert bad.value == 0
 
 
 def test_nondivergent_flow_matches_oracle():
