@@ -760,11 +760,11 @@ def reference(args, rank, ws):
             'e2e': {'value': v, 'unit': 'cell-steps/s', 'h2d_bytes_per_step': 0, 'd2h_bytes_per_step': 0}}
 
 
-def sor_measurement(args, cells=2048, eps=1e-4):
+def sor_measurement(args, cells=4096, eps=1e-4):
     """The reference's own solver (main_ElSolv_SOR: masked spherical
     Laplacian, fixed Chebyshev relaxation schedule, absolute stop on the
-    correction norm, eps = 1e-4 as calc_lib.h) on the 2048^2 basin (chi, B
-    and the five coefficients, 270 MB, exceed L2).  The right-hand side is a
+    correction norm, eps = 1e-4 as calc_lib.h) on the 4096^2 basin (chi, B,
+    the five coefficients and the reciprocal diagonal, 1.3 GB, exceed L2).  The right-hand side is a
     smooth random field of the size of a flow divergence (1e-9 /s), as
     computeVelocityPotential passes one.  A call after the first (first_guess
     false, as every call but the first from the diagnostics) is capped by the
@@ -825,7 +825,7 @@ def main():
         elif args.workload == 'helmholtz':
             out = helmholtz_measurement(args, cells=args.cells if args.cells != 1024 else 4096)
         elif args.workload == 'sor':
-            out = sor_measurement(args, cells=args.cells if args.cells != 1024 else 2048)
+            out = sor_measurement(args, cells=args.cells if args.cells != 1024 else 4096)
         else:
             out = linear_rg_measurement(args)
         print(json.dumps(out))

@@ -1274,9 +1274,10 @@ int orc_helmholtz_sor(int nx, int ny, const double *cx, const double *cy, const 
           double w = i > 0 ? psi[k - 1] : 0., e = i < nx - 1 ? psi[k + 1] : 0.;
           double s = j > 0 ? psi[k - nx] : 0., nn = j < ny - 1 ? psi[k + nx] : 0.;
           double ce = i < nx - 1 ? cx[k + 1] : 0., cn = j < ny - 1 ? cy[k + nx] : 0.;
-          double off = cx[k] * w + ce * e + cy[k] * s + cn * nn;
+          /* explicit fused multiply-adds (C99 fma, correctly rounded) */
+          double off = fma(cx[k], w, fma(ce, e, fma(cy[k], s, cn * nn)));
           double gs = (rhs[k] - off) * rcc[k];
-          psi[k] = psi[k] + omega * (gs - psi[k]);
+          psi[k] = fma(omega, gs - psi[k], psi[k]);
         }
     sweeps++;
     if (sweeps % 16 == 0 || sweeps == max_sweeps) {

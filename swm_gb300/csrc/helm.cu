@@ -10,7 +10,8 @@
 // ||rhs - A psi||_2 / ||rhs||_2, checked every CHECK sweeps in FP64.
 //
 // Two solvers: FP64 sweeps (bit for bit with the FP64 restatement, this file
-// is compiled without FMA contraction), and mixed precision: FP32 sweeps on
+// is compiled without FMA contraction and the update's fused multiply-adds
+// are explicit in both), and mixed precision: FP32 sweeps on
 // the correction equation A e = r, with r = rhs - A psi formed in FP64 and
 // psi += e accumulated in FP64 (iterative refinement).  An autotuner picks
 // the relaxation factor in a given range from short trial solves and the
@@ -59,20 +60,58 @@ __global__ void k_h_coeff64(int nx, int ny, const double *__restrict__ h, double
   rcc[k] = 1. / (-(((cxw + cxe) + cys) + cyn) - lambda);
 }
 
-__global__ void k_h_sweep64(int nx, int ny, const double *__restrict__ cx, const double *__restrict__ cy,
-                            const double *__restrict__ rcc, const int8_t *__restrict__ mask,
-                            const double *__restrict__ rhs, double *psi, double omega, int colour) {
-  const int j = blockIdx.y * blockDim.y + threadIdx.y;
-  const int i = 2 * (blockIdx.x * blockDim.x + threadIdx.x) + ((j + colour) & 1);
-  if (i >= nx || j >= ny) return;
-  const size_t k = (size_t)i + (size_t)nx * j;
-  if (!mask[k]) return;
-  const double cxe = i < nx - 1 ? cx[k + 1] : 0., cyn = j < ny - 1 ? cy[k + nx] : 0.;
-  const double w = i > 0 ? psi[k - 1] : 0., e = i < nx - 1 ? psi[k + 1] : 0.;
-  const double s = j > 0 ? psi[k - nx] : 0., n = j < ny - 1 ? psi[k + nx] : 0.;
-  const double off = cx[k] * w + cxe * e + cy[k] * s + cyn * n;
-  const double gs = (rhs[k] - off) * rcc[k];
-  psi[k] = psi[k] + omega * (gs - psi[k]);
+// FP64 sweeps run on a colour-split layout: cell (i, j) of colour (i + j) % 2
+// sits at j * W + i / 2 of its colour's arrays (W = ceil(nx / 2)) with its
+// four face coefficients (0 at the frame), reciprocal diagonal, rhs and mask,
+// so a colour pass reads only its own colour's arrays and the other
+// colour's psi, contiguous, one thread per cell of the colour
+struct Split64 {
+  double *c[2][4];  // west, east, south, north face coefficients
+  double *rcc[2], *rhs[2], *psi[2];
+  uint8_t *mask[2];  // 0 also on the padding of rows with fewer cells
+};
+
+__global__ void k_h_split_coeff64(int nx, int ny, int W, const double *__restrict__ cx, const double *__restrict__ cy,
+                                  const double *__restrict__ rcc, const int8_t *__restrict__ mask, Split64 s) {
+  const size_t k = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (k >= (size_t)nx * ny) return;
+  const int i = (int)(k % nx), j = (int)(k / nx), col = (i + j) & 1;
+  const size_t q = (size_t)j * W + (i >> 1);
+  s.c[col][0][q] = cx[k];
+  s.c[col][1][q] = i < nx - 1 ? cx[k + 1] : 0.;
+  s.c[col][2][q] = cy[k];
+  s.c[col][3][q] = j < ny - 1 ? cy[k + nx] : 0.;
+  s.rcc[col][q] = rcc[k];
+  s.mask[col][q] = mask[k] != 0;
+}
+
+// natural <-> colour-split copy of one field (join 0: natural -> split)
+__global__ void k_h_split64(int nx, int ny, int W, double *nat, double *s0, double *s1, int join) {
+  const size_t k = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (k >= (size_t)nx * ny) return;
+  const int i = (int)(k % nx), j = (int)(k / nx);
+  double *sp = ((i + j) & 1) ? s1 : s0;
+  const size_t q = (size_t)j * W + (i >> 1);
+  if (join) nat[k] = sp[q];
+  else sp[q] = nat[k];
+}
+
+// one colour of an FP64 sweep: off = cw w + ce e + cs s + cn n as nested
+// fused multiply-adds, psi += omega ((rhs - off) / diag - psi) as one more
+// (the arithmetic of orc_helmholtz_sor)
+__global__ void k_h_sweep64(int nx, int ny, int W, Split64 s, int col, double omega) {
+  const size_t q = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (q >= (size_t)W * ny || !s.mask[col][q]) return;
+  const int j = (int)(q / W), i = 2 * (int)(q - (size_t)j * W) + ((j + col) & 1);
+  const double *P = s.psi[col ^ 1];
+  const size_t r0 = (size_t)j * W;
+  const double w = i > 0 ? P[r0 + ((i - 1) >> 1)] : 0., e = i < nx - 1 ? P[r0 + ((i + 1) >> 1)] : 0.;
+  const double so = j > 0 ? P[r0 - W + (i >> 1)] : 0., n = j < ny - 1 ? P[r0 + W + (i >> 1)] : 0.;
+  const double off =
+      __fma_rn(s.c[col][0][q], w, __fma_rn(s.c[col][1][q], e, __fma_rn(s.c[col][2][q], so, s.c[col][3][q] * n)));
+  const double gs = (s.rhs[col][q] - off) * s.rcc[col][q];
+  double *x = s.psi[col];
+  x[q] = __fma_rn(omega, gs - x[q], x[q]);
 }
 
 // one colour of an FP32 sweep over the whole grid (the arithmetic of k_h_tbr)
@@ -323,6 +362,9 @@ __global__ void k_h_axpy(double *psi, const float *e32, size_t n, double scale) 
 struct swm_helm {
   int device = -1;  // the CUDA device the solver was created on
   double *cx = nullptr, *cy = nullptr, *rcc = nullptr;  // FP64 coefficients
+  swm::Split64 s64 = {};  // the FP64 sweeps' colour-split arrays (first FP64 solve)
+  bool has_s64 = false;
+  int W = 0;              // cells of a colour-split row
   int nx = 0, ny = 0;
   size_t n = 0;
   double dx = 0, dy = 0, lambda = 0;
@@ -349,11 +391,40 @@ dim3 sweep_grid(const swm_helm *h, dim3 b) {
   return dim3((unsigned)(((h->nx + 1) / 2 + b.x - 1) / b.x), (unsigned)((h->ny + b.y - 1) / b.y));
 }
 
-void sweep64(swm_helm *h, double omega, dim3 b) {
-  const dim3 g = sweep_grid(h, b);
+void sweep64(swm_helm *h, double omega) {
+  const unsigned g = (unsigned)(((size_t)h->W * h->ny + 255) / 256);
   for (int colour = 0; colour < 2; colour++)
-    k_h_sweep64<<<g, b, 0, h->stream>>>(h->nx, h->ny, h->cx, h->cy, h->rcc, h->mask, h->rhs, h->psi, omega, colour);
+    k_h_sweep64<<<g, 256, 0, h->stream>>>(h->nx, h->ny, h->W, h->s64, colour, omega);
   h->launches += 2;
+}
+
+// the colour-split arrays of the FP64 sweeps, set up at the first FP64 solve
+int split64_setup(swm_helm *h) {
+  if (h->has_s64) return SWM_GPU_OK;
+  h->W = (h->nx + 1) / 2;
+  const size_t ns = (size_t)h->W * h->ny;
+  Split64 &s = h->s64;
+  for (int col = 0; col < 2; col++) {
+    for (int f = 0; f < 4; f++) SWM_CK(cudaMalloc((void **)&s.c[col][f], ns * 8));
+    SWM_CK(cudaMalloc((void **)&s.rcc[col], ns * 8));
+    SWM_CK(cudaMalloc((void **)&s.rhs[col], ns * 8));
+    SWM_CK(cudaMalloc((void **)&s.psi[col], ns * 8));
+    SWM_CK(cudaMalloc((void **)&s.mask[col], ns));
+    SWM_CK(cudaMemsetAsync(s.mask[col], 0, ns, h->stream));
+  }
+  h->has_s64 = true;
+  const unsigned nb = (unsigned)((h->n + 255) / 256);
+  k_h_split_coeff64<<<nb, 256, 0, h->stream>>>(h->nx, h->ny, h->W, h->cx, h->cy, h->rcc, h->mask, s);
+  h->launches++;
+  SWM_CK(cudaGetLastError());
+  return SWM_GPU_OK;
+}
+
+// one field between the natural layout and the FP64 sweeps' split layout
+void split64_field(swm_helm *h, double *nat, double *const *sp, int join) {
+  const unsigned nb = (unsigned)((h->n + 255) / 256);
+  k_h_split64<<<nb, 256, 0, h->stream>>>(h->nx, h->ny, h->W, nat, sp[0], sp[1], join);
+  h->launches++;
 }
 
 void sweep32(swm_helm *h, float omega, dim3 b) {
@@ -454,6 +525,10 @@ void helm_free(swm_helm *h) {
   cudaFreeHost(h->host);
   cudaFree(h->hinv32); cudaFree(h->e32); cudaFree(h->r32); cudaFree(h->mask); cudaFree(h->e32b);
   cudaFree(h->cx); cudaFree(h->cy); cudaFree(h->rcc);
+  for (int col = 0; col < 2; col++) {
+    for (int f = 0; f < 4; f++) cudaFree(h->s64.c[col][f]);
+    cudaFree(h->s64.rcc[col]); cudaFree(h->s64.rhs[col]); cudaFree(h->s64.psi[col]); cudaFree(h->s64.mask[col]);
+  }
   if (h->stream) cudaStreamDestroy(h->stream);
   delete h;
 }
@@ -541,12 +616,16 @@ int swm_helm_solve_fp64(swm_helm *h, const double *rhs, double *psi, double omeg
   SWM_CK(cudaMemcpyAsync(h->psi, psi, h->n * 8, cudaMemcpyHostToDevice, h->stream));
   double bn;
   HTRY(rhs_norm(h, &bn));
+  HTRY(split64_setup(h));
+  split64_field(h, h->rhs, h->s64.rhs, 0);
+  split64_field(h, h->psi, h->s64.psi, 0);
   int s = 0;
   double rel = 1.;
   while (s < max_sweeps) {
     int blk = std::min(HELM_CHECK, max_sweeps - s);
-    for (int q = 0; q < blk; q++) sweep64(h, omega, h->blk);
+    for (int q = 0; q < blk; q++) sweep64(h, omega);
     s += blk;
+    split64_field(h, h->psi, h->s64.psi, 1);  // the residual reads the natural layout
     double r2;
     HTRY(resid2<double>(h, h->hinv, h->rhs, h->psi, nullptr, &r2));
     rel = bn > 0 ? std::sqrt(r2) / bn : std::sqrt(r2);

@@ -53,7 +53,9 @@ struct SorCtl {
 
 struct SorState {
   double *c[5] = {};       // ElSolvSOR_c(:,:,1..5), natural layout (set-up only)
-  double *chi = nullptr, *B = nullptr;   // natural layout
+  double *chi = nullptr, *B = nullptr;   // natural layout; chi: calc_lib::chi, kept between
+                                         // swm_gpu_nondivergent calls
+  double *chi_io = nullptr;              // natural layout: elsolv_sor_gpu_solve's chi
   double *cs[2][5] = {};   // coefficients split by colour
   double *rc4[2] = {};     // 1 / ElSolvSOR_c(:,:,5), split by colour
   uint8_t *ms[2] = {};     // ocean mask split by colour (0 also on the padding of odd rows)
@@ -309,7 +311,7 @@ void sor_free(swm_gpu_ctx *c) {
     cudaFree(s->ms[col]);
   }
   cudaFree(s->bad);
-  cudaFree(s->chi); cudaFree(s->B); cudaFree(s->partial); cudaFree(s->ctl);
+  cudaFree(s->chi); cudaFree(s->chi_io); cudaFree(s->B); cudaFree(s->partial); cudaFree(s->ctl);
   cudaFree(s->und); cudaFree(s->vnd);
   delete s;
   c->sor = nullptr;
@@ -342,6 +344,7 @@ int elsolv_sor_gpu_init(swm_gpu_ctx *c) {
   SWM_CK(cudaMalloc((void **)&s->bad, sizeof(int)));
   SWM_CK(cudaMemsetAsync(s->bad, 0, sizeof(int), c->stream));
   SWM_CK(cudaMalloc((void **)&s->chi, n * 8));
+  SWM_CK(cudaMalloc((void **)&s->chi_io, n * 8));
   SWM_CK(cudaMalloc((void **)&s->B, n * 8));
   SWM_CK(cudaMalloc((void **)&s->partial, (size_t)s->nblocks * 8));
   SWM_CK(cudaMalloc((void **)&s->ctl, sizeof(SorCtl)));
@@ -399,16 +402,16 @@ int sor_graph(swm_gpu_ctx *c, SorState *s) {
 
 }  // namespace
 
-// main_ElSolv_SOR on the device arrays s->B (right-hand side) and s->chi
+// main_ElSolv_SOR on the device arrays s->B (right-hand side) and chi
 // (first guess in, solution out), natural layout; returns
 // SWM_GPU_ENOT_CONVERGED after max_count iterations
-static int sor_solve_device(swm_gpu_ctx *c, double eps, int first_guess, int *iters, double *anorm) {
+static int sor_solve_device(swm_gpu_ctx *c, double *chi, double eps, int first_guess, int *iters, double *anorm) {
   SorState *s = c->sor;
   const int mx = c->nx > c->ny ? c->nx : c->ny;
   const int max_count = first_guess ? (int)lround(1000. * mx) : (int)lround(10. * mx);
   const unsigned nb = (unsigned)((c->n + 255) / 256);
   k_sor_split<<<nb, 256, 0, c->stream>>>(s->B, s->Bs[0], s->Bs[1], c->nx, c->ny, s->W, 0);
-  k_sor_split<<<nb, 256, 0, c->stream>>>(s->chi, s->chis[0], s->chis[1], c->nx, c->ny, s->W, 0);
+  k_sor_split<<<nb, 256, 0, c->stream>>>(chi, s->chis[0], s->chis[1], c->nx, c->ny, s->W, 0);
   c->launches += 2;
   SorCtl ctl = {};
   ctl.relax = 1.;
@@ -425,7 +428,7 @@ static int sor_solve_device(swm_gpu_ctx *c, double eps, int first_guess, int *it
     SWM_CK(cudaStreamSynchronize(c->stream));
     if (ctl.done) break;
   }
-  k_sor_split<<<nb, 256, 0, c->stream>>>(s->chi, s->chis[0], s->chis[1], c->nx, c->ny, s->W, 1);
+  k_sor_split<<<nb, 256, 0, c->stream>>>(chi, s->chis[0], s->chis[1], c->nx, c->ny, s->W, 1);
   c->launches++;
   SWM_CK(cudaGetLastError());
   if (anorm) *anorm = ctl.anorm;
@@ -447,9 +450,9 @@ int elsolv_sor_gpu_solve(swm_gpu_ctx *c, const double *B, double *chi, double ep
   SorState *s = c->sor;
   size_t n = c->n;
   SWM_CK(cudaMemcpyAsync(s->B, B, n * 8, cudaMemcpyHostToDevice, c->stream));
-  SWM_CK(cudaMemcpyAsync(s->chi, chi, n * 8, cudaMemcpyHostToDevice, c->stream));
-  int rc = sor_solve_device(c, eps, first_guess, iters, anorm);
-  SWM_CK(cudaMemcpyAsync(chi, s->chi, n * 8, cudaMemcpyDeviceToHost, c->stream));
+  SWM_CK(cudaMemcpyAsync(s->chi_io, chi, n * 8, cudaMemcpyHostToDevice, c->stream));
+  int rc = sor_solve_device(c, s->chi_io, eps, first_guess, iters, anorm);
+  SWM_CK(cudaMemcpyAsync(chi, s->chi_io, n * 8, cudaMemcpyDeviceToHost, c->stream));
   SWM_CK(cudaStreamSynchronize(c->stream));
   return rc;
 }
@@ -499,7 +502,7 @@ int swm_gpu_nondivergent(swm_gpu_ctx *c, int first_guess, double eps, double *u_
   k_sor_divergence<<<g, b, 0, c->stream>>>(d, d.u0, d.v0, s->B);
   c->launches++;
   SWM_CK(cudaGetLastError());
-  int rc = sor_solve_device(c, eps, first_guess, iters, nullptr);
+  int rc = sor_solve_device(c, s->chi, eps, first_guess, iters, nullptr);
   if (rc != SWM_GPU_OK && rc != SWM_GPU_ENOT_CONVERGED) return rc;
   k_sor_nondiv<<<g, b, 0, c->stream>>>(d, s->chi, d.u0, d.v0, s->und, s->vnd);
   c->launches++;

@@ -77,6 +77,35 @@ def test_plain_bit_exact_on_sphere(name, guard):
         assert np.isnan(g.tracer_field(0, 'CH')).any()
 
 
+def test_sor_and_nondivergent_flow_on_sphere():
+    """The drop-in main_ElSolv_SOR and the non-divergent correction on the
+    spherical test_nonlinear grid (cos(lat) 0.91-1 in the coefficients) from
+    the state after NSTEPS steps: chi bit for bit with the oracle when the
+    iteration counts agree (they agree or differ by one: the correction norm
+    is a parallel sum on the GPU)."""
+    case = _case('test_nonlinear')
+    o = _oracle(case)
+    g = GpuModel('plain_fp64')
+    run_case(case, g, nsteps=NSTEPS, with_diag=False)
+    o.sor_init()
+    g.sor_init()
+    B = o.divergence(o.field('u'), o.field('v'))
+    assert np.abs(B).max() > 0
+    xo, io, _ = o.sor_solve(B, np.zeros_like(B), 1e-4, True)
+    xg, ig, _ = g.sor_solve(B, np.zeros_like(B), 1e-4, True)
+    assert io > 0 and abs(ig - io) <= 1, (io, ig)
+    if ig == io:
+        assert np.array_equal(xo, xg)
+    assert np.abs(xo - xg).max() <= 1e-6 * np.abs(xo).max()
+    uo, vo, co, io2 = o.nondivergent(o.field('u'), o.field('v'), np.zeros_like(B), True)
+    ug, vg, cg, ig2, rc = g.nondivergent(True)
+    assert rc == 0 and io2 > 0 and abs(ig2 - io2) <= 1, (io2, ig2)
+    if ig2 == io2:
+        assert np.array_equal(cg, co) and np.array_equal(ug, uo) and np.array_equal(vg, vo)
+    assert np.abs(ug - uo).max() <= 1e-6 * np.abs(uo).max()
+    g.close()
+
+
 @pytest.mark.parametrize('path', ['fused_fp64', 'fused_fp32c'])
 @pytest.mark.parametrize('name,biharmonic', [('test_nonlinear', False), ('test_nonlinear', True),
                                              ('test_nl_tracer', False), ('test_fixed_length_output', False)])
