@@ -257,6 +257,11 @@ def double_gyre_line(args, rank, ws, steps, warmup, side=True):
     prof = case['streams'][0]['rec1'][0][:, 0]
     rows_pin[:] = prof[None, :] * (1.0 + 1e-3 * np.cos(np.arange(k_e2e) * 2e-3))[:, None]
     outs = torch.empty((k_e2e, 3), dtype=torch.float64).pin_memory().numpy()
+    # untimed warm-up steps of the same call (its first use sets up the
+    # monitor's device tables)
+    w_e2e = min(E2E_WARMUP, k_e2e)
+    g.run_monitor(itt, w_e2e, 0, rows_pin[:w_e2e], outs[:w_e2e])
+    itt += w_e2e
     g.synchronize()
     t0 = time.perf_counter()
     g.run_monitor(itt, k_e2e, 0, rows_pin, outs)
@@ -268,7 +273,8 @@ def double_gyre_line(args, rank, ws, steps, warmup, side=True):
                    'per_step': "H2D: the step's wind-stress row profile, read from pinned host memory by the "
                                'step kernel before the step; swm_gpu_step + swm_gpu_advance; D2H: the FP64 '
                                'domain integrals of the new state, written into pinned host memory; all steps '
-                               'issued by swm_gpu_run_monitor; wall clock including the final wait; no L2 flush'}
+                               'issued by swm_gpu_run_monitor; wall clock including the final wait; no L2 flush; '
+                               'after %d untimed monitored warm-up steps' % w_e2e}
     if rank == 0 and side:
         line.update(side_measurements(args, case, g, stream, flush, ncell))
         line['speedup_vs_fp64_plain'] = line['plain_fp64']['ms_per_step'] / step_ms
@@ -407,6 +413,11 @@ def ensemble_line(args, rank, ws):
     for i, c in enumerate(cases):
         rows[:, off[i]:off[i + 1]] = c['streams'][0]['rec1'][0][:, 0][None, :] * mod[:, None]
     outs = torch.empty((k_e2e, len(cases), 3), dtype=torch.float64).pin_memory().numpy()
+    # untimed warm-up steps of the same call (its first use sets up the
+    # monitor's device tables)
+    w_e2e = min(E2E_WARMUP, k_e2e)
+    ens.run_monitor(itt, w_e2e, rows[:w_e2e], outs[:w_e2e])
+    itt += w_e2e
     ens.synchronize()
     barrier(ws)
     note('ensemble: end-to-end steps')
@@ -422,7 +433,7 @@ def ensemble_line(args, rank, ws):
                                'host memory); the batched step; D2H: every member\'s FP64 domain integrals '
                                '(volume, potential and kinetic energy) of the new state into pinned host memory; '
                                'all steps issued by swm_gpu_ensemble_run_monitor; wall clock including the final '
-                               'wait'}
+                               'wait; after %d untimed monitored warm-up steps' % w_e2e}
     ens.close()
     for g in ms:
         g.close()
@@ -452,6 +463,7 @@ def ensemble_line(args, rank, ws):
 
 # array points of the 256-member ensemble the committed ncu summary covers
 ENSEMBLE_256_POINTS = 12043762
+E2E_WARMUP = 3  # untimed monitored steps before the timed end-to-end call
 
 
 def plain_one_by_one(cases):
@@ -732,16 +744,14 @@ def oracle_ensemble(cases, warmup, steps, budget_s, threads=None):
     return done / t, t / steps * 1e3, sample, threads
 
 
-def cpu_baseline(cases, budget_s=20.0, sample=32):
-    """The oracle on a sample of the ensemble's members (spread over the
-    sizes), all host cores, member-parallel."""
-    n = len(cases)
-    order = sorted(range(n), key=lambda i: cases[i]['config']['nx'] * cases[i]['config']['ny'])
-    pick = sorted({order[round(q * (n - 1) / max(sample - 1, 1))] for q in range(min(sample, n))})
-    v, _, desc, threads = oracle_ensemble([cases[i] for i in pick], 2, 3, budget_s)
+def cpu_baseline(cases, steps=200, budget_s=15.0):
+    """The oracle on the ensemble's members, all host cores, member-parallel:
+    about 10-15 s of CPU work (every member each step, or a round-robin
+    share when the steps would exceed budget_s)."""
+    v, _, desc, threads = oracle_ensemble(cases, 2, steps, budget_s)
     return {'value': v, 'unit': 'cell-steps/s', 'cores': threads, 'kind': 'port',
-            'sample': '%d of the %d ensemble members spread over the sizes, 3 timed steps (%s); FP64 C '
-                      'restatement of the reference loops' % (len(pick), n, desc)}
+            'sample': '%d timed steps of the %d-member ensemble (%s); FP64 C restatement of the reference '
+                      'loops' % (steps, len(cases), desc)}
 
 
 def reference(args, rank, ws):

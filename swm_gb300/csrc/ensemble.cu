@@ -207,8 +207,15 @@ int ens_capture(swm_gpu_ensemble *e, int64_t itt0) {
   const int phase0 = e->phase;
   const int64_t l0 = e->launches;
   SWM_CK(cudaStreamBeginCapture(e->stream, cudaStreamCaptureModeThreadLocal));
+  // each phase has its own queue head: one reset of all of them serves the
+  // graph's six steps
+  cudaError_t me = cudaMemsetAsync(e->next, 0, ENS_PHASES * sizeof(int), e->stream);
   int rc = SWM_GPU_OK;
-  for (int s = 1; s <= ENS_PHASES && rc == SWM_GPU_OK; s++) rc = ens_step(e, itt0 + s);
+  if (me != cudaSuccess) {
+    set_error(std::string("swm_gpu_ensemble_run: cudaMemsetAsync: ") + cudaGetErrorString(me));
+    rc = SWM_GPU_ECUDA;
+  }
+  for (int s = 1; s <= ENS_PHASES && rc == SWM_GPU_OK; s++) rc = ens_step(e, itt0 + s, nullptr, false);
   cudaGraph_t g = nullptr;
   cudaError_t ce = cudaStreamEndCapture(e->stream, &g);
   e->graph_launches = e->launches - l0;
