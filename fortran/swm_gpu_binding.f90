@@ -308,6 +308,15 @@ module swm_gpu_binding
       type(c_ptr), value :: ctx
       integer(c_int64_t), value :: ticket
     end function swm_gpu_ready
+    integer(c_int) function swm_gpu_host_register(host, bytes) bind(C)
+      import :: c_int, c_int64_t, c_ptr
+      type(c_ptr), value :: host
+      integer(c_int64_t), value :: bytes
+    end function swm_gpu_host_register
+    integer(c_int) function swm_gpu_host_unregister(host) bind(C)
+      import :: c_int, c_ptr
+      type(c_ptr), value :: host
+    end function swm_gpu_host_unregister
     integer(c_int) function swm_gpu_get_metric(ctx, which, grid, host_out) bind(C)
       import :: c_int, c_ptr
       type(c_ptr), value :: ctx

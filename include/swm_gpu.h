@@ -205,6 +205,16 @@ int swm_gpu_set_field(swm_gpu_ctx *ctx, int field, const double *host_in);
 int swm_gpu_get_field_async(swm_gpu_ctx *ctx, int field, double *host_out, int64_t *ticket);
 int swm_gpu_wait(swm_gpu_ctx *ctx, int64_t ticket);
 int swm_gpu_ready(swm_gpu_ctx *ctx, int64_t ticket);
+/* Page-lock (pin) a host array the caller owns, and release it: a pinned
+   destination lets swm_gpu_get_field_async overlap the following steps.  A
+   Fortran host pins its output arrays once (c_loc, size in bytes); the
+   Python host's asynchronous writer pins its buffer pool.  Wait for every
+   copy into the array before unpinning it.  Tickets and pinned arrays may
+   be used from a writer thread while the host thread steps the model: the
+   library's calls are thread-safe for one context as long as only one
+   thread issues work on it. */
+int swm_gpu_host_register(void *host, int64_t bytes);
+int swm_gpu_host_unregister(void *host);
 /* 1-D metric: which = 0 lat, 1 cos, 2 tan, 3 f; grid = 0 H, 1 u, 2 v, 3 eta */
 int swm_gpu_get_metric(swm_gpu_ctx *ctx, int which, int grid, double *host_out);
 int swm_gpu_get_mask(swm_gpu_ctx *ctx, int grid, int8_t *host_out);

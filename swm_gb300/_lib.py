@@ -56,6 +56,7 @@ def _sigs():
         'swm_gpu_get_field': (I, [P, I, P]), 'swm_gpu_set_field': (I, [P, I, P]),
         'swm_gpu_get_field_async': (I, [P, I, P, C.POINTER(C.c_int64)]), 'swm_gpu_wait': (I, [P, I64]),
         'swm_gpu_ready': (I, [P, I64]),
+        'swm_gpu_host_register': (I, [P, I64]), 'swm_gpu_host_unregister': (I, [P]),
         'swm_gpu_get_metric': (I, [P, I, I, P]), 'swm_gpu_get_mask': (I, [P, I, P]),
         'swm_gpu_streamfunction': (I, [P, P]),
         'swm_gpu_diag_accumulate': (I, [P, I, I, I, D]),

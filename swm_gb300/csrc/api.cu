@@ -729,6 +729,18 @@ int swm_gpu_ready(swm_gpu_ctx *c, int64_t ticket) {
   return -1;
 }
 
+int swm_gpu_host_register(void *host, int64_t bytes) {
+  SWM_REQUIRE(host && bytes > 0, "swm_gpu_host_register: bad arguments");
+  SWM_CK(cudaHostRegister(host, (size_t)bytes, cudaHostRegisterDefault));
+  return SWM_GPU_OK;
+}
+
+int swm_gpu_host_unregister(void *host) {
+  SWM_REQUIRE(host, "swm_gpu_host_unregister: bad arguments");
+  SWM_CK(cudaHostUnregister(host));
+  return SWM_GPU_OK;
+}
+
 int swm_gpu_diag_accumulate(swm_gpu_ctx *c, int slot, int f, int square, double weight) {
   SWM_ON_DEVICE(c ? c->device : -1);
   SWM_REQUIRE(c && c->stage >= 5 && slot >= 0 && slot < 4096, "swm_gpu_diag_accumulate: bad arguments");

@@ -9,6 +9,7 @@
 #pragma once
 #include <cuda_runtime.h>
 #include <stdint.h>
+#include <atomic>
 #include <string>
 #include <vector>
 #include "../../include/swm_gpu.h"
@@ -151,7 +152,7 @@ struct swm_gpu_ctx {
   Trc32State *trc32 = nullptr;      // tracers of the FP32 compensated path
   std::vector<swm::DiagAcc> diag;   // averaging buffers by slot
   std::vector<cudaEvent_t> async_ev;  // ring of events for swm_gpu_get_field_async
-  int64_t async_next = 0;             // next ticket
+  std::atomic<int64_t> async_next{0};  // next ticket (read by a writer thread's waits)
   double *psi = nullptr, *psi_tmp = nullptr;  // streamfunction and its zonal sums
   double *rows_buf = nullptr;       // 2 x Ny staging rows of swm_gpu_set_stream_rows
   const swm::MonitorStep *mon = nullptr;  // the next FP32 pair step is a monitored step

@@ -51,12 +51,19 @@ class DiagTask:
         self.buffer = self.buffer + dT * d
         self.count = self.count + dT
 
-    def process(self, itt, fetch, device=None, slot=None):
+    def process(self, itt, fetch, device=None, slot=None, emit=None):
         """device: a backend with diag_accumulate/diag_mean (the averaging
-        buffer then lives on the GPU and one field crosses per period)."""
+        buffer then lives on the GPU and one field crosses per period).
+        emit(task, time, data): where a record goes (data None: the task's
+        variable as of now); default: kept in self.times / self.records."""
+        self._emit = emit or (lambda task, time, data: task._keep(time, fetch(task.name) if data is None else data))
         if device is not None and self.type == 'A':
             return self._process_device(itt, device, slot)
         return self._process_host(itt, fetch)
+
+    def _keep(self, time, data):
+        self.times.append(time)
+        self.records.append(np.array(data, copy=True))
 
     def _process_device(self, itt, dev, slot):
         k = itt - self.dsi
@@ -68,8 +75,7 @@ class DiagTask:
         if dT < self.dt and k != 0:
             dev.diag_accumulate(slot, field, self.square, self.dt - dT)
             mean, _ = dev.diag_mean(slot)
-            self.times.append(self.dt * itt - dT)
-            self.records.append(mean)
+            self._emit(self, self.dt * itt - dT, mean)
         dev.diag_accumulate(slot, field, self.square, dT)
 
     def _process_host(self, itt, fetch):
@@ -77,8 +83,7 @@ class DiagTask:
         if math.fmod(k, self.nstep) != 0:
             return
         if self.type == 'S':
-            self.times.append(itt * self.dt)
-            self.records.append(fetch(self.name).copy())
+            self._emit(self, itt * self.dt, None)
         elif self.type == 'A':
             per = self.period if self.period != 2.628e6 else self.meant_out
             dT = min(math.fmod(self.dt * k, per), self.dt)
@@ -86,20 +91,22 @@ class DiagTask:
             if dT < self.dt and k != 0:
                 self._add(data, self.dt - dT)
                 self.buffer = self.buffer / self.count
-                self.times.append(self.dt * itt - dT)
-                self.records.append(self.buffer.copy())
+                self._emit(self, self.dt * itt - dT, self.buffer.copy())
                 self.buffer = np.zeros_like(self.buffer)
                 self.count = 0.0
             self._add(data, dT)
         elif self.type == 'I':
             if itt == 0:
-                self.times.append(0.0)
-                self.records.append(fetch(self.name).copy())
+                self._emit(self, 0.0, None)
 
 
 class Driver:
-    def __init__(self, case, backend, device_averages=True, device_streams=True):
+    def __init__(self, case, backend, device_averages=True, device_streams=True, writer=None):
+        """writer: an AsyncWriter (host/writer.py); each diagnostics record
+        then also goes to the task's netCDF file, snapshots as asynchronous
+        device copies, so the time loop does not wait for them."""
         self.case, self.b = case, backend
+        self.writer = writer
         self.device_averages = device_averages
         # time-dependent forcing records kept on the device, interpolated there
         self.device_streams = device_streams and hasattr(backend, 'stream_interp')
@@ -107,6 +114,7 @@ class Driver:
         self.itt = 0
         self.tasks = []
         self._psi_cache = None
+        self._masks = {}
 
     # -- init sequence: model.f90 initModel :71-144 ---------------------
     def init(self, with_diag=True):
@@ -141,6 +149,9 @@ class Driver:
         if with_diag:
             self.tasks = [DiagTask(s, c['Nt'], c['diag_start_ind'], c['dt'], c['meant_out'])
                           for s in case['diag']]
+            if self.writer is not None:  # createTaskDS (diagTask.f90:344-371) at task set-up
+                for t in self.tasks:
+                    self._task_file(t)
             self.diag()
 
     def _feed_streams(self, itt):
@@ -167,8 +178,38 @@ class Driver:
             return
         self._psi_cache = None
         dev = self.b if self.device_averages and hasattr(self.b, 'diag_accumulate') else None
+        emit = self._emit if self.writer is not None else None
         for slot, t in enumerate(self.tasks):
-            t.process(self.itt, self.fetch, dev, slot)
+            t.process(self.itt, self.fetch, dev, slot, emit)
+
+    def _emit(self, task, time, data):
+        """A record to the task's file through the writer (writeTaskToFile,
+        diagTask.f90:231-253): a snapshot of a state field as an asynchronous
+        device copy, anything else (means, PSI) from the host.  The writer
+        thread appends the record to task.records after writing it."""
+        field, grid = DIAG_VARS[task.name]
+        fh = self._task_file(task)
+        if grid not in self._masks:
+            self._masks[grid] = self.b.ocean(grid)
+        task.times.append(time)
+        if data is None and task.name != 'PSI' and hasattr(self.b, 'field_async'):
+            self.writer.submit_field(self.b, field, fh, time, self._masks[grid], records=task.records)
+        else:
+            self.writer.submit_host(self.fetch(task.name) if data is None else data, fh, time, self._masks[grid],
+                                    records=task.records)
+
+    def _task_file(self, task):
+        from .writer import grid_coords
+        fn = task.spec['filename']
+        if fn not in self.writer.files:
+            lon, lat = grid_coords(self.cfg, DIAG_VARS[task.name][1])
+            self.writer.file(fn, task.spec.get('ovarname') or task.spec['varname'], lon, lat)
+        return self.writer.files[fn]
+
+    def finish(self):
+        """Writes the records still in flight and closes the output files."""
+        if self.writer is not None:
+            self.writer.close()
 
     # -- time loop: model.f90 timestepModel :153-197 ---------------------
     def run(self, nsteps=None, with_diag=True):

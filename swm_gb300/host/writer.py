@@ -1,0 +1,201 @@
+"""Asynchronous diagnostics output for the host mirror.
+
+Restates the reference's netCDF output of a diagnostics task: the dataset
+createDSEuler builds (io_module.f90:305-374: dimensions LONGITUDE, LATITUDE
+and an unlimited TIME, the coordinate variables with their units, the
+variable with its missing_value attribute) and the time slice putVarEuler
+writes (io_module.f90:504-529: missing value on land of the variable's grid
+and on non-finite values, the time coordinate, the record count), called
+from writeTaskToFile (diagTask.f90:231-253).
+
+The reference writes synchronously inside the time loop.  Here a snapshot
+is a device-to-host copy into a pinned buffer issued on the model's stream
+(swm_gpu_get_field_async), and one writer thread waits for the copy and
+writes the record, so the host thread goes on stepping the model while the
+copy and the file write are in flight.  Records reach each file in the
+order they were submitted.  A bounded pool of buffers per field shape keeps
+the memory fixed: when every buffer is in flight, a submit waits for the
+oldest write to finish.
+"""
+import os
+import queue
+import threading
+
+import numpy as np
+
+MISS_VAL_DEF = float(np.float32(1e37))  # default-real literal (include/io.h:32)
+TUNIT = 'seconds since 0000-01-01 00:00:00'  # include/io.h:83
+
+
+def grid_coords(cfg, grid):
+    """(lon, lat) in degrees of one grid, as domain_module.f90:121-128 forms
+    them from lon_s/lon_e/lat_s/lat_e: H and u on the corners in longitude,
+    v and eta half a cell east; H and v on the corners in latitude, u and
+    eta half a cell north."""
+    nx, ny = cfg['nx'], cfg['ny']
+    lon_s, lon_e, lat_s, lat_e = cfg['lon_s'], cfg['lon_e'], cfg['lat_s'], cfg['lat_e']
+    lat = (np.arange(ny, dtype=np.float64) * (lat_e - lat_s)) / (ny - 1) + lat_s
+    lon = (np.arange(nx, dtype=np.float64) * (lon_e - lon_s)) / (nx - 1) + lon_s
+    if grid in ('u', 'eta'):
+        lat = lat + (lat_e - lat_s) / (2. * (ny - 1))
+    if grid in ('v', 'eta'):
+        lon = lon + (lon_e - lon_s) / (2. * (nx - 1))
+    return lon, lat
+
+
+class EulerFile:
+    """One output dataset of a 2-D variable (createDSEuler) and its records
+    (putVarEuler).  netCDF-3 classic through scipy.io.netcdf_file."""
+
+    def __init__(self, path, varname, lon, lat, time_unit=TUNIT, missval=MISS_VAL_DEF):
+        from scipy.io import netcdf_file
+        self.path, self.varname, self.missval = path, varname, missval
+        self.nc = netcdf_file(path, 'w', version=1)
+        nc = self.nc
+        nc.createDimension('TIME', None)  # scipy writes the unlimited dimension first
+        nc.createDimension('LONGITUDE', len(lon))
+        nc.createDimension('LATITUDE', len(lat))
+        for name, vals, units in (('LONGITUDE', lon, 'degrees_east'), ('LATITUDE', lat, 'degrees_north')):
+            v = nc.createVariable(name, 'd', (name,))
+            v.units, v.long_name = units, name
+            v[:] = vals
+        t = nc.createVariable('TIME', 'd', ('TIME',))
+        t.units, t.long_name = time_unit, 'TIME'
+        self.var = nc.createVariable(varname, 'd', ('TIME', 'LATITUDE', 'LONGITUDE'))
+        self.var.missing_value = np.float64(missval)
+        self.nrec = 0
+
+    def put(self, data, time, ocean=None, records=None):
+        """One time slice: missing value where ocean != 1 and where the value
+        is not finite; then the time coordinate; nrec + 1.  records: a list
+        that also receives a copy of the data as given."""
+        if records is not None:
+            records.append(np.array(data, dtype=np.float64, copy=True))
+        d = np.array(data, dtype=np.float64, copy=True)
+        if ocean is not None:
+            d[ocean != 1] = self.missval
+        d[~np.isfinite(d)] = self.missval
+        self.var[self.nrec] = d
+        self.nc.variables['TIME'][self.nrec] = time
+        self.nrec += 1
+
+    def close(self):
+        if self.nc is not None:
+            self.nc.flush()
+            self.nc.close()
+            self.nc = None
+
+
+PAGE = 4096
+
+
+class _Pool:
+    """Fixed buffers of one shape, pinned through the library when the
+    backend can pin (swm_gpu_host_register).  Each buffer covers whole pages
+    of its own allocation, so no two pinned ranges share a page."""
+
+    def __init__(self, shape, n, pin):
+        self.free = queue.Queue()
+        self.pages, self.pin = [], pin
+        nbytes = int(np.prod(shape)) * 8
+        span = -(-nbytes // PAGE) * PAGE
+        for _ in range(n):
+            raw = np.empty(span + PAGE, dtype=np.uint8)
+            off = (-raw.ctypes.data) % PAGE
+            region = raw[off:off + span]
+            if pin is not None:
+                pin[0](region)
+            self.pages.append((raw, region))
+            self.free.put(region[:nbytes].view(np.float64).reshape(shape))
+
+    def release(self):
+        if self.pin is not None:
+            for _, region in self.pages:
+                self.pin[1](region)
+
+
+class AsyncWriter:
+    """Writer thread for the diagnostics files of one model.
+
+    submit_field(backend, field, fh, time, ocean): the field's copy as of this
+    point of the model's stream goes into a pooled (pinned) buffer; the
+    writer thread waits for it and writes the record to fh.
+    submit_host(data, fh, time, ocean): a host array (a device mean, the
+    streamfunction) written the same way, after a copy.
+    Both return at once unless every buffer of the shape is in flight.
+    close() writes what is queued, joins the thread and closes the files."""
+
+    def __init__(self, outdir, buffers=4, time_unit=TUNIT):
+        self.outdir, self.nbuf, self.time_unit = outdir, buffers, time_unit
+        os.makedirs(outdir, exist_ok=True)
+        self.files = {}
+        self.pools = {}
+        self.q = queue.Queue()
+        self.error = None
+        self.submitted = 0
+        self.from_device = 0  # records submitted as asynchronous device copies
+        self.written = 0
+        self.thread = threading.Thread(target=self._run, name='swm-writer', daemon=True)
+        self.thread.start()
+
+    def file(self, filename, varname, lon, lat):
+        if filename not in self.files:
+            self.files[filename] = EulerFile(os.path.join(self.outdir, filename), varname, lon, lat, self.time_unit)
+        return self.files[filename]
+
+    def _pool(self, shape, backend):
+        pin = None
+        if backend is not None and hasattr(backend, 'host_register'):
+            pin = (backend.host_register, backend.host_unregister)
+        key = (shape, id(backend) if pin else None)
+        if key not in self.pools:
+            self.pools[key] = _Pool(shape, self.nbuf, pin)
+        return self.pools[key]
+
+    def submit_field(self, backend, field, fh, time, ocean=None, records=None):
+        self._check()
+        pool = self._pool((backend.ny, backend.nx), backend)
+        buf = pool.free.get()  # waits while every buffer of the shape is in flight
+        ticket = backend.field_async(field, buf)
+        self.submitted += 1
+        self.from_device += 1
+        self.q.put((backend, ticket, buf, pool, fh, time, ocean, records))
+
+    def submit_host(self, data, fh, time, ocean=None, records=None):
+        self._check()
+        self.submitted += 1
+        self.q.put((None, None, np.array(data, dtype=np.float64, copy=True), None, fh, time, ocean, records))
+
+    def _run(self):
+        while True:
+            item = self.q.get()
+            if item is None:
+                return
+            backend, ticket, buf, pool, fh, time, ocean, records = item
+            try:
+                if backend is not None:
+                    backend.wait(ticket)
+                if self.error is None:
+                    fh.put(buf, time, ocean, records)
+                    self.written += 1
+            except Exception as e:  # reported to the host thread at its next call
+                self.error = e
+            finally:
+                if pool is not None:
+                    pool.free.put(buf)
+
+    def _check(self):
+        if self.error is not None:
+            raise RuntimeError('diagnostics writer failed: %r' % (self.error,))
+
+    def close(self):
+        if self.thread is not None:
+            self.q.put(None)
+            self.thread.join()
+            self.thread = None
+        for fh in self.files.values():
+            fh.close()
+        for p in self.pools.values():
+            p.release()
+        self.pools = {}
+        self._check()

@@ -182,6 +182,13 @@ class GpuModel:
     def ready(self, ticket):
         return self.L.swm_gpu_ready(self.ctx, ticket)
 
+    def host_register(self, arr):
+        """Pin a host array (swm_gpu_host_register) for asynchronous copies."""
+        check(self.L.swm_gpu_host_register(_p(arr), arr.nbytes))
+
+    def host_unregister(self, arr):
+        check(self.L.swm_gpu_host_unregister(_p(arr)))
+
     def set_field(self, name, arr):
         a = _f64(arr)
         check(self.L.swm_gpu_set_field(self.ctx, FIELD_ID[self._ALIAS.get(name, name)], _p(a)))

@@ -37,13 +37,19 @@ CASES = {
 
 
 def read_output(path):
+    """Records, times and the dataset's layout: coordinates, variable name
+    and missing value (what the asynchronous writer must reproduce)."""
     from scipy.io import netcdf_file
     nc = netcdf_file(path, 'r', mmap=False)
     var = [k for k in nc.variables if k not in ('LONGITUDE', 'LATITUDE', 'TIME')][0]
     data = np.array(nc.variables[var].data, dtype=np.float64)
     t = np.array(nc.variables['TIME'].data, dtype=np.float64)
+    layout = {'lon': np.array(nc.variables['LONGITUDE'].data, dtype=np.float64),
+              'lat': np.array(nc.variables['LATITUDE'].data, dtype=np.float64),
+              'var': np.array(var),
+              'missval': np.array([float(np.asarray(nc.variables[var]._attributes['missing_value']).ravel()[0])])}
     nc.close()
-    return t, data
+    return t, data, layout
 
 
 def main(ref):
@@ -54,9 +60,11 @@ def main(ref):
         case['diag'] = [t for t in case['diag'] if t['filename'] in outs]
         extra = {}
         for fn in outs:
-            t, data = read_output(os.path.join(d, 'output', 'reference_000000000001_' + fn))
+            t, data, layout = read_output(os.path.join(d, 'output', 'reference_000000000001_' + fn))
             extra['time__' + fn] = t
             extra['data__' + fn] = data
+            for k, v in layout.items():
+                extra[k + '__' + fn] = v
         save_case(os.path.join(HERE, name + '.npz'), case, extra)
         print(name, os.path.getsize(os.path.join(HERE, name + '.npz')))
 
