@@ -64,7 +64,7 @@ def parse():
     ap.add_argument('--device-only', action='store_true',
                     help='only the warm-up and timed device steps (the form to run under ncu)')
     ap.add_argument('--workload', default='ensemble',
-                    choices=['ensemble', 'double_gyre', 'tracer', 'helmholtz', 'linear_rg', 'sor'],
+                    choices=['ensemble', 'double_gyre', 'tracer', 'helmholtz', 'linear_rg', 'sor', 'output'],
                     help='ensemble: the headline line; the others print that measurement alone')
     return ap.parse_args()
 
@@ -454,6 +454,8 @@ def ensemble_line(args, rank, ws):
         line['sor'] = sor_measurement(args)
         note('linear reduced gravity')
         line['linear_rg'] = linear_rg_measurement(args)
+        note('diagnostics output')
+        line['output'] = output_measurement(args)
     if rank == 0 and ws == 1 and not args.quick:
         note('cpu baseline')
         line['cpu_baseline'] = cpu_baseline(cases)
@@ -633,6 +635,50 @@ def helmholtz_measurement(args, cells=4096, rtol=1e-10):
                                   'note': 'sweeps only counted; residual passes included in the time'}}
     out['mixed_speedup'] = out['fp64']['time_to_solution_s'] / out['mixed']['time_to_solution_s']
     g.close()
+    return out
+
+
+def output_measurement(args, cells=1024, steps=2000, records=4):
+    """Diagnostics output while the model steps: the 1024^2 double gyre on
+    the FP32 pair path with snapshot tasks of u, v and eta (`records`
+    records each over `steps` steps, netCDF files in the reference's layout
+    in a scratch directory), written synchronously in the time loop as the
+    reference does, or by the asynchronous writer (device copies into
+    pinned buffers, a writer thread), against the same steps without
+    output.  Wall clock around the time loop and the writer's drain."""
+    import shutil
+    import tempfile
+    from swm_gb300.host import synthetic
+    from swm_gb300.host.driver import Driver
+    from swm_gb300.host.writer import AsyncWriter
+    from swm_gb300.model import GpuModel
+    base = synthetic.double_gyre(cells, nsteps=steps)
+    base['diag'] = [dict(filename='%s.nc' % v.lower(), varname=v, type='S', frequency=records, period=2.628e6,
+                         process='A') for v in ('U', 'V', 'ETA')]
+    out = {'workload': 'double_gyre_%dx%d_fp32c_snapshots' % (cells, cells), 'steps': steps,
+           'records_per_field': records, 'fields': 3,
+           'bytes_per_record': base['config']['nx'] * base['config']['ny'] * 8}
+    tmp = tempfile.mkdtemp(prefix='swm_out_')
+    try:
+        for mode in ('none', 'synchronous', 'asynchronous'):
+            g = GpuModel('fused_fp32c')
+            w = None if mode == 'none' else AsyncWriter(os.path.join(tmp, mode), inline=(mode == 'synchronous'))
+            drv = Driver(base, g, writer=w)
+            drv.init(with_diag=mode != 'none')
+            drv.run(10, with_diag=False)  # tuning and warm-up
+            g.synchronize()
+            t0 = time.perf_counter()
+            drv.run(steps, with_diag=mode != 'none')
+            g.synchronize()
+            drv.finish()
+            out['ms_per_step_' + mode] = (time.perf_counter() - t0) / steps * 1e3
+            if w is not None:
+                out['records_' + mode] = w.written
+            g.close()
+    finally:
+        shutil.rmtree(tmp, ignore_errors=True)
+    a, b, c = out['ms_per_step_none'], out['ms_per_step_synchronous'], out['ms_per_step_asynchronous']
+    out['output_cost_hidden'] = 1.0 - (c - a) / (b - a) if b > a else None
     return out
 
 
@@ -834,6 +880,8 @@ def main():
                                      err_steps=0 if args.device_only else 1000)
         elif args.workload == 'helmholtz':
             out = helmholtz_measurement(args, cells=args.cells if args.cells != 1024 else 4096)
+        elif args.workload == 'output':
+            out = output_measurement(args)
         elif args.workload == 'sor':
             out = sor_measurement(args, cells=args.cells if args.cells != 1024 else 4096)
         else:

@@ -64,6 +64,7 @@ class EulerFile:
         self.var = nc.createVariable(varname, 'd', ('TIME', 'LATITUDE', 'LONGITUDE'))
         self.var.missing_value = np.float64(missval)
         self.nrec = 0
+        self._land = None  # the land mask of the first record's grid
 
     def put(self, data, time, ocean=None, records=None):
         """One time slice: missing value where ocean != 1 and where the value
@@ -73,8 +74,10 @@ class EulerFile:
             records.append(np.array(data, dtype=np.float64, copy=True))
         d = np.array(data, dtype=np.float64, copy=True)
         if ocean is not None:
-            d[ocean != 1] = self.missval
-        d[~np.isfinite(d)] = self.missval
+            if self._land is None or self._land.shape != ocean.shape:
+                self._land = ocean != 1
+            np.copyto(d, self.missval, where=self._land)
+        np.copyto(d, self.missval, where=~np.isfinite(d))
         self.var[self.nrec] = d
         self.nc.variables['TIME'][self.nrec] = time
         self.nrec += 1
@@ -125,8 +128,10 @@ class AsyncWriter:
     Both return at once unless every buffer of the shape is in flight.
     close() writes what is queued, joins the thread and closes the files."""
 
-    def __init__(self, outdir, buffers=4, time_unit=TUNIT):
-        self.outdir, self.nbuf, self.time_unit = outdir, buffers, time_unit
+    def __init__(self, outdir, buffers=4, time_unit=TUNIT, inline=False):
+        """inline: write in the calling thread with synchronous reads, as the
+        reference does (for comparison)."""
+        self.outdir, self.nbuf, self.time_unit, self.inline = outdir, buffers, time_unit, inline
         os.makedirs(outdir, exist_ok=True)
         self.files = {}
         self.pools = {}
@@ -154,6 +159,11 @@ class AsyncWriter:
 
     def submit_field(self, backend, field, fh, time, ocean=None, records=None):
         self._check()
+        if self.inline:
+            self.submitted += 1
+            fh.put(backend.field(field), time, ocean, records)
+            self.written += 1
+            return
         pool = self._pool((backend.ny, backend.nx), backend)
         buf = pool.free.get()  # waits while every buffer of the shape is in flight
         ticket = backend.field_async(field, buf)
@@ -163,6 +173,11 @@ class AsyncWriter:
 
     def submit_host(self, data, fh, time, ocean=None, records=None):
         self._check()
+        if self.inline:
+            self.submitted += 1
+            fh.put(data, time, ocean, records)
+            self.written += 1
+            return
         self.submitted += 1
         self.q.put((None, None, np.array(data, dtype=np.float64, copy=True), None, fh, time, ocean, records))
 
