@@ -13,12 +13,14 @@ is a device-to-host copy into a pinned buffer issued on the model's stream
 (swm_gpu_get_field_async), and one writer thread waits for the copy and
 writes the record, so the host thread goes on stepping the model while the
 copy and the file write are in flight.  Records reach each file in the
-order they were submitted.  A bounded pool of buffers per field shape keeps
+order they were submitted.  The files are netCDF-3 classic (CDF-1), written
+here directly (no netCDF library on either machine).  A bounded pool of buffers per field shape keeps
 the memory fixed: when every buffer is in flight, a submit waits for the
 oldest write to finish.
 """
 import os
 import queue
+import struct
 import threading
 
 import numpy as np
@@ -43,26 +45,65 @@ def grid_coords(cfg, grid):
     return lon, lat
 
 
+def _nc_name(name):
+    b = name.encode()
+    return struct.pack('>i', len(b)) + b + b'\0' * (-len(b) % 4)
+
+
+def _nc_att_list(atts):
+    """NC_ATTRIBUTE list of (name, value): str as NC_CHAR, float as NC_DOUBLE."""
+    if not atts:
+        return struct.pack('>ii', 0, 0)
+    out = struct.pack('>ii', 0x0C, len(atts))
+    for name, val in atts:
+        out += _nc_name(name)
+        if isinstance(val, str):
+            b = val.encode()
+            out += struct.pack('>ii', 2, len(b)) + b + b'\0' * (-len(b) % 4)
+        else:
+            out += struct.pack('>ii', 6, 1) + struct.pack('>d', float(val))
+    return out
+
+
 class EulerFile:
     """One output dataset of a 2-D variable (createDSEuler) and its records
-    (putVarEuler).  netCDF-3 classic through scipy.io.netcdf_file."""
+    (putVarEuler), as a netCDF-3 classic file written here directly: the
+    header and the coordinates at creation, then each record (TIME and the
+    field, big-endian doubles) appended where the format puts it, and the
+    record count in the header updated after every record, so the file is
+    complete at any time.  Writing a record releases the interpreter lock
+    for the copy to the file."""
 
     def __init__(self, path, varname, lon, lat, time_unit=TUNIT, missval=MISS_VAL_DEF):
-        from scipy.io import netcdf_file
         self.path, self.varname, self.missval = path, varname, missval
-        self.nc = netcdf_file(path, 'w', version=1)
-        nc = self.nc
-        nc.createDimension('TIME', None)  # scipy writes the unlimited dimension first
-        nc.createDimension('LONGITUDE', len(lon))
-        nc.createDimension('LATITUDE', len(lat))
-        for name, vals, units in (('LONGITUDE', lon, 'degrees_east'), ('LATITUDE', lat, 'degrees_north')):
-            v = nc.createVariable(name, 'd', (name,))
-            v.units, v.long_name = units, name
-            v[:] = vals
-        t = nc.createVariable('TIME', 'd', ('TIME',))
-        t.units, t.long_name = time_unit, 'TIME'
-        self.var = nc.createVariable(varname, 'd', ('TIME', 'LATITUDE', 'LONGITUDE'))
-        self.var.missing_value = np.float64(missval)
+        self.nx, self.ny = len(lon), len(lat)
+        dims = [('TIME', 0), ('LONGITUDE', self.nx), ('LATITUDE', self.ny)]
+        head = b'CDF\x01' + struct.pack('>i', 0)  # magic, numrecs
+        head += struct.pack('>ii', 0x0A, len(dims)) + b''.join(_nc_name(n) + struct.pack('>i', l) for n, l in dims)
+        head += struct.pack('>ii', 0, 0)  # no global attributes
+        # (name, dimension ids, attributes, bytes per record or in all)
+        var_defs = [('LONGITUDE', [1], [('units', 'degrees_east'), ('long_name', 'LONGITUDE')], 8 * self.nx),
+                    ('LATITUDE', [2], [('units', 'degrees_north'), ('long_name', 'LATITUDE')], 8 * self.ny),
+                    ('TIME', [0], [('units', time_unit), ('long_name', 'TIME')], 8),
+                    (varname, [0, 2, 1], [('missing_value', missval)], 8 * self.nx * self.ny)]
+
+        def var_list(begins):
+            out = struct.pack('>ii', 0x0B, len(var_defs))
+            for (name, dimids, atts, vsize), begin in zip(var_defs, begins):
+                out += _nc_name(name) + struct.pack('>i', len(dimids)) + b''.join(struct.pack('>i', d) for d in dimids)
+                out += _nc_att_list(atts) + struct.pack('>iii', 6, vsize, begin)
+            return out
+
+        hlen = len(head) + len(var_list([0] * 4))
+        begins = [hlen, hlen + 8 * self.nx]
+        self.rec0 = begins[1] + 8 * self.ny
+        begins += [self.rec0, self.rec0 + 8]
+        self.recsize = 8 + 8 * self.nx * self.ny
+        self.f = open(path, 'wb')
+        self.f.write(head + var_list(begins))
+        self.f.write(np.asarray(lon, dtype='>f8').tobytes())
+        self.f.write(np.asarray(lat, dtype='>f8').tobytes())
+        self.f.flush()
         self.nrec = 0
         self._land = None  # the land mask of the first record's grid
 
@@ -78,15 +119,18 @@ class EulerFile:
                 self._land = ocean != 1
             np.copyto(d, self.missval, where=self._land)
         np.copyto(d, self.missval, where=~np.isfinite(d))
-        self.var[self.nrec] = d
-        self.nc.variables['TIME'][self.nrec] = time
+        self.f.seek(self.rec0 + self.nrec * self.recsize)
+        self.f.write(struct.pack('>d', float(time)))
+        self.f.write(d.astype('>f8').tobytes())
         self.nrec += 1
+        self.f.seek(4)
+        self.f.write(struct.pack('>i', self.nrec))
+        self.f.flush()
 
     def close(self):
-        if self.nc is not None:
-            self.nc.flush()
-            self.nc.close()
-            self.nc = None
+        if self.f is not None:
+            self.f.close()
+            self.f = None
 
 
 PAGE = 4096
