@@ -210,7 +210,11 @@ class AsyncWriter:
             return
         pool = self._pool((backend.ny, backend.nx), backend)
         buf = pool.free.get()  # waits while every buffer of the shape is in flight
-        ticket = backend.field_async(field, buf)
+        try:
+            ticket = backend.field_async(field, buf)
+        except Exception:
+            pool.free.put(buf)
+            raise
         self.submitted += 1
         self.from_device += 1
         self.q.put((backend, ticket, buf, pool, fh, time, ocean, records))
