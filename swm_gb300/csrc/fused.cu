@@ -472,7 +472,6 @@ int fused_prepare(swm_gpu_ctx *c) {
     bool nl_wind = s.type == SWM_FRC_WIND && cf.mode == SWM_MODE_NONLINEAR &&
                    (s.comp == SWM_CMP_ZONAL || s.comp == SWM_CMP_MERID);
     if (!nl_wind) {  // added to the forcing fields every step (dyn_forcing)
-      SWM_REQUIRE(s.type != SWM_FRC_EMF, "fused paths: time-dependent eddy momentum flux forcing runs on the plain path");
       f->dyn_F = true;
       continue;
     }
@@ -892,6 +891,49 @@ __global__ void k_stream_add(int n, int type, const double *d1, const double *d2
   F[k] = (T)((double)F[k] + a);
 }
 
+// a time-dependent eddy momentum flux stream's part of the step's forcing
+// (the divergence of the flux on the u and v points, as the plain path's
+// forcing update forms it: U2 into F_x, V2 into F_y, REY into both), in the
+// same FP64 arithmetic, added to the fused paths' forcing fields
+template <typename T>
+__global__ void k_stream_emf(Dev d, int comp, const double *__restrict__ dd, T *Fx, T *Fy) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x, j = blockIdx.y * blockDim.y + threadIdx.y;
+  const int nx = d.nx, ny = d.ny;
+  if (i >= nx || j >= ny) return;
+  auto ix = [nx](int ii, int jj) { return (size_t)ii + (size_t)nx * (size_t)jj; };
+  auto p1 = [](int a, int n) { return a + 1 == n ? 0 : a + 1; };
+  auto m1 = [](int a, int n) { return a == 0 ? n - 1 : a - 1; };
+  const size_t k = ix(i, j);
+  const double A = d.A;
+  const double *He = d.Hg[GE], *Hu = d.Hg[GU], *Hv = d.Hg[GV], *H = d.Hg[GH];
+  const double *cu = d.cosl[GU], *cv = d.cosl[GV];
+  const int8_t *oU = d.ocean[GU], *oV = d.ocean[GV];
+  // 4-point mean of dd from the H corners to the eta point (ii, jj)
+  auto h2eta = [&](int ii, int jj) {
+    return .25 * dd[ix(p1(ii, nx), p1(jj, ny))] + .25 * dd[ix(ii, jj)] + .25 * dd[ix(ii, p1(jj, ny))] +
+           .25 * dd[ix(p1(ii, nx), jj)];
+  };
+  if (comp == SWM_CMP_U2) {
+    if (oU[k] != 1) return;
+    const int im = m1(i, nx);
+    Fx[k] = (T)((double)Fx[k] +
+                (-(h2eta(i, j) * He[k] - h2eta(im, j) * He[ix(im, j)]) / (2 * A * d.dLambda * cu[j] * Hu[k])));
+  } else if (comp == SWM_CMP_V2) {
+    if (oV[k] != 1) return;
+    const int jm = m1(j, ny);
+    Fy[k] = (T)((double)Fy[k] + (-(cu[j] * He[k] * h2eta(i, j) - cu[jm] * He[ix(i, jm)] * h2eta(i, jm)) /
+                                  (8 * A * d.dTheta * cv[j] * Hv[k])));
+  } else {
+    const int jp = p1(j, ny), ip = p1(i, nx);
+    if (oU[k] == 1)
+      Fx[k] = (T)((double)Fx[k] + (-(cv[jp] * dd[ix(i, jp)] * H[ix(i, jp)] - cv[j] * dd[k] * H[k]) /
+                                    (2 * A * d.dTheta * cu[j] * Hu[k])));
+    if (oV[k] == 1)
+      Fy[k] = (T)((double)Fy[k] +
+                  (-(dd[ix(ip, j)] * H[ix(ip, j)] - dd[k] * H[k]) / (2 * A * d.dLambda * cv[j] * Hv[k])));
+  }
+}
+
 // the mean-state terms of the coming step into the forcing fields
 static int ms_terms(swm_gpu_ctx *c) {
   FusedState *f = c->fused;
@@ -939,6 +981,16 @@ static int dyn_forcing(swm_gpu_ctx *c, int64_t itt) {
     const Stream &st = c->streams[q];
     if (st.is_const) continue;
     if (st.type == SWM_FRC_WIND && nonlin) continue;  // recomputed by the step kernel
+    if (st.type == SWM_FRC_EMF) {
+      const Dev d = c->dev();
+      const dim3 b(32, 8), g((c->nx + 31) / 32, (c->ny + 7) / 8);
+      if (f->comp)
+        k_stream_emf<float><<<g, b, 0, c->stream>>>(d, st.comp, st.d1, (float *)f->F[0], (float *)f->F[1]);
+      else
+        k_stream_emf<double><<<g, b, 0, c->stream>>>(d, st.comp, st.d1, (double *)f->F[0], (double *)f->F[1]);
+      c->launches++;
+      continue;
+    }
     const int k = st.type == SWM_FRC_HEAT ? 2 : (st.comp == SWM_CMP_ZONAL ? 0 : (st.comp == SWM_CMP_MERID ? 1 : 2));
     const int g = k == 0 ? GU : (k == 1 ? GV : GE);
     const double *D = (st.type == SWM_FRC_WIND && c->cfg.barotropic) ? c->d_H[g] : nullptr;
