@@ -349,6 +349,10 @@ int swm_gpu_ensemble_create(swm_gpu_ctx *const *members, int n, swm_gpu_ensemble
     if (!c->march_rows) c->march_rows = 16;  // the ensemble tunes its own strip rows
     int rc = fused_prepare(c);
     if (rc != SWM_GPU_OK) return rc;
+    // the batched step reads each member's forcing fields as they are; a
+    // member whose forcing fields change every step is stepped on its own
+    SWM_REQUIRE(!fused_dynamic_forcing(c), "swm_gpu_ensemble_create: members with time-dependent forcing other "
+                                           "than the nonlinear wind stress are stepped on their own");
     int a, b;
     fused_indices(c, &a, &b);
     int mx = c->cfg.lateral_mixing ? (c->cfg.mixing_kind == SWM_MIX_BIHARMONIC ? 2 : 1) : 0;

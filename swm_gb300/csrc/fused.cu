@@ -1008,6 +1008,8 @@ static int dyn_forcing(swm_gpu_ctx *c, int64_t itt) {
   return SWM_GPU_OK;
 }
 
+bool fused_dynamic_forcing(const swm_gpu_ctx *c) { return c->fused && c->fused->dyn_F; }
+
 static int launch_fp32c(swm_gpu_ctx *c, int64_t itt) {
   P32 p;
   make_p32(c, itt, p);

@@ -182,6 +182,9 @@ int march_ens_launch(int mix, bool std_cfg, int pf, const P32 *tab, const int4 *
 // (hi, lo) cell-area pairs (3 x ny), for the ensemble's monitored steps
 int fused_monitor_inputs(swm_gpu_ctx *c, int comp, float **wind_rows, const float2 **area_pairs);
 bool march_std_params(const P32 &p);
+// the context's fused path rewrites its forcing fields every step (streams
+// other than the nonlinear wind stress, or the mean-state terms)
+bool fused_dynamic_forcing(const swm_gpu_ctx *c);
 int march_prefetch_level(size_t points, bool integ);
 // more bytes than the device's L2 holds
 bool exceeds_l2(double bytes);

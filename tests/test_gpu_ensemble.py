@@ -123,6 +123,20 @@ def test_ensemble_rejects_other_paths():
         GpuEnsemble(ms)
 
 
+def test_ensemble_rejects_members_with_per_step_forcing():
+    """A custom forcing stream with records that change in time makes the
+    member's forcing fields change every step, which the batched step does
+    not recompute: such a member is refused."""
+    cases = _cases(2)
+    ny, nx = cases[1]['config']['ny'], cases[1]['config']['nx']
+    recs = np.stack([np.full((ny, nx), 1e-7), np.full((ny, nx), 2e-7)])
+    cases[1]['streams'].append(dict(type=2, comp=0, omega=0.0, rec1=recs, dt1=900.0, chunksize=2, rec2=None,
+                                    dt2=0.0))
+    ms = _models(cases)
+    with pytest.raises(SwmGpuError, match='time-dependent forcing'):
+        GpuEnsemble(ms)
+
+
 @pytest.mark.parametrize('biharmonic', [False, True])
 def test_ensemble_monitor_matches_steps_and_integrals(biharmonic):
     """swm_gpu_ensemble_run_monitor (each step: every member's wind rows in,
