@@ -175,7 +175,7 @@ int swm_gpu_destroy(swm_gpu_ctx *c) {
   for (int q = 0; q < 2; q++) { F(c->u[q]); F(c->v[q]); F(c->eta[q]); F(c->gsq[q]); }
   for (int q = 0; q < 3; q++) { F(c->Gu[q]); F(c->Gv[q]); F(c->Ge[q]); F(c->impl[q]); F(c->glin[q]); F(c->F[q]); F(c->Fc[q]); }
   F(c->edens); F(c->pot); F(c->zeta); F(c->mu); F(c->mv); F(c->pll); F(c->plt); F(c->lmu); F(c->lmv);
-  F(c->ones); F(c->ubs); F(c->vbs); F(c->zbs); F(c->trc_coeff); F(c->rows_buf); F(c->march_tiles);
+  F(c->ones); F(c->latp[0]); F(c->latp[1]); F(c->latuv); F(c->ubs); F(c->vbs); F(c->zbs); F(c->trc_coeff); F(c->rows_buf); F(c->march_tiles);
   for (auto &s : c->streams) { F(s.d1); F(s.d2); F(s.rec[0]); F(s.rec[1]); }
   for (auto &t : c->tracers) {
     F(t.CH[0]); F(t.CH[1]); F(t.G[0]); F(t.G[1]); F(t.G[2]); F(t.C); F(t.C0); F(t.gamma); F(t.impl);
@@ -464,6 +464,7 @@ static bool graph_eligible(const swm_gpu_ctx *c) {
 static int graph_capture(swm_gpu_ctx *c, int64_t itt0) {
   invalidate_graph(c);
   if (c->cfg.path != SWM_PATH_PLAIN_FP64) TRY(fused_prepare(c));  // allocates on first use
+  else TRY(plain_prepare(c));
   const int n0 = c->n0, g0 = c->g0, phase = (int)(c->advances % GRAPH_STEPS);
   const int64_t l0 = c->launches;
   SWM_CK(cudaStreamBeginCapture(c->stream, cudaStreamCaptureModeThreadLocal));

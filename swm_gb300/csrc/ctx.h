@@ -139,6 +139,9 @@ struct swm_gpu_ctx {
   double *pll = nullptr, *plt = nullptr, *lmu = nullptr, *lmv = nullptr;
   double *bh[4] = {};    // biharmonic scratch (first-pass pll, plt, lu, lv)
   double *ones = nullptr;
+  // lateral-mixing coefficients of the plain path per row and mask case
+  // (plain.cu k_latmix_tab_*): for up to two values of Ah, and the uv table
+  double *latp[2] = {}, latp_ah[2] = {0., 0.}, *latuv = nullptr;
   double *impl[3] = {}, *gsq[2] = {}, *glin[3] = {};
   double *F[3] = {}, *Fc[3] = {};
   double *ubs = nullptr, *vbs = nullptr, *zbs = nullptr;
@@ -179,6 +182,7 @@ void host_damping_finish(swm_gpu_ctx *c);
 // plain.cu
 int plain_diagnostics(swm_gpu_ctx *c, int64_t itt);
 int plain_step(swm_gpu_ctx *c, int64_t itt);
+int plain_prepare(swm_gpu_ctx *c);                // tables the plain step reads (before a capture)
 int plain_forcing_update(swm_gpu_ctx *c, int64_t itt, int constant_part);
 int plain_fill(swm_gpu_ctx *c, double *p, double value);
 // tracer.cu

@@ -14,14 +14,19 @@ namespace swm {
 __device__ __forceinline__ int ip1(int i, int n) { return i + 1 == n ? 0 : i + 1; }
 __device__ __forceinline__ int im1(int i, int n) { return i == 0 ? n - 1 : i - 1; }
 
+// 1 / max(count, 1) for a count of ocean points 0..4: the reference's
+// division, taken from its correctly rounded values (1/3 is the constant the
+// division by 3 rounds to)
+__device__ __forceinline__ double inv_count(int n) { return n >= 4 ? .25 : (n == 3 ? 1. / 3. : (n == 2 ? .5 : 1.)); }
+
 // mask-normalised interpolation weights (calc_lib.f90:253-265, 320-335)
 __device__ __forceinline__ double ip2_noland(const double *v, const int8_t *m, size_t k1, size_t k2) {
-  double w = 1. / fmax((double)(m[k1] + m[k2]), 1.);
+  double w = inv_count(m[k1] + m[k2]);
   return ((double)m[k1] * w) * v[k1] + ((double)m[k2] * w) * v[k2];
 }
 __device__ __forceinline__ double ip4_noland(const double *v, const int8_t *m, size_t k1, size_t k2,
                                              size_t k3, size_t k4) {
-  double w = 1. / fmax((double)(m[k1] + m[k2] + m[k3] + m[k4]), 1.);
+  double w = inv_count(m[k1] + m[k2] + m[k3] + m[k4]);
   return ((double)m[k1] * w) * v[k1] + ((double)m[k2] * w) * v[k2] + ((double)m[k3] * w) * v[k3] +
          ((double)m[k4] * w) * v[k4];
 }
@@ -105,57 +110,94 @@ __global__ void k_massflux(Dev d) {
   if (d.ocean[GV][k] == 1) d.mv[k] = d.Dv[k] * d.v0[k];
 }
 
-// SWM_LateralMixing_compute_p (swm_lateralmixing_module.f90:215-240) with the
-// coefficients of _init_p_coefficients (:132-145) evaluated in place.
-__global__ void k_latmix_p(Dev d, double Ah, const double *u, const double *v, const double *Dp,
-                           const double *Dhp, double *pll, double *plt) {
+// Lateral-mixing coefficients of _init_p_coefficients (:132-145) and
+// lat_mixing_u/v (:84-97).  They depend on the row (cos and tan of the
+// latitude) and on two mask bits of the point, so they are formed once per
+// row and mask case by the same expressions, in the same order, and the
+// step kernels look them up: the values are bit for bit those formed per
+// point (this file is compiled without FMA contraction).
+constexpr int LATP_N = 14;  // pll: c0, c1[3], c2[3]; plt: c0, c1[3], c2[3]
+constexpr int LATUV_N = 10; // lu: c0, c1[2], c2[2]; lv: c0, c1[2], c2[2]
+
+// case of a coefficient that carries mask bit a (with neighbour bit b) in
+// the term a * tan / max(a + b, 1): 0 when a = 0, 1 + b otherwise
+__device__ __forceinline__ int latp_case(int a, int b) { return a ? 1 + b : 0; }
+
+__global__ void k_latmix_tab_p(Dev d, double Ah, double *tab) {
+  const int j = blockIdx.x * blockDim.x + threadIdx.x;
+  if (j >= d.ny) return;
+  const double A = d.A, bc = 1.;
+  double *T = tab + (size_t)LATP_N * j;
+  for (int q = 0; q < 3; q++) {  // mask cases (own bit, other bit): (0, 0), (1, 0), (1, 1)
+    const int8_t a = q > 0, b = q > 1;
+    {  // pll: c1 carries ovp (a), c2 carries ov (a)
+      const int o = a + b;
+      const double ot = (double)(o > 1 ? o : 1), tn = d.tanl[GE][j];
+      T[1 + q] = Ah / A * (bc / d.dTheta + a * tn / ot);
+      T[4 + q] = Ah / A * (-bc / d.dTheta + a * tn / ot);
+    }
+    {  // plt: c1 carries ou (a), c2 carries oum (a)
+      const int o = a + b;
+      const double ot = (double)(o > 1 ? o : 1), tn = d.tanl[GH][j];
+      T[8 + q] = -Ah / A * (bc / d.dTheta + a * tn / ot);
+      T[11 + q] = -Ah / A * (-bc / d.dTheta + a * tn / ot);
+    }
+  }
+  T[0] = -Ah * bc / d.dLambda / A / d.cosl[GE][j];
+  T[7] = -Ah * bc / d.dLambda / A / d.cosl[GH][j];
+}
+
+__global__ void k_latmix_tab_uv(Dev d, double *tab) {
+  const int j = blockIdx.x * blockDim.x + threadIdx.x;
+  if (j >= d.ny) return;
+  const double A = d.A, bc = 1.;
+  double *T = tab + (size_t)LATUV_N * j;
+  for (int q = 0; q < 2; q++) {  // ot = 1, 2
+    const double ot = (double)(q + 1);
+    const double tu = d.tanl[GU][j], tv = d.tanl[GV][j];
+    T[1 + q] = -(bc / A / d.dTheta - 2. * tu / A / ot);
+    T[3 + q] = -(-bc / A / d.dTheta - 2. * tu / A / ot);
+    T[6 + q] = -(-bc / A / d.dTheta + 2. * tv / A / ot);
+    T[8 + q] = -(bc / A / d.dTheta + 2. * tv / A / ot);
+  }
+  T[0] = -bc / A / d.cosl[GU][j] / d.dLambda;
+  T[5] = -bc / A / d.cosl[GV][j] / d.dLambda;
+}
+
+// SWM_LateralMixing_compute_p (swm_lateralmixing_module.f90:215-240), the
+// coefficients from the table of this Ah
+__global__ void k_latmix_p(Dev d, const double *__restrict__ tab, const double *u, const double *v,
+                           const double *Dp, const double *Dhp, double *pll, double *plt) {
   KERNEL_PROLOGUE
-  double A = d.A;
+  const double *T = tab + (size_t)LATP_N * j;
   if (d.ocean[GE][k] == 1) {
     size_t kjp = IDX(i, ip1(j, d.ny));
-    double bc = 1.;
     int8_t ov = d.ocean[GV][k], ovp = d.ocean[GV][kjp];
-    int o = ov + ovp;
-    double ot = (double)(o > 1 ? o : 1), tn = d.tanl[GE][j];
-    double c0 = -Ah * bc / d.dLambda / A / d.cosl[GE][j];
-    double c1 = Ah / A * (bc / d.dTheta + ovp * tn / ot);
-    double c2 = Ah / A * (-bc / d.dTheta + ov * tn / ot);
+    double c0 = T[0], c1 = T[1 + latp_case(ovp, ov)], c2 = T[4 + latp_case(ov, ovp)];
     pll[k] = Dp[k] * (c0 * (u[IDX(ip1(i, d.nx), j)] - u[k]) + c1 * v[kjp] + c2 * v[k]);
   }
   if (d.ocean[GH][k] == 1) {
     size_t kjm = IDX(i, im1(j, d.ny));
-    double bc = 1.;
     int8_t ou = d.ocean[GU][k], oum = d.ocean[GU][kjm];
-    int o = ou + oum;
-    double ot = (double)(o > 1 ? o : 1), tn = d.tanl[GH][j];
-    double c0 = -Ah * bc / d.dLambda / A / d.cosl[GH][j];
-    double c1 = -Ah / A * (bc / d.dTheta + ou * tn / ot);
-    double c2 = -Ah / A * (-bc / d.dTheta + oum * tn / ot);
+    double c0 = T[7], c1 = T[8 + latp_case(ou, oum)], c2 = T[11 + latp_case(oum, ou)];
     plt[k] = Dhp[k] * (c0 * (v[k] - v[IDX(im1(i, d.nx), j)]) + c1 * u[k] + c2 * u[kjm]);
   }
 }
 
-// SWM_LateralMixing_compute_uv (:162-186) with lat_mixing_u/v (:84-97)
-__global__ void k_latmix_uv(Dev d, const double *pll, const double *plt, const double *Dup,
-                            const double *Dvp, double *lu, double *lv) {
+// SWM_LateralMixing_compute_uv (:162-186) with lat_mixing_u/v (:84-97) from
+// the table
+__global__ void k_latmix_uv(Dev d, const double *__restrict__ tab, const double *pll, const double *plt,
+                            const double *Dup, const double *Dvp, double *lu, double *lv) {
   KERNEL_PROLOGUE
-  double A = d.A;
+  const double *T = tab + (size_t)LATUV_N * j;
   if (d.ocean[GU][k] == 1) {
-    double bc = 1., tn = d.tanl[GU][j];
-    int o = d.ocean[GH][k] + d.ocean[GH][IDX(i, ip1(j, d.ny))];
-    double ot = (double)(o > 1 ? o : 1);
-    double c0 = -bc / A / d.cosl[GU][j] / d.dLambda;
-    double c1 = -(bc / A / d.dTheta - 2. * tn / A / ot);
-    double c2 = -(-bc / A / d.dTheta - 2. * tn / A / ot);
+    const int q = d.ocean[GH][k] + d.ocean[GH][IDX(i, ip1(j, d.ny))] > 1;
+    double c0 = T[0], c1 = T[1 + q], c2 = T[3 + q];
     lu[k] = (c0 * (pll[k] - pll[IDX(im1(i, d.nx), j)]) + c1 * plt[IDX(i, ip1(j, d.ny))] + c2 * plt[k]) / Dup[k];
   }
   if (d.ocean[GV][k] == 1) {
-    double bc = 1., tn = d.tanl[GV][j];
-    int o = d.ocean[GE][k] + d.ocean[GE][IDX(i, im1(j, d.ny))];
-    double ot = (double)(o > 1 ? o : 1);
-    double c0 = -bc / A / d.cosl[GV][j] / d.dLambda;
-    double c1 = -(-bc / A / d.dTheta + 2. * tn / A / ot);
-    double c2 = -(bc / A / d.dTheta + 2. * tn / A / ot);
+    const int q = d.ocean[GE][k] + d.ocean[GE][IDX(i, im1(j, d.ny))] > 1;
+    double c0 = T[5], c1 = T[6 + q], c2 = T[8 + q];
     lv[k] = (c0 * (plt[IDX(ip1(i, d.nx), j)] - plt[k]) + c1 * pll[k] + c2 * pll[IDX(i, im1(j, d.ny))]) / Dvp[k];
   }
 }
@@ -382,20 +424,74 @@ int plain_forcing_update(swm_gpu_ctx *c, int64_t itt, int constant_part) {
   return SWM_GPU_OK;
 }
 
+// the coefficient table of k_latmix_p for this Ah (formed on first use)
+static int latp_table(swm_gpu_ctx *c, double Ah, const double **out) {
+  for (int q = 0; q < 2; q++)
+    if (c->latp[q] && c->latp_ah[q] == Ah) {
+      *out = c->latp[q];
+      return SWM_GPU_OK;
+    }
+  const int q = c->latp[0] ? 1 : 0;
+  SWM_REQUIRE(!c->latp[q], "lateral mixing: more than two mixing coefficients");
+  SWM_CK(cudaMalloc((void **)&c->latp[q], (size_t)LATP_N * c->ny * sizeof(double)));
+  c->latp_ah[q] = Ah;
+  k_latmix_tab_p<<<(c->ny + 127) / 128, 128, 0, c->stream>>>(c->dev(), Ah, c->latp[q]);
+  c->launches++;
+  SWM_CK(cudaGetLastError());
+  *out = c->latp[q];
+  return SWM_GPU_OK;
+}
+
+static int latuv_table(swm_gpu_ctx *c, const double **out) {
+  if (!c->latuv) {
+    SWM_CK(cudaMalloc((void **)&c->latuv, (size_t)LATUV_N * c->ny * sizeof(double)));
+    k_latmix_tab_uv<<<(c->ny + 127) / 128, 128, 0, c->stream>>>(c->dev(), c->latuv);
+    c->launches++;
+    SWM_CK(cudaGetLastError());
+  }
+  *out = c->latuv;
+  return SWM_GPU_OK;
+}
+
+#define PTRY(x)                          \
+  do {                                   \
+    int rc_ = (x);                       \
+    if (rc_ != SWM_GPU_OK) return rc_;   \
+  } while (0)
+
+// the coefficient tables the plain step needs, formed before a stream
+// capture records steps (they are allocated on first use)
+int plain_prepare(swm_gpu_ctx *c) {
+  if (!c->cfg.lateral_mixing) return SWM_GPU_OK;
+  const double *t = nullptr;
+  PTRY(latuv_table(c, &t));
+  if (c->cfg.mixing_kind == SWM_MIX_BIHARMONIC) {
+    PTRY(latp_table(c, 1., &t));
+    return latp_table(c, -c->cfg.bih, &t);
+  }
+  return latp_table(c, c->cfg.Ah, &t);
+}
+
 // SWM_timestep_step (swm_nonlinear_timestep_module.f90:164-180)
 int plain_step(swm_gpu_ctx *c, int64_t itt) {
   Dev d = c->dev();
   if (c->cfg.lateral_mixing) {
+    const double *tuv = nullptr, *tp = nullptr;
+    PTRY(latuv_table(c, &tuv));
     if (c->cfg.mixing_kind == SWM_MIX_BIHARMONIC) {
       // project extension: Laplacian-type operator with unit thickness and
       // Ah = 1, then the thickness-weighted operator with Ah = -bih
-      LAUNCH(k_latmix_p, d, 1., d.u0, d.v0, c->ones, c->ones, c->bh[0], c->bh[1]);
-      LAUNCH(k_latmix_uv, d, c->bh[0], c->bh[1], c->ones, c->ones, c->bh[2], c->bh[3]);
-      LAUNCH(k_latmix_p, d, -c->cfg.bih, c->bh[2], c->bh[3], d.D, d.Dh, d.pll, d.plt);
+      const double *t1 = nullptr;
+      PTRY(latp_table(c, 1., &t1));
+      PTRY(latp_table(c, -c->cfg.bih, &tp));
+      LAUNCH(k_latmix_p, d, t1, d.u0, d.v0, c->ones, c->ones, c->bh[0], c->bh[1]);
+      LAUNCH(k_latmix_uv, d, tuv, c->bh[0], c->bh[1], c->ones, c->ones, c->bh[2], c->bh[3]);
+      LAUNCH(k_latmix_p, d, tp, c->bh[2], c->bh[3], d.D, d.Dh, d.pll, d.plt);
     } else {
-      LAUNCH(k_latmix_p, d, c->cfg.Ah, d.u0, d.v0, d.D, d.Dh, d.pll, d.plt);
+      PTRY(latp_table(c, c->cfg.Ah, &tp));
+      LAUNCH(k_latmix_p, d, tp, d.u0, d.v0, d.D, d.Dh, d.pll, d.plt);
     }
-    LAUNCH(k_latmix_uv, d, d.pll, d.plt, d.Du, d.Dv, d.lmu, d.lmv);
+    LAUNCH(k_latmix_uv, d, tuv, d.pll, d.plt, d.Du, d.Dv, d.lmu, d.lmv);
   }
   LAUNCH(k_tend_eta, d);
   LAUNCH(k_tend_u, d);
