@@ -31,6 +31,13 @@ swm::Dev swm_gpu_ctx::dev() const {
   d.tau_scale = cfg.tau_scale;
   d.RHO0 = cfg.RHO0;
   d.lbc = cfg.lbc;
+  d.pdiv = pdiv ? 1 : 0;
+  d.r_dLambda = 1. / hg.dLambda;
+  d.r_dTheta = 1. / hg.dTheta;
+  d.AdT = cfg.A * hg.dTheta;
+  d.r_AdT = 1. / d.AdT;
+  d.prow = prow;
+  for (int q = 0; q < 3; q++) d.rimpl[q] = rimpl[q];
   for (int q = 0; q < 4; q++) {
     d.ocean[q] = d_ocean[q];
     d.cosl[q] = d_cos[q];
@@ -175,7 +182,8 @@ int swm_gpu_destroy(swm_gpu_ctx *c) {
   for (int q = 0; q < 2; q++) { F(c->u[q]); F(c->v[q]); F(c->eta[q]); F(c->gsq[q]); }
   for (int q = 0; q < 3; q++) { F(c->Gu[q]); F(c->Gv[q]); F(c->Ge[q]); F(c->impl[q]); F(c->glin[q]); F(c->F[q]); F(c->Fc[q]); }
   F(c->edens); F(c->pot); F(c->zeta); F(c->mu); F(c->mv); F(c->pll); F(c->plt); F(c->lmu); F(c->lmv);
-  F(c->ones); F(c->latp[0]); F(c->latp[1]); F(c->latuv); F(c->ubs); F(c->vbs); F(c->zbs); F(c->trc_coeff); F(c->rows_buf); F(c->march_tiles);
+  F(c->ones); F(c->latp[0]); F(c->latp[1]); F(c->latuv); F(c->prow); F(c->rimpl[0]); F(c->rimpl[1]);
+  F(c->rimpl[2]); F(c->pdiv_bad); F(c->ubs); F(c->vbs); F(c->zbs); F(c->trc_coeff); F(c->rows_buf); F(c->march_tiles);
   for (auto &s : c->streams) { F(s.d1); F(s.d2); F(s.rec[0]); F(s.rec[1]); }
   for (auto &t : c->tracers) {
     F(t.CH[0]); F(t.CH[1]); F(t.G[0]); F(t.G[1]); F(t.G[2]); F(t.C); F(t.C0); F(t.gamma); F(t.impl);

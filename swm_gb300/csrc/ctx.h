@@ -95,6 +95,12 @@ struct Tracer {
 struct Dev {
   int nx, ny, mode, qbf, barotropic, lateral_mixing, itt_is_zero;
   double dt, G, A, dLambda, dTheta, minD, tau_scale, RHO0, lbc;
+  // the plain path's divisions by fixed divisors (divide.cuh); pdiv 0: the
+  // division operator everywhere
+  int pdiv;
+  double r_dLambda, r_dTheta, AdT, r_AdT;  // 1/dLambda, 1/dTheta, A dTheta, 1/(A dTheta)
+  const double *prow;                      // PROW_N per row (plain.cu)
+  const double *rimpl[3];                  // 1 / impl_u, _v, _eta
   const int8_t *ocean[4];
   const double *cosl[4], *tanl[4], *f[4];
   double *Hg[4];  // H, H_u, H_v, H_eta on the device (H/H_u/H_v overwritten at itt=0 in linear modes)
@@ -142,6 +148,12 @@ struct swm_gpu_ctx {
   // lateral-mixing coefficients of the plain path per row and mask case
   // (plain.cu k_latmix_tab_*): for up to two values of Ah, and the uv table
   double *latp[2] = {}, latp_ah[2] = {0., 0.}, *latuv = nullptr;
+  // the plain path's fixed divisors and their reciprocals (plain_prepare):
+  // per row A cos_eta, A cos_u dLambda, cos_H and the vorticity factors;
+  // per point 1 / impl_u, _v, _eta; prow_ok: every divisor in div_fast's range
+  double *prow = nullptr, *rimpl[3] = {};
+  int *pdiv_bad = nullptr;
+  bool pdiv = false, pdiv_ready = false;
   double *impl[3] = {}, *gsq[2] = {}, *glin[3] = {};
   double *F[3] = {}, *Fc[3] = {};
   double *ubs = nullptr, *vbs = nullptr, *zbs = nullptr;

@@ -6,6 +6,7 @@
 // are unpadded (Nx, Ny); neighbour indices wrap periodically like the
 // reference's cshift index vectors (domain_module.f90:106-115).
 #include "ctx.h"
+#include "divide.cuh"
 
 namespace swm {
 
@@ -61,17 +62,55 @@ __global__ void k_D_interp(Dev d) {
   d.Dv[k] = dv;
 }
 
+// The plain path's fixed divisors per row (plain_prepare): PROW_N doubles,
+// the divisor and its reciprocal for A cos_eta (continuity), A cos_u dLambda
+// (zonal pressure gradient) and cos_H (vorticity), then the vorticity's
+// factors bc / (A cos_H dLambda) for bc = 1 and bc = lbc.  Divisions by them
+// go through div_fast (divide.cuh): the quotients are the division
+// operator's, bit for bit.
+constexpr int PROW_N = 8;
+
+__global__ void k_plain_rows(Dev d, double *prow, int *bad) {
+  const int j = blockIdx.x * blockDim.x + threadIdx.x;
+  if (j >= d.ny) return;
+  double *P = prow + (size_t)PROW_N * j;
+  const double bE = d.A * d.cosl[GE][j], bU = d.A * d.cosl[GU][j] * d.dLambda, cH = d.cosl[GH][j];
+  P[0] = bE; P[1] = 1. / bE;
+  P[2] = bU; P[3] = 1. / bU;
+  P[4] = cH; P[5] = 1. / cH;
+  P[6] = 1. / (d.A * d.cosl[GH][j] * d.dLambda);
+  P[7] = d.lbc / (d.A * d.cosl[GH][j] * d.dLambda);
+  if (!div_rn_range(bE) || !div_rn_range(bU) || !div_rn_range(cH)) atomicOr(bad, 1);
+}
+
+// 1 / impl per point; every point's impl in div_fast's range
+__global__ void k_plain_rimpl(Dev d, double *r0, double *r1, double *r2, int *bad) {
+  const size_t k = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (k >= (size_t)d.nx * d.ny) return;
+  const double a = d.impl_u[k], b = d.impl_v[k], e = d.impl_e[k];
+  r0[k] = 1. / a;
+  r1[k] = 1. / b;
+  r2[k] = 1. / e;
+  if (!div_rn_range(a) || !div_rn_range(b) || !div_rn_range(e)) atomicOr(bad, 1);
+}
+
 // computeRelVort -> vorticityFromVelocities2D (calc_lib.f90:663-678)
 __global__ void k_vorticity(Dev d) {
   KERNEL_PROLOGUE
   size_t ki = IDX(im1(i, d.nx), j), kj = IDX(i, im1(j, d.ny));
-  double bc = d.ocean[GH][k] == 1 ? 1. : d.lbc;
+  const bool ocean_h = d.ocean[GH][k] == 1;
+  double bc = ocean_h ? 1. : d.lbc;
+  const double *P = d.prow + (size_t)PROW_N * j;
   double dvdx, dudy;
   if (d.ocean[GV][ki] + d.ocean[GV][k] == 0) dvdx = 0.;
-  else dvdx = bc / (d.A * d.cosl[GH][j] * d.dLambda) * (d.v0[k] - d.v0[ki]);
-  if (d.ocean[GU][k] + d.ocean[GU][kj] == 0) dudy = 0.;
-  else dudy = bc * (d.cosl[GU][j] * d.u0[k] - d.cosl[GU][im1(j, d.ny)] * d.u0[kj]) / (d.A * d.dTheta);
-  d.zeta[k] = dvdx - dudy / d.cosl[GH][j];
+  else dvdx = (d.pdiv ? P[ocean_h ? 6 : 7] : bc / (d.A * d.cosl[GH][j] * d.dLambda)) * (d.v0[k] - d.v0[ki]);
+  if (d.ocean[GU][k] + d.ocean[GU][kj] == 0) {
+    dudy = 0.;
+  } else {
+    const double num = bc * (d.cosl[GU][j] * d.u0[k] - d.cosl[GU][im1(j, d.ny)] * d.u0[kj]);
+    dudy = d.pdiv ? div_fast(num, d.AdT, d.r_AdT) : num / (d.A * d.dTheta);
+  }
+  d.zeta[k] = dvdx - (d.pdiv ? div_fast(dudy, P[4], P[5]) : dudy / d.cosl[GH][j]);
 }
 
 // computePotVort (:230-257)
@@ -93,7 +132,7 @@ __global__ void k_edens(Dev d) {
   if (d.mode == SWM_MODE_NONLINEAR) {
     double a = .5 * (d.u0[ku] * d.u0[ku]) + .5 * (d.u0[k] * d.u0[k]);
     double b = .5 * (d.v0[kv] * d.v0[kv]) + .5 * (d.v0[k] * d.v0[k]);
-    d.edens[k] = (a + b) / 2. + d.G * d.eta0[k];
+    d.edens[k] = (a + b) * .5 + d.G * d.eta0[k];  // halving: the same rounding as / 2
   } else if (d.mode == SWM_MODE_LIN_MEAN) {
     double a = .5 * (d.u0[ku] * d.ubs[ku]) + .5 * (d.u0[k] * d.ubs[k]);
     double b = .5 * (d.v0[kv] * d.vbs[kv]) + .5 * (d.v0[k] * d.vbs[k]);
@@ -186,19 +225,23 @@ __global__ void k_latmix_p(Dev d, const double *__restrict__ tab, const double *
 
 // SWM_LateralMixing_compute_uv (:162-186) with lat_mixing_u/v (:84-97) from
 // the table
+// unit: the thicknesses are 1 (the biharmonic operator's first pass), and
+// x / 1 = x exactly
 __global__ void k_latmix_uv(Dev d, const double *__restrict__ tab, const double *pll, const double *plt,
-                            const double *Dup, const double *Dvp, double *lu, double *lv) {
+                            const double *Dup, const double *Dvp, double *lu, double *lv, int unit) {
   KERNEL_PROLOGUE
   const double *T = tab + (size_t)LATUV_N * j;
   if (d.ocean[GU][k] == 1) {
     const int q = d.ocean[GH][k] + d.ocean[GH][IDX(i, ip1(j, d.ny))] > 1;
     double c0 = T[0], c1 = T[1 + q], c2 = T[3 + q];
-    lu[k] = (c0 * (pll[k] - pll[IDX(im1(i, d.nx), j)]) + c1 * plt[IDX(i, ip1(j, d.ny))] + c2 * plt[k]) / Dup[k];
+    const double x = c0 * (pll[k] - pll[IDX(im1(i, d.nx), j)]) + c1 * plt[IDX(i, ip1(j, d.ny))] + c2 * plt[k];
+    lu[k] = unit ? x : x / Dup[k];
   }
   if (d.ocean[GV][k] == 1) {
     const int q = d.ocean[GE][k] + d.ocean[GE][IDX(i, im1(j, d.ny))] > 1;
     double c0 = T[5], c1 = T[6 + q], c2 = T[8 + q];
-    lv[k] = (c0 * (plt[IDX(ip1(i, d.nx), j)] - plt[k]) + c1 * pll[k] + c2 * pll[IDX(i, im1(j, d.ny))]) / Dvp[k];
+    const double x = c0 * (plt[IDX(ip1(i, d.nx), j)] - plt[k]) + c1 * pll[k] + c2 * pll[IDX(i, im1(j, d.ny))];
+    lv[k] = unit ? x : x / Dvp[k];
   }
 }
 
@@ -208,7 +251,9 @@ __global__ void k_tend_eta(Dev d) {
   if (d.ocean[GE][k] != 1) return;
   int ip = ip1(i, d.nx), jp = ip1(j, d.ny);
   const double *cV = d.cosl[GV];
-  double t = -(d.mu[IDX(ip, j)] - d.mu[k]) / d.dLambda - (d.mv[IDX(i, jp)] * cV[jp] - d.mv[k] * cV[j]) / d.dTheta;
+  auto dL = [&](double x) { return d.pdiv ? div_fast(x, d.dLambda, d.r_dLambda) : x / d.dLambda; };
+  auto dT = [&](double x) { return d.pdiv ? div_fast(x, d.dTheta, d.r_dTheta) : x / d.dTheta; };
+  double t = dL(-(d.mu[IDX(ip, j)] - d.mu[k])) - dT(d.mv[IDX(i, jp)] * cV[jp] - d.mv[k] * cV[j]);
   if (d.mode == SWM_MODE_LIN_MEAN) {
     const int8_t *oE = d.ocean[GE];
     int qi = ip1(j % d.nx, d.nx);  // ip1(j): zonal index taken from j in the reference (:360)
@@ -216,10 +261,10 @@ __global__ void k_tend_eta(Dev d) {
     double eb = ip2_noland(d.eta0, oE, k, IDX(im1(i, d.nx), j));
     double ec = ip2_noland(d.eta0, oE, IDX(i, jp), IDX(i, im1(jp, d.ny)));
     double ed = ip2_noland(d.eta0, oE, k, IDX(i, im1(j, d.ny)));
-    t = t - (ea * d.ubs[IDX(ip, j)] - eb * d.ubs[k]) / d.dLambda -
-        (cV[jp] * ec * d.vbs[IDX(i, jp)] - cV[j] * ed * d.vbs[k]) / d.dTheta;
+    t = t - dL(ea * d.ubs[IDX(ip, j)] - eb * d.ubs[k]) - dT(cV[jp] * ec * d.vbs[IDX(i, jp)] - cV[j] * ed * d.vbs[k]);
   }
-  d.Ge[2][k] = t / (d.A * d.cosl[GE][j]) + d.Fe[k];
+  const double *P = d.prow + (size_t)PROW_N * j;
+  d.Ge[2][k] = (d.pdiv ? div_fast(t, P[0], P[1]) : t / (d.A * d.cosl[GE][j])) + d.Fe[k];
 }
 
 // SWM_timestep_nonlinear, zonal momentum (:378-409)
@@ -230,7 +275,9 @@ __global__ void k_tend_u(Dev d) {
   size_t a1 = IDX(i, jp), a2 = IDX(im, j), a3 = IDX(im, jp);
   double g = ip2(d.pot, a1, k) * ip4(d.mv, a1, a2, a3, k);
   if (d.mode == SWM_MODE_LIN_MEAN) g = g + ip2(d.zeta, a1, k) * ip4(d.vbs, a1, a2, a3, k);
-  g = g - ((d.edens[k] - d.edens[IDX(im, j)]) / (d.A * d.cosl[GU][j] * d.dLambda));
+  const double *P = d.prow + (size_t)PROW_N * j;
+  const double de = d.edens[k] - d.edens[IDX(im, j)];
+  g = g - (d.pdiv ? div_fast(de, P[2], P[3]) : de / (d.A * d.cosl[GU][j] * d.dLambda));
   if (d.qbf) {
     double vv = ip4(d.v0, a1, a2, a3, k);
     double q = d.gsq_u[k] * sqrt(d.u0[k] * d.u0[k] + (vv * vv)) * d.u0[k];
@@ -249,7 +296,8 @@ __global__ void k_tend_v(Dev d) {
   size_t a1 = IDX(ip, j), a2 = IDX(i, jm), a4 = IDX(ip, jm);
   double g = -ip2(d.pot, a1, k) * ip4(d.mu, a1, a2, k, a4);
   if (d.mode == SWM_MODE_LIN_MEAN) g = g - ip2(d.zeta, a1, k) * ip4(d.ubs, a1, a2, k, a4);
-  g = g - ((d.edens[k] - d.edens[IDX(i, jm)]) / (d.A * d.dTheta));
+  const double de = d.edens[k] - d.edens[IDX(i, jm)];
+  g = g - (d.pdiv ? div_fast(de, d.AdT, d.r_AdT) : de / (d.A * d.dTheta));
   if (d.qbf) {
     double uu = ip4(d.u0, a1, a2, k, a4);
     double q = d.gsq_v[k] * sqrt(d.v0[k] * d.v0[k] + (uu * uu)) * d.v0[k];
@@ -275,14 +323,14 @@ __global__ void k_integrate(Dev d, ABCoef ab) {
     b = b + d.dt * ab.c[t] * d.Gu[t][k];
     c = c + d.dt * ab.c[t] * d.Gv[t][k];
   }
-  a = a / d.impl_e[k];
+  a = d.pdiv ? div_fast(a, d.impl_e[k], d.rimpl[2][k]) : a / d.impl_e[k];
   if (d.mode == SWM_MODE_NONLINEAR) {
     double lim = d.minD - d.Hg[GE][k];
     if (a < lim) a = lim;
   }
   d.eta1[k] = a;
-  d.u1[k] = b / d.impl_u[k];
-  d.v1[k] = c / d.impl_v[k];
+  d.u1[k] = d.pdiv ? div_fast(b, d.impl_u[k], d.rimpl[0][k]) : b / d.impl_u[k];
+  d.v1[k] = d.pdiv ? div_fast(c, d.impl_v[k], d.rimpl[1][k]) : c / d.impl_v[k];
 }
 
 // SWM_forcing_update reset (swm_forcing_module.f90:141-149)
@@ -462,6 +510,27 @@ static int latuv_table(swm_gpu_ctx *c, const double **out) {
 // the coefficient tables the plain step needs, formed before a stream
 // capture records steps (they are allocated on first use)
 int plain_prepare(swm_gpu_ctx *c) {
+  if (!c->pdiv_ready && !(c->impl[0] && c->impl[1] && c->impl[2])) {
+    c->pdiv = false;  // no damping factors yet: the division operator
+  } else if (!c->pdiv_ready) {
+    const size_t n = c->n;
+    SWM_CK(cudaMalloc((void **)&c->prow, (size_t)PROW_N * c->ny * sizeof(double)));
+    for (int q = 0; q < 3; q++) SWM_CK(cudaMalloc((void **)&c->rimpl[q], n * sizeof(double)));
+    SWM_CK(cudaMalloc((void **)&c->pdiv_bad, sizeof(int)));
+    SWM_CK(cudaMemsetAsync(c->pdiv_bad, 0, sizeof(int), c->stream));
+    const Dev d = c->dev();
+    k_plain_rows<<<(c->ny + 127) / 128, 128, 0, c->stream>>>(d, c->prow, c->pdiv_bad);
+    k_plain_rimpl<<<(unsigned)((n + 255) / 256), 256, 0, c->stream>>>(d, c->rimpl[0], c->rimpl[1], c->rimpl[2],
+                                                                   c->pdiv_bad);
+    c->launches += 2;
+    SWM_CK(cudaGetLastError());
+    int bad = 0;
+    SWM_CK(cudaMemcpyAsync(&bad, c->pdiv_bad, sizeof(int), cudaMemcpyDeviceToHost, c->stream));
+    SWM_CK(cudaStreamSynchronize(c->stream));
+    c->pdiv = !bad && div_host_range(c->hg.dLambda) && div_host_range(c->hg.dTheta) &&
+              div_host_range(c->cfg.A * c->hg.dTheta);
+    c->pdiv_ready = true;
+  }
   if (!c->cfg.lateral_mixing) return SWM_GPU_OK;
   const double *t = nullptr;
   PTRY(latuv_table(c, &t));
@@ -474,6 +543,7 @@ int plain_prepare(swm_gpu_ctx *c) {
 
 // SWM_timestep_step (swm_nonlinear_timestep_module.f90:164-180)
 int plain_step(swm_gpu_ctx *c, int64_t itt) {
+  PTRY(plain_prepare(c));
   Dev d = c->dev();
   if (c->cfg.lateral_mixing) {
     const double *tuv = nullptr, *tp = nullptr;
@@ -485,13 +555,13 @@ int plain_step(swm_gpu_ctx *c, int64_t itt) {
       PTRY(latp_table(c, 1., &t1));
       PTRY(latp_table(c, -c->cfg.bih, &tp));
       LAUNCH(k_latmix_p, d, t1, d.u0, d.v0, c->ones, c->ones, c->bh[0], c->bh[1]);
-      LAUNCH(k_latmix_uv, d, tuv, c->bh[0], c->bh[1], c->ones, c->ones, c->bh[2], c->bh[3]);
+      LAUNCH(k_latmix_uv, d, tuv, c->bh[0], c->bh[1], c->ones, c->ones, c->bh[2], c->bh[3], 1);
       LAUNCH(k_latmix_p, d, tp, c->bh[2], c->bh[3], d.D, d.Dh, d.pll, d.plt);
     } else {
       PTRY(latp_table(c, c->cfg.Ah, &tp));
       LAUNCH(k_latmix_p, d, tp, d.u0, d.v0, d.D, d.Dh, d.pll, d.plt);
     }
-    LAUNCH(k_latmix_uv, d, tuv, d.pll, d.plt, d.Du, d.Dv, d.lmu, d.lmv);
+    LAUNCH(k_latmix_uv, d, tuv, d.pll, d.plt, d.Du, d.Dv, d.lmu, d.lmv, 0);
   }
   LAUNCH(k_tend_eta, d);
   LAUNCH(k_tend_u, d);

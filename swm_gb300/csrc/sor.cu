@@ -37,6 +37,7 @@
 #include <string>
 #include <vector>
 #include "ctx.h"
+#include "divide.cuh"
 
 // device control block of a solve
 struct SorCtl {
@@ -102,30 +103,6 @@ __global__ void k_sor_split(double *nat, double *s0, double *s1, int nx, int ny,
   const size_t q = (size_t)j * W + (i >> 1);
   if (join) nat[k] = sp[q];
   else sp[q] = nat[k];
-}
-
-// a / b rounded to nearest from y = 1/b rounded to nearest, by Markstein's
-// theorem (P. Markstein, "Computation of elementary functions on the IBM
-// RISC System/6000 processor", IBM J. Res. Dev. 34, 1990; also Muller et
-// al., Handbook of Floating-Point Arithmetic, the FMA-based division
-// section): if y is within half an ulp of 1/b and q within one ulp of a/b,
-// then q + (a - b q) y, each operation rounded to nearest and the remainder
-// taken with one FMA, is a/b rounded to nearest.  q = a y can be up to 1.5
-// ulp off, so a first correction brings it within an ulp and the second
-// gives the rounded quotient.  Valid while no step underflows or overflows:
-// for a and b with binary exponents in [-500, 500] (div_rn_range).
-__device__ __forceinline__ double div_rn(double a, double b, double y) {
-  double q = __dmul_rn(a, y);
-  double r = __fma_rn(-q, b, a);
-  q = __fma_rn(r, y, q);
-  r = __fma_rn(-q, b, a);
-  return __fma_rn(r, y, q);
-}
-
-// x is finite, nonzero, normal and of binary exponent in [-500, 500]
-__device__ __forceinline__ bool div_rn_range(double x) {
-  const unsigned e = ((unsigned)__double2hiint(x) >> 20) & 0x7ffu;
-  return e - 523u <= 1000u;
 }
 
 // set-up: the reciprocal diagonal and the split ocean mask of colour col;
