@@ -20,16 +20,18 @@ __device__ __forceinline__ int im1(int i, int n) { return i == 0 ? n - 1 : i - 1
 // division by 3 rounds to)
 __device__ __forceinline__ double inv_count(int n) { return n >= 4 ? .25 : (n == 3 ? 1. / 3. : (n == 2 ? .5 : 1.)); }
 
-// mask-normalised interpolation weights (calc_lib.f90:253-265, 320-335)
+// mask-normalised interpolation weights (calc_lib.f90:253-265, 320-335):
+// the mask (0 or 1) times the weight is the weight or +0, as the product
+// rounds, taken by a select
+__device__ __forceinline__ double mw(int8_t m, double w) { return m ? w : 0.; }
 __device__ __forceinline__ double ip2_noland(const double *v, const int8_t *m, size_t k1, size_t k2) {
   double w = inv_count(m[k1] + m[k2]);
-  return ((double)m[k1] * w) * v[k1] + ((double)m[k2] * w) * v[k2];
+  return mw(m[k1], w) * v[k1] + mw(m[k2], w) * v[k2];
 }
 __device__ __forceinline__ double ip4_noland(const double *v, const int8_t *m, size_t k1, size_t k2,
                                              size_t k3, size_t k4) {
   double w = inv_count(m[k1] + m[k2] + m[k3] + m[k4]);
-  return ((double)m[k1] * w) * v[k1] + ((double)m[k2] * w) * v[k2] + ((double)m[k3] * w) * v[k3] +
-         ((double)m[k4] * w) * v[k4];
+  return mw(m[k1], w) * v[k1] + mw(m[k2], w) * v[k2] + mw(m[k3], w) * v[k3] + mw(m[k4], w) * v[k4];
 }
 __device__ __forceinline__ double ip2(const double *v, size_t k1, size_t k2) { return .5 * v[k1] + .5 * v[k2]; }
 __device__ __forceinline__ double ip4(const double *v, size_t k1, size_t k2, size_t k3, size_t k4) {
