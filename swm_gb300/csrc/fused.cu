@@ -141,7 +141,7 @@ __global__ void __launch_bounds__(NT) k_fused(FP<T> p) {
       if (ti < TX + HALO - 1 && tj < TY + HALO - 1 && oE(q)) {  // needs (i+1, j), (i, j+1)
         const T *r = row(tj);
         int ov = oV(q), ovp = oV(q + W);
-        T tE = r[R_TE] / T(max(ov + ovp, 1));
+        T tE = r[R_TE] * recip_cnt<T>(ov + ovp);  // counts 0..2: exactly the division
         T c0 = Ah * r[R_PC0];
         T c1 = Ah * (p.q1 + T(ovp) * tE);
         T c2 = Ah * (-p.q1 + T(ov) * tE);
@@ -150,7 +150,7 @@ __global__ void __launch_bounds__(NT) k_fused(FP<T> p) {
       if (ti > -HALO && tj > -HALO && oH(q)) {  // needs (i-1, j), (i, j-1)
         const T *r = row(tj);
         int ou = oU(q), oum = oU(q - W);
-        T tH = r[R_TH] / T(max(ou + oum, 1));
+        T tH = r[R_TH] * recip_cnt<T>(ou + oum);
         T c0 = Ah * r[R_HC0];
         T c1 = -Ah * (p.q1 + T(ou) * tH);
         T c2 = -Ah * (-p.q1 + T(oum) * tH);
@@ -164,7 +164,7 @@ __global__ void __launch_bounds__(NT) k_fused(FP<T> p) {
   auto lat_u = [&](int q, int tj, bool weighted) {
     const T *r = row(tj);
     int o = oH(q) + oH(q + W);
-    T t2 = T(2) * r[R_TU] / T(max(o, 1));
+    T t2 = T(2) * r[R_TU] * recip_cnt<T>(o);
     T m0 = -r[R_RU_DL], m1 = -(p.q1 - t2), m2 = p.q1 + t2;
     T s = m0 * (sPLL[q] - sPLL[q - 1]) + m1 * sPLT[q + W] + m2 * sPLT[q];
     return weighted ? s / Du_at(q) : s;
@@ -172,7 +172,7 @@ __global__ void __launch_bounds__(NT) k_fused(FP<T> p) {
   auto lat_v = [&](int q, int tj, bool weighted) {
     const T *r = row(tj);
     int o = oE(q) + oE(q - W);
-    T t2 = T(2) * r[R_TV] / T(max(o, 1));
+    T t2 = T(2) * r[R_TV] * recip_cnt<T>(o);
     T m0 = -r[R_RV_DL], m1 = p.q1 - t2, m2 = -(p.q1 + t2);
     T s = m0 * (sPLT[q + 1] - sPLT[q]) + m1 * sPLL[q] + m2 * sPLL[q - W];
     return weighted ? s / Dv_at(q) : s;

@@ -312,6 +312,7 @@ __global__ void k_tend_v(Dev d) {
 
 struct ABCoef {
   double c[3];
+  double dtc[3];  // dt * c[t], the product the reference forms first (host, the same rounding)
   int tstep;
 };
 
@@ -321,9 +322,9 @@ __global__ void k_integrate(Dev d, ABCoef ab) {
   KERNEL_PROLOGUE
   double a = d.eta0[k], b = d.u0[k], c = d.v0[k];
   for (int t = 0; t < ab.tstep; t++) {
-    a = a + d.dt * ab.c[t] * d.Ge[t][k];
-    b = b + d.dt * ab.c[t] * d.Gu[t][k];
-    c = c + d.dt * ab.c[t] * d.Gv[t][k];
+    a = a + ab.dtc[t] * d.Ge[t][k];
+    b = b + ab.dtc[t] * d.Gu[t][k];
+    c = c + ab.dtc[t] * d.Gv[t][k];
   }
   a = d.pdiv ? div_fast(a, d.impl_e[k], d.rimpl[2][k]) : a / d.impl_e[k];
   if (d.mode == SWM_MODE_NONLINEAR) {
@@ -572,7 +573,10 @@ int plain_step(swm_gpu_ctx *c, int64_t itt) {
   ab.tstep = (int)(itt < 3 ? itt : 3);
   const double chi = c->cfg.ab_chi;
   double tab[4][3] = {{0, 0, 0}, {1., 0, 0}, {-0.5 - chi, 1.5 + chi, 0}, {5. / 12., -16. / 12., 23. / 12.}};
-  for (int q = 0; q < 3; q++) ab.c[q] = tab[ab.tstep][q];
+  for (int q = 0; q < 3; q++) {
+    ab.c[q] = tab[ab.tstep][q];
+    ab.dtc[q] = c->cfg.dt * ab.c[q];
+  }
   LAUNCH(k_integrate, d, ab);
   SWM_CK(cudaGetLastError());
   return SWM_GPU_OK;
