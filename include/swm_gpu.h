@@ -316,11 +316,14 @@ int elsolv_sor_gpu_solve(swm_gpu_ctx *ctx, const double *B, double *chi, double 
    dTheta).  Outputs may be NULL. */
 int swm_gpu_nondivergent(swm_gpu_ctx *ctx, int first_guess, double eps, double *u_nd, double *v_nd, double *chi,
                          int *iterations);
-/* Self-check of the half-sweep's division (a / b formed from the reciprocal
-   of b by two Markstein corrections) against the division operator, on n
-   pseudo-random pairs from seed over the exponent range the half-sweep uses
-   it for, special significands included; *mismatches counts the pairs whose
-   quotients differ in any bit.  Runs on the current device and waits. */
+/* Self-check of the division by a fixed divisor that the SOR half-sweep
+   and the plain path use (a / b formed from the reciprocal of b by two
+   Markstein corrections, other numerators by exact branches) against the
+   division operator, on n pseudo-random pairs from seed: divisors over the
+   exponent range it is used for, special significands and numerators
+   outside that range included; *mismatches counts the pairs whose quotients
+   differ in any bit (two NaNs count as equal).  Runs on the current device
+   and waits. */
 int swm_gpu_check_division(int64_t n, int64_t seed, int64_t *mismatches);
 
 /* ---- variable-coefficient Helmholtz solver (extension of ElSolv_SOR) ----

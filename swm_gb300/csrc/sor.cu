@@ -241,7 +241,9 @@ __global__ void k_sor_nondiv(Dev d, const double *chi, const double *u, const do
 
 // the pair of k_div_check's sample k: splitmix64 bits; one pair in four
 // takes a special significand (all ones, all zeros, or one of them with the
-// lowest bits flipped) for a, b or both
+// lowest bits flipped) for a, b or both; one numerator in eight lies
+// outside div_rn's range (zeros, subnormal, tiny, huge, infinite, NaN), so
+// div_fast's other branches are checked too
 __device__ uint64_t mix64(uint64_t z) {
   z += 0x9e3779b97f4a7c15ull;
   z = (z ^ (z >> 30)) * 0xbf58476d1ce4e5b9ull;
@@ -266,10 +268,18 @@ __global__ void k_div_check(int64_t n, uint64_t seed, unsigned long long *bad) {
     const uint64_t h = mix64(seed ^ mix64((uint64_t)k));
     const uint64_t r[4] = {mix64(h + 1), mix64(h + 2), mix64(h + 3), mix64(h + 4)};
     const int sp = (int)(h & 15);  // 0, 1, 2: special a, b, both
-    const double a = sample_operand(r[0], r[1], sp == 0 || sp == 2);
+    double a = sample_operand(r[0], r[1], sp == 0 || sp == 2);
     const double b = sample_operand(r[2], r[3], sp == 1 || sp == 2);
-    const double q = __ddiv_rn(a, b), y = __ddiv_rn(1., b);
-    mism += __double_as_longlong(div_rn(a, b, y)) != __double_as_longlong(q);
+    if (((h >> 4) & 7) == 0) {  // one sample in eight: a numerator outside div_rn's range
+      const uint64_t sign = (r[1] >> 41) & 1, man = r[0] & 0xfffffffffffffull;
+      const uint64_t lo = 1 + (r[1] >> 16) % 522, hi = 1524 + (r[1] >> 16) % 523;  // exponent fields
+      const uint64_t bits[8] = {0, 0, man, lo << 52 | man, hi << 52 | man, 0x7ffull << 52, 0x7ffull << 52,
+                                0x7ffull << 52 | 1};  // +-0, subnormal, tiny, huge, inf, inf, NaN
+      a = __longlong_as_double((long long)((sign << 63) | bits[(h >> 7) & 7]));
+    }
+    const double q = __ddiv_rn(a, b), y = __ddiv_rn(1., b), f = div_fast(a, b, y);
+    const bool same = __double_as_longlong(f) == __double_as_longlong(q) || (q != q && f != f);
+    mism += !same;
   }
   for (int o = 16; o > 0; o >>= 1) mism += __shfl_down_sync(0xffffffffu, mism, o);
   if ((threadIdx.x & 31) == 0 && mism) atomicAdd(bad, mism);

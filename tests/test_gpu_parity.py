@@ -114,10 +114,12 @@ def test_sor_matches_oracle(shape):
 
 
 def test_sor_division_is_correctly_rounded():
-    """The half-sweep divides by the diagonal through its reciprocal and two
-    Markstein corrections; on 2^26 pairs over the exponent range it serves
-    (all-ones and power-of-two significands among them) the quotient equals
-    the division operator's in every bit."""
+    """The SOR half-sweep and the plain path divide by fixed divisors through
+    their reciprocals and two Markstein corrections (div_fast); on 2^26 pairs
+    per seed (divisors over the exponent range it serves, all-ones and
+    power-of-two significands among them; one numerator in eight zero,
+    subnormal, tiny, huge, infinite or NaN) the quotient equals the division
+    operator's in every bit."""
     from swm_gb300 import _lib
     import ctypes
     lib = _lib.lib()
