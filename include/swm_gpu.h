@@ -194,6 +194,10 @@ int swm_gpu_run_monitor(swm_gpu_ctx *ctx, int64_t itt0, int64_t nsteps, int stre
 
 /* ---- host access (the registry pointers the diagnostics read) ---- */
 int swm_gpu_get_field(swm_gpu_ctx *ctx, int field, double *host_out);
+/* swm_gpu_set_field: the state (u, v, eta) at any time; static fields
+   (depths, damping and drag factors, constant forcing, basic state) at any
+   time on the plain path, and before the first step on the fused paths
+   (SWM_GPU_EINVAL afterwards: those paths keep their own copies). */
 int swm_gpu_set_field(swm_gpu_ctx *ctx, int field, const double *host_in);
 /* Output without stalling the time loop (for a writer thread; the reference
    writes its diagnostics synchronously, io_module.f90:504-529): the copy of

@@ -775,9 +775,18 @@ int swm_gpu_set_field(swm_gpu_ctx *c, int f, const double *in) {
   double *p = nullptr;
   field_ptr(c, f, &p);
   SWM_REQUIRE(p, "swm_gpu_set_field: unknown field or not allocated");
+  // static fields (depths, damping, drag, constant forcing, basic state)
+  // that the fused paths copied when they set up their own state
+  const bool static_field = (f >= SWM_F_H && f <= SWM_F_FETA) || (f >= SWM_F_U_BS && f <= SWM_F_ZETA_BS);
+  SWM_REQUIRE(!(static_field && c->cfg.path != SWM_PATH_PLAIN_FP64 && c->fused),
+              "swm_gpu_set_field: on the fused paths, set static fields before the first step");
   TRY(h2d(c, p, in, c->n));
   SWM_CK(cudaStreamSynchronize(c->stream));
   if (c->cfg.path != SWM_PATH_PLAIN_FP64 && c->stage >= 5 && f <= SWM_F_ETA) TRY(fused_load_state(c));
+  if (f == SWM_F_IMPL_U || f == SWM_F_IMPL_V || f == SWM_F_IMPL_ETA) {
+    c->pdiv_ready = false;  // the plain path's reciprocals of the damping factors are formed again
+    invalidate_graph(c);
+  }
   return SWM_GPU_OK;
 }
 

@@ -517,9 +517,10 @@ int plain_prepare(swm_gpu_ctx *c) {
     c->pdiv = false;  // no damping factors yet: the division operator
   } else if (!c->pdiv_ready) {
     const size_t n = c->n;
-    SWM_CK(cudaMalloc((void **)&c->prow, (size_t)PROW_N * c->ny * sizeof(double)));
-    for (int q = 0; q < 3; q++) SWM_CK(cudaMalloc((void **)&c->rimpl[q], n * sizeof(double)));
-    SWM_CK(cudaMalloc((void **)&c->pdiv_bad, sizeof(int)));
+    if (!c->prow) SWM_CK(cudaMalloc((void **)&c->prow, (size_t)PROW_N * c->ny * sizeof(double)));
+    for (int q = 0; q < 3; q++)
+      if (!c->rimpl[q]) SWM_CK(cudaMalloc((void **)&c->rimpl[q], n * sizeof(double)));
+    if (!c->pdiv_bad) SWM_CK(cudaMalloc((void **)&c->pdiv_bad, sizeof(int)));
     SWM_CK(cudaMemsetAsync(c->pdiv_bad, 0, sizeof(int), c->stream));
     const Dev d = c->dev();
     k_plain_rows<<<(c->ny + 127) / 128, 128, 0, c->stream>>>(d, c->prow, c->pdiv_bad);

@@ -166,3 +166,26 @@ def test_nondivergent_flow_matches_oracle():
     ug, vg, _, _, rc = g.nondivergent(True)
     assert rc == 0
     assert np.abs(o.divergence(ug, vg)[inner]).sum() < 0.5 * d0
+
+
+def test_damping_factors_set_during_a_run():
+    """impl_u set between steps: the plain path forms the reciprocals of its
+    damping factors again (and drops its step graph), so the run stays bit
+    for bit with the oracle given the same field; the fused paths, which
+    keep their own copies, refuse static fields once they have stepped."""
+    from swm_gb300 import SwmGpuError
+    case = synthetic.double_gyre((40, 32), biharmonic=False, nsteps=60)
+    o, g = _pair(case, 20)
+    impl = o.field('impl_u') * 1.5
+    o.set_field('impl_u', impl)
+    g.set_field('impl_u', impl)
+    o.run_steady(15)
+    g.run(20, 15)  # long enough for a graph replay
+    for f in STATE:
+        assert np.array_equal(o.field(f), g.field(f)), f
+    f32 = GpuModel('fused_fp32c')
+    run_case(case, f32, nsteps=3, with_diag=False)
+    with pytest.raises(SwmGpuError, match='before the first step'):
+        f32.set_field('impl_u', impl)
+    f32.close()
+    g.close()
