@@ -178,3 +178,51 @@ def test_l2_prefetch_does_not_change_results(variant, monkeypatch):
         for a, b in zip(fields[0][:3], other[:3]):
             assert np.array_equal(a, b)
         assert np.all(np.abs(fields[0][3] - other[3]) <= 1e-12 * scale)
+
+
+TINY = [(6, 5), (9, 4), (31, 7), (33, 9), (65, 3), (4, 40)]
+
+
+@pytest.mark.parametrize('path,tol', [('plain_fp64', 0.0), ('fused_fp64', 1e-11), ('fused_fp32c', 1e-5)])
+def test_tiny_and_narrow_basins(path, tol):
+    """Basins narrower than a strip or a tile (4 to 65 cells wide, 3 to 40
+    rows), where halos wrap around the whole basin and most cells are
+    coast: every path against the oracle after 30 steps."""
+    from harness import rel_l2
+    for shape in TINY:
+        case = synthetic.double_gyre(shape, biharmonic=True, nsteps=30)
+        o = OracleBackend()
+        run_case(case, o, nsteps=30, with_diag=False)
+        g = GpuModel(path)
+        run_case(case, g, nsteps=30, with_diag=False)
+        for f in ('u', 'v', 'eta'):
+            if tol == 0.0:
+                assert np.array_equal(g.field(f), o.field(f)), (shape, f)
+            else:
+                m = o.ocean(f).astype(bool)
+                assert rel_l2(g.field(f), o.field(f), m) <= tol, (shape, f, rel_l2(g.field(f), o.field(f), m))
+        g.close()
+
+
+def test_tiny_basins_batched():
+    """The same tiny and narrow basins as ensemble members, against each
+    member stepped alone on the single-basin FP32 path."""
+    from harness import rel_l2
+    from swm_gb300.model import GpuEnsemble
+    from swm_gb300.host.driver import Driver
+    cases = [synthetic.double_gyre(s, biharmonic=True, nsteps=40) for s in TINY]
+    batched, alone = [], []
+    for c in cases:
+        for lst in (batched, alone):
+            g = GpuModel('fused_fp32c')
+            Driver(c, g).init(with_diag=False)
+            lst.append(g)
+    ens = GpuEnsemble(batched)
+    ens.run(0, 30)
+    ens.synchronize()
+    for a, b in zip(batched, alone):
+        b.run(0, 30)
+        for f in ('u', 'v', 'eta'):
+            m = b.ocean(f).astype(bool)
+            assert rel_l2(a.field(f), b.field(f), m) <= 1e-6, f
+    ens.close()
