@@ -105,6 +105,10 @@ typedef struct swm_gpu_ctx swm_gpu_ctx;
 const char *swm_gpu_last_error(void);
 int swm_gpu_create(const swm_gpu_config *cfg, swm_gpu_ctx **out);
 int swm_gpu_destroy(swm_gpu_ctx *ctx);
+/* waits for the context's stream; SWM_GPU_EDEVICE when a step kernel that
+   stages its rows by bulk asynchronous copies (SWM_GB300_MARCH_PREFETCH=3)
+   gave up waiting for a row (the same holds for
+   swm_gpu_ensemble_synchronize) */
 int swm_gpu_synchronize(swm_gpu_ctx *ctx);
 /* the CUDA stream (cudaStream_t) every call of this context runs on */
 void *swm_gpu_stream(swm_gpu_ctx *ctx);

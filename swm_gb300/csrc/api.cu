@@ -199,7 +199,7 @@ int swm_gpu_synchronize(swm_gpu_ctx *c) {
   SWM_ON_DEVICE(c ? c->device : -1);
   SWM_REQUIRE(c, "null context");
   SWM_CK(cudaStreamSynchronize(c->stream));
-  return SWM_GPU_OK;
+  return march_ring_check();
 }
 
 void *swm_gpu_stream(swm_gpu_ctx *c) { return c ? (void *)c->stream : nullptr; }

@@ -389,6 +389,8 @@ int swm_gpu_ensemble_create(swm_gpu_ctx *const *members, int n, swm_gpu_ensemble
   size_t points = 0;
   for (int i = 0; i < n; i++) points += (size_t)members[i]->nx * members[i]->ny;
   e->pf = march_prefetch_level(points, false);
+  for (int i = 0; i < n && e->pf == 3; i++)
+    if (members[i]->nx < RING_MIN_NX) e->pf = 2;  // the row ring wants basins RING_MIN_NX wide
   for (P32 &q : tab) q.pf = e->pf;
   // Tiles: every member's strips cut into row groups of equal estimated
   // cost (as the single-basin step kernel's tiles), all members' tiles in
@@ -623,7 +625,7 @@ int swm_gpu_ensemble_synchronize(swm_gpu_ensemble *e) {
   SWM_ON_DEVICE(e ? e->device : -1);
   SWM_REQUIRE(e, "swm_gpu_ensemble_synchronize: null ensemble");
   SWM_CK(cudaStreamSynchronize(e->stream));
-  return SWM_GPU_OK;
+  return march_ring_check();
 }
 
 void *swm_gpu_ensemble_stream(swm_gpu_ensemble *e) { return e ? (void *)e->stream : nullptr; }

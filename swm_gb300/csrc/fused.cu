@@ -360,8 +360,10 @@ struct FusedState {
 
 namespace swm {
 
+// 16 bytes more than asked: the step kernel's row copies move whole 16-byte
+// words and may read up to 12 bytes past a field's last element
 static int dmalloc(void **p, size_t bytes) {
-  cudaError_t e = cudaMalloc(p, bytes);
+  cudaError_t e = cudaMalloc(p, bytes + 16);
   if (e != cudaSuccess) {
     set_error(std::string("cudaMalloc: ") + cudaGetErrorString(e));
     return SWM_GPU_ENOMEM;

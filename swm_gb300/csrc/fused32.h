@@ -186,6 +186,12 @@ bool march_std_params(const P32 &p);
 // other than the nonlinear wind stress, or the mean-state terms)
 bool fused_dynamic_forcing(const swm_gpu_ctx *c);
 int march_prefetch_level(size_t points, bool integ);
+// level 3 (the row ring) serves basins at least this wide; narrower strips
+// wrap around the periodic boundary more than once
+constexpr int RING_MIN_NX = 32;
+// SWM_GPU_EDEVICE when a step kernel's warp gave up waiting for its row
+// copies since the library was loaded (reads a device counter; synchronises)
+int march_ring_check();
 // more bytes than the device's L2 holds
 bool exceeds_l2(double bytes);
 

@@ -3,7 +3,8 @@
 // Each warp owns a strip of 32 columns (lane = column) and S output rows.  It
 // walks up the strip one row per iteration, keeping the last rows of every
 // intermediate field in registers; x-neighbours come from warp shuffles, so
-// the kernel uses no shared memory and no block barrier.  When row J has
+// the kernel needs no shared memory and no block barrier (the row-ring
+// instances, PF = 3, stage their input rows in shared memory).  When row J has
 // been loaded, the stress tensor and fluxes needed by row J-2 are complete
 // and row J-2 is updated (the biharmonic operator needs two rows of
 // look-ahead).  The outer HALO lanes of a strip are recomputed by the
@@ -60,6 +61,101 @@ __device__ __forceinline__ int wrapm(int g, int n) {
 }
 __device__ __forceinline__ float rcnt(int c) { return c <= 1 ? 1.f : (c == 2 ? 0.5f : (c == 3 ? 0.33333334f : 0.25f)); }
 
+// ---- row ring (march_strip's PF = 3) ----------------------------------------
+//
+// Each warp stages the rows it is about to read in a ring of RING slots of
+// shared memory, filled by bulk asynchronous copies (cp.async.bulk, the TMA
+// engine) and tracked by one mbarrier per slot, so that the compute lanes
+// issue no global loads for the state, depth, mask and increments: a slot
+// holds, for one input row J, the 32 columns of the warp of the seven state
+// and depth fields and of the mask, and the six increments of output row
+// J - 2.  A field's row segment is copied as the 16-byte aligned span that
+// covers it (bulk copies move whole 16-byte words), in at most two pieces:
+// the columns inside [0, nx) and the columns that wrap around the periodic
+// boundary; the second piece is placed right after the first.  Allocations
+// of the fields leave 16 bytes after their last element, so an aligned span
+// never leaves its allocation.  Lanes 0..27 each issue one copy, field
+// (lane >> 1), piece (lane & 1).
+constexpr int RING = 4;                                // rows in flight per warp
+constexpr int RING_FB = 192;                           // one float field (at most 44 floats used)
+constexpr int RING_MB = 128;                           // the mask (at most 60 uint16 used)
+constexpr int RING_NF = 13;                            // float fields per slot
+constexpr int RING_SLOT = RING_NF * RING_FB + RING_MB;  // bytes of one slot
+constexpr int RING_WARP = RING * RING_SLOT;            // bytes of one warp's ring
+constexpr unsigned long long RING_WAIT_NS = 1000000000ull;  // a row that has not arrived after 1 s
+
+struct RingW {
+  const float *ptr;  // the warp's ring
+  uint32_t slots;    // its shared-window address
+  uint32_t bars;     // and that of its RING mbarriers
+  uint32_t phase;    // parity bit of each slot's next phase
+};
+
+
+__device__ __forceinline__ uint32_t smem_addr(const void *p) { return (uint32_t)__cvta_generic_to_shared(p); }
+__device__ __forceinline__ void mbar_init(uint32_t bar, unsigned count) {
+  asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(bar), "r"(count) : "memory");
+}
+__device__ __forceinline__ void mbar_fence_init() {
+  asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+  asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+}
+__device__ __forceinline__ void mbar_expect_tx(uint32_t bar, uint32_t bytes) {
+  asm volatile("{\n\t.reg .b64 st;\n\tmbarrier.arrive.expect_tx.shared::cta.b64 st, [%0], %1;\n\t}" ::"r"(bar),
+               "r"(bytes)
+               : "memory");
+}
+__device__ __forceinline__ bool mbar_try(uint32_t bar, uint32_t parity) {
+  uint32_t ok;
+  asm volatile(
+      "{\n\t.reg .pred p;\n\tmbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\tselp.u32 %0, 1, 0, p;\n\t}"
+      : "=r"(ok)
+      : "r"(bar), "r"(parity)
+      : "memory");
+  return ok != 0;
+}
+__device__ __forceinline__ unsigned long long globaltimer_ns() {
+  unsigned long long t;
+  asm volatile("mov.u64 %0, %globaltimer;" : "=l"(t));
+  return t;
+}
+// every lane waits for the phase; false (the same on every lane) when the
+// phase has not completed within RING_WAIT_NS
+__device__ __forceinline__ bool mbar_wait_warp(uint32_t bar, uint32_t parity) {
+  bool done = mbar_try(bar, parity);
+  if (__all_sync(FULL, done)) return true;
+  const unsigned long long t0 = globaltimer_ns();
+  for (;;) {
+    if (!done) done = mbar_try(bar, parity);
+    if (__all_sync(FULL, done)) return true;
+    if (__any_sync(FULL, globaltimer_ns() - t0 > RING_WAIT_NS)) return false;
+  }
+}
+__device__ __forceinline__ void bulk_g2s(uint32_t dst, const void *src, uint32_t bytes, uint32_t bar) {
+  asm volatile("cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(dst),
+               "l"(src), "r"(bytes), "r"(bar)
+               : "memory");
+}
+// warps whose row copies did not arrive in time (the step kernels' results
+// are then wrong; the host reports it)
+__device__ unsigned g_ring_timeouts;
+
+// the ring of warp w of the block and its mbarriers, initialised (every
+// lane of the warp calls it)
+__device__ __forceinline__ RingW ring_setup(unsigned char *ring, unsigned long long *bars, int w, int lane) {
+  RingW r;
+  r.ptr = reinterpret_cast<const float *>(ring + (size_t)w * RING_WARP);
+  r.slots = smem_addr(ring + (size_t)w * RING_WARP);
+  r.bars = smem_addr(bars + w * RING);
+  r.phase = 0;
+  if (lane == 0) {
+    for (int k = 0; k < RING; k++) mbar_init(r.bars + 8u * k, 1);
+    mbar_fence_init();
+  }
+  __syncwarp();
+  return r;
+}
+
 // mask word: bits 0-3 own (H, u, v, eta), 4-7 column i-1, 8-11 column i+1
 #define MH(m) ((m) & 1)
 #define MU_(m) (((m) >> 1) & 1)
@@ -91,9 +187,15 @@ __device__ __forceinline__ void comp_damp(float hi, float lo, float inc, float d
 // next output row's increments (PF >= 1), which it would otherwise load in
 // the iteration that uses them, and for the input rows two ahead (PF = 2),
 // so that rows not in L2 do not wait on DRAM (march_prefetch_level).
+// PF = 3: the rows come through the warp's row ring rw instead (bulk copies
+// RING - 1 rows ahead; needs nx >= RING_MIN_NX).  Returns false when a row
+// did not arrive in time (the warp's copies still in flight are waited for,
+// within the same limit, before it returns).
 template <int MIX, bool INTEG = false, bool STD = false, int PF = 0>
-__device__ __forceinline__ void march_strip(const P32 &p, const int bx, const int ry0, const int lane, const int S,
-                                            const float2 *area = nullptr, F2 *acc = nullptr) {
+__device__ __forceinline__ bool march_strip(const P32 &p, const int bx, const int ry0, const int lane, const int S,
+                                            const float2 *area = nullptr, F2 *acc = nullptr,
+                                            RingW *rw = nullptr) {
+  constexpr bool RG = PF == 3;
   constexpr int H = MIX == 2 ? 2 : 1;
   constexpr int TI = 32 - 2 * H;
   const int nx = p.nx, ny = p.ny;
@@ -113,11 +215,85 @@ __device__ __forceinline__ void march_strip(const P32 &p, const int bx, const in
   int off[3] = {};            // row offsets nx * j of rows J, J-1, J-2
 
   int J = ry0 - 3;
+  const int J0 = J;
   const int jend = min(ry0 + S, ny) + 2;
   int noff = nx * wrapm(J, ny);
-  unsigned n_m = p.mask16[gi + noff];
-  float n_uh = p.uh0[gi + noff], n_ul = p.ul0[gi + noff], n_vh = p.vh0[gi + noff], n_vl = p.vl0[gi + noff];
-  float n_eh = p.eh0[gi + noff], n_el = p.el0[gi + noff], n_he = p.He[gi + noff];
+  unsigned n_m = 0;
+  float n_uh = 0.f, n_ul = 0.f, n_vh = 0.f, n_vl = 0.f, n_eh = 0.f, n_el = 0.f, n_he = 0.f;
+  if (!RG) {
+    n_m = p.mask16[gi + noff];
+    n_uh = p.uh0[gi + noff]; n_ul = p.ul0[gi + noff]; n_vh = p.vh0[gi + noff]; n_vl = p.vl0[gi + noff];
+    n_eh = p.eh0[gi + noff]; n_el = p.el0[gi + noff]; n_he = p.He[gi + noff];
+  }
+
+  // ---- row ring (PF = 3) ----
+  // the warp's columns gx0 .. gx0+31: piece 0 [am, am+wm) inside the basin,
+  // piece 1 [aw, aw+ww) the columns that wrap around
+  const int gx0 = bx * TI - H;
+  const int am = max(gx0, 0), wm = min(gx0 + 32, nx) - am;
+  const int aw = gx0 < 0 ? gx0 + nx : 0, ww = gx0 < 0 ? -gx0 : max(gx0 + 32 - nx, 0);
+  const bool inw = gx < 0 || gx >= nx;
+  const int lofs = gi - (inw ? aw : am);  // the lane's column within its piece
+  // element index of the lane's column in a field's slot region, for the
+  // row at offset r and an alignment of al + 1 elements
+  auto ridx = [&](int r, int al) {
+    const int s0 = (r + am) & al;
+    return inw ? ((s0 + wm + al) & ~al) + ((r + aw) & al) + lofs : s0 + lofs;
+  };
+  // the lane's copy: field fi (0-6 uh ul vh vl eh el He of row J, 7-12
+  // Ge1 Ge2 Gu1 Gu2 Gv1 Gv2 of row J-2, 13 the mask of row J), piece pc
+  const int fi = lane >> 1, pc = lane & 1;
+  const int pa = pc ? aw : am, pw = pc ? ww : wm;
+  const int fes = fi == 13 ? 2 : 4, fal = fi == 13 ? 7 : 3;
+  const char *fsrc = nullptr;
+  if (RG) {
+    const void *f = nullptr;
+    switch (fi) {
+      case 0: f = p.uh0; break;
+      case 1: f = p.ul0; break;
+      case 2: f = p.vh0; break;
+      case 3: f = p.vl0; break;
+      case 4: f = p.eh0; break;
+      case 5: f = p.el0; break;
+      case 6: f = p.He; break;
+      case 7: f = p.Ge1; break;
+      case 8: f = p.Ge2; break;
+      case 9: f = p.Gu1; break;
+      case 10: f = p.Gu2; break;
+      case 11: f = p.Gv1; break;
+      case 12: f = p.Gv2; break;
+      case 13: f = p.mask16; break;
+      default: break;
+    }
+    fsrc = static_cast<const char *>(f);
+  }
+  // copies of input row Jr and of the increments of output row Jr - 2 into
+  // the slot of Jr
+  auto issue = [&](int Jr) {
+    const int s = (Jr - J0) & (RING - 1);
+    const uint32_t bar = rw->bars + 8u * s;
+    const int o = Jr - 2;
+    const bool incr = fi >= 7 && fi <= 12;
+    const bool act = fsrc != nullptr && pw > 0 && (!incr || (o >= ry0 && o < ry0 + S && o < ny));
+    uint32_t bytes = 0, dst = 0;
+    const char *src = nullptr;
+    if (act) {
+      const int r = nx * (incr ? o : wrapm(Jr, ny));
+      const int s0 = (r + pa) & fal;
+      bytes = (uint32_t)(((s0 + pw + fal) & ~fal) * fes);
+      const int before = pc ? (((r + am) & fal) + wm + fal) & ~fal : 0;  // elements of piece 0
+      dst = rw->slots + (uint32_t)(s * RING_SLOT + (fi == 13 ? RING_NF * RING_FB : fi * RING_FB) + before * fes);
+      src = fsrc + (size_t)(r + pa - s0) * fes;
+    }
+    const uint32_t tx = __reduce_add_sync(FULL, bytes);
+    if (lane == 0) mbar_expect_tx(bar, tx);
+    __syncwarp();
+    if (act) bulk_g2s(dst, src, bytes, bar);
+  };
+  const float *rs = nullptr;  // the slot of the current row, as floats
+  if (RG)
+    for (int k = 0; k < RING - 1; k++)
+      if (J0 + k < jend) issue(J0 + k);
 
   // one iteration; FAST: every cell of the warp's 4-row window is ocean on
   // all four grids, so every mask test is compile-time true
@@ -146,7 +322,13 @@ __device__ __forceinline__ void march_strip(const P32 &p, const int bx, const in
     // monitored instances, whose sums leave no register for it)
     float wxo = 0.f, wyo = 0.f;
     if (upd) {
-      g1e = p.Ge1[ko]; g2e = p.Ge2[ko]; g1u = p.Gu1[ko]; g2u = p.Gu2[ko]; g1v = p.Gv1[ko]; g2v = p.Gv2[ko];
+      if (RG) {
+        constexpr int FW = RING_FB / 4;
+        const float *g = rs + ridx(off[2], 3);
+        g1e = g[7 * FW]; g2e = g[8 * FW]; g1u = g[9 * FW]; g2u = g[10 * FW]; g1v = g[11 * FW]; g2v = g[12 * FW];
+      } else {
+        g1e = p.Ge1[ko]; g2e = p.Ge2[ko]; g1u = p.Gu1[ko]; g2u = p.Gu2[ko]; g1v = p.Gv1[ko]; g2v = p.Gv2[ko];
+      }
       if (!INTEG && wind_rows) {
         if (p.wind_x) wxo = p.wx[o];
         if (p.wind_y) wyo = p.wy[o];
@@ -461,18 +643,44 @@ __device__ __forceinline__ void march_strip(const P32 &p, const int bx, const in
     }
     pll1[1] = pll1[0]; plt1[1] = plt1[0]; lu1[1] = lu1[0]; lv1[1] = lv1[0];
     pll2[1] = pll2[0]; plt2[1] = plt2[0];
-    m[0] = n_m; uh[0] = n_uh; ul[0] = n_ul; vh[0] = n_vh; vl[0] = n_vl;
-    eh[0] = n_eh; el[0] = n_el; he[0] = n_he;
-    off[0] = noff;
-    if (J + 1 < jend) {  // prefetch row J+1
-      int jw = wrapm(J + 1, ny);
-      noff = nx * jw;
-      const int kn = gi + noff;
-      n_m = p.mask16[kn];
-      n_uh = p.uh0[kn]; n_ul = p.ul0[kn]; n_vh = p.vh0[kn]; n_vl = p.vl0[kn];
-      n_eh = p.eh0[kn]; n_el = p.el0[kn]; n_he = p.He[kn];
+    if (RG) {
+      // the slot of row J + RING - 1 is the one row J - 1 used: every lane
+      // has read it (warp barrier) before the copies overwrite it
+      __syncwarp();
+      if (J + RING - 1 < jend) issue(J + RING - 1);
+      const int sl = (J - J0) & (RING - 1);
+      if (!mbar_wait_warp(rw->bars + 8u * sl, (rw->phase >> sl) & 1u)) {
+        // the rows issued after this one: wait for their copies (each again
+        // within the limit) so that none lands after the warp has left
+        for (int k = 1; k < RING && J + k < jend; k++) {
+          const int s2 = (J + k - J0) & (RING - 1);
+          mbar_wait_warp(rw->bars + 8u * s2, (rw->phase >> s2) & 1u);
+        }
+        return false;
+      }
+      rw->phase ^= 1u << sl;
+      constexpr int FW = RING_FB / 4;
+      rs = rw->ptr + sl * (RING_SLOT / 4);
+      const float *f = rs + ridx(noff, 3);
+      uh[0] = f[0]; ul[0] = f[FW]; vh[0] = f[2 * FW]; vl[0] = f[3 * FW];
+      eh[0] = f[4 * FW]; el[0] = f[5 * FW]; he[0] = f[6 * FW];
+      m[0] = reinterpret_cast<const uint16_t *>(rs + RING_NF * FW)[ridx(noff, 7)];
+      off[0] = noff;
+      if (J + 1 < jend) noff = nx * wrapm(J + 1, ny);
+    } else {
+      m[0] = n_m; uh[0] = n_uh; ul[0] = n_ul; vh[0] = n_vh; vl[0] = n_vl;
+      eh[0] = n_eh; el[0] = n_el; he[0] = n_he;
+      off[0] = noff;
+      if (J + 1 < jend) {  // prefetch row J+1
+        int jw = wrapm(J + 1, ny);
+        noff = nx * jw;
+        const int kn = gi + noff;
+        n_m = p.mask16[kn];
+        n_uh = p.uh0[kn]; n_ul = p.ul0[kn]; n_vh = p.vh0[kn]; n_vl = p.vl0[kn];
+        n_eh = p.eh0[kn]; n_el = p.el0[kn]; n_he = p.He[kn];
+      }
     }
-    if (PF >= 1) {
+    if (PF == 1 || PF == 2) {
       if (PF == 2 && J + 2 < jend) {  // the input rows two ahead
         const int k2 = gi + nx * wrapm(J + 2, ny);
         prefetch_l2(p.mask16 + k2);
@@ -493,6 +701,7 @@ __device__ __forceinline__ void march_strip(const P32 &p, const int bx, const in
     if (interior) body(std::true_type{});
     else body(std::false_type{});
   }
+  return true;
 }
 
 #if MARCH_COLS == 2
@@ -601,7 +810,17 @@ __global__ void __launch_bounds__(128, MARCH_MINB) k_march(P32 p, const int2 *__
   const int2 t = tiles[4 * b + (threadIdx.x >> 5)];
   const int S = t.y & 255;
   F2 acc[4];
-  if (S > 0) MARCH_STRIP<MIX, INTEG, STD, PF>(p, t.x, t.y >> 8, lane, S, mi.area, acc);
+  __shared__ __align__(128) unsigned char ring[PF == 3 ? 4 * RING_WARP : 16];
+  __shared__ unsigned long long rbar[PF == 3 ? 4 * RING : 1];
+  if (S > 0) {
+    if constexpr (PF == 3) {
+      RingW rw = ring_setup(ring, rbar, threadIdx.x >> 5, lane);
+      if (!march_strip<MIX, INTEG, STD, PF>(p, t.x, t.y >> 8, lane, S, mi.area, acc, &rw) && lane == 0)
+        atomicAdd(&g_ring_timeouts, 1u);
+    } else {
+      MARCH_STRIP<MIX, INTEG, STD, PF>(p, t.x, t.y >> 8, lane, S, mi.area, acc);
+    }
+  }
   if (INTEG) {
     grid_dep_trigger();
     march_integrals_block(mi, acc, b, gridDim.x - 1);
@@ -623,7 +842,11 @@ __global__ void __launch_bounds__(128, MARCH_MINB) k_march_ens(const P32 *__rest
                                                                const float2 *const *__restrict__ areas,
                                                                double *__restrict__ partial) {
   __shared__ P32 sp[4];
+  __shared__ __align__(128) unsigned char ring[PF == 3 ? 4 * RING_WARP : 16];
+  __shared__ unsigned long long rbar[PF == 3 ? 4 * RING : 1];
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  RingW rw{};
+  if (PF == 3) rw = ring_setup(ring, rbar, warp, lane);
   for (;;) {
     int t = 0;
     if (lane == 0) t = atomicAdd(next, 1);
@@ -634,7 +857,28 @@ __global__ void __launch_bounds__(128, MARCH_MINB) k_march_ens(const P32 *__rest
     int *dst = reinterpret_cast<int *>(&sp[warp]);
     for (int k = lane; k < (int)(sizeof(P32) / sizeof(int)); k += 32) dst[k] = src[k];
     __syncwarp();
-    if (INTEG) {
+    if (PF == 3) {
+      bool ok;
+      if (INTEG) {
+        F2 acc[4];
+        ok = march_strip<MIX, true, STD, PF>(sp[warp], d.y, d.z, lane, d.w, areas[d.x], acc, &rw);
+        for (int o = 16; o > 0; o >>= 1)
+#pragma unroll
+          for (int q = 0; q < 4; q++) {
+            const float h = __shfl_down_sync(FULL, acc[q].h, o), l = __shfl_down_sync(FULL, acc[q].l, o);
+            acc[q].add(h, l);
+          }
+        if (lane == 0)
+#pragma unroll
+          for (int q = 0; q < 4; q++) partial[4 * (size_t)t + q] = acc[q].value();
+      } else {
+        ok = march_strip<MIX, false, STD, PF>(sp[warp], d.y, d.z, lane, d.w, nullptr, nullptr, &rw);
+      }
+      if (!ok) {
+        if (lane == 0) atomicAdd(&g_ring_timeouts, 1u);
+        return;
+      }
+    } else if (INTEG) {
       F2 acc[4];
       MARCH_STRIP<MIX, true, STD, PF>(sp[warp], d.y, d.z, lane, d.w, areas[d.x], acc);
       for (int o = 16; o > 0; o >>= 1)
@@ -829,15 +1073,46 @@ bool exceeds_l2(double bytes) {
 // may follow other work that evicted them, and the increments it loads last
 // then wait on DRAM: 1 (measured on the 1025^2 basin: 5 % faster from a cold
 // L2, 1 % slower from a warm one).  SWM_GB300_MARCH_PREFETCH=0/1/2 forces it.
+// SWM_GB300_MARCH_PREFETCH=3 stages the rows through the warps' row rings
+// (bulk asynchronous copies) instead, in basins at least RING_MIN_NX wide.
 int march_prefetch_level(size_t points, bool integ) {
   const char *e = getenv("SWM_GB300_MARCH_PREFETCH");
-  if (e && e[0] >= '0' && e[0] <= '2' && e[1] == 0) return e[0] - '0';
+  if (e && e[0] >= '0' && e[0] <= (MARCH_COLS == 1 ? '3' : '2') && e[1] == 0) return e[0] - '0';
   if (march_state_exceeds_l2(points)) return 2;
   return integ ? 0 : 1;
 }
 
+static bool g_ring_launched = false;  // a ring instance has run: march_ring_check reads the counter
+
+// the ring instances want shared memory rather than L1 for their four
+// 42 KB blocks per SM
+template <class K>
+static void ring_carveout(K *k) {
+  cudaFuncSetAttribute(k, cudaFuncAttributePreferredSharedMemoryCarveout, (int)cudaSharedmemCarveoutMaxShared);
+}
+
+int march_ring_check() {
+  if (!g_ring_launched) return SWM_GPU_OK;
+  unsigned v = 0;
+  SWM_CK(cudaMemcpyFromSymbol(&v, g_ring_timeouts, sizeof(v)));
+  if (v) {
+    set_error("FP32 step kernel: " + std::to_string(v) + " warps gave up waiting for their row copies");
+    return SWM_GPU_EDEVICE;
+  }
+  return SWM_GPU_OK;
+}
+
 template <int MIX, bool STD, int PF>
 static void launch_mix_s(const P32 &p, const MarchGrid &g, cudaStream_t st, const MarchInteg *mi) {
+  if (PF == 3) {
+    static bool set = false;
+    if (!set) {
+      ring_carveout(k_march<MIX, true, STD, PF>);
+      ring_carveout(k_march<MIX, false, STD, PF>);
+      set = true;
+    }
+    g_ring_launched = true;
+  }
   if (!mi) {
     k_march<MIX, false, STD, PF><<<g.blocks, 128, 0, st>>>(p, g.tiles, MarchInteg{});
     return;
@@ -857,7 +1132,8 @@ static void launch_mix_p(const P32 &p, const MarchGrid &g, cudaStream_t st, cons
   q.pf = pf;
   launch_mix_s<MIX, STD, 0>(q, g, st, mi);
 #else
-  if (pf == 2) launch_mix_s<MIX, STD, 2>(p, g, st, mi);
+  if (pf == 3 && p.nx >= RING_MIN_NX) launch_mix_s<MIX, STD, 3>(p, g, st, mi);
+  else if (pf >= 2) launch_mix_s<MIX, STD, 2>(p, g, st, mi);
   else if (pf == 1) launch_mix_s<MIX, STD, 1>(p, g, st, mi);
   else launch_mix_s<MIX, STD, 0>(p, g, st, mi);
 #endif
@@ -957,6 +1233,7 @@ static int resident_blocks_of() {  // blocks of k_march resident on the whole GP
     int per_sm = 0, sms = 0, dev = 0;
     cudaGetDevice(&dev);
     cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    if (PF == 3) ring_carveout(k_march<MIX, false, STD, PF>);
     cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_march<MIX, false, STD, PF>, 128, 0);
     b = sms * (per_sm > 0 ? per_sm : 1);
   }
@@ -969,6 +1246,7 @@ static int resident_blocks_p(int pf) {
   (void)pf;  // one instance serves every level
   return resident_blocks_of<MIX, STD, 0>();
 #else
+  if (pf == 3) return resident_blocks_of<MIX, STD, 3>();
   return pf == 2 ? resident_blocks_of<MIX, STD, 2>()
                  : (pf == 1 ? resident_blocks_of<MIX, STD, 1>() : resident_blocks_of<MIX, STD, 0>());
 #endif
@@ -981,7 +1259,8 @@ static int resident_blocks_m(bool s, int pf) {
 
 static int resident_blocks(const P32 &p) {
   const bool s = march_std(p);
-  const int pf = march_prefetch_level((size_t)p.nx * p.ny, false);
+  int pf = march_prefetch_level((size_t)p.nx * p.ny, false);
+  if (pf == 3 && p.nx < RING_MIN_NX) pf = 2;
   if (p.mix == 2) return resident_blocks_m<2>(s, pf);
   if (p.mix == 1) return resident_blocks_m<1>(s, pf);
   return resident_blocks_m<0>(s, pf);
@@ -1063,9 +1342,11 @@ static int ens_launch_m(const P32 *tab, const int4 *tiles, int ntiles, int *next
     int per_sm = 0, sms = 0, dev = 0;
     SWM_CK(cudaGetDevice(&dev));
     SWM_CK(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
+    if (PF == 3) ring_carveout(k_march_ens<MIX, STD, PF, INTEG>);
     SWM_CK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_march_ens<MIX, STD, PF, INTEG>, 128, 0));
     blocks = sms * (per_sm > 0 ? per_sm : 1);
   }
+  if (PF == 3) g_ring_launched = true;
   int need = (ntiles + 3) / 4;
   k_march_ens<MIX, STD, PF, INTEG><<<need < blocks ? need : blocks, 128, 0, st>>>(
       tab, tiles, ntiles, next, mi ? mi->areas : nullptr, mi ? mi->partial : nullptr);
@@ -1086,6 +1367,7 @@ static int ens_launch_p(int pf, const P32 *tab, const int4 *tiles, int ntiles, i
   (void)pf;  // the level is in the parameter blocks
   return ens_launch_i<MIX, STD, 0>(tab, tiles, ntiles, next, mi, st);
 #else
+  if (pf == 3) return ens_launch_i<MIX, STD, 3>(tab, tiles, ntiles, next, mi, st);
   if (pf == 2) return ens_launch_i<MIX, STD, 2>(tab, tiles, ntiles, next, mi, st);
   if (pf == 1) return ens_launch_i<MIX, STD, 1>(tab, tiles, ntiles, next, mi, st);
   return ens_launch_i<MIX, STD, 0>(tab, tiles, ntiles, next, mi, st);

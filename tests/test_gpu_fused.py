@@ -152,25 +152,27 @@ def test_strip_rows_do_not_change_results(variant, monkeypatch):
 
 @pytest.mark.parametrize('variant', ['biharmonic', 'laplace_qbf'])
 def test_l2_prefetch_does_not_change_results(variant, monkeypatch):
-    """The step kernel's L2 prefetch levels (none, the next row's increments,
-    also the input rows two ahead; forced here) change no result: the same
-    steps, plain and monitored, give the same state bit for bit with and
-    without it.  The monitored integrals come from separately compiled
-    instances, whose pair sums may round differently: within 1e-12 of each
-    sum's scale."""
+    """The step kernel's row-loading levels (none, the next row's increments
+    prefetched to L2, also the input rows two ahead, the rows staged through
+    the warps' shared-memory rings by bulk asynchronous copies; forced here)
+    change no result: the same steps, plain and monitored, give the same
+    state bit for bit at every level.  The monitored integrals come from
+    separately compiled instances, whose pair sums may round differently:
+    within 1e-12 of each sum's scale."""
     from test_gpu_diag import _numpy_integrals
     import torch
     from swm_gb300.host.driver import Driver
     case = _case(variant, 60)
     ny = case['config']['ny']
     fields = []
-    for pf in ('0', '1', '2'):
+    for pf in ('0', '1', '2', '3'):
         monkeypatch.setenv('SWM_GB300_MARCH_PREFETCH', pf)
         g = GpuModel('fused_fp32c')
         Driver(case, g).init(with_diag=False)
         g.run(0, 30)
         out = torch.empty((10, 3), dtype=torch.float64).pin_memory().numpy()
         g.run_monitor(30, 10, 0, None, out)
+        g.synchronize()  # reports a warp that gave up waiting for its rows
         fields.append([g.field(f) for f in ('u', 'v', 'eta')] + [out.copy()])
         _, scale = _numpy_integrals(case, g)
         g.close()
@@ -226,3 +228,45 @@ def test_tiny_basins_batched():
             m = b.ocean(f).astype(bool)
             assert rel_l2(a.field(f), b.field(f), m) <= 1e-6, f
     ens.close()
+
+
+@pytest.mark.parametrize('biharmonic', [False, True])
+def test_row_ring_bit_identical(biharmonic, monkeypatch):
+    """Rows staged through the warps' row rings (bulk asynchronous copies of
+    16-byte aligned spans, in two pieces where a strip wraps around the
+    periodic boundary) give the state that direct loads give, bit for bit:
+    basins 34 to 201 points wide, so that row starts fall on every alignment
+    and the last strip wraps by 1 to 29 columns, alone and batched in an
+    ensemble; no warp gives up waiting for its rows."""
+    from swm_gb300.model import GpuEnsemble
+    from swm_gb300.host.driver import Driver
+    shapes = [(33, 9), (64, 3), (46, 31), (128, 20), (200, 33)]
+    cases = [synthetic.double_gyre(s, biharmonic=biharmonic, nsteps=30) for s in shapes]
+    runs = {}
+    for pf in ('2', '3'):
+        monkeypatch.setenv('SWM_GB300_MARCH_PREFETCH', pf)
+        alone = []
+        for c in cases:
+            g = GpuModel('fused_fp32c')
+            Driver(c, g).init(with_diag=False)
+            g.run(0, 30)
+            g.synchronize()
+            alone.append([g.field(f) for f in ('u', 'v', 'eta')])
+            g.close()
+        members = []
+        for c in cases:
+            g = GpuModel('fused_fp32c')
+            Driver(c, g).init(with_diag=False)
+            members.append(g)
+        ens = GpuEnsemble(members)
+        ens.run(0, 30)
+        ens.synchronize()
+        batched = [[g.field(f) for f in ('u', 'v', 'eta')] for g in members]
+        ens.close()
+        for g in members:
+            g.close()
+        runs[pf] = (alone, batched)
+    for kind in (0, 1):
+        for s, a, b in zip(shapes, runs['2'][kind], runs['3'][kind]):
+            for f, x, y in zip(('u', 'v', 'eta'), a, b):
+                assert np.array_equal(x, y), (kind, s, f)
