@@ -73,6 +73,7 @@ __global__ void k_ens_integrals(const EnsInt *__restrict__ d, double *__restrict
 __global__ void k_ens_rows(const double *__restrict__ rows, const int *__restrict__ row_member,
                            const int *__restrict__ row_off, float *const *__restrict__ w, int nrows,
                            int *__restrict__ queue_head) {
+  grid_dep_wait();  // the previous step has finished reading the rows
   const int r = blockIdx.x * blockDim.x + threadIdx.x;
   if (r == 0) *queue_head = 0;
   if (r >= nrows || !rows) return;
@@ -86,6 +87,7 @@ __global__ void k_ens_rows(const double *__restrict__ rows, const int *__restric
 __global__ void k_ens_tile_sums(const double *__restrict__ partial, const int *__restrict__ tile_off,
                                 const int *__restrict__ tiles_of, const double *__restrict__ G, int n,
                                 double *__restrict__ out) {
+  grid_dep_wait();  // the step's tile sums are written
   const int i = (int)((blockIdx.x * blockDim.x + threadIdx.x) >> 5), lane = threadIdx.x & 31;
   if (i >= n) return;  // whole warps leave together
   double s[4] = {0., 0., 0., 0.};
@@ -572,15 +574,20 @@ int swm_gpu_ensemble_run_monitor(swm_gpu_ensemble *e, int64_t itt0, int64_t nste
         rd = d;
       }
     }
-    k_ens_rows<<<rd ? (M->nrows + 255) / 256 : 1, 256, 0, e->stream>>>(rd, M->row_member, M->d_row_off, M->w,
-                                                                     M->nrows, e->next + e->phase);
+    // the three kernels of a monitored step are launched programmatically:
+    // each may be launched while its predecessor finishes and waits for it
+    // on the device (grid_dep_wait), so no launch latency separates them
+    SWM_CK(launch_programmatic(k_ens_rows, dim3(rd ? (M->nrows + 255) / 256 : 1), dim3(256), e->stream, rd,
+                               (const int *)M->row_member, (const int *)M->d_row_off, (float *const *)M->w,
+                               M->nrows, e->next + e->phase));
     e->launches++;
     const EnsInteg mi{M->areas, M->partial};
     rc = ens_step(e, itt, &mi, false);
     if (rc != SWM_GPU_OK) return rc;
     double *od = out_dev ? out_dev + 3 * n * (size_t)s : M->res;
-    k_ens_tile_sums<<<(unsigned)((32 * n + 127) / 128), 128, 0, e->stream>>>(M->partial, M->tile_off, M->tiles_of,
-                                                                           M->G, (int)n, od);
+    SWM_CK(launch_programmatic(k_ens_tile_sums, dim3((unsigned)((32 * n + 127) / 128)), dim3(128), e->stream,
+                               (const double *)M->partial, (const int *)M->tile_off, (const int *)M->tiles_of,
+                               (const double *)M->G, (int)n, od));
     e->launches++;
     if (!out_dev) SWM_CK(cudaMemcpyAsync(os, M->res, 3 * n * sizeof(double), cudaMemcpyDeviceToHost, e->stream));
   }

@@ -845,6 +845,7 @@ __global__ void __launch_bounds__(128, MARCH_MINB) k_march_ens(const P32 *__rest
   __shared__ __align__(128) unsigned char ring[PF == 3 ? 4 * RING_WARP : 16];
   __shared__ unsigned long long rbar[PF == 3 ? 4 * RING : 1];
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  if (INTEG) grid_dep_wait();  // monitored steps are launched programmatically
   RingW rw{};
   if (PF == 3) rw = ring_setup(ring, rbar, warp, lane);
   for (;;) {
@@ -1348,6 +1349,12 @@ static int ens_launch_m(const P32 *tab, const int4 *tiles, int ntiles, int *next
   }
   if (PF == 3) g_ring_launched = true;
   int need = (ntiles + 3) / 4;
+  if (INTEG) {  // a monitored step: launched programmatically (k_ens_rows before it, k_ens_tile_sums after)
+    SWM_CK(launch_programmatic(k_march_ens<MIX, STD, PF, INTEG>, dim3(need < blocks ? need : blocks), dim3(128), st,
+                               tab, (const int4 *)tiles, ntiles, next, (const float2 *const *)mi->areas,
+                               (double *)mi->partial));
+    return SWM_GPU_OK;
+  }
   k_march_ens<MIX, STD, PF, INTEG><<<need < blocks ? need : blocks, 128, 0, st>>>(
       tab, tiles, ntiles, next, mi ? mi->areas : nullptr, mi ? mi->partial : nullptr);
   return SWM_GPU_OK;
