@@ -237,7 +237,10 @@ def test_row_ring_bit_identical(biharmonic, monkeypatch):
     periodic boundary) give the state that direct loads give, bit for bit:
     basins 34 to 201 points wide, so that row starts fall on every alignment
     and the last strip wraps by 1 to 29 columns, alone and batched in an
-    ensemble; no warp gives up waiting for its rows."""
+    ensemble, plain and monitored steps; no warp gives up waiting for its
+    rows.  The monitored ensemble steps' energies come from separately
+    compiled instances, whose pair sums may round differently: 1e-12."""
+    import torch
     from swm_gb300.model import GpuEnsemble
     from swm_gb300.host.driver import Driver
     shapes = [(33, 9), (64, 3), (46, 31), (128, 20), (200, 33)]
@@ -260,13 +263,18 @@ def test_row_ring_bit_identical(biharmonic, monkeypatch):
             members.append(g)
         ens = GpuEnsemble(members)
         ens.run(0, 30)
+        out = torch.empty((8, len(cases), 3), dtype=torch.float64).pin_memory().numpy()
+        ens.run_monitor(30, 8, None, out)
         ens.synchronize()
         batched = [[g.field(f) for f in ('u', 'v', 'eta')] for g in members]
         ens.close()
         for g in members:
             g.close()
-        runs[pf] = (alone, batched)
+        runs[pf] = (alone, batched, out.copy())
     for kind in (0, 1):
         for s, a, b in zip(shapes, runs['2'][kind], runs['3'][kind]):
             for f, x, y in zip(('u', 'v', 'eta'), a, b):
                 assert np.array_equal(x, y), (kind, s, f)
+    o2, o3 = runs['2'][2], runs['3'][2]
+    assert np.isfinite(o3).all() and np.all(o2[:, :, 1:] > 0)
+    assert np.all(np.abs(o2[:, :, 1:] - o3[:, :, 1:]) <= 1e-12 * o2[:, :, 1:])  # the two energies
