@@ -164,15 +164,18 @@ __device__ __forceinline__ RingW ring_setup(unsigned char *ring, unsigned long l
 #define LV(m) (((m) >> 6) & 1)
 #define LE(m) (((m) >> 7) & 1)
 
-// (hi + lo + inc) * (1 - dp) as a new (hi, lo) pair
+// (hi + lo + inc) * (1 - dp) as a new (hi, lo) pair.  Both roundings are
+// recovered by Fast2Sum (Dekker 1971), which is exact when the larger operand
+// comes first: for s - c always (c = s dp, 0 <= dp < 1); for hi + inc while
+// the step's increment is below the state, which fails only where the state
+// passes through zero, and there the error left is a rounding of the
+// increment, far below the pair's precision relative to the field.
 __device__ __forceinline__ void comp_damp(float hi, float lo, float inc, float dp, float &nh, float &nl) {
-  float s = hi + inc;
-  float bb = s - hi;
-  float e = (hi - (s - bb)) + (inc - bb) + lo;
-  float c = s * dp;
-  float t = s - c;
-  float bt = t - s;
-  float e2 = (s - (t - bt)) + (-c - bt);
+  const float s = hi + inc;
+  float e = (inc - (s - hi)) + lo;
+  const float c = s * dp;
+  const float t = s - c;
+  const float e2 = (s - t) - c;
   e = e + e2 - e * dp;
   nh = t + e;
   nl = e - (nh - t);
