@@ -60,14 +60,16 @@ __device__ __forceinline__ float face(int flux, float vel, float cLm, float cL, 
   return (oL ? cL : 0.f) * (den == 2 ? 0.5f : 1.f) + (oR ? cR : 0.f) * (den == 2 ? 0.5f : 1.f);
 }
 
+// (hi + lo + inc) * (1 - dp) as a new (hi, lo) pair, the two roundings
+// recovered by Fast2Sum (Dekker 1971): exact for s - c (c = s dp, 0 <= dp <
+// 1), and for hi + inc wherever the increment is below the tracer content,
+// which fails only where the content passes through zero
 __device__ __forceinline__ void comp_update(float hi, float lo, float inc, float dp, float &nh, float &nl) {
-  float s = hi + inc;
-  float bb = s - hi;
-  float e = (hi - (s - bb)) + (inc - bb) + lo;
-  float c = s * dp;
-  float t = s - c;
-  float bt = t - s;
-  float e2 = (s - (t - bt)) + (-c - bt);
+  const float s = hi + inc;
+  float e = (inc - (s - hi)) + lo;
+  const float c = s * dp;
+  const float t = s - c;
+  const float e2 = (s - t) - c;
   e = e + e2 - e * dp;
   nh = t + e;
   nl = e - (nh - t);
