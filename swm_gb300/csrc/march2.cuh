@@ -13,9 +13,11 @@
 // 32-bit word (column 2l in bits 0-15, 2l+1 in bits 16-31), so a mask test
 // gives a bit per column (0x00001 / 0x10000).
 //
-// Formulas and precision rules are those of march_strip (march.cu); the
-// packed operations are never contracted, so products that must be exact
-// (TwoProd) are explicit FMAs and plain sums stay separate operations.
+// Formulas and precision rules are those of march_strip (march.cu), except
+// that the compensated update recovers its roundings by TwoSum rather than
+// Fast2Sum (exact in more cases, three more operations); the packed
+// operations are never contracted, so products that must be exact (TwoProd)
+// are explicit FMAs and plain sums stay separate operations.
 
 namespace v2 {
 __device__ __forceinline__ float2 operator+(float2 a, float2 b) { return __fadd2_rn(a, b); }
