@@ -11,11 +11,8 @@
 // kernel therefore moves the state in and out once, reads the two older
 // increments and writes the newest one -- the algorithmic minimum.
 //
-// T = double: FP64 fused path.  T = float with COMP: the state is a pair of
-// binary32 words (hi + lo, ~48 significant bits); tendencies are evaluated in
-// binary32 from hi and the Adams-Bashforth increment is added with TwoSum and
-// a compensated division by the implicit damping factor, so rounding errors
-// do not accumulate in the state over long integrations.
+// T = double: the FP64 fused path.  (The FP32 compensated path is the row
+// marching kernel of march.cu.)
 //
 // Arithmetic follows the reference formulas (swm_nonlinear_timestep_module.f90
 // :182-449, swm_lateralmixing_module.f90:66-240, time_integration_module.f90
@@ -48,8 +45,6 @@ struct FP {
   const T *wx, *wy;
   const T *u0, *v0, *e0;
   T *u1, *v1, *e1;
-  const float *ul0, *vl0, *el0;
-  float *ul1, *vl1, *el1;
   const T *Gu1, *Gu2, *Gv1, *Gv2, *Ge1, *Ge2;
   T *Gu3, *Gv3, *Ge3;
 };
@@ -69,20 +64,7 @@ __device__ __forceinline__ T recip_cnt(int c) {
   return c <= 1 ? T(1) : (c == 2 ? T(0.5) : (c == 3 ? T(1) / T(3) : T(0.25)));
 }
 
-// compensated a + b (a = hi + lo pair, b float) followed by division by d
-__device__ __forceinline__ void comp_update(float hi, float lo, float inc, float d, float &nh, float &nl) {
-  float s = hi + inc;
-  float bb = s - hi;
-  float e = (hi - (s - bb)) + (inc - bb);
-  e = e + lo;
-  float q = s / d;
-  float r = fmaf(-q, d, s);
-  float ql = (r + e) / d;
-  nh = q + ql;
-  nl = ql - (nh - q);
-}
-
-template <typename T, int HALO, bool COMP>
+template <typename T, int HALO>
 __global__ void __launch_bounds__(NT) k_fused(FP<T> p) {
   constexpr int W = TX + 2 * HALO, HH = TY + 2 * HALO, NS = W * HH;
   __shared__ T sU[NS], sV[NS], sE[NS], sD[NS], sMU[NS], sMV[NS], sPOT[NS], sB[NS], sPLL[NS], sPLT[NS];
@@ -287,22 +269,11 @@ __global__ void __launch_bounds__(NT) k_fused(FP<T> p) {
     T incu = p.dt * (p.ab0 * p.Gu1[k] + p.ab1 * p.Gu2[k] + p.ab2 * gu);
     T incv = p.dt * (p.ab0 * p.Gv1[k] + p.ab1 * p.Gv2[k] + p.ab2 * gv);
     T lim = p.minD - p.He[k];
-    if constexpr (COMP) {
-      float nh, nlo;
-      comp_update(sE[q], p.el0[k], ince, ie, nh, nlo);
-      if (nl && nh < lim) { nh = lim; nlo = 0.f; }
-      p.e1[k] = nh; p.el1[k] = nlo;
-      comp_update(sU[q], p.ul0[k], incu, iu, nh, nlo);
-      p.u1[k] = nh; p.ul1[k] = nlo;
-      comp_update(sV[q], p.vl0[k], incv, iv, nh, nlo);
-      p.v1[k] = nh; p.vl1[k] = nlo;
-    } else {
-      T e = (sE[q] + ince) / ie;
-      if (nl && e < lim) e = lim;
-      p.e1[k] = e;
-      p.u1[k] = (sU[q] + incu) / iu;
-      p.v1[k] = (sV[q] + incv) / iv;
-    }
+    T e = (sE[q] + ince) / ie;
+    if (nl && e < lim) e = lim;
+    p.e1[k] = e;
+    p.u1[k] = (sU[q] + incu) / iu;
+    p.v1[k] = (sV[q] + incv) / iv;
   }
 }
 
@@ -648,11 +619,11 @@ static void fill_common(swm_gpu_ctx *c, FP<T> &p, int64_t itt) {
   p.wy = (const T *)f->wy;
 }
 
-template <typename T, bool COMP>
+template <typename T>
 static void launch_fused(swm_gpu_ctx *c, const FP<T> &p) {
   dim3 grid((c->nx + TX - 1) / TX, (c->ny + TY - 1) / TY);
-  if (p.mix == 2) k_fused<T, 2, COMP><<<grid, NT, 0, c->stream>>>(p);
-  else k_fused<T, 1, COMP><<<grid, NT, 0, c->stream>>>(p);
+  if (p.mix == 2) k_fused<T, 2><<<grid, NT, 0, c->stream>>>(p);
+  else k_fused<T, 1><<<grid, NT, 0, c->stream>>>(p);
   c->launches++;
 }
 
@@ -1040,7 +1011,7 @@ int fused_step(swm_gpu_ctx *c, int64_t itt) {
     p.Gu1 = d.Gu[0]; p.Gu2 = d.Gu[1]; p.Gu3 = d.Gu[2];
     p.Gv1 = d.Gv[0]; p.Gv2 = d.Gv[1]; p.Gv3 = d.Gv[2];
     p.Ge1 = d.Ge[0]; p.Ge2 = d.Ge[1]; p.Ge3 = d.Ge[2];
-    launch_fused<double, false>(c, p);
+    launch_fused<double>(c, p);
   } else {
     FTRY(launch_fp32c(c, itt));
     // the pair state advances here; the host-side advance only rotates the
