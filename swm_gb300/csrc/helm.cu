@@ -280,43 +280,6 @@ __global__ void k_h_resid_c(int nx, int ny, const double *__restrict__ cx, const
   if (threadIdx.x == 0) partial[blockIdx.x] = red[0];
 }
 
-// r = rhs - A psi on ocean cells (0 elsewhere); per-block partial sums of r^2
-// in FP64.  r may be null.
-template <typename T>
-__global__ void k_h_resid(int nx, int ny, const T *__restrict__ h, const int8_t *__restrict__ mask,
-                          const T *__restrict__ rhs, const T *__restrict__ psi, T rdx2, T rdy2, T lambda, double *r,
-                          double *partial) {
-  __shared__ double red[256];
-  double acc = 0.;
-  const size_t n = (size_t)nx * ny;
-  for (size_t k = (size_t)blockIdx.x * blockDim.x + threadIdx.x; k < n; k += (size_t)gridDim.x * blockDim.x) {
-    const int i = (int)(k % nx), j = (int)(k / nx);
-    double rr = 0.;
-    if (mask[k]) {
-      // in FP64 whatever the storage type: the residual of the stored iterate
-      const double hk = h[k], dx2 = rdx2, dy2 = rdy2;
-      const double cxw = i > 0 ? (0.5 * (hk + (double)h[k - 1])) * dx2 : 0.;
-      const double cxe = i < nx - 1 ? (0.5 * ((double)h[k + 1] + hk)) * dx2 : 0.;
-      const double cys = j > 0 ? (0.5 * (hk + (double)h[k - nx])) * dy2 : 0.;
-      const double cyn = j < ny - 1 ? (0.5 * ((double)h[k + nx] + hk)) * dy2 : 0.;
-      const double cc = -(((cxw + cxe) + cys) + cyn) - (double)lambda;
-      const double w = i > 0 ? (double)psi[k - 1] : 0., e = i < nx - 1 ? (double)psi[k + 1] : 0.;
-      const double s = j > 0 ? (double)psi[k - nx] : 0., nn = j < ny - 1 ? (double)psi[k + nx] : 0.;
-      const double ap = cxw * w + cxe * e + cys * s + cyn * nn + cc * (double)psi[k];
-      rr = (double)rhs[k] - ap;
-    }
-    if (r) r[k] = rr;
-    acc += rr * rr;
-  }
-  red[threadIdx.x] = acc;
-  __syncthreads();
-  for (int w = blockDim.x / 2; w > 0; w >>= 1) {
-    if (threadIdx.x < w) red[threadIdx.x] += red[threadIdx.x + w];
-    __syncthreads();
-  }
-  if (threadIdx.x == 0) partial[blockIdx.x] = red[0];
-}
-
 __global__ void k_h_sumsq(const double *x, const int8_t *mask, size_t n, double *partial) {
   __shared__ double red[256];
   double acc = 0.;
